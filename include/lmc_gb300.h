@@ -1,0 +1,241 @@
+/*
+ * lmc_gb300.h - C ABI of the GB300-native lattice Monte Carlo hot path.
+ *
+ * Plain C types only (pointers, sizes, int status codes); no C++ or PyTorch
+ * types cross this boundary. Every call returns LMC_OK (0) or an lmc_status
+ * code; lmc_last_error() gives the message of the calling thread's last
+ * failure. Nothing throws across the ABI.
+ *
+ * Lattices are perfect cubic FCC supercells of n x n x n conventional cells
+ * (4 n^3 sites) addressed by the lattice ids the reference assigns after
+ * Config::ReassignLatticeVector (lmc/cfg/src/Config.cpp:466-552), i.e.
+ * id = hx * 2n^2 + hy * n + hz / 2 in half-lattice coordinates. Species are
+ * int8 codes: the rank of the element's name in the string order of the
+ * model's alphabet, which is the barrier element set plus "X" (vacancy), the
+ * same order as the reference's std::set<Element> (lmc/cfg/include/Element.hpp:44-49).
+ *
+ * Threading: a context owns one CUDA stream on one device; calls on one
+ * context must be serialised by the caller, distinct contexts are independent.
+ */
+#ifndef LMC_GB300_H_
+#define LMC_GB300_H_
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lmc_status {
+  LMC_OK = 0,
+  LMC_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument / std::runtime_error in the reference */
+  LMC_ERR_OUT_OF_RANGE = 2,     /* std::out_of_range (.at(), ClusterIndexer::GetIndex, GetPairFlatIndex) */
+  LMC_ERR_IO = 3,               /* "Cannot open <file>" */
+  LMC_ERR_CUDA = 4,             /* CUDA runtime failure */
+  LMC_ERR_NO_DEVICE = 5,        /* no CUDA device / extension unusable */
+  LMC_ERR_NUMERIC = 6,          /* NaN / inf / non-positive total rate detected on the device */
+  LMC_ERR_STOPPED = 7,          /* run stopped by lmc_request_stop or a device wait limit */
+  LMC_ERR_UNSUPPORTED = 8       /* input outside the supported domain (e.g. n < 6) */
+} lmc_status;
+
+const char *lmc_strerror(int status);
+const char *lmc_last_error(void);
+const char *lmc_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Model: element alphabet + coefficient file contents                        */
+/* ------------------------------------------------------------------------- */
+typedef struct lmc_model lmc_model;
+
+/* Quartic barrier parameters of one migrating element
+ * (ParametersQuartic, lmc/pred/include/EnergyUtility.h:73-86). */
+typedef struct lmc_quartic_params {
+  int k_mmm, k_mm2;                   /* rows of U_mmm / U_mm2 */
+  const double *mu_x_mmm, *sigma_x_mmm; /* f_mmm each */
+  const double *mu_x_mm2, *sigma_x_mm2; /* f_mm2 each */
+  const double *u_mmm;                /* k_mmm x f_mmm, row-major */
+  const double *u_mm2;                /* k_mm2 x f_mm2, row-major */
+  const double *theta_d;              /* k_mmm */
+  const double *theta_ks;             /* k_mm2 */
+  double mu_d, sigma_d, mu_ks, sigma_ks;
+} lmc_quartic_params;
+
+/* E0 barrier parameters (ParametersE0, EnergyUtility.h:88-95). */
+typedef struct lmc_e0_params {
+  int k_mmm;
+  const double *mu_x_mmm, *sigma_x_mmm; /* f_mmm each */
+  const double *u_mmm;                  /* k_mmm x f_mmm, row-major */
+  const double *theta_e0;               /* k_mmm */
+  double mu_e0, sigma_e0;
+} lmc_e0_params;
+
+/* Creates a model for the barrier element set `element_names` (the reference's
+ * `element_set` parameter-file key, e.g. {"Al","Mg","Zn"}); "X" is added to the
+ * species alphabet automatically. Replaces the element-set handling of the
+ * predictor constructors (VacancyMigrationPredictorQuartic.cpp:16-37). */
+int lmc_model_create(const char *const *element_names, int num_elements, lmc_model **out);
+/* Parses a reference coefficient JSON ("Base".theta plus per-element Quartic
+ * and, when present, E0 blocks) into a new model: the constructors'
+ * JSON handling (VacancyMigrationPredictorQuartic.cpp:38-63,
+ * VacancyMigrationPredictorE0.cpp:22-40, EnergyPredictor.cpp:24-33). */
+int lmc_model_load_json(const char *path, const char *const *element_names, int num_elements, lmc_model **out);
+void lmc_model_destroy(lmc_model *model);
+/* Species alphabet size (element set + X) and the code of a name (-1 if absent). */
+int lmc_model_num_species(const lmc_model *model);
+int lmc_model_species_code(const lmc_model *model, const char *name);
+/* Writes the alphabet as a space-separated string. */
+int lmc_model_alphabet(const lmc_model *model, char *buf, int buflen);
+/* Layout: length of "Base".theta, MMM and MM2 feature counts. */
+int lmc_model_layout(const lmc_model *model, int *num_theta, int *f_mmm, int *f_mm2);
+/* Orbit size of every MMM (which=0) or MM2 (which=1) feature: feature value =
+ * one-hot numerator / orbit size (GetOneHotParametersFromMap, EnergyUtility.cpp:790-792). */
+int lmc_model_feature_orbit_sizes(const lmc_model *model, int which, int32_t *sizes);
+int lmc_model_set_base_theta(lmc_model *model, const double *theta, int n);
+int lmc_model_set_quartic(lmc_model *model, const char *migrant, const lmc_quartic_params *p);
+int lmc_model_set_e0(lmc_model *model, const char *migrant, const lmc_e0_params *p);
+
+/* ------------------------------------------------------------------------- */
+/* Host-only queries (no GPU needed): geometry and encodings                  */
+/* ------------------------------------------------------------------------- */
+/* Sorted 1/2/3NN ids of `site` in an n^3 supercell (Config.cpp:955-1045): 42 ids. */
+int lmc_geom_neighbors(int n, int64_t site, int64_t *out42);
+/* Sorted id lists of a 1NN pair (GetSortedLatticeVectorStateOfPair and
+ * GetSymmetricallySortedLatticeVector{MMM,MM2}, EnergyUtility.cpp:45-104,261-287). */
+int lmc_geom_pair_lists(int n, int64_t first, int64_t second, int64_t *state60, int64_t *mmm58, int64_t *mm258);
+/* Sorted 1-3NN id list of a site (GetSortedLatticeVectorStateOfSite): 43 ids. */
+int lmc_geom_site_list(int n, int64_t site, int64_t *out43);
+/* Cluster-mapping sizes: counts[0..7] state-pair clusters per label,
+ * counts[8..15] site clusters per label, counts[16] MMM orbits, counts[17] MM2
+ * orbits, counts[18] MMM clusters, counts[19] MM2 clusters. */
+int lmc_geom_mapping_sizes(int *counts20);
+/* Flattened MMM (which=0) / MM2 (which=1) mapping: per cluster (orbit, a, b),
+ * b = -1 for singlets; `cap` clusters at most. Returns the cluster count in *n. */
+int lmc_geom_env_mapping(int which, int32_t *orbit_a_b, int cap, int *n);
+
+/* Integer encodings of a 1NN jump pair on a host lattice (species codes):
+ * the ElementCluster start/end counts behind GetDe (num_theta each,
+ * VacancyMigrationPredictorQuartic.cpp:112-166) and the MMM / MM2-forward /
+ * MM2-backward one-hot numerators (feature value = numerator / orbit size,
+ * EnergyUtility.cpp:743-796). Any pointer may be NULL. */
+int lmc_host_encode_pair(const lmc_model *model, int n, const int8_t *species, int64_t first, int64_t second,
+                         int32_t *state_start, int32_t *state_end, int32_t *mmm, int32_t *mm2_fwd,
+                         int32_t *mm2_bwd);
+
+/* ------------------------------------------------------------------------- */
+/* Device context                                                            */
+/* ------------------------------------------------------------------------- */
+typedef struct lmc_ctx lmc_ctx;
+
+/* Uploads the model's folded coefficient tables to `device` and creates the
+ * context's stream. Fails with LMC_ERR_NO_DEVICE when no GPU is usable. */
+int lmc_ctx_create(const lmc_model *model, int device, lmc_ctx **out);
+void lmc_ctx_destroy(lmc_ctx *ctx);
+int lmc_ctx_synchronize(lmc_ctx *ctx);
+
+/* Lattices ("replicas"): R cubic supercells with edges n[r] (6 <= n <= 1000),
+ * species concatenated in replica order (host pointer). Replaces the Config
+ * species storage read by Config::GetElementAtLatticeId (Config.cpp:132-135). */
+int lmc_ctx_set_lattices(lmc_ctx *ctx, int num_replicas, const int32_t *n, const int8_t *species);
+int lmc_ctx_get_lattices(lmc_ctx *ctx, int8_t *species);
+/* Total sites over all replicas and the site offset of replica r. */
+int64_t lmc_ctx_total_sites(const lmc_ctx *ctx);
+int64_t lmc_ctx_replica_offset(const lmc_ctx *ctx, int replica);
+/* Device address of the species arena (for device-resident callers). */
+void *lmc_ctx_species_device_ptr(lmc_ctx *ctx);
+
+/* Barrier predictors over a batch of 1NN pairs (first = vacancy site,
+ * second = migrating atom) of one replica; host arrays of length m.
+ * kind 0 = Quartic (VacancyMigrationPredictorQuartic::GetBarrierAndDiffFromLatticeIdPair,
+ * VacancyMigrationPredictorQuartic.cpp:247-276), kind 1 = E0
+ * (VacancyMigrationPredictorE0.cpp:153-159). d / ks (Quartic) or e0 (E0) may be NULL. */
+#define LMC_BARRIER_QUARTIC 0
+#define LMC_BARRIER_E0 1
+int lmc_barrier_batch(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs, int m, double *ea, double *de,
+                      double *d_or_e0, double *ks);
+/* Device-resident variant: pairs/outputs are device pointers, asynchronous on the context stream. */
+int lmc_barrier_batch_device(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs_dev, int m, double *ea_dev,
+                             double *de_dev);
+
+/* Integer encodings of a batch of 1NN jump pairs computed on the device (same
+ * layout as lmc_host_encode_pair, m consecutive records per array). */
+int lmc_encode_batch(lmc_ctx *ctx, int replica, const int64_t *pairs, int m, int32_t *state_start,
+                     int32_t *state_end, int32_t *mmm, int32_t *mm2_fwd, int32_t *mm2_bwd);
+
+/* Pair-swap energy change (EnergyChangePredictorPairSite::GetDeFromLatticeIdPair,
+ * EnergyChangePredictorPairSite.cpp:69-192) for a batch of arbitrary site pairs. */
+int lmc_de_pairs(lmc_ctx *ctx, int replica, const int64_t *pairs, int m, double *de);
+
+/* Total energy (EnergyPredictor::GetEnergy, EnergyPredictor.cpp:40-96,173-177)
+ * of one replica; counts (num_theta int64, may be NULL) receives the integer
+ * cluster census behind it. */
+int lmc_energy(lmc_ctx *ctx, int replica, double *energy, int64_t *counts);
+
+/* ------------------------------------------------------------------------- */
+/* Kinetic MC (KineticMcFirstOmp semantics, KineticMcAbstract.cpp:140-190)    */
+/* ------------------------------------------------------------------------- */
+#define LMC_RNG_MT19937_64 0 /* std::mt19937_64 + libstdc++ distributions: same stream as the reference */
+#define LMC_RNG_PHILOX 1     /* Philox4x32-10 counter-based, one stream per replica */
+
+typedef struct lmc_kmc_options {
+  int rng;                 /* LMC_RNG_* */
+  uint64_t seed;           /* replica r uses seed + r */
+  int barrier_kind;        /* LMC_BARRIER_QUARTIC or LMC_BARRIER_E0 */
+  int rate_corrector;      /* RateCorrector time factor (RateCorrector.hpp:17-24) */
+  const double *tt_time;   /* optional T(t) table (TimeTemperatureInterpolator), NULL if unused */
+  const double *tt_temp;
+  int tt_len;
+  int warps_per_replica;   /* 0 = autotuned */
+  int replicas_per_block;  /* 0 = autotuned */
+} lmc_kmc_options;
+
+/* Per-step record of replica `trace_replica` (for parity checks and logs). */
+typedef struct lmc_kmc_step {
+  int64_t vacancy;     /* vacancy site before the step */
+  int64_t target;      /* selected neighbour (lattice id) */
+  int32_t selected;    /* index in the id-sorted 1NN list */
+  int32_t pad;
+  double ea, de;       /* barrier and energy change of the selected event */
+  double total_rate;   /* sum of exp(-Ea beta) over the 12 events (no prefactor) */
+  double time;         /* simulated time after the step */
+  double energy;       /* energy after the step */
+} lmc_kmc_step;
+
+/* Initialises KMC state for every replica: temperature[r] (K), vacancy = the
+ * lowest-id X site, time = 0, energy = 0. */
+int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options *opt);
+/* Runs `steps` steps on every replica in one persistent launch. If trace is
+ * non-NULL it receives `steps` records of replica trace_replica; events12
+ * (NULL or 12 * 3 * steps doubles: target id, Ea, dE per id-sorted event)
+ * receives the full event lists of that replica. */
+int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace, double *events12);
+/* Per-replica state (any pointer may be NULL). */
+int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy);
+/* Device time (ms) of the last lmc_kmc_run / lmc_cmc_run launch (CUDA events on the context stream). */
+int lmc_last_run_ms(lmc_ctx *ctx, double *ms);
+
+/* ------------------------------------------------------------------------- */
+/* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */
+/* ------------------------------------------------------------------------- */
+#define LMC_CMC_REFERENCE_BATCH 0 /* mt19937_64 stream, batch of `batch` pairs as the reference draws them */
+#define LMC_CMC_THROUGHPUT 1      /* Philox, many non-overlapping pairs per round (see DESIGN) */
+
+typedef struct lmc_cmc_options {
+  int mode;          /* LMC_CMC_* */
+  uint64_t seed;
+  int batch;         /* reference-batch mode: pairs per batch (the OpenMP thread count) */
+  int candidates;    /* throughput mode: candidate pairs per round, 0 = automatic */
+} lmc_cmc_options;
+
+/* Runs CMC on one replica until at least `attempts` Metropolis tests were made.
+ * energy_io: in = current energy, out = energy after the run.
+ * attempts_done / accepted: totals of this call. */
+int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts, const lmc_cmc_options *opt,
+                double *energy_io, uint64_t *attempts_done, uint64_t *accepted);
+
+/* Host-writable stop flag polled by persistent kernels; also clears it when value = 0. */
+int lmc_request_stop(lmc_ctx *ctx, int value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LMC_GB300_H_ */

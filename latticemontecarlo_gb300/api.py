@@ -1,0 +1,224 @@
+"""Python front end of the C ABI (``include/lmc_gb300.h``).
+
+Thin wrappers that marshal numpy arrays into the library; every computation
+runs in ``liblmc_gb300.so`` (CUDA kernels for sm_103a). There is no CPU
+fallback: a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+
+from . import _native as N
+from ._native import check, ptr
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Model:
+    """Species alphabet and coefficient blocks (one reference coefficient file)."""
+
+    def __init__(self, handle: int, elements):
+        self._h = C.c_void_p(handle)
+        self.elements = list(elements)
+        nt, fm, f2 = C.c_int(), C.c_int(), C.c_int()
+        check(N.lib.lmc_model_layout(self._h, C.byref(nt), C.byref(fm), C.byref(f2)))
+        self.num_theta, self.f_mmm, self.f_mm2 = nt.value, fm.value, f2.value
+        buf = C.create_string_buffer(128)
+        check(N.lib.lmc_model_alphabet(self._h, buf, 128))
+        self.alphabet = buf.value.decode().split()
+
+    @classmethod
+    def create(cls, elements) -> "Model":
+        h = C.c_void_p()
+        check(N.lib.lmc_model_create(N.cstrings(elements), len(elements), C.byref(h)))
+        return cls(h.value, elements)
+
+    @classmethod
+    def from_json(cls, path, elements) -> "Model":
+        h = C.c_void_p()
+        check(N.lib.lmc_model_load_json(str(path).encode(), N.cstrings(elements), len(elements), C.byref(h)))
+        return cls(h.value, elements)
+
+    @classmethod
+    def from_coefficients(cls, coeffs: dict, elements) -> "Model":
+        """Builds a model from an in-memory coefficient dict (same layout as the JSON file)."""
+        m = cls.create(elements)
+        theta = _f64(coeffs["Base"]["theta"])
+        check(N.lib.lmc_model_set_base_theta(m._h, ptr(theta, C.c_double), theta.size))
+        for name, blk in coeffs.items():
+            if name == "Base" or m.code(name) < 0:
+                continue
+            arr = {k: _f64(v) for k, v in blk.items() if isinstance(v, list)}
+            if "U_mm2" in arr:
+                p = N.QuarticParams(arr["U_mmm"].shape[0], arr["U_mm2"].shape[0],
+                                    ptr(arr["mu_x_mmm"], C.c_double), ptr(arr["sigma_x_mmm"], C.c_double),
+                                    ptr(arr["mu_x_mm2"], C.c_double), ptr(arr["sigma_x_mm2"], C.c_double),
+                                    ptr(arr["U_mmm"], C.c_double), ptr(arr["U_mm2"], C.c_double),
+                                    ptr(arr["theta_D"], C.c_double), ptr(arr["theta_Ks"], C.c_double),
+                                    blk["mu_D"], blk["sigma_D"], blk["mu_Ks"], blk["sigma_Ks"])
+                check(N.lib.lmc_model_set_quartic(m._h, name.encode(), C.byref(p)))
+            if "theta_e0" in arr:
+                p = N.E0Params(arr["U_mmm"].shape[0], ptr(arr["mu_x_mmm"], C.c_double),
+                               ptr(arr["sigma_x_mmm"], C.c_double), ptr(arr["U_mmm"], C.c_double),
+                               ptr(arr["theta_e0"], C.c_double), blk["mu_e0"], blk["sigma_e0"])
+                check(N.lib.lmc_model_set_e0(m._h, name.encode(), C.byref(p)))
+        return m
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            N.lib.lmc_model_destroy(h)
+            self._h = None
+
+    def code(self, name: str) -> int:
+        return N.lib.lmc_model_species_code(self._h, name.encode())
+
+    def orbit_sizes(self, which: int) -> np.ndarray:
+        out = np.zeros(self.f_mmm if which == 0 else self.f_mm2, np.int32)
+        check(N.lib.lmc_model_feature_orbit_sizes(self._h, which, ptr(out, C.c_int32)))
+        return out
+
+    def host_encode_pair(self, n: int, species: np.ndarray, first: int, second: int):
+        sp = np.ascontiguousarray(species, dtype=np.int8)
+        cs, ce = np.zeros(self.num_theta, np.int32), np.zeros(self.num_theta, np.int32)
+        mm = np.zeros(self.f_mmm, np.int32)
+        mf, mb = np.zeros(self.f_mm2, np.int32), np.zeros(self.f_mm2, np.int32)
+        check(N.lib.lmc_host_encode_pair(self._h, n, ptr(sp, C.c_int8), first, second,
+                                         *[ptr(x, C.c_int32) for x in (cs, ce, mm, mf, mb)]))
+        return cs, ce, mm, mf, mb
+
+
+class KmcTrace:
+    """Per-step records of one replica (numpy structured view of lmc_kmc_step)."""
+
+    DTYPE = np.dtype([("vacancy", np.int64), ("target", np.int64), ("selected", np.int32), ("pad", np.int32),
+                      ("ea", np.float64), ("de", np.float64), ("total_rate", np.float64), ("time", np.float64),
+                      ("energy", np.float64)])
+
+
+class Context:
+    """A model's tables and a set of lattices ("replicas") resident on one GPU."""
+
+    def __init__(self, model: Model, device: int = 0):
+        self.model = model
+        h = C.c_void_p()
+        check(N.lib.lmc_ctx_create(model._h, device, C.byref(h)))
+        self._h = h
+        self.ns = np.zeros(0, np.int32)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            N.lib.lmc_ctx_destroy(h)
+            self._h = None
+
+    # lattices -------------------------------------------------------------
+    def set_lattices(self, ns, species: np.ndarray) -> None:
+        ns = np.ascontiguousarray(ns, dtype=np.int32)
+        sp = np.ascontiguousarray(species, dtype=np.int8)
+        check(N.lib.lmc_ctx_set_lattices(self._h, ns.size, ptr(ns, C.c_int32), ptr(sp, C.c_int8)))
+        self.ns = ns
+
+    def get_lattices(self) -> np.ndarray:
+        out = np.empty(int(N.lib.lmc_ctx_total_sites(self._h)), np.int8)
+        check(N.lib.lmc_ctx_get_lattices(self._h, ptr(out, C.c_int8)))
+        return out
+
+    def replica_offset(self, r: int) -> int:
+        return int(N.lib.lmc_ctx_replica_offset(self._h, r))
+
+    # predictors -----------------------------------------------------------
+    def barrier_batch(self, pairs, replica: int = 0, kind: int = N.LMC_BARRIER_QUARTIC):
+        p = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        m = p.shape[0]
+        ea, de, x, ks = (np.zeros(m) for _ in range(4))
+        check(N.lib.lmc_barrier_batch(self._h, replica, kind, ptr(p, C.c_int64), m, ptr(ea, C.c_double),
+                                      ptr(de, C.c_double), ptr(x, C.c_double), ptr(ks, C.c_double)))
+        return ea, de, x, ks
+
+    def encode_batch(self, pairs, replica: int = 0):
+        p = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        m, mo = p.shape[0], self.model
+        cs, ce = np.zeros((m, mo.num_theta), np.int32), np.zeros((m, mo.num_theta), np.int32)
+        mm = np.zeros((m, mo.f_mmm), np.int32)
+        mf, mb = np.zeros((m, mo.f_mm2), np.int32), np.zeros((m, mo.f_mm2), np.int32)
+        check(N.lib.lmc_encode_batch(self._h, replica, ptr(p, C.c_int64), m,
+                                     *[ptr(x, C.c_int32) for x in (cs, ce, mm, mf, mb)]))
+        return cs, ce, mm, mf, mb
+
+    def de_pairs(self, pairs, replica: int = 0) -> np.ndarray:
+        p = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        de = np.zeros(p.shape[0])
+        check(N.lib.lmc_de_pairs(self._h, replica, ptr(p, C.c_int64), p.shape[0], ptr(de, C.c_double)))
+        return de
+
+    def energy(self, replica: int = 0):
+        e = C.c_double()
+        counts = np.zeros(self.model.num_theta, np.int64)
+        check(N.lib.lmc_energy(self._h, replica, C.byref(e), ptr(counts, C.c_int64)))
+        return e.value, counts
+
+    # kinetic MC -----------------------------------------------------------
+    def kmc_init(self, temperatures, seed: int = 0, rng: int = N.LMC_RNG_PHILOX, kind: int = N.LMC_BARRIER_QUARTIC,
+                 rate_corrector: bool = False, tt=None, warps_per_replica: int = 0, replicas_per_block: int = 0):
+        temps = np.ascontiguousarray(np.broadcast_to(np.asarray(temperatures, np.float64), (self.ns.size,)))
+        self._tt = None
+        opt = N.KmcOptions(rng, seed, kind, int(rate_corrector), None, None, 0, warps_per_replica,
+                           replicas_per_block)
+        if tt is not None:
+            t0, t1 = _f64(tt[0]), _f64(tt[1])
+            self._tt = (t0, t1)
+            opt.tt_time, opt.tt_temp, opt.tt_len = ptr(t0, C.c_double), ptr(t1, C.c_double), t0.size
+        check(N.lib.lmc_kmc_init(self._h, ptr(temps, C.c_double), C.byref(opt)))
+
+    def kmc_run(self, steps: int, trace_replica: int | None = None, events: bool = False):
+        trace = np.zeros(steps, KmcTrace.DTYPE) if trace_replica is not None else None
+        ev = np.zeros((steps, 12, 3)) if (events and trace_replica is not None) else None
+        check(N.lib.lmc_kmc_run(self._h, steps, -1 if trace_replica is None else trace_replica,
+                                trace.ctypes.data_as(C.POINTER(N.KmcStep)) if trace is not None else None,
+                                ptr(ev, C.c_double) if ev is not None else None))
+        return trace, ev
+
+    def kmc_state(self):
+        r = self.ns.size
+        vac, steps = np.zeros(r, np.int64), np.zeros(r, np.uint64)
+        time, energy = np.zeros(r), np.zeros(r)
+        check(N.lib.lmc_kmc_get_state(self._h, ptr(vac, C.c_int64), ptr(steps, C.c_uint64), ptr(time, C.c_double),
+                                      ptr(energy, C.c_double)))
+        return vac, steps, time, energy
+
+    def last_run_ms(self) -> float:
+        ms = C.c_double()
+        check(N.lib.lmc_last_run_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    # canonical MC ---------------------------------------------------------
+    def cmc_run(self, temperature: float, attempts: int, replica: int = 0, mode: int = N.LMC_CMC_THROUGHPUT,
+                seed: int = 0, batch: int = 1, candidates: int = 0, energy: float = 0.0):
+        opt = N.CmcOptions(mode, seed, batch, candidates)
+        e = C.c_double(energy)
+        done, acc = C.c_uint64(), C.c_uint64()
+        check(N.lib.lmc_cmc_run(self._h, replica, temperature, attempts, C.byref(opt), C.byref(e), C.byref(done),
+                                C.byref(acc)))
+        return e.value, done.value, acc.value
+
+    def request_stop(self, value: int = 1) -> None:
+        check(N.lib.lmc_request_stop(self._h, value))
+
+
+def load_coefficients(path) -> dict:
+    with open(path) as f:
+        return json.load(f)
+
+
+def write_coefficients(coeffs: dict, path) -> Path:
+    path = Path(path)
+    with open(path, "w") as f:
+        json.dump(coeffs, f)
+    return path

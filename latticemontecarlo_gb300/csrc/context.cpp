@@ -1,0 +1,1111 @@
+// C ABI of the GB300 lattice-MC hot path (include/lmc_gb300.h): models,
+// host-only geometry queries, device contexts, table packing and launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <ios>
+#include <tuple>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/lmc_gb300.h"
+#include "geometry.hpp"
+#include "kernels.cuh"
+#include "model.hpp"
+
+namespace {
+thread_local std::string g_error;
+
+struct LmcError : std::runtime_error {
+  int code;
+  LmcError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void CudaCheck(cudaError_t err, const char *what) {
+  if (err != cudaSuccess) throw LmcError(LMC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+template <typename F>
+int Guard(F &&f) {
+  try {
+    f();
+    return LMC_OK;
+  } catch (const LmcError &e) {
+    g_error = e.what();
+    return e.code;
+  } catch (const std::out_of_range &e) {
+    g_error = e.what();
+    return LMC_ERR_OUT_OF_RANGE;
+  } catch (const std::ios_base::failure &e) {
+    g_error = e.what();
+    return LMC_ERR_IO;
+  } catch (const std::invalid_argument &e) {
+    g_error = e.what();
+    return LMC_ERR_INVALID_ARGUMENT;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+    return LMC_ERR_INVALID_ARGUMENT;
+  }
+}
+
+void Require(bool ok, int code, const std::string &msg) {
+  if (!ok) throw LmcError(code, msg);
+}
+
+int8_t Pack4(int v) { return static_cast<int8_t>(v); }
+
+uint32_t PackEnv(const lmc::EnvCluster &c, int base) {
+  const uint32_t b = c.b < 0 ? 63u : static_cast<uint32_t>(c.b);
+  return static_cast<uint32_t>(c.a) | (b << 6) | (static_cast<uint32_t>(c.mode) << 12) | (static_cast<uint32_t>(base) << 14);
+}
+
+// Device buffer owned by a context.
+struct DevBuf {
+  void *p{nullptr};
+  size_t bytes{0};
+  void Alloc(size_t b) {
+    Free();
+    if (b == 0) b = 16;
+    CudaCheck(cudaMalloc(&p, b), "cudaMalloc");
+    bytes = b;
+  }
+  void Ensure(size_t b) {
+    if (b > bytes) Alloc(b);
+  }
+  void Free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+}  // namespace
+
+struct lmc_model {
+  lmc::Model m;
+};
+
+struct lmc_ctx {
+  int device{0};
+  cudaStream_t stream{nullptr};
+  cudaEvent_t ev0{nullptr}, ev1{nullptr};
+  lmc::Model model;
+  lmc::FoldedModel fm;
+  lmc::DevTables t{};
+  std::vector<DevBuf> tables;
+  // lattices
+  int num_replicas{0};
+  std::vector<int> n;
+  std::vector<long long> offsets;
+  long long total_sites{0};
+  DevBuf species, lat_off, lat_n;
+  // batch scratch
+  DevBuf pairs, out0, out1, out2, out3, status, counts, energy, enc;
+  // KMC
+  bool kmc_ready{false};
+  lmc_kmc_options kmc_opt{};
+  DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
+  int tt_len{0};
+  // CMC
+  DevBuf c_mark, c_mark_list, c_claim, c_cand, c_eacc, c_stats;
+  std::map<int, std::pair<uint64_t, DevBuf>> c_mt;  // per replica: seed and MT state
+  // host-mapped stop flag
+  int *h_stop{nullptr};
+  int *d_stop{nullptr};
+  double last_ms{0};
+
+  ~lmc_ctx() {
+    for (auto &b : tables) b.Free();
+    for (DevBuf *b : {&species, &lat_off, &lat_n, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
+                      &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
+                      &k_tt_time, &k_tt_temp, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+      b->Free();
+    for (auto &kv : c_mt) kv.second.second.Free();
+    if (h_stop) cudaFreeHost(h_stop);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  const T *Upload(const std::vector<T> &v) {
+    DevBuf b;
+    b.Alloc(std::max<size_t>(v.size() * sizeof(T), 16));
+    if (!v.empty()) CudaCheck(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+    tables.push_back(b);
+    return b.as<T>();
+  }
+  void Sync() { CudaCheck(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+  int ReadStatus() {
+    int st = 0;
+    CudaCheck(cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "status copy");
+    Sync();
+    return st;
+  }
+  void ClearStatus() { CudaCheck(cudaMemsetAsync(status.p, 0, sizeof(int), stream), "status clear"); }
+  void CheckReplica(int r) const {
+    Require(r >= 0 && r < num_replicas, LMC_ERR_OUT_OF_RANGE, "replica index out of range");
+  }
+};
+
+namespace {
+
+void RaiseStatus(int st, const char *what) {
+  if (st == 0) return;
+  std::string m = std::string(what) + ": ";
+  if (st & lmc::kStatusBadSite) throw LmcError(LMC_ERR_OUT_OF_RANGE, m + "lattice id out of range");
+  if (st & lmc::kStatusNotNeighbor)
+    throw LmcError(LMC_ERR_OUT_OF_RANGE, m + "Neighbor not found for lattice pair in GetPairFlatIndex");
+  if (st & lmc::kStatusNoCoefficients)
+    throw LmcError(LMC_ERR_OUT_OF_RANGE, m + "migrating element has no coefficients");
+  if (st & lmc::kStatusBadCluster) throw LmcError(LMC_ERR_OUT_OF_RANGE, m + "Cluster not found in ClusterIndexer");
+  if (st & lmc::kStatusXInEnv)
+    throw LmcError(LMC_ERR_OUT_OF_RANGE, m + "vacancy inside a jump environment has no one-hot slot");
+  if (st & lmc::kStatusNumeric) throw LmcError(LMC_ERR_NUMERIC, m + "non-finite barrier or non-positive total rate");
+  if (st & lmc::kStatusStopped) throw LmcError(LMC_ERR_STOPPED, m + "stopped");
+}
+
+// Builds and uploads every read-only table of a context.
+void BuildTables(lmc_ctx *c) {
+  const auto &pt = lmc::GetPairTables();
+  const auto &fm = c->fm;
+  lmc::DevTables &t = c->t;
+  std::vector<int8_t> dir, st_off, mmm_off, mm2_off, site_off;
+  for (int d = 0; d < lmc::kDirections; ++d) {
+    for (int v : {pt.dir[d].x, pt.dir[d].y, pt.dir[d].z, 0}) dir.push_back(Pack4(v));
+    for (int k = 0; k < lmc::kStateSites; ++k)
+      for (int v : {pt.state_off[d][k].x, pt.state_off[d][k].y, pt.state_off[d][k].z, 0}) st_off.push_back(Pack4(v));
+    for (int k = 0; k < lmc::kEnvSites; ++k) {
+      for (int v : {pt.mmm_off[d][k].x, pt.mmm_off[d][k].y, pt.mmm_off[d][k].z, 0}) mmm_off.push_back(Pack4(v));
+      for (int v : {pt.mm2_off[d][k].x, pt.mm2_off[d][k].y, pt.mm2_off[d][k].z, 0}) mm2_off.push_back(Pack4(v));
+    }
+  }
+  for (int k = 0; k < lmc::kSiteSites; ++k)
+    for (int v : {pt.site_off[k].x, pt.site_off[k].y, pt.site_off[k].z, 0}) site_off.push_back(Pack4(v));
+  // jump dE clusters: state clusters with exactly one pair site
+  std::vector<uint32_t> de_cl, state_all;
+  for (const auto &cl : pt.state_clusters) {
+    uint32_t w = static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(cl.size) << 3);
+    for (int q = 0; q < 3; ++q) w |= static_cast<uint32_t>(q < cl.size ? cl.idx[q] : 0) << (5 + 6 * q);
+    state_all.push_back(w);
+    int has_first = 0, has_second = 0;
+    std::vector<int> others;
+    for (int q = 0; q < cl.size; ++q) {
+      if (cl.idx[q] == pt.pos_first) has_first = 1;
+      else if (cl.idx[q] == pt.pos_second) has_second = 1;
+      else others.push_back(cl.idx[q]);
+    }
+    if (has_first + has_second != 1 || others.empty()) continue;
+    uint32_t d = static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(has_second) << 3) |
+                 (static_cast<uint32_t>(others[0]) << 4) | (static_cast<uint32_t>(others.size() > 1 ? others[1] : 63) << 10);
+    de_cl.push_back(d);
+  }
+  auto env = [&](const lmc::EnvEncoding &e) {
+    std::vector<uint32_t> out;
+    const auto off = e.OrbitOffsets(fm.num_onehot);
+    Require(off.back() < (1 << 14), LMC_ERR_UNSUPPORTED, "feature layout too large");
+    for (const auto &cl : e.clusters) out.push_back(PackEnv(cl, off[cl.orbit]));
+    return out;
+  };
+  std::vector<uint32_t> mmm_cl = env(pt.mmm), mm2_cl = env(pt.mm2);
+  std::vector<uint32_t> site_cl;
+  for (const auto &cl : pt.site_clusters) {
+    std::vector<int> others;
+    for (int q = 0; q < cl.size; ++q)
+      if (cl.idx[q] != pt.site_center) others.push_back(cl.idx[q]);
+    const uint32_t o1 = others.size() > 0 ? others[0] : 63, o2 = others.size() > 1 ? others[1] : 63;
+    site_cl.push_back(static_cast<uint32_t>(cl.label) | (o1 << 3) | (o2 << 9));
+  }
+  auto site_index = [&](lmc::I3 s) {
+    for (int k = 0; k < lmc::kSiteSites; ++k)
+      if (pt.site_off[k] == s) return k;
+    throw std::logic_error("census offset not in the site list");
+  };
+  std::vector<uint32_t> census;
+  for (const auto &tr : pt.census_triplets)
+    census.push_back(static_cast<uint32_t>(tr.label) | (static_cast<uint32_t>(site_index(tr.s2)) << 3) |
+                     (static_cast<uint32_t>(site_index(tr.s3)) << 9));
+  // KMC neighbourhood of a vacancy: union of the 12 jumps' lists
+  std::vector<lmc::I3> local;
+  auto add = [&](lmc::I3 s) {
+    if (std::find(local.begin(), local.end(), s) == local.end()) local.push_back(s);
+  };
+  for (int d = 0; d < lmc::kDirections; ++d) {
+    const int db = lmc::DirectionIndex(lmc::I3{0, 0, 0} - pt.dir[d]);
+    for (int k = 0; k < lmc::kStateSites; ++k) add(pt.state_off[d][k]);
+    for (int k = 0; k < lmc::kEnvSites; ++k) {
+      add(pt.mmm_off[d][k]);
+      add(pt.mm2_off[d][k]);
+      add(pt.dir[d] + pt.mm2_off[db][k]);
+    }
+  }
+  std::sort(local.begin(), local.end(), [](lmc::I3 a, lmc::I3 b) {
+    return std::tie(a.x, a.y, a.z) < std::tie(b.x, b.y, b.z);
+  });
+  Require(static_cast<int>(local.size()) == lmc::kLocalSites, LMC_ERR_UNSUPPORTED, "unexpected KMC neighbourhood size");
+  auto lidx = [&](lmc::I3 s) {
+    return static_cast<uint8_t>(std::find(local.begin(), local.end(), s) - local.begin());
+  };
+  std::vector<int8_t> local_off;
+  for (const auto &s : local)
+    for (int v : {s.x, s.y, s.z, 0}) local_off.push_back(Pack4(v));
+  std::vector<uint8_t> l_st, l_mmm, l_mm2f, l_mm2b;
+  for (int d = 0; d < lmc::kDirections; ++d) {
+    const int db = lmc::DirectionIndex(lmc::I3{0, 0, 0} - pt.dir[d]);
+    for (int k = 0; k < lmc::kStateSites; ++k) l_st.push_back(lidx(pt.state_off[d][k]));
+    for (int k = 0; k < lmc::kEnvSites; ++k) {
+      l_mmm.push_back(lidx(pt.mmm_off[d][k]));
+      l_mm2f.push_back(lidx(pt.mm2_off[d][k]));
+      l_mm2b.push_back(lidx(pt.dir[d] + pt.mm2_off[db][k]));
+    }
+  }
+  // small model tables
+  Require(fm.num_onehot <= lmc::kMaxOnehot - 1, LMC_ERR_UNSUPPORTED, "too many one-hot elements");
+  std::vector<int8_t> rank(8, lmc::kMaxOnehot - 1), slot(8, -1), ptype(192, -1);
+  for (int code = 0; code < fm.num_species; ++code) {
+    rank[code] = fm.onehot_rank[code] < 0 ? lmc::kMaxOnehot - 1 : fm.onehot_rank[code];
+    slot[code] = fm.migrant_slot[code];
+  }
+  for (int mode = 0; mode < 3; ++mode)
+    for (int ra = 0; ra < fm.num_onehot; ++ra)
+      for (int rb = 0; rb < fm.num_onehot; ++rb)
+        ptype[(mode * 8 + ra) * 8 + rb] = static_cast<int8_t>(lmc::PairType(mode, ra, rb, fm.num_onehot));
+  const int slots = static_cast<int>(fm.slot_code.size());
+  Require(slots <= lmc::kMaxSlots, LMC_ERR_UNSUPPORTED, "too many migrating elements");
+  std::vector<uint8_t> hq(lmc::kMaxSlots, 0), he(lmc::kMaxSlots, 0);
+  std::vector<double> form(lmc::kMaxSlots * 12, 0.0);
+  std::vector<long long> wd, wks, we0;
+  for (int sidx = 0; sidx < slots; ++sidx) {
+    hq[sidx] = fm.has_quartic[sidx];
+    he[sidx] = fm.has_e0[sidx];
+    const lmc::FoldedForm *forms[3] = {&fm.quartic_d[sidx], &fm.quartic_ks[sidx], &fm.e0[sidx]};
+    for (int q = 0; q < 3; ++q) {
+      form[sidx * 12 + q * 4 + 0] = std::ldexp(1.0, -forms[q]->shift);
+      form[sidx * 12 + q * 4 + 1] = forms[q]->c;
+      form[sidx * 12 + q * 4 + 2] = forms[q]->sigma;
+      form[sidx * 12 + q * 4 + 3] = forms[q]->mu;
+    }
+    wd.insert(wd.end(), fm.quartic_d[sidx].w.begin(), fm.quartic_d[sidx].w.end());
+    wks.insert(wks.end(), fm.quartic_ks[sidx].w.begin(), fm.quartic_ks[sidx].w.end());
+    we0.insert(we0.end(), fm.e0[sidx].w.begin(), fm.e0[sidx].w.end());
+  }
+  std::vector<long long> wde(fm.w_de.begin(), fm.w_de.end());
+  t.dir = c->Upload(dir);
+  t.state_off = c->Upload(st_off);
+  t.mmm_off = c->Upload(mmm_off);
+  t.mm2_off = c->Upload(mm2_off);
+  t.site_off = c->Upload(site_off);
+  t.local_off = c->Upload(local_off);
+  t.local_st = c->Upload(l_st);
+  t.local_mmm = c->Upload(l_mmm);
+  t.local_mm2f = c->Upload(l_mm2f);
+  t.local_mm2b = c->Upload(l_mm2b);
+  t.de_cl = c->Upload(de_cl);
+  t.mmm_cl = c->Upload(mmm_cl);
+  t.mm2_cl = c->Upload(mm2_cl);
+  t.site_cl = c->Upload(site_cl);
+  t.census_tri = c->Upload(census);
+  t.state_all = c->Upload(state_all);
+  t.n_de_cl = static_cast<int>(de_cl.size());
+  t.n_mmm_cl = static_cast<int>(mmm_cl.size());
+  t.n_mm2_cl = static_cast<int>(mm2_cl.size());
+  t.n_site_cl = static_cast<int>(site_cl.size());
+  t.n_census_tri = static_cast<int>(census.size());
+  t.n_state_all = static_cast<int>(state_all.size());
+  t.pos_first = pt.pos_first;
+  t.pos_second = pt.pos_second;
+  t.site_center = pt.site_center;
+  t.num_species = fm.num_species;
+  t.num_onehot = fm.num_onehot;
+  t.x_code = fm.x_code;
+  t.num_theta = fm.num_theta;
+  t.f_mmm = fm.f_mmm;
+  t.f_mm2 = fm.f_mm2;
+  t.num_slots = slots;
+  t.onehot_rank = c->Upload(rank);
+  t.migrant_slot = c->Upload(slot);
+  t.pairtype = c->Upload(ptype);
+  t.has_quartic = c->Upload(hq);
+  t.has_e0 = c->Upload(he);
+  t.cluster_index = c->Upload(fm.cluster_index);
+  t.w_de = c->Upload(wde);
+  t.de_scale = std::ldexp(1.0, -fm.de_shift);
+  t.w_d = c->Upload(wd);
+  t.w_ks = c->Upload(wks);
+  t.w_e0 = c->Upload(we0);
+  t.form = c->Upload(form);
+  t.theta = c->Upload(fm.theta);
+  t.census_bonds = c->Upload(fm.census_bonds);
+}
+
+std::vector<std::string> Names(const char *const *names, int n) {
+  Require(names != nullptr && n > 0, LMC_ERR_INVALID_ARGUMENT, "empty element set");
+  std::vector<std::string> v;
+  for (int i = 0; i < n; ++i) {
+    Require(names[i] != nullptr, LMC_ERR_INVALID_ARGUMENT, "null element name");
+    v.emplace_back(names[i]);
+  }
+  return v;
+}
+
+int CodeOf(const lmc::Model &m, const char *name) {
+  Require(name != nullptr, LMC_ERR_INVALID_ARGUMENT, "null element name");
+  const int c = m.Code(name);
+  Require(c >= 0, LMC_ERR_OUT_OF_RANGE, std::string("element ") + name + " is not in the model alphabet");
+  return c;
+}
+
+std::vector<double> Vec(const double *p, int n, const char *what) {
+  Require(p != nullptr || n == 0, LMC_ERR_INVALID_ARGUMENT, std::string(what) + " is null");
+  return std::vector<double>(p, p + n);
+}
+
+void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
+  // Enough warps to fill the GPU: one warp per replica when there are
+  // thousands of replicas, up to one warp per jump for a single trajectory.
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const long long target = static_cast<long long>(sms) * 24;
+  int best = 12;
+  for (int cand : {1, 2, 3, 4, 6, 12})
+    if (static_cast<long long>(c->num_replicas) * cand >= target) {
+      best = cand;
+      break;
+    }
+  *g = best;
+  *rpb = std::max(1, 8 / best);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *lmc_strerror(int status) {
+  switch (status) {
+    case LMC_OK: return "ok";
+    case LMC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case LMC_ERR_OUT_OF_RANGE: return "out of range";
+    case LMC_ERR_IO: return "i/o error";
+    case LMC_ERR_CUDA: return "CUDA error";
+    case LMC_ERR_NO_DEVICE: return "no usable CUDA device";
+    case LMC_ERR_NUMERIC: return "numeric error";
+    case LMC_ERR_STOPPED: return "stopped";
+    case LMC_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char *lmc_last_error(void) { return g_error.c_str(); }
+const char *lmc_version(void) { return "lmc_gb300 0.1 sm_103a"; }
+
+int lmc_model_create(const char *const *element_names, int num_elements, lmc_model **out) {
+  return Guard([&] {
+    Require(out != nullptr, LMC_ERR_INVALID_ARGUMENT, "out is null");
+    auto m = std::make_unique<lmc_model>();
+    m->m = lmc::MakeModel(Names(element_names, num_elements));
+    *out = m.release();
+  });
+}
+
+int lmc_model_load_json(const char *path, const char *const *element_names, int num_elements, lmc_model **out) {
+  return Guard([&] {
+    Require(out != nullptr && path != nullptr, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    auto m = std::make_unique<lmc_model>();
+    m->m = lmc::MakeModel(Names(element_names, num_elements));
+    lmc::LoadJson(m->m, path);
+    *out = m.release();
+  });
+}
+
+void lmc_model_destroy(lmc_model *model) { delete model; }
+
+int lmc_model_num_species(const lmc_model *model) { return model ? model->m.NumSpecies() : -1; }
+
+int lmc_model_species_code(const lmc_model *model, const char *name) {
+  if (!model || !name) return -1;
+  return model->m.Code(name);
+}
+
+int lmc_model_alphabet(const lmc_model *model, char *buf, int buflen) {
+  return Guard([&] {
+    Require(model && buf && buflen > 0, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    std::string s;
+    for (size_t i = 0; i < model->m.alphabet.size(); ++i) s += (i ? " " : "") + model->m.alphabet[i];
+    Require(static_cast<int>(s.size()) < buflen, LMC_ERR_INVALID_ARGUMENT, "buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+  });
+}
+
+int lmc_model_layout(const lmc_model *model, int *num_theta, int *f_mmm, int *f_mm2) {
+  return Guard([&] {
+    Require(model != nullptr, LMC_ERR_INVALID_ARGUMENT, "model is null");
+    if (num_theta) *num_theta = model->m.num_theta;
+    if (f_mmm) *f_mmm = model->m.FeaturesMmm();
+    if (f_mm2) *f_mm2 = model->m.FeaturesMm2();
+  });
+}
+
+int lmc_model_feature_orbit_sizes(const lmc_model *model, int which, int32_t *sizes) {
+  return Guard([&] {
+    Require(model && sizes && (which == 0 || which == 1), LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    const auto &e = which == 0 ? lmc::GetPairTables().mmm : lmc::GetPairTables().mm2;
+    const auto off = e.OrbitOffsets(model->m.NumOnehot());
+    for (size_t o = 0; o < e.orbits.size(); ++o)
+      for (int j = off[o]; j < off[o + 1]; ++j) sizes[j] = e.orbits[o].size;
+  });
+}
+
+int lmc_model_set_base_theta(lmc_model *model, const double *theta, int n) {
+  return Guard([&] {
+    Require(model != nullptr, LMC_ERR_INVALID_ARGUMENT, "model is null");
+    Require(n == model->m.num_theta, LMC_ERR_INVALID_ARGUMENT,
+            "theta has " + std::to_string(n) + " entries, expected " + std::to_string(model->m.num_theta));
+    model->m.base_theta = Vec(theta, n, "theta");
+  });
+}
+
+int lmc_model_set_quartic(lmc_model *model, const char *migrant, const lmc_quartic_params *p) {
+  return Guard([&] {
+    Require(model && p, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    const int code = CodeOf(model->m, migrant);
+    const int fm = model->m.FeaturesMmm(), f2 = model->m.FeaturesMm2();
+    Require(p->k_mmm > 0 && p->k_mm2 > 0, LMC_ERR_INVALID_ARGUMENT, "k must be positive");
+    lmc::QuarticBlock q;
+    q.k_mmm = p->k_mmm;
+    q.k_mm2 = p->k_mm2;
+    q.mu_x_mmm = Vec(p->mu_x_mmm, fm, "mu_x_mmm");
+    q.sigma_x_mmm = Vec(p->sigma_x_mmm, fm, "sigma_x_mmm");
+    q.mu_x_mm2 = Vec(p->mu_x_mm2, f2, "mu_x_mm2");
+    q.sigma_x_mm2 = Vec(p->sigma_x_mm2, f2, "sigma_x_mm2");
+    q.u_mmm = Vec(p->u_mmm, p->k_mmm * fm, "u_mmm");
+    q.u_mm2 = Vec(p->u_mm2, p->k_mm2 * f2, "u_mm2");
+    q.theta_d = Vec(p->theta_d, p->k_mmm, "theta_d");
+    q.theta_ks = Vec(p->theta_ks, p->k_mm2, "theta_ks");
+    q.mu_d = p->mu_d;
+    q.sigma_d = p->sigma_d;
+    q.mu_ks = p->mu_ks;
+    q.sigma_ks = p->sigma_ks;
+    model->m.quartic[code] = std::move(q);
+  });
+}
+
+int lmc_model_set_e0(lmc_model *model, const char *migrant, const lmc_e0_params *p) {
+  return Guard([&] {
+    Require(model && p, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    const int code = CodeOf(model->m, migrant);
+    const int fm = model->m.FeaturesMmm();
+    Require(p->k_mmm > 0, LMC_ERR_INVALID_ARGUMENT, "k must be positive");
+    lmc::E0Block b;
+    b.k_mmm = p->k_mmm;
+    b.mu_x_mmm = Vec(p->mu_x_mmm, fm, "mu_x_mmm");
+    b.sigma_x_mmm = Vec(p->sigma_x_mmm, fm, "sigma_x_mmm");
+    b.u_mmm = Vec(p->u_mmm, p->k_mmm * fm, "u_mmm");
+    b.theta_e0 = Vec(p->theta_e0, p->k_mmm, "theta_e0");
+    b.mu_e0 = p->mu_e0;
+    b.sigma_e0 = p->sigma_e0;
+    model->m.e0[code] = std::move(b);
+  });
+}
+
+int lmc_geom_neighbors(int n, int64_t site, int64_t *out42) {
+  return Guard([&] {
+    Require(n >= 6 && out42, LMC_ERR_INVALID_ARGUMENT, "n must be >= 6");
+    const lmc::Fcc fcc{n};
+    Require(site >= 0 && site < fcc.NumSites(), LMC_ERR_OUT_OF_RANGE, "site out of range");
+    int k = 0;
+    for (int shell = 1; shell <= 3; ++shell)
+      for (auto id : lmc::SortedNeighbors(fcc, site, shell)) out42[k++] = id;
+  });
+}
+
+int lmc_geom_pair_lists(int n, int64_t first, int64_t second, int64_t *state60, int64_t *mmm58, int64_t *mm258) {
+  return Guard([&] {
+    Require(n >= 6, LMC_ERR_INVALID_ARGUMENT, "n must be >= 6");
+    const lmc::Fcc fcc{n};
+    const auto &pt = lmc::GetPairTables();
+    Require(first >= 0 && second >= 0 && first < fcc.NumSites() && second < fcc.NumSites(), LMC_ERR_OUT_OF_RANGE,
+            "site out of range");
+    const lmc::I3 hi = fcc.Coord(first), hj = fcc.Coord(second);
+    auto mi = [&](int v) { const int m2 = 2 * n; v %= m2; if (v < 0) v += m2; return v >= n ? v - m2 : v; };
+    const lmc::I3 d{mi(hj.x - hi.x), mi(hj.y - hi.y), mi(hj.z - hi.z)};
+    const int di = lmc::DirectionIndex(d);
+    Require(di >= 0, LMC_ERR_OUT_OF_RANGE, "Neighbor not found for lattice pair in GetPairFlatIndex");
+    for (int k = 0; k < lmc::kStateSites && state60; ++k) state60[k] = fcc.Id(fcc.Wrap(hi + pt.state_off[di][k]));
+    for (int k = 0; k < lmc::kEnvSites && mmm58; ++k) mmm58[k] = fcc.Id(fcc.Wrap(hi + pt.mmm_off[di][k]));
+    for (int k = 0; k < lmc::kEnvSites && mm258; ++k) mm258[k] = fcc.Id(fcc.Wrap(hi + pt.mm2_off[di][k]));
+  });
+}
+
+int lmc_geom_site_list(int n, int64_t site, int64_t *out43) {
+  return Guard([&] {
+    Require(n >= 6 && out43, LMC_ERR_INVALID_ARGUMENT, "n must be >= 6");
+    const lmc::Fcc fcc{n};
+    Require(site >= 0 && site < fcc.NumSites(), LMC_ERR_OUT_OF_RANGE, "site out of range");
+    const auto &pt = lmc::GetPairTables();
+    const lmc::I3 h = fcc.Coord(site);
+    for (int k = 0; k < lmc::kSiteSites; ++k) out43[k] = fcc.Id(fcc.Wrap(h + pt.site_off[k]));
+  });
+}
+
+int lmc_geom_mapping_sizes(int *counts20) {
+  return Guard([&] {
+    Require(counts20 != nullptr, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    const auto &pt = lmc::GetPairTables();
+    std::fill(counts20, counts20 + 20, 0);
+    for (const auto &c : pt.state_clusters) ++counts20[c.label];
+    for (const auto &c : pt.site_clusters) ++counts20[8 + c.label];
+    counts20[16] = static_cast<int>(pt.mmm.orbits.size());
+    counts20[17] = static_cast<int>(pt.mm2.orbits.size());
+    counts20[18] = static_cast<int>(pt.mmm.clusters.size());
+    counts20[19] = static_cast<int>(pt.mm2.clusters.size());
+  });
+}
+
+int lmc_geom_env_mapping(int which, int32_t *orbit_a_b, int cap, int *n) {
+  return Guard([&] {
+    Require(which == 0 || which == 1, LMC_ERR_INVALID_ARGUMENT, "which must be 0 (MMM) or 1 (MM2)");
+    const auto &e = which == 0 ? lmc::GetPairTables().mmm : lmc::GetPairTables().mm2;
+    if (n) *n = static_cast<int>(e.clusters.size());
+    for (int i = 0; i < static_cast<int>(e.clusters.size()) && i < cap && orbit_a_b; ++i) {
+      orbit_a_b[3 * i] = e.clusters[i].orbit;
+      orbit_a_b[3 * i + 1] = e.clusters[i].a;
+      orbit_a_b[3 * i + 2] = e.clusters[i].b;
+    }
+  });
+}
+
+int lmc_host_encode_pair(const lmc_model *model, int n, const int8_t *species, int64_t first, int64_t second,
+                         int32_t *state_start, int32_t *state_end, int32_t *mmm, int32_t *mm2_fwd,
+                         int32_t *mm2_bwd) {
+  return Guard([&] {
+    Require(model && species && n >= 6, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    lmc::HostEncodePair(model->m, n, species, first, second, state_start, state_end, mmm, mm2_fwd, mm2_bwd);
+  });
+}
+
+int lmc_ctx_create(const lmc_model *model, int device, lmc_ctx **out) {
+  return Guard([&] {
+    Require(model && out, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+      cudaGetLastError();
+      throw LmcError(LMC_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    Require(device >= 0 && device < count, LMC_ERR_NO_DEVICE, "device index out of range");
+    CudaCheck(cudaSetDevice(device), "cudaSetDevice");
+    auto c = std::make_unique<lmc_ctx>();
+    c->device = device;
+    c->model = model->m;
+    c->fm = lmc::Fold(c->model);
+    CudaCheck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    CudaCheck(cudaEventCreate(&c->ev0), "cudaEventCreate");
+    CudaCheck(cudaEventCreate(&c->ev1), "cudaEventCreate");
+    CudaCheck(cudaHostAlloc(reinterpret_cast<void **>(&c->h_stop), sizeof(int), cudaHostAllocMapped),
+              "cudaHostAlloc");
+    *c->h_stop = 0;
+    CudaCheck(cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->d_stop), c->h_stop, 0), "mapped pointer");
+    BuildTables(c.get());
+    c->status.Alloc(sizeof(int));
+    c->counts.Alloc(sizeof(unsigned long long) * 256);
+    c->energy.Alloc(sizeof(double) * 4);
+    *out = c.release();
+  });
+}
+
+void lmc_ctx_destroy(lmc_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+}
+
+int lmc_ctx_synchronize(lmc_ctx *ctx) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    ctx->Sync();
+  });
+}
+
+int lmc_ctx_set_lattices(lmc_ctx *ctx, int num_replicas, const int32_t *n, const int8_t *species) {
+  return Guard([&] {
+    Require(ctx && n && species && num_replicas > 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    std::vector<int> nn(n, n + num_replicas);
+    std::vector<long long> off(num_replicas);
+    long long total = 0;
+    for (int r = 0; r < num_replicas; ++r) {
+      Require(nn[r] >= 6 && nn[r] <= 1000, LMC_ERR_UNSUPPORTED, "supercell edge must be in [6, 1000]");
+      off[r] = total;
+      total += 4LL * nn[r] * nn[r] * nn[r];
+    }
+    const int e = ctx->fm.num_species;
+    for (long long i = 0; i < total; ++i)
+      Require(species[i] >= 0 && species[i] < e, LMC_ERR_OUT_OF_RANGE, "species code out of range");
+    if (total + 64 > static_cast<long long>(ctx->species.bytes)) ctx->species.Alloc(total + 64);
+    ctx->lat_off.Alloc(sizeof(long long) * num_replicas);
+    ctx->lat_n.Alloc(sizeof(int) * num_replicas);
+    CudaCheck(cudaMemcpyAsync(ctx->species.p, species, total, cudaMemcpyHostToDevice, ctx->stream), "H2D species");
+    CudaCheck(cudaMemcpyAsync(ctx->lat_off.p, off.data(), sizeof(long long) * num_replicas, cudaMemcpyHostToDevice,
+                              ctx->stream),
+              "H2D offsets");
+    CudaCheck(cudaMemcpyAsync(ctx->lat_n.p, nn.data(), sizeof(int) * num_replicas, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D n");
+    ctx->Sync();
+    ctx->num_replicas = num_replicas;
+    ctx->n = nn;
+    ctx->offsets = off;
+    ctx->total_sites = total;
+    ctx->kmc_ready = false;
+  });
+}
+
+int lmc_ctx_get_lattices(lmc_ctx *ctx, int8_t *species) {
+  return Guard([&] {
+    Require(ctx && species && ctx->num_replicas > 0, LMC_ERR_INVALID_ARGUMENT, "no lattices");
+    CudaCheck(cudaMemcpyAsync(species, ctx->species.p, ctx->total_sites, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+  });
+}
+
+int64_t lmc_ctx_total_sites(const lmc_ctx *ctx) { return ctx ? ctx->total_sites : -1; }
+int64_t lmc_ctx_replica_offset(const lmc_ctx *ctx, int replica) {
+  if (!ctx || replica < 0 || replica >= ctx->num_replicas) return -1;
+  return ctx->offsets[replica];
+}
+void *lmc_ctx_species_device_ptr(lmc_ctx *ctx) { return ctx ? ctx->species.p : nullptr; }
+
+static void BarrierBatchImpl(lmc_ctx *ctx, int replica, int kind, const long long *d_pairs, int m, double *d_ea,
+                             double *d_de, double *d_x, double *d_ks) {
+  ctx->CheckReplica(replica);
+  Require(kind == LMC_BARRIER_QUARTIC || kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT, "unknown barrier kind");
+  ctx->ClearStatus();
+  CudaCheck(lmc::LaunchBarrierBatch(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                    d_pairs, m, kind, d_ea, d_de, d_x, d_ks, ctx->status.as<int>(), ctx->stream),
+            "barrier kernel");
+}
+
+int lmc_barrier_batch(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs, int m, double *ea, double *de,
+                      double *d_or_e0, double *ks) {
+  return Guard([&] {
+    Require(ctx && pairs && ea && de && m >= 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    if (m == 0) return;
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ctx->pairs.Ensure(sizeof(long long) * 2 * m);
+    for (DevBuf *b : {&ctx->out0, &ctx->out1, &ctx->out2, &ctx->out3}) b->Ensure(sizeof(double) * m);
+    CudaCheck(cudaMemcpyAsync(ctx->pairs.p, pairs, sizeof(long long) * 2 * m, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D pairs");
+    BarrierBatchImpl(ctx, replica, kind, ctx->pairs.as<long long>(), m, ctx->out0.as<double>(), ctx->out1.as<double>(),
+                     ctx->out2.as<double>(), ctx->out3.as<double>());
+    CudaCheck(cudaMemcpyAsync(ea, ctx->out0.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(de, ctx->out1.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (d_or_e0)
+      CudaCheck(cudaMemcpyAsync(d_or_e0, ctx->out2.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (ks) CudaCheck(cudaMemcpyAsync(ks, ctx->out3.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    RaiseStatus(ctx->ReadStatus(), "barrier batch");
+  });
+}
+
+int lmc_barrier_batch_device(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs_dev, int m, double *ea_dev,
+                             double *de_dev) {
+  return Guard([&] {
+    Require(ctx && pairs_dev && ea_dev && de_dev && m >= 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    if (m == 0) return;
+    BarrierBatchImpl(ctx, replica, kind, reinterpret_cast<const long long *>(pairs_dev), m, ea_dev, de_dev, nullptr,
+                     nullptr);
+  });
+}
+
+int lmc_encode_batch(lmc_ctx *ctx, int replica, const int64_t *pairs, int m, int32_t *state_start,
+                     int32_t *state_end, int32_t *mmm, int32_t *mm2_fwd, int32_t *mm2_bwd) {
+  return Guard([&] {
+    Require(ctx && pairs && m > 0 && state_start && state_end && mmm && mm2_fwd && mm2_bwd, LMC_ERR_INVALID_ARGUMENT,
+            "bad argument");
+    ctx->CheckReplica(replica);
+    const auto &t = ctx->t;
+    const size_t per = 2 * t.num_theta + t.f_mmm + 2 * t.f_mm2;
+    ctx->enc.Ensure(sizeof(int) * per * m);
+    ctx->pairs.Ensure(sizeof(long long) * 2 * m);
+    CudaCheck(cudaMemcpyAsync(ctx->pairs.p, pairs, sizeof(long long) * 2 * m, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D pairs");
+    CudaCheck(cudaMemsetAsync(ctx->enc.p, 0, sizeof(int) * per * m, ctx->stream), "memset");
+    int *base = ctx->enc.as<int>();
+    int *cs = base, *ce = cs + static_cast<size_t>(t.num_theta) * m, *om = ce + static_cast<size_t>(t.num_theta) * m;
+    int *of = om + static_cast<size_t>(t.f_mmm) * m, *ob = of + static_cast<size_t>(t.f_mm2) * m;
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchEncodeBatch(t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                     ctx->pairs.as<long long>(), m, cs, ce, om, of, ob, ctx->status.as<int>(),
+                                     ctx->stream),
+              "encode kernel");
+    auto d2h = [&](int32_t *dst, int *src, size_t cnt) {
+      CudaCheck(cudaMemcpyAsync(dst, src, sizeof(int) * cnt, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    };
+    d2h(state_start, cs, static_cast<size_t>(t.num_theta) * m);
+    d2h(state_end, ce, static_cast<size_t>(t.num_theta) * m);
+    d2h(mmm, om, static_cast<size_t>(t.f_mmm) * m);
+    d2h(mm2_fwd, of, static_cast<size_t>(t.f_mm2) * m);
+    d2h(mm2_bwd, ob, static_cast<size_t>(t.f_mm2) * m);
+    RaiseStatus(ctx->ReadStatus(), "encode batch");
+  });
+}
+
+int lmc_de_pairs(lmc_ctx *ctx, int replica, const int64_t *pairs, int m, double *de) {
+  return Guard([&] {
+    Require(ctx && pairs && de && m >= 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    if (m == 0) return;
+    ctx->CheckReplica(replica);
+    ctx->pairs.Ensure(sizeof(long long) * 2 * m);
+    ctx->out0.Ensure(sizeof(double) * m);
+    CudaCheck(cudaMemcpyAsync(ctx->pairs.p, pairs, sizeof(long long) * 2 * m, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D pairs");
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchDePairs(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                 ctx->pairs.as<long long>(), m, ctx->out0.as<double>(), ctx->status.as<int>(),
+                                 ctx->stream),
+              "dE kernel");
+    CudaCheck(cudaMemcpyAsync(de, ctx->out0.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    RaiseStatus(ctx->ReadStatus(), "pair dE");
+  });
+}
+
+int lmc_energy(lmc_ctx *ctx, int replica, double *energy, int64_t *counts) {
+  return Guard([&] {
+    Require(ctx && energy, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    ctx->CheckReplica(replica);
+    // dominant species of the lattice: the solvent for dilute alloys
+    int base = 0;
+    {
+      const auto &fm = ctx->fm;
+      base = fm.x_code == 0 ? 1 : 0;
+      for (int c = 0; c < fm.num_species; ++c)
+        if (ctx->model.alphabet[c] == "Al") base = c;
+    }
+    CudaCheck(lmc::LaunchCensus(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica], base,
+                                ctx->counts.as<unsigned long long>(), ctx->energy.as<double>(), ctx->stream),
+              "census kernel");
+    CudaCheck(cudaMemcpyAsync(energy, ctx->energy.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (counts)
+      CudaCheck(cudaMemcpyAsync(counts, ctx->counts.p, sizeof(int64_t) * ctx->t.num_theta, cudaMemcpyDeviceToHost,
+                                ctx->stream),
+                "D2H");
+    ctx->Sync();
+  });
+}
+
+int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options *opt) {
+  return Guard([&] {
+    Require(ctx && temperature && opt && ctx->num_replicas > 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    Require(opt->rng == LMC_RNG_MT19937_64 || opt->rng == LMC_RNG_PHILOX, LMC_ERR_INVALID_ARGUMENT, "unknown rng");
+    Require(opt->barrier_kind == LMC_BARRIER_QUARTIC || opt->barrier_kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT,
+            "unknown barrier kind");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int R = ctx->num_replicas;
+    for (int r = 0; r < R; ++r)
+      Require(temperature[r] > 0 && std::isfinite(temperature[r]), LMC_ERR_INVALID_ARGUMENT, "temperature must be > 0");
+    ctx->kmc_opt = *opt;
+    ctx->k_vac.Ensure(sizeof(long long) * R);
+    ctx->k_steps.Ensure(sizeof(unsigned long long) * R);
+    ctx->k_time.Ensure(sizeof(double) * R);
+    ctx->k_energy.Ensure(sizeof(double) * R);
+    ctx->k_temp.Ensure(sizeof(double) * R);
+    ctx->k_cvac.Ensure(sizeof(double) * R);
+    ctx->k_csol.Ensure(sizeof(double) * R);
+    ctx->k_rng.Ensure(sizeof(uint32_t) * lmc::kRngWords * R);
+    // first vacancy and species histogram of every replica
+    DevBuf hist;
+    hist.Alloc(sizeof(unsigned long long) * lmc::kMaxSpecies * R);
+    std::vector<long long> first(R, std::numeric_limits<long long>::max());
+    CudaCheck(cudaMemcpyAsync(ctx->k_vac.p, first.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D");
+    CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+    CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>(), ctx->lat_n.as<int>(), R,
+                                     ctx->fm.x_code, ctx->fm.num_species, ctx->k_vac.as<long long>(),
+                                     hist.as<unsigned long long>(), ctx->stream),
+              "scan kernel");
+    std::vector<unsigned long long> h(lmc::kMaxSpecies * R);
+    CudaCheck(cudaMemcpyAsync(first.data(), ctx->k_vac.p, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
+    CudaCheck(cudaMemcpyAsync(h.data(), hist.p, hist.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    hist.Free();
+    for (int r = 0; r < R; ++r)
+      Require(first[r] != std::numeric_limits<long long>::max(), LMC_ERR_INVALID_ARGUMENT, "vacancy not found");
+    const int al = ctx->model.Code("Al");
+    std::vector<double> cvac(R, -1.0), csol(R, 0.0);
+    if (opt->rate_corrector) {
+      for (int r = 0; r < R; ++r) {
+        const double nsites = 4.0 * ctx->n[r] * ctx->n[r] * ctx->n[r];
+        unsigned long long sol = 0;
+        for (int c = 0; c < ctx->fm.num_species; ++c)
+          if (c != ctx->fm.x_code && c != al) sol += h[r * lmc::kMaxSpecies + c];
+        cvac[r] = static_cast<double>(h[r * lmc::kMaxSpecies + ctx->fm.x_code]) / nsites;
+        csol[r] = static_cast<double>(sol) / nsites;
+      }
+    }
+    std::vector<uint32_t> rng(static_cast<size_t>(lmc::kRngWords) * R, 0);
+    for (int r = 0; r < R; ++r) {
+      uint32_t *w = rng.data() + static_cast<size_t>(lmc::kRngWords) * r;
+      if (opt->rng == LMC_RNG_MT19937_64) {
+        lmc::MtSeed(opt->seed + static_cast<uint64_t>(r), w);
+      } else {
+        w[0] = static_cast<uint32_t>(opt->seed);
+        w[1] = static_cast<uint32_t>(opt->seed >> 32);
+      }
+    }
+    std::vector<unsigned long long> zeros_u(R, 0);
+    std::vector<double> zeros_d(R, 0.0), temp(temperature, temperature + R);
+    CudaCheck(cudaMemcpyAsync(ctx->k_steps.p, zeros_u.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_time.p, zeros_d.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_energy.p, zeros_d.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_temp.p, temp.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_cvac.p, cvac.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_csol.p, csol.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(ctx->k_rng.p, rng.data(), rng.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    ctx->tt_len = 0;
+    if (opt->tt_len > 0) {
+      Require(opt->tt_time && opt->tt_temp, LMC_ERR_INVALID_ARGUMENT, "T(t) table pointers are null");
+      std::vector<std::pair<double, double>> pts;
+      for (int i = 0; i < opt->tt_len; ++i) pts.emplace_back(opt->tt_time[i], opt->tt_temp[i]);
+      std::sort(pts.begin(), pts.end());
+      for (size_t i = 1; i < pts.size(); ++i)
+        Require(std::abs(pts[i].first - pts[i - 1].first) >= 1e-12, LMC_ERR_INVALID_ARGUMENT,
+                "2 adjacent x values are equal.");
+      std::vector<double> tt, tv;
+      for (auto &p : pts) {
+        tt.push_back(p.first);
+        tv.push_back(p.second);
+      }
+      ctx->k_tt_time.Ensure(8 * tt.size());
+      ctx->k_tt_temp.Ensure(8 * tv.size());
+      CudaCheck(cudaMemcpyAsync(ctx->k_tt_time.p, tt.data(), 8 * tt.size(), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      CudaCheck(cudaMemcpyAsync(ctx->k_tt_temp.p, tv.data(), 8 * tv.size(), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      ctx->tt_len = opt->tt_len;
+    }
+    ctx->Sync();
+    ctx->kmc_ready = true;
+  });
+}
+
+int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace, double *events12) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (steps == 0) return;
+    static_assert(sizeof(lmc_kmc_step) == sizeof(lmc::KmcTraceRec), "trace record layout");
+    lmc::KmcDevState s{};
+    s.vacancy = ctx->k_vac.as<long long>();
+    s.steps = ctx->k_steps.as<unsigned long long>();
+    s.time = ctx->k_time.as<double>();
+    s.energy = ctx->k_energy.as<double>();
+    s.temperature = ctx->k_temp.as<double>();
+    s.corr_cvac = ctx->k_cvac.as<double>();
+    s.corr_csol = ctx->k_csol.as<double>();
+    s.rng = ctx->k_rng.as<uint32_t>();
+    s.lat_off = ctx->lat_off.as<long long>();
+    s.lat_n = ctx->lat_n.as<int>();
+    s.num_replicas = ctx->num_replicas;
+    s.rng_kind = ctx->kmc_opt.rng;
+    s.barrier_kind = ctx->kmc_opt.barrier_kind;
+    s.tt_time = ctx->tt_len ? ctx->k_tt_time.as<double>() : nullptr;
+    s.tt_temp = ctx->tt_len ? ctx->k_tt_temp.as<double>() : nullptr;
+    s.tt_len = ctx->tt_len;
+    lmc::KmcLaunch l{};
+    int g = ctx->kmc_opt.warps_per_replica, rpb = ctx->kmc_opt.replicas_per_block;
+    int dg, drpb;
+    KmcDefaults(ctx, &dg, &drpb);
+    if (g <= 0) g = dg;
+    if (rpb <= 0) rpb = drpb;
+    Require(g == 1 || g == 2 || g == 3 || g == 4 || g == 6 || g == 12, LMC_ERR_INVALID_ARGUMENT,
+            "warps_per_replica must divide 12");
+    Require(g * rpb <= 32, LMC_ERR_INVALID_ARGUMENT, "block too large");
+    l.warps_per_replica = g;
+    l.replicas_per_block = rpb;
+    l.steps = steps;
+    l.trace_replica = -1;
+    if (trace || events12) {
+      ctx->CheckReplica(trace_replica);
+      l.trace_replica = trace_replica;
+      if (trace) {
+        ctx->k_trace.Ensure(sizeof(lmc::KmcTraceRec) * steps);
+        l.trace = ctx->k_trace.as<lmc::KmcTraceRec>();
+      }
+      if (events12) {
+        ctx->k_events.Ensure(sizeof(double) * 36 * steps);
+        l.events12 = ctx->k_events.as<double>();
+      }
+    }
+    l.stop_flag = ctx->d_stop;
+    l.status = ctx->status.as<int>();
+    ctx->ClearStatus();
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    if (trace)
+      CudaCheck(cudaMemcpyAsync(trace, l.trace, sizeof(lmc::KmcTraceRec) * steps, cudaMemcpyDeviceToHost, ctx->stream),
+                "D2H trace");
+    if (events12)
+      CudaCheck(cudaMemcpyAsync(events12, l.events12, sizeof(double) * 36 * steps, cudaMemcpyDeviceToHost, ctx->stream),
+                "D2H events");
+    const int st = ctx->ReadStatus();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(st, "KMC run");
+  });
+}
+
+int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    const size_t R = ctx->num_replicas;
+    if (vacancy) CudaCheck(cudaMemcpyAsync(vacancy, ctx->k_vac.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (steps) CudaCheck(cudaMemcpyAsync(steps, ctx->k_steps.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (time) CudaCheck(cudaMemcpyAsync(time, ctx->k_time.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (energy) CudaCheck(cudaMemcpyAsync(energy, ctx->k_energy.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+  });
+}
+
+int lmc_last_run_ms(lmc_ctx *ctx, double *ms) {
+  return Guard([&] {
+    Require(ctx && ms, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    *ms = ctx->last_ms;
+  });
+}
+
+int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts, const lmc_cmc_options *opt,
+                double *energy_io, uint64_t *attempts_done, uint64_t *accepted) {
+  return Guard([&] {
+    Require(ctx && opt && energy_io, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    ctx->CheckReplica(replica);
+    Require(temperature > 0 && std::isfinite(temperature), LMC_ERR_INVALID_ARGUMENT, "temperature must be > 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int n = ctx->n[replica];
+    const long long nsites = 4LL * n * n * n;
+    int8_t *lat = ctx->species.as<int8_t>() + ctx->offsets[replica];
+    const double beta = 1.0 / 8.617333262145e-5 / temperature;  // McAbstract.cpp:29
+    ctx->c_stats.Ensure(sizeof(unsigned long long) * 4 + sizeof(double) * 2);
+    unsigned long long *d_done = ctx->c_stats.as<unsigned long long>();
+    int *d_quit = reinterpret_cast<int *>(d_done + 2);
+    double *d_energy = reinterpret_cast<double *>(d_done + 4);
+    CudaCheck(cudaMemsetAsync(d_done, 0, sizeof(unsigned long long) * 4, ctx->stream), "memset");
+    {
+      // both CMC modes redraw pairs until the two species differ: refuse a
+      // lattice with a single species instead of spinning on it
+      DevBuf hist, first;
+      hist.Alloc(sizeof(unsigned long long) * lmc::kMaxSpecies);
+      first.Alloc(sizeof(long long));
+      const long long big = std::numeric_limits<long long>::max();
+      CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+      CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>() + replica,
+                                       ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, ctx->fm.num_species,
+                                       first.as<long long>(), hist.as<unsigned long long>(), ctx->stream),
+                "scan kernel");
+      unsigned long long h[lmc::kMaxSpecies];
+      CudaCheck(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+      ctx->Sync();
+      int present = 0;
+      for (int c = 0; c < ctx->fm.num_species; ++c) present += h[c] > 0;
+      Require(present >= 2, LMC_ERR_INVALID_ARGUMENT, "canonical MC needs at least two species in the lattice");
+    }
+    CudaCheck(cudaMemcpyAsync(d_energy, energy_io, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    ctx->ClearStatus();
+    double e_out = *energy_io;
+    if (opt->mode == LMC_CMC_REFERENCE_BATCH) {
+      Require(opt->batch >= 1 && opt->batch <= 256, LMC_ERR_INVALID_ARGUMENT, "batch must be in [1, 256]");
+      auto &slot = ctx->c_mt[replica];
+      if (slot.second.p == nullptr || slot.first != opt->seed) {
+        std::vector<uint32_t> w(lmc::kRngWords);
+        lmc::MtSeed(opt->seed, w.data());
+        slot.second.Alloc(sizeof(uint32_t) * lmc::kRngWords);
+        CudaCheck(cudaMemcpy(slot.second.p, w.data(), sizeof(uint32_t) * lmc::kRngWords, cudaMemcpyHostToDevice), "H2D");
+        slot.first = opt->seed;
+      }
+      if (ctx->c_mark.bytes < static_cast<size_t>(nsites)) {
+        ctx->c_mark.Alloc(nsites);
+        CudaCheck(cudaMemset(ctx->c_mark.p, 0, nsites), "memset");
+      }
+      ctx->c_mark_list.Ensure(sizeof(long long) * 86 * opt->batch);
+      lmc::CmcRefArgs a{};
+      a.n = n;
+      a.beta = beta;
+      a.attempts = attempts;
+      a.batch = opt->batch;
+      a.rng = slot.second.as<uint32_t>();
+      a.mark = ctx->c_mark.as<unsigned char>();
+      a.mark_list = ctx->c_mark_list.as<long long>();
+      a.energy = d_energy;
+      a.done = d_done;
+      a.accepted = d_done + 1;
+      a.status = ctx->status.as<int>();
+      CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+      CudaCheck(lmc::LaunchCmcReference(ctx->t, lat, a, ctx->stream), "CMC kernel");
+      CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+      CudaCheck(cudaMemcpyAsync(&e_out, d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    } else if (opt->mode == LMC_CMC_THROUGHPUT) {
+      int cand = opt->candidates;
+      if (cand <= 0) cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, nsites / 256)));
+      Require(cand <= 65535, LMC_ERR_INVALID_ARGUMENT, "at most 65535 candidates per round");
+      ctx->c_claim.Ensure(sizeof(unsigned long long) * nsites);
+      ctx->c_cand.Ensure(sizeof(long long) * 2 * cand);
+      int sms = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+      ctx->c_eacc.Ensure(sizeof(double) * sms * 8);
+      CudaCheck(cudaMemsetAsync(ctx->c_claim.p, 0, sizeof(unsigned long long) * nsites, ctx->stream), "memset");
+      CudaCheck(cudaMemsetAsync(ctx->c_eacc.p, 0, sizeof(double) * sms * 8, ctx->stream), "memset");
+      lmc::CmcTpArgs a{};
+      a.n = n;
+      a.beta = beta;
+      a.attempts = attempts;
+      a.candidates = cand;
+      a.seed = opt->seed;
+      a.claim = ctx->c_claim.as<unsigned long long>();
+      a.cand = ctx->c_cand.as<long long>();
+      a.energy_acc = ctx->c_eacc.as<double>();
+      a.done = d_done;
+      a.accepted = d_done + 1;
+      a.quit = d_quit;
+      a.status = ctx->status.as<int>();
+      a.stop_flag = ctx->d_stop;
+      CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+      CudaCheck(lmc::LaunchCmcThroughput(ctx->t, lat, a, ctx->device, ctx->stream), "CMC kernel");
+      CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+      std::vector<double> eacc(sms * 8);
+      CudaCheck(cudaMemcpyAsync(eacc.data(), ctx->c_eacc.p, sizeof(double) * sms * 8, cudaMemcpyDeviceToHost,
+                                ctx->stream),
+                "D2H");
+      ctx->Sync();
+      for (double v : eacc) e_out += v;
+    } else {
+      throw LmcError(LMC_ERR_INVALID_ARGUMENT, "unknown CMC mode");
+    }
+    unsigned long long stats[2] = {0, 0};
+    CudaCheck(cudaMemcpyAsync(stats, d_done, sizeof(stats), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    const int st = ctx->ReadStatus();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(st, "CMC run");
+    *energy_io = e_out;
+    if (attempts_done) *attempts_done = stats[0];
+    if (accepted) *accepted = stats[1];
+  });
+}
+
+int lmc_request_stop(lmc_ctx *ctx, int value) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    *reinterpret_cast<volatile int *>(ctx->h_stop) = value;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,1320 @@
+// sm_103a kernels of the lattice-MC hot path.
+//
+//  K1 barrier_batch_kernel   batched Quartic / E0 migration barriers
+//                            (VacancyMigrationPredictorQuartic.cpp:112-276, VacancyMigrationPredictorE0.cpp:77-159)
+//  K1e encode_batch_kernel   the integer encodings behind K1 (for bit-exact checks)
+//  K2 de_pairs_kernel        PairSite swap energy change (EnergyChangePredictorPairSite.cpp:69-192)
+//  K3 census_kernel          EnergyPredictor full-lattice census (EnergyPredictor.cpp:40-96)
+//  K4 kmc_kernel             persistent batched-replica KMC (KineticMcAbstract.cpp:140-190,
+//                            KineticMcFirstOmp.cpp:52-82)
+//  K5 cmc_ref_kernel         CanonicalMcOmp batch semantics on the reference's RNG stream
+//     cmc_tp_kernel          throughput CMC: cooperative rounds of non-overlapping swaps
+//
+// All cluster sums are int64 fixed point (weights folded on the host, see
+// model.hpp), so they are exact and independent of summation order; FP64 is
+// used only for the per-candidate epilogue, the rate sum and the clock.
+// Lattice loads inside kernels that also write the lattice use plain
+// (coherent) loads, never the read-only path.
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace lmc {
+namespace {
+
+constexpr double kBoltzmannEv = 8.617333262145e-5;  // lmc/cfg/include/Constants.hpp:31
+constexpr double kPrefactor = 1e13;                 // lmc/cfg/include/Constants.hpp:32
+constexpr int kArr = 240;                           // per-warp sorted arrays: 60 + 3 * 58 (+pad)
+
+// (dx+1)*9 + (dy+1)*3 + (dz+1) -> index of the 1NN direction (lexicographic
+// order of the 12 offsets), -1 otherwise.
+__constant__ int8_t c_dir_of[27] = {-1, -1, -1, -1, -1, 0,  -1, 3,  -1, -1, 1,  -1, 4, -1,
+                                    5,  -1, 2,  -1, -1, 8, -1, 9, -1, 10, -1, 11, -1};
+
+struct H3 {
+  int x, y, z;
+};
+
+__device__ __forceinline__ H3 SiteCoord(long long id, int n) {
+  const long long plane = 2LL * n * n;
+  const int hx = static_cast<int>(id / plane);
+  const long long r = id - static_cast<long long>(hx) * plane;
+  const int hy = static_cast<int>(r / n);
+  const int k = static_cast<int>(r - static_cast<long long>(hy) * n);
+  return {hx, hy, 2 * k + ((hx + hy) & 1)};
+}
+
+// Id of h + (dx, dy, dz) with periodic wrap; |offset| <= 4 < 2n.
+__device__ __forceinline__ long long NeighborId(H3 h, int dx, int dy, int dz, int n) {
+  const int m = 2 * n;
+  int x = h.x + dx, y = h.y + dy, z = h.z + dz;
+  x += (x < 0) ? m : 0;
+  x -= (x >= m) ? m : 0;
+  y += (y < 0) ? m : 0;
+  y -= (y >= m) ? m : 0;
+  z += (z < 0) ? m : 0;
+  z -= (z >= m) ? m : 0;
+  return static_cast<long long>(x) * 2 * n * n + static_cast<long long>(y) * n + (z >> 1);
+}
+
+__device__ __forceinline__ int MinImage(int d, int n) {
+  const int m = 2 * n;
+  d %= m;
+  if (d < -n) d += m;
+  if (d >= n) d -= m;
+  return d;
+}
+
+__device__ __forceinline__ int DirIndex(int dx, int dy, int dz) {
+  if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) return -1;
+  return c_dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)];
+}
+
+__device__ __forceinline__ long long WarpSum(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double WarpSumD(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Shared-memory copies of the small model tables.
+struct SmallTables {
+  int8_t rank[8];
+  int8_t slot[8];
+  int8_t pairtype[192];
+  uint8_t has_quartic[kMaxSlots];
+  uint8_t has_e0[kMaxSlots];
+  uint8_t pad[4];
+};
+
+__device__ __forceinline__ void StageSmall(const DevTables &t, SmallTables *s) {
+  for (int i = threadIdx.x; i < 192; i += blockDim.x) s->pairtype[i] = t.pairtype[i];
+  if (threadIdx.x < 8) {
+    s->rank[threadIdx.x] = t.onehot_rank[threadIdx.x];
+    s->slot[threadIdx.x] = t.migrant_slot[threadIdx.x];
+  }
+  if (threadIdx.x < kMaxSlots) {
+    s->has_quartic[threadIdx.x] = t.has_quartic[threadIdx.x];
+    s->has_e0[threadIdx.x] = t.has_e0[threadIdx.x];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void StageArray(const T *src, T *dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+struct JumpAcc {
+  long long de, d, ks;
+  unsigned bad;
+};
+
+// Per-lane partial sums of one jump's three linear forms from the sorted
+// species arrays: st = state list codes (60), rm/rf/rb = MMM / MM2-forward /
+// MM2-backward one-hot ranks (58 each, rank 7 = no slot).
+//   de: sum over state clusters with exactly one pair site of
+//       W(end tuple) - W(start tuple)   (clusters with both pair sites cancel)
+//   d : sum over MMM clusters of the D (Quartic) or e0 (E0) weights
+//   ks: sum over MM2 clusters of the forward and backward lists (Quartic)
+template <bool kQuartic>
+__device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const int8_t *st, const int8_t *rm,
+                                            const int8_t *rf, const int8_t *rb, const uint32_t *s_de,
+                                            const uint32_t *s_mmm, const uint32_t *s_mm2, const int8_t *s_pt,
+                                            int lane) {
+  JumpAcc a{0, 0, 0, 0u};
+  const int e = t.num_species;
+  const int x = t.x_code;
+  const int si = st[t.pos_first];
+  const int sj = st[t.pos_second];
+  const long long *__restrict__ wde = t.w_de;
+  for (int c = lane; c < t.n_de_cl; c += 32) {
+    const uint32_t w = s_de[c];
+    const int label = w & 7, side = (w >> 3) & 1, o1 = (w >> 4) & 63, o2 = (w >> 10) & 63;
+    const int c1 = st[o1];
+    const bool has2 = o2 != 63;
+    const int c2 = has2 ? st[o2] : 0;
+    const int cs = side ? sj : si;
+    const int ce = side ? x : sj;
+    const int tail = c1 * e + c2;
+    const long long ws = __ldg(&wde[(label * e + cs) * e * e + tail]);
+    const long long we = __ldg(&wde[(label * e + ce) * e * e + tail]);
+    a.de += we - ws;
+    const int nx_other = (c1 == x) + (has2 && c2 == x);
+    if (nx_other + (cs == x) >= 2 || nx_other + (ce == x) >= 2) a.bad |= kStatusBadCluster;
+  }
+  const long long *__restrict__ wd = (kQuartic ? t.w_d : t.w_e0) + static_cast<long long>(slot) * t.f_mmm;
+  for (int c = lane; c < t.n_mmm_cl; c += 32) {
+    const uint32_t w = s_mmm[c];
+    const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
+    const int ra = rm[ia];
+    const int rbv = ib == 63 ? 0 : rm[ib];
+    const int tt = s_pt[(mode * 8 + ra) * 8 + rbv];
+    if (tt >= 0) a.d += __ldg(&wd[base + tt]);
+    else a.bad |= kStatusXInEnv;
+  }
+  if (kQuartic) {
+    const long long *__restrict__ wk = t.w_ks + static_cast<long long>(slot) * t.f_mm2;
+    for (int c = lane; c < t.n_mm2_cl; c += 32) {
+      const uint32_t w = s_mm2[c];
+      const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
+      const int fa = rf[ia], ba = rb[ia];
+      const int fb = ib == 63 ? 0 : rf[ib];
+      const int bb = ib == 63 ? 0 : rb[ib];
+      const int tf = s_pt[(mode * 8 + fa) * 8 + fb];
+      const int tb = s_pt[(mode * 8 + ba) * 8 + bb];
+      if (tf >= 0) a.ks += __ldg(&wk[base + tf]);
+      else a.bad |= kStatusXInEnv;
+      if (tb >= 0) a.ks += __ldg(&wk[base + tb]);
+      else a.bad |= kStatusXInEnv;
+    }
+  }
+  return a;
+}
+
+// FP64 epilogue of one jump. With P = Ks * D^2 the reference's closed form
+// (VacancyMigrationPredictorQuartic.cpp:269-274) is exactly
+//   Ea = (P + 12 dE)^2 (P^2 + 8 P dE - 48 dE^2) / (64 P^3)
+// because its sqrt argument 9b^2 - 32ac equals 4 a Ks > 0, i.e. delta = Ks / D.
+struct JumpOut {
+  double ea, de, d_or_e0, ks;
+};
+__device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, int kind, int slot, long long acc_de,
+                                                long long acc_d, long long acc_ks) {
+  JumpOut o;
+  o.de = static_cast<double>(acc_de) * t.de_scale;
+  const double *f = t.form + slot * 12;
+  if (kind == 0) {
+    const double log_d = f[2] * (static_cast<double>(acc_d) * f[0] - f[1]) + f[3];
+    const double log_ks = f[6] * (static_cast<double>(acc_ks) * f[4] - f[5]) + f[7];
+    const double p = exp(log_ks + 2.0 * log_d);
+    const double q = p + 12.0 * o.de;
+    o.ea = q * q * (p * p + 8.0 * p * o.de - 48.0 * o.de * o.de) / (64.0 * p * p * p);
+    o.d_or_e0 = log_d;
+    o.ks = log_ks;
+  } else {
+    const double log_e0 = f[10] * (static_cast<double>(acc_d) * f[8] - f[9]) + f[11];
+    const double e0 = exp(log_e0);
+    o.ea = fmax(0.0, e0 + o.de / 2);
+    o.d_or_e0 = e0;
+    o.ks = 0.0;
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// K1: batched barriers, one warp per pair.
+// ---------------------------------------------------------------------------
+struct JumpSmem {
+  uint32_t *de, *mmm, *mm2;
+  SmallTables *small;
+  int8_t *arr;
+};
+__device__ __forceinline__ JumpSmem CarveJumpSmem(const DevTables &t, unsigned char *smem) {
+  JumpSmem s;
+  s.de = reinterpret_cast<uint32_t *>(smem);
+  s.mmm = s.de + t.n_de_cl;
+  s.mm2 = s.mmm + t.n_mmm_cl;
+  s.small = reinterpret_cast<SmallTables *>(s.mm2 + t.n_mm2_cl);
+  s.arr = reinterpret_cast<int8_t *>(s.small + 1);
+  return s;
+}
+__device__ __forceinline__ void StageJump(const DevTables &t, const JumpSmem &s) {
+  StageArray(t.de_cl, s.de, t.n_de_cl);
+  StageArray(t.mmm_cl, s.mmm, t.n_mmm_cl);
+  StageArray(t.mm2_cl, s.mm2, t.n_mm2_cl);
+  StageSmall(t, s.small);
+}
+size_t JumpSmemBytes(const DevTables &t, int warps) {
+  size_t b = 4u * (t.n_de_cl + t.n_mmm_cl + t.n_mm2_cl) + sizeof(SmallTables) + static_cast<size_t>(warps) * kArr;
+  return (b + 15) & ~size_t(15);
+}
+
+// Resolves a (first, second) pair: returns the direction index of second - first
+// and of first - second, or a status bit.
+__device__ __forceinline__ int ResolvePair(long long i, long long j, int n, H3 *hi, H3 *hj, int *di, int *db) {
+  const long long nsites = 4LL * n * n * n;
+  if (i < 0 || j < 0 || i >= nsites || j >= nsites) return kStatusBadSite;
+  *hi = SiteCoord(i, n);
+  *hj = SiteCoord(j, n);
+  const int dx = MinImage(hj->x - hi->x, n), dy = MinImage(hj->y - hi->y, n), dz = MinImage(hj->z - hi->z, n);
+  *di = DirIndex(dx, dy, dz);
+  *db = DirIndex(-dx, -dy, -dz);
+  return *di < 0 ? kStatusNotNeighbor : 0;
+}
+
+// Gathers the sorted arrays of jump (hi -> hj) straight from the lattice.
+__device__ __forceinline__ void GatherJump(const DevTables &t, const int8_t *species, int n, H3 hi, H3 hj, int di,
+                                           int db, const SmallTables *sm, int8_t *st, int8_t *rm, int8_t *rf,
+                                           int8_t *rb, int lane) {
+  for (int k = lane; k < kStateSites; k += 32) {
+    const int8_t *o = t.state_off + (di * kStateSites + k) * 4;
+    st[k] = species[NeighborId(hi, o[0], o[1], o[2], n)];
+  }
+  for (int k = lane; k < kEnvSites; k += 32) {
+    const int8_t *a = t.mmm_off + (di * kEnvSites + k) * 4;
+    const int8_t *b = t.mm2_off + (di * kEnvSites + k) * 4;
+    const int8_t *c = t.mm2_off + (db * kEnvSites + k) * 4;
+    rm[k] = sm->rank[species[NeighborId(hi, a[0], a[1], a[2], n)]];
+    rf[k] = sm->rank[species[NeighborId(hi, b[0], b[1], b[2], n)]];
+    rb[k] = sm->rank[species[NeighborId(hj, c[0], c[1], c[2], n)]];
+  }
+}
+
+__global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                                     const long long *__restrict__ pairs, int m, int kind, double *ea, double *de,
+                                     double *d_or_e0, double *ks, int *status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const JumpSmem s = CarveJumpSmem(t, smem);
+  StageJump(t, s);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *st = s.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  unsigned bad_all = 0;
+  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
+    H3 hi, hj;
+    int di = -1, db = -1;
+    unsigned bad = ResolvePair(pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+    int slot = -1;
+    if (!bad) {
+      GatherJump(t, species, n, hi, hj, di, db, s.small, st, rm, rf, rb, lane);
+      __syncwarp();
+      slot = s.small->slot[st[t.pos_second]];
+      if (slot < 0 || (kind == 0 ? !s.small->has_quartic[slot] : !s.small->has_e0[slot])) bad = kStatusNoCoefficients;
+    }
+    if (bad) {
+      if (lane == 0) {
+        ea[p] = nan("");
+        de[p] = nan("");
+      }
+      bad_all |= bad;
+      __syncwarp();
+      continue;
+    }
+    JumpAcc a = kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane)
+                          : EvalJump<false>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane);
+    const long long acc_de = WarpSum(a.de), acc_d = WarpSum(a.d), acc_ks = WarpSum(a.ks);
+    const unsigned b = __reduce_or_sync(0xffffffffu, a.bad);
+    if (lane == 0) {
+      const JumpOut o = JumpEpilogue(t, kind, slot, acc_de, acc_d, acc_ks);
+      ea[p] = o.ea;
+      de[p] = o.de;
+      if (d_or_e0) d_or_e0[p] = kind == 0 ? exp(o.d_or_e0) : o.d_or_e0;
+      if (ks) ks[p] = kind == 0 ? exp(o.ks) : 0.0;
+      if (!isfinite(o.ea)) bad_all |= kStatusNumeric;
+    }
+    bad_all |= b;
+    __syncwarp();
+  }
+  if (bad_all && lane == 0) atomicOr(status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
+// K1e: integer encodings (ElementCluster start/end counts, one-hot numerators).
+// ---------------------------------------------------------------------------
+__global__ void encode_batch_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                                    const long long *__restrict__ pairs, int m, int *state_start, int *state_end,
+                                    int *mmm, int *mm2f, int *mm2b, int *status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const JumpSmem s = CarveJumpSmem(t, smem);
+  StageJump(t, s);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *st = s.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const int e = t.num_species;
+  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
+    H3 hi, hj;
+    int di = -1, db = -1;
+    unsigned bad = ResolvePair(pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+    if (bad) {
+      if (lane == 0) atomicOr(status, static_cast<int>(bad));
+      continue;
+    }
+    GatherJump(t, species, n, hi, hj, di, db, s.small, st, rm, rf, rb, lane);
+    __syncwarp();
+    const int sj = st[t.pos_second];
+    int *cs = state_start + static_cast<long long>(p) * t.num_theta;
+    int *ce = state_end + static_cast<long long>(p) * t.num_theta;
+    for (int c = lane; c < t.n_state_all; c += 32) {
+      const uint32_t w = t.state_all[c];
+      const int label = w & 7, size = (w >> 3) & 3;
+      int k[3] = {static_cast<int>((w >> 5) & 63), static_cast<int>((w >> 11) & 63), static_cast<int>((w >> 17) & 63)};
+      int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+      for (int q = 0; q < size; ++q) {
+        a[q] = st[k[q]];
+        b[q] = k[q] == t.pos_first ? sj : (k[q] == t.pos_second ? t.x_code : a[q]);
+      }
+      const int ia = t.cluster_index[((label * e + a[0]) * e + a[1]) * e + a[2]];
+      const int ib = t.cluster_index[((label * e + b[0]) * e + b[1]) * e + b[2]];
+      if (ia < 0 || ib < 0) {
+        atomicOr(status, kStatusBadCluster);
+        continue;
+      }
+      atomicAdd(&cs[ia], 1);
+      atomicAdd(&ce[ib], 1);
+    }
+    int *om = mmm + static_cast<long long>(p) * t.f_mmm;
+    for (int c = lane; c < t.n_mmm_cl; c += 32) {
+      const uint32_t w = s.mmm[c];
+      const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
+      const int tt = s.small->pairtype[(mode * 8 + rm[ia]) * 8 + (ib == 63 ? 0 : rm[ib])];
+      if (tt >= 0) atomicAdd(&om[base + tt], 1);
+      else atomicOr(status, kStatusXInEnv);
+    }
+    int *of = mm2f + static_cast<long long>(p) * t.f_mm2;
+    int *ob = mm2b + static_cast<long long>(p) * t.f_mm2;
+    for (int c = lane; c < t.n_mm2_cl; c += 32) {
+      const uint32_t w = s.mm2[c];
+      const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
+      const int tf = s.small->pairtype[(mode * 8 + rf[ia]) * 8 + (ib == 63 ? 0 : rf[ib])];
+      const int tb = s.small->pairtype[(mode * 8 + rb[ia]) * 8 + (ib == 63 ? 0 : rb[ib])];
+      if (tf >= 0) atomicAdd(&of[base + tf], 1);
+      else atomicOr(status, kStatusXInEnv);
+      if (tb >= 0) atomicAdd(&ob[base + tb], 1);
+      else atomicOr(status, kStatusXInEnv);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K2: PairSite energy change of swapping the species of two sites.
+//   dE = sum over clusters c of site(a) with b not in c of W(c; a -> s_b) - W(c)
+//      + sum over clusters c of site(b) with a not in c of W(c; b -> s_a) - W(c)
+// which equals both the uncoupled (two site terms) and the coupled (pair
+// mapping, GetClusterParametersMappingStatePairOf) branches of the reference:
+// clusters containing both sites keep their multiset and cancel.
+// ---------------------------------------------------------------------------
+struct SiteSmem {
+  uint32_t *cl;
+  int8_t *off;   // [43][4]
+  int8_t *arr;   // per warp 2 x 44
+};
+__device__ __forceinline__ SiteSmem CarveSiteSmem(const DevTables &t, unsigned char *smem) {
+  SiteSmem s;
+  s.cl = reinterpret_cast<uint32_t *>(smem);
+  s.off = reinterpret_cast<int8_t *>(s.cl + t.n_site_cl);
+  s.arr = s.off + kSiteSites * 4;
+  return s;
+}
+size_t SiteSmemBytes(const DevTables &t, int warps) {
+  size_t b = 4u * t.n_site_cl + kSiteSites * 4 + static_cast<size_t>(warps) * 88;
+  return (b + 15) & ~size_t(15);
+}
+
+// Partial (per-lane) fixed-point dE of swapping the species at the centres of
+// the site arrays sa / sb. pa / pb: index of the other centre in each list or -1.
+__device__ __forceinline__ long long SwapDePartial(const DevTables &t, const uint32_t *cl, const int8_t *sa,
+                                                   const int8_t *sb, int pa, int pb, int lane) {
+  const int e = t.num_species;
+  const int ca = sa[t.site_center], cb = sb[t.site_center];
+  const long long *__restrict__ w = t.w_de;
+  long long acc = 0;
+  for (int c = lane; c < t.n_site_cl; c += 32) {
+    const uint32_t d = cl[c];
+    const int label = d & 7, o1 = (d >> 3) & 63, o2 = (d >> 9) & 63;
+    const int base = label * e;
+    if (o1 != pb && o2 != pb) {
+      const int tail = (o1 == 63 ? 0 : sa[o1]) * e + (o2 == 63 ? 0 : sa[o2]);
+      acc += __ldg(&w[(base + cb) * e * e + tail]) - __ldg(&w[(base + ca) * e * e + tail]);
+    }
+    if (o1 != pa && o2 != pa) {
+      const int tail = (o1 == 63 ? 0 : sb[o1]) * e + (o2 == 63 ? 0 : sb[o2]);
+      acc += __ldg(&w[(base + ca) * e * e + tail]) - __ldg(&w[(base + cb) * e * e + tail]);
+    }
+  }
+  return acc;
+}
+
+// Gathers the 43-site lists of a and b and locates each centre in the other list.
+__device__ __forceinline__ void GatherSwap(const int8_t *off, const int8_t *species, int n, H3 ha, H3 hb,
+                                           int8_t *sa, int8_t *sb, int *pa, int *pb, int lane) {
+  const int dx = MinImage(hb.x - ha.x, n), dy = MinImage(hb.y - ha.y, n), dz = MinImage(hb.z - ha.z, n);
+  int found_b = -1, found_a = -1;
+  for (int k = lane; k < kSiteSites; k += 32) {
+    const int8_t *o = off + k * 4;
+    sa[k] = species[NeighborId(ha, o[0], o[1], o[2], n)];
+    sb[k] = species[NeighborId(hb, o[0], o[1], o[2], n)];
+    if (o[0] == dx && o[1] == dy && o[2] == dz) found_b = k;
+    if (o[0] == -dx && o[1] == -dy && o[2] == -dz) found_a = k;
+  }
+  *pb = __reduce_max_sync(0xffffffffu, found_b);
+  *pa = __reduce_max_sync(0xffffffffu, found_a);
+  __syncwarp();
+}
+
+__global__ void de_pairs_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                                const long long *__restrict__ pairs, int m, double *de, int *status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *sa = s.arr + warp * 88, *sb = sa + 44;
+  const long long nsites = 4LL * n * n * n;
+  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
+    const long long a = pairs[2 * p], b = pairs[2 * p + 1];
+    if (a < 0 || b < 0 || a >= nsites || b >= nsites) {
+      if (lane == 0) {
+        de[p] = nan("");
+        atomicOr(status, kStatusBadSite);
+      }
+      continue;
+    }
+    if (species[a] == species[b]) {
+      if (lane == 0) de[p] = 0.0;
+      continue;
+    }
+    int pa, pb;
+    GatherSwap(s.off, species, n, SiteCoord(a, n), SiteCoord(b, n), sa, sb, &pa, &pb, lane);
+    const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
+    if (lane == 0) de[p] = static_cast<double>(acc) * t.de_scale;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K3: full-lattice cluster census. One thread per site, shared-memory
+// histogram; clusters made only of the dominant species are counted in
+// registers per label and merged once per warp (they are most of the lattice).
+// ---------------------------------------------------------------------------
+constexpr int kCensusThreads = 256;
+__global__ void __launch_bounds__(kCensusThreads) census_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                                                                int base_code, unsigned long long *counts) {
+  __shared__ unsigned int hist[512];
+  __shared__ uint32_t s_tri[160];
+  __shared__ int8_t s_off[kSiteSites * 4];
+  __shared__ int8_t s_label[kSiteSites];
+  __shared__ int16_t s_idx[8 * 6 * 6 * 6];
+  __shared__ int8_t s_sp[kCensusThreads * 44];
+  const int e = t.num_species;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) hist[i] = 0;
+  StageArray(t.census_tri, s_tri, t.n_census_tri);
+  StageArray(t.site_off, s_off, kSiteSites * 4);
+  StageArray(t.cluster_index, s_idx, 8 * e * e * e);
+  __syncthreads();
+  for (int k = threadIdx.x; k < kSiteSites; k += blockDim.x) {
+    const int x = s_off[k * 4], y = s_off[k * 4 + 1], z = s_off[k * 4 + 2];
+    const int n2 = x * x + y * y + z * z;
+    s_label[k] = n2 == 2 ? 1 : (n2 == 4 ? 2 : (n2 == 6 ? 3 : 0));
+  }
+  __syncthreads();
+  const long long nsites = 4LL * n * n * n;
+  int8_t *sp = s_sp + threadIdx.x * 44;
+  unsigned base_count[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long site = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; site < nsites;
+       site += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const H3 h = SiteCoord(site, n);
+    bool all_base = true;
+    for (int k = 0; k < kSiteSites; ++k) {
+      const int8_t v = species[NeighborId(h, s_off[k * 4], s_off[k * 4 + 1], s_off[k * 4 + 2], n)];
+      sp[k] = v;
+      all_base &= v == base_code;
+    }
+    const int c0 = sp[t.site_center];
+    if (all_base) {
+      base_count[0] += 1;
+      base_count[1] += 12;
+      base_count[2] += 6;
+      base_count[3] += 24;
+      for (int q = 0; q < t.n_census_tri; ++q) base_count[s_tri[q] & 7] += 1;
+      continue;
+    }
+    atomicAdd(&hist[s_idx[(0 * e + c0) * e * e]], 1u);
+    for (int k = 0; k < kSiteSites; ++k) {
+      const int l = s_label[k];
+      if (l == 0) continue;
+      const int c1 = sp[k];
+      if (c0 == base_code && c1 == base_code) base_count[l] += 1;
+      else atomicAdd(&hist[s_idx[((l * e + c0) * e + c1) * e]], 1u);
+    }
+    for (int q = 0; q < t.n_census_tri; ++q) {
+      const uint32_t w = s_tri[q];
+      const int l = w & 7;
+      const int c1 = sp[(w >> 3) & 63], c2 = sp[(w >> 9) & 63];
+      if (c0 == base_code && c1 == base_code && c2 == base_code) base_count[l] += 1;
+      else atomicAdd(&hist[s_idx[((l * e + c0) * e + c1) * e + c2]], 1u);
+    }
+  }
+  // merge the per-label dominant-species counts
+  for (int l = 0; l < 8; ++l) {
+    unsigned v = base_count[l];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) {
+      const int idx = l == 0 ? s_idx[(0 * e + base_code) * e * e]
+                             : (l <= 3 ? s_idx[((l * e + base_code) * e + base_code) * e]
+                                       : s_idx[((l * e + base_code) * e + base_code) * e + base_code]);
+      atomicAdd(&hist[idx], v);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < t.num_theta; i += blockDim.x)
+    if (hist[i]) atomicAdd(&counts[i], static_cast<unsigned long long>(hist[i]));
+}
+
+// Energy = sum_idx theta_idx * (count_idx / bonds_idx), sequential in index
+// order without contraction, as the reference's GetEncode + dot
+// (EnergyPredictor.cpp:87-95,173-177).
+__global__ void census_energy_kernel(DevTables t, const unsigned long long *counts, double *energy) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < t.num_theta; ++i) {
+    const double enc = __ddiv_rn(static_cast<double>(counts[i]), t.census_bonds[i]);
+    s = __dadd_rn(s, __dmul_rn(t.theta[i], enc));
+  }
+  *energy = s;
+}
+
+// ---------------------------------------------------------------------------
+// Random numbers.
+//  * std::mt19937_64 with libstdc++'s generate_canonical<double, 53> and
+//    uniform_int_distribution (Lemire's multiply-and-reject, Lemire 2019),
+//    so device draws equal the reference's for the same seed.
+//  * Philox4x32-10 (Salmon et al., SC'11) for production streams.
+// ---------------------------------------------------------------------------
+struct Mt {
+  unsigned long long *mt;  // 312 words
+  unsigned *idx;
+};
+__device__ __forceinline__ unsigned long long MtNext(Mt s) {
+  constexpr int kN = 312, kM = 156;
+  constexpr unsigned long long kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL;
+  constexpr unsigned long long kA = 0xB5026F5AA96619E9ULL;
+  unsigned i = *s.idx;
+  if (i >= kN) {
+    for (int k = 0; k < kN; ++k) {
+      const unsigned long long x = (s.mt[k] & kUpper) | (s.mt[(k + 1) % kN] & kLower);
+      s.mt[k] = s.mt[(k + kM) % kN] ^ (x >> 1) ^ ((x & 1ULL) ? kA : 0ULL);
+    }
+    i = 0;
+  }
+  unsigned long long y = s.mt[i];
+  *s.idx = i + 1;
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  y ^= y >> 43;
+  return y;
+}
+// generate_canonical<double, 53>(mt19937_64): one draw scaled by 2^-64, values
+// that round up to 1 become the largest double below 1.
+__device__ __forceinline__ double MtUniform(Mt s) {
+  const double u = __ull2double_rn(MtNext(s)) * 5.421010862427522170e-20;  // 2^-64
+  return u >= 1.0 ? 0.99999999999999988898 : u;
+}
+// uniform_int_distribution<size_t>(0, range - 1) on a 64-bit engine.
+__device__ __forceinline__ unsigned long long MtBelow(Mt s, unsigned long long range) {
+  unsigned long long x = MtNext(s);
+  unsigned long long low = x * range;
+  if (low < range) {
+    const unsigned long long threshold = (0ULL - range) % range;
+    while (low < threshold) {
+      x = MtNext(s);
+      low = x * range;
+    }
+  }
+  return __umul64hi(x, range);
+}
+
+struct Philox {
+  uint32_t c[4], k[2];
+};
+__device__ __forceinline__ uint4 PhiloxRound10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                               uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return make_uint4(c0, c1, c2, c3);
+}
+// 53-bit uniform in [0, 1) from two 32-bit words; the (0, 1] variant adds one ulp.
+__device__ __forceinline__ double U01(uint32_t hi, uint32_t lo) {
+  const unsigned long long v = ((static_cast<unsigned long long>(hi) << 32) | lo) >> 11;
+  return static_cast<double>(v) * 1.1102230246251565404e-16;  // 2^-53
+}
+__device__ __forceinline__ double U01Open(uint32_t hi, uint32_t lo) {
+  const unsigned long long v = ((static_cast<unsigned long long>(hi) << 32) | lo) >> 11;
+  return static_cast<double>(v + 1) * 1.1102230246251565404e-16;
+}
+
+// ---------------------------------------------------------------------------
+// K4: persistent batched-replica KMC. A block owns R replicas with G warps
+// each; per step: gather the 135-site neighbourhood of the vacancy, evaluate
+// the 12 jumps (warp g takes jumps g, g+G, ...), then warp 0 of the replica
+// turns them into rates, draws (u1, u2), selects the event and updates the
+// lattice, clock and energy.
+// ---------------------------------------------------------------------------
+struct KmcShared {
+  int8_t local[kLocalSites + 1];
+  int8_t pad0[7];
+  long long acc[12][3];
+  int slot[12];
+  long long ids[12];
+  double beta;
+  double corr;
+};
+
+__device__ __forceinline__ double InterpT(const double *tt, const double *tv, int len, double time) {
+  // TimeTemperatureInterpolator::GetTemperature (TimeTemperatureInterpolator.cpp:44-65)
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (tt[mid] < time) lo = mid + 1;
+    else hi = mid;
+  }
+  if (lo == len) return tv[len - 1];
+  if (lo == 0 && time <= tt[0]) return tv[0];
+  const double ux = tt[lo], uy = tv[lo], lx = tt[lo - 1], ly = tv[lo - 1];
+  return ly + ((time - lx) / (ux - lx)) * (uy - ly);
+}
+
+__global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int g_per = l.warps_per_replica;
+  const int rpb = l.replicas_per_block;
+  // carve: jump tables, small tables, local-index tables, per-replica state, per-warp arrays
+  uint32_t *s_de = reinterpret_cast<uint32_t *>(smem);
+  uint32_t *s_mmm = s_de + t.n_de_cl;
+  uint32_t *s_mm2 = s_mmm + t.n_mmm_cl;
+  SmallTables *s_small = reinterpret_cast<SmallTables *>(s_mm2 + t.n_mm2_cl);
+  uint8_t *s_lst = reinterpret_cast<uint8_t *>(s_small + 1);   // [12][60]
+  uint8_t *s_lmmm = s_lst + 12 * kStateSites;                    // [12][58]
+  uint8_t *s_lmm2f = s_lmmm + 12 * kEnvSites;
+  uint8_t *s_lmm2b = s_lmm2f + 12 * kEnvSites;
+  int8_t *s_loff = reinterpret_cast<int8_t *>(s_lmm2b + 12 * kEnvSites);  // [135][4]
+  size_t off = reinterpret_cast<size_t>(s_loff + kLocalSites * 4);
+  off = (off + 15) & ~size_t(15);
+  KmcShared *s_rep = reinterpret_cast<KmcShared *>(off);
+  int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
+
+  StageArray(t.de_cl, s_de, t.n_de_cl);
+  StageArray(t.mmm_cl, s_mmm, t.n_mmm_cl);
+  StageArray(t.mm2_cl, s_mm2, t.n_mm2_cl);
+  StageSmall(t, s_small);
+  StageArray(t.local_st, s_lst, 12 * kStateSites);
+  StageArray(t.local_mmm, s_lmmm, 12 * kEnvSites);
+  StageArray(t.local_mm2f, s_lmm2f, 12 * kEnvSites);
+  StageArray(t.local_mm2b, s_lmm2b, 12 * kEnvSites);
+  StageArray(t.local_off, s_loff, kLocalSites * 4);
+  __syncthreads();
+
+  __shared__ int s_stop;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rl = warp / g_per;         // replica within block
+  const int g = warp - rl * g_per;     // warp within replica
+  const int r = blockIdx.x * rpb + rl;
+  const bool active = r < s.num_replicas;
+  KmcShared &rs = s_rep[rl];
+  int8_t *st = s_arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const int n = active ? s.lat_n[r] : 6;
+  int8_t *lat = species + (active ? s.lat_off[r] : 0);
+  long long vac = active ? s.vacancy[r] : 0;
+  const bool leader = g == 0 && lane == 0;
+  unsigned bad_all = 0;
+  double time = 0, energy = 0;
+  unsigned long long step0 = 0, steps_done = 0;
+  if (active && leader) {
+    time = s.time[r];
+    energy = s.energy[r];
+    step0 = s.steps[r];
+  }
+  Mt mt{nullptr, nullptr};
+  if (active && s.rng_kind == 0) {
+    uint32_t *w = s.rng + static_cast<long long>(r) * kRngWords;
+    mt.mt = reinterpret_cast<unsigned long long *>(w);
+    mt.idx = w + 2 * 312;
+  }
+  const int e = t.num_species;
+  for (unsigned long long it = 0; it < l.steps; ++it) {
+    // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
+    if (active) {
+      const H3 h = SiteCoord(vac, n);
+      for (int k = g * 32 + lane; k < kLocalSites; k += g_per * 32) {
+        const int8_t *o = s_loff + k * 4;
+        rs.local[k] = lat[NeighborId(h, o[0], o[1], o[2], n)];
+      }
+      if (g == 0 && lane < 12) {
+        const int8_t *o = t.dir + lane * 4;
+        rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
+      }
+      if (leader) {
+        double temp = s.temperature[r];
+        if (s.tt_len > 0) temp = InterpT(s.tt_time, s.tt_temp, s.tt_len, time);
+        rs.beta = 1.0 / kBoltzmannEv / temp;
+        double corr = 1.0;
+        if (s.corr_cvac[r] >= 0.0) {
+          // RateCorrector::GetTimeCorrectionFactor (RateCorrector.hpp:17-24)
+          const double cv = 1.64 * exp(-(0.66 / kBoltzmannEv / temp - 0.7));
+          corr = s.corr_cvac[r] / cv / (1 - 13 * s.corr_csol[r]);
+        }
+        rs.corr = corr;
+      }
+    }
+    if (threadIdx.x == 0) s_stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
+    __syncthreads();
+    if (s_stop) {
+      bad_all |= kStatusStopped;
+      break;
+    }
+    // ---- phase 2: the 12 jump evaluations ----
+    if (active) {
+      for (int c = g; c < 12; c += g_per) {
+        const uint8_t *lst = s_lst + c * kStateSites;
+        for (int k = lane; k < kStateSites; k += 32) st[k] = rs.local[lst[k]];
+        for (int k = lane; k < kEnvSites; k += 32) {
+          rm[k] = s_small->rank[rs.local[s_lmmm[c * kEnvSites + k]]];
+          rf[k] = s_small->rank[rs.local[s_lmm2f[c * kEnvSites + k]]];
+          rb[k] = s_small->rank[rs.local[s_lmm2b[c * kEnvSites + k]]];
+        }
+        __syncwarp();
+        const int mig = st[t.pos_second];
+        const int slot = s_small->slot[mig];
+        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+        JumpAcc a{0, 0, 0, 0u};
+        if (ok) {
+          a = s.barrier_kind == 0
+                  ? EvalJump<true>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, s_small->pairtype, lane)
+                  : EvalJump<false>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, s_small->pairtype, lane);
+        }
+        const long long v0 = WarpSum(a.de), v1 = WarpSum(a.d), v2 = WarpSum(a.ks);
+        bad_all |= __reduce_or_sync(0xffffffffu, a.bad);
+        if (lane == 0) {
+          rs.acc[c][0] = v0;
+          rs.acc[c][1] = v1;
+          rs.acc[c][2] = v2;
+          // a jump onto another vacancy has no coefficients: rate 0
+          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // ---- phase 3: rates, selection, update (warp 0 of the replica) ----
+    if (active && g == 0) {
+      double ea = 0, de = 0, k = 0;
+      long long id = 0x7fffffffffffffffLL;
+      if (lane < 12) {
+        const int slot = rs.slot[lane];
+        id = rs.ids[lane];
+        if (slot >= 0) {
+          const JumpOut o = JumpEpilogue(t, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+          ea = o.ea;
+          de = o.de;
+          k = exp(-ea * rs.beta);  // JumpEvent forward rate (JumpEvent.cpp:6-13)
+        } else if (slot == -1) {
+          bad_all |= kStatusNoCoefficients;
+        }
+      }
+      // lane q takes the event of rank q in the id-sorted 1NN list
+      int rank = 0;
+      for (int q = 0; q < 12; ++q) {
+        const long long oid = __shfl_sync(0xffffffffu, id, q);
+        rank += (q != lane) && (oid < id);
+      }
+      int src = 0;
+      for (int q = 0; q < 12; ++q)
+        if (__shfl_sync(0xffffffffu, rank, q) == lane) src = q;
+      const double k_s = __shfl_sync(0xffffffffu, k, src);
+      const double ea_s = __shfl_sync(0xffffffffu, ea, src);
+      const double de_s = __shfl_sync(0xffffffffu, de, src);
+      const long long id_s = __shfl_sync(0xffffffffu, id, src);
+      // total rate and prefix sums, sequential in id order (the reference's
+      // single-thread reduction, KineticMcFirstOmp.cpp:55-68)
+      double total = 0.0, mycum = 0.0;
+      for (int q = 0; q < 12; ++q) {
+        total += __shfl_sync(0xffffffffu, k_s, q);
+        if (lane == q) mycum = total;
+      }
+      double u1 = 0, u2 = 0;
+      if (lane == 0) {
+        if (s.rng_kind == 0) {
+          u1 = MtUniform(mt);  // KineticMcFirstOmp::CalculateTime draws first
+          u2 = MtUniform(mt);  // then KineticMcFirstAbstract::SelectEvent
+        } else {
+          const unsigned long long ctr = step0 + it;
+          const uint4 x = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                        static_cast<uint32_t>(r), 0x4b4d43u, s.rng[r * kRngWords],
+                                        s.rng[r * kRngWords + 1]);
+          u1 = U01Open(x.x, x.y);
+          u2 = U01(x.z, x.w);
+        }
+      }
+      u1 = __shfl_sync(0xffffffffu, u1, 0);
+      u2 = __shfl_sync(0xffffffffu, u2, 0);
+      bool hit;
+      if (s.rng_kind == 0) {
+        // cumulative probabilities k_i / total summed in order, first one >= u2
+        // (std::lower_bound in KineticMcFirstAbstract::SelectEvent)
+        const double p = k_s / total;
+        double cp = 0.0, mycp = 0.0;
+        for (int q = 0; q < 12; ++q) {
+          cp += __shfl_sync(0xffffffffu, p, q);
+          if (lane == q) mycp = cp;
+        }
+        hit = lane < 12 && mycp >= u2;
+      } else {
+        hit = lane < 12 && mycum >= u2 * total;
+      }
+      const unsigned ballot = __ballot_sync(0xffffffffu, hit);
+      const int sel = ballot ? __ffs(ballot) - 1 : 11;  // past the end: the last event
+      const long long tgt = __shfl_sync(0xffffffffu, id_s, sel);
+      const double ea_sel = __shfl_sync(0xffffffffu, ea_s, sel);
+      const double de_sel = __shfl_sync(0xffffffffu, de_s, sel);
+      if (lane == 0) {
+        if (!(total > 0.0) || !isfinite(total)) bad_all |= kStatusNumeric;
+        const double dt = -log(u1) / total / kPrefactor * rs.corr;
+        time += dt;
+        energy += de_sel;
+        lat[vac] = lat[tgt];  // Config::LatticeJump: the migrating atom takes the vacancy site
+        lat[tgt] = static_cast<int8_t>(t.x_code);
+        if (r == l.trace_replica && l.trace) {
+          KmcTraceRec rec;
+          rec.vacancy = vac;
+          rec.target = tgt;
+          rec.selected = sel;
+          rec.pad = 0;
+          rec.ea = ea_sel;
+          rec.de = de_sel;
+          rec.total_rate = total;
+          rec.time = time;
+          rec.energy = energy;
+          l.trace[it] = rec;
+        }
+        rs.ids[0] = tgt;
+      }
+      if (r == l.trace_replica && l.events12 && lane < 12) {
+        double *ev = l.events12 + it * 36 + lane * 3;
+        ev[0] = static_cast<double>(id_s);
+        ev[1] = ea_s;
+        ev[2] = de_s;
+      }
+      vac = tgt;
+    }
+    __syncthreads();
+    if (active && g != 0) vac = rs.ids[0];
+    ++steps_done;
+    __syncthreads();
+  }
+  if (active && leader) {
+    s.vacancy[r] = vac;
+    s.time[r] = time;
+    s.energy[r] = energy;
+    s.steps[r] = step0 + steps_done;
+  }
+  if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
+// K5a: CanonicalMcOmp batch semantics on the reference's RNG stream (one warp).
+// Batch build (CanonicalMcOmp.cpp:40-79): up to `batch` pairs; each pair is
+// redrawn until both sites are outside the exclusion set (1-3NN of chosen
+// sites), giving up the batch after 50 tries; pair draws repeat until the two
+// species differ (CanonicalMcAbstract.cpp:43-51). dE of all pairs on the
+// unchanged lattice, then sequential Metropolis (CanonicalMcAbstract.cpp:86-101).
+// ---------------------------------------------------------------------------
+constexpr int kCmcRefMaxBatch = 256;
+__global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  __shared__ unsigned long long s_mt[312];
+  __shared__ unsigned s_idx;
+  __shared__ long long s_pair[kCmcRefMaxBatch][2];
+  __shared__ double s_de[kCmcRefMaxBatch];
+  __shared__ int s_nb;
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  const unsigned long long *gmt = reinterpret_cast<const unsigned long long *>(a.rng);
+  for (int i = threadIdx.x; i < 312; i += blockDim.x) s_mt[i] = gmt[i];
+  if (threadIdx.x == 0) s_idx = a.rng[2 * 312];
+  __syncthreads();
+  const int lane = threadIdx.x;
+  const Mt mt{s_mt, &s_idx};
+  const int n = a.n;
+  const unsigned long long nsites = 4ULL * n * n * n;
+  int8_t *sa = s.arr, *sb = sa + 44;
+  double energy = *a.energy;
+  unsigned long long done = 0, accepted = 0;
+  long long nmark = 0;
+  while (done < a.attempts) {
+    if (lane == 0) {
+      int nb = 0;
+      nmark = 0;
+      for (int i = 0; i < a.batch; ++i) {
+        int ct = 0;
+        long long l1, l2;
+        bool exhausted = false;
+        for (;;) {
+          // GenerateLatticeIdJumpPair: redraw until the species differ (bounded:
+          // the host rejects single-species lattices, the cap is a safety net)
+          unsigned draws = 0;
+          do {
+            l1 = static_cast<long long>(MtBelow(mt, nsites));
+            l2 = static_cast<long long>(MtBelow(mt, nsites));
+          } while (species[l1] == species[l2] && ++draws < (1u << 24));
+          if (species[l1] == species[l2]) {
+            exhausted = true;
+            break;
+          }
+          ++ct;
+          if (ct == 50) break;
+          if (!a.mark[l1] && !a.mark[l2]) break;
+        }
+        if (exhausted) {
+          atomicOr(a.status, kStatusNumeric);
+          break;
+        }
+        if (ct == 50) break;
+        for (const long long c : {l1, l2}) {
+          const H3 h = SiteCoord(c, n);
+          for (int k = 0; k < kSiteSites; ++k) {
+            const int8_t *o = s.off + k * 4;
+            const long long id = NeighborId(h, o[0], o[1], o[2], n);
+            if (!a.mark[id]) {
+              a.mark[id] = 1;
+              a.mark_list[nmark++] = id;
+            }
+          }
+        }
+        s_pair[nb][0] = l1;
+        s_pair[nb][1] = l2;
+        ++nb;
+      }
+      s_nb = nb;
+    }
+    __syncwarp();
+    const int nb = s_nb;
+    for (int i = 0; i < nb; ++i) {
+      int pa, pb;
+      GatherSwap(s.off, species, n, SiteCoord(s_pair[i][0], n), SiteCoord(s_pair[i][1], n), sa, sb, &pa, &pb, lane);
+      const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
+      if (lane == 0) s_de[i] = static_cast<double>(acc) * t.de_scale;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      for (int i = 0; i < nb; ++i) {
+        const double dE = s_de[i];
+        bool acc = dE < 0;
+        if (!acc) acc = MtUniform(mt) < exp(-dE * a.beta);
+        if (acc) {
+          const long long l1 = s_pair[i][0], l2 = s_pair[i][1];
+          const int8_t v = species[l1];
+          species[l1] = species[l2];
+          species[l2] = v;
+          energy += dE;
+          ++accepted;
+        }
+        ++done;
+      }
+      for (long long q = 0; q < nmark; ++q) a.mark[a.mark_list[q]] = 0;
+      if (nb == 0) done = a.attempts;  // no pair could be placed: stop rather than spin
+    }
+    done = __shfl_sync(0xffffffffu, done, 0);
+    __syncwarp();
+  }
+  if (lane == 0) {
+    *a.energy = energy;
+    *a.done = done;
+    *a.accepted = accepted;
+  }
+  __syncwarp();
+  unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
+  for (int i = lane; i < 312; i += 32) gw[i] = s_mt[i];
+  if (lane == 0) a.rng[2 * 312] = s_idx;
+}
+
+// ---------------------------------------------------------------------------
+// K5b: throughput CMC. Each round draws `candidates` different-species pairs
+// (Philox), resolves overlaps by random priority (a pair survives only if its
+// priority is the largest on every site within 3NN of both its sites, so two
+// survivors are never within 3NN of each other and their dE terms are
+// independent), evaluates dE on the unchanged lattice and applies Metropolis to
+// each survivor independently. Survivors are the Metropolis attempts.
+// ---------------------------------------------------------------------------
+constexpr int kCmcTpThreads = 256;
+__global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8_t *species, CmcTpArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  __shared__ double s_energy;
+  __shared__ unsigned long long s_done, s_acc;
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  if (threadIdx.x == 0) {
+    s_energy = 0.0;
+    s_done = 0;
+    s_acc = 0;
+  }
+  __syncthreads();
+  const int n = a.n;
+  const unsigned long long nsites = 4ULL * n * n * n;
+  const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *sa = s.arr + warp * 88, *sb = sa + 44;
+  const long long gtid = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  const long long gthreads = static_cast<long long>(gridDim.x) * blockDim.x;
+  const uint32_t k0 = static_cast<uint32_t>(a.seed), k1 = static_cast<uint32_t>(a.seed >> 32);
+  unsigned long long prev_done = 0;
+  int empty_rounds = 0;
+  for (unsigned long long round = 1;; ++round) {
+    // Termination is decided from words written before the last grid barrier,
+    // so every thread reads the same values and leaves in the same round.
+    const unsigned long long now = *reinterpret_cast<volatile unsigned long long *>(a.done);
+    if (now >= a.attempts || *reinterpret_cast<volatile int *>(a.quit)) break;
+    empty_rounds = now == prev_done ? empty_rounds + 1 : 0;
+    prev_done = now;
+    if (empty_rounds > 4096) {  // no swappable pair found for thousands of rounds
+      if (gtid == 0) atomicOr(a.status, kStatusNumeric);
+      break;
+    }
+    // phase A: candidates and claims
+    for (long long c = gtid; c < a.candidates; c += gthreads) {
+      long long l1 = -1, l2 = -1;
+      uint32_t prio = 0;
+      for (uint32_t tr = 0; tr < 64; ++tr) {
+        const uint4 x = PhiloxRound10(static_cast<uint32_t>(round), static_cast<uint32_t>(round >> 32),
+                                      static_cast<uint32_t>(c), tr, k0, k1);
+        const long long c1 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.x) << 32) | x.y, nsites));
+        const long long c2 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.z) << 32) | x.w, nsites));
+        if (c1 != c2 && species[c1] != species[c2]) {
+          l1 = c1;
+          l2 = c2;
+          prio = (x.x ^ x.w) & 0xFFFF0000u;
+          break;
+        }
+      }
+      a.cand[2 * c] = l1;
+      a.cand[2 * c + 1] = l2;
+      if (l1 < 0) continue;
+      const unsigned long long key = (round << 32) | prio | static_cast<uint32_t>(c & 0xFFFF);
+      for (const long long e : {l1, l2}) {
+        const H3 h = SiteCoord(e, n);
+        for (int k = 0; k < kSiteSites; ++k) {
+          const int8_t *o = s.off + k * 4;
+          atomicMax(&a.claim[NeighborId(h, o[0], o[1], o[2], n)], key);
+        }
+      }
+    }
+    grid.sync();
+    // phase B: survivors -> dE -> Metropolis
+    for (long long c = static_cast<long long>(blockIdx.x) * warps + warp; c < a.candidates;
+         c += static_cast<long long>(gridDim.x) * warps) {
+      const long long l1 = a.cand[2 * c], l2 = a.cand[2 * c + 1];
+      if (l1 < 0) continue;
+      const unsigned long long c1 = a.claim[l1], c2 = a.claim[l2];
+      const uint32_t lowbits = static_cast<uint32_t>(c1);
+      // our key: round in the high word and candidate index in the low 16 bits
+      if (c1 != c2 || (c1 >> 32) != round || (lowbits & 0xFFFF) != static_cast<uint32_t>(c & 0xFFFF)) continue;
+      int pa, pb;
+      GatherSwap(s.off, species, n, SiteCoord(l1, n), SiteCoord(l2, n), sa, sb, &pa, &pb, lane);
+      const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
+      if (lane == 0) {
+        const double dE = static_cast<double>(acc) * t.de_scale;
+        bool ok = dE < 0;
+        if (!ok) {
+          const uint4 x = PhiloxRound10(static_cast<uint32_t>(round), static_cast<uint32_t>(round >> 32),
+                                        static_cast<uint32_t>(c), 0xACCE97u, k0, k1);
+          ok = U01(x.x, x.y) < exp(-dE * a.beta);
+        }
+        if (ok) {
+          const int8_t v = species[l1];
+          species[l1] = species[l2];
+          species[l2] = v;
+          atomicAdd(&s_energy, dE);
+          atomicAdd(&s_acc, 1ULL);
+        }
+        atomicAdd(&s_done, 1ULL);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_done) {
+      atomicAdd(a.done, s_done);
+      atomicAdd(a.accepted, s_acc);
+      s_done = 0;
+      s_acc = 0;
+    }
+    // only one thread reads the host-written stop flag; the decision travels
+    // through the quit word and the grid barrier
+    if (gtid == 0 && a.stop_flag && *a.stop_flag) {
+      atomicOr(a.status, kStatusStopped);
+      atomicExch(a.quit, 1);
+    }
+    grid.sync();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) a.energy_acc[blockIdx.x] = s_energy;
+}
+
+// Lowest-id vacancy (Config::GetVacancyLatticeId, Config.cpp:298-310) and a
+// species histogram per replica.
+__global__ void replica_scan_kernel(const int8_t *__restrict__ species, const long long *lat_off, const int *lat_n,
+                                    int num_replicas, int x_code, int num_species, long long *first_x,
+                                    unsigned long long *hist) {
+  const int r = blockIdx.y;
+  if (r >= num_replicas) return;
+  const int n = lat_n[r];
+  const long long nsites = 4LL * n * n * n;
+  const int8_t *lat = species + lat_off[r];
+  long long best = 0x7fffffffffffffffLL;
+  unsigned long long local[kMaxSpecies] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nsites;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int c = lat[i];
+    if (c == x_code && i < best) best = i;
+    if (c >= 0 && c < kMaxSpecies) local[c] += 1;
+  }
+  atomicMin(&first_x[r], best);
+  for (int c = 0; c < num_species; ++c)
+    if (local[c]) atomicAdd(&hist[r * kMaxSpecies + c], local[c]);
+}
+
+}  // namespace
+
+cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, const int *lat_n, int num_replicas,
+                              int x_code, int num_species, long long *first_x, unsigned long long *hist,
+                              cudaStream_t stream) {
+  dim3 grid(64, num_replicas);
+  replica_scan_kernel<<<grid, 256, 0, stream>>>(species, lat_off, lat_n, num_replicas, x_code, num_species, first_x,
+                                                hist);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kJumpWarps = 8;
+int Blocks(long long work, int per_block) {
+  long long b = (work + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > 65535LL * 8) b = 65535LL * 8;
+  return static_cast<int>(b);
+}
+}  // namespace
+
+cudaError_t LaunchBarrierBatch(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                               int kind, double *ea, double *de, double *d_or_e0, double *ks, int *status,
+                               cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  const size_t sm = JumpSmemBytes(t, kJumpWarps);
+  barrier_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, kind, ea, de,
+                                                                              d_or_e0, ks, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchEncodeBatch(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                              int *state_start, int *state_end, int *mmm, int *mm2f, int *mm2b, int *status,
+                              cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  const size_t sm = JumpSmemBytes(t, kJumpWarps);
+  encode_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, state_start,
+                                                                             state_end, mmm, mm2f, mm2b, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m, double *de,
+                          int *status, cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  const size_t sm = SiteSmemBytes(t, kJumpWarps);
+  de_pairs_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, de, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
+                         unsigned long long *counts, double *energy, cudaStream_t stream) {
+  cudaError_t err = cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * t.num_theta, stream);
+  if (err != cudaSuccess) return err;
+  const long long nsites = 4LL * n * n * n;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long blocks = (nsites + kCensusThreads - 1) / kCensusThreads;
+  const long long cap = static_cast<long long>(sms) * 8;
+  if (blocks > cap) blocks = cap;
+  census_kernel<<<static_cast<int>(blocks), kCensusThreads, 0, stream>>>(t, species, n, base_code, counts);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  census_energy_kernel<<<1, 32, 0, stream>>>(t, counts, energy);
+  return cudaGetLastError();
+}
+
+size_t KmcSharedBytes(const DevTables &t, int warps_per_replica, int replicas_per_block) {
+  size_t b = 4u * (t.n_de_cl + t.n_mmm_cl + t.n_mm2_cl) + sizeof(SmallTables) + 12 * kStateSites +
+             3 * 12 * kEnvSites + kLocalSites * 4;
+  b = (b + 15) & ~size_t(15);
+  b += sizeof(KmcShared) * replicas_per_block;
+  b += static_cast<size_t>(kArr) * warps_per_replica * replicas_per_block;
+  return (b + 15) & ~size_t(15);
+}
+
+cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
+                      cudaStream_t stream) {
+  const int threads = l.warps_per_replica * l.replicas_per_block * 32;
+  const int blocks = (s.num_replicas + l.replicas_per_block - 1) / l.replicas_per_block;
+  const size_t sm = KmcSharedBytes(t, l.warps_per_replica, l.replicas_per_block);
+  cudaError_t err = cudaFuncSetAttribute(kmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  kmc_kernel<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream) {
+  if (a.batch < 1 || a.batch > kCmcRefMaxBatch) return cudaErrorInvalidValue;
+  const size_t sm = SiteSmemBytes(t, 1);
+  cmc_ref_kernel<<<1, 32, sm, stream>>>(t, species, a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTpArgs &a, int device,
+                                cudaStream_t stream) {
+  const size_t sm = SiteSmemBytes(t, kCmcTpThreads / 32);
+  int per_sm = 0, sms = 0;
+  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cmc_tp_kernel, kCmcTpThreads, sm);
+  if (err != cudaSuccess) return err;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+  int blocks = sms * per_sm;
+  const int needed = (a.candidates + (kCmcTpThreads / 32) - 1) / (kCmcTpThreads / 32);
+  if (blocks > needed) blocks = needed < 1 ? 1 : needed;
+  DevTables tt = t;
+  CmcTpArgs aa = a;
+  int8_t *sp = species;
+  void *args[] = {&tt, &sp, &aa};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(cmc_tp_kernel), blocks, kCmcTpThreads, args, sm,
+                                     stream);
+}
+
+void MtSeed(uint64_t seed, uint32_t *words) {
+  // std::mt19937_64 seeding (the C++ standard, [rand.eng.mers]):
+  // x0 = seed, x_i = 6364136223846793005 * (x_{i-1} ^ (x_{i-1} >> 62)) + i.
+  unsigned long long *mt = reinterpret_cast<unsigned long long *>(words);
+  mt[0] = seed;
+  for (int i = 1; i < 312; ++i) mt[i] = 6364136223846793005ULL * (mt[i - 1] ^ (mt[i - 1] >> 62)) + i;
+  words[2 * 312] = 312;  // next draw twists
+  words[2 * 312 + 1] = 0;
+}
+
+}  // namespace lmc

@@ -1,0 +1,117 @@
+// Launch interface of the sm_103a kernels (implemented in kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_tables.hpp"
+#include "model.hpp"
+
+namespace lmc {
+
+// Per-replica KMC state (structure of arrays, device memory).
+struct KmcDevState {
+  long long *vacancy;
+  unsigned long long *steps;
+  double *time;
+  double *energy;
+  double *temperature;        // base temperature (used when no T(t) table)
+  double *corr_cvac;          // rate-corrector inputs; negative = disabled
+  double *corr_csol;
+  uint32_t *rng;              // per replica: kRngWords words
+  const long long *lat_off;   // site offset of each replica in the species arena
+  const int *lat_n;           // cube edge of each replica
+  int num_replicas;
+  int rng_kind;               // 0 = MT19937-64, 1 = Philox
+  int barrier_kind;           // 0 = Quartic, 1 = E0
+  const double *tt_time;      // optional T(t) table
+  const double *tt_temp;
+  int tt_len;
+};
+
+constexpr int kRngWords = 2 * 312 + 2;  // MT19937-64 state (312 x u64) + index; Philox uses 4 words
+
+struct KmcTraceRec {
+  long long vacancy, target;
+  int selected, pad;
+  double ea, de, total_rate, time, energy;
+};
+
+struct KmcLaunch {
+  int warps_per_replica;
+  int replicas_per_block;
+  unsigned long long steps;
+  int trace_replica;             // -1 = none
+  KmcTraceRec *trace;            // device, steps records
+  double *events12;              // device, steps * 36 doubles, may be null
+  volatile int *stop_flag;       // host-mapped, may be null
+  int *status;                   // device status word (bit flags)
+};
+
+// Status bits written by kernels.
+constexpr int kStatusNotNeighbor = 1;     // a queried pair is not 1NN
+constexpr int kStatusNoCoefficients = 2;  // migrating element without coefficients
+constexpr int kStatusBadCluster = 4;      // ElementCluster outside the indexer (e.g. two vacancies)
+constexpr int kStatusXInEnv = 8;          // vacancy inside an MMM/MM2 environment
+constexpr int kStatusNumeric = 16;        // NaN / inf / non-positive total rate
+constexpr int kStatusStopped = 32;        // stop flag observed
+constexpr int kStatusBadSite = 64;        // site id out of range
+
+cudaError_t LaunchBarrierBatch(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                               int kind, double *ea, double *de, double *d_or_e0, double *ks, int *status,
+                               cudaStream_t stream);
+cudaError_t LaunchEncodeBatch(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                              int *state_start, int *state_end, int *mmm, int *mm2f, int *mm2b, int *status,
+                              cudaStream_t stream);
+cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m, double *de,
+                          int *status, cudaStream_t stream);
+cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
+                         unsigned long long *counts, double *energy, cudaStream_t stream);
+cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
+                      cudaStream_t stream);
+size_t KmcSharedBytes(const DevTables &t, int warps_per_replica, int replicas_per_block);
+
+// Reference-batch CMC (one warp, mt19937_64 stream, batch = `batch` pairs).
+struct CmcRefArgs {
+  int n;
+  double beta;
+  unsigned long long attempts;
+  int batch;
+  uint32_t *rng;             // MT state
+  unsigned char *mark;       // N bytes scratch, zero on entry and on exit
+  long long *mark_list;      // batch * 86 entries scratch
+  double *energy;            // in/out
+  unsigned long long *done;  // attempts done
+  unsigned long long *accepted;
+  int *status;
+};
+cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream);
+
+// Throughput CMC (cooperative persistent grid, Philox, priority-resolved rounds).
+struct CmcTpArgs {
+  int n;
+  double beta;
+  unsigned long long attempts;
+  int candidates;            // candidate pairs per round
+  unsigned long long seed;
+  unsigned long long *claim; // N words scratch (round-stamped priorities)
+  long long *cand;           // 2 * candidates scratch
+  double *energy_acc;        // per-block energy change accumulators (gridDim)
+  unsigned long long *done;
+  unsigned long long *accepted;
+  int *quit;                 // device word, zero on entry
+  int *status;
+  volatile int *stop_flag;
+};
+cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTpArgs &a, int device,
+                                cudaStream_t stream);
+
+// first_x[r] must be preset to INT64_MAX and hist (num_replicas x kMaxSpecies) to 0.
+cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, const int *lat_n, int num_replicas,
+                              int x_code, int num_species, long long *first_x, unsigned long long *hist,
+                              cudaStream_t stream);
+
+// Host-side reference seeding of std::mt19937_64 (state words for the device).
+void MtSeed(uint64_t seed, uint32_t *words);
+
+}  // namespace lmc
