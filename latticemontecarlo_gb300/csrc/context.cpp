@@ -193,7 +193,7 @@ void BuildTables(lmc_ctx *c) {
   for (int k = 0; k < lmc::kSiteSites; ++k)
     for (int v : {pt.site_off[k].x, pt.site_off[k].y, pt.site_off[k].z, 0}) site_off.push_back(Pack4(v));
   // jump dE clusters: state clusters with exactly one pair site
-  std::vector<uint32_t> de_cl, state_all;
+  std::vector<uint32_t> de_cl, de_both, state_all;
   for (const auto &cl : pt.state_clusters) {
     uint32_t w = static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(cl.size) << 3);
     for (int q = 0; q < 3; ++q) w |= static_cast<uint32_t>(q < cl.size ? cl.idx[q] : 0) << (5 + 6 * q);
@@ -205,7 +205,13 @@ void BuildTables(lmc_ctx *c) {
       else if (cl.idx[q] == pt.pos_second) has_second = 1;
       else others.push_back(cl.idx[q]);
     }
-    if (has_first + has_second != 1 || others.empty()) continue;
+    if (has_first + has_second == 2 || others.empty()) {
+      const uint32_t kind = has_first + has_second == 2 ? 2u : (has_first ? 0u : 1u);
+      const uint32_t o = others.empty() ? 63u : static_cast<uint32_t>(others[0]);
+      Require(others.size() <= 1, LMC_ERR_UNSUPPORTED, "unexpected cluster shape");
+      de_both.push_back(static_cast<uint32_t>(cl.label) | (kind << 3) | (o << 5));
+      continue;
+    }
     uint32_t d = static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(has_second) << 3) |
                  (static_cast<uint32_t>(others[0]) << 4) | (static_cast<uint32_t>(others.size() > 1 ? others[1] : 63) << 10);
     de_cl.push_back(d);
@@ -300,7 +306,11 @@ void BuildTables(lmc_ctx *c) {
     we0.insert(we0.end(), fm.e0[sidx].w.begin(), fm.e0[sidx].w.end());
   }
   std::vector<long long> wde(fm.w_de.begin(), fm.w_de.end());
+  std::vector<int8_t> dir_of(27, -1);
+  for (int d = 0; d < lmc::kDirections; ++d)
+    dir_of[(pt.dir[d].x + 1) * 9 + (pt.dir[d].y + 1) * 3 + (pt.dir[d].z + 1)] = static_cast<int8_t>(d);
   t.dir = c->Upload(dir);
+  t.dir_of = c->Upload(dir_of);
   t.state_off = c->Upload(st_off);
   t.mmm_off = c->Upload(mmm_off);
   t.mm2_off = c->Upload(mm2_off);
@@ -311,6 +321,8 @@ void BuildTables(lmc_ctx *c) {
   t.local_mm2f = c->Upload(l_mm2f);
   t.local_mm2b = c->Upload(l_mm2b);
   t.de_cl = c->Upload(de_cl);
+  t.de_both = c->Upload(de_both);
+  t.n_de_both = static_cast<int>(de_both.size());
   t.mmm_cl = c->Upload(mmm_cl);
   t.mm2_cl = c->Upload(mm2_cl);
   t.site_cl = c->Upload(site_cl);

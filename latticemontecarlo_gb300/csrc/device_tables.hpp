@@ -21,6 +21,7 @@ constexpr int kMaxSlots = 6;
 struct DevTables {
   // geometry
   const int8_t *dir;         // [12][4] 1NN offsets (half units)
+  const int8_t *dir_of;      // [27] (dx+1)*9+(dy+1)*3+(dz+1) -> direction index or -1
   const int8_t *state_off;   // [12][60][4]
   const int8_t *mmm_off;     // [12][58][4]
   const int8_t *mm2_off;     // [12][58][4]
@@ -31,6 +32,10 @@ struct DevTables {
   const uint8_t *local_mm2f; // [12][58]
   const uint8_t *local_mm2b; // [12][58] backward (second -> first) MM2 list of jump c
   const uint32_t *de_cl;
+  // state clusters holding both pair sites, and the two singlets:
+  // [0,3) label [3,5) kind (0 first singlet, 1 second singlet, 2 both) [5,11) other site (63 = none)
+  const uint32_t *de_both;
+  int n_de_both;
   const uint32_t *mmm_cl;
   const uint32_t *mm2_cl;
   const uint32_t *site_cl;

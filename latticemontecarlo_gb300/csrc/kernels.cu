@@ -31,11 +31,6 @@ constexpr double kBoltzmannEv = 8.617333262145e-5;  // lmc/cfg/include/Constants
 constexpr double kPrefactor = 1e13;                 // lmc/cfg/include/Constants.hpp:32
 constexpr int kArr = 240;                           // per-warp sorted arrays: 60 + 3 * 58 (+pad)
 
-// (dx+1)*9 + (dy+1)*3 + (dz+1) -> index of the 1NN direction (lexicographic
-// order of the 12 offsets), -1 otherwise.
-__constant__ int8_t c_dir_of[27] = {-1, -1, -1, -1, -1, 0,  -1, 3,  -1, -1, 1,  -1, 4, -1,
-                                    5,  -1, 2,  -1, -1, 8, -1, 9, -1, 10, -1, 11, -1};
-
 struct H3 {
   int x, y, z;
 };
@@ -70,9 +65,11 @@ __device__ __forceinline__ int MinImage(int d, int n) {
   return d;
 }
 
-__device__ __forceinline__ int DirIndex(int dx, int dy, int dz) {
+// Direction index of a half-unit offset via the host-built 27-entry table
+// ((dx+1)*9 + (dy+1)*3 + (dz+1) -> index of the 1NN offset, -1 otherwise).
+__device__ __forceinline__ int DirIndex(const int8_t *dir_of, int dx, int dy, int dz) {
   if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) return -1;
-  return c_dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)];
+  return __ldg(&dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
 }
 
 __device__ __forceinline__ long long WarpSum(long long v) {
@@ -151,6 +148,30 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
     a.de += we - ws;
     const int nx_other = (c1 == x) + (has2 && c2 == x);
     if (nx_other + (cs == x) >= 2 || nx_other + (ce == x) >= 2) a.bad |= kStatusBadCluster;
+  }
+  if (si != x) {
+    // Clusters holding both pair sites and the two singlets keep their
+    // multiset (and cancel) only when the first site is the vacancy; for any
+    // other first species GetDe counts them (VacancyMigrationPredictorQuartic.cpp:127-154).
+    for (int c = lane; c < t.n_de_both; c += 32) {
+      const uint32_t w = t.de_both[c];
+      const int label = w & 7, kind = (w >> 3) & 3, o = (w >> 5) & 63;
+      const int co = o == 63 ? 0 : st[o];
+      long long ws, we;
+      if (kind == 0) {         // singlet of the first site: s_i -> migrant
+        ws = __ldg(&wde[(label * e + si) * e * e]);
+        we = __ldg(&wde[(label * e + sj) * e * e]);
+      } else if (kind == 1) {  // singlet of the second site: migrant -> X
+        ws = __ldg(&wde[(label * e + sj) * e * e]);
+        we = __ldg(&wde[(label * e + x) * e * e]);
+      } else {                 // {first, second, other}: (s_i, s_j) -> (s_j, X)
+        ws = __ldg(&wde[((label * e + si) * e + sj) * e + co]);
+        we = __ldg(&wde[((label * e + sj) * e + x) * e + co]);
+        const int nx = (si == x) + (sj == x) + (o != 63 && co == x);
+        if (nx >= 2 || (sj == x) + (o != 63 && co == x) >= 1) a.bad |= kStatusBadCluster;
+      }
+      a.de += we - ws;
+    }
   }
   const long long *__restrict__ wd = (kQuartic ? t.w_d : t.w_e0) + static_cast<long long>(slot) * t.f_mmm;
   for (int c = lane; c < t.n_mmm_cl; c += 32) {
@@ -241,14 +262,15 @@ size_t JumpSmemBytes(const DevTables &t, int warps) {
 
 // Resolves a (first, second) pair: returns the direction index of second - first
 // and of first - second, or a status bit.
-__device__ __forceinline__ int ResolvePair(long long i, long long j, int n, H3 *hi, H3 *hj, int *di, int *db) {
+__device__ __forceinline__ int ResolvePair(const int8_t *dir_of, long long i, long long j, int n, H3 *hi, H3 *hj,
+                                           int *di, int *db) {
   const long long nsites = 4LL * n * n * n;
   if (i < 0 || j < 0 || i >= nsites || j >= nsites) return kStatusBadSite;
   *hi = SiteCoord(i, n);
   *hj = SiteCoord(j, n);
   const int dx = MinImage(hj->x - hi->x, n), dy = MinImage(hj->y - hi->y, n), dz = MinImage(hj->z - hi->z, n);
-  *di = DirIndex(dx, dy, dz);
-  *db = DirIndex(-dx, -dy, -dz);
+  *di = DirIndex(dir_of, dx, dy, dz);
+  *db = DirIndex(dir_of, -dx, -dy, -dz);
   return *di < 0 ? kStatusNotNeighbor : 0;
 }
 
@@ -285,7 +307,7 @@ __global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ spe
   for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
     H3 hi, hj;
     int di = -1, db = -1;
-    unsigned bad = ResolvePair(pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+    unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
     int slot = -1;
     if (!bad) {
       GatherJump(t, species, n, hi, hj, di, db, s.small, st, rm, rf, rb, lane);
@@ -338,7 +360,7 @@ __global__ void encode_batch_kernel(DevTables t, const int8_t *__restrict__ spec
   for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
     H3 hi, hj;
     int di = -1, db = -1;
-    unsigned bad = ResolvePair(pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+    unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
     if (bad) {
       if (lane == 0) atomicOr(status, static_cast<int>(bad));
       continue;

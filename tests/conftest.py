@@ -27,11 +27,20 @@ def golden():
     return G, load
 
 
+def _build_native():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("lmc_native_build", ROOT / "latticemontecarlo_gb300" / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+
+
+_build_native()
+
+
 @pytest.fixture(scope="session")
 def native():
-    from latticemontecarlo_gb300 import build
-
-    build.build()
     from latticemontecarlo_gb300 import _native
     return _native
 
