@@ -1,0 +1,376 @@
+"""Benchmark of the lattice-MC hot path on GB300.
+
+One JSON line on rank 0. The headline workload is the batched-replica KMC
+configuration: 4096 independent trajectories, cubic supercells with edges
+n ~ U{8..24} (2048 to 55296 sites), one vacancy each, Al/Mg/Zn 0.96/0.02/0.02,
+T ~ U(350, 550) K, 1e4 steps per replica in total. One bench step is one
+persistent launch that advances every replica by 1000 KMC steps (so the
+default --steps 10 covers the whole 1e4-step workload). `value` is KMC
+events/s over all replicas with the lattices resident in HBM; `e2e` is the same
+metric through the public C ABI with host buffers (lattice upload, KMC init,
+run, lattice and state download inside the timed region). The CMC pair-swap
+configuration (30^3 FCC, 108000 sites, Al/Mg/Zn/Cu 0.94/0.02/0.02/0.02,
+T = 500 K) is reported alongside under "cmc".
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle, compiled C, OpenMP) on the host cores for the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "KMC events/s and CMC swaps/s at 1 GB300; surrogate vs plain at <=5 meV barrier MAE"
+KMC_STEPS_PER_BENCH_STEP = 1000
+BYTES_PER_EVENT = 225       # algorithmic HBM bytes per KMC event
+BYTES_PER_ATTEMPT = 100     # algorithmic HBM bytes per CMC attempt
+L2_BYTES = 129 * 1024 * 1024
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def kmc_inputs(seed: int, replicas: int):
+    from latticemontecarlo_gb300 import synthetic as S
+    cfg = S.KMC_BATCHED
+    coeffs = S.make_coefficients(cfg["elements"], seed)
+    ns, species, temps = S.batched_replicas(seed, replicas, cfg["n_range"], cfg["fractions"], cfg["T_range"],
+                                            cfg["elements"])
+    return cfg, coeffs, ns, species, temps
+
+
+def cmc_inputs(seed: int):
+    from latticemontecarlo_gb300 import synthetic as S
+    cfg = S.CMC_SINGLE
+    coeffs = S.make_coefficients(cfg["elements"], seed)
+    sp = S.make_lattice(cfg["n"], cfg["fractions"], 0, seed, cfg["elements"])
+    return cfg, coeffs, sp
+
+
+def run_ours(args, rank, world, local):
+    import torch  # device memory for the L2 flush and distributed plumbing only
+
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import _native as N
+
+    device = local
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seed = 1234 + rank
+    cfg, coeffs, ns, species, temps = kmc_inputs(seed, args.replicas)
+    model = Model.from_coefficients(coeffs, list(cfg["elements"]))
+    ctx = Context(model, device=device)
+    ctx.set_lattices(ns, species)
+    ctx.kmc_init(temps, seed=seed, rng=N.LMC_RNG_PHILOX)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    events_per_step = int(ns.size) * args.kmc_steps_per_launch
+    for _ in range(args.warmup):
+        ctx.kmc_run(args.kmc_steps_per_launch)
+    kernel_ms = []
+    barrier()
+    with ClockSampler(device) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # evict L2 between timed steps (outside the kernel timing)
+            torch.cuda.synchronize()
+            ctx.kmc_run(args.kmc_steps_per_launch)
+            kernel_ms.append(ctx.last_run_ms())
+    barrier()
+    t_ms = float(np.sum(kernel_ms))
+    if world > 1:
+        t = torch.tensor([t_ms], device=f"cuda:{device}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+    total_events = events_per_step * args.steps * world
+    value = total_events / (t_ms / 1e3)
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(1, min(args.steps, 3))
+    h2d = species.nbytes + ns.nbytes + temps.nbytes
+    d2h = species.nbytes + ns.size * (8 + 8 + 8 + 8)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.set_lattices(ns, species)
+        ctx.kmc_init(temps, seed=seed, rng=N.LMC_RNG_PHILOX)
+        ctx.kmc_run(args.kmc_steps_per_launch)
+        out = ctx.get_lattices()
+        vac, st, tm, en = ctx.kmc_state()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    assert out.size == species.size and np.all(st == args.kmc_steps_per_launch)
+    e2e_value = events_per_step * e2e_steps * world / e2e_s
+    peak, peak_kind = peaks()
+    launch_ms = t_ms / args.steps
+    achieved = BYTES_PER_EVENT * events_per_step / (launch_ms / 1e3) / 1e9
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "events/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int64 fixed-point cluster sums + f64 rates/clock",
+        "data": "synthetic (seeded lattices and coefficients; the reference ships none)",
+        "config": {"workload": "batched replica KMC: 4096 FCC supercells n~U{8..24}, 1 vacancy, "
+                               "Al/Mg/Zn .96/.02/.02, T~U(350,550) K, 1e3 KMC steps per replica per step",
+                   "replicas": int(ns.size), "sites_total": int(species.size),
+                   "kmc_steps_per_step": args.kmc_steps_per_launch, "rng": "philox4x32-10",
+                   "l2": "flushed between timed steps (2x L2 write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": args.traffic, "peak_source": peak_kind,
+                     "kernel": "kmc_kernel", "bytes_per_event": BYTES_PER_EVENT},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+    }
+    if args.cmc_steps > 0:
+        result["cmc"] = run_cmc(args, device, flush, barrier)
+    return result, (cfg, coeffs, ns, species, temps)
+
+
+def run_cmc(args, device, flush, barrier):
+    import torch
+
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import _native as N
+
+    cfg, coeffs, sp = cmc_inputs(4321)
+    model = Model.from_coefficients(coeffs, list(cfg["elements"]))
+    ctx = Context(model, device=device)
+    ctx.set_lattices([cfg["n"]], sp)
+    attempts = args.cmc_sweeps_per_step * sp.size
+    e = 0.0
+    for _ in range(2):
+        e, _, _ = ctx.cmc_run(cfg["T"], attempts, mode=N.LMC_CMC_THROUGHPUT, seed=1, energy=e)
+    ms, done_total = [], 0
+    barrier()
+    for k in range(args.cmc_steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e, done, acc = ctx.cmc_run(cfg["T"], attempts, mode=N.LMC_CMC_THROUGHPUT, seed=2 + k, energy=e)
+        ms.append(ctx.last_run_ms())
+        done_total += done
+    barrier()
+    value = done_total / (np.sum(ms) / 1e3)
+    peak, _ = peaks()
+    return {"value": value, "unit": "swaps/s (Metropolis attempts)",
+            "workload": "CMC 30^3 FCC (108000 sites), Al/Mg/Zn/Cu .94/.02/.02/.02, T=500 K, "
+                        f"{args.cmc_sweeps_per_step} sweeps per step, non-overlapping pairs per round",
+            "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
+            "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement of the reference path (baseline)
+# ---------------------------------------------------------------------------
+def cpu_kmc_baseline(seed: int, threads: int, steps_per_replica: int):
+    """Independent trajectories, one per host thread (the reference's own advice
+    for many trajectories, KineticMcAbstract.cpp:188-189), with the barrier memo
+    that plays the role of its LRU cache. Returns events/s over all threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    cfg = S.KMC_BATCHED
+    coeffs = S.make_coefficients(cfg["elements"], seed)
+    ns, species, temps = S.batched_replicas(seed, threads, cfg["n_range"], cfg["fractions"], cfg["T_range"],
+                                            cfg["elements"])
+    offs = np.concatenate([[0], np.cumsum(4 * ns.astype(np.int64) ** 3)])
+    jobs = []
+    for r in range(threads):
+        lat = O.Lattice(int(ns[r]))
+        m = O.Model(cfg["elements"], coeffs, lat)
+        jobs.append((lat, m, species[offs[r]:offs[r + 1]].copy(), float(temps[r])))
+
+    def one(job):
+        lat, m, sp, T = job
+        t0 = time.perf_counter()
+        O.kmc(m, lat, sp, T, seed, steps_per_replica, memo=True)
+        return time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes releases the GIL in the C call
+        list(ex.map(one, jobs))
+    wall = time.perf_counter() - t0
+    return threads * steps_per_replica / wall, wall
+
+
+def cpu_cmc_baseline(threads: int, attempts: int):
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    cfg = S.CMC_SINGLE
+    coeffs = S.make_coefficients(cfg["elements"], 4321)
+    sp = S.make_lattice(cfg["n"], cfg["fractions"], 0, 4321, cfg["elements"])
+    lat = O.Lattice(cfg["n"])
+    m = O.Model(cfg["elements"], coeffs, lat)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    done, _, _, _ = O.cmc(m, lat, sp, cfg["T"], 1, attempts, threads)
+    wall = time.perf_counter() - t0
+    return done / wall, wall
+
+
+def run_reference(args, rank, world):
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    kmc_vals, walls = [], []
+    for _ in range(args.warmup):
+        cpu_kmc_baseline(99, threads, max(50, args.cpu_kmc_steps // 10))
+    for k in range(args.steps):
+        v, w = cpu_kmc_baseline(7 + k, threads, args.cpu_kmc_steps)
+        kmc_vals.append(v)
+        walls.append(w)
+    value = float(np.mean(kmc_vals))
+    cmc_v, cmc_w = cpu_cmc_baseline(threads, args.cpu_cmc_attempts)
+    sample = (f"{threads} independent KMC trajectories (one per host thread, n~U{{8..24}}), "
+              f"{args.cpu_kmc_steps} steps each per step, barrier memo on")
+    return {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(walls) * 1e3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference algorithm)",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": "batched replica KMC (same distribution of supercells, compositions and "
+                               "temperatures), CPU sample", "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cmc": {"value": cmc_v, "unit": "swaps/s (Metropolis attempts)", "cores": threads,
+                "sample": f"{args.cpu_cmc_attempts} attempts, batch = {threads} (CanonicalMcOmp)"},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--replicas", type=int, default=4096)
+    ap.add_argument("--kmc-steps-per-launch", type=int, default=KMC_STEPS_PER_BENCH_STEP)
+    ap.add_argument("--cmc-steps", type=int, default=5)
+    ap.add_argument("--cmc-sweeps-per-step", type=int, default=2)
+    ap.add_argument("--cpu-kmc-steps", type=int, default=1500)
+    ap.add_argument("--cpu-cmc-attempts", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
+    args = ap.parse_args()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, rank, world)), flush=True)
+        return
+    result, _ = run_ours(args, rank, world, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            v, w = cpu_kmc_baseline(7, threads, args.cpu_kmc_steps)
+            result["cpu_baseline"] = {
+                "value": v, "unit": "events/s", "cores": threads, "kind": "port",
+                "sample": f"{threads} independent KMC trajectories (n~U{{8..24}}, one per host thread), "
+                          f"{args.cpu_kmc_steps} steps each, oracle C restatement with barrier memo, "
+                          f"{w:.1f} s wall"}
+        print(json.dumps(result), flush=True)
+
+
+if __name__ == "__main__":
+    main()

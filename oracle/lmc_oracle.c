@@ -1460,6 +1460,7 @@ int64_t orc_cmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T
                 int batch, double *energy_io, double *energy_trace, int64_t cap, int64_t *accepted) {
   orc_mt g;
   orc_mt_seed(&g, seed);
+  (void)maps_for(m, lat); /* build the mappings before any parallel region */
   const double beta = 1.0 / kBoltzmann / T;
   const uint64_t N = (uint64_t)lat->N;
   uint8_t *mark = (uint8_t *)calloc(N, 1);
@@ -1503,12 +1504,15 @@ int64_t orc_cmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T
       pairs[nb][1] = l2;
       ++nb;
     }
-    for (int i = 0; i < nb; ++i)
-      if (orc_pair_site_de(m, lat, sp, pairs[i][0], pairs[i][1], &des[i])) {
-        done = -1;
-        break;
-      }
-    if (done < 0) break;
+    /* the batch's dE on the unchanged lattice, one pair per OpenMP thread
+     * (CanonicalMcOmp.cpp:75-78) */
+    int failed = 0;
+#pragma omp parallel for schedule(static) reduction(| : failed)
+    for (int i = 0; i < nb; ++i) failed |= orc_pair_site_de(m, lat, sp, pairs[i][0], pairs[i][1], &des[i]) != 0;
+    if (failed) {
+      done = -1;
+      break;
+    }
     /* sequential Metropolis (CanonicalMcAbstract.cpp:86-101) */
     for (int i = 0; i < nb; ++i) {
       if (energy_trace && done < cap) energy_trace[done] = energy;
