@@ -173,17 +173,20 @@ def run_ours(args, rank, world, local):
         t_ms = float(t.item())
     total_events = events_per_step * args.steps * world
     value = total_events / (t_ms / 1e3)
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (pinned host memory)
+    pinned = torch.empty(species.size, dtype=torch.int8, pin_memory=True).numpy()
+    pinned[:] = species
+    species_out = torch.empty(species.size, dtype=torch.int8, pin_memory=True).numpy()
     e2e_steps = max(1, min(args.steps, 3))
     h2d = species.nbytes + ns.nbytes + temps.nbytes
     d2h = species.nbytes + ns.size * (8 + 8 + 8 + 8)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.set_lattices(ns, species)
+        ctx.set_lattices(ns, pinned)
         ctx.kmc_init(temps, seed=seed, rng=N.LMC_RNG_PHILOX)
         ctx.kmc_run(args.kmc_steps_per_launch)
-        out = ctx.get_lattices()
+        out = ctx.get_lattices(species_out)
         vac, st, tm, en = ctx.kmc_state()
     barrier()
     e2e_s = time.perf_counter() - t0

@@ -125,8 +125,11 @@ class Context:
         check(N.lib.lmc_ctx_set_lattices(self._h, ns.size, ptr(ns, C.c_int32), ptr(sp, C.c_int8)))
         self.ns = ns
 
-    def get_lattices(self) -> np.ndarray:
-        out = np.empty(int(N.lib.lmc_ctx_total_sites(self._h)), np.int8)
+    def get_lattices(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Copies every replica's species back (into `out` when given, e.g. pinned memory)."""
+        if out is None:
+            out = np.empty(int(N.lib.lmc_ctx_total_sites(self._h)), np.int8)
+        assert out.dtype == np.int8 and out.size == int(N.lib.lmc_ctx_total_sites(self._h))
         check(N.lib.lmc_ctx_get_lattices(self._h, ptr(out, C.c_int8)))
         return out
 

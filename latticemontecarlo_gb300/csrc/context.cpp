@@ -108,7 +108,8 @@ struct lmc_ctx {
   std::vector<int> n;
   std::vector<long long> offsets;
   long long total_sites{0};
-  DevBuf species, lat_off, lat_n;
+  DevBuf species, lat_off, lat_n, scan;
+  std::vector<unsigned long long> scan_host;  // per replica species histogram + invalid count
   // batch scratch
   DevBuf pairs, out0, out1, out2, out3, status, counts, energy, enc;
   // KMC
@@ -126,7 +127,7 @@ struct lmc_ctx {
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
-    for (DevBuf *b : {&species, &lat_off, &lat_n, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
+    for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
                       &k_tt_time, &k_tt_temp, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
@@ -659,19 +660,32 @@ int lmc_ctx_set_lattices(lmc_ctx *ctx, int num_replicas, const int32_t *n, const
       off[r] = total;
       total += 4LL * nn[r] * nn[r] * nn[r];
     }
-    const int e = ctx->fm.num_species;
-    for (long long i = 0; i < total; ++i)
-      Require(species[i] >= 0 && species[i] < e, LMC_ERR_OUT_OF_RANGE, "species code out of range");
     if (total + 64 > static_cast<long long>(ctx->species.bytes)) ctx->species.Alloc(total + 64);
-    ctx->lat_off.Alloc(sizeof(long long) * num_replicas);
-    ctx->lat_n.Alloc(sizeof(int) * num_replicas);
+    ctx->lat_off.Ensure(sizeof(long long) * num_replicas);
+    ctx->lat_n.Ensure(sizeof(int) * num_replicas);
+    ctx->scan.Ensure(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * num_replicas);
     CudaCheck(cudaMemcpyAsync(ctx->species.p, species, total, cudaMemcpyHostToDevice, ctx->stream), "H2D species");
     CudaCheck(cudaMemcpyAsync(ctx->lat_off.p, off.data(), sizeof(long long) * num_replicas, cudaMemcpyHostToDevice,
                               ctx->stream),
               "H2D offsets");
     CudaCheck(cudaMemcpyAsync(ctx->lat_n.p, nn.data(), sizeof(int) * num_replicas, cudaMemcpyHostToDevice, ctx->stream),
               "H2D n");
+    // species codes are validated on the device (the last histogram column counts bad codes)
+    CudaCheck(cudaMemsetAsync(ctx->scan.p, 0, sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * num_replicas,
+                              ctx->stream),
+              "memset");
+    CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>(), ctx->lat_n.as<int>(),
+                                     num_replicas, ctx->fm.x_code, ctx->fm.num_species, nullptr,
+                                     ctx->scan.as<unsigned long long>(), ctx->stream),
+              "scan kernel");
+    ctx->scan_host.resize(static_cast<size_t>(lmc::kMaxSpecies + 1) * num_replicas);
+    CudaCheck(cudaMemcpyAsync(ctx->scan_host.data(), ctx->scan.p, sizeof(unsigned long long) * ctx->scan_host.size(),
+                              cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
     ctx->Sync();
+    for (int r = 0; r < num_replicas; ++r)
+      Require(ctx->scan_host[static_cast<size_t>(r) * (lmc::kMaxSpecies + 1) + lmc::kMaxSpecies] == 0,
+              LMC_ERR_OUT_OF_RANGE, "species code out of range in replica " + std::to_string(r));
     ctx->num_replicas = num_replicas;
     ctx->n = nn;
     ctx->offsets = off;
@@ -833,7 +847,7 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     ctx->k_rng.Ensure(sizeof(uint32_t) * lmc::kRngWords * R);
     // first vacancy and species histogram of every replica
     DevBuf hist;
-    hist.Alloc(sizeof(unsigned long long) * lmc::kMaxSpecies * R);
+    hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * R);
     std::vector<long long> first(R, std::numeric_limits<long long>::max());
     CudaCheck(cudaMemcpyAsync(ctx->k_vac.p, first.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, ctx->stream),
               "H2D");
@@ -842,7 +856,7 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
                                      ctx->fm.x_code, ctx->fm.num_species, ctx->k_vac.as<long long>(),
                                      hist.as<unsigned long long>(), ctx->stream),
               "scan kernel");
-    std::vector<unsigned long long> h(lmc::kMaxSpecies * R);
+    std::vector<unsigned long long> h((lmc::kMaxSpecies + 1) * R);
     CudaCheck(cudaMemcpyAsync(first.data(), ctx->k_vac.p, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
               "D2H");
     CudaCheck(cudaMemcpyAsync(h.data(), hist.p, hist.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
@@ -857,8 +871,8 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
         const double nsites = 4.0 * ctx->n[r] * ctx->n[r] * ctx->n[r];
         unsigned long long sol = 0;
         for (int c = 0; c < ctx->fm.num_species; ++c)
-          if (c != ctx->fm.x_code && c != al) sol += h[r * lmc::kMaxSpecies + c];
-        cvac[r] = static_cast<double>(h[r * lmc::kMaxSpecies + ctx->fm.x_code]) / nsites;
+          if (c != ctx->fm.x_code && c != al) sol += h[r * (lmc::kMaxSpecies + 1) + c];
+        cvac[r] = static_cast<double>(h[r * (lmc::kMaxSpecies + 1) + ctx->fm.x_code]) / nsites;
         csol[r] = static_cast<double>(sol) / nsites;
       }
     }
@@ -1013,7 +1027,7 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
       // both CMC modes redraw pairs until the two species differ: refuse a
       // lattice with a single species instead of spinning on it
       DevBuf hist, first;
-      hist.Alloc(sizeof(unsigned long long) * lmc::kMaxSpecies);
+      hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1));
       first.Alloc(sizeof(long long));
       const long long big = std::numeric_limits<long long>::max();
       CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
@@ -1022,7 +1036,7 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
                                        ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, ctx->fm.num_species,
                                        first.as<long long>(), hist.as<unsigned long long>(), ctx->stream),
                 "scan kernel");
-      unsigned long long h[lmc::kMaxSpecies];
+      unsigned long long h[lmc::kMaxSpecies + 1];
       CudaCheck(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
       ctx->Sync();
       int present = 0;

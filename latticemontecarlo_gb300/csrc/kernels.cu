@@ -1202,15 +1202,18 @@ __global__ void replica_scan_kernel(const int8_t *__restrict__ species, const lo
   const int8_t *lat = species + lat_off[r];
   long long best = 0x7fffffffffffffffLL;
   unsigned long long local[kMaxSpecies] = {0, 0, 0, 0, 0, 0};
+  unsigned long long invalid = 0;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nsites;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int c = lat[i];
     if (c == x_code && i < best) best = i;
-    if (c >= 0 && c < kMaxSpecies) local[c] += 1;
+    if (c >= 0 && c < num_species) local[c] += 1;
+    else invalid += 1;
   }
-  atomicMin(&first_x[r], best);
+  if (first_x) atomicMin(&first_x[r], best);
   for (int c = 0; c < num_species; ++c)
-    if (local[c]) atomicAdd(&hist[r * kMaxSpecies + c], local[c]);
+    if (local[c]) atomicAdd(&hist[r * (kMaxSpecies + 1) + c], local[c]);
+  if (invalid) atomicAdd(&hist[r * (kMaxSpecies + 1) + kMaxSpecies], invalid);
 }
 
 }  // namespace
@@ -1218,7 +1221,7 @@ __global__ void replica_scan_kernel(const int8_t *__restrict__ species, const lo
 cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, const int *lat_n, int num_replicas,
                               int x_code, int num_species, long long *first_x, unsigned long long *hist,
                               cudaStream_t stream) {
-  dim3 grid(64, num_replicas);
+  dim3 grid(num_replicas > 256 ? 8 : 64, num_replicas);
   replica_scan_kernel<<<grid, 256, 0, stream>>>(species, lat_off, lat_n, num_replicas, x_code, num_species, first_x,
                                                 hist);
   return cudaGetLastError();

@@ -106,7 +106,8 @@ struct CmcTpArgs {
 cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTpArgs &a, int device,
                                 cudaStream_t stream);
 
-// first_x[r] must be preset to INT64_MAX and hist (num_replicas x kMaxSpecies) to 0.
+// first_x (may be null) must be preset to INT64_MAX and hist (num_replicas x (kMaxSpecies + 1),
+// the last column counting codes outside the alphabet) to 0.
 cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, const int *lat_n, int num_replicas,
                               int x_code, int num_species, long long *first_x, unsigned long long *hist,
                               cudaStream_t stream);
