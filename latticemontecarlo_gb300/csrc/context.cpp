@@ -826,6 +826,25 @@ int lmc_energy(lmc_ctx *ctx, int replica, double *energy, int64_t *counts) {
   });
 }
 
+int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *energy_dev) {
+  return Guard([&] {
+    Require(ctx && species_dev && energy_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    Require(n >= 6 && n <= 1000, LMC_ERR_UNSUPPORTED, "supercell edge must be in [6, 1000]");
+    Require(ctx->t.num_theta <= lmc::kNoAllocMaxTheta, LMC_ERR_UNSUPPORTED,
+            "lmc_energy_noalloc: the model's " + std::to_string(ctx->t.num_theta) +
+                " cluster counters exceed the " + std::to_string(lmc::kNoAllocMaxTheta) +
+                "-entry static scratch");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    unsigned long long *scratch = nullptr;
+    CudaCheck(lmc::NoAllocCensusScratch(ctx->device, &scratch), "cudaGetSymbolAddress");
+    int base = ctx->fm.x_code == 0 ? 1 : 0;
+    for (int c = 0; c < ctx->fm.num_species; ++c)
+      if (ctx->model.alphabet[c] == "Al") base = c;
+    // LaunchCensus clears the counters it uses before the census kernel runs.
+    CudaCheck(lmc::LaunchCensus(ctx->t, species_dev, n, base, scratch, energy_dev, ctx->stream), "census kernel");
+  });
+}
+
 int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options *opt) {
   return Guard([&] {
     Require(ctx && temperature && opt && ctx->num_replicas > 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");

@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "kernels.cuh"
 
@@ -1330,6 +1331,35 @@ cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTp
   void *args[] = {&tt, &sp, &aa};
   return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(cmc_tp_kernel), blocks, kCmcTpThreads, args, sm,
                                      stream);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free census: the cluster histogram lives in a file-scope device
+// array shared by every call on a device (see lmc_energy_noalloc).
+// ---------------------------------------------------------------------------
+namespace {
+static __device__ __align__(256) unsigned long long g_noalloc_census_counts[kNoAllocMaxTheta];
+}  // namespace
+
+cudaError_t NoAllocCensusScratch(int device, unsigned long long **ptr) {
+  // The array's host-side name is only a stand-in; the device address is
+  // looked up once per device, with that device current.
+  static std::mutex mu;
+  static unsigned long long *addr[kNoAllocMaxDevices] = {};
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (addr[device] == nullptr) {
+    int current = -1;
+    cudaError_t err = cudaGetDevice(&current);
+    if (err != cudaSuccess) return err;
+    if (current != device) return cudaErrorInvalidDevice;
+    void *p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noalloc_census_counts);
+    if (err != cudaSuccess) return err;
+    addr[device] = static_cast<unsigned long long *>(p);
+  }
+  *ptr = addr[device];
+  return cudaSuccess;
 }
 
 void MtSeed(uint64_t seed, uint32_t *words) {

@@ -112,6 +112,13 @@ cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, c
                               int x_code, int num_species, long long *first_x, unsigned long long *hist,
                               cudaStream_t stream);
 
+// Scratch of the allocation-free census: a file-scope device array of
+// kNoAllocMaxTheta counters. Returns its device address for `device`, which
+// must be the current device; the lookup happens on the first call per device.
+constexpr int kNoAllocMaxTheta = 512;
+constexpr int kNoAllocMaxDevices = 64;
+cudaError_t NoAllocCensusScratch(int device, unsigned long long **ptr);
+
 // Host-side reference seeding of std::mt19937_64 (state words for the device).
 void MtSeed(uint64_t seed, uint32_t *words);
 
