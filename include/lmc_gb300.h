@@ -204,7 +204,14 @@ typedef struct lmc_kmc_options {
   int tt_len;
   int warps_per_replica;   /* 0 = autotuned */
   int replicas_per_block;  /* 0 = autotuned */
+  int evaluation;          /* LMC_EVAL_SPARSE (default) or LMC_EVAL_DENSE; identical results */
 } lmc_kmc_options;
+
+/* Jump evaluation inside the KMC kernel: both give bit-identical barriers.
+ * Sparse: constant all-solvent sums plus corrections for the clusters that touch
+ * a non-solvent site (fast for dilute alloys). Dense: every cluster term. */
+#define LMC_EVAL_SPARSE 0
+#define LMC_EVAL_DENSE 1
 
 /* Per-step record of replica `trace_replica` (for parity checks and logs). */
 typedef struct lmc_kmc_step {

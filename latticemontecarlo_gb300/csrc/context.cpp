@@ -117,6 +117,9 @@ struct lmc_ctx {
   lmc_kmc_options kmc_opt{};
   DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
   int tt_len{0};
+  // sparse KMC tables (built for the dominant species at lmc_kmc_init)
+  std::vector<DevBuf> sparse_bufs;
+  lmc::KmcSparse sparse{};
   // CMC
   DevBuf c_mark, c_mark_list, c_claim, c_cand, c_eacc, c_stats;
   std::map<int, std::pair<uint64_t, DevBuf>> c_mt;  // per replica: seed and MT state
@@ -132,6 +135,7 @@ struct lmc_ctx {
                       &k_tt_time, &k_tt_temp, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
+    for (auto &b : sparse_bufs) b.Free();
     if (h_stop) cudaFreeHost(h_stop);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -139,11 +143,11 @@ struct lmc_ctx {
   }
 
   template <typename T>
-  const T *Upload(const std::vector<T> &v) {
+  const T *Upload(const std::vector<T> &v, std::vector<DevBuf> *into = nullptr) {
     DevBuf b;
     b.Alloc(std::max<size_t>(v.size() * sizeof(T), 16));
     if (!v.empty()) CudaCheck(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
-    tables.push_back(b);
+    (into ? into : &tables)->push_back(b);
     return b.as<T>();
   }
   void Sync() { CudaCheck(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
@@ -381,6 +385,134 @@ int CodeOf(const lmc::Model &m, const char *name) {
 std::vector<double> Vec(const double *p, int n, const char *what) {
   Require(p != nullptr || n == 0, LMC_ERR_INVALID_ARGUMENT, std::string(what) + " is null");
   return std::vector<double>(p, p + n);
+}
+
+// Tables of the sparse KMC evaluation for dominant species `base` (see KmcSparse).
+void BuildSparse(lmc_ctx *c, int base) {
+  const auto &pt = lmc::GetPairTables();
+  const auto &fm = c->fm;
+  const int e = fm.num_species, x = fm.x_code, eh = fm.num_onehot;
+  const int rb0 = fm.onehot_rank[base];
+  Require(rb0 >= 0 && base != x, LMC_ERR_INVALID_ARGUMENT, "dominant species has no one-hot slot");
+  for (auto &b : c->sparse_bufs) b.Free();
+  c->sparse_bufs.clear();
+  lmc::KmcSparse sp{};
+  sp.base_code = base;
+  // state incidence: clusters with exactly one pair site, keyed by each other site
+  std::vector<std::vector<uint32_t>> by_pos(lmc::kStateSites);
+  std::vector<long long> base_de(e, 0);
+  auto w = [&](int label, int c0, int c1, int c2) { return static_cast<long long>(fm.w_de[((label * e + c0) * e + c1) * e + c2]); };
+  for (const auto &cl : pt.state_clusters) {
+    int has_first = 0, has_second = 0;
+    std::vector<int> others;
+    for (int q = 0; q < cl.size; ++q) {
+      if (cl.idx[q] == pt.pos_first) has_first = 1;
+      else if (cl.idx[q] == pt.pos_second) has_second = 1;
+      else others.push_back(cl.idx[q]);
+    }
+    if (has_first + has_second != 1 || others.empty()) continue;  // cancel when the first site is the vacancy
+    for (size_t k = 0; k < others.size(); ++k) {
+      const uint32_t partner = others.size() > 1 ? static_cast<uint32_t>(others[1 - k]) : 63u;
+      by_pos[others[k]].push_back(static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(has_second) << 3) | (partner << 4));
+    }
+    const int b2 = others.size() > 1 ? base : 0;
+    for (int m = 0; m < e; ++m) {
+      const long long v = w(cl.label, m, base, b2) - w(cl.label, x, base, b2);
+      base_de[m] += has_second ? -v : v;
+    }
+  }
+  std::vector<uint16_t> st_off(lmc::kStateSites + 1, 0);
+  std::vector<uint32_t> st_inc;
+  for (int p = 0; p < lmc::kStateSites; ++p) {
+    st_off[p] = static_cast<uint16_t>(st_inc.size());
+    st_inc.insert(st_inc.end(), by_pos[p].begin(), by_pos[p].end());
+  }
+  st_off[lmc::kStateSites] = static_cast<uint16_t>(st_inc.size());
+  // dE correction per (label, migrant, c1, c2): f = (W(M, c1, c2) - W(X, c1, c2)) - (same at base)
+  std::vector<long long> f_de(static_cast<size_t>(8) * e * e * e, 0);
+  for (int label = 1; label < 8; ++label)
+    for (int m = 0; m < e; ++m)
+      for (int c1 = 0; c1 < e; ++c1)
+        for (int c2 = 0; c2 < e; ++c2) {
+          const int b2 = label <= 3 ? 0 : base;
+          if (label <= 3 && c2 != 0) continue;
+          f_de[((label * e + m) * e + c1) * e + c2] =
+              (w(label, m, c1, c2) - w(label, x, c1, c2)) - (w(label, m, base, b2) - w(label, x, base, b2));
+        }
+  // environment incidence and W - W(base) tables
+  auto env_inc = [&](const lmc::EnvEncoding &enc, std::vector<uint16_t> &off, std::vector<uint32_t> &inc) {
+    const auto ooff = enc.OrbitOffsets(eh);
+    std::vector<std::vector<uint32_t>> bp(lmc::kEnvSites);
+    for (const auto &cl : enc.clusters) {
+      const uint32_t fb = static_cast<uint32_t>(ooff[cl.orbit]);
+      const uint32_t mode = static_cast<uint32_t>(cl.mode);
+      const uint32_t pb = cl.b < 0 ? 63u : static_cast<uint32_t>(cl.b);
+      bp[cl.a].push_back(fb | (mode << 14) | (pb << 16) | (1u << 22));
+      if (cl.b >= 0) bp[cl.b].push_back(fb | (mode << 14) | (static_cast<uint32_t>(cl.a) << 16));
+    }
+    off.assign(lmc::kEnvSites + 1, 0);
+    inc.clear();
+    for (int p = 0; p < lmc::kEnvSites; ++p) {
+      off[p] = static_cast<uint16_t>(inc.size());
+      inc.insert(inc.end(), bp[p].begin(), bp[p].end());
+    }
+    off[lmc::kEnvSites] = static_cast<uint16_t>(inc.size());
+  };
+  std::vector<uint16_t> mmm_off, mm2_off;
+  std::vector<uint32_t> mmm_inc, mm2_inc;
+  env_inc(pt.mmm, mmm_off, mmm_inc);
+  env_inc(pt.mm2, mm2_off, mm2_inc);
+  auto delta = [&](const lmc::EnvEncoding &enc, const std::vector<int64_t> &wv, std::vector<long long> &out,
+                   long long *base_sum, int mult) {
+    const auto ooff = enc.OrbitOffsets(eh);
+    for (size_t o = 0; o < enc.orbits.size(); ++o) {
+      const long long w0 = wv[ooff[o] + lmc::PairType(enc.orbits[o].mode, rb0, rb0, eh)];
+      for (int j = ooff[o]; j < ooff[o + 1]; ++j) out.push_back(wv[j] - w0);
+      *base_sum += static_cast<long long>(mult) * w0 * enc.orbits[o].size;
+    }
+  };
+  const int slots = static_cast<int>(fm.slot_code.size());
+  std::vector<long long> dwd, dwks, dwe0, base_form(3 * std::max(1, slots), 0);
+  for (int sidx = 0; sidx < slots; ++sidx) {
+    delta(pt.mmm, fm.quartic_d[sidx].w, dwd, &base_form[sidx * 3 + 0], 1);
+    delta(pt.mm2, fm.quartic_ks[sidx].w, dwks, &base_form[sidx * 3 + 1], 2);
+    delta(pt.mmm, fm.e0[sidx].w, dwe0, &base_form[sidx * 3 + 2], 1);
+  }
+  // local index -> list position for each jump
+  std::vector<uint8_t> pos(4 * 12 * 136, 255);
+  std::vector<uint8_t> l_st(12 * lmc::kStateSites), l_mmm(12 * lmc::kEnvSites), l_f(12 * lmc::kEnvSites),
+      l_b(12 * lmc::kEnvSites);
+  CudaCheck(cudaMemcpy(l_st.data(), c->t.local_st, l_st.size(), cudaMemcpyDeviceToHost), "D2H");
+  CudaCheck(cudaMemcpy(l_mmm.data(), c->t.local_mmm, l_mmm.size(), cudaMemcpyDeviceToHost), "D2H");
+  CudaCheck(cudaMemcpy(l_f.data(), c->t.local_mm2f, l_f.size(), cudaMemcpyDeviceToHost), "D2H");
+  CudaCheck(cudaMemcpy(l_b.data(), c->t.local_mm2b, l_b.size(), cudaMemcpyDeviceToHost), "D2H");
+  for (int d = 0; d < 12; ++d) {
+    for (int k = 0; k < lmc::kStateSites; ++k)
+      if (k != pt.pos_first && k != pt.pos_second) pos[(0 * 12 + d) * 136 + l_st[d * lmc::kStateSites + k]] = k;
+    for (int k = 0; k < lmc::kEnvSites; ++k) {
+      pos[(1 * 12 + d) * 136 + l_mmm[d * lmc::kEnvSites + k]] = static_cast<uint8_t>(k);
+      pos[(2 * 12 + d) * 136 + l_f[d * lmc::kEnvSites + k]] = static_cast<uint8_t>(k);
+      pos[(3 * 12 + d) * 136 + l_b[d * lmc::kEnvSites + k]] = static_cast<uint8_t>(k);
+    }
+  }
+  auto &B = c->sparse_bufs;
+  sp.inc_st_off = c->Upload(st_off, &B);
+  sp.inc_st = c->Upload(st_inc, &B);
+  sp.inc_mmm_off = c->Upload(mmm_off, &B);
+  sp.inc_mmm = c->Upload(mmm_inc, &B);
+  sp.inc_mm2_off = c->Upload(mm2_off, &B);
+  sp.inc_mm2 = c->Upload(mm2_inc, &B);
+  sp.pos = c->Upload(pos, &B);
+  sp.f_de = c->Upload(f_de, &B);
+  sp.base_de = c->Upload(base_de, &B);
+  sp.dw_d = c->Upload(dwd, &B);
+  sp.dw_ks = c->Upload(dwks, &B);
+  sp.dw_e0 = c->Upload(dwe0, &B);
+  sp.base_form = c->Upload(base_form, &B);
+  sp.n_inc_st = static_cast<int>(st_inc.size());
+  sp.n_inc_mmm = static_cast<int>(mmm_inc.size());
+  sp.n_inc_mm2 = static_cast<int>(mm2_inc.size());
+  c->sparse = sp;
 }
 
 void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
@@ -883,6 +1015,17 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     hist.Free();
     for (int r = 0; r < R; ++r)
       Require(first[r] != std::numeric_limits<long long>::max(), LMC_ERR_INVALID_ARGUMENT, "vacancy not found");
+    // dominant species with a one-hot slot: the base of the sparse evaluation
+    {
+      std::vector<unsigned long long> tot(ctx->fm.num_species, 0);
+      for (int r = 0; r < R; ++r)
+        for (int c = 0; c < ctx->fm.num_species; ++c) tot[c] += h[r * (lmc::kMaxSpecies + 1) + c];
+      int base = -1;
+      for (int c = 0; c < ctx->fm.num_species; ++c)
+        if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || tot[c] > tot[base])) base = c;
+      Require(base >= 0, LMC_ERR_INVALID_ARGUMENT, "no element of the barrier set in the lattices");
+      BuildSparse(ctx, base);
+    }
     const int al = ctx->model.Code("Al");
     std::vector<double> cvac(R, -1.0), csol(R, 0.0);
     if (opt->rate_corrector) {
@@ -989,6 +1132,8 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     }
     l.stop_flag = ctx->d_stop;
     l.status = ctx->status.as<int>();
+    l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
+    l.sp = ctx->sparse;
     ctx->ClearStatus();
     CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
     CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");

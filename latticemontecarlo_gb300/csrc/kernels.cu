@@ -714,6 +714,89 @@ __device__ __forceinline__ double InterpT(const double *tt, const double *tv, in
   return ly + ((time - lx) / (ux - lx)) * (uy - ly);
 }
 
+// Sparse evaluation of jump c (see KmcSparse): per-lane partial corrections.
+__device__ __forceinline__ JumpAcc EvalJumpSparse(const DevTables &t, const KmcSparse &sp, const int8_t *local,
+                                                  const unsigned *nbmask, int c, int mig, int slot, bool quartic,
+                                                  const uint16_t *s_ist_off, const uint32_t *s_ist,
+                                                  const uint16_t *s_immm_off, const uint32_t *s_immm,
+                                                  const uint16_t *s_imm2_off, const uint32_t *s_imm2,
+                                                  const uint8_t *s_pos, const uint8_t *s_lst, const uint8_t *s_lmmm,
+                                                  const uint8_t *s_lmm2f, const uint8_t *s_lmm2b,
+                                                  const SmallTables *sm, int lane) {
+  JumpAcc a{0, 0, 0, 0u};
+  const int e = t.num_species, x = t.x_code, base = sp.base_code;
+  const uint8_t *pst = s_pos + (0 * 12 + c) * 136, *pmm = s_pos + (1 * 12 + c) * 136;
+  const uint8_t *pf = s_pos + (2 * 12 + c) * 136, *pb = s_pos + (3 * 12 + c) * 136;
+  const uint8_t *lst = s_lst + c * kStateSites, *lmm = s_lmmm + c * kEnvSites;
+  const uint8_t *lf = s_lmm2f + c * kEnvSites, *lb = s_lmm2b + c * kEnvSites;
+  const long long *__restrict__ fde = sp.f_de;
+  const long long *__restrict__ wd = (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * t.f_mmm;
+  const long long *__restrict__ wk = sp.dw_ks + static_cast<long long>(slot) * t.f_mm2;
+  for (int w = 0; w < 5; ++w) {
+    unsigned m = nbmask[w];
+    while (m) {
+      const int l = w * 32 + __ffs(m) - 1;
+      m &= m - 1;
+      const int code = local[l];
+      const int rp = sm->rank[code];
+      int p = pst[l];
+      if (p != 255) {  // energy change: clusters with one pair site, l among the others
+        if (code == x) a.bad |= kStatusBadCluster;
+        for (int q = s_ist_off[p] + lane; q < s_ist_off[p + 1]; q += 32) {
+          const uint32_t v = s_ist[q];
+          const int label = v & 7, side = (v >> 3) & 1, partner = (v >> 4) & 63;
+          int c2 = 0;
+          if (partner != 63) {
+            c2 = local[lst[partner]];
+            if (c2 != base && partner < p) continue;  // counted at the partner
+          }
+          const long long f = __ldg(&fde[((label * e + mig) * e + code) * e + c2]);
+          a.de += side ? -f : f;
+        }
+      }
+      p = pmm[l];
+      if (p != 255) {  // MMM (D or e0)
+        for (int q = s_immm_off[p] + lane; q < s_immm_off[p + 1]; q += 32) {
+          const uint32_t v = s_immm[q];
+          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
+          int rq = 0;
+          if (partner != 63) {
+            const int cq = local[lmm[partner]];
+            if (cq != base && partner < p) continue;
+            rq = sm->rank[cq];
+          }
+          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
+          if (tt >= 0) a.d += __ldg(&wd[fb + tt]);
+          else a.bad |= kStatusXInEnv;
+        }
+      }
+      if (!quartic) continue;
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir) {  // MM2 forward and backward (Ks)
+        const uint8_t *pl = dir ? pb : pf;
+        const uint8_t *ll = dir ? lb : lf;
+        p = pl[l];
+        if (p == 255) continue;
+        for (int q = s_imm2_off[p] + lane; q < s_imm2_off[p + 1]; q += 32) {
+          const uint32_t v = s_imm2[q];
+          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
+          int rq = 0;
+          if (partner != 63) {
+            const int cq = local[ll[partner]];
+            if (cq != base && partner < p) continue;
+            rq = sm->rank[cq];
+          }
+          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
+          if (tt >= 0) a.ks += __ldg(&wk[fb + tt]);
+          else a.bad |= kStatusXInEnv;
+        }
+      }
+    }
+  }
+  return a;
+}
+
+template <bool kSparse>
 __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
@@ -732,6 +815,25 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
   off = (off + 15) & ~size_t(15);
   KmcShared *s_rep = reinterpret_cast<KmcShared *>(off);
   int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
+  // sparse tables follow the per-warp arrays
+  uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + (kSparse ? 0 : rpb * g_per * kArr));
+  uint16_t *s_ist_off = reinterpret_cast<uint16_t *>(s_pos + 4 * 12 * 136);
+  uint16_t *s_immm_off = s_ist_off + 61;
+  uint16_t *s_imm2_off = s_immm_off + 59;
+  size_t off2 = reinterpret_cast<size_t>(s_imm2_off + 59);
+  off2 = (off2 + 3) & ~size_t(3);
+  uint32_t *s_ist = reinterpret_cast<uint32_t *>(off2);
+  uint32_t *s_immm = s_ist + l.sp.n_inc_st;
+  uint32_t *s_imm2 = s_immm + l.sp.n_inc_mmm;
+  if (kSparse) {
+    StageArray(l.sp.pos, s_pos, 4 * 12 * 136);
+    StageArray(l.sp.inc_st_off, s_ist_off, 61);
+    StageArray(l.sp.inc_mmm_off, s_immm_off, 59);
+    StageArray(l.sp.inc_mm2_off, s_imm2_off, 59);
+    StageArray(l.sp.inc_st, s_ist, l.sp.n_inc_st);
+    StageArray(l.sp.inc_mmm, s_immm, l.sp.n_inc_mmm);
+    StageArray(l.sp.inc_mm2, s_imm2, l.sp.n_inc_mm2);
+  }
 
   StageArray(t.de_cl, s_de, t.n_de_cl);
   StageArray(t.mmm_cl, s_mmm, t.n_mmm_cl);
@@ -804,7 +906,37 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
       break;
     }
     // ---- phase 2: the 12 jump evaluations ----
-    if (active) {
+    if (active && kSparse) {
+      unsigned nbmask[5];
+#pragma unroll
+      for (int w = 0; w < 5; ++w) {
+        const int k = w * 32 + lane;
+        nbmask[w] = __ballot_sync(0xffffffffu, k < kLocalSites && rs.local[k] != l.sp.base_code);
+      }
+      for (int c = g; c < 12; c += g_per) {
+        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
+        const int slot = s_small->slot[mig];
+        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+        JumpAcc a{0, 0, 0, 0u};
+        if (ok)
+          a = EvalJumpSparse(t, l.sp, rs.local, nbmask, c, mig, slot, s.barrier_kind == 0, s_ist_off, s_ist,
+                             s_immm_off, s_immm, s_imm2_off, s_imm2, s_pos, s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_small,
+                             lane);
+        const long long v0 = WarpSum(a.de), v1 = WarpSum(a.d), v2 = WarpSum(a.ks);
+        bad_all |= __reduce_or_sync(0xffffffffu, a.bad);
+        if (lane == 0) {
+          if (ok) {
+            const long long *bf = l.sp.base_form + slot * 3;
+            rs.acc[c][0] = l.sp.base_de[mig] + v0;
+            rs.acc[c][1] = (s.barrier_kind == 0 ? bf[0] : bf[2]) + v1;
+            rs.acc[c][2] = bf[1] + v2;
+          }
+          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+        }
+        __syncwarp();
+      }
+    }
+    if (active && !kSparse) {
       for (int c = g; c < 12; c += g_per) {
         const uint8_t *lst = s_lst + c * kStateSites;
         for (int k = lane; k < kStateSites; k += 32) st[k] = rs.local[lst[k]];
@@ -1287,12 +1419,18 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
   return cudaGetLastError();
 }
 
-size_t KmcSharedBytes(const DevTables &t, int warps_per_replica, int replicas_per_block) {
+size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l) {
   size_t b = 4u * (t.n_de_cl + t.n_mmm_cl + t.n_mm2_cl) + sizeof(SmallTables) + 12 * kStateSites +
              3 * 12 * kEnvSites + kLocalSites * 4;
   b = (b + 15) & ~size_t(15);
-  b += sizeof(KmcShared) * replicas_per_block;
-  b += static_cast<size_t>(kArr) * warps_per_replica * replicas_per_block;
+  b += sizeof(KmcShared) * l.replicas_per_block;
+  if (l.sparse) {
+    b += 4 * 12 * 136 + 2 * (61 + 59 + 59);
+    b = (b + 3) & ~size_t(3);
+    b += 4u * (l.sp.n_inc_st + l.sp.n_inc_mmm + l.sp.n_inc_mm2);
+  } else {
+    b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
+  }
   return (b + 15) & ~size_t(15);
 }
 
@@ -1300,10 +1438,18 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
                       cudaStream_t stream) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
   const int blocks = (s.num_replicas + l.replicas_per_block - 1) / l.replicas_per_block;
-  const size_t sm = KmcSharedBytes(t, l.warps_per_replica, l.replicas_per_block);
-  cudaError_t err = cudaFuncSetAttribute(kmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
-  if (err != cudaSuccess) return err;
-  kmc_kernel<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  const size_t sm = KmcSharedBytes(t, l);
+  if (l.sparse) {
+    cudaError_t err = cudaFuncSetAttribute(kmc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(sm));
+    if (err != cudaSuccess) return err;
+    kmc_kernel<true><<<blocks, threads, sm, stream>>>(t, species, s, l);
+  } else {
+    cudaError_t err = cudaFuncSetAttribute(kmc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(sm));
+    if (err != cudaSuccess) return err;
+    kmc_kernel<false><<<blocks, threads, sm, stream>>>(t, species, s, l);
+  }
   return cudaGetLastError();
 }
 

@@ -37,6 +37,30 @@ struct KmcTraceRec {
   double ea, de, total_rate, time, energy;
 };
 
+// Tables of the sparse jump evaluation (built for one dominant "base" species):
+// every cluster sum is the all-base sum (a per-migrant constant) plus
+// corrections W[c, t_c] - W[c, base...] for the clusters incident to non-base
+// sites, each cluster attributed to its lowest-position non-base site.
+//  state incidence entry: [0,3) label [3] side (0 first, 1 second) [4,10) partner (63 = none)
+//  env incidence entry:   [0,14) feature base [14,16) mode [16,22) partner (63 = none) [22] site is first
+struct KmcSparse {
+  const uint16_t *inc_st_off;   // [61] CSR offsets by state-list position
+  const uint32_t *inc_st;
+  const uint16_t *inc_mmm_off;  // [59]
+  const uint32_t *inc_mmm;
+  const uint16_t *inc_mm2_off;  // [59]
+  const uint32_t *inc_mm2;
+  const uint8_t *pos;           // [4][12][136]: local index -> position in the state / MMM / MM2f / MM2b list, 255 none
+  const long long *f_de;        // [8][E][E][E] dE correction of one cluster, indexed (label, migrant, c1, c2)
+  const long long *base_de;     // [E] all-base dE per migrant code
+  const long long *dw_d;        // [slot][f_mmm] W - W(base block entry)
+  const long long *dw_ks;       // [slot][f_mm2]
+  const long long *dw_e0;       // [slot][f_mmm]
+  const long long *base_form;   // [slot][3] all-base sums of D, Ks (forward + backward), e0
+  int base_code;
+  int n_inc_st, n_inc_mmm, n_inc_mm2;
+};
+
 struct KmcLaunch {
   int warps_per_replica;
   int replicas_per_block;
@@ -46,6 +70,8 @@ struct KmcLaunch {
   double *events12;              // device, steps * 36 doubles, may be null
   volatile int *stop_flag;       // host-mapped, may be null
   int *status;                   // device status word (bit flags)
+  int sparse;                    // 1: sparse solute corrections, 0: dense cluster sums
+  KmcSparse sp;
 };
 
 // Status bits written by kernels.
@@ -69,7 +95,7 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
                          unsigned long long *counts, double *energy, cudaStream_t stream);
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                       cudaStream_t stream);
-size_t KmcSharedBytes(const DevTables &t, int warps_per_replica, int replicas_per_block);
+size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
 
 // Reference-batch CMC (one warp, mt19937_64 stream, batch = `batch` pairs).
 struct CmcRefArgs {

@@ -77,13 +77,14 @@ def test_barrier_errors(api, golden):
         ctx.barrier_batch([[0, 4 * n ** 3]])
 
 
-@pytest.mark.parametrize("warps", [1, 3, 12])
-def test_kmc_reference_stream(api, golden, warps):
-    """mt19937_64 stream: the event sequence equals the reference's."""
+@pytest.mark.parametrize("warps,evaluation", [(1, 0), (3, 0), (12, 0), (1, 1), (12, 1)])
+def test_kmc_reference_stream(api, golden, warps, evaluation):
+    """mt19937_64 stream: the event sequence equals the reference's (sparse and dense evaluation)."""
     G, load = golden
     fx = load("kmc_ternary")
     ctx, el, coeffs, n, sp = ctx_for(api, G, "kmc_ternary")
-    ctx.kmc_init([G.KMC_T], seed=G.KMC_SEED, rng=0, warps_per_replica=warps, replicas_per_block=1)
+    ctx.kmc_init([G.KMC_T], seed=G.KMC_SEED, rng=0, warps_per_replica=warps, replicas_per_block=1,
+                 evaluation=evaluation)
     tr, ev = ctx.kmc_run(G.KMC_STEPS, trace_replica=0, events=True)
     ref = fx["steps"]  # steps vacancy target selected Ea dE total time energy
     assert np.array_equal(tr["vacancy"], ref[:, 1].astype(np.int64))
@@ -199,3 +200,38 @@ def test_census_full_size(api, oracle_mod):
     e_ref, c_ref = oracle_mod.energy(m, lat, sp)
     assert np.array_equal(counts, c_ref)
     assert e == e_ref
+
+
+def test_sparse_equals_dense_bitwise(api):
+    """The sparse solute-correction evaluation and the dense cluster sums give
+    identical trajectories (exact int64 sums), here on concentrated lattices
+    where many clusters hold several solutes."""
+    from latticemontecarlo_gb300 import synthetic as S
+    el = ("Al", "Cu", "Mg", "Zn")
+    coeffs = S.make_coefficients(el, 21)
+    ns, sp, temps = S.batched_replicas(5, 24, n_range=(8, 11),
+                                       fractions={"Al": 0.55, "Cu": 0.15, "Mg": 0.15, "Zn": 0.15}, elements=el)
+    out = []
+    for evaluation in (0, 1):
+        ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+        ctx.set_lattices(ns, sp)
+        ctx.kmc_init(temps, seed=17, rng=1, evaluation=evaluation)
+        tr, ev = ctx.kmc_run(400, trace_replica=3, events=True)
+        out.append((ctx.get_lattices(), ctx.kmc_state(), tr, ev))
+    (l0, s0, t0, e0), (l1, s1, t1, e1) = out
+    assert np.array_equal(l0, l1)
+    for a, b in zip(s0, s1):
+        assert np.array_equal(a, b)
+    assert np.array_equal(t0, t1) and np.array_equal(e0, e1)
+
+
+def test_invalid_species_rejected(api, golden):
+    from latticemontecarlo_gb300 import LmcError
+    G, load = golden
+    el, coeffs, n, sp = G.case_inputs("pred_ternary")
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+    bad = sp.copy()
+    bad[17] = 9
+    with pytest.raises(LmcError) as e:
+        ctx.set_lattices([n], bad)
+    assert "species code out of range" in str(e.value)
