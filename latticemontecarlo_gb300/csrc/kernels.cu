@@ -698,6 +698,8 @@ struct KmcShared {
   long long ids[12];
   double beta;
   double corr;
+  int stop;
+  int pad1;
 };
 
 __device__ __forceinline__ double InterpT(const double *tt, const double *tv, int len, double time) {
@@ -796,8 +798,19 @@ __device__ __forceinline__ JumpAcc EvalJumpSparse(const DevTables &t, const KmcS
   return a;
 }
 
+// Synchronises the warps of one replica only: nothing for a single warp
+// (beyond the warp itself), a named barrier (id 1 + replica slot) otherwise,
+// so replicas sharing a block never wait for one another.
+__device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
+  if (g_per == 1) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + rl), "r"(g_per * 32) : "memory");
+  }
+}
+
 template <bool kSparse>
-__global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
+__global__ void __launch_bounds__(256, 3) kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
   const int rpb = l.replicas_per_block;
@@ -846,7 +859,6 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
   StageArray(t.local_off, s_loff, kLocalSites * 4);
   __syncthreads();
 
-  __shared__ int s_stop;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rl = warp / g_per;         // replica within block
   const int g = warp - rl * g_per;     // warp within replica
@@ -874,6 +886,7 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
     mt.idx = w + 2 * 312;
   }
   const int e = t.num_species;
+  if (!active) return;  // no block-wide barrier below this point
   for (unsigned long long it = 0; it < l.steps; ++it) {
     // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
     if (active) {
@@ -897,11 +910,11 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
           corr = s.corr_cvac[r] / cv / (1 - 13 * s.corr_csol[r]);
         }
         rs.corr = corr;
+        rs.stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
       }
     }
-    if (threadIdx.x == 0) s_stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
-    __syncthreads();
-    if (s_stop) {
+    ReplicaSync(g_per, rl);
+    if (rs.stop) {
       bad_all |= kStatusStopped;
       break;
     }
@@ -967,7 +980,7 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
         __syncwarp();
       }
     }
-    __syncthreads();
+    ReplicaSync(g_per, rl);
     // ---- phase 3: rates, selection, update (warp 0 of the replica) ----
     if (active && g == 0) {
       double ea = 0, de = 0, k = 0;
@@ -1000,9 +1013,20 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
       // total rate and prefix sums, sequential in id order (the reference's
       // single-thread reduction, KineticMcFirstOmp.cpp:55-68)
       double total = 0.0, mycum = 0.0;
-      for (int q = 0; q < 12; ++q) {
-        total += __shfl_sync(0xffffffffu, k_s, q);
-        if (lane == q) mycum = total;
+      if (s.rng_kind == 0) {
+        for (int q = 0; q < 12; ++q) {
+          total += __shfl_sync(0xffffffffu, k_s, q);
+          if (lane == q) mycum = total;
+        }
+      } else {
+        // production streams: inclusive scan in log2(16) = 4 shuffle steps
+        mycum = lane < 12 ? k_s : 0.0;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+          const double v = __shfl_up_sync(0xffffffffu, mycum, o);
+          if (lane >= o) mycum += v;
+        }
+        total = __shfl_sync(0xffffffffu, mycum, 11);
       }
       double u1 = 0, u2 = 0;
       if (lane == 0) {
@@ -1069,10 +1093,10 @@ __global__ void kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunc
       }
       vac = tgt;
     }
-    __syncthreads();
+    ReplicaSync(g_per, rl);
     if (active && g != 0) vac = rs.ids[0];
     ++steps_done;
-    __syncthreads();
+    ReplicaSync(g_per, rl);
   }
   if (active && leader) {
     s.vacancy[r] = vac;
