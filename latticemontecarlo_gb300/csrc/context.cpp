@@ -528,7 +528,7 @@ void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
       break;
     }
   *g = best;
-  *rpb = std::max(1, 8 / best);  // 256-thread blocks (the kernel's launch bounds)
+  *rpb = std::max(1, 8 / best);  // 256-thread blocks (the kernel allows up to 384)
 }
 
 }  // namespace
@@ -1113,7 +1113,7 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     if (rpb <= 0) rpb = drpb;
     Require(g == 1 || g == 2 || g == 3 || g == 4 || g == 6 || g == 12, LMC_ERR_INVALID_ARGUMENT,
             "warps_per_replica must divide 12");
-    Require(g * rpb <= 8, LMC_ERR_INVALID_ARGUMENT, "at most 8 warps per block (256 threads)");
+    Require(g * rpb <= 12, LMC_ERR_INVALID_ARGUMENT, "at most 12 warps per block (384 threads)");
     Require(g == 1 || rpb <= 15, LMC_ERR_INVALID_ARGUMENT, "at most 15 multi-warp replicas per block");
     l.warps_per_replica = g;
     l.replicas_per_block = rpb;

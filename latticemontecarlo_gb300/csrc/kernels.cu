@@ -810,7 +810,7 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
 }
 
 template <bool kSparse>
-__global__ void __launch_bounds__(256, 3) kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
+__global__ void __launch_bounds__(384, 2) kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
   const int rpb = l.replicas_per_block;
