@@ -699,7 +699,7 @@ struct KmcShared {
   double beta;
   double corr;
   int stop;
-  int pad1;
+  unsigned nbmask[5];  // non-base sites of the local neighbourhood (135 bits)
 };
 
 __device__ __forceinline__ double InterpT(const double *tt, const double *tv, int len, double time) {
@@ -798,6 +798,104 @@ __device__ __forceinline__ JumpAcc EvalJumpSparse(const DevTables &t, const KmcS
   return a;
 }
 
+// Sparse evaluation with one lane per (jump, half): lane c < 12 takes the
+// energy change and the MMM sum of jump c, lane 12 + c the MM2 forward and
+// backward sums. Each lane walks its incidence lists sequentially; returns the
+// lane's two partial sums (part 0: dE, D-or-e0; part 1: Ks, unused).
+struct LaneAcc {
+  long long a, b;
+  unsigned bad;
+};
+__device__ __forceinline__ LaneAcc EvalJumpLanes(const DevTables &t, const KmcSparse &sp, const int8_t *local,
+                                              const unsigned *nbmask, int c, int part, int mig, int slot, bool quartic,
+                                              const uint16_t *s_ist_off, const uint32_t *s_ist,
+                                              const uint16_t *s_immm_off, const uint32_t *s_immm,
+                                              const uint16_t *s_imm2_off, const uint32_t *s_imm2,
+                                              const uint8_t *s_pos, const uint8_t *s_lst, const uint8_t *s_lmmm,
+                                              const uint8_t *s_lmm2f, const uint8_t *s_lmm2b, const SmallTables *sm) {
+  long long acc_a = 0, acc_b = 0;
+  unsigned bad = 0;
+  const int e = t.num_species, x = t.x_code, base = sp.base_code;
+  const long long *__restrict__ fde = sp.f_de;
+  const long long *__restrict__ wd = (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * t.f_mmm;
+  const long long *__restrict__ wk = sp.dw_ks + static_cast<long long>(slot) * t.f_mm2;
+  const uint8_t *pA = s_pos + ((part == 0 ? 0 : 2) * 12 + c) * 136;  // state or MM2 forward
+  const uint8_t *pB = s_pos + ((part == 0 ? 1 : 3) * 12 + c) * 136;  // MMM or MM2 backward
+  const uint8_t *lA = part == 0 ? s_lst + c * kStateSites : s_lmm2f + c * kEnvSites;
+  const uint8_t *lB = part == 0 ? s_lmmm + c * kEnvSites : s_lmm2b + c * kEnvSites;
+  const uint16_t *offB = part == 0 ? s_immm_off : s_imm2_off;
+  const uint32_t *incB = part == 0 ? s_immm : s_imm2;
+  const long long *__restrict__ wB = part == 0 ? wd : wk;
+  for (int w = 0; w < 5; ++w) {
+    unsigned m = nbmask[w];
+    while (m) {
+      const int l = w * 32 + __ffs(m) - 1;
+      m &= m - 1;
+      const int code = local[l];
+      const int rp = sm->rank[code];
+      int p = pA[l];
+      if (p != 255) {
+        if (part == 0) {
+          if (code == x) bad |= kStatusBadCluster;
+          const int end = s_ist_off[p + 1];
+#pragma unroll 2
+          for (int q = s_ist_off[p]; q < end; ++q) {
+            const uint32_t v = s_ist[q];
+            const int label = v & 7, side = (v >> 3) & 1, partner = (v >> 4) & 63;
+            int c2 = 0;
+            if (partner != 63) {
+              c2 = local[lA[partner]];
+              if (c2 != base && partner < p) continue;
+            }
+            const long long f = __ldg(&fde[((label * e + mig) * e + code) * e + c2]);
+            acc_a += side ? -f : f;
+          }
+        } else if (quartic) {
+          const int end = s_imm2_off[p + 1];
+#pragma unroll 2
+          for (int q = s_imm2_off[p]; q < end; ++q) {
+            const uint32_t v = s_imm2[q];
+            const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
+            int rq = 0;
+            if (partner != 63) {
+              const int cq = local[lA[partner]];
+              if (cq != base && partner < p) continue;
+              rq = sm->rank[cq];
+            }
+            const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
+            if (tt >= 0) acc_a += __ldg(&wk[fb + tt]);
+            else bad |= kStatusXInEnv;
+          }
+        }
+      }
+      if (part == 1 && !quartic) continue;
+      p = pB[l];
+      if (p != 255) {
+        const int end = offB[p + 1];
+#pragma unroll 2
+        for (int q = offB[p]; q < end; ++q) {
+          const uint32_t v = incB[q];
+          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
+          int rq = 0;
+          if (partner != 63) {
+            const int cq = local[lB[partner]];
+            if (cq != base && partner < p) continue;
+            rq = sm->rank[cq];
+          }
+          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
+          if (tt >= 0) {
+            if (part == 0) acc_b += __ldg(&wB[fb + tt]);
+            else acc_a += __ldg(&wB[fb + tt]);
+          } else {
+            bad |= kStatusXInEnv;
+          }
+        }
+      }
+    }
+  }
+  return {acc_a, acc_b, bad};
+}
+
 // Synchronises the warps of one replica only: nothing for a single warp
 // (beyond the warp itself), a named barrier (id 1 + replica slot) otherwise,
 // so replicas sharing a block never wait for one another.
@@ -809,8 +907,11 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
   }
 }
 
-template <bool kSparse>
-__global__ void __launch_bounds__(384, 2) kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
+// kWide: blocks of up to 384 threads (12 warps per replica); otherwise up to
+// 256 threads with a register budget for 4 resident blocks per SM.
+template <bool kSparse, bool kWide>
+__global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
+    kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
   const int rpb = l.replicas_per_block;
@@ -920,13 +1021,40 @@ __global__ void __launch_bounds__(384, 2) kmc_kernel(DevTables t, int8_t *specie
     }
     // ---- phase 2: the 12 jump evaluations ----
     if (active && kSparse) {
-      unsigned nbmask[5];
 #pragma unroll
       for (int w = 0; w < 5; ++w) {
         const int k = w * 32 + lane;
-        nbmask[w] = __ballot_sync(0xffffffffu, k < kLocalSites && rs.local[k] != l.sp.base_code);
+        const unsigned mk = __ballot_sync(0xffffffffu, k < kLocalSites && rs.local[k] != l.sp.base_code);
+        if (g == 0 && lane == 0) rs.nbmask[w] = mk;
       }
-      for (int c = g; c < 12; c += g_per) {
+      ReplicaSync(g_per, rl);
+      const unsigned *nbmask = rs.nbmask;
+      if (g_per == 1) {
+        // one lane per (jump, half); lanes 24..31 idle
+        const int c = lane % 12, part = lane / 12;
+        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
+        const int slot = s_small->slot[mig];
+        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+        LaneAcc la{0, 0, 0u};
+        if (lane < 24 && ok)
+          la = EvalJumpLanes(t, l.sp, rs.local, nbmask, c, part, mig, slot, s.barrier_kind == 0, s_ist_off, s_ist,
+                             s_immm_off, s_immm, s_imm2_off, s_imm2, s_pos, s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_small);
+        const long long va = la.a, vb = la.b;
+        const unsigned bad = la.bad;
+        const long long ks = __shfl_down_sync(0xffffffffu, va, 12);
+        bad_all |= __reduce_or_sync(0xffffffffu, bad);
+        if (lane < 12) {
+          if (ok) {
+            const long long *bf = l.sp.base_form + slot * 3;
+            rs.acc[c][0] = l.sp.base_de[mig] + va;
+            rs.acc[c][1] = (s.barrier_kind == 0 ? bf[0] : bf[2]) + vb;
+            rs.acc[c][2] = bf[1] + ks;
+          }
+          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+        }
+        __syncwarp();
+      }
+      for (int c = g; g_per > 1 && c < 12; c += g_per) {
         const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
         const int slot = s_small->slot[mig];
         const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
@@ -1463,17 +1591,17 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
   const int blocks = (s.num_replicas + l.replicas_per_block - 1) / l.replicas_per_block;
   const size_t sm = KmcSharedBytes(t, l);
-  if (l.sparse) {
-    cudaError_t err = cudaFuncSetAttribute(kmc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(sm));
+  const bool wide = threads > 256;
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
     if (err != cudaSuccess) return err;
-    kmc_kernel<true><<<blocks, threads, sm, stream>>>(t, species, s, l);
-  } else {
-    cudaError_t err = cudaFuncSetAttribute(kmc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(sm));
-    if (err != cudaSuccess) return err;
-    kmc_kernel<false><<<blocks, threads, sm, stream>>>(t, species, s, l);
-  }
+    kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
+    return cudaSuccess;
+  };
+  cudaError_t err;
+  if (l.sparse) err = wide ? launch(kmc_kernel<true, true>) : launch(kmc_kernel<true, false>);
+  else err = wide ? launch(kmc_kernel<false, true>) : launch(kmc_kernel<false, false>);
+  if (err != cudaSuccess) return err;
   return cudaGetLastError();
 }
 
