@@ -398,10 +398,30 @@ void BuildSparse(lmc_ctx *c, int base) {
   c->sparse_bufs.clear();
   lmc::KmcSparse sp{};
   sp.base_code = base;
-  // state incidence: clusters with exactly one pair site, keyed by each other site
-  std::vector<std::vector<uint32_t>> by_pos(lmc::kStateSites);
-  std::vector<long long> base_de(e, 0);
-  auto w = [&](int label, int c0, int c1, int c2) { return static_cast<long long>(fm.w_de[((label * e + c0) * e + c1) * e + c2]); };
+  auto w = [&](int label, int c0, int c1, int c2) {
+    return static_cast<long long>(fm.w_de[((label * e + c0) * e + c1) * e + c2]);
+  };
+  // energy-change term of one cluster whose pair site holds M (first site) and
+  // whose other sites hold (c1, c2), base subtracted; symmetric in (c1, c2)
+  std::vector<long long> f_de(static_cast<size_t>(8) * e * e * e, 0), p_de(f_de.size(), 0);
+  auto F = [&](int label, int m, int c1, int c2) { return f_de[((label * e + m) * e + c1) * e + c2]; };
+  for (int label = 1; label < 8; ++label)
+    for (int m = 0; m < e; ++m)
+      for (int c1 = 0; c1 < e; ++c1)
+        for (int c2 = 0; c2 < e; ++c2) {
+          if (label <= 3 && c2 != 0) continue;
+          const int b2 = label <= 3 ? 0 : base;
+          f_de[((label * e + m) * e + c1) * e + c2] =
+              (w(label, m, c1, c2) - w(label, x, c1, c2)) - (w(label, m, base, b2) - w(label, x, base, b2));
+        }
+  for (int label = 4; label < 8; ++label)
+    for (int m = 0; m < e; ++m)
+      for (int c1 = 0; c1 < e; ++c1)
+        for (int c2 = 0; c2 < e; ++c2)
+          p_de[((label * e + m) * e + c1) * e + c2] = F(label, m, c1, c2) - F(label, m, c1, base) - F(label, m, base, c2);
+  // state-list clusters with exactly one pair site
+  std::vector<long long> base_de(e, 0), s_de(static_cast<size_t>(e) * lmc::kStateSites * e, 0);
+  std::vector<uint16_t> px_st(lmc::kStateSites * lmc::kStateSites, 0xFFFF);
   for (const auto &cl : pt.state_clusters) {
     int has_first = 0, has_second = 0;
     std::vector<int> others;
@@ -411,72 +431,72 @@ void BuildSparse(lmc_ctx *c, int base) {
       else others.push_back(cl.idx[q]);
     }
     if (has_first + has_second != 1 || others.empty()) continue;  // cancel when the first site is the vacancy
-    for (size_t k = 0; k < others.size(); ++k) {
-      const uint32_t partner = others.size() > 1 ? static_cast<uint32_t>(others[1 - k]) : 63u;
-      by_pos[others[k]].push_back(static_cast<uint32_t>(cl.label) | (static_cast<uint32_t>(has_second) << 3) | (partner << 4));
-    }
+    const long long sign = has_second ? -1 : 1;
     const int b2 = others.size() > 1 ? base : 0;
-    for (int m = 0; m < e; ++m) {
-      const long long v = w(cl.label, m, base, b2) - w(cl.label, x, base, b2);
-      base_de[m] += has_second ? -v : v;
+    for (int m = 0; m < e; ++m) base_de[m] += sign * (w(cl.label, m, base, b2) - w(cl.label, x, base, b2));
+    for (size_t k = 0; k < others.size(); ++k) {
+      const int p = others[k];
+      for (int m = 0; m < e; ++m)
+        for (int sp_code = 0; sp_code < e; ++sp_code)
+          s_de[(static_cast<size_t>(m) * lmc::kStateSites + p) * e + sp_code] += sign * F(cl.label, m, sp_code, b2);
+    }
+    if (others.size() == 2) {
+      const uint16_t code = static_cast<uint16_t>(cl.label | (has_second << 3));
+      for (int o = 0; o < 2; ++o) {
+        uint16_t &slot = px_st[others[o] * lmc::kStateSites + others[1 - o]];
+        if ((slot & 0xFF) == 0xFF) slot = static_cast<uint16_t>((slot & 0xFF00) | code);
+        else if ((slot >> 8) == 0xFF) slot = static_cast<uint16_t>((slot & 0x00FF) | (code << 8));
+        else Require(false, LMC_ERR_UNSUPPORTED, "more than two triplets share a site pair");
+      }
     }
   }
-  std::vector<uint16_t> st_off(lmc::kStateSites + 1, 0);
-  std::vector<uint32_t> st_inc;
-  for (int p = 0; p < lmc::kStateSites; ++p) {
-    st_off[p] = static_cast<uint16_t>(st_inc.size());
-    st_inc.insert(st_inc.end(), by_pos[p].begin(), by_pos[p].end());
-  }
-  st_off[lmc::kStateSites] = static_cast<uint16_t>(st_inc.size());
-  // dE correction per (label, migrant, c1, c2): f = (W(M, c1, c2) - W(X, c1, c2)) - (same at base)
-  std::vector<long long> f_de(static_cast<size_t>(8) * e * e * e, 0);
-  for (int label = 1; label < 8; ++label)
-    for (int m = 0; m < e; ++m)
-      for (int c1 = 0; c1 < e; ++c1)
-        for (int c2 = 0; c2 < e; ++c2) {
-          const int b2 = label <= 3 ? 0 : base;
-          if (label <= 3 && c2 != 0) continue;
-          f_de[((label * e + m) * e + c1) * e + c2] =
-              (w(label, m, c1, c2) - w(label, x, c1, c2)) - (w(label, m, base, b2) - w(label, x, base, b2));
-        }
-  // environment incidence and W - W(base) tables
-  auto env_inc = [&](const lmc::EnvEncoding &enc, std::vector<uint16_t> &off, std::vector<uint32_t> &inc) {
+  // environment lists: W - W(base block entry) per feature, single-site terms, pair lookup
+  const int slots = static_cast<int>(fm.slot_code.size());
+  std::vector<long long> dwd, dwks, dwe0, base_form(3 * std::max(1, slots), 0);
+  std::vector<long long> s_env(static_cast<size_t>(std::max(1, slots)) * 3 * lmc::kEnvSites * 8, 0);
+  std::vector<uint32_t> px_env(2 * lmc::kEnvSites * lmc::kEnvSites, 0xFFFFFFFFu);
+  auto env_tables = [&](const lmc::EnvEncoding &enc, int which) {
     const auto ooff = enc.OrbitOffsets(eh);
-    std::vector<std::vector<uint32_t>> bp(lmc::kEnvSites);
+    Require(ooff.back() < (1 << 20), LMC_ERR_UNSUPPORTED, "too many environment features");
     for (const auto &cl : enc.clusters) {
-      const uint32_t fb = static_cast<uint32_t>(ooff[cl.orbit]);
-      const uint32_t mode = static_cast<uint32_t>(cl.mode);
-      const uint32_t pb = cl.b < 0 ? 63u : static_cast<uint32_t>(cl.b);
-      bp[cl.a].push_back(fb | (mode << 14) | (pb << 16) | (1u << 22));
-      if (cl.b >= 0) bp[cl.b].push_back(fb | (mode << 14) | (static_cast<uint32_t>(cl.a) << 16));
+      if (cl.b < 0) continue;
+      const uint32_t v = static_cast<uint32_t>(ooff[cl.orbit]) | (static_cast<uint32_t>(cl.mode) << 20);
+      uint32_t &ab = px_env[(which * lmc::kEnvSites + cl.a) * lmc::kEnvSites + cl.b];
+      uint32_t &ba = px_env[(which * lmc::kEnvSites + cl.b) * lmc::kEnvSites + cl.a];
+      Require(ab == 0xFFFFFFFFu && ba == 0xFFFFFFFFu, LMC_ERR_UNSUPPORTED, "two clusters share a site pair");
+      ab = v | (1u << 22);
+      ba = v;
     }
-    off.assign(lmc::kEnvSites + 1, 0);
-    inc.clear();
-    for (int p = 0; p < lmc::kEnvSites; ++p) {
-      off[p] = static_cast<uint16_t>(inc.size());
-      inc.insert(inc.end(), bp[p].begin(), bp[p].end());
-    }
-    off[lmc::kEnvSites] = static_cast<uint16_t>(inc.size());
+    return ooff;
   };
-  std::vector<uint16_t> mmm_off, mm2_off;
-  std::vector<uint32_t> mmm_inc, mm2_inc;
-  env_inc(pt.mmm, mmm_off, mmm_inc);
-  env_inc(pt.mm2, mm2_off, mm2_inc);
-  auto delta = [&](const lmc::EnvEncoding &enc, const std::vector<int64_t> &wv, std::vector<long long> &out,
-                   long long *base_sum, int mult) {
-    const auto ooff = enc.OrbitOffsets(eh);
+  const auto off_mmm = env_tables(pt.mmm, 0);
+  const auto off_mm2 = env_tables(pt.mm2, 1);
+  auto delta = [&](const lmc::EnvEncoding &enc, const std::vector<int> &ooff, const std::vector<int64_t> &wv,
+                   std::vector<long long> &out, long long *base_sum, int mult, long long *single) {
+    const size_t first = out.size();
     for (size_t o = 0; o < enc.orbits.size(); ++o) {
       const long long w0 = wv[ooff[o] + lmc::PairType(enc.orbits[o].mode, rb0, rb0, eh)];
       for (int j = ooff[o]; j < ooff[o + 1]; ++j) out.push_back(wv[j] - w0);
       *base_sum += static_cast<long long>(mult) * w0 * enc.orbits[o].size;
     }
+    const long long *dw = out.data() + first;
+    for (const auto &cl : enc.clusters) {
+      const int fb = ooff[cl.orbit];
+      for (int r = 0; r < eh; ++r) {
+        if (cl.b < 0) {
+          single[cl.a * 8 + r] += dw[fb + lmc::PairType(0, r, 0, eh)];
+        } else {
+          single[cl.a * 8 + r] += dw[fb + lmc::PairType(cl.mode, r, rb0, eh)];
+          single[cl.b * 8 + r] += dw[fb + lmc::PairType(cl.mode, rb0, r, eh)];
+        }
+      }
+    }
   };
-  const int slots = static_cast<int>(fm.slot_code.size());
-  std::vector<long long> dwd, dwks, dwe0, base_form(3 * std::max(1, slots), 0);
   for (int sidx = 0; sidx < slots; ++sidx) {
-    delta(pt.mmm, fm.quartic_d[sidx].w, dwd, &base_form[sidx * 3 + 0], 1);
-    delta(pt.mm2, fm.quartic_ks[sidx].w, dwks, &base_form[sidx * 3 + 1], 2);
-    delta(pt.mmm, fm.e0[sidx].w, dwe0, &base_form[sidx * 3 + 2], 1);
+    long long *sg = s_env.data() + static_cast<size_t>(sidx) * 3 * lmc::kEnvSites * 8;
+    delta(pt.mmm, off_mmm, fm.quartic_d[sidx].w, dwd, &base_form[sidx * 3 + 0], 1, sg);
+    delta(pt.mm2, off_mm2, fm.quartic_ks[sidx].w, dwks, &base_form[sidx * 3 + 1], 2, sg + lmc::kEnvSites * 8);
+    delta(pt.mmm, off_mmm, fm.e0[sidx].w, dwe0, &base_form[sidx * 3 + 2], 1, sg + 2 * lmc::kEnvSites * 8);
   }
   // local index -> list position for each jump
   std::vector<uint8_t> pos(4 * 12 * 136, 255);
@@ -496,22 +516,18 @@ void BuildSparse(lmc_ctx *c, int base) {
     }
   }
   auto &B = c->sparse_bufs;
-  sp.inc_st_off = c->Upload(st_off, &B);
-  sp.inc_st = c->Upload(st_inc, &B);
-  sp.inc_mmm_off = c->Upload(mmm_off, &B);
-  sp.inc_mmm = c->Upload(mmm_inc, &B);
-  sp.inc_mm2_off = c->Upload(mm2_off, &B);
-  sp.inc_mm2 = c->Upload(mm2_inc, &B);
   sp.pos = c->Upload(pos, &B);
-  sp.f_de = c->Upload(f_de, &B);
+  sp.s_de = c->Upload(s_de, &B);
+  sp.s_env = c->Upload(s_env, &B);
+  sp.px_st = c->Upload(px_st, &B);
+  sp.px_env = c->Upload(px_env, &B);
+  sp.p_de = c->Upload(p_de, &B);
   sp.base_de = c->Upload(base_de, &B);
   sp.dw_d = c->Upload(dwd, &B);
   sp.dw_ks = c->Upload(dwks, &B);
   sp.dw_e0 = c->Upload(dwe0, &B);
   sp.base_form = c->Upload(base_form, &B);
-  sp.n_inc_st = static_cast<int>(st_inc.size());
-  sp.n_inc_mmm = static_cast<int>(mmm_inc.size());
-  sp.n_inc_mm2 = static_cast<int>(mm2_inc.size());
+  sp.center = l_st[pt.pos_first];
   c->sparse = sp;
 }
 

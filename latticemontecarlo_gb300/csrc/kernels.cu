@@ -699,7 +699,9 @@ struct KmcShared {
   double beta;
   double corr;
   int stop;
-  unsigned nbmask[5];  // non-base sites of the local neighbourhood (135 bits)
+  int nbk;                          // non-base sites in the neighbourhood (sparse evaluation)
+  uint8_t nb_l[kMaxSparseSites];    // their local indices
+  int8_t nb_code[kMaxSparseSites];  // and species
 };
 
 __device__ __forceinline__ double InterpT(const double *tt, const double *tv, int len, double time) {
@@ -716,180 +718,87 @@ __device__ __forceinline__ double InterpT(const double *tt, const double *tv, in
   return ly + ((time - lx) / (ux - lx)) * (uy - ly);
 }
 
-// Sparse evaluation of jump c (see KmcSparse): per-lane partial corrections.
-__device__ __forceinline__ JumpAcc EvalJumpSparse(const DevTables &t, const KmcSparse &sp, const int8_t *local,
-                                                  const unsigned *nbmask, int c, int mig, int slot, bool quartic,
-                                                  const uint16_t *s_ist_off, const uint32_t *s_ist,
-                                                  const uint16_t *s_immm_off, const uint32_t *s_immm,
-                                                  const uint16_t *s_imm2_off, const uint32_t *s_imm2,
-                                                  const uint8_t *s_pos, const uint8_t *s_lst, const uint8_t *s_lmmm,
-                                                  const uint8_t *s_lmm2f, const uint8_t *s_lmm2b,
-                                                  const SmallTables *sm, int lane) {
-  JumpAcc a{0, 0, 0, 0u};
-  const int e = t.num_species, x = t.x_code, base = sp.base_code;
-  const uint8_t *pst = s_pos + (0 * 12 + c) * 136, *pmm = s_pos + (1 * 12 + c) * 136;
-  const uint8_t *pf = s_pos + (2 * 12 + c) * 136, *pb = s_pos + (3 * 12 + c) * 136;
-  const uint8_t *lst = s_lst + c * kStateSites, *lmm = s_lmmm + c * kEnvSites;
-  const uint8_t *lf = s_lmm2f + c * kEnvSites, *lb = s_lmm2b + c * kEnvSites;
-  const long long *__restrict__ fde = sp.f_de;
-  const long long *__restrict__ wd = (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * t.f_mmm;
-  const long long *__restrict__ wk = sp.dw_ks + static_cast<long long>(slot) * t.f_mm2;
-  for (int w = 0; w < 5; ++w) {
-    unsigned m = nbmask[w];
-    while (m) {
-      const int l = w * 32 + __ffs(m) - 1;
-      m &= m - 1;
-      const int code = local[l];
-      const int rp = sm->rank[code];
-      int p = pst[l];
-      if (p != 255) {  // energy change: clusters with one pair site, l among the others
-        if (code == x) a.bad |= kStatusBadCluster;
-        for (int q = s_ist_off[p] + lane; q < s_ist_off[p + 1]; q += 32) {
-          const uint32_t v = s_ist[q];
-          const int label = v & 7, side = (v >> 3) & 1, partner = (v >> 4) & 63;
-          int c2 = 0;
-          if (partner != 63) {
-            c2 = local[lst[partner]];
-            if (c2 != base && partner < p) continue;  // counted at the partner
-          }
-          const long long f = __ldg(&fde[((label * e + mig) * e + code) * e + c2]);
-          a.de += side ? -f : f;
-        }
-      }
-      p = pmm[l];
-      if (p != 255) {  // MMM (D or e0)
-        for (int q = s_immm_off[p] + lane; q < s_immm_off[p + 1]; q += 32) {
-          const uint32_t v = s_immm[q];
-          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
-          int rq = 0;
-          if (partner != 63) {
-            const int cq = local[lmm[partner]];
-            if (cq != base && partner < p) continue;
-            rq = sm->rank[cq];
-          }
-          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
-          if (tt >= 0) a.d += __ldg(&wd[fb + tt]);
-          else a.bad |= kStatusXInEnv;
-        }
-      }
-      if (!quartic) continue;
-#pragma unroll
-      for (int dir = 0; dir < 2; ++dir) {  // MM2 forward and backward (Ks)
-        const uint8_t *pl = dir ? pb : pf;
-        const uint8_t *ll = dir ? lb : lf;
-        p = pl[l];
-        if (p == 255) continue;
-        for (int q = s_imm2_off[p] + lane; q < s_imm2_off[p + 1]; q += 32) {
-          const uint32_t v = s_imm2[q];
-          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
-          int rq = 0;
-          if (partner != 63) {
-            const int cq = local[ll[partner]];
-            if (cq != base && partner < p) continue;
-            rq = sm->rank[cq];
-          }
-          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
-          if (tt >= 0) a.ks += __ldg(&wk[fb + tt]);
-          else a.bad |= kStatusXInEnv;
-        }
-      }
-    }
-  }
-  return a;
+// Pair term of one environment pair cluster (see KmcSparse): the cluster's
+// entry minus the two entries with one site at the base species.
+__device__ __forceinline__ long long EnvPairTerm(uint32_t v, const long long *__restrict__ w, int rp, int rq, int rb0,
+                                                 const int8_t *pt) {
+  const int fb = v & 0xFFFFF, mode = (v >> 20) & 3;
+  const bool first = (v >> 22) & 1;
+  const int ra = first ? rp : rq, rb = first ? rq : rp;
+  if (ra == kMaxOnehot - 1 || rb == kMaxOnehot - 1) return 0;  // flagged by the single-site terms
+  const int8_t *row = pt + mode * 64;
+  return __ldg(&w[fb + row[ra * 8 + rb]]) - __ldg(&w[fb + row[ra * 8 + rb0]]) - __ldg(&w[fb + row[rb0 * 8 + rb]]);
 }
 
-// Sparse evaluation with one lane per (jump, half): lane c < 12 takes the
-// energy change and the MMM sum of jump c, lane 12 + c the MM2 forward and
-// backward sums. Each lane walks its incidence lists sequentially; returns the
-// lane's two partial sums (part 0: dE, D-or-e0; part 1: Ks, unused).
 struct LaneAcc {
   long long a, b;
   unsigned bad;
 };
-__device__ __forceinline__ LaneAcc EvalJumpLanes(const DevTables &t, const KmcSparse &sp, const int8_t *local,
-                                              const unsigned *nbmask, int c, int part, int mig, int slot, bool quartic,
-                                              const uint16_t *s_ist_off, const uint32_t *s_ist,
-                                              const uint16_t *s_immm_off, const uint32_t *s_immm,
-                                              const uint16_t *s_imm2_off, const uint32_t *s_imm2,
-                                              const uint8_t *s_pos, const uint8_t *s_lst, const uint8_t *s_lmmm,
-                                              const uint8_t *s_lmm2f, const uint8_t *s_lmm2b, const SmallTables *sm) {
+
+// Sparse evaluation of one half of jump c over the replica's non-base sites
+// (nb_l local indices, nb_code species, k of them). Part 0 sums the energy
+// change (list A = state) and the D or e0 form (list B = MMM); part 1 sums the
+// Ks form over MM2 forward (A) and backward (B). Returns the corrections to
+// the all-base constants.
+__device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint8_t *s_pos, const uint16_t *s_pxst,
+                                                 const uint32_t *s_pxenv, const SmallTables *sm, const uint8_t *nb_l,
+                                                 const int8_t *nb_code, int k_sites, int e, int x, int f_mmm,
+                                                 int f_mm2, int c, int part, int mig, int slot, bool quartic) {
   long long acc_a = 0, acc_b = 0;
   unsigned bad = 0;
-  const int e = t.num_species, x = t.x_code, base = sp.base_code;
-  const long long *__restrict__ fde = sp.f_de;
-  const long long *__restrict__ wd = (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * t.f_mmm;
-  const long long *__restrict__ wk = sp.dw_ks + static_cast<long long>(slot) * t.f_mm2;
-  const uint8_t *pA = s_pos + ((part == 0 ? 0 : 2) * 12 + c) * 136;  // state or MM2 forward
-  const uint8_t *pB = s_pos + ((part == 0 ? 1 : 3) * 12 + c) * 136;  // MMM or MM2 backward
-  const uint8_t *lA = part == 0 ? s_lst + c * kStateSites : s_lmm2f + c * kEnvSites;
-  const uint8_t *lB = part == 0 ? s_lmmm + c * kEnvSites : s_lmm2b + c * kEnvSites;
-  const uint16_t *offB = part == 0 ? s_immm_off : s_imm2_off;
-  const uint32_t *incB = part == 0 ? s_immm : s_imm2;
-  const long long *__restrict__ wB = part == 0 ? wd : wk;
-  for (int w = 0; w < 5; ++w) {
-    unsigned m = nbmask[w];
-    while (m) {
-      const int l = w * 32 + __ffs(m) - 1;
-      m &= m - 1;
-      const int code = local[l];
-      const int rp = sm->rank[code];
-      int p = pA[l];
-      if (p != 255) {
+  const int rb0 = sm->rank[sp.base_code];
+  const uint8_t *pos_a = s_pos + ((part == 0 ? 0 : 2) * 12 + c) * 136;
+  const uint8_t *pos_b = s_pos + ((part == 0 ? 1 : 3) * 12 + c) * 136;
+  const long long *__restrict__ sg_a =
+      part == 0 ? sp.s_de + mig * kStateSites * e : sp.s_env + (slot * 3 + 1) * kEnvSites * 8;
+  const long long *__restrict__ sg_b = sp.s_env + (slot * 3 + (part == 1 ? 1 : (quartic ? 0 : 2))) * kEnvSites * 8;
+  const long long *__restrict__ w_a = sp.dw_ks + static_cast<long long>(slot) * f_mm2;
+  const long long *__restrict__ w_b =
+      part == 1 ? w_a : (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * f_mmm;
+  const uint32_t *px_a = s_pxenv + kEnvSites * kEnvSites;
+  const uint32_t *px_b = s_pxenv + (part == 1 ? kEnvSites * kEnvSites : 0);
+  const long long *__restrict__ pde = sp.p_de + mig * e * e;
+  for (int k = 0; k < k_sites; ++k) {
+    const int l = nb_l[k], code = nb_code[k];
+    const int rp = sm->rank[code];
+    const int pa = pos_a[l], pb = pos_b[l];
+    if (pa != 255) {
+      if (part == 0) {
+        if (code == x) bad |= kStatusBadCluster;
+        acc_a += __ldg(&sg_a[pa * e + code]);
+      } else {
+        if (rp == kMaxOnehot - 1) bad |= kStatusXInEnv;
+        acc_a += __ldg(&sg_a[pa * 8 + rp]);
+      }
+    }
+    if (pb != 255) {
+      if (rp == kMaxOnehot - 1) bad |= kStatusXInEnv;
+      acc_b += __ldg(&sg_b[pb * 8 + rp]);
+    }
+    for (int k2 = 0; k2 < k; ++k2) {
+      const int l2 = nb_l[k2];
+      const int qa = pos_a[l2], qb = pos_b[l2];
+      if (pa != 255 && qa != 255) {
         if (part == 0) {
-          if (code == x) bad |= kStatusBadCluster;
-          const int end = s_ist_off[p + 1];
-#pragma unroll 2
-          for (int q = s_ist_off[p]; q < end; ++q) {
-            const uint32_t v = s_ist[q];
-            const int label = v & 7, side = (v >> 3) & 1, partner = (v >> 4) & 63;
-            int c2 = 0;
-            if (partner != 63) {
-              c2 = local[lA[partner]];
-              if (c2 != base && partner < p) continue;
+          const unsigned v = s_pxst[pa * kStateSites + qa];
+          if (v != 0xFFFFu) {
+            const int c2 = nb_code[k2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const unsigned t3 = (v >> (8 * h)) & 0xFF;
+              if (t3 == 0xFF) continue;
+              const long long f = __ldg(&pde[(((t3 & 7) * e * e) * e) + code * e + c2]);
+              acc_a += (t3 & 8) ? -f : f;
             }
-            const long long f = __ldg(&fde[((label * e + mig) * e + code) * e + c2]);
-            acc_a += side ? -f : f;
           }
-        } else if (quartic) {
-          const int end = s_imm2_off[p + 1];
-#pragma unroll 2
-          for (int q = s_imm2_off[p]; q < end; ++q) {
-            const uint32_t v = s_imm2[q];
-            const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
-            int rq = 0;
-            if (partner != 63) {
-              const int cq = local[lA[partner]];
-              if (cq != base && partner < p) continue;
-              rq = sm->rank[cq];
-            }
-            const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
-            if (tt >= 0) acc_a += __ldg(&wk[fb + tt]);
-            else bad |= kStatusXInEnv;
-          }
+        } else {
+          const uint32_t v = px_a[pa * kEnvSites + qa];
+          if (v != 0xFFFFFFFFu) acc_a += EnvPairTerm(v, w_a, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
         }
       }
-      if (part == 1 && !quartic) continue;
-      p = pB[l];
-      if (p != 255) {
-        const int end = offB[p + 1];
-#pragma unroll 2
-        for (int q = offB[p]; q < end; ++q) {
-          const uint32_t v = incB[q];
-          const int fb = v & 0x3FFF, mode = (v >> 14) & 3, partner = (v >> 16) & 63, first = (v >> 22) & 1;
-          int rq = 0;
-          if (partner != 63) {
-            const int cq = local[lB[partner]];
-            if (cq != base && partner < p) continue;
-            rq = sm->rank[cq];
-          }
-          const int tt = first ? sm->pairtype[(mode * 8 + rp) * 8 + rq] : sm->pairtype[(mode * 8 + rq) * 8 + rp];
-          if (tt >= 0) {
-            if (part == 0) acc_b += __ldg(&wB[fb + tt]);
-            else acc_a += __ldg(&wB[fb + tt]);
-          } else {
-            bad |= kStatusXInEnv;
-          }
-        }
+      if (pb != 255 && qb != 255) {
+        const uint32_t v = px_b[pb * kEnvSites + qb];
+        if (v != 0xFFFFFFFFu) acc_b += EnvPairTerm(v, w_b, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
       }
     }
   }
@@ -930,23 +839,13 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
   KmcShared *s_rep = reinterpret_cast<KmcShared *>(off);
   int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
   // sparse tables follow the per-warp arrays
-  uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + (kSparse ? 0 : rpb * g_per * kArr));
-  uint16_t *s_ist_off = reinterpret_cast<uint16_t *>(s_pos + 4 * 12 * 136);
-  uint16_t *s_immm_off = s_ist_off + 61;
-  uint16_t *s_imm2_off = s_immm_off + 59;
-  size_t off2 = reinterpret_cast<size_t>(s_imm2_off + 59);
-  off2 = (off2 + 3) & ~size_t(3);
-  uint32_t *s_ist = reinterpret_cast<uint32_t *>(off2);
-  uint32_t *s_immm = s_ist + l.sp.n_inc_st;
-  uint32_t *s_imm2 = s_immm + l.sp.n_inc_mmm;
+  uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + rpb * g_per * kArr);        // [4][12][136]
+  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_pos + 4 * 12 * 136);          // [60][60]
+  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pxst + kStateSites * kStateSites);  // [2][58][58]
   if (kSparse) {
     StageArray(l.sp.pos, s_pos, 4 * 12 * 136);
-    StageArray(l.sp.inc_st_off, s_ist_off, 61);
-    StageArray(l.sp.inc_mmm_off, s_immm_off, 59);
-    StageArray(l.sp.inc_mm2_off, s_imm2_off, 59);
-    StageArray(l.sp.inc_st, s_ist, l.sp.n_inc_st);
-    StageArray(l.sp.inc_mmm, s_immm, l.sp.n_inc_mmm);
-    StageArray(l.sp.inc_mm2, s_imm2, l.sp.n_inc_mm2);
+    StageArray(l.sp.px_st, s_pxst, kStateSites * kStateSites);
+    StageArray(l.sp.px_env, s_pxenv, 2 * kEnvSites * kEnvSites);
   }
 
   StageArray(t.de_cl, s_de, t.n_de_cl);
@@ -1020,64 +919,55 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
       break;
     }
     // ---- phase 2: the 12 jump evaluations ----
-    if (active && kSparse) {
+    if (kSparse) {
+      // list the non-base sites of the neighbourhood (warp 0)
+      if (g == 0) {
+        int k_sites = 0;
 #pragma unroll
-      for (int w = 0; w < 5; ++w) {
-        const int k = w * 32 + lane;
-        const unsigned mk = __ballot_sync(0xffffffffu, k < kLocalSites && rs.local[k] != l.sp.base_code);
-        if (g == 0 && lane == 0) rs.nbmask[w] = mk;
+        for (int w = 0; w < 5; ++w) {
+          const int k = w * 32 + lane;
+          const int code = k < kLocalSites ? rs.local[k] : l.sp.base_code;
+          const bool nb = code != l.sp.base_code && k != l.sp.center;
+          const unsigned mk = __ballot_sync(0xffffffffu, nb);
+          const int idx = k_sites + __popc(mk & ((1u << lane) - 1u));
+          if (nb && idx < kMaxSparseSites) {
+            rs.nb_l[idx] = static_cast<uint8_t>(k);
+            rs.nb_code[idx] = static_cast<int8_t>(code);
+          }
+          k_sites += __popc(mk);
+        }
+        if (lane == 0) rs.nbk = k_sites;
       }
       ReplicaSync(g_per, rl);
-      const unsigned *nbmask = rs.nbmask;
-      if (g_per == 1) {
-        // one lane per (jump, half); lanes 24..31 idle
-        const int c = lane % 12, part = lane / 12;
-        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
-        const int slot = s_small->slot[mig];
-        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
-        LaneAcc la{0, 0, 0u};
-        if (lane < 24 && ok)
-          la = EvalJumpLanes(t, l.sp, rs.local, nbmask, c, part, mig, slot, s.barrier_kind == 0, s_ist_off, s_ist,
-                             s_immm_off, s_immm, s_imm2_off, s_imm2, s_pos, s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_small);
-        const long long va = la.a, vb = la.b;
-        const unsigned bad = la.bad;
-        const long long ks = __shfl_down_sync(0xffffffffu, va, 12);
-        bad_all |= __reduce_or_sync(0xffffffffu, bad);
-        if (lane < 12) {
-          if (ok) {
-            const long long *bf = l.sp.base_form + slot * 3;
-            rs.acc[c][0] = l.sp.base_de[mig] + va;
-            rs.acc[c][1] = (s.barrier_kind == 0 ? bf[0] : bf[2]) + vb;
-            rs.acc[c][2] = bf[1] + ks;
-          }
-          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
-        }
-        __syncwarp();
-      }
-      for (int c = g; g_per > 1 && c < 12; c += g_per) {
-        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
-        const int slot = s_small->slot[mig];
-        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
-        JumpAcc a{0, 0, 0, 0u};
-        if (ok)
-          a = EvalJumpSparse(t, l.sp, rs.local, nbmask, c, mig, slot, s.barrier_kind == 0, s_ist_off, s_ist,
-                             s_immm_off, s_immm, s_imm2_off, s_imm2, s_pos, s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_small,
-                             lane);
-        const long long v0 = WarpSum(a.de), v1 = WarpSum(a.d), v2 = WarpSum(a.ks);
-        bad_all |= __reduce_or_sync(0xffffffffu, a.bad);
-        if (lane == 0) {
-          if (ok) {
-            const long long *bf = l.sp.base_form + slot * 3;
-            rs.acc[c][0] = l.sp.base_de[mig] + v0;
-            rs.acc[c][1] = (s.barrier_kind == 0 ? bf[0] : bf[2]) + v1;
-            rs.acc[c][2] = bf[1] + v2;
-          }
-          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
-        }
-        __syncwarp();
-      }
     }
-    if (active && !kSparse) {
+    const bool sparse_step = kSparse && rs.nbk <= kMaxSparseSites;
+    if (sparse_step) {
+      // one lane per (jump, half): item = lane * G + g, items 0..23
+      const int item = lane * g_per + g;
+      const int c = item % 12, part = item / 12;
+      LaneAcc la{0, 0, 0u};
+      if (item < 24) {
+        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
+        const int slot = s_small->slot[mig];
+        const bool quartic = s.barrier_kind == 0;
+        const bool ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+        if (ok && (part == 0 || quartic))
+          la = EvalJumpPairs(l.sp, s_pos, s_pxst, s_pxenv, s_small, rs.nb_l, rs.nb_code, rs.nbk, e, t.x_code,
+                             t.f_mmm, t.f_mm2, c, part, mig, slot, quartic);
+        if (ok) {
+          const long long *bf = l.sp.base_form + slot * 3;
+          if (part == 0) {
+            rs.acc[c][0] = l.sp.base_de[mig] + la.a;
+            rs.acc[c][1] = (quartic ? bf[0] : bf[2]) + la.b;
+          } else {
+            rs.acc[c][2] = bf[1] + la.a + la.b;
+          }
+        }
+        if (part == 0) rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+      }
+      bad_all |= __reduce_or_sync(0xffffffffu, la.bad);
+    }
+    if (!sparse_step) {
       for (int c = g; c < 12; c += g_per) {
         const uint8_t *lst = s_lst + c * kStateSites;
         for (int k = lane; k < kStateSites; k += 32) st[k] = rs.local[lst[k]];
@@ -1576,13 +1466,8 @@ size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l) {
              3 * 12 * kEnvSites + kLocalSites * 4;
   b = (b + 15) & ~size_t(15);
   b += sizeof(KmcShared) * l.replicas_per_block;
-  if (l.sparse) {
-    b += 4 * 12 * 136 + 2 * (61 + 59 + 59);
-    b = (b + 3) & ~size_t(3);
-    b += 4u * (l.sp.n_inc_st + l.sp.n_inc_mmm + l.sp.n_inc_mm2);
-  } else {
-    b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
-  }
+  b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
+  if (l.sparse) b += 4 * 12 * 136 + 2 * kStateSites * kStateSites + 4 * 2 * kEnvSites * kEnvSites;
   return (b + 15) & ~size_t(15);
 }
 

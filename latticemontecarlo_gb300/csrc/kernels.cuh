@@ -37,28 +37,31 @@ struct KmcTraceRec {
   double ea, de, total_rate, time, energy;
 };
 
-// Tables of the sparse jump evaluation (built for one dominant "base" species):
-// every cluster sum is the all-base sum (a per-migrant constant) plus
-// corrections W[c, t_c] - W[c, base...] for the clusters incident to non-base
-// sites, each cluster attributed to its lowest-position non-base site.
-//  state incidence entry: [0,3) label [3] side (0 first, 1 second) [4,10) partner (63 = none)
-//  env incidence entry:   [0,14) feature base [14,16) mode [16,22) partner (63 = none) [22] site is first
+// Tables of the sparse jump evaluation, built for one dominant "base" species b.
+// With all non-pair sites at b a jump's sums are per-migrant constants. Any
+// cluster holds at most two sites other than the pair sites, so by
+// inclusion-exclusion the exact sums are
+//   constant + sum over non-base sites p of S[list][p][species(p)]
+//            + sum over non-base pairs (p, q) sharing a cluster of a pair term,
+// all in the same int64 fixed point as the dense evaluation (bit-identical,
+// since wrapping integer sums do not depend on their order).
+// Lists: 0 state (energy change), 1 MMM, 2 MM2 forward, 3 MM2 backward.
+constexpr int kMaxSparseSites = 32;  // more non-base neighbourhood sites: dense evaluation for that step
 struct KmcSparse {
-  const uint16_t *inc_st_off;   // [61] CSR offsets by state-list position
-  const uint32_t *inc_st;
-  const uint16_t *inc_mmm_off;  // [59]
-  const uint32_t *inc_mmm;
-  const uint16_t *inc_mm2_off;  // [59]
-  const uint32_t *inc_mm2;
-  const uint8_t *pos;           // [4][12][136]: local index -> position in the state / MMM / MM2f / MM2b list, 255 none
-  const long long *f_de;        // [8][E][E][E] dE correction of one cluster, indexed (label, migrant, c1, c2)
-  const long long *base_de;     // [E] all-base dE per migrant code
-  const long long *dw_d;        // [slot][f_mmm] W - W(base block entry)
-  const long long *dw_ks;       // [slot][f_mm2]
-  const long long *dw_e0;       // [slot][f_mmm]
-  const long long *base_form;   // [slot][3] all-base sums of D, Ks (forward + backward), e0
+  const uint8_t *pos;      // [4][12][136]: local index -> position in list of jump c, 255 none
+  const long long *s_de;   // [E migrant][60][E species]: single-site energy-change terms
+  const long long *s_env;  // [slot][3 forms: D, Ks, e0][58][8 ranks]: single-site feature terms
+  const uint16_t *px_st;   // [60][60]: up to two triplets sharing the sites, (label | side << 3) per byte, 0xFF none
+  const uint32_t *px_env;  // [2: MMM, MM2][58][58]: feature base | mode << 20 | (row site is the cluster's
+                           // first) << 22 of the pair cluster, ~0 none
+  const long long *p_de;   // [8][E][E][E]: pair term of a triplet, F(c1, c2) - F(c1, b) - F(b, c2)
+  const long long *base_de;    // [E] all-base energy change per migrant code
+  const long long *dw_d;       // [slot][f_mmm] W - W(block entry of the base pair type)
+  const long long *dw_ks;      // [slot][f_mm2]
+  const long long *dw_e0;      // [slot][f_mmm]
+  const long long *base_form;  // [slot][3] all-base sums of D, Ks (forward + backward), e0
   int base_code;
-  int n_inc_st, n_inc_mmm, n_inc_mm2;
+  int center;  // local index of the vacancy site
 };
 
 struct KmcLaunch {

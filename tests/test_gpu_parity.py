@@ -202,20 +202,25 @@ def test_census_full_size(api, oracle_mod):
     assert e == e_ref
 
 
-def test_sparse_equals_dense_bitwise(api):
-    """The sparse solute-correction evaluation and the dense cluster sums give
-    identical trajectories (exact int64 sums), here on concentrated lattices
-    where many clusters hold several solutes."""
+@pytest.mark.parametrize("base_fraction,warps", [(0.96, 1), (0.85, 1), (0.85, 2), (0.78, 1), (0.55, 1)])
+def test_sparse_equals_dense_bitwise(api, base_fraction, warps):
+    """The sparse evaluation (single-site plus pair corrections to the all-base
+    sums) and the dense cluster sums give identical trajectories (exact int64
+    sums). At 0.85 most clusters near a solute hold several solutes; near 0.78
+    the neighbourhood's solute count crosses the sparse limit from step to step
+    (both paths in one trajectory); at 0.55 every step takes the dense path."""
     from latticemontecarlo_gb300 import synthetic as S
     el = ("Al", "Cu", "Mg", "Zn")
     coeffs = S.make_coefficients(el, 21)
+    rest = (1.0 - base_fraction) / 3
     ns, sp, temps = S.batched_replicas(5, 24, n_range=(8, 11),
-                                       fractions={"Al": 0.55, "Cu": 0.15, "Mg": 0.15, "Zn": 0.15}, elements=el)
+                                       fractions={"Al": base_fraction, "Cu": rest, "Mg": rest, "Zn": rest},
+                                       elements=el)
     out = []
     for evaluation in (0, 1):
         ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
         ctx.set_lattices(ns, sp)
-        ctx.kmc_init(temps, seed=17, rng=1, evaluation=evaluation)
+        ctx.kmc_init(temps, seed=17, rng=1, evaluation=evaluation, warps_per_replica=warps)
         tr, ev = ctx.kmc_run(400, trace_replica=3, events=True)
         out.append((ctx.get_lattices(), ctx.kmc_state(), tr, ev))
     (l0, s0, t0, e0), (l1, s1, t1, e1) = out
