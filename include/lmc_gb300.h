@@ -237,6 +237,12 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
 int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy);
 /* Device time (ms) of the last lmc_kmc_run / lmc_cmc_run launch (CUDA events on the context stream). */
 int lmc_last_run_ms(lmc_ctx *ctx, double *ms);
+/* Launch shape of lmc_kmc_run under the current options: warps per replica,
+ * replicas per block, resident blocks per SM and dynamic shared memory per
+ * block. No reference counterpart (GPU launch introspection, used by the
+ * autotuner and the benchmark record). Any output may be NULL. */
+int lmc_kmc_launch_info(lmc_ctx *ctx, int *warps_per_replica, int *replicas_per_block, int *blocks_per_sm,
+                        int64_t *shared_bytes);
 
 /* ------------------------------------------------------------------------- */
 /* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */

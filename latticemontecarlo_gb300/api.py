@@ -197,6 +197,14 @@ class Context:
                                       ptr(energy, C.c_double)))
         return vac, steps, time, energy
 
+    def kmc_launch_info(self) -> dict:
+        """Block shape and occupancy the next kmc_run uses."""
+        g, rpb, per_sm = C.c_int(), C.c_int(), C.c_int()
+        smem = np.zeros(1, np.int64)
+        check(N.lib.lmc_kmc_launch_info(self._h, C.byref(g), C.byref(rpb), C.byref(per_sm), ptr(smem, C.c_int64)))
+        return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "blocks_per_sm": per_sm.value,
+                "shared_bytes": int(smem[0])}
+
     def last_run_ms(self) -> float:
         ms = C.c_double()
         check(N.lib.lmc_last_run_ms(self._h, C.byref(ms)))

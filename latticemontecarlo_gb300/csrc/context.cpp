@@ -421,7 +421,7 @@ void BuildSparse(lmc_ctx *c, int base) {
           p_de[((label * e + m) * e + c1) * e + c2] = F(label, m, c1, c2) - F(label, m, c1, base) - F(label, m, base, c2);
   // state-list clusters with exactly one pair site
   std::vector<long long> base_de(e, 0), s_de(static_cast<size_t>(e) * lmc::kStateSites * e, 0);
-  std::vector<uint16_t> px_st(lmc::kStateSites * lmc::kStateSites, 0xFFFF);
+  std::vector<uint16_t> px_st(lmc::kTriState, 0xFFFF);
   for (const auto &cl : pt.state_clusters) {
     int has_first = 0, has_second = 0;
     std::vector<int> others;
@@ -442,30 +442,26 @@ void BuildSparse(lmc_ctx *c, int base) {
     }
     if (others.size() == 2) {
       const uint16_t code = static_cast<uint16_t>(cl.label | (has_second << 3));
-      for (int o = 0; o < 2; ++o) {
-        uint16_t &slot = px_st[others[o] * lmc::kStateSites + others[1 - o]];
-        if ((slot & 0xFF) == 0xFF) slot = static_cast<uint16_t>((slot & 0xFF00) | code);
-        else if ((slot >> 8) == 0xFF) slot = static_cast<uint16_t>((slot & 0x00FF) | (code << 8));
-        else Require(false, LMC_ERR_UNSUPPORTED, "more than two triplets share a site pair");
-      }
+      uint16_t &slot = px_st[lmc::Tri(others[0], others[1])];
+      if ((slot & 0xFF) == 0xFF) slot = static_cast<uint16_t>((slot & 0xFF00) | code);
+      else if ((slot >> 8) == 0xFF) slot = static_cast<uint16_t>((slot & 0x00FF) | (code << 8));
+      else Require(false, LMC_ERR_UNSUPPORTED, "more than two triplets share a site pair");
     }
   }
   // environment lists: W - W(base block entry) per feature, single-site terms, pair lookup
   const int slots = static_cast<int>(fm.slot_code.size());
   std::vector<long long> dwd, dwks, dwe0, base_form(3 * std::max(1, slots), 0);
   std::vector<long long> s_env(static_cast<size_t>(std::max(1, slots)) * 3 * lmc::kEnvSites * 8, 0);
-  std::vector<uint32_t> px_env(2 * lmc::kEnvSites * lmc::kEnvSites, 0xFFFFFFFFu);
+  std::vector<uint32_t> px_env(2 * lmc::kTriEnv, 0xFFFFFFFFu);
   auto env_tables = [&](const lmc::EnvEncoding &enc, int which) {
     const auto ooff = enc.OrbitOffsets(eh);
     Require(ooff.back() < (1 << 20), LMC_ERR_UNSUPPORTED, "too many environment features");
     for (const auto &cl : enc.clusters) {
       if (cl.b < 0) continue;
       const uint32_t v = static_cast<uint32_t>(ooff[cl.orbit]) | (static_cast<uint32_t>(cl.mode) << 20);
-      uint32_t &ab = px_env[(which * lmc::kEnvSites + cl.a) * lmc::kEnvSites + cl.b];
-      uint32_t &ba = px_env[(which * lmc::kEnvSites + cl.b) * lmc::kEnvSites + cl.a];
-      Require(ab == 0xFFFFFFFFu && ba == 0xFFFFFFFFu, LMC_ERR_UNSUPPORTED, "two clusters share a site pair");
-      ab = v | (1u << 22);
-      ba = v;
+      uint32_t &v_tri = px_env[which * lmc::kTriEnv + lmc::Tri(cl.a, cl.b)];
+      Require(v_tri == 0xFFFFFFFFu && cl.a != cl.b, LMC_ERR_UNSUPPORTED, "two clusters share a site pair");
+      v_tri = v | (cl.a < cl.b ? (1u << 22) : 0u);
     }
     return ooff;
   };
@@ -545,6 +541,25 @@ void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
     }
   *g = best;
   *rpb = std::max(1, 8 / best);  // 256-thread blocks (the kernel allows up to 384)
+}
+
+// Block shape and evaluation of the KMC launch from the options (0 = default).
+lmc::KmcLaunch KmcShape(const lmc_ctx *ctx) {
+  lmc::KmcLaunch l{};
+  int g = ctx->kmc_opt.warps_per_replica, rpb = ctx->kmc_opt.replicas_per_block;
+  int dg, drpb;
+  KmcDefaults(ctx, &dg, &drpb);
+  if (g <= 0) g = dg;
+  if (rpb <= 0) rpb = drpb;
+  Require(g == 1 || g == 2 || g == 3 || g == 4 || g == 6 || g == 12, LMC_ERR_INVALID_ARGUMENT,
+          "warps_per_replica must divide 12");
+  Require(g * rpb <= 12, LMC_ERR_INVALID_ARGUMENT, "at most 12 warps per block (384 threads)");
+  Require(g == 1 || rpb <= 15, LMC_ERR_INVALID_ARGUMENT, "at most 15 multi-warp replicas per block");
+  l.warps_per_replica = g;
+  l.replicas_per_block = rpb;
+  l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
+  l.sp = ctx->sparse;
+  return l;
 }
 
 }  // namespace
@@ -1098,6 +1113,22 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
   });
 }
 
+int lmc_kmc_launch_info(lmc_ctx *ctx, int *warps_per_replica, int *replicas_per_block, int *blocks_per_sm,
+                        int64_t *shared_bytes) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const lmc::KmcLaunch l = KmcShape(ctx);
+    int per_sm = 0;
+    size_t bytes = 0;
+    CudaCheck(lmc::KmcOccupancy(ctx->t, l, &per_sm, &bytes), "KMC occupancy");
+    if (warps_per_replica) *warps_per_replica = l.warps_per_replica;
+    if (replicas_per_block) *replicas_per_block = l.replicas_per_block;
+    if (blocks_per_sm) *blocks_per_sm = per_sm;
+    if (shared_bytes) *shared_bytes = static_cast<int64_t>(bytes);
+  });
+}
+
 int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace, double *events12) {
   return Guard([&] {
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
@@ -1121,18 +1152,7 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     s.tt_time = ctx->tt_len ? ctx->k_tt_time.as<double>() : nullptr;
     s.tt_temp = ctx->tt_len ? ctx->k_tt_temp.as<double>() : nullptr;
     s.tt_len = ctx->tt_len;
-    lmc::KmcLaunch l{};
-    int g = ctx->kmc_opt.warps_per_replica, rpb = ctx->kmc_opt.replicas_per_block;
-    int dg, drpb;
-    KmcDefaults(ctx, &dg, &drpb);
-    if (g <= 0) g = dg;
-    if (rpb <= 0) rpb = drpb;
-    Require(g == 1 || g == 2 || g == 3 || g == 4 || g == 6 || g == 12, LMC_ERR_INVALID_ARGUMENT,
-            "warps_per_replica must divide 12");
-    Require(g * rpb <= 12, LMC_ERR_INVALID_ARGUMENT, "at most 12 warps per block (384 threads)");
-    Require(g == 1 || rpb <= 15, LMC_ERR_INVALID_ARGUMENT, "at most 15 multi-warp replicas per block");
-    l.warps_per_replica = g;
-    l.replicas_per_block = rpb;
+    lmc::KmcLaunch l = KmcShape(ctx);
     l.steps = steps;
     l.trace_replica = -1;
     if (trace || events12) {
@@ -1149,8 +1169,6 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     }
     l.stop_flag = ctx->d_stop;
     l.status = ctx->status.as<int>();
-    l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
-    l.sp = ctx->sparse;
     ctx->ClearStatus();
     CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
     CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");

@@ -704,6 +704,19 @@ struct KmcShared {
   int8_t nb_code[kMaxSparseSites];  // and species
 };
 
+// 1 / kT and the vacancy-concentration time correction at temperature `temp`
+// (RateCorrector::GetTimeCorrectionFactor, RateCorrector.hpp:17-24; 1 without one).
+__device__ __forceinline__ void TemperatureFactors(const KmcDevState &s, int r, double temp, double *beta,
+                                                   double *corr) {
+  *beta = 1.0 / kBoltzmannEv / temp;
+  double c = 1.0;
+  if (s.corr_cvac[r] >= 0.0) {
+    const double cv = 1.64 * exp(-(0.66 / kBoltzmannEv / temp - 0.7));
+    c = s.corr_cvac[r] / cv / (1 - 13 * s.corr_csol[r]);
+  }
+  *corr = c;
+}
+
 __device__ __forceinline__ double InterpT(const double *tt, const double *tv, int len, double time) {
   // TimeTemperatureInterpolator::GetTemperature (TimeTemperatureInterpolator.cpp:44-65)
   int lo = 0, hi = len;
@@ -720,10 +733,11 @@ __device__ __forceinline__ double InterpT(const double *tt, const double *tv, in
 
 // Pair term of one environment pair cluster (see KmcSparse): the cluster's
 // entry minus the two entries with one site at the base species.
-__device__ __forceinline__ long long EnvPairTerm(uint32_t v, const long long *__restrict__ w, int rp, int rq, int rb0,
-                                                 const int8_t *pt) {
+__device__ __forceinline__ long long EnvPairTerm(uint32_t v, const long long *__restrict__ w, int p, int q, int rp,
+                                                 int rq, int rb0, const int8_t *pt) {
   const int fb = v & 0xFFFFF, mode = (v >> 20) & 3;
-  const bool first = (v >> 22) & 1;
+  const bool lower_first = (v >> 22) & 1;
+  const bool first = (p < q) == lower_first;  // p is the cluster's first site
   const int ra = first ? rp : rq, rb = first ? rq : rp;
   if (ra == kMaxOnehot - 1 || rb == kMaxOnehot - 1) return 0;  // flagged by the single-site terms
   const int8_t *row = pt + mode * 64;
@@ -755,8 +769,8 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
   const long long *__restrict__ w_a = sp.dw_ks + static_cast<long long>(slot) * f_mm2;
   const long long *__restrict__ w_b =
       part == 1 ? w_a : (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * f_mmm;
-  const uint32_t *px_a = s_pxenv + kEnvSites * kEnvSites;
-  const uint32_t *px_b = s_pxenv + (part == 1 ? kEnvSites * kEnvSites : 0);
+  const uint32_t *px_a = s_pxenv + kTriEnv;
+  const uint32_t *px_b = s_pxenv + (part == 1 ? kTriEnv : 0);
   const long long *__restrict__ pde = sp.p_de + mig * e * e;
   for (int k = 0; k < k_sites; ++k) {
     const int l = nb_l[k], code = nb_code[k];
@@ -780,7 +794,7 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
       const int qa = pos_a[l2], qb = pos_b[l2];
       if (pa != 255 && qa != 255) {
         if (part == 0) {
-          const unsigned v = s_pxst[pa * kStateSites + qa];
+          const unsigned v = s_pxst[Tri(pa, qa)];
           if (v != 0xFFFFu) {
             const int c2 = nb_code[k2];
 #pragma unroll
@@ -792,13 +806,13 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
             }
           }
         } else {
-          const uint32_t v = px_a[pa * kEnvSites + qa];
-          if (v != 0xFFFFFFFFu) acc_a += EnvPairTerm(v, w_a, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
+          const uint32_t v = px_a[Tri(pa, qa)];
+          if (v != 0xFFFFFFFFu) acc_a += EnvPairTerm(v, w_a, pa, qa, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
         }
       }
       if (pb != 255 && qb != 255) {
-        const uint32_t v = px_b[pb * kEnvSites + qb];
-        if (v != 0xFFFFFFFFu) acc_b += EnvPairTerm(v, w_b, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
+        const uint32_t v = px_b[Tri(pb, qb)];
+        if (v != 0xFFFFFFFFu) acc_b += EnvPairTerm(v, w_b, pb, qb, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
       }
     }
   }
@@ -840,12 +854,12 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
   int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
   // sparse tables follow the per-warp arrays
   uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + rpb * g_per * kArr);        // [4][12][136]
-  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_pos + 4 * 12 * 136);          // [60][60]
-  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pxst + kStateSites * kStateSites);  // [2][58][58]
+  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pos + 4 * 12 * 136);  // [2][kTriEnv]
+  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_pxenv + 2 * kTriEnv);   // [kTriState]
   if (kSparse) {
     StageArray(l.sp.pos, s_pos, 4 * 12 * 136);
-    StageArray(l.sp.px_st, s_pxst, kStateSites * kStateSites);
-    StageArray(l.sp.px_env, s_pxenv, 2 * kEnvSites * kEnvSites);
+    StageArray(l.sp.px_st, s_pxst, kTriState);
+    StageArray(l.sp.px_env, s_pxenv, 2 * kTriEnv);
   }
 
   StageArray(t.de_cl, s_de, t.n_de_cl);
@@ -877,8 +891,16 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
   if (active && leader) {
     time = s.time[r];
     energy = s.energy[r];
-    step0 = s.steps[r];
   }
+  if (active && g == 0) step0 = s.steps[r];
+  uint32_t key0 = 0, key1 = 0;  // Philox key of the replica
+  if (active && g == 0 && s.rng_kind != 0) {
+    key0 = s.rng[r * kRngWords];
+    key1 = s.rng[r * kRngWords + 1];
+  }
+  // Philox draws for 32 steps at a time: lane j holds -log(u1) and u2 of
+  // step (it & ~31) + j, so the FP64 logarithm runs once per 32 steps
+  double nlog_blk = 0.0, u2_blk = 0.0;
   Mt mt{nullptr, nullptr};
   if (active && s.rng_kind == 0) {
     uint32_t *w = s.rng + static_cast<long long>(r) * kRngWords;
@@ -887,6 +909,7 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
   }
   const int e = t.num_species;
   if (!active) return;  // no block-wide barrier below this point
+  if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
   for (unsigned long long it = 0; it < l.steps; ++it) {
     // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
     if (active) {
@@ -900,16 +923,8 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
         rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
       }
       if (leader) {
-        double temp = s.temperature[r];
-        if (s.tt_len > 0) temp = InterpT(s.tt_time, s.tt_temp, s.tt_len, time);
-        rs.beta = 1.0 / kBoltzmannEv / temp;
-        double corr = 1.0;
-        if (s.corr_cvac[r] >= 0.0) {
-          // RateCorrector::GetTimeCorrectionFactor (RateCorrector.hpp:17-24)
-          const double cv = 1.64 * exp(-(0.66 / kBoltzmannEv / temp - 0.7));
-          corr = s.corr_cvac[r] / cv / (1 - 13 * s.corr_csol[r]);
-        }
-        rs.corr = corr;
+        if (s.tt_len > 0)
+          TemperatureFactors(s, r, InterpT(s.tt_time, s.tt_temp, s.tt_len, time), &rs.beta, &rs.corr);
         rs.stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
       }
     }
@@ -1046,22 +1061,24 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
         }
         total = __shfl_sync(0xffffffffu, mycum, 11);
       }
-      double u1 = 0, u2 = 0;
-      if (lane == 0) {
-        if (s.rng_kind == 0) {
-          u1 = MtUniform(mt);  // KineticMcFirstOmp::CalculateTime draws first
-          u2 = MtUniform(mt);  // then KineticMcFirstAbstract::SelectEvent
-        } else {
-          const unsigned long long ctr = step0 + it;
-          const uint4 x = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
-                                        static_cast<uint32_t>(r), 0x4b4d43u, s.rng[r * kRngWords],
-                                        s.rng[r * kRngWords + 1]);
-          u1 = U01Open(x.x, x.y);
-          u2 = U01(x.z, x.w);
+      double nlog_u1 = 0, u2 = 0;  // -log(u1) for the clock, u2 for the selection
+      if (s.rng_kind == 0) {
+        if (lane == 0) {
+          nlog_u1 = -log(MtUniform(mt));  // KineticMcFirstOmp::CalculateTime draws first
+          u2 = MtUniform(mt);             // then KineticMcFirstAbstract::SelectEvent
         }
+        u2 = __shfl_sync(0xffffffffu, u2, 0);
+      } else {
+        if ((it & 31) == 0) {
+          const unsigned long long ctr = step0 + it + lane;
+          const uint4 x = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                        static_cast<uint32_t>(r), 0x4b4d43u, key0, key1);
+          nlog_blk = -log(U01Open(x.x, x.y));
+          u2_blk = U01(x.z, x.w);
+        }
+        nlog_u1 = __shfl_sync(0xffffffffu, nlog_blk, static_cast<int>(it & 31));
+        u2 = __shfl_sync(0xffffffffu, u2_blk, static_cast<int>(it & 31));
       }
-      u1 = __shfl_sync(0xffffffffu, u1, 0);
-      u2 = __shfl_sync(0xffffffffu, u2, 0);
       bool hit;
       if (s.rng_kind == 0) {
         // cumulative probabilities k_i / total summed in order, first one >= u2
@@ -1083,7 +1100,7 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
       const double de_sel = __shfl_sync(0xffffffffu, de_s, sel);
       if (lane == 0) {
         if (!(total > 0.0) || !isfinite(total)) bad_all |= kStatusNumeric;
-        const double dt = -log(u1) / total / kPrefactor * rs.corr;
+        const double dt = nlog_u1 / total / kPrefactor * rs.corr;
         time += dt;
         energy += de_sel;
         lat[vac] = lat[tgt];  // Config::LatticeJump: the migrating atom takes the vacancy site
@@ -1467,8 +1484,27 @@ size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l) {
   b = (b + 15) & ~size_t(15);
   b += sizeof(KmcShared) * l.replicas_per_block;
   b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
-  if (l.sparse) b += 4 * 12 * 136 + 2 * kStateSites * kStateSites + 4 * 2 * kEnvSites * kEnvSites;
+  if (l.sparse) b += 4 * 12 * 136 + 4 * 2 * kTriEnv + 2 * kTriState;
   return (b + 15) & ~size_t(15);
+}
+
+template <typename K>
+static cudaError_t PrepareKmc(K kern, size_t sm) {
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+}
+
+cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes) {
+  const int threads = l.warps_per_replica * l.replicas_per_block * 32;
+  const size_t sm = KmcSharedBytes(t, l);
+  const bool wide = threads > 256;
+  auto query = [&](auto kern) -> cudaError_t {
+    cudaError_t err = PrepareKmc(kern, sm);
+    if (err != cudaSuccess) return err;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, threads, sm);
+  };
+  *shared_bytes = sm;
+  if (l.sparse) return wide ? query(kmc_kernel<true, true>) : query(kmc_kernel<true, false>);
+  return wide ? query(kmc_kernel<false, true>) : query(kmc_kernel<false, false>);
 }
 
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
@@ -1478,7 +1514,7 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
   const size_t sm = KmcSharedBytes(t, l);
   const bool wide = threads > 256;
   auto launch = [&](auto kern) -> cudaError_t {
-    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+    cudaError_t err = PrepareKmc(kern, sm);
     if (err != cudaSuccess) return err;
     kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
     return cudaSuccess;

@@ -46,13 +46,20 @@ struct KmcTraceRec {
 // all in the same int64 fixed point as the dense evaluation (bit-identical,
 // since wrapping integer sums do not depend on their order).
 // Lists: 0 state (energy change), 1 MMM, 2 MM2 forward, 3 MM2 backward.
-constexpr int kMaxSparseSites = 32;  // more non-base neighbourhood sites: dense evaluation for that step
+constexpr int kMaxSparseSites = 32;
+constexpr int kTriState = 60 * 59 / 2, kTriEnv = 58 * 57 / 2;
+__host__ __device__ __forceinline__ int Tri(int p, int q) {
+  const int hi = p > q ? p : q, lo = p > q ? q : p;
+  return hi * (hi - 1) / 2 + lo;
+}  // more non-base neighbourhood sites: dense evaluation for that step
 struct KmcSparse {
   const uint8_t *pos;      // [4][12][136]: local index -> position in list of jump c, 255 none
   const long long *s_de;   // [E migrant][60][E species]: single-site energy-change terms
   const long long *s_env;  // [slot][3 forms: D, Ks, e0][58][8 ranks]: single-site feature terms
-  const uint16_t *px_st;   // [60][60]: up to two triplets sharing the sites, (label | side << 3) per byte, 0xFF none
-  const uint32_t *px_env;  // [2: MMM, MM2][58][58]: feature base | mode << 20 | (row site is the cluster's
+  // site-pair lookups, strict lower triangles: entry (p, q), p != q, at
+  // Tri(max, min) = max * (max - 1) / 2 + min
+  const uint16_t *px_st;   // [1770]: up to two triplets holding both sites, (label | side << 3) per byte, 0xFF none
+  const uint32_t *px_env;  // [2: MMM, MM2][1653]: feature base | mode << 20 | (lower site is the cluster's
                            // first) << 22 of the pair cluster, ~0 none
   const long long *p_de;   // [8][E][E][E]: pair term of a triplet, F(c1, c2) - F(c1, b) - F(b, c2)
   const long long *base_de;    // [E] all-base energy change per migrant code
@@ -99,6 +106,8 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                       cudaStream_t stream);
 size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
+// Resident blocks per SM and dynamic shared memory of the KMC launch `l`.
+cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes);
 
 // Reference-batch CMC (one warp, mt19937_64 stream, batch = `batch` pairs).
 struct CmcRefArgs {
