@@ -420,8 +420,8 @@ void BuildSparse(lmc_ctx *c, int base) {
         for (int c2 = 0; c2 < e; ++c2)
           p_de[((label * e + m) * e + c1) * e + c2] = F(label, m, c1, c2) - F(label, m, c1, base) - F(label, m, base, c2);
   // state-list clusters with exactly one pair site
-  std::vector<long long> base_de(e, 0), s_de(static_cast<size_t>(e) * lmc::kStateSites * e, 0);
-  std::vector<uint16_t> px_st(lmc::kTriState, 0xFFFF);
+  std::vector<long long> base_de(e, 0), s_de(static_cast<size_t>(e) * (lmc::kStateSites + 1) * e, 0);
+  std::vector<uint16_t> px_st(lmc::kTriState + 1, 0);
   for (const auto &cl : pt.state_clusters) {
     int has_first = 0, has_second = 0;
     std::vector<int> others;
@@ -438,30 +438,39 @@ void BuildSparse(lmc_ctx *c, int base) {
       const int p = others[k];
       for (int m = 0; m < e; ++m)
         for (int sp_code = 0; sp_code < e; ++sp_code)
-          s_de[(static_cast<size_t>(m) * lmc::kStateSites + p) * e + sp_code] += sign * F(cl.label, m, sp_code, b2);
+          s_de[(static_cast<size_t>(m) * (lmc::kStateSites + 1) + p) * e + sp_code] += sign * F(cl.label, m, sp_code, b2);
     }
     if (others.size() == 2) {
       const uint16_t code = static_cast<uint16_t>(cl.label | (has_second << 3));
+      Require(cl.label >= 4, LMC_ERR_UNSUPPORTED, "unexpected triplet label");
       uint16_t &slot = px_st[lmc::Tri(others[0], others[1])];
-      if ((slot & 0xFF) == 0xFF) slot = static_cast<uint16_t>((slot & 0xFF00) | code);
-      else if ((slot >> 8) == 0xFF) slot = static_cast<uint16_t>((slot & 0x00FF) | (code << 8));
+      if ((slot & 0xFF) == 0) slot = static_cast<uint16_t>((slot & 0xFF00) | code);
+      else if ((slot >> 8) == 0) slot = static_cast<uint16_t>((slot & 0x00FF) | (code << 8));
       else Require(false, LMC_ERR_UNSUPPORTED, "more than two triplets share a site pair");
     }
   }
   // environment lists: W - W(base block entry) per feature, single-site terms, pair lookup
   const int slots = static_cast<int>(fm.slot_code.size());
   std::vector<long long> dwd, dwks, dwe0, base_form(3 * std::max(1, slots), 0);
-  std::vector<long long> s_env(static_cast<size_t>(std::max(1, slots)) * 3 * lmc::kEnvSites * 8, 0);
-  std::vector<uint32_t> px_env(2 * lmc::kTriEnv, 0xFFFFFFFFu);
+  std::vector<long long> s_env(static_cast<size_t>(std::max(1, slots)) * 3 * (lmc::kEnvSites + 1) * 8, 0);
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  std::vector<uint32_t> px_env(2 * (lmc::kTriEnv + 1), kNone);
   auto env_tables = [&](const lmc::EnvEncoding &enc, int which) {
     const auto ooff = enc.OrbitOffsets(eh);
     Require(ooff.back() < (1 << 20), LMC_ERR_UNSUPPORTED, "too many environment features");
     for (const auto &cl : enc.clusters) {
       if (cl.b < 0) continue;
       const uint32_t v = static_cast<uint32_t>(ooff[cl.orbit]) | (static_cast<uint32_t>(cl.mode) << 20);
-      uint32_t &v_tri = px_env[which * lmc::kTriEnv + lmc::Tri(cl.a, cl.b)];
-      Require(v_tri == 0xFFFFFFFFu && cl.a != cl.b, LMC_ERR_UNSUPPORTED, "two clusters share a site pair");
+      uint32_t &v_tri = px_env[which * (lmc::kTriEnv + 1) + lmc::Tri(cl.a, cl.b)];
+      Require(v_tri == kNone && cl.a != cl.b, LMC_ERR_UNSUPPORTED, "two clusters share a site pair");
       v_tri = v | (cl.a < cl.b ? (1u << 22) : 0u);
+    }
+    // no cluster: an ordered-pair entry in the block of 64 zeros after the features
+    const uint32_t none = static_cast<uint32_t>(ooff.back()) | (1u << 20);
+    for (int i = 0; i <= lmc::kTriEnv; ++i) {
+      uint32_t &v = px_env[which * (lmc::kTriEnv + 1) + i];
+      if (v == kNone) v = none;
+      else Require(i < lmc::kTriEnv, LMC_ERR_UNSUPPORTED, "pair lookup overflow");
     }
     return ooff;
   };
@@ -475,6 +484,7 @@ void BuildSparse(lmc_ctx *c, int base) {
       for (int j = ooff[o]; j < ooff[o + 1]; ++j) out.push_back(wv[j] - w0);
       *base_sum += static_cast<long long>(mult) * w0 * enc.orbits[o].size;
     }
+    out.insert(out.end(), 64, 0);  // zero block addressed by "no cluster" lookups
     const long long *dw = out.data() + first;
     for (const auto &cl : enc.clusters) {
       const int fb = ooff[cl.orbit];
@@ -489,10 +499,10 @@ void BuildSparse(lmc_ctx *c, int base) {
     }
   };
   for (int sidx = 0; sidx < slots; ++sidx) {
-    long long *sg = s_env.data() + static_cast<size_t>(sidx) * 3 * lmc::kEnvSites * 8;
+    long long *sg = s_env.data() + static_cast<size_t>(sidx) * 3 * (lmc::kEnvSites + 1) * 8;
     delta(pt.mmm, off_mmm, fm.quartic_d[sidx].w, dwd, &base_form[sidx * 3 + 0], 1, sg);
-    delta(pt.mm2, off_mm2, fm.quartic_ks[sidx].w, dwks, &base_form[sidx * 3 + 1], 2, sg + lmc::kEnvSites * 8);
-    delta(pt.mmm, off_mmm, fm.e0[sidx].w, dwe0, &base_form[sidx * 3 + 2], 1, sg + 2 * lmc::kEnvSites * 8);
+    delta(pt.mm2, off_mm2, fm.quartic_ks[sidx].w, dwks, &base_form[sidx * 3 + 1], 2, sg + (lmc::kEnvSites + 1) * 8);
+    delta(pt.mmm, off_mmm, fm.e0[sidx].w, dwe0, &base_form[sidx * 3 + 2], 1, sg + 2 * (lmc::kEnvSites + 1) * 8);
   }
   // local index -> list position for each jump
   std::vector<uint8_t> pos(4 * 12 * 136, 255);
@@ -511,8 +521,27 @@ void BuildSparse(lmc_ctx *c, int base) {
       pos[(3 * 12 + d) * 136 + l_b[d * lmc::kEnvSites + k]] = static_cast<uint8_t>(k);
     }
   }
+  // local pairs that share a cluster in some jump's list
+  std::vector<uint32_t> inter(lmc::kLocalSites * lmc::kInterWords, 0u);
+  auto mark = [&](int a, int b) {
+    inter[a * lmc::kInterWords + (b >> 5)] |= 1u << (b & 31);
+    inter[b * lmc::kInterWords + (a >> 5)] |= 1u << (a & 31);
+  };
+  for (int d = 0; d < 12; ++d) {
+    for (int p = 0; p < lmc::kStateSites; ++p)
+      for (int q = 0; q < p; ++q)
+        if (px_st[lmc::Tri(p, q)] != 0) mark(l_st[d * lmc::kStateSites + p], l_st[d * lmc::kStateSites + q]);
+    const uint8_t *lists[3] = {l_mmm.data(), l_f.data(), l_b.data()};
+    for (int li = 0; li < 3; ++li)
+      for (int p = 0; p < lmc::kEnvSites; ++p)
+        for (int q = 0; q < p; ++q)
+          if (px_env[(li == 0 ? 0 : 1) * (lmc::kTriEnv + 1) + lmc::Tri(p, q)] !=
+              px_env[(li == 0 ? 0 : 1) * (lmc::kTriEnv + 1) + lmc::kTriEnv])
+            mark(lists[li][d * lmc::kEnvSites + p], lists[li][d * lmc::kEnvSites + q]);
+  }
   auto &B = c->sparse_bufs;
   sp.pos = c->Upload(pos, &B);
+  sp.inter = c->Upload(inter, &B);
   sp.s_de = c->Upload(s_de, &B);
   sp.s_env = c->Upload(s_env, &B);
   sp.px_st = c->Upload(px_st, &B);
@@ -524,6 +553,8 @@ void BuildSparse(lmc_ctx *c, int base) {
   sp.dw_e0 = c->Upload(dwe0, &B);
   sp.base_form = c->Upload(base_form, &B);
   sp.center = l_st[pt.pos_first];
+  sp.dw_stride_mmm = off_mmm.back() + 64;
+  sp.dw_stride_mm2 = off_mm2.back() + 64;
   c->sparse = sp;
 }
 

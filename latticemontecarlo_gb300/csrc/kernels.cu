@@ -700,8 +700,10 @@ struct KmcShared {
   double corr;
   int stop;
   int nbk;                          // non-base sites in the neighbourhood (sparse evaluation)
-  uint8_t nb_l[kMaxSparseSites];    // their local indices
-  int8_t nb_code[kMaxSparseSites];  // and species
+  int npairs;                       // pairs of them that share a cluster in some jump
+  uint8_t nb_l[kMaxSparseSites + 1];    // their local indices; padding: kLocalSites (in no list)
+  int8_t nb_code[kMaxSparseSites + 1];  // and species; padding: the base species
+  uint16_t pairs[kMaxSparsePairs];      // (k | k2 << 8), k2 < k indices into nb_l; padding: (32, 32)
 };
 
 // 1 / kT and the vacancy-concentration time correction at temperature `temp`
@@ -732,16 +734,21 @@ __device__ __forceinline__ double InterpT(const double *tt, const double *tv, in
 }
 
 // Pair term of one environment pair cluster (see KmcSparse): the cluster's
-// entry minus the two entries with one site at the base species.
+// entry minus the two entries with one site at the base species. "No cluster"
+// lookups address a block of zeros. A site of rank kMaxOnehot - 1 (a vacancy
+// or an element without a one-hot slot) is flagged by the single-site terms;
+// its pair type is clamped so the loads stay in bounds.
 __device__ __forceinline__ long long EnvPairTerm(uint32_t v, const long long *__restrict__ w, int p, int q, int rp,
                                                  int rq, int rb0, const int8_t *pt) {
   const int fb = v & 0xFFFFF, mode = (v >> 20) & 3;
   const bool lower_first = (v >> 22) & 1;
   const bool first = (p < q) == lower_first;  // p is the cluster's first site
   const int ra = first ? rp : rq, rb = first ? rq : rp;
-  if (ra == kMaxOnehot - 1 || rb == kMaxOnehot - 1) return 0;  // flagged by the single-site terms
   const int8_t *row = pt + mode * 64;
-  return __ldg(&w[fb + row[ra * 8 + rb]]) - __ldg(&w[fb + row[ra * 8 + rb0]]) - __ldg(&w[fb + row[rb0 * 8 + rb]]);
+  const int t_ab = max(0, static_cast<int>(row[ra * 8 + rb]));
+  const int t_a0 = max(0, static_cast<int>(row[ra * 8 + rb0]));
+  const int t_0b = max(0, static_cast<int>(row[rb0 * 8 + rb]));
+  return __ldg(&w[fb + t_ab]) - __ldg(&w[fb + t_a0]) - __ldg(&w[fb + t_0b]);
 }
 
 struct LaneAcc {
@@ -750,71 +757,76 @@ struct LaneAcc {
 };
 
 // Sparse evaluation of one half of jump c over the replica's non-base sites
-// (nb_l local indices, nb_code species, k of them). Part 0 sums the energy
-// change (list A = state) and the D or e0 form (list B = MMM); part 1 sums the
-// Ks form over MM2 forward (A) and backward (B). Returns the corrections to
-// the all-base constants.
+// and their interacting pairs (lists padded to multiples of 4 with entries
+// that fall outside every list). Part 0 sums the energy change (list A =
+// state) and the D or e0 form (list B = MMM); part 1 sums the Ks form over MM2
+// forward (A) and backward (B). Branch-free, four entries at a time, so the
+// table loads of independent entries overlap. Returns the corrections to the
+// all-base constants.
 __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint8_t *s_pos, const uint16_t *s_pxst,
-                                                 const uint32_t *s_pxenv, const SmallTables *sm, const uint8_t *nb_l,
-                                                 const int8_t *nb_code, int k_sites, int e, int x, int f_mmm,
-                                                 int f_mm2, int c, int part, int mig, int slot, bool quartic) {
+                                                 const uint32_t *s_pxenv, const SmallTables *sm, const KmcShared &rs,
+                                                 int e, int x, int c, int part, int mig, int slot, bool quartic) {
   long long acc_a = 0, acc_b = 0;
   unsigned bad = 0;
   const int rb0 = sm->rank[sp.base_code];
   const uint8_t *pos_a = s_pos + ((part == 0 ? 0 : 2) * 12 + c) * 136;
   const uint8_t *pos_b = s_pos + ((part == 0 ? 1 : 3) * 12 + c) * 136;
+  constexpr int kEnvRows = kEnvSites + 1, kStateRows = kStateSites + 1;
   const long long *__restrict__ sg_a =
-      part == 0 ? sp.s_de + mig * kStateSites * e : sp.s_env + (slot * 3 + 1) * kEnvSites * 8;
-  const long long *__restrict__ sg_b = sp.s_env + (slot * 3 + (part == 1 ? 1 : (quartic ? 0 : 2))) * kEnvSites * 8;
-  const long long *__restrict__ w_a = sp.dw_ks + static_cast<long long>(slot) * f_mm2;
+      part == 0 ? sp.s_de + mig * kStateRows * e : sp.s_env + (slot * 3 + 1) * kEnvRows * 8;
+  const long long *__restrict__ sg_b = sp.s_env + (slot * 3 + (part == 1 ? 1 : (quartic ? 0 : 2))) * kEnvRows * 8;
+  const int stride_a = part == 0 ? e : 8, zero_a = part == 0 ? kStateSites : kEnvSites;
+  const long long *__restrict__ w_a = sp.dw_ks + static_cast<long long>(slot) * sp.dw_stride_mm2;
   const long long *__restrict__ w_b =
-      part == 1 ? w_a : (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * f_mmm;
-  const uint32_t *px_a = s_pxenv + kTriEnv;
-  const uint32_t *px_b = s_pxenv + (part == 1 ? kTriEnv : 0);
+      part == 1 ? w_a : (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * sp.dw_stride_mmm;
+  const uint32_t *px_a = s_pxenv + (kTriEnv + 1);
+  const uint32_t *px_b = s_pxenv + (part == 1 ? kTriEnv + 1 : 0);
   const long long *__restrict__ pde = sp.p_de + mig * e * e;
-  for (int k = 0; k < k_sites; ++k) {
-    const int l = nb_l[k], code = nb_code[k];
-    const int rp = sm->rank[code];
-    const int pa = pos_a[l], pb = pos_b[l];
-    if (pa != 255) {
-      if (part == 0) {
-        if (code == x) bad |= kStatusBadCluster;
-        acc_a += __ldg(&sg_a[pa * e + code]);
-      } else {
-        if (rp == kMaxOnehot - 1) bad |= kStatusXInEnv;
-        acc_a += __ldg(&sg_a[pa * 8 + rp]);
-      }
-    }
-    if (pb != 255) {
-      if (rp == kMaxOnehot - 1) bad |= kStatusXInEnv;
-      acc_b += __ldg(&sg_b[pb * 8 + rp]);
-    }
-    for (int k2 = 0; k2 < k; ++k2) {
-      const int l2 = nb_l[k2];
-      const int qa = pos_a[l2], qb = pos_b[l2];
-      if (pa != 255 && qa != 255) {
-        if (part == 0) {
-          const unsigned v = s_pxst[Tri(pa, qa)];
-          if (v != 0xFFFFu) {
-            const int c2 = nb_code[k2];
+  // single-site terms
+  const int k_sites = rs.nbk;
+  for (int k0 = 0; k0 < k_sites; k0 += 4) {
+    long long va[4], vb[4];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const unsigned t3 = (v >> (8 * h)) & 0xFF;
-              if (t3 == 0xFF) continue;
-              const long long f = __ldg(&pde[(((t3 & 7) * e * e) * e) + code * e + c2]);
-              acc_a += (t3 & 8) ? -f : f;
-            }
-          }
-        } else {
-          const uint32_t v = px_a[Tri(pa, qa)];
-          if (v != 0xFFFFFFFFu) acc_a += EnvPairTerm(v, w_a, pa, qa, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
-        }
-      }
-      if (pb != 255 && qb != 255) {
-        const uint32_t v = px_b[Tri(pb, qb)];
-        if (v != 0xFFFFFFFFu) acc_b += EnvPairTerm(v, w_b, pb, qb, rp, sm->rank[nb_code[k2]], rb0, sm->pairtype);
-      }
+    for (int u = 0; u < 4; ++u) {
+      const int l = rs.nb_l[k0 + u], code = rs.nb_code[k0 + u];
+      const int rp = sm->rank[code];
+      const int pa = pos_a[l], pb = pos_b[l];
+      const bool in_a = pa != 255, in_b = pb != 255;
+      va[u] = __ldg(&sg_a[(in_a ? pa : zero_a) * stride_a + (part == 0 ? code : rp)]);
+      vb[u] = __ldg(&sg_b[(in_b ? pb : kEnvSites) * 8 + rp]);
+      const bool bad_rank = rp == kMaxOnehot - 1;
+      bad |= (part == 0 && in_a && code == x) ? kStatusBadCluster : 0u;
+      bad |= (((part == 1 && in_a) || in_b) && bad_rank) ? kStatusXInEnv : 0u;
     }
+    acc_a += (va[0] + va[1]) + (va[2] + va[3]);
+    acc_b += (vb[0] + vb[1]) + (vb[2] + vb[3]);
+  }
+  // pair terms over the pairs that share a cluster in some jump
+  const int n_pairs = rs.npairs;
+  for (int i0 = 0; i0 < n_pairs; i0 += 4) {
+    long long va[4], vb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned pk = rs.pairs[i0 + u];
+      const int k = pk & 0xFF, k2 = pk >> 8;
+      const int l = rs.nb_l[k], l2 = rs.nb_l[k2];
+      const int code = rs.nb_code[k], c2 = rs.nb_code[k2];
+      const int pa = pos_a[l], qa = pos_a[l2], pb = pos_b[l], qb = pos_b[l2];
+      const int rp = sm->rank[code], rq = sm->rank[c2];
+      const bool both_a = pa != 255 && qa != 255, both_b = pb != 255 && qb != 255;
+      if (part == 0) {
+        const unsigned v = s_pxst[both_a ? Tri(pa, qa) : kTriState];
+        const unsigned t0 = v & 0xFF, t1 = v >> 8;
+        const long long f0 = __ldg(&pde[((t0 & 7) * e * e) * e + code * e + c2]);
+        const long long f1 = __ldg(&pde[((t1 & 7) * e * e) * e + code * e + c2]);
+        va[u] = ((t0 & 8) ? -f0 : f0) + ((t1 & 8) ? -f1 : f1);
+      } else {
+        va[u] = EnvPairTerm(px_a[both_a ? Tri(pa, qa) : kTriEnv], w_a, pa, qa, rp, rq, rb0, sm->pairtype);
+      }
+      vb[u] = EnvPairTerm(px_b[both_b ? Tri(pb, qb) : kTriEnv], w_b, pb, qb, rp, rq, rb0, sm->pairtype);
+    }
+    acc_a += (va[0] + va[1]) + (va[2] + va[3]);
+    acc_b += (vb[0] + vb[1]) + (vb[2] + vb[3]);
   }
   return {acc_a, acc_b, bad};
 }
@@ -854,12 +866,14 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
   int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
   // sparse tables follow the per-warp arrays
   uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + rpb * g_per * kArr);        // [4][12][136]
-  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pos + 4 * 12 * 136);  // [2][kTriEnv]
-  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_pxenv + 2 * kTriEnv);   // [kTriState]
+  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pos + 4 * 12 * 136);  // [2][kTriEnv + 1]
+  uint32_t *s_inter = s_pxenv + 2 * (kTriEnv + 1);                           // [135][5]
+  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_inter + kLocalSites * kInterWords);  // [kTriState + 1]
   if (kSparse) {
     StageArray(l.sp.pos, s_pos, 4 * 12 * 136);
-    StageArray(l.sp.px_st, s_pxst, kTriState);
-    StageArray(l.sp.px_env, s_pxenv, 2 * kTriEnv);
+    StageArray(l.sp.px_st, s_pxst, kTriState + 1);
+    StageArray(l.sp.px_env, s_pxenv, 2 * (kTriEnv + 1));
+    StageArray(l.sp.inter, s_inter, kLocalSites * kInterWords);
   }
 
   StageArray(t.de_cl, s_de, t.n_de_cl);
@@ -951,11 +965,51 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
           }
           k_sites += __popc(mk);
         }
-        if (lane == 0) rs.nbk = k_sites;
+        // padding up to the next multiple of 4 (and the fixed entry 32)
+        if (lane >= k_sites && lane < ((k_sites + 3) & ~3)) {
+          rs.nb_l[lane] = static_cast<uint8_t>(kLocalSites);
+          rs.nb_code[lane] = static_cast<int8_t>(l.sp.base_code);
+        }
+        if (lane == 0) {
+          rs.nb_l[kMaxSparseSites] = static_cast<uint8_t>(kLocalSites);
+          rs.nb_code[kMaxSparseSites] = static_cast<int8_t>(l.sp.base_code);
+        }
+        __syncwarp();
+        // interacting pairs (k2 < k): lane k tests its row of the interaction table
+        unsigned pm = 0;
+        if (k_sites <= kMaxSparseSites && lane < k_sites) {
+          const uint32_t *row = s_inter + rs.nb_l[lane] * kInterWords;
+          for (int k2 = 0; k2 < lane; ++k2) {
+            const int l2 = rs.nb_l[k2];
+            pm |= ((row[l2 >> 5] >> (l2 & 31)) & 1u) << k2;
+          }
+        }
+        const int cnt = __popc(pm);
+        int pre = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, pre, o);
+          if (lane >= o) pre += v;
+        }
+        const int n_pairs = __shfl_sync(0xffffffffu, pre, 31);
+        pre -= cnt;
+        if (n_pairs <= kMaxSparsePairs) {
+          while (pm) {
+            const int k2 = __ffs(pm) - 1;
+            pm &= pm - 1;
+            rs.pairs[pre++] = static_cast<uint16_t>(lane | (k2 << 8));
+          }
+          if (lane < ((n_pairs + 3) & ~3) - n_pairs)
+            rs.pairs[n_pairs + lane] = static_cast<uint16_t>(kMaxSparseSites | (kMaxSparseSites << 8));
+        }
+        if (lane == 0) {
+          rs.nbk = k_sites;
+          rs.npairs = n_pairs;
+        }
       }
       ReplicaSync(g_per, rl);
     }
-    const bool sparse_step = kSparse && rs.nbk <= kMaxSparseSites;
+    const bool sparse_step = kSparse && rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
     if (sparse_step) {
       // one lane per (jump, half): item = lane * G + g, items 0..23
       const int item = lane * g_per + g;
@@ -967,8 +1021,7 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
         const bool quartic = s.barrier_kind == 0;
         const bool ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
         if (ok && (part == 0 || quartic))
-          la = EvalJumpPairs(l.sp, s_pos, s_pxst, s_pxenv, s_small, rs.nb_l, rs.nb_code, rs.nbk, e, t.x_code,
-                             t.f_mmm, t.f_mm2, c, part, mig, slot, quartic);
+          la = EvalJumpPairs(l.sp, s_pos, s_pxst, s_pxenv, s_small, rs, e, t.x_code, c, part, mig, slot, quartic);
         if (ok) {
           const long long *bf = l.sp.base_form + slot * 3;
           if (part == 0) {
@@ -1484,7 +1537,7 @@ size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l) {
   b = (b + 15) & ~size_t(15);
   b += sizeof(KmcShared) * l.replicas_per_block;
   b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
-  if (l.sparse) b += 4 * 12 * 136 + 4 * 2 * kTriEnv + 2 * kTriState;
+  if (l.sparse) b += 4 * 12 * 136 + 4 * 2 * (kTriEnv + 1) + 4 * kLocalSites * kInterWords + 2 * (kTriState + 1);
   return (b + 15) & ~size_t(15);
 }
 

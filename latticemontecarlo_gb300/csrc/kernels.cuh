@@ -46,27 +46,32 @@ struct KmcTraceRec {
 // all in the same int64 fixed point as the dense evaluation (bit-identical,
 // since wrapping integer sums do not depend on their order).
 // Lists: 0 state (energy change), 1 MMM, 2 MM2 forward, 3 MM2 backward.
-constexpr int kMaxSparseSites = 32;
+constexpr int kMaxSparseSites = 32;  // more non-base neighbourhood sites: dense evaluation for that step
+constexpr int kMaxSparsePairs = 96;  // more interacting non-base pairs: dense evaluation for that step
+constexpr int kInterWords = 5;       // 135-bit rows of the local pair-interaction table
 constexpr int kTriState = 60 * 59 / 2, kTriEnv = 58 * 57 / 2;
 __host__ __device__ __forceinline__ int Tri(int p, int q) {
   const int hi = p > q ? p : q, lo = p > q ? q : p;
   return hi * (hi - 1) / 2 + lo;
-}  // more non-base neighbourhood sites: dense evaluation for that step
+}
 struct KmcSparse {
-  const uint8_t *pos;      // [4][12][136]: local index -> position in list of jump c, 255 none
-  const long long *s_de;   // [E migrant][60][E species]: single-site energy-change terms
-  const long long *s_env;  // [slot][3 forms: D, Ks, e0][58][8 ranks]: single-site feature terms
+  const uint8_t *pos;      // [4][12][136]: local index -> position in list of jump c, 255 none (column 135: none)
+  const uint32_t *inter;   // [135][5]: bit b of row a set when local sites a, b share a cluster in some jump
+  const long long *s_de;   // [E migrant][61][E species]: single-site energy-change terms, row 60 zero
+  const long long *s_env;  // [slot][3 forms: D, Ks, e0][59][8 ranks]: single-site feature terms, row 58 zero
   // site-pair lookups, strict lower triangles: entry (p, q), p != q, at
-  // Tri(max, min) = max * (max - 1) / 2 + min
-  const uint16_t *px_st;   // [1770]: up to two triplets holding both sites, (label | side << 3) per byte, 0xFF none
-  const uint32_t *px_env;  // [2: MMM, MM2][1653]: feature base | mode << 20 | (lower site is the cluster's
-                           // first) << 22 of the pair cluster, ~0 none
-  const long long *p_de;   // [8][E][E][E]: pair term of a triplet, F(c1, c2) - F(c1, b) - F(b, c2)
+  // Tri(max, min) = max * (max - 1) / 2 + min, one extra "none" entry at the end
+  const uint16_t *px_st;   // [kTriState + 1]: up to two triplets holding both sites, (label | side << 3) per
+                           // byte, 0 none (label 0 rows of p_de are zero)
+  const uint32_t *px_env;  // [2: MMM, MM2][kTriEnv + 1]: feature base | mode << 20 | (lower site is the
+                           // cluster's first) << 22 of the pair cluster; none points at the zero block
+  const long long *p_de;   // [8][E][E][E]: pair term of a triplet, F(c1, c2) - F(c1, b) - F(b, c2); label 0 zero
   const long long *base_de;    // [E] all-base energy change per migrant code
-  const long long *dw_d;       // [slot][f_mmm] W - W(block entry of the base pair type)
-  const long long *dw_ks;      // [slot][f_mm2]
-  const long long *dw_e0;      // [slot][f_mmm]
+  const long long *dw_d;       // [slot][dw_stride_mmm] W - W(block entry of the base pair type), then 64 zeros
+  const long long *dw_ks;      // [slot][dw_stride_mm2]
+  const long long *dw_e0;      // [slot][dw_stride_mmm]
   const long long *base_form;  // [slot][3] all-base sums of D, Ks (forward + backward), e0
+  int dw_stride_mmm, dw_stride_mm2;
   int base_code;
   int center;  // local index of the vacancy site
 };
