@@ -215,19 +215,20 @@ __device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, int kind, in
   JumpOut o;
   o.de = static_cast<double>(acc_de) * t.de_scale;
   const double *f = t.form + slot * 12;
+  // log D (quartic) or log e0 from the MMM sum, log Ks from the MM2 sum
+  const double *fa = f + (kind == 0 ? 0 : 8);
+  const double log_a = fa[2] * (static_cast<double>(acc_d) * fa[0] - fa[1]) + fa[3];
+  const double log_ks = kind == 0 ? f[6] * (static_cast<double>(acc_ks) * f[4] - f[5]) + f[7] : 0.0;
+  const double v = exp(kind == 0 ? log_ks + 2.0 * log_a : log_a);
   if (kind == 0) {
-    const double log_d = f[2] * (static_cast<double>(acc_d) * f[0] - f[1]) + f[3];
-    const double log_ks = f[6] * (static_cast<double>(acc_ks) * f[4] - f[5]) + f[7];
-    const double p = exp(log_ks + 2.0 * log_d);
+    const double p = v;
     const double q = p + 12.0 * o.de;
     o.ea = q * q * (p * p + 8.0 * p * o.de - 48.0 * o.de * o.de) / (64.0 * p * p * p);
-    o.d_or_e0 = log_d;
+    o.d_or_e0 = log_a;
     o.ks = log_ks;
   } else {
-    const double log_e0 = f[10] * (static_cast<double>(acc_d) * f[8] - f[9]) + f[11];
-    const double e0 = exp(log_e0);
-    o.ea = fmax(0.0, e0 + o.de / 2);
-    o.d_or_e0 = e0;
+    o.ea = fmax(0.0, v + o.de / 2);
+    o.d_or_e0 = v;
     o.ks = 0.0;
   }
   return o;
@@ -708,7 +709,7 @@ struct KmcShared {
 
 // 1 / kT and the vacancy-concentration time correction at temperature `temp`
 // (RateCorrector::GetTimeCorrectionFactor, RateCorrector.hpp:17-24; 1 without one).
-__device__ __forceinline__ void TemperatureFactors(const KmcDevState &s, int r, double temp, double *beta,
+__device__ __noinline__ void TemperatureFactors(const KmcDevState &s, int r, double temp, double *beta,
                                                    double *corr) {
   *beta = 1.0 / kBoltzmannEv / temp;
   double c = 1.0;
@@ -831,6 +832,62 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
   return {acc_a, acc_b, bad};
 }
 
+// Dense evaluation of the replica's 12 jumps (warp g takes jumps g, g + G, ...):
+// gathers each jump's sorted state / MMM / MM2 lists into the warp's arrays and
+// sums the cluster tables. Returns the status bits.
+struct DenseArgs {
+  const uint8_t *lst, *lmmm, *lmm2f, *lmm2b;
+  const uint32_t *de, *mmm, *mm2;
+  const SmallTables *small;
+  int8_t *st, *rm, *rf, *rb;
+};
+__device__ __forceinline__ unsigned DenseJumps(const DevTables &t, KmcShared &rs, const DenseArgs &d, int kind, int g,
+                                               int g_per, int lane) {
+  unsigned bad_all = 0;
+  for (int c = g; c < 12; c += g_per) {
+    const uint8_t *lst = d.lst + c * kStateSites;
+    for (int k = lane; k < kStateSites; k += 32) d.st[k] = rs.local[lst[k]];
+    for (int k = lane; k < kEnvSites; k += 32) {
+      d.rm[k] = d.small->rank[rs.local[d.lmmm[c * kEnvSites + k]]];
+      d.rf[k] = d.small->rank[rs.local[d.lmm2f[c * kEnvSites + k]]];
+      d.rb[k] = d.small->rank[rs.local[d.lmm2b[c * kEnvSites + k]]];
+    }
+    __syncwarp();
+    const int mig = d.st[t.pos_second];
+    const int slot = d.small->slot[mig];
+    const bool ok = slot >= 0 && (kind == 0 ? d.small->has_quartic[slot] : d.small->has_e0[slot]);
+    JumpAcc a{0, 0, 0, 0u};
+    if (ok) {
+      a = kind == 0 ? EvalJump<true>(t, slot, d.st, d.rm, d.rf, d.rb, d.de, d.mmm, d.mm2, d.small->pairtype, lane)
+                    : EvalJump<false>(t, slot, d.st, d.rm, d.rf, d.rb, d.de, d.mmm, d.mm2, d.small->pairtype, lane);
+    }
+    const long long v0 = WarpSum(a.de), v1 = WarpSum(a.d), v2 = WarpSum(a.ks);
+    bad_all |= __reduce_or_sync(0xffffffffu, a.bad);
+    if (lane == 0) {
+      rs.acc[c][0] = v0;
+      rs.acc[c][1] = v1;
+      rs.acc[c][2] = v2;
+      // a jump onto another vacancy has no coefficients: rate 0
+      rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+    }
+    __syncwarp();
+  }
+  return bad_all;
+}
+// Out-of-line copy for kernels where the dense evaluation is the rare path.
+__device__ __noinline__ unsigned DenseJumpsCold(const DevTables &t, KmcShared &rs, const DenseArgs &d, int kind, int g,
+                                                int g_per, int lane) {
+  return DenseJumps(t, rs, d, kind, g, g_per, lane);
+}
+
+// The reference's two draws per step on its mt19937_64 stream: u1 for the
+// clock (returned as -log(u1)), then u2 for the selection.
+__device__ __noinline__ double2 MtStepDraws(Mt mt) {
+  const double nlog = -log(MtUniform(mt));  // KineticMcFirstOmp::CalculateTime draws first
+  const double u2 = MtUniform(mt);          // then KineticMcFirstAbstract::SelectEvent
+  return make_double2(nlog, u2);
+}
+
 // Synchronises the warps of one replica only: nothing for a single warp
 // (beyond the warp itself), a named barrier (id 1 + replica slot) otherwise,
 // so replicas sharing a block never wait for one another.
@@ -846,7 +903,8 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
 // 256 threads with a register budget for 4 resident blocks per SM.
 template <bool kSparse, bool kWide>
 __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
-    kmc_kernel(DevTables t, int8_t *species, KmcDevState s, KmcLaunch l) {
+    kmc_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcDevState s,
+               const __grid_constant__ KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
   const int rpb = l.replicas_per_block;
@@ -1036,35 +1094,9 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
       bad_all |= __reduce_or_sync(0xffffffffu, la.bad);
     }
     if (!sparse_step) {
-      for (int c = g; c < 12; c += g_per) {
-        const uint8_t *lst = s_lst + c * kStateSites;
-        for (int k = lane; k < kStateSites; k += 32) st[k] = rs.local[lst[k]];
-        for (int k = lane; k < kEnvSites; k += 32) {
-          rm[k] = s_small->rank[rs.local[s_lmmm[c * kEnvSites + k]]];
-          rf[k] = s_small->rank[rs.local[s_lmm2f[c * kEnvSites + k]]];
-          rb[k] = s_small->rank[rs.local[s_lmm2b[c * kEnvSites + k]]];
-        }
-        __syncwarp();
-        const int mig = st[t.pos_second];
-        const int slot = s_small->slot[mig];
-        const bool ok = slot >= 0 && (s.barrier_kind == 0 ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
-        JumpAcc a{0, 0, 0, 0u};
-        if (ok) {
-          a = s.barrier_kind == 0
-                  ? EvalJump<true>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, s_small->pairtype, lane)
-                  : EvalJump<false>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, s_small->pairtype, lane);
-        }
-        const long long v0 = WarpSum(a.de), v1 = WarpSum(a.d), v2 = WarpSum(a.ks);
-        bad_all |= __reduce_or_sync(0xffffffffu, a.bad);
-        if (lane == 0) {
-          rs.acc[c][0] = v0;
-          rs.acc[c][1] = v1;
-          rs.acc[c][2] = v2;
-          // a jump onto another vacancy has no coefficients: rate 0
-          rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
-        }
-        __syncwarp();
-      }
+      const DenseArgs da{s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_de, s_mmm, s_mm2, s_small, st, rm, rf, rb};
+      bad_all |= kSparse ? DenseJumpsCold(t, rs, da, s.barrier_kind, g, g_per, lane)
+                         : DenseJumps(t, rs, da, s.barrier_kind, g, g_per, lane);
     }
     ReplicaSync(g_per, rl);
     // ---- phase 3: rates, selection, update (warp 0 of the replica) ----
@@ -1117,8 +1149,9 @@ __global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
       double nlog_u1 = 0, u2 = 0;  // -log(u1) for the clock, u2 for the selection
       if (s.rng_kind == 0) {
         if (lane == 0) {
-          nlog_u1 = -log(MtUniform(mt));  // KineticMcFirstOmp::CalculateTime draws first
-          u2 = MtUniform(mt);             // then KineticMcFirstAbstract::SelectEvent
+          const double2 d = MtStepDraws(mt);
+          nlog_u1 = d.x;
+          u2 = d.y;
         }
         u2 = __shfl_sync(0xffffffffu, u2, 0);
       } else {
