@@ -563,15 +563,20 @@ void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
   // thousands of replicas, up to one warp per jump for a single trajectory.
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const long long r = c->num_replicas;
   const long long target = static_cast<long long>(sms) * 24;
   int best = 12;
   for (int cand : {1, 2, 3, 4, 6, 12})
-    if (static_cast<long long>(c->num_replicas) * cand >= target) {
+    if (r * cand >= target) {
       best = cand;
       break;
     }
   *g = best;
-  *rpb = std::max(1, 8 / best);  // 256-thread blocks (the kernel allows up to 384)
+  *rpb = std::max(1, 8 / best);  // 256-thread blocks
+  if (best == 1 && c->kmc_opt.evaluation != LMC_EVAL_DENSE && r <= 28LL * sms) {
+    // one block per SM holding an equal share of the replicas
+    *rpb = static_cast<int>((r + sms - 1) / sms);
+  }
 }
 
 // Block shape and evaluation of the KMC launch from the options (0 = default).
@@ -584,7 +589,8 @@ lmc::KmcLaunch KmcShape(const lmc_ctx *ctx) {
   if (rpb <= 0) rpb = drpb;
   Require(g == 1 || g == 2 || g == 3 || g == 4 || g == 6 || g == 12, LMC_ERR_INVALID_ARGUMENT,
           "warps_per_replica must divide 12");
-  Require(g * rpb <= 12, LMC_ERR_INVALID_ARGUMENT, "at most 12 warps per block (384 threads)");
+  Require(g * rpb <= 12 || (g == 1 && rpb <= 28), LMC_ERR_INVALID_ARGUMENT,
+          "at most 12 warps per block (384 threads), or 28 single-warp replicas");
   Require(g == 1 || rpb <= 15, LMC_ERR_INVALID_ARGUMENT, "at most 15 multi-warp replicas per block");
   l.warps_per_replica = g;
   l.replicas_per_block = rpb;

@@ -899,10 +899,14 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
   }
 }
 
-// kWide: blocks of up to 384 threads (12 warps per replica); otherwise up to
-// 256 threads with a register budget for 4 resident blocks per SM.
-template <bool kSparse, bool kWide>
-__global__ void __launch_bounds__(kWide ? 384 : 256, kWide ? 2 : 4)
+// Block shapes (kShape): 0 up to 256 threads with a register budget for 4
+// resident blocks per SM; 1 up to 384 threads (12 warps per replica), 2
+// resident blocks; 2 one block per SM of up to 28 single-warp replicas (one
+// copy of the staged tables per SM, 72 registers per thread).
+constexpr int kShapeThreads[3] = {256, 384, 896};
+constexpr int kShapeBlocks[3] = {4, 2, 1};
+template <bool kSparse, int kShape>
+__global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     kmc_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcDevState s,
                const __grid_constant__ KmcLaunch l) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1579,36 +1583,38 @@ static cudaError_t PrepareKmc(K kern, size_t sm) {
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
 }
 
+// Kernel instance for the launch shape of `l`.
+using KmcKernelFn = void (*)(DevTables, int8_t *, KmcDevState, KmcLaunch);
+static KmcKernelFn KmcKernelFor(const KmcLaunch &l) {
+  const int threads = l.warps_per_replica * l.replicas_per_block * 32;
+  const int shape = threads <= kShapeThreads[0] ? 0 : (threads <= kShapeThreads[1] ? 1 : 2);
+  if (l.sparse) return shape == 0 ? kmc_kernel<true, 0> : (shape == 1 ? kmc_kernel<true, 1> : kmc_kernel<true, 2>);
+  return shape == 0 ? kmc_kernel<false, 0> : (shape == 1 ? kmc_kernel<false, 1> : kmc_kernel<false, 2>);
+}
+
 cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
+  if (threads > kShapeThreads[2] || (threads > kShapeThreads[1] && l.warps_per_replica != 1))
+    return cudaErrorInvalidConfiguration;
   const size_t sm = KmcSharedBytes(t, l);
-  const bool wide = threads > 256;
-  auto query = [&](auto kern) -> cudaError_t {
-    cudaError_t err = PrepareKmc(kern, sm);
-    if (err != cudaSuccess) return err;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, threads, sm);
-  };
+  const KmcKernelFn kern = KmcKernelFor(l);
+  cudaError_t err = PrepareKmc(kern, sm);
+  if (err != cudaSuccess) return err;
   *shared_bytes = sm;
-  if (l.sparse) return wide ? query(kmc_kernel<true, true>) : query(kmc_kernel<true, false>);
-  return wide ? query(kmc_kernel<false, true>) : query(kmc_kernel<false, false>);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, threads, sm);
 }
 
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                       cudaStream_t stream) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
+  if (threads > kShapeThreads[2] || (threads > kShapeThreads[1] && l.warps_per_replica != 1))
+    return cudaErrorInvalidConfiguration;
   const int blocks = (s.num_replicas + l.replicas_per_block - 1) / l.replicas_per_block;
   const size_t sm = KmcSharedBytes(t, l);
-  const bool wide = threads > 256;
-  auto launch = [&](auto kern) -> cudaError_t {
-    cudaError_t err = PrepareKmc(kern, sm);
-    if (err != cudaSuccess) return err;
-    kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
-    return cudaSuccess;
-  };
-  cudaError_t err;
-  if (l.sparse) err = wide ? launch(kmc_kernel<true, true>) : launch(kmc_kernel<true, false>);
-  else err = wide ? launch(kmc_kernel<false, true>) : launch(kmc_kernel<false, false>);
+  const KmcKernelFn kern = KmcKernelFor(l);
+  cudaError_t err = PrepareKmc(kern, sm);
   if (err != cudaSuccess) return err;
+  kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
   return cudaGetLastError();
 }
 
