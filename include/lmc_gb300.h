@@ -188,6 +188,12 @@ int lmc_energy(lmc_ctx *ctx, int replica, double *energy, int64_t *counts);
  * serialised by the caller. */
 int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *energy_dev);
 
+/* Self-check of the device FP64 helpers the barrier epilogue, the rates and the
+ * clock use (GB300 runs FP64 at 1/64 of the FP32 rate): fn 0 evaluates the
+ * table-driven exponential and CUDA's exp, fn 1 the Newton reciprocal and
+ * 1.0 / x, on n host doubles. No reference counterpart (numerics test hook). */
+int lmc_fastmath_check(lmc_ctx *ctx, int fn, const double *x, int64_t n, double *fast, double *ref);
+
 /* ------------------------------------------------------------------------- */
 /* Kinetic MC (KineticMcFirstOmp semantics, KineticMcAbstract.cpp:140-190)    */
 /* ------------------------------------------------------------------------- */

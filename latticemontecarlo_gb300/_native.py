@@ -123,6 +123,7 @@ SIGNATURES = {
     "lmc_de_pairs": (C.c_int, [_P, C.c_int, _I64P, C.c_int, _DP]),
     "lmc_energy": (C.c_int, [_P, C.c_int, _DP, _I64P]),
     "lmc_energy_noalloc": (C.c_int, [_P, _P, C.c_int, _P]),
+    "lmc_fastmath_check": (C.c_int, [_P, C.c_int, _DP, C.c_int64, _DP, _DP]),
     "lmc_kmc_init": (C.c_int, [_P, _DP, C.POINTER(KmcOptions)]),
     "lmc_kmc_run": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(KmcStep), _DP]),
     "lmc_kmc_get_state": (C.c_int, [_P, _I64P, _U64P, _DP, _DP]),

@@ -361,6 +361,19 @@ void BuildTables(lmc_ctx *c) {
   t.w_ks = c->Upload(wks);
   t.w_e0 = c->Upload(we0);
   t.form = c->Upload(form);
+  // ExpFast constants: 2^(j/256) rounded from extended precision; ln2/256
+  // split into a 34-bit head (exact products with |n| < 2^18) and a tail
+  {
+    std::vector<double> tab(256);
+    for (int j = 0; j < 256; ++j) tab[j] = static_cast<double>(std::exp2(static_cast<long double>(j) / 256.0L));
+    const long double l = std::log(2.0L) / 256.0L;
+    int ex = 0;
+    const long double mant = std::frexp(l, &ex);
+    const long double head = std::ldexp(std::round(std::ldexp(mant, 34)), ex - 34);
+    t.exp_tab = c->Upload(tab);
+    t.exp_l1 = static_cast<double>(head);
+    t.exp_l2 = static_cast<double>(l - head);
+  }
   t.theta = c->Upload(fm.theta);
   t.census_bonds = c->Upload(fm.census_bonds);
 }
@@ -1042,6 +1055,28 @@ int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *e
       if (ctx->model.alphabet[c] == "Al") base = c;
     // LaunchCensus clears the counters it uses before the census kernel runs.
     CudaCheck(lmc::LaunchCensus(ctx->t, species_dev, n, base, scratch, energy_dev, ctx->stream), "census kernel");
+  });
+}
+
+int lmc_fastmath_check(lmc_ctx *ctx, int fn, const double *x, int64_t n, double *fast, double *ref) {
+  return Guard([&] {
+    Require(ctx && x && fast && ref && n >= 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    Require(fn == 0 || fn == 1, LMC_ERR_INVALID_ARGUMENT, "fn must be 0 (exp) or 1 (reciprocal)");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n);
+    DevBuf dx, df, dr;
+    dx.Alloc(bytes);
+    df.Alloc(bytes);
+    dr.Alloc(bytes);
+    CudaCheck(cudaMemcpyAsync(dx.p, x, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(lmc::LaunchFastmathCheck(ctx->t, fn, dx.as<double>(), n, df.as<double>(), dr.as<double>(), ctx->stream),
+              "fastmath kernel");
+    CudaCheck(cudaMemcpyAsync(fast, df.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(ref, dr.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaStreamSynchronize(ctx->stream), "sync");
+    dx.Free();
+    df.Free();
+    dr.Free();
   });
 }
 

@@ -58,6 +58,8 @@ struct DevTables {
   const long long *w_ks;         // [slot][f_mm2]
   const long long *w_e0;         // [slot][f_mmm]
   const double *form;            // [kMaxSlots][12]: {d: scale, c, sigma, mu}, {ks: ...}, {e0: ...}
+  const double *exp_tab;         // [256] 2^(j/256) for ExpFast
+  double exp_l1, exp_l2;         // ln2/256 split for ExpFast
   const double *theta;           // [num_theta]
   const double *census_bonds;    // [num_theta]
 };

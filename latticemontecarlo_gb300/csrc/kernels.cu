@@ -22,6 +22,7 @@
 #include <mutex>
 
 #include "kernels.cuh"
+#include "fastmath.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -210,8 +211,8 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
 struct JumpOut {
   double ea, de, d_or_e0, ks;
 };
-__device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, int kind, int slot, long long acc_de,
-                                                long long acc_d, long long acc_ks) {
+__device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, const ExpConsts &ec, int kind, int slot,
+                                                long long acc_de, long long acc_d, long long acc_ks) {
   JumpOut o;
   o.de = static_cast<double>(acc_de) * t.de_scale;
   const double *f = t.form + slot * 12;
@@ -219,11 +220,11 @@ __device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, int kind, in
   const double *fa = f + (kind == 0 ? 0 : 8);
   const double log_a = fa[2] * (static_cast<double>(acc_d) * fa[0] - fa[1]) + fa[3];
   const double log_ks = kind == 0 ? f[6] * (static_cast<double>(acc_ks) * f[4] - f[5]) + f[7] : 0.0;
-  const double v = exp(kind == 0 ? log_ks + 2.0 * log_a : log_a);
+  const double v = ExpFast(kind == 0 ? log_ks + 2.0 * log_a : log_a, ec);
   if (kind == 0) {
     const double p = v;
     const double q = p + 12.0 * o.de;
-    o.ea = q * q * (p * p + 8.0 * p * o.de - 48.0 * o.de * o.de) / (64.0 * p * p * p);
+    o.ea = q * q * (p * p + 8.0 * p * o.de - 48.0 * o.de * o.de) * RcpFast(64.0 * p * p * p);
     o.d_or_e0 = log_a;
     o.ks = log_ks;
   } else {
@@ -331,7 +332,7 @@ __global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ spe
     const long long acc_de = WarpSum(a.de), acc_d = WarpSum(a.d), acc_ks = WarpSum(a.ks);
     const unsigned b = __reduce_or_sync(0xffffffffu, a.bad);
     if (lane == 0) {
-      const JumpOut o = JumpEpilogue(t, kind, slot, acc_de, acc_d, acc_ks);
+      const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
       ea[p] = o.ea;
       de[p] = o.de;
       if (d_or_e0) d_or_e0[p] = kind == 0 ? exp(o.d_or_e0) : o.d_or_e0;
@@ -924,7 +925,8 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   int8_t *s_loff = reinterpret_cast<int8_t *>(s_lmm2b + 12 * kEnvSites);  // [135][4]
   size_t off = reinterpret_cast<size_t>(s_loff + kLocalSites * 4);
   off = (off + 15) & ~size_t(15);
-  KmcShared *s_rep = reinterpret_cast<KmcShared *>(off);
+  double *s_exp = reinterpret_cast<double *>(off);  // [256] ExpFast table
+  KmcShared *s_rep = reinterpret_cast<KmcShared *>(s_exp + kExpTableSize);
   int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
   // sparse tables follow the per-warp arrays
   uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + rpb * g_per * kArr);        // [4][12][136]
@@ -947,7 +949,9 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   StageArray(t.local_mm2f, s_lmm2f, 12 * kEnvSites);
   StageArray(t.local_mm2b, s_lmm2b, 12 * kEnvSites);
   StageArray(t.local_off, s_loff, kLocalSites * 4);
+  StageArray(t.exp_tab, s_exp, kExpTableSize);
   __syncthreads();
+  const ExpConsts ec{s_exp, t.exp_l1, t.exp_l2};
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rl = warp / g_per;         // replica within block
@@ -1111,10 +1115,11 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
         const int slot = rs.slot[lane];
         id = rs.ids[lane];
         if (slot >= 0) {
-          const JumpOut o = JumpEpilogue(t, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+          const JumpOut o =
+              JumpEpilogue(t, ec, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
           ea = o.ea;
           de = o.de;
-          k = exp(-ea * rs.beta);  // JumpEvent forward rate (JumpEvent.cpp:6-13)
+          k = ExpFast(-ea * rs.beta, ec);  // JumpEvent forward rate (JumpEvent.cpp:6-13)
         } else if (slot == -1) {
           bad_all |= kStatusNoCoefficients;
         }
@@ -1190,7 +1195,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       const double de_sel = __shfl_sync(0xffffffffu, de_s, sel);
       if (lane == 0) {
         if (!(total > 0.0) || !isfinite(total)) bad_all |= kStatusNumeric;
-        const double dt = nlog_u1 / total / kPrefactor * rs.corr;
+        const double dt = nlog_u1 * RcpFast(total * kPrefactor) * rs.corr;
         time += dt;
         energy += de_sel;
         lat[vac] = lat[tgt];  // Config::LatticeJump: the migrating atom takes the vacancy site
@@ -1572,6 +1577,7 @@ size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l) {
   size_t b = 4u * (t.n_de_cl + t.n_mmm_cl + t.n_mm2_cl) + sizeof(SmallTables) + 12 * kStateSites +
              3 * 12 * kEnvSites + kLocalSites * 4;
   b = (b + 15) & ~size_t(15);
+  b += sizeof(double) * kExpTableSize;
   b += sizeof(KmcShared) * l.replicas_per_block;
   b += static_cast<size_t>(kArr) * l.warps_per_replica * l.replicas_per_block;
   if (l.sparse) b += 4 * 12 * 136 + 4 * 2 * (kTriEnv + 1) + 4 * kLocalSites * kInterWords + 2 * (kTriState + 1);
@@ -1642,6 +1648,25 @@ cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTp
   void *args[] = {&tt, &sp, &aa};
   return cudaLaunchCooperativeKernel(reinterpret_cast<void *>(cmc_tp_kernel), blocks, kCmcTpThreads, args, sm,
                                      stream);
+}
+
+// Self-check of the FP64 helpers: fn 0 ExpFast / exp, fn 1 RcpFast / 1.0 / x.
+__global__ void fastmath_check_kernel(DevTables t, int fn, const double *x, long long n, double *fast, double *ref) {
+  const ExpConsts ec{t.exp_tab, t.exp_l1, t.exp_l2};
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double v = x[i];
+    fast[i] = fn == 0 ? ExpFast(v, ec) : RcpFast(v);
+    ref[i] = fn == 0 ? exp(v) : 1.0 / v;
+  }
+}
+
+cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, long long n, double *fast, double *ref,
+                                cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = (n + 255) / 256;
+  fastmath_check_kernel<<<static_cast<int>(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(t, fn, x, n, fast, ref);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

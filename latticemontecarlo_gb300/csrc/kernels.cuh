@@ -111,6 +111,9 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                       cudaStream_t stream);
 size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
+// fn 0: ExpFast and exp; fn 1: RcpFast and 1 / x, over n device doubles.
+cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, long long n, double *fast, double *ref,
+                                cudaStream_t stream);
 // Resident blocks per SM and dynamic shared memory of the KMC launch `l`.
 cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes);
 
