@@ -59,6 +59,19 @@ __device__ __forceinline__ long long NeighborId(H3 h, int dx, int dy, int dz, in
   return static_cast<long long>(x) * 2 * n * n + static_cast<long long>(y) * n + (z >> 1);
 }
 
+// h + (dx, dy, dz) with periodic wrap (half units); |offset| <= 4 < 2n.
+__device__ __forceinline__ H3 WrapCoord(H3 h, int dx, int dy, int dz, int n) {
+  const int m = 2 * n;
+  int x = h.x + dx, y = h.y + dy, z = h.z + dz;
+  x += (x < 0) ? m : 0;
+  x -= (x >= m) ? m : 0;
+  y += (y < 0) ? m : 0;
+  y -= (y >= m) ? m : 0;
+  z += (z < 0) ? m : 0;
+  z -= (z >= m) ? m : 0;
+  return {x, y, z};
+}
+
 __device__ __forceinline__ int MinImage(int d, int n) {
   const int m = 2 * n;
   d %= m;
@@ -701,6 +714,7 @@ struct KmcShared {
   double beta;
   double corr;
   int stop;
+  int dsel;                         // direction index of the selected jump
   int nbk;                          // non-base sites in the neighbourhood (sparse evaluation)
   int npairs;                       // pairs of them that share a cluster in some jump
   uint8_t nb_l[kMaxSparseSites + 1];    // their local indices; padding: kLocalSites (in no list)
@@ -805,10 +819,10 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
   }
   // pair terms over the pairs that share a cluster in some jump
   const int n_pairs = rs.npairs;
-  for (int i0 = 0; i0 < n_pairs; i0 += 4) {
-    long long va[4], vb[4];
+  for (int i0 = 0; i0 < n_pairs; i0 += 2) {
+    long long va[2], vb[2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
       const unsigned pk = rs.pairs[i0 + u];
       const int k = pk & 0xFF, k2 = pk >> 8;
       const int l = rs.nb_l[k], l2 = rs.nb_l[k2];
@@ -827,8 +841,8 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
       }
       vb[u] = EnvPairTerm(px_b[both_b ? Tri(pb, qb) : kTriEnv], w_b, pb, qb, rp, rq, rb0, sm->pairtype);
     }
-    acc_a += (va[0] + va[1]) + (va[2] + va[3]);
-    acc_b += (vb[0] + vb[1]) + (vb[2] + vb[3]);
+    acc_a += va[0] + va[1];
+    acc_b += vb[0] + vb[1];
   }
   return {acc_a, acc_b, bad};
 }
@@ -990,10 +1004,11 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   const int e = t.num_species;
   if (!active) return;  // no block-wide barrier below this point
   if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
+  H3 hv = SiteCoord(vac, n);  // vacancy coordinates, advanced by the selected direction each step
   for (unsigned long long it = 0; it < l.steps; ++it) {
     // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
     if (active) {
-      const H3 h = SiteCoord(vac, n);
+      const H3 h = hv;
       for (int k = g * 32 + lane; k < kLocalSites; k += g_per * 32) {
         const int8_t *o = s_loff + k * 4;
         rs.local[k] = lat[NeighborId(h, o[0], o[1], o[2], n)];
@@ -1190,6 +1205,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       }
       const unsigned ballot = __ballot_sync(0xffffffffu, hit);
       const int sel = ballot ? __ffs(ballot) - 1 : 11;  // past the end: the last event
+      const int dsel = __shfl_sync(0xffffffffu, src, sel);
       const long long tgt = __shfl_sync(0xffffffffu, id_s, sel);
       const double ea_sel = __shfl_sync(0xffffffffu, ea_s, sel);
       const double de_sel = __shfl_sync(0xffffffffu, de_s, sel);
@@ -1214,6 +1230,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
           l.trace[it] = rec;
         }
         rs.ids[0] = tgt;
+        rs.dsel = dsel;
       }
       if (r == l.trace_replica && l.events12 && lane < 12) {
         double *ev = l.events12 + it * 36 + lane * 3;
@@ -1225,6 +1242,10 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     }
     ReplicaSync(g_per, rl);
     if (active && g != 0) vac = rs.ids[0];
+    {
+      const int8_t *o = t.dir + rs.dsel * 4;
+      hv = WrapCoord(hv, o[0], o[1], o[2], n);
+    }
     ++steps_done;
     ReplicaSync(g_per, rl);
   }
