@@ -36,6 +36,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "KMC events/s and CMC swaps/s at 1 GB300; surrogate vs plain at <=5 meV barrier MAE"
 KMC_STEPS_PER_BENCH_STEP = 1000
 BYTES_PER_EVENT = 225       # algorithmic HBM bytes per KMC event
+# DRAM bytes (read + write) of one full-size kmc_kernel launch (4096 replicas x 1000 steps), one ncu
+# capture with the L2 flushed before the launch; the command and figures are in the kmc_kernel
+# summary under profiles/. The lattices and tables stay in L2, hence far below the algorithmic bytes.
+KMC_TRAFFIC_PER_LAUNCH = 53.52e6 + 4.68e6
 BYTES_PER_ATTEMPT = 100     # algorithmic HBM bytes per CMC attempt
 L2_BYTES = 129 * 1024 * 1024
 
@@ -195,6 +199,9 @@ def run_ours(args, rank, world, local):
     peak, peak_kind = peaks()
     launch_ms = t_ms / args.steps
     achieved = BYTES_PER_EVENT * events_per_step / (launch_ms / 1e3) / 1e9
+    traffic = args.traffic
+    if traffic is None and args.replicas == 4096 and args.kmc_steps_per_launch == KMC_STEPS_PER_BENCH_STEP:
+        traffic = KMC_TRAFFIC_PER_LAUNCH
     result = {
         "metric": METRIC,
         "value": value,
@@ -216,7 +223,7 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": args.traffic, "peak_source": peak_kind,
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "kmc_kernel", "bytes_per_event": BYTES_PER_EVENT},
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
