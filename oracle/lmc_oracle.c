@@ -1335,12 +1335,51 @@ static uint64_t fnv(const uint8_t *k, int n) {
   return h;
 }
 
+/* TimeTemperatureInterpolator::GetTemperature (TimeTemperatureInterpolator.cpp:44-65):
+ * first point with time >= t (std::lower_bound), clamped at both ends, linear between. */
+static double interp_temperature(const double *tt, const double *tv, int len, double t) {
+  int lo = 0;
+  while (lo < len && tt[lo] < t) ++lo;
+  if (lo == len) return tv[len - 1];
+  if (lo == 0 && t <= tt[0]) return tv[0];
+  const double ux = tt[lo], uy = tv[lo], lx = tt[lo - 1], ly = tv[lo - 1];
+  const double dy = uy - ly, dx = ux - lx;
+  return ly + ((t - lx) / dx) * dy;
+}
+
+/* RateCorrector::GetTimeCorrectionFactor (RateCorrector.hpp:17-24). */
+static double time_correction(double cvac, double csol, double T) {
+  const double cv = 1.64 * exp(-(0.66 / kBoltzmann / T - 0.7));
+  return cvac / cv / (1 - 13 * csol);
+}
+
 int orc_kmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps, int kind,
             int memo, double *trace8, double *events36) {
+  return orc_kmc_ex(m, lat, sp, T, seed, steps, kind, memo, trace8, events36, NULL, NULL, 0, 0);
+}
+
+int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
+               int kind, int memo, double *trace8, double *events36, const double *tt_time, const double *tt_temp,
+               int tt_len, int rate_corrector) {
   orc_mt g;
   orc_mt_seed(&g, seed);
   const mappings *mp = maps_for(m, lat);
-  const double beta = 1.0 / kBoltzmann / T;
+  double beta = 1.0 / kBoltzmann / T;
+  /* RateCorrector(config.GetVacancyConcentration(), config.GetSoluteConcentration(Element("Al")))
+   * (KineticMcAbstract.cpp:35; Config.cpp:373-391) */
+  double cvac = 0.0, csol = 0.0;
+  if (rate_corrector) {
+    int al = -1;
+    for (int c = 0; c < m->E; ++c)
+      if (strcmp(m->names[c], "Al") == 0) al = c;
+    int64_t nx = 0, ns = 0;
+    for (int64_t i = 0; i < lat->N; ++i) {
+      if (sp[i] == m->x_code) ++nx;
+      else if (sp[i] != al) ++ns;
+    }
+    cvac = (double)nx / (double)lat->N;
+    csol = (double)ns / (double)lat->N;
+  }
   /* GetVacancyLatticeId: first X in atom order (Config.cpp:298-310) */
   int64_t vac = -1;
   for (int64_t at = 0; at < lat->N && vac < 0; ++at)
@@ -1358,6 +1397,11 @@ int orc_kmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, ui
   double time = 0.0, energy = 0.0;
   int rc = 0;
   for (int64_t st = 0; st < steps && !rc; ++st) {
+    /* KineticMcFirstAbstract::UpdateTemperature (KineticMcAbstract.cpp:45-50) */
+    if (tt_len > 0) {
+      T = interp_temperature(tt_time, tt_temp, tt_len, time);
+      beta = 1.0 / kBoltzmann / T;
+    }
     double ea[12], de[12], k[12];
     const int64_t *nb = lat->nn[vac];
     double total = 0.0;
@@ -1419,7 +1463,8 @@ int orc_kmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, ui
       cum[i] = cp;
     }
     const double u1 = orc_mt_uniform(&g);
-    const double dt = -log(u1) / total / kPrefactor;
+    /* CalculateTime() * GetTimeCorrectionFactor() (KineticMcAbstract.cpp:52-57,146) */
+    const double dt = -log(u1) / total / kPrefactor * (rate_corrector ? time_correction(cvac, csol, T) : 1.0);
     const double u2 = orc_mt_uniform(&g);
     int sel = 11;
     for (int i = 0; i < 12; ++i)
