@@ -211,6 +211,9 @@ typedef struct lmc_kmc_options {
   int warps_per_replica;   /* 0 = autotuned */
   int replicas_per_block;  /* 0 = autotuned */
   int evaluation;          /* LMC_EVAL_SPARSE (default) or LMC_EVAL_DENSE; identical results */
+  int early_stop;          /* IsEscaped (KineticMcAbstract.cpp:192-223): a replica whose vacancy has only
+                              solvent (its most frequent element) in the 1-3NN shells completes that step
+                              and takes no further steps */
 } lmc_kmc_options;
 
 /* Jump evaluation inside the KMC kernel: both give bit-identical barriers.
@@ -241,6 +244,8 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
 int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace, double *events12);
 /* Per-replica state (any pointer may be NULL). */
 int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy);
+/* Per replica 1 when its trajectory ended by the early stop (KineticMcAbstract.cpp:213-220), else 0. */
+int lmc_kmc_get_escaped(lmc_ctx *ctx, uint8_t *escaped);
 /* Device time (ms) of the last lmc_kmc_run / lmc_cmc_run launch (CUDA events on the context stream). */
 int lmc_last_run_ms(lmc_ctx *ctx, double *ms);
 /* Launch shape of lmc_kmc_run under the current options: warps per replica,

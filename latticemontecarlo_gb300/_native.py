@@ -65,6 +65,7 @@ class KmcOptions(C.Structure):
         ("rng", C.c_int), ("seed", C.c_uint64), ("barrier_kind", C.c_int), ("rate_corrector", C.c_int),
         ("tt_time", C.POINTER(C.c_double)), ("tt_temp", C.POINTER(C.c_double)), ("tt_len", C.c_int),
         ("warps_per_replica", C.c_int), ("replicas_per_block", C.c_int), ("evaluation", C.c_int),
+        ("early_stop", C.c_int),
     ]
 
 
@@ -127,6 +128,7 @@ SIGNATURES = {
     "lmc_kmc_init": (C.c_int, [_P, _DP, C.POINTER(KmcOptions)]),
     "lmc_kmc_run": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(KmcStep), _DP]),
     "lmc_kmc_get_state": (C.c_int, [_P, _I64P, _U64P, _DP, _DP]),
+    "lmc_kmc_get_escaped": (C.c_int, [_P, C.POINTER(C.c_uint8)]),
     "lmc_last_run_ms": (C.c_int, [_P, _DP]),
     "lmc_kmc_launch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _I64P]),
     "lmc_cmc_run": (C.c_int, [_P, C.c_int, C.c_double, C.c_uint64, C.POINTER(CmcOptions), _DP, _U64P, _U64P]),

@@ -170,11 +170,11 @@ class Context:
     # kinetic MC -----------------------------------------------------------
     def kmc_init(self, temperatures, seed: int = 0, rng: int = N.LMC_RNG_PHILOX, kind: int = N.LMC_BARRIER_QUARTIC,
                  rate_corrector: bool = False, tt=None, warps_per_replica: int = 0, replicas_per_block: int = 0,
-                 evaluation: int = N.LMC_EVAL_SPARSE):
+                 evaluation: int = N.LMC_EVAL_SPARSE, early_stop: bool = False):
         temps = np.ascontiguousarray(np.broadcast_to(np.asarray(temperatures, np.float64), (self.ns.size,)))
         self._tt = None
         opt = N.KmcOptions(rng, seed, kind, int(rate_corrector), None, None, 0, warps_per_replica,
-                           replicas_per_block, evaluation)
+                           replicas_per_block, evaluation, int(early_stop))
         if tt is not None:
             t0, t1 = _f64(tt[0]), _f64(tt[1])
             self._tt = (t0, t1)
@@ -204,6 +204,12 @@ class Context:
         check(N.lib.lmc_kmc_launch_info(self._h, C.byref(g), C.byref(rpb), C.byref(per_sm), ptr(smem, C.c_int64)))
         return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "blocks_per_sm": per_sm.value,
                 "shared_bytes": int(smem[0])}
+
+    def kmc_escaped(self) -> np.ndarray:
+        """Per replica True when the early stop ended its trajectory."""
+        out = np.zeros(self.ns.size, np.uint8)
+        check(N.lib.lmc_kmc_get_escaped(self._h, ptr(out, C.c_uint8)))
+        return out.astype(bool)
 
     def last_run_ms(self) -> float:
         ms = C.c_double()

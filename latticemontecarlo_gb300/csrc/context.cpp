@@ -116,6 +116,7 @@ struct lmc_ctx {
   bool kmc_ready{false};
   lmc_kmc_options kmc_opt{};
   DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
+  DevBuf k_solvent, k_escaped;
   int tt_len{0};
   // sparse KMC tables (built for the dominant species at lmc_kmc_init)
   std::vector<DevBuf> sparse_bufs;
@@ -132,7 +133,7 @@ struct lmc_ctx {
     for (auto &b : tables) b.Free();
     for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
-                      &k_tt_time, &k_tt_temp, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -321,6 +322,14 @@ void BuildTables(lmc_ctx *c) {
   t.mm2_off = c->Upload(mm2_off);
   t.site_off = c->Upload(site_off);
   t.local_off = c->Upload(local_off);
+  {
+    std::vector<uint8_t> shell;
+    for (int sh = 1; sh <= 3; ++sh)
+      for (const auto &o : lmc::ShellOffsets(sh)) shell.push_back(lidx(o));
+    Require(shell.size() == 42, LMC_ERR_UNSUPPORTED, "unexpected neighbour shells");
+    for (uint8_t v : shell) Require(v < lmc::kLocalSites, LMC_ERR_UNSUPPORTED, "shell site outside the neighbourhood");
+    t.shell_local = c->Upload(shell);
+  }
   t.local_st = c->Upload(l_st);
   t.local_mmm = c->Upload(l_mmm);
   t.local_mm2f = c->Upload(l_mm2f);
@@ -1099,6 +1108,9 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     ctx->k_cvac.Ensure(sizeof(double) * R);
     ctx->k_csol.Ensure(sizeof(double) * R);
     ctx->k_rng.Ensure(sizeof(uint32_t) * lmc::kRngWords * R);
+    ctx->k_solvent.Ensure(R);
+    ctx->k_escaped.Ensure(R);
+    CudaCheck(cudaMemsetAsync(ctx->k_escaped.p, 0, R, ctx->stream), "memset");
     // first vacancy and species histogram of every replica
     DevBuf hist;
     hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * R);
@@ -1128,6 +1140,16 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
         if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || tot[c] > tot[base])) base = c;
       Require(base >= 0, LMC_ERR_INVALID_ARGUMENT, "no element of the barrier set in the lattices");
       BuildSparse(ctx, base);
+    }
+    {
+      // Config::GetSolventElement (Config.cpp:411-422): most frequent species per replica
+      std::vector<int8_t> solvent(R, 0);
+      for (int r = 0; r < R; ++r)
+        for (int c = 1; c < ctx->fm.num_species; ++c)
+          if (h[r * (lmc::kMaxSpecies + 1) + c] > h[r * (lmc::kMaxSpecies + 1) + solvent[r]])
+            solvent[r] = static_cast<int8_t>(c);
+      CudaCheck(cudaMemcpyAsync(ctx->k_solvent.p, solvent.data(), R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      ctx->Sync();
     }
     const int al = ctx->model.Code("Al");
     std::vector<double> cvac(R, -1.0), csol(R, 0.0);
@@ -1215,6 +1237,9 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     s.temperature = ctx->k_temp.as<double>();
     s.corr_cvac = ctx->k_cvac.as<double>();
     s.corr_csol = ctx->k_csol.as<double>();
+    s.early_stop = ctx->kmc_opt.early_stop ? 1 : 0;
+    s.solvent = ctx->k_solvent.as<int8_t>();
+    s.escaped = ctx->k_escaped.as<uint8_t>();
     s.rng = ctx->k_rng.as<uint32_t>();
     s.lat_off = ctx->lat_off.as<long long>();
     s.lat_n = ctx->lat_n.as<int>();
@@ -1256,6 +1281,16 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
     ctx->last_ms = ms;
     RaiseStatus(st, "KMC run");
+  });
+}
+
+int lmc_kmc_get_escaped(lmc_ctx *ctx, uint8_t *escaped) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready && escaped, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CudaCheck(cudaMemcpyAsync(escaped, ctx->k_escaped.p, ctx->num_replicas, cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
+    ctx->Sync();
   });
 }
 

@@ -715,6 +715,7 @@ struct KmcShared {
   double corr;
   int stop;
   int dsel;                         // direction index of the selected jump
+  int escaped;                      // early stop: this step's vacancy had only solvent in its 1-3NN shells
   int nbk;                          // non-base sites in the neighbourhood (sparse evaluation)
   int npairs;                       // pairs of them that share a cluster in some jump
   uint8_t nb_l[kMaxSparseSites + 1];    // their local indices; padding: kLocalSites (in no list)
@@ -1002,7 +1003,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     mt.idx = w + 2 * 312;
   }
   const int e = t.num_species;
-  if (!active) return;  // no block-wide barrier below this point
+  if (!active || (s.early_stop && s.escaped[r])) return;  // no block-wide barrier below this point
   if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
   H3 hv = SiteCoord(vac, n);  // vacancy coordinates, advanced by the selected direction each step
   for (unsigned long long it = 0; it < l.steps; ++it) {
@@ -1232,6 +1233,14 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
         rs.ids[0] = tgt;
         rs.dsel = dsel;
       }
+      if (s.early_stop) {
+        // IsEscaped on the configuration before the jump (rs.local is this step's gather)
+        const int sv = s.solvent[r];
+        bool solvent_only = rs.local[t.shell_local[lane]] == sv;
+        if (lane < 10) solvent_only = solvent_only && rs.local[t.shell_local[32 + lane]] == sv;
+        const bool esc = __all_sync(0xffffffffu, solvent_only);
+        if (lane == 0) rs.escaped = esc ? 1 : 0;
+      }
       if (r == l.trace_replica && l.events12 && lane < 12) {
         double *ev = l.events12 + it * 36 + lane * 3;
         ev[0] = static_cast<double>(id_s);
@@ -1247,7 +1256,12 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       hv = WrapCoord(hv, o[0], o[1], o[2], n);
     }
     ++steps_done;
+    const bool escaped_now = s.early_stop && rs.escaped;
     ReplicaSync(g_per, rl);
+    if (escaped_now) {
+      if (leader) s.escaped[r] = 1;
+      break;
+    }
   }
   if (active && leader) {
     s.vacancy[r] = vac;

@@ -27,6 +27,9 @@ struct KmcDevState {
   const double *tt_time;      // optional T(t) table
   const double *tt_temp;
   int tt_len;
+  int early_stop;             // IsEscaped: stop a replica whose vacancy is surrounded by solvent
+  const int8_t *solvent;      // per replica: most frequent species code
+  uint8_t *escaped;           // per replica: 1 once the early stop ended the trajectory
 };
 
 constexpr int kRngWords = 2 * 312 + 2;  // MT19937-64 state (312 x u64) + index; Philox uses 4 words

@@ -1355,12 +1355,24 @@ static double time_correction(double cvac, double csol, double T) {
 
 int orc_kmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps, int kind,
             int memo, double *trace8, double *events36) {
-  return orc_kmc_ex(m, lat, sp, T, seed, steps, kind, memo, trace8, events36, NULL, NULL, 0, 0);
+  return orc_kmc_ex(m, lat, sp, T, seed, steps, kind, memo, trace8, events36, NULL, NULL, 0, 0, 0, NULL);
+}
+
+/* Config::GetSolventElement (Config.cpp:411-422): the most frequent element. */
+static int solvent_code(const orc_model *m, const orc_lattice *lat, const int8_t *sp) {
+  int64_t count[MAXE] = {0};
+  for (int64_t i = 0; i < lat->N; ++i) ++count[sp[i]];
+  int best = 0;
+  for (int c = 1; c < m->E; ++c)
+    if (count[c] > count[best]) best = c;
+  return best;
 }
 
 int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
                int kind, int memo, double *trace8, double *events36, const double *tt_time, const double *tt_temp,
-               int tt_len, int rate_corrector) {
+               int tt_len, int rate_corrector, int early_stop, int64_t *steps_done) {
+  const int solvent = early_stop ? solvent_code(m, lat, sp) : -1;
+  if (steps_done) *steps_done = 0;
   orc_mt g;
   orc_mt_seed(&g, seed);
   const mappings *mp = maps_for(m, lat);
@@ -1492,9 +1504,19 @@ int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T,
       t[6] = time;
       t[7] = energy;
     }
+    /* KineticMcFirstAbstract::IsEscaped (KineticMcAbstract.cpp:192-223): checked on the
+     * configuration before the jump; the step completes, then the run ends */
+    int escaped = 0;
+    if (early_stop) {
+      escaped = 1;
+      for (int q = 0; q < 42; ++q)
+        if (sp[nb[q]] != solvent) escaped = 0;
+    }
     sp[vac] = sp[j];
     sp[j] = (int8_t)m->x_code;
     vac = j;
+    if (steps_done) *steps_done = st + 1;
+    if (escaped) break;
   }
   free(tab);
   free(itab);

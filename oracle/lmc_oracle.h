@@ -104,11 +104,12 @@ uint64_t orc_mt_below(orc_mt *g, uint64_t range);  /* uniform_int_distribution<s
 int orc_kmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps, int kind,
             int memo, double *trace8, double *events36);
 /* orc_kmc with a time-temperature schedule (tt_len > 0: T(t) interpolated as
- * TimeTemperatureInterpolator does, at the start of every step) and the
- * RateCorrector time factor (rate_corrector != 0). */
+ * TimeTemperatureInterpolator does, at the start of every step), the
+ * RateCorrector time factor (rate_corrector != 0) and the IsEscaped early stop
+ * (early_stop != 0); steps_done (nullable) receives the steps executed. */
 int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
                int kind, int memo, double *trace8, double *events36, const double *tt_time, const double *tt_temp,
-               int tt_len, int rate_corrector);
+               int tt_len, int rate_corrector, int early_stop, int64_t *steps_done);
 
 /* CanonicalMcOmp with batch size `batch` (CanonicalMcOmp.cpp:40-92,
  * CanonicalMcAbstract.cpp:43-101): runs until `attempts` Metropolis tests were

@@ -70,7 +70,7 @@ def lib() -> C.CDLL:
             "orc_energy": (C.c_int, [P, P, I8P, I64P, DP]),
             "orc_kmc": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, DP, DP]),
             "orc_kmc_ex": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, DP, DP, DP, DP,
-                                     C.c_int, C.c_int]),
+                                     C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]),
             "orc_cmc": (I64, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, DP, DP, I64, I64P]),
         }
         for name, (res, args) in sig.items():
@@ -231,21 +231,26 @@ def energy(model: Model, lat: Lattice, species):
 
 
 def kmc(model: Model, lat: Lattice, species, T: float, seed: int, steps: int, kind: int = 0, memo: bool = False,
-        events: bool = False, tt=None, rate_corrector: bool = False):
+        events: bool = False, tt=None, rate_corrector: bool = False, early_stop: bool = False):
     """Runs the restated KineticMcFirstOmp loop; species is modified in place.
-    tt = (times, temperatures) enables the time-temperature schedule."""
+    tt = (times, temperatures) enables the time-temperature schedule. With
+    early_stop the trace is cut at the escape step (IsEscaped)."""
     trace = np.zeros((steps, 8))
     ev = np.zeros((steps, 12, 3)) if events else None
     t0 = t1 = None
+    done = C.c_int64()
     if tt is not None:
         t0 = np.ascontiguousarray(tt[0], dtype=np.float64)
         t1 = np.ascontiguousarray(tt[1], dtype=np.float64)
     rc = lib().orc_kmc_ex(model.h, lat.h, _sp(species), T, seed, steps, kind, int(memo), _p(trace, C.c_double),
                           _p(ev, C.c_double) if events else None, _p(t0, C.c_double) if t0 is not None else None,
                           _p(t1, C.c_double) if t1 is not None else None, 0 if t0 is None else t0.size,
-                          int(rate_corrector))
+                          int(rate_corrector), int(early_stop), C.byref(done))
     if rc:
         raise OracleError(f"orc_kmc rc={rc}")
+    if early_stop:
+        trace = trace[:done.value]
+        ev = ev[:done.value] if ev is not None else None
     return trace, ev
 
 

@@ -77,3 +77,21 @@ def test_kmc_stop_flag(native, golden, oracle_mod):
     ref, _ = oracle_mod.kmc(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, 120)
     _compare(tr, ref)
     assert ctx.kmc_state()[1][0] == 120
+
+
+@pytest.mark.parametrize("evaluation", [0, 1])
+def test_kmc_early_stop(native, golden, oracle_mod, evaluation):
+    """IsEscaped: with seed 103 the oracle's trajectory escapes at step 193 (the
+    vacancy's 1-3NN shells hold only the solvent); the GPU run stops there too
+    and later launches leave the replica untouched."""
+    G, ctx, lat, m, sp = _setup(native, golden, oracle_mod)
+    ref, _ = oracle_mod.kmc(m, lat, sp.copy(), G.KMC_T, 103, 500, early_stop=True)
+    assert 0 < len(ref) < 500
+    ctx.kmc_init([G.KMC_T], seed=103, rng=native.LMC_RNG_MT19937_64, early_stop=True, evaluation=evaluation)
+    tr, _ = ctx.kmc_run(500, trace_replica=0)
+    _compare(tr[:len(ref)], ref)
+    assert ctx.kmc_state()[1][0] == len(ref) and ctx.kmc_escaped()[0]
+    before = ctx.get_lattices().copy()
+    ctx.kmc_run(50)
+    assert ctx.kmc_state()[1][0] == len(ref)
+    assert np.array_equal(ctx.get_lattices(), before)
