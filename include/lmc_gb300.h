@@ -266,6 +266,9 @@ typedef struct lmc_cmc_options {
   uint64_t seed;
   int batch;         /* reference-batch mode: pairs per batch (the OpenMP thread count) */
   int candidates;    /* throughput mode: candidate pairs per round, 0 = automatic */
+  double *energy_trace; /* reference-batch mode, optional host array of attempts + batch doubles: the
+                           energy before every Metropolis test (what CanonicalMcOmp::Simulate hands to
+                           ThermodynamicAveraging::AddEnergy and Dump, CanonicalMcOmp.cpp:82-90) */
 } lmc_cmc_options;
 
 /* Runs CMC on one replica until at least `attempts` Metropolis tests were made.

@@ -78,7 +78,8 @@ class KmcStep(C.Structure):
 
 
 class CmcOptions(C.Structure):
-    _fields_ = [("mode", C.c_int), ("seed", C.c_uint64), ("batch", C.c_int), ("candidates", C.c_int)]
+    _fields_ = [("mode", C.c_int), ("seed", C.c_uint64), ("batch", C.c_int), ("candidates", C.c_int),
+                ("energy_trace", C.POINTER(C.c_double))]
 
 
 _P = C.c_void_p

@@ -219,7 +219,7 @@ class Context:
     # canonical MC ---------------------------------------------------------
     def cmc_run(self, temperature: float, attempts: int, replica: int = 0, mode: int = N.LMC_CMC_THROUGHPUT,
                 seed: int = 0, batch: int = 1, candidates: int = 0, energy: float = 0.0):
-        opt = N.CmcOptions(mode, seed, batch, candidates)
+        opt = N.CmcOptions(mode, seed, batch, candidates, None)
         e = C.c_double(energy)
         done, acc = C.c_uint64(), C.c_uint64()
         check(N.lib.lmc_cmc_run(self._h, replica, temperature, attempts, C.byref(opt), C.byref(e), C.byref(done),

@@ -37,6 +37,33 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
 
 
+HOST = PKG / "host"
+EXE = PKG / "bin" / "lmc_gb300"
+
+
+def _has_zlib() -> bool:
+    proc = subprocess.run(["g++", "-x", "c++", "-E", "-"], input="#include <zlib.h>\n", capture_output=True, text=True)
+    return proc.returncode == 0
+
+
+def build_host(verbose: bool = False, force: bool = False) -> Path:
+    """The C++ host mirror (lmc_host.cpp) and the `lmc_gb300 -p param.txt` executable,
+    linked against liblmc_gb300.so (rpath to the package directory)."""
+    sources = [HOST / "lmc_host.cpp", HOST / "main.cpp"]
+    inputs = sources + [HOST / "lmc_host.hpp", ROOT / "include" / "lmc_gb300.h", LIB]
+    if EXE.exists() and not force and EXE.stat().st_mtime >= max(p.stat().st_mtime for p in inputs):
+        return EXE
+    EXE.parent.mkdir(exist_ok=True)
+    libs = ["-lz"] if _has_zlib() else []
+    tmp = EXE.with_suffix(".tmp")
+    _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", str(HOST), *map(str, sources), "-o", str(tmp), "-L", str(PKG),
+          "-llmc_gb300", "-Wl,-rpath,$ORIGIN/..", *libs])
+    os.replace(tmp, EXE)
+    if verbose:
+        print(f"built {EXE}", file=sys.stderr)
+    return EXE
+
+
 def build(verbose: bool = False, force: bool = False) -> Path:
     cuda = cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
@@ -72,3 +99,4 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
 if __name__ == "__main__":
     build(verbose="-v" in sys.argv, force="-f" in sys.argv)
+    build_host(verbose="-v" in sys.argv, force="-f" in sys.argv)

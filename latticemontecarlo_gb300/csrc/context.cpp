@@ -116,7 +116,7 @@ struct lmc_ctx {
   bool kmc_ready{false};
   lmc_kmc_options kmc_opt{};
   DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
-  DevBuf k_solvent, k_escaped;
+  DevBuf k_solvent, k_escaped, c_trace;
   int tt_len{0};
   // sparse KMC tables (built for the dominant species at lmc_kmc_init)
   std::vector<DevBuf> sparse_bufs;
@@ -133,7 +133,7 @@ struct lmc_ctx {
     for (auto &b : tables) b.Free();
     for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
-                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -1379,10 +1379,19 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
       a.done = d_done;
       a.accepted = d_done + 1;
       a.status = ctx->status.as<int>();
+      const size_t trace_n = static_cast<size_t>(attempts) + opt->batch;
+      if (opt->energy_trace) {
+        ctx->c_trace.Ensure(sizeof(double) * trace_n);
+        a.energy_trace = ctx->c_trace.as<double>();
+      }
       CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
       CudaCheck(lmc::LaunchCmcReference(ctx->t, lat, a, ctx->stream), "CMC kernel");
       CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
       CudaCheck(cudaMemcpyAsync(&e_out, d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+      if (opt->energy_trace)
+        CudaCheck(cudaMemcpyAsync(opt->energy_trace, ctx->c_trace.p, sizeof(double) * trace_n, cudaMemcpyDeviceToHost,
+                                  ctx->stream),
+                  "D2H");
     } else if (opt->mode == LMC_CMC_THROUGHPUT) {
       int cand = opt->candidates;
       if (cand <= 0) cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, nsites / 256)));

@@ -1361,6 +1361,7 @@ __global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
     if (lane == 0) {
       for (int i = 0; i < nb; ++i) {
         const double dE = s_de[i];
+        if (a.energy_trace) a.energy_trace[done] = energy;
         bool acc = dE < 0;
         if (!acc) acc = MtUniform(mt) < exp(-dE * a.beta);
         if (acc) {

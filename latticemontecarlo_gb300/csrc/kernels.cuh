@@ -130,6 +130,7 @@ struct CmcRefArgs {
   unsigned char *mark;       // N bytes scratch, zero on entry and on exit
   long long *mark_list;      // batch * 86 entries scratch
   double *energy;            // in/out
+  double *energy_trace;      // optional: energy before every test (attempts + batch entries)
   unsigned long long *done;  // attempts done
   unsigned long long *accepted;
   int *status;

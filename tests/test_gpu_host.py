@@ -1,0 +1,155 @@
+"""C++ host mirror on the GPU, against the reference's golden vectors and the oracle:
+
+* the predictor classes (pred::VacancyMigrationPredictorQuarticLru / E0,
+  EnergyChangePredictorPairSite, EnergyPredictor) with the reference's
+  signatures, on a CFG file read by cfg::Config::ReadConfig;
+* `lmc_gb300 -p param.txt` with simulation_method KineticMcFirstOmp: every row
+  of kmc_log.txt (time, T, energy, Ea, dE, atom id of the jumping atom,
+  unwrapped vacancy position) against the oracle trajectory replayed on the host;
+* simulation_method CanonicalMcOmp: cmc_log.txt energies and the final
+  configuration against the oracle's CanonicalMcOmp run on the same stream."""
+import gzip
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from host_util import EXE, build_check, write_cfg
+
+pytestmark = pytest.mark.gpu
+
+EA_RTOL = 1e-9
+DE_ATOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def check(native):
+    import importlib.util
+    from host_util import PKG
+    spec = importlib.util.spec_from_file_location("lmc_build", PKG / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build_host()
+    return build_check()
+
+
+def _alphabet(el):
+    return sorted(set(el) | {"X"})
+
+
+def test_predictor_classes(check, golden, tmp_path):
+    G, load = golden
+    fx = load("pred_ternary")
+    el, coeffs, n, sp = G.case_inputs("pred_ternary")
+    write_cfg(tmp_path / "start.cfg", n, sp, _alphabet(el))
+    (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
+    ok = fx["jump_ok"].astype(bool)
+    pairs = fx["pair"]
+    args = [str(check), "predict", str(tmp_path / "coeffs.json"), str(tmp_path / "start.cfg"), ",".join(el)]
+    args += [str(int(v)) for v in pairs.reshape(-1)]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = [list(map(float, line.split())) for line in r.stdout.strip().splitlines()]
+    out, energy = np.array(rows[:-1]), rows[-1][0]
+    np.testing.assert_allclose(out[ok, 0], fx["quartic"][:, 0], rtol=EA_RTOL)
+    np.testing.assert_allclose(out[ok, 1], fx["quartic"][:, 1], rtol=0, atol=DE_ATOL)
+    np.testing.assert_allclose(out[ok, 2], fx["e0"][:, 0], rtol=EA_RTOL, atol=1e-15)
+    np.testing.assert_allclose(out[:, 3], fx["pairsite"], rtol=0, atol=DE_ATOL)
+    assert energy == float(fx["energy"])
+
+
+def _run(tmp_path, params):
+    (tmp_path / "param.txt").write_text("".join(f"{k} {v}\n" for k, v in params.items()))
+    r = subprocess.run([str(EXE), "-p", "param.txt"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r
+
+
+def _read_log(path):
+    lines = path.read_text().strip().splitlines()
+    return lines[0].split("\t"), np.array([[float(v) for v in ln.split("\t")] for ln in lines[1:]])
+
+
+def test_kmc_executable(check, golden, oracle_mod, tmp_path):
+    G, load = golden
+    el, coeffs, n, sp = G.case_inputs("kmc_ternary")
+    alpha = _alphabet(el)
+    write_cfg(tmp_path / "start.cfg", n, sp, alpha)
+    (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
+    steps = 300
+    _run(tmp_path, {"simulation_method": "KineticMcFirstOmp", "config_filename": "start.cfg",
+                    "json_coefficients_filename": "coeffs.json", "log_dump_steps": 1, "config_dump_steps": 100,
+                    "maximum_steps": steps, "thermodynamic_averaging_steps": 0, "temperature": G.KMC_T,
+                    "element_set": " ".join(el), "seed": G.KMC_SEED})
+    head, log = _read_log(tmp_path / "kmc_log.txt")
+    assert head == ["steps", "time", "temperature", "energy", "Ea", "dE", "selected", "vac1", "vac2", "vac3"]
+    # Simulate runs while steps <= maximum_steps: maximum_steps + 1 steps
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    ref, _ = oracle_mod.kmc(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, steps + 1)
+    assert log.shape[0] == steps + 1
+    assert np.array_equal(log[:, 0], np.arange(steps + 1))
+    t_before = np.concatenate([[0.0], ref[:-1, 6]])
+    e_before = np.concatenate([[0.0], ref[:-1, 7]])
+    np.testing.assert_allclose(log[:, 1], t_before, rtol=1e-9, atol=1e-300)
+    assert np.all(log[:, 2] == G.KMC_T)
+    np.testing.assert_allclose(log[:, 3], e_before, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(log[:, 4], ref[:, 3], rtol=EA_RTOL)
+    np.testing.assert_allclose(log[:, 5], ref[:, 4], rtol=0, atol=DE_ATOL)
+    # atom ids (atom i starts on lattice id i) and the unwrapped vacancy position, replayed here
+    atom = np.arange(4 * n ** 3)
+    shift = np.zeros((atom.size, 3))
+    L = n * 4.046
+
+    def rel(i):
+        plane = 2 * n * n
+        hx, rem = divmod(int(i), plane)
+        hy, k = divmod(rem, n)
+        return np.array([hx, hy, 2 * k + ((hx + hy) & 1)]) / (2.0 * n)
+
+    for s in range(steps + 1):
+        vac, tgt = int(ref[s, 0]), int(ref[s, 1])
+        assert log[s, 6] == atom[tgt]
+        np.testing.assert_allclose(log[s, 7:10], (rel(vac) + shift[atom[vac]]) * L, rtol=0, atol=1e-9)
+        d = rel(tgt) - rel(vac)
+        img = np.where(np.abs(d) > 0.5 + 1e-8, np.floor(d + 0.5), 0)
+        shift[atom[vac]] -= img
+        shift[atom[tgt]] += img
+        atom[vac], atom[tgt] = atom[tgt], atom[vac]
+    for name in ("0.cfg.gz", "100.cfg.gz", "200.cfg.gz", "300.cfg.gz", "end.cfg.gz"):
+        assert (tmp_path / name).exists(), name
+    # end.cfg.gz is the lattice before the last step's jump
+    txt = gzip.decompress((tmp_path / "end.cfg.gz").read_bytes()).decode().splitlines()
+    assert txt[0] == f"Number of particles = {4 * n ** 3}"
+
+
+def test_cmc_executable(check, golden, oracle_mod, tmp_path):
+    G, load = golden
+    el, coeffs, n, sp = G.case_inputs("cmc_quaternary")
+    alpha = _alphabet(el)
+    write_cfg(tmp_path / "start.cfg", n, sp, alpha)
+    (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
+    steps, batch, avg = 3000, G.CMC_BATCH, 200
+    _run(tmp_path, {"simulation_method": "CanonicalMcOmp", "config_filename": "start.cfg",
+                    "json_coefficients_filename": "coeffs.json", "log_dump_steps": 1, "config_dump_steps": 100000,
+                    "maximum_steps": steps, "thermodynamic_averaging_steps": avg, "temperature": G.CMC_T,
+                    "element_set": " ".join(el), "seed": G.CMC_SEED, "cmc_batch": batch})
+    head, log = _read_log(tmp_path / "cmc_log.txt")
+    assert head == ["steps", "temperature", "energy", "average_energy", "absolute_energy"]
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    work = sp.copy()
+    done, e_final, acc, trace = oracle_mod.cmc(m, lat, work, G.CMC_T, G.CMC_SEED, steps + 1, batch, trace=True)
+    assert log.shape[0] == steps + 1
+    np.testing.assert_allclose(log[:, 2], trace[:steps + 1], rtol=0, atol=1e-10)
+    # ThermodynamicAveraging over the last `avg` energies (ThermodynamicAveraging.cpp:6-42)
+    beta = 1.0 / 8.617333262145e-5 / G.CMC_T
+    for s in (0, 57, 1999, steps):
+        w = trace[max(0, s + 1 - avg): s + 1]
+        mu = w.mean()
+        x = w - mu
+        ref_avg = (x * np.exp(-x * beta)).sum() / np.exp(-x * beta).sum() + mu
+        np.testing.assert_allclose(log[s, 3], ref_avg, rtol=1e-9, atol=1e-12)
+    e0, _ = oracle_mod.energy(m, lat, sp)
+    np.testing.assert_allclose(log[:, 4], e0 + trace[:steps + 1], rtol=0, atol=1e-9)
