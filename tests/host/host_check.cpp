@@ -1,8 +1,9 @@
 // Test driver for the C++ host mirror (lmc_host.hpp), used by tests/test_host.py.
 //   host_check cfg-roundtrip <dir>              CFG write/read (plain and gzip) with atom tracking
 //   host_check param <file>                     parsed api::Parameter keys
-//   host_check predict <json> <cfg> <elements,comma> <a> <b> [<a> <b> ...]
-//                                               Ea dE (Quartic), Ea (E0), swap dE per pair, then the energy
+//   host_check predict <json> <cfg> <elements,comma> <m> <a b> x m <a b> ...
+//                                               Ea dE (Quartic) and Ea (E0) for the m jump pairs, swap dE
+//                                               for the remaining pairs, then the energy
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -74,12 +75,23 @@ int main(int argc, char **argv) {
       const pred::EnergyChangePredictorPairSite pair_site(argv[2], c, els);
       const pred::EnergyPredictor energy(argv[2], els);
       std::cout.precision(17);
-      for (int i = 5; i + 1 < argc; i += 2) {
+      const int jumps = std::atoi(argv[5]);
+      for (int i = 6, k = 0; i + 1 < argc; i += 2, ++k) {
         const std::pair<size_t, size_t> p{std::strtoull(argv[i], nullptr, 10), std::strtoull(argv[i + 1], nullptr, 10)};
-        const auto q = quartic.GetBarrierAndDiffFromLatticeIdPair(c, p);
-        const auto z = e0.GetBarrierAndDiffFromLatticeIdPair(c, p);
-        std::cout << q.first << ' ' << q.second << ' ' << z.first << ' ' << pair_site.GetDeFromLatticeIdPair(c, p)
-                  << '\n';
+        if (k < jumps) {
+          const auto q = quartic.GetBarrierAndDiffFromLatticeIdPair(c, p);
+          const auto z = e0.GetBarrierAndDiffFromLatticeIdPair(c, p);
+          std::cout << q.first << ' ' << q.second << ' ' << z.first << '\n';
+        } else {
+          std::cout << pair_site.GetDeFromLatticeIdPair(c, p) << '\n';
+        }
+      }
+      // a non-neighbour pair is out of range for the barrier predictor, as GetPairFlatIndex
+      try {
+        (void)quartic.GetBarrierAndDiffFromLatticeIdPair(c, {0, c.GetNumLattices() / 2});
+        std::cout << "no exception\n";
+      } catch (const std::out_of_range &) {
+        std::cout << "out_of_range\n";
       }
       std::cout << energy.GetEnergy(c) << std::endl;
       return 0;

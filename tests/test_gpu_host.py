@@ -44,19 +44,22 @@ def test_predictor_classes(check, golden, tmp_path):
     el, coeffs, n, sp = G.case_inputs("pred_ternary")
     write_cfg(tmp_path / "start.cfg", n, sp, _alphabet(el))
     (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
-    ok = fx["jump_ok"].astype(bool)
+    jumps = fx["pair"][fx["jump_ok"].astype(bool)]
     pairs = fx["pair"]
-    args = [str(check), "predict", str(tmp_path / "coeffs.json"), str(tmp_path / "start.cfg"), ",".join(el)]
-    args += [str(int(v)) for v in pairs.reshape(-1)]
+    args = [str(check), "predict", str(tmp_path / "coeffs.json"), str(tmp_path / "start.cfg"), ",".join(el),
+            str(len(jumps))]
+    args += [str(int(v)) for v in np.concatenate([jumps, pairs]).reshape(-1)]
     r = subprocess.run(args, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    rows = [list(map(float, line.split())) for line in r.stdout.strip().splitlines()]
-    out, energy = np.array(rows[:-1]), rows[-1][0]
-    np.testing.assert_allclose(out[ok, 0], fx["quartic"][:, 0], rtol=EA_RTOL)
-    np.testing.assert_allclose(out[ok, 1], fx["quartic"][:, 1], rtol=0, atol=DE_ATOL)
-    np.testing.assert_allclose(out[ok, 2], fx["e0"][:, 0], rtol=EA_RTOL, atol=1e-15)
-    np.testing.assert_allclose(out[:, 3], fx["pairsite"], rtol=0, atol=DE_ATOL)
-    assert energy == float(fx["energy"])
+    lines = r.stdout.strip().splitlines()
+    assert lines[-2] == "out_of_range"
+    q = np.array([list(map(float, ln.split())) for ln in lines[:len(jumps)]])
+    de = np.array([float(ln) for ln in lines[len(jumps):len(jumps) + len(pairs)]])
+    np.testing.assert_allclose(q[:, 0], fx["quartic"][:, 0], rtol=EA_RTOL)
+    np.testing.assert_allclose(q[:, 1], fx["quartic"][:, 1], rtol=0, atol=DE_ATOL)
+    np.testing.assert_allclose(q[:, 2], fx["e0"][:, 0], rtol=EA_RTOL, atol=1e-15)
+    np.testing.assert_allclose(de, fx["pairsite"], rtol=0, atol=DE_ATOL)
+    assert float(lines[-1]) == float(fx["energy"])
 
 
 def _run(tmp_path, params):
@@ -67,8 +70,9 @@ def _run(tmp_path, params):
 
 
 def _read_log(path):
+    # the reference prints Vector_d values space-separated under tab-separated headers
     lines = path.read_text().strip().splitlines()
-    return lines[0].split("\t"), np.array([[float(v) for v in ln.split("\t")] for ln in lines[1:]])
+    return lines[0].split("\t"), np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
 
 
 def test_kmc_executable(check, golden, oracle_mod, tmp_path):
@@ -141,15 +145,16 @@ def test_cmc_executable(check, golden, oracle_mod, tmp_path):
     m = oracle_mod.Model(el, coeffs, lat)
     work = sp.copy()
     done, e_final, acc, trace = oracle_mod.cmc(m, lat, work, G.CMC_T, G.CMC_SEED, steps + 1, batch, trace=True)
-    assert log.shape[0] == steps + 1
-    np.testing.assert_allclose(log[:, 2], trace[:steps + 1], rtol=0, atol=1e-10)
+    # Simulate finishes the batch it is in: steps_ may pass maximum_steps_ (CanonicalMcOmp.cpp:82-90)
+    assert done >= steps + 1 and log.shape[0] == done
+    np.testing.assert_allclose(log[:, 2], trace, rtol=0, atol=1e-10)
     # ThermodynamicAveraging over the last `avg` energies (ThermodynamicAveraging.cpp:6-42)
     beta = 1.0 / 8.617333262145e-5 / G.CMC_T
-    for s in (0, 57, 1999, steps):
+    for s in (0, 57, 1999, done - 1):
         w = trace[max(0, s + 1 - avg): s + 1]
         mu = w.mean()
         x = w - mu
         ref_avg = (x * np.exp(-x * beta)).sum() / np.exp(-x * beta).sum() + mu
         np.testing.assert_allclose(log[s, 3], ref_avg, rtol=1e-9, atol=1e-12)
     e0, _ = oracle_mod.energy(m, lat, sp)
-    np.testing.assert_allclose(log[:, 4], e0 + trace[:steps + 1], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(log[:, 4], e0 + trace, rtol=0, atol=1e-9)
