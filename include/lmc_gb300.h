@@ -195,6 +195,52 @@ int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *e
 int lmc_fastmath_check(lmc_ctx *ctx, int fn, const double *x, int64_t n, double *fast, double *ref);
 
 /* ------------------------------------------------------------------------- */
+/* Learned barrier surrogate (no reference counterpart: the plain predictor    */
+/* above is its fallback and the judge of its error)                          */
+/* ------------------------------------------------------------------------- */
+/* Ensemble of `members` MLPs in -> hidden -> hidden -> 1 (GELU), BF16 weights and
+ * activations on the tensor cores, FP32 accumulation, FP32 master weights, Adam.
+ * Features (bf16 rows, passed as uint16_t): the one-hot rank of the 58 MMM-ordered
+ * environment sites of a jump (VacancyMigrationPredictorQuartic's MMM list), then of
+ * the migrant, zero padded to in_features (a multiple of 64). */
+typedef struct lmc_mlp lmc_mlp;
+int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_t seed, lmc_mlp **out);
+void lmc_mlp_destroy(lmc_mlp *mlp);
+int lmc_mlp_layout(const lmc_mlp *mlp, int *in_features, int *hidden, int *members, int64_t *num_params);
+/* Flat FP32 parameters in the order W1 [M*H][in], b1 [M*H], W2 [M][H][H], b2 [M*H], w3 [M*H], b3 [M]. */
+int lmc_mlp_get_params(lmc_mlp *mlp, float *params);
+int lmc_mlp_set_params(lmc_mlp *mlp, const float *params);
+/* Labels are standardised as (ea - mean) / std inside; predictions come back in eV. */
+int lmc_mlp_set_label_scale(lmc_mlp *mlp, float mean, float std_dev);
+/* Gradients (flat, parameter order) of every member's mean squared error on one batch
+ * (host arrays; batch a multiple of 64), and the per-member loss. Nothing is updated. */
+int lmc_mlp_gradients(lmc_mlp *mlp, const uint16_t *features, const float *labels, int batch, float *grad,
+                      float *loss);
+/* Trains every member on the same shuffled batches (device arrays, n samples); loss
+ * (nullable, per member) is the mean loss of the last epoch in standardised units. */
+int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *features_dev, const float *labels_dev, int64_t n, int batch,
+                  int epochs, float lr, uint64_t seed, float *loss);
+/* Ensemble mean and spread (max - min over members), eV, for n feature rows (device arrays). */
+int lmc_mlp_predict(lmc_mlp *mlp, const uint16_t *features_dev, int64_t n, float *mean_dev, float *spread_dev);
+
+/* Feature row length of a context's model: at least 59 x one-hot alphabet, padded to 64. */
+int lmc_surrogate_feature_count(const lmc_ctx *ctx, int *min_features, int *padded_features);
+/* Training data: `count` seeded random neighbourhoods (solute fraction ~ U(solute_lo, solute_hi),
+ * solutes equally likely, the rest the base element), their features and the plain
+ * predictor's barrier (ea_dev float; ea64_dev / de64_dev optional double). Device arrays. */
+int lmc_surrogate_dataset(lmc_ctx *ctx, uint64_t seed, int64_t count, double solute_lo, double solute_hi, int kind,
+                          int in_features, uint16_t *features_dev, float *ea_dev, double *ea64_dev, double *de64_dev);
+/* Features of lattice jumps (pairs first -> second, device arrays). */
+int lmc_surrogate_features(lmc_ctx *ctx, int replica, const int64_t *pairs_dev, int m, int in_features,
+                           uint16_t *features_dev);
+/* Surrogate barriers of m jumps (device arrays): the ensemble mean, or the plain predictor
+ * (lmc_barrier_batch) where the ensemble spread exceeds threshold_ev; fallback_dev (nullable)
+ * flags those pairs and num_fallback (nullable) counts them. */
+int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, int kind, const int64_t *pairs_dev,
+                                       int m, float threshold_ev, double *ea_dev, uint8_t *fallback_dev,
+                                       int *num_fallback);
+
+/* ------------------------------------------------------------------------- */
 /* Kinetic MC (KineticMcFirstOmp semantics, KineticMcAbstract.cpp:140-190)    */
 /* ------------------------------------------------------------------------- */
 #define LMC_RNG_MT19937_64 0 /* std::mt19937_64 + libstdc++ distributions: same stream as the reference */

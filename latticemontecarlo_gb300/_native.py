@@ -126,6 +126,23 @@ SIGNATURES = {
     "lmc_energy": (C.c_int, [_P, C.c_int, _DP, _I64P]),
     "lmc_energy_noalloc": (C.c_int, [_P, _P, C.c_int, _P]),
     "lmc_fastmath_check": (C.c_int, [_P, C.c_int, _DP, C.c_int64, _DP, _DP]),
+    "lmc_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(_P)]),
+    "lmc_mlp_destroy": (None, [_P]),
+    "lmc_mlp_layout": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _I64P]),
+    "lmc_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "lmc_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "lmc_mlp_set_label_scale": (C.c_int, [_P, C.c_float, C.c_float]),
+    "lmc_mlp_gradients": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float)]),
+    "lmc_mlp_train": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64,
+                                C.POINTER(C.c_float)]),
+    "lmc_mlp_predict": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
+    "lmc_surrogate_feature_count": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "lmc_surrogate_dataset": (C.c_int, [_P, C.c_uint64, C.c_int64, C.c_double, C.c_double, C.c_int, C.c_int, _P, _P,
+                                        _P, _P]),
+    "lmc_surrogate_features": (C.c_int, [_P, C.c_int, _P, C.c_int, C.c_int, _P]),
+    "lmc_surrogate_barrier_batch_device": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.c_float, _P, _P,
+                                                     C.POINTER(C.c_int)]),
     "lmc_kmc_init": (C.c_int, [_P, _DP, C.POINTER(KmcOptions)]),
     "lmc_kmc_run": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(KmcStep), _DP]),
     "lmc_kmc_get_state": (C.c_int, [_P, _I64P, _U64P, _DP, _DP]),

@@ -107,6 +107,7 @@ class Context:
 
     def __init__(self, model: Model, device: int = 0):
         self.model = model
+        self.device = device
         h = C.c_void_p()
         check(N.lib.lmc_ctx_create(model._h, device, C.byref(h)))
         self._h = h
@@ -228,6 +229,100 @@ class Context:
 
     def request_stop(self, value: int = 1) -> None:
         check(N.lib.lmc_request_stop(self._h, value))
+
+
+class Surrogate:
+    """BF16 MLP barrier surrogate (lmc_mlp_*): an ensemble trained on the plain
+    predictor's barriers. Device arrays are torch tensors (features bfloat16
+    [n][in_features], labels float32); torch only provides the device memory."""
+
+    def __init__(self, in_features: int, hidden: int = 256, members: int = 4, seed: int = 0, device: int = 0):
+        h = C.c_void_p()
+        check(N.lib.lmc_mlp_create(device, in_features, hidden, members, seed, C.byref(h)))
+        self._h = h
+        self.in_features, self.hidden, self.members = in_features, hidden, members
+        n = np.zeros(1, np.int64)
+        check(N.lib.lmc_mlp_layout(h, None, None, None, ptr(n, C.c_int64)))
+        self.num_params = int(n[0])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            N.lib.lmc_mlp_destroy(h)
+            self._h = None
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(N.lib.lmc_mlp_get_params(self._h, ptr(out, C.c_float)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.num_params
+        check(N.lib.lmc_mlp_set_params(self._h, ptr(p, C.c_float)))
+
+    def set_label_scale(self, mean: float, std: float) -> None:
+        check(N.lib.lmc_mlp_set_label_scale(self._h, float(mean), float(std)))
+
+    def gradients(self, features_bf16_bits: np.ndarray, labels: np.ndarray):
+        x = np.ascontiguousarray(features_bf16_bits, np.uint16)
+        t = np.ascontiguousarray(labels, np.float32)
+        g = np.zeros(self.num_params, np.float32)
+        loss = np.zeros(self.members, np.float32)
+        check(N.lib.lmc_mlp_gradients(self._h, x.ctypes.data_as(C.c_void_p), ptr(t, C.c_float), t.size,
+                                      ptr(g, C.c_float), ptr(loss, C.c_float)))
+        return g, loss
+
+    def train(self, features, labels, batch: int = 4096, epochs: int = 10, lr: float = 2e-3, seed: int = 0):
+        loss = np.zeros(self.members, np.float32)
+        check(N.lib.lmc_mlp_train(self._h, C.c_void_p(features.data_ptr()), C.c_void_p(labels.data_ptr()),
+                                  features.shape[0], batch, epochs, lr, seed, ptr(loss, C.c_float)))
+        return loss
+
+    def predict(self, features):
+        import torch
+        n = features.shape[0]
+        mean = torch.empty(n, dtype=torch.float32, device=features.device)
+        spread = torch.empty(n, dtype=torch.float32, device=features.device)
+        check(N.lib.lmc_mlp_predict(self._h, C.c_void_p(features.data_ptr()), n, C.c_void_p(mean.data_ptr()),
+                                    C.c_void_p(spread.data_ptr())))
+        return mean, spread
+
+
+def surrogate_feature_count(ctx: "Context") -> int:
+    mn, pad = C.c_int(), C.c_int()
+    check(N.lib.lmc_surrogate_feature_count(ctx._h, C.byref(mn), C.byref(pad)))
+    return pad.value
+
+
+def surrogate_dataset(ctx: "Context", seed: int, count: int, solute_lo: float, solute_hi: float, in_features: int,
+                      kind: int = N.LMC_BARRIER_QUARTIC, with_de: bool = False):
+    """Seeded random environments with their features and plain-predictor barriers (torch tensors)."""
+    import torch
+    dev = f"cuda:{ctx.device}"
+    x = torch.empty((count, in_features), dtype=torch.bfloat16, device=dev)
+    ea = torch.empty(count, dtype=torch.float32, device=dev)
+    ea64 = torch.empty(count, dtype=torch.float64, device=dev)
+    de64 = torch.empty(count, dtype=torch.float64, device=dev) if with_de else None
+    check(N.lib.lmc_surrogate_dataset(ctx._h, seed, count, solute_lo, solute_hi, kind, in_features,
+                                      C.c_void_p(x.data_ptr()), C.c_void_p(ea.data_ptr()),
+                                      C.c_void_p(ea64.data_ptr()),
+                                      C.c_void_p(de64.data_ptr()) if de64 is not None else None))
+    return x, ea, ea64, de64
+
+
+def surrogate_barriers(ctx: "Context", model: Surrogate, pairs_dev, threshold_ev: float = 0.010, replica: int = 0,
+                       kind: int = N.LMC_BARRIER_QUARTIC):
+    """Ensemble barriers of lattice jumps with the plain predictor as fallback (torch tensors)."""
+    import torch
+    m = pairs_dev.shape[0]
+    ea = torch.empty(m, dtype=torch.float64, device=pairs_dev.device)
+    flag = torch.empty(m, dtype=torch.uint8, device=pairs_dev.device)
+    nfb = C.c_int()
+    check(N.lib.lmc_surrogate_barrier_batch_device(ctx._h, model._h, replica, kind, C.c_void_p(pairs_dev.data_ptr()),
+                                                   m, threshold_ev, C.c_void_p(ea.data_ptr()),
+                                                   C.c_void_p(flag.data_ptr()), C.byref(nfb)))
+    return ea, flag, nfb.value
 
 
 def load_coefficients(path) -> dict:

@@ -18,45 +18,14 @@
 #include "geometry.hpp"
 #include "kernels.cuh"
 #include "model.hpp"
+#include "abi_common.hpp"
 
 namespace {
-thread_local std::string g_error;
-
-struct LmcError : std::runtime_error {
-  int code;
-  LmcError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
-};
-
-void CudaCheck(cudaError_t err, const char *what) {
-  if (err != cudaSuccess) throw LmcError(LMC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
-}
-
-template <typename F>
-int Guard(F &&f) {
-  try {
-    f();
-    return LMC_OK;
-  } catch (const LmcError &e) {
-    g_error = e.what();
-    return e.code;
-  } catch (const std::out_of_range &e) {
-    g_error = e.what();
-    return LMC_ERR_OUT_OF_RANGE;
-  } catch (const std::ios_base::failure &e) {
-    g_error = e.what();
-    return LMC_ERR_IO;
-  } catch (const std::invalid_argument &e) {
-    g_error = e.what();
-    return LMC_ERR_INVALID_ARGUMENT;
-  } catch (const std::exception &e) {
-    g_error = e.what();
-    return LMC_ERR_INVALID_ARGUMENT;
-  }
-}
-
-void Require(bool ok, int code, const std::string &msg) {
-  if (!ok) throw LmcError(code, msg);
-}
+using lmc::abi::CudaCheck;
+using lmc::abi::g_error;
+using lmc::abi::Guard;
+using lmc::abi::LmcError;
+using lmc::abi::Require;
 
 int8_t Pack4(int v) { return static_cast<int8_t>(v); }
 
@@ -117,6 +86,7 @@ struct lmc_ctx {
   lmc_kmc_options kmc_opt{};
   DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
   DevBuf k_solvent, k_escaped, c_trace;
+  DevBuf s_feat, s_mean, s_spread, s_fb_pairs, s_fb_index, s_fb_ea, s_fb_de;
   int tt_len{0};
   // sparse KMC tables (built for the dominant species at lmc_kmc_init)
   std::vector<DevBuf> sparse_bufs;
@@ -133,7 +103,8 @@ struct lmc_ctx {
     for (auto &b : tables) b.Free();
     for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
-                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &s_feat, &s_mean, &s_spread,
+                      &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -1064,6 +1035,131 @@ int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *e
       if (ctx->model.alphabet[c] == "Al") base = c;
     // LaunchCensus clears the counters it uses before the census kernel runs.
     CudaCheck(lmc::LaunchCensus(ctx->t, species_dev, n, base, scratch, energy_dev, ctx->stream), "census kernel");
+  });
+}
+
+namespace {
+int SurrogateBase(const lmc_ctx *ctx) {
+  const int al = ctx->model.Code("Al");
+  if (al >= 0 && al != ctx->fm.x_code) return al;
+  for (int c = 0; c < ctx->fm.num_species; ++c)
+    if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0) return c;
+  return -1;
+}
+}  // namespace
+
+int lmc_surrogate_feature_count(const lmc_ctx *ctx, int *min_features, int *padded_features) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    const int need = (lmc::kEnvSites + 1) * ctx->fm.num_onehot;
+    if (min_features) *min_features = need;
+    if (padded_features) *padded_features = (need + 63) / 64 * 64;
+  });
+}
+
+int lmc_surrogate_dataset(lmc_ctx *ctx, uint64_t seed, int64_t count, double solute_lo, double solute_hi, int kind,
+                          int in_features, uint16_t *features_dev, float *ea_dev, double *ea64_dev, double *de64_dev) {
+  return Guard([&] {
+    Require(ctx && features_dev && ea_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    Require(count >= 0, LMC_ERR_INVALID_ARGUMENT, "count < 0");
+    Require(0.0 <= solute_lo && solute_lo <= solute_hi && solute_hi <= 1.0, LMC_ERR_INVALID_ARGUMENT,
+            "need 0 <= solute_lo <= solute_hi <= 1");
+    Require(kind == LMC_BARRIER_QUARTIC || kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT, "unknown barrier kind");
+    Require(in_features >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
+            "in_features below 59 x the one-hot alphabet");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    lmc::SurrogateGen g{};
+    g.seed = seed;
+    g.count = count;
+    g.solute_lo = static_cast<float>(solute_lo);
+    g.solute_hi = static_cast<float>(solute_hi);
+    g.base_code = SurrogateBase(ctx);
+    Require(g.base_code >= 0, LMC_ERR_INVALID_ARGUMENT, "no base species with a one-hot slot");
+    g.kind = kind;
+    g.in_pad = in_features;
+    g.features = reinterpret_cast<__nv_bfloat16 *>(features_dev);
+    g.ea = ea_dev;
+    g.ea64 = ea64_dev;
+    g.de64 = de64_dev;
+    g.status = ctx->status.as<int>();
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchSurrogateDataset(ctx->t, g, ctx->stream), "dataset kernel");
+    RaiseStatus(ctx->ReadStatus(), "surrogate dataset");
+  });
+}
+
+int lmc_surrogate_features(lmc_ctx *ctx, int replica, const int64_t *pairs_dev, int m, int in_features,
+                           uint16_t *features_dev) {
+  return Guard([&] {
+    Require(ctx && pairs_dev && features_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    ctx->CheckReplica(replica);
+    Require(in_features >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
+            "in_features below 59 x the one-hot alphabet");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                           reinterpret_cast<const long long *>(pairs_dev), m, in_features,
+                                           reinterpret_cast<__nv_bfloat16 *>(features_dev), ctx->status.as<int>(),
+                                           ctx->stream),
+              "features kernel");
+    RaiseStatus(ctx->ReadStatus(), "surrogate features");
+  });
+}
+
+int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, int kind, const int64_t *pairs_dev,
+                                       int m, float threshold_ev, double *ea_dev, uint8_t *fallback_dev,
+                                       int *num_fallback) {
+  return Guard([&] {
+    Require(ctx && mlp && pairs_dev && ea_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    Require(m >= 0, LMC_ERR_INVALID_ARGUMENT, "m < 0");
+    ctx->CheckReplica(replica);
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int in = 0;
+    Require(lmc_mlp_layout(mlp, &in, nullptr, nullptr, nullptr) == LMC_OK, LMC_ERR_INVALID_ARGUMENT, "bad mlp");
+    Require(in >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
+            "the network's input is narrower than the features of this model");
+    if (m == 0) {
+      if (num_fallback) *num_fallback = 0;
+      return;
+    }
+    const size_t mm = static_cast<size_t>(m);
+    ctx->s_feat.Ensure(sizeof(uint16_t) * mm * in);
+    ctx->s_mean.Ensure(sizeof(float) * mm);
+    ctx->s_spread.Ensure(sizeof(float) * mm);
+    ctx->s_fb_pairs.Ensure(sizeof(long long) * 2 * mm);
+    ctx->s_fb_index.Ensure(sizeof(int) * (mm + 1));
+    ctx->s_fb_ea.Ensure(sizeof(double) * mm);
+    ctx->s_fb_de.Ensure(sizeof(double) * mm);
+    const auto *pairs = reinterpret_cast<const long long *>(pairs_dev);
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica], pairs, m, in,
+                                           ctx->s_feat.as<__nv_bfloat16>(), ctx->status.as<int>(), ctx->stream),
+              "features kernel");
+    // the network runs on its own stream: order it after the features
+    ctx->Sync();
+    const int st = lmc_mlp_predict(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(),
+                                   ctx->s_spread.as<float>());
+    if (st != LMC_OK) throw LmcError(st, lmc_last_error());
+    int *d_count = ctx->s_fb_index.as<int>() + mm;
+    CudaCheck(cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream), "memset");
+    CudaCheck(lmc::LaunchFallbackCompact(pairs, ctx->s_mean.as<float>(), ctx->s_spread.as<float>(), m, threshold_ev,
+                                         ctx->s_fb_pairs.as<long long>(), ctx->s_fb_index.as<int>(), d_count,
+                                         fallback_dev, ctx->stream),
+              "fallback kernel");
+    int count = 0;
+    CudaCheck(cudaMemcpyAsync(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    if (count > 0)
+      CudaCheck(lmc::LaunchBarrierBatch(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                        ctx->s_fb_pairs.as<long long>(), count, kind, ctx->s_fb_ea.as<double>(),
+                                        ctx->s_fb_de.as<double>(), nullptr, nullptr, ctx->status.as<int>(),
+                                        ctx->stream),
+                "barrier kernel");
+    CudaCheck(lmc::LaunchFallbackMerge(ctx->s_mean.as<float>(), m, ctx->s_fb_ea.as<double>(), ctx->s_fb_index.as<int>(),
+                                       d_count, ea_dev, ctx->stream),
+              "merge kernel");
+    RaiseStatus(ctx->ReadStatus(), "surrogate barriers");
+    if (num_fallback) *num_fallback = count;
   });
 }
 

@@ -23,6 +23,7 @@
 
 #include "kernels.cuh"
 #include "fastmath.cuh"
+#include <cuda_bf16.h>
 
 namespace cg = cooperative_groups;
 
@@ -696,6 +697,138 @@ __device__ __forceinline__ double U01(uint32_t hi, uint32_t lo) {
 __device__ __forceinline__ double U01Open(uint32_t hi, uint32_t lo) {
   const unsigned long long v = ((static_cast<unsigned long long>(hi) << 32) | lo) >> 11;
   return static_cast<double>(v + 1) * 1.1102230246251565404e-16;
+}
+
+// ---------------------------------------------------------------------------
+// K6: surrogate training data and features.
+//
+// Features of a jump (MLP input, bf16 row of in_pad values): the one-hot rank
+// of each of the 58 MMM-ordered environment sites (58 x E' values, E' = one-hot
+// alphabet size, vacancies excluded), then the one-hot rank of the migrant
+// (E' values), zero padded.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void WriteFeatures(const int8_t *rm, int mig_rank, int eh, int in_pad,
+                                              __nv_bfloat16 *row, int lane) {
+  const int env = kEnvSites * eh;
+  for (int idx = lane; idx < in_pad; idx += 32) {
+    bool one = false;
+    if (idx < env) one = rm[idx / eh] == idx % eh;
+    else if (idx < env + eh) one = mig_rank == idx - env;
+    row[idx] = __float2bfloat16(one ? 1.0f : 0.0f);
+  }
+}
+
+// One warp per sample: a 135-site neighbourhood drawn with Philox (counter =
+// (sample, lane, round), key = seed): the centre is the vacancy, every other
+// site a solute with probability f ~ U(solute_lo, solute_hi) (solutes equally
+// likely) and the base species otherwise; jump direction = sample mod 12. The
+// label is the plain predictor's barrier (dense cluster sums + FP64 epilogue).
+__global__ void surrogate_dataset_kernel(DevTables t, SurrogateGen g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const JumpSmem s = CarveJumpSmem(t, smem);
+  StageJump(t, s);
+  const int warps = blockDim.x >> 5;
+  int8_t *locals = reinterpret_cast<int8_t *>(s.arr + warps * kArr);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *st = s.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  int8_t *local = locals + warp * 144;
+  const int e = t.num_species, eh = t.num_onehot;
+  // solutes: every non-vacancy species other than the base
+  int solutes[8], ns = 0;
+  for (int c = 0; c < e; ++c)
+    if (c != t.x_code && c != g.base_code) solutes[ns++] = c;
+  unsigned bad_all = 0;
+  for (long long i = static_cast<long long>(blockIdx.x) * warps + warp; i < g.count;
+       i += static_cast<long long>(gridDim.x) * warps) {
+    const uint32_t k0 = static_cast<uint32_t>(g.seed), k1 = static_cast<uint32_t>(g.seed >> 32);
+    const uint4 head = PhiloxRound10(static_cast<uint32_t>(i), static_cast<uint32_t>(i >> 32), 0xFFFFu, 0x53u, k0, k1);
+    const float f = g.solute_lo + (g.solute_hi - g.solute_lo) * (head.x * 2.3283064365386963e-10f);
+    const int c = static_cast<int>(i % 12);
+    for (int r = 0; r < 2; ++r) {
+      const uint4 x = PhiloxRound10(static_cast<uint32_t>(i), static_cast<uint32_t>(i >> 32), lane, r, k0, k1);
+      const uint32_t v[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int site = lane + 32 * (4 * r + q);
+        if (site >= kLocalSites) continue;
+        const float u = (v[q] >> 8) * 5.9604644775390625e-8f;  // 24-bit uniform
+        int code = g.base_code;
+        if (u < f && ns > 0) code = solutes[min(ns - 1, static_cast<int>(u / f * ns))];
+        local[site] = static_cast<int8_t>(code);
+      }
+    }
+    __syncwarp();
+    const uint8_t *lst = t.local_st + c * kStateSites;
+    if (lane == 0) local[lst[t.pos_first]] = static_cast<int8_t>(t.x_code);
+    __syncwarp();
+    for (int k = lane; k < kStateSites; k += 32) st[k] = local[lst[k]];
+    for (int k = lane; k < kEnvSites; k += 32) {
+      rm[k] = s.small->rank[local[t.local_mmm[c * kEnvSites + k]]];
+      rf[k] = s.small->rank[local[t.local_mm2f[c * kEnvSites + k]]];
+      rb[k] = s.small->rank[local[t.local_mm2b[c * kEnvSites + k]]];
+    }
+    __syncwarp();
+    const int mig = st[t.pos_second];
+    const int slot = s.small->slot[mig];
+    const bool ok = slot >= 0 && (g.kind == 0 ? s.small->has_quartic[slot] : s.small->has_e0[slot]);
+    JumpAcc a{0, 0, 0, 0u};
+    if (ok)
+      a = g.kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane)
+                      : EvalJump<false>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane);
+    const long long acc_de = WarpSum(a.de), acc_d = WarpSum(a.d), acc_ks = WarpSum(a.ks);
+    bad_all |= __reduce_or_sync(0xffffffffu, a.bad) | (ok ? 0u : kStatusNoCoefficients);
+    if (lane == 0) {
+      double ea = nan(""), de = nan("");
+      if (ok) {
+        const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, g.kind, slot, acc_de, acc_d, acc_ks);
+        ea = o.ea;
+        de = o.de;
+      }
+      g.ea[i] = static_cast<float>(ea);
+      if (g.ea64) g.ea64[i] = ea;
+      if (g.de64) g.de64[i] = de;
+    }
+    WriteFeatures(rm, s.small->rank[mig], eh, g.in_pad, g.features + i * g.in_pad, lane);
+    __syncwarp();
+  }
+  if (bad_all && lane == 0) atomicOr(g.status, static_cast<int>(bad_all));
+}
+
+// Features of lattice jumps (pairs first -> second), one warp per pair.
+__global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                                          const long long *__restrict__ pairs, int m, int in_pad,
+                                          __nv_bfloat16 *features, int *status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  SmallTables *sm = reinterpret_cast<SmallTables *>(smem);
+  int8_t *arr = reinterpret_cast<int8_t *>(sm + 1);
+  StageSmall(t, sm);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *rm = arr + warp * 64;
+  unsigned bad_all = 0;
+  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
+    H3 hi, hj;
+    int di = -1, db = -1;
+    const unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+    int mig_rank = kMaxOnehot - 1;
+    if (!bad) {
+      for (int k = lane; k < kEnvSites; k += 32) {
+        const int8_t *a = t.mmm_off + (di * kEnvSites + k) * 4;
+        rm[k] = sm->rank[species[NeighborId(hi, a[0], a[1], a[2], n)]];
+      }
+      mig_rank = sm->rank[species[pairs[2 * p + 1]]];
+    } else {
+      for (int k = lane; k < kEnvSites; k += 32) rm[k] = kMaxOnehot - 1;
+    }
+    bad_all |= bad;
+    __syncwarp();
+    WriteFeatures(rm, mig_rank, t.num_onehot, in_pad, features + static_cast<long long>(p) * in_pad, lane);
+    __syncwarp();
+  }
+  if (bad_all && lane == 0) atomicOr(status, static_cast<int>(bad_all));
 }
 
 // ---------------------------------------------------------------------------
@@ -1570,6 +1703,75 @@ cudaError_t LaunchBarrierBatch(const DevTables &t, const int8_t *species, int n,
   const size_t sm = JumpSmemBytes(t, kJumpWarps);
   barrier_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, kind, ea, de,
                                                                               d_or_e0, ks, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSurrogateDataset(const DevTables &t, const SurrogateGen &g, cudaStream_t stream) {
+  if (g.count <= 0) return cudaSuccess;
+  if (g.in_pad < (kEnvSites + 1) * t.num_onehot) return cudaErrorInvalidValue;
+  const size_t sm = JumpSmemBytes(t, kJumpWarps) + kJumpWarps * 144;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long need = (g.count + kJumpWarps - 1) / kJumpWarps;
+  const int blocks = static_cast<int>(need < sms * 8LL ? need : sms * 8LL);
+  cudaError_t err = cudaFuncSetAttribute(surrogate_dataset_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  surrogate_dataset_kernel<<<blocks, kJumpWarps * 32, sm, stream>>>(t, g);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSurrogateFeatures(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                                    int in_pad, __nv_bfloat16 *features, int *status, cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  if (in_pad < (kEnvSites + 1) * t.num_onehot) return cudaErrorInvalidValue;
+  const size_t sm = sizeof(SmallTables) + kJumpWarps * 64;
+  surrogate_features_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, in_pad,
+                                                                                  features, status);
+  return cudaGetLastError();
+}
+
+namespace {
+// Pairs whose ensemble spread exceeds the threshold (or whose mean is not finite) go to the plain predictor.
+__global__ void fallback_compact_kernel(const long long *pairs, const float *mean, const float *spread, int m,
+                                        float threshold, long long *fb_pairs, int *fb_index, int *count,
+                                        uint8_t *flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const bool fb = !(spread[i] <= threshold) || !isfinite(mean[i]);
+  if (flag) flag[i] = fb ? 1 : 0;
+  if (!fb) return;
+  const int k = atomicAdd(count, 1);
+  fb_pairs[2 * k] = pairs[2 * i];
+  fb_pairs[2 * k + 1] = pairs[2 * i + 1];
+  fb_index[k] = i;
+}
+// Surrogate means first; the plain barriers of the fallback pairs are scattered over them afterwards.
+__global__ void fallback_merge_kernel(const float *mean, int m, double *ea) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) ea[i] = static_cast<double>(mean[i]);
+}
+__global__ void fallback_scatter_kernel(const double *fb_ea, const int *fb_index, const int *count, double *ea) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < *count) ea[fb_index[k]] = fb_ea[k];
+}
+}  // namespace
+
+cudaError_t LaunchFallbackCompact(const long long *pairs, const float *mean, const float *spread, int m,
+                                  float threshold, long long *fb_pairs, int *fb_index, int *count, uint8_t *flag,
+                                  cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  fallback_compact_kernel<<<(m + 255) / 256, 256, 0, stream>>>(pairs, mean, spread, m, threshold, fb_pairs, fb_index,
+                                                               count, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchFallbackMerge(const float *mean, int m, const double *fb_ea, const int *fb_index, const int *count,
+                                double *ea, cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  fallback_merge_kernel<<<(m + 255) / 256, 256, 0, stream>>>(mean, m, ea);
+  fallback_scatter_kernel<<<(m + 255) / 256, 256, 0, stream>>>(fb_ea, fb_index, count, ea);
   return cudaGetLastError();
 }
 

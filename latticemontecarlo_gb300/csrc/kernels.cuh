@@ -1,5 +1,6 @@
 // Launch interface of the sm_103a kernels (implemented in kernels.cu).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -114,6 +115,30 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                       cudaStream_t stream);
 size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
+
+// Surrogate training data (see surrogate_dataset_kernel).
+struct SurrogateGen {
+  unsigned long long seed;
+  long long count;
+  float solute_lo, solute_hi;  // per-sample solute fraction range
+  int base_code;               // species filling the non-solute sites
+  int kind;                    // 0 Quartic, 1 E0
+  int in_pad;                  // feature row length (>= 59 x one-hot alphabet)
+  __nv_bfloat16 *features;     // [count][in_pad]
+  float *ea;                   // [count]
+  double *ea64, *de64;         // optional [count]
+  int *status;
+};
+cudaError_t LaunchSurrogateDataset(const DevTables &t, const SurrogateGen &g, cudaStream_t stream);
+// Surrogate fallback: compact the pairs whose ensemble spread exceeds `threshold`
+// (flag per pair, optional), then merge the plain barriers of those pairs into ea.
+cudaError_t LaunchFallbackCompact(const long long *pairs, const float *mean, const float *spread, int m,
+                                  float threshold, long long *fb_pairs, int *fb_index, int *count, uint8_t *flag,
+                                  cudaStream_t stream);
+cudaError_t LaunchFallbackMerge(const float *mean, int m, const double *fb_ea, const int *fb_index, const int *count,
+                                double *ea, cudaStream_t stream);
+cudaError_t LaunchSurrogateFeatures(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
+                                    int in_pad, __nv_bfloat16 *features, int *status, cudaStream_t stream);
 // fn 0: ExpFast and exp; fn 1: RcpFast and 1 / x, over n device doubles.
 cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, long long n, double *fast, double *ref,
                                 cudaStream_t stream);

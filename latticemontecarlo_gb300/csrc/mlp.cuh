@@ -1,0 +1,43 @@
+// Device side of the BF16 MLP barrier surrogate (see mlp.cu).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace lmc {
+
+// Parameters of an ensemble (FP32 master copy, flat: W1, b1, W2, b2, w3, b3) and
+// the BF16 copies the GEMMs read.
+struct MlpDev {
+  int in, hidden, members;
+  float *w1, *b1, *w2, *b2, *w3, *b3;
+  __nv_bfloat16 *w1h, *w2h, *w2t;
+};
+
+// Activations of one batch (sizes for batch B, M members, H hidden).
+struct MlpWork {
+  float *z1, *z2;                 // [B][M*H]
+  __nv_bfloat16 *h1, *h2, *h1t;   // [B][M*H], h1t [M*H][B]
+  __nv_bfloat16 *dz1, *dz1t, *dz2, *dz2t;
+  float *y;                       // [M][B]
+};
+
+// Parameter count of an ensemble.
+inline long long MlpParamCount(int in, int hidden, int members) {
+  return static_cast<long long>(members) * (static_cast<long long>(hidden) * in + hidden +
+                                            static_cast<long long>(hidden) * hidden + hidden + hidden + 1);
+}
+
+cudaError_t MlpForward(const MlpDev &d, const __nv_bfloat16 *x, int batch, MlpWork &w, bool keep_ht, cudaStream_t s);
+// Gradients of the mean squared error of every member (flat, parameter order) and the per-member loss.
+cudaError_t MlpBackward(const MlpDev &d, const __nv_bfloat16 *x, const __nv_bfloat16 *xt, const float *t, int batch,
+                        MlpWork &w, float *grad, float *loss, cudaStream_t s);
+cudaError_t MlpGather(const __nv_bfloat16 *x, const float *labels, const int *idx, int batch, int in, float mean,
+                      float inv_std, __nv_bfloat16 *xb, float *tb, cudaStream_t s);
+cudaError_t MlpTranspose(const __nv_bfloat16 *in, int rows, int cols, __nv_bfloat16 *out, cudaStream_t s);
+cudaError_t MlpAdam(float *p, const float *grad, float *m1, float *m2, long long n, float lr, int step, cudaStream_t s);
+cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s);
+cudaError_t MlpEnsemble(const float *y, int batch, int members, float mean_label, float std_label, float *mean,
+                        float *spread, cudaStream_t s);
+
+}  // namespace lmc
