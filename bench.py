@@ -230,6 +230,8 @@ def run_ours(args, rank, world, local):
     }
     if args.cmc_steps > 0:
         result["cmc"] = run_cmc(args, device, flush, barrier)
+    if args.surrogate_samples > 0:
+        result["surrogate"] = run_surrogate(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -264,6 +266,124 @@ def run_cmc(args, device, flush, barrier):
             "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+
+
+def _vacancy_grid_lattice(n: int, spacing: int, fractions, seed: int, elements):
+    """n^3 FCC cells, vacancies on every site with all half-lattice coordinates
+    divisible by `spacing` (far enough apart that no jump environment holds a
+    second vacancy), the rest drawn i.i.d. from `fractions`; returns species and
+    the 12 jumps of every vacancy as (vacancy, neighbour) pairs."""
+    from latticemontecarlo_gb300 import synthetic as S
+    alpha = S.alphabet(elements)
+    rng = np.random.default_rng(seed)
+    names = list(fractions)
+    probs = np.array([fractions[k] for k in names], float)
+    probs /= probs.sum()
+    nsites = 4 * n ** 3
+    sp = np.array([alpha.index(k) for k in names], np.int8)[rng.choice(len(names), size=nsites, p=probs)]
+    m = 2 * n
+    g = np.arange(0, m, spacing)
+    hx, hy, hz = (a.ravel() for a in np.meshgrid(g, g, g, indexing="ij"))
+    vac = hx * 2 * n * n + hy * n + hz // 2
+    sp[vac] = alpha.index("X")
+    dirs = np.array([(a, b, 0) for a in (-1, 1) for b in (-1, 1)] + [(a, 0, b) for a in (-1, 1) for b in (-1, 1)] +
+                    [(0, a, b) for a in (-1, 1) for b in (-1, 1)])
+    pairs = []
+    for d in dirs:
+        x, y, z = (hx + d[0]) % m, (hy + d[1]) % m, (hz + d[2]) % m
+        pairs.append(np.stack([vac, x * 2 * n * n + y * n + z // 2], 1))
+    return sp, np.concatenate(pairs).astype(np.int64)
+
+
+def run_surrogate(args, device):
+    """Learned barrier surrogate (BF16 MLP ensemble on the tensor cores) against the
+    plain barrier predictor on the same lattice jumps, plus its accuracy."""
+    import ctypes as C
+
+    import torch
+
+    from latticemontecarlo_gb300 import api
+    from latticemontecarlo_gb300 import _native as N
+    from latticemontecarlo_gb300 import synthetic as S
+
+    el = ("Al", "Mg", "Zn")
+    coeffs = S.make_coefficients(el, 1234)
+    model = api.Model.from_coefficients(coeffs, list(el))
+    ctx = api.Context(model, device=device)
+    n, spacing = 96, 8
+    sp, pairs = _vacancy_grid_lattice(n, spacing, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 77, el)
+    ctx.set_lattices([n], sp)
+    nin = api.surrogate_feature_count(ctx)
+    # training data and training (2e6 barriers of the plain predictor)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, ea, _, _ = api.surrogate_dataset(ctx, 1, args.surrogate_samples, 0.0, 0.3, nin)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = api.Surrogate(nin, 256, 4, seed=1, device=device)
+    net.set_label_scale(float(ea.mean()), float(ea.std()))
+    t0 = time.perf_counter()
+    net.train(x, ea, batch=4096, epochs=args.surrogate_epochs, lr=2e-3, seed=2)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    flop_fwd = 2 * (nin * 1024 + 4 * 256 * 256 + 1024)  # per sample, 4 members
+    train_tflops = 3 * flop_fwd * args.surrogate_samples * args.surrogate_epochs / t_train / 1e12
+    del x, ea
+    xt, _, eat, _ = api.surrogate_dataset(ctx, 99, 1 << 17, 0.0, 0.3, nin)
+    mean_t, _ = net.predict(xt)
+    mae_heldout = float((mean_t.double() - eat).abs().mean())
+    # the same jumps through both paths
+    pd = torch.from_numpy(pairs).to(f"cuda:{device}")
+    m = pd.shape[0]
+    ea_plain = torch.empty(m, dtype=torch.float64, device=pd.device)
+    de_plain = torch.empty(m, dtype=torch.float64, device=pd.device)
+
+    def plain():
+        N.check(N.lib.lmc_barrier_batch_device(ctx._h, 0, 0, C.c_void_p(pd.data_ptr()), m,
+                                               C.c_void_p(ea_plain.data_ptr()), C.c_void_p(de_plain.data_ptr())))
+        N.check(N.lib.lmc_ctx_synchronize(ctx._h))
+
+    res = {}
+
+    def surrogate():
+        res["out"] = api.surrogate_barriers(ctx, net, pd, 0.010)
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    t_plain = timed(plain, 20)
+    t_sur = timed(surrogate, 20)
+    ea_sur, flag, nfb = res["out"]
+    mae_lattice = float((ea_sur - ea_plain).abs().mean())
+    # the network alone on a large feature batch: the tensor-core roofline
+    xb, _, _, _ = api.surrogate_dataset(ctx, 5, 1 << 20, 0.0, 0.3, nin)
+    t_mlp = timed(lambda: net.predict(xb), 5)
+    mlp_tflops = flop_fwd * xb.shape[0] / t_mlp / 1e12
+    peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
+    return {
+        "workload": f"{m} jumps ({m // 12} vacancies) in a {n}^3-cell FCC lattice, Al/Mg/Zn .96/.02/.02; "
+                    f"surrogate MLP {nin}-256-256-1 GELU x4 (bf16, fp32 accumulate), fallback spread > 10 meV",
+        "plain_barriers_per_s": m / t_plain,
+        "surrogate_barriers_per_s": m / t_sur,
+        "surrogate_over_plain": t_plain / t_sur,
+        "fallback_fraction": nfb / m,
+        "mae_mev_vs_plain_fp64": {"lattice_jumps_with_fallback": 1e3 * mae_lattice,
+                                  "held_out_random_envs_network_only": 1e3 * mae_heldout},
+        "network_barriers_per_s": xb.shape[0] / t_mlp,
+        "timing": "wall clock over 20 device-synchronised calls (two streams per surrogate call)",
+        "training": {"samples": args.surrogate_samples, "epochs": args.surrogate_epochs, "dataset_s": t_data,
+                     "train_s": t_train, "tflops": train_tflops},
+        "roofline": {"bound": "tensor", "kernel": "gemm_nt_kernel (mma.sync bf16)", "achieved": mlp_tflops,
+                     "peak": peak, "unit": "TFLOP/s", "frac": mlp_tflops / peak},
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -361,6 +481,8 @@ def main():
     ap.add_argument("--cpu-kmc-steps", type=int, default=1500)
     ap.add_argument("--cpu-cmc-attempts", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
+    ap.add_argument("--surrogate-epochs", type=int, default=30)
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
     args = ap.parse_args()
     rank, world, local = dist_info()
