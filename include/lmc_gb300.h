@@ -220,6 +220,9 @@ int lmc_mlp_gradients(lmc_mlp *mlp, const uint16_t *features, const float *label
  * (nullable, per member) is the mean loss of the last epoch in standardised units. */
 int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *features_dev, const float *labels_dev, int64_t n, int batch,
                   int epochs, float lr, uint64_t seed, float *loss);
+/* Inference kernels: 0 automatic (the fused tcgen05 kernel when hidden = 256 and
+ * in_features <= 256), 1 tcgen05, 2 the mma.sync GEMMs of training. */
+int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path);
 /* Ensemble mean and spread (max - min over members), eV, for n feature rows (device arrays). */
 int lmc_mlp_predict(lmc_mlp *mlp, const uint16_t *features_dev, int64_t n, float *mean_dev, float *spread_dev);
 

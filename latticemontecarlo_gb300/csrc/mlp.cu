@@ -45,12 +45,8 @@ __device__ __forceinline__ void Mma16816(float *c, const uint32_t *a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__device__ __forceinline__ float Gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float GeluGrad(float z) {
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
-  return cdf + z * pdf;
-}
+__device__ __forceinline__ float Gelu(float z) { return MlpGelu(z); }
+__device__ __forceinline__ float GeluGrad(float z) { return MlpGeluGrad(z); }
 
 // Epilogues.
 enum Epi : int {

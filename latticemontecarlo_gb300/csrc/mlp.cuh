@@ -6,6 +6,24 @@
 
 namespace lmc {
 
+// GELU, tanh form (Hendrycks & Gimpel, 2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
+// with the hardware tanh approximation (relative error ~2^-11, below BF16 resolution).
+#ifdef __CUDACC__
+__device__ __forceinline__ float MlpTanh(float u) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+__device__ __forceinline__ float MlpGelu(float z) {
+  const float t = MlpTanh(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
+  return 0.5f * z * (1.0f + t);
+}
+__device__ __forceinline__ float MlpGeluGrad(float z) {
+  const float t = MlpTanh(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f, z * z, 1.0f);
+}
+#endif
+
 // Parameters of an ensemble (FP32 master copy, flat: W1, b1, W2, b2, w3, b3) and
 // the BF16 copies the GEMMs read.
 struct MlpDev {
@@ -37,6 +55,11 @@ cudaError_t MlpGather(const __nv_bfloat16 *x, const float *labels, const int *id
 cudaError_t MlpTranspose(const __nv_bfloat16 *in, int rows, int cols, __nv_bfloat16 *out, cudaStream_t s);
 cudaError_t MlpAdam(float *p, const float *grad, float *m1, float *m2, long long n, float lr, int step, cudaStream_t s);
 cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s);
+// Fused tcgen05 inference (mlp_tc.cu): hidden 256, in <= 256 and a multiple of 64.
+bool MlpTcSupported(const MlpDev &d);
+size_t MlpTcSharedBytes(int in);
+cudaError_t MlpTcPredict(const MlpDev &d, const __nv_bfloat16 *x, long long n, float mean_label, float std_label,
+                         float *mean, float *spread, int *status, cudaStream_t s);
 cudaError_t MlpEnsemble(const float *y, int batch, int members, float mean_label, float std_label, float *mean,
                         float *spread, cudaStream_t s);
 

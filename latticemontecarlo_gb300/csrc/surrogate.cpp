@@ -39,6 +39,8 @@ struct lmc_mlp {
   float *params{nullptr}, *grad{nullptr}, *m1{nullptr}, *m2{nullptr}, *loss{nullptr};
   float label_mean{0.f}, label_std{1.f};
   int step{0};
+  int path{0};  // inference: 0 automatic (tcgen05 when supported), 1 tcgen05, 2 mma.sync
+  int *status{nullptr};
   int cap{0};
   lmc::MlpWork w{};
   __nv_bfloat16 *xb{nullptr}, *xt{nullptr};
@@ -115,6 +117,7 @@ int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_
     m->m1 = DevAlloc<float>(m->num_params, &m->owned);
     m->m2 = DevAlloc<float>(m->num_params, &m->owned);
     m->loss = DevAlloc<float>(members, &m->owned);
+    m->status = DevAlloc<int>(1, &m->owned);
     const long long H = hidden, M = members;
     m->d.w1 = m->params;
     m->d.b1 = m->d.w1 + M * H * in_features;
@@ -261,11 +264,32 @@ int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *x_dev, const float *labels_dev, 
   });
 }
 
+int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path) {
+  return Guard([&] {
+    Require(mlp != nullptr, LMC_ERR_INVALID_ARGUMENT, "mlp is null");
+    Require(path >= 0 && path <= 2, LMC_ERR_INVALID_ARGUMENT, "path must be 0, 1 or 2");
+    Require(path != 1 || lmc::MlpTcSupported(mlp->d), LMC_ERR_UNSUPPORTED,
+            "the tcgen05 path needs hidden = 256 and in_features <= 256");
+    mlp->path = path;
+  });
+}
+
 int lmc_mlp_predict(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean_dev, float *spread_dev) {
   return Guard([&] {
     Require(mlp && x_dev && mean_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
     Require(n >= 0, LMC_ERR_INVALID_ARGUMENT, "n < 0");
     CudaCheck(cudaSetDevice(mlp->device), "cudaSetDevice");
+    if (mlp->path != 2 && lmc::MlpTcSupported(mlp->d)) {
+      CudaCheck(cudaMemsetAsync(mlp->status, 0, sizeof(int), mlp->stream), "memset");
+      CudaCheck(lmc::MlpTcPredict(mlp->d, reinterpret_cast<const __nv_bfloat16 *>(x_dev), n, mlp->label_mean,
+                                  mlp->label_std, mean_dev, spread_dev, mlp->status, mlp->stream),
+                "tcgen05 inference");
+      int st = 0;
+      CudaCheck(cudaMemcpyAsync(&st, mlp->status, sizeof(int), cudaMemcpyDeviceToHost, mlp->stream), "D2H");
+      CudaCheck(cudaStreamSynchronize(mlp->stream), "sync");
+      Require(st == 0, LMC_ERR_STOPPED, "tcgen05 inference: a tensor-core wait expired");
+      return;
+    }
     mlp->Reserve(kPredictChunk);
     const auto *x = reinterpret_cast<const __nv_bfloat16 *>(x_dev);
     for (int64_t off = 0; off < n; off += kPredictChunk) {

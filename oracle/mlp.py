@@ -2,17 +2,14 @@
 the checker of the GPU's forward and backward kernels, never on the product path).
 
 Architecture per member m: z1 = x W1[m]^T + b1[m], h1 = GELU(z1), z2 = h1 W2[m]^T + b2[m],
-h2 = GELU(z2), y = h2 . w3[m] + b3[m]; loss_m = mean_b (y - t)^2. GELU is the exact
-x * Phi(x). Parameters are the flat layout of lmc_mlp_get_params:
+h2 = GELU(z2), y = h2 . w3[m] + b3[m]; loss_m = mean_b (y - t)^2. GELU is the tanh
+form 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) (exact tanh here). Parameters are the flat layout of lmc_mlp_get_params:
 W1 [M*H][in], b1 [M*H], W2 [M][H][H], b2 [M*H], w3 [M*H], b3 [M]."""
 from __future__ import annotations
 
 import math
 
 import numpy as np
-
-_erf = np.vectorize(math.erf)
-
 
 def bf16_round(a: np.ndarray) -> np.ndarray:
     """Round float32 values to bfloat16 (nearest even), returned as float64."""
@@ -37,12 +34,16 @@ def unpack(p: np.ndarray, in_features: int, hidden: int, members: int):
     return W1, b1, W2, b2, w3, b3
 
 
+_C = math.sqrt(2.0 / math.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + 0.044715 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def forward_backward(p, x, t, in_features, hidden, members, bf16_weights=True):
@@ -78,3 +79,17 @@ def forward_backward(p, x, t, in_features, hidden, members, bf16_weights=True):
         gb1[sl] = dz1.sum(0)
     flat = np.concatenate([gW1.ravel(), gb1.ravel(), gW2.ravel(), gb2.ravel(), gw3.ravel(), gb3.ravel()])
     return np.array(losses), flat
+
+
+def predict(p, x, in_features, hidden, members, bf16_weights=True):
+    """Per-member outputs y [members][B] (float64, standardised label units)."""
+    p = np.asarray(p, np.float64)
+    W1, b1, W2, b2, w3, b3 = unpack(p, in_features, hidden, members)
+    if bf16_weights:
+        W1, W2 = bf16_round(W1), bf16_round(W2)
+    h1 = gelu(np.asarray(x, np.float64) @ W1.T + b1)
+    out = []
+    for m in range(members):
+        sl = slice(m * hidden, (m + 1) * hidden)
+        out.append(gelu(h1[:, sl] @ W2[m].T + b2[m]) @ w3[m] + b3[m])
+    return np.array(out)

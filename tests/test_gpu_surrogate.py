@@ -106,3 +106,27 @@ def test_trained_ensemble(setup):
     fb = spread > 0.010
     merged = torch.where(fb, ea64t, mean.double())
     assert float((merged - ea64t).abs().mean()) <= mae
+
+
+def test_tcgen05_inference(setup):
+    """The fused tcgen05 kernel against the mma.sync path and the float64 network,
+    on 1000 rows (a partial last tile of 128)."""
+    torch, api, ctx, el, coeffs, nin = setup
+    from oracle import mlp as R
+    net = api.Surrogate(nin, 256, 4, seed=3)
+    x, ea, _, _ = api.surrogate_dataset(ctx, 31, 1 << 16, 0.0, 0.3, nin)
+    net.set_label_scale(float(ea.mean()), float(ea.std()))
+    net.train(x, ea, batch=4096, epochs=2, lr=2e-3, seed=4)
+    xs = x[:1000].contiguous()
+    net.set_inference_path(1)
+    m_tc, s_tc = net.predict(xs)
+    net.set_inference_path(2)
+    m_ref, s_ref = net.predict(xs)
+    net.set_inference_path(0)
+    m_tc, s_tc, m_ref, s_ref = (t.double().cpu().numpy() for t in (m_tc, s_tc, m_ref, s_ref))
+    assert np.all(np.isfinite(m_tc))
+    np.testing.assert_allclose(m_tc, m_ref, rtol=0, atol=2e-3)
+    np.testing.assert_allclose(s_tc, s_ref, rtol=0, atol=3e-3)
+    y = R.predict(net.params(), R.bf16_bits_to_float(_bits(xs)), nin, 256, 4)
+    mu, sd = float(np.float32(float(ea.mean()))), float(np.float32(float(ea.std())))
+    np.testing.assert_allclose(m_tc, mu + sd * y.mean(0), rtol=0, atol=3e-3)
