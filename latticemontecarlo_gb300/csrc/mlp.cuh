@@ -30,6 +30,11 @@ struct MlpDev {
   int in, hidden, members;
   float *w1, *b1, *w2, *b2, *w3, *b3;
   __nv_bfloat16 *w1h, *w2h, *w2t;
+  // W1 and W2 again, cut into 256-row x 32-K blocks stored contiguously in the
+  // tensor cores' shared-memory operand layout (see mlp_tc.cu), so one bulk copy
+  // moves a block: member m, block c of W1 at (m * in / 32 + c) * 8192 elements,
+  // of W2 at (m * hidden / 32 + c) * 8192 elements.
+  __nv_bfloat16 *w1_tiles, *w2_tiles;
 };
 
 // Activations of one batch (sizes for batch B, M members, H hidden).

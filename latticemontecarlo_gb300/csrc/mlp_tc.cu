@@ -1,19 +1,28 @@
 // Fused ensemble inference of the BF16 barrier surrogate on the 5th-generation
 // tensor cores (tcgen05): one persistent CTA per SM walks tiles of 128 samples.
 // Per tile and member m:
-//   D1 (TMEM, 128 x 256 fp32) = X (smem) . W1[m]^T          tcgen05.mma kind::f16, K in chunks of 64
-//   H1 (smem, bf16)            = GELU(D1 + b1[m])            tcgen05.ld epilogue, written in operand layout
+//   D1 (TMEM, 128 x 256 fp32) = X (smem) . W1[m]^T            tcgen05.mma kind::f16
+//   H1 (smem, bf16)            = GELU(D1 + b1[m])              epilogue warps (tcgen05.ld)
 //   D2 (TMEM)                  = H1 . W2[m]^T
-//   y_m                        = GELU(D2 + b2[m]) . w3[m] + b3[m]   (in registers, one row per thread pair)
-// then the ensemble mean and spread. Weight chunks (256 rows x 64 K, 32 KB) stream
-// through a double buffer with cp.async while the tensor cores work on the other.
+//   y_m                        = GELU(D2 + b2[m]) . w3[m] + b3[m]
+// then the ensemble mean and spread.
+//
+// Warp roles, coordinated by mbarriers (no block-wide barrier inside the loop):
+//   warp 0     producer: cp.async of the X tiles (fence.proxy.async, then arrive),
+//              and one bulk copy (cp.async.bulk, completing on the stage's
+//              mbarrier) per weight block of 256 rows x 32 K (16 KB, pre-tiled in
+//              global memory) into a ring of kStages buffers;
+//   warp 1     one thread issues the MMAs and the tcgen05.commit arrivals;
+//   warps 2-9  epilogue: TMEM lane group = warp % 4, column half = (warp - 2) / 4.
+// The layer-1 MMAs of member m + 1 overlap the layer-2 epilogue of member m.
 //
 // Operand layout in shared memory (K-major, no swizzle): 8-row x 16-byte core
-// matrices; element (r, k) of a tile with K columns sits at
-//   (r / 8) * (K / 8) * 128 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
-// i.e. leading-dimension (K) byte offset 128 and stride (8-row group) byte offset
-// K * 16. Every wait on the tensor cores is bounded; on expiry the kernel records
-// kMlpTimeout, waits (bounded) for its last commit, frees its TMEM and returns.
+// matrices; an operand tile of 32 K columns keeps element (r, k) at
+//   (r / 8) * 512 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// i.e. leading (K) byte offset 128 and 8-row stride 512; X and H1 are stored as
+// consecutive such tiles. Every wait is bounded and also polls a shared abort
+// flag: on expiry the kernel records kMlpTimeout, drains its MMAs (bounded wait
+// on a final commit) and its copies, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -24,22 +33,26 @@
 namespace lmc {
 namespace {
 
-constexpr int kTcRows = 128;       // samples per tile (MMA M)
-constexpr int kTcHidden = 256;     // MMA N and the hidden width
-constexpr int kTcChunk = 64;       // K per weight chunk
-constexpr int kTcThreads = 256;    // 8 warps: TMEM lane group = warp % 4, column half = warp / 4
+constexpr int kTcRows = 128;     // samples per tile (MMA M)
+constexpr int kTcHidden = 256;   // MMA N and the hidden width
+constexpr int kTcK = 32;         // K per operand tile / weight chunk
+constexpr int kTcTile = kTcRows * kTcK;           // elements of a 128 x 32 operand tile
+constexpr int kTcChunkElems = kTcHidden * kTcK;   // elements of a 256 x 32 weight chunk (16 KB)
+constexpr int kTcStages = 6;
+constexpr int kTcThreads = 320;  // 10 warps
 constexpr uint32_t kTmemCols = 512;
 constexpr int kMlpTimeout = 1;
 constexpr long long kWaitLimit = 1LL << 26;
+constexpr uint32_t kSbo = kTcK * 16;  // 8-row group stride of a 32-wide operand tile
 
 __device__ __forceinline__ uint32_t Smem(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ uint64_t OperandDesc(uint32_t addr, uint32_t sbo) {
+__device__ __forceinline__ uint64_t OperandDesc(uint32_t addr) {
   uint64_t d = static_cast<uint64_t>((addr & 0x3FFFF) >> 4);
-  d |= static_cast<uint64_t>(128 >> 4) << 16;             // leading (K) byte offset between core matrices
-  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;  // stride byte offset between 8-row groups
-  d |= static_cast<uint64_t>(1) << 46;                    // descriptor version of sm_100 and later
-  return d;                                               // base offset 0, no swizzle
+  d |= static_cast<uint64_t>(128 >> 4) << 16;  // leading (K) byte offset between core matrices
+  d |= static_cast<uint64_t>(kSbo >> 4) << 32; // stride byte offset between 8-row groups
+  d |= static_cast<uint64_t>(1) << 46;         // descriptor version of sm_100 and later
+  return d;                                    // base offset 0, no swizzle
 }
 
 // kind::f16 instruction descriptor: D fp32, A and B bf16, both K-major, N = 256, M = 128.
@@ -54,23 +67,55 @@ __device__ __forceinline__ void Mma(uint32_t tmem, uint64_t a, uint64_t b, bool 
 __device__ __forceinline__ void Commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(Smem(bar)));
 }
-// Waits for the completion of the barrier phase with the given parity; false on expiry.
-__device__ __forceinline__ bool WaitPhase(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ void Arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(Smem(bar)) : "memory");
+}
+__device__ __forceinline__ void BarInit(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(Smem(bar)), "r"(count));
+}
+__device__ __forceinline__ bool TryWait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(Smem(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the completion of the barrier phase with the given parity. False
+// when it expires or another warp gave up (the abort flag), which it then sets.
+__device__ __forceinline__ bool Wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
   for (long long it = 0; it < kWaitLimit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(Smem(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
+    if (TryWait(bar, parity)) return true;
+    if ((it & 63) == 0 && *abort) return false;
   }
+  *abort = 1;
   return false;
+}
+// Bounded wait that ignores the abort flag (draining work already issued).
+__device__ __forceinline__ bool WaitDrain(uint64_t *bar, uint32_t parity) {
+  for (long long it = 0; it < kWaitLimit; ++it)
+    if (TryWait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void ArriveExpectTx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(Smem(bar)), "r"(bytes) : "memory");
+}
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on `bar`.
+__device__ __forceinline__ void BulkCopy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(Smem(dst)),
+      "l"(src), "r"(bytes), "r"(Smem(bar))
+      : "memory");
 }
 __device__ __forceinline__ void CpAsync16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(Smem(smem)), "l"(gmem));
 }
-__device__ __forceinline__ void CpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void CpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int kPending>
+__device__ __forceinline__ void CpAsyncWait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
+}
 __device__ __forceinline__ void FenceAsyncSmem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void TmemLoad32(uint32_t addr, float *v) {
@@ -88,18 +133,18 @@ __device__ __forceinline__ void TmemLoad32(uint32_t addr, float *v) {
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Loads rows [row0, row0 + rows) x K columns [k0, k0 + 64) of a row-major bf16
-// matrix (leading dimension ld) into a 64-wide operand tile (zeros past `valid` rows).
-__device__ __forceinline__ void LoadChunk(__nv_bfloat16 *dst, const __nv_bfloat16 *src, int ld, int rows, int valid,
-                                          int k0) {
-  char *d = reinterpret_cast<char *>(dst);
-  for (int c = threadIdx.x; c < rows * 8; c += kTcThreads) {
-    const int r = c >> 3, kc = c & 7;
-    char *to = d + (r >> 3) * (kTcChunk / 8) * 128 + kc * 128 + (r & 7) * 16;
-    if (r < valid) CpAsync16(to, src + static_cast<long long>(r) * ld + k0 + kc * 8);
-    else *reinterpret_cast<uint4 *>(to) = make_uint4(0, 0, 0, 0);
-  }
+// Byte offset of element (r, k) in a sequence of 32-wide operand tiles of `rows` rows.
+__device__ __forceinline__ uint32_t TileOffset(int rows, int r, int k) {
+  return static_cast<uint32_t>((k / kTcK) * rows * kTcK * 2 + (r >> 3) * kSbo + ((k % kTcK) >> 3) * 128 + (r & 7) * 16);
 }
+
+struct TcBars {
+  uint64_t full[kTcStages], empty[kTcStages];
+  uint64_t x_full, x_empty, d1_full, d1_empty, h1_full, h1_empty, d2_full, d2_empty, part_full, part_empty, done;
+  int abort;
+  uint32_t tmem;
+  float partial[kTcRows];
+};
 
 }  // namespace
 
@@ -108,174 +153,225 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         float *mean, float *spread, int *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int K1 = d.in, members = d.members;
-  const int k1_chunks = K1 / kTcChunk, k2_chunks = kTcHidden / kTcChunk;
-  // X tile as k1_chunks tiles of 128 x 64, H1 as 4 tiles of 128 x 64, two 256 x 64 weight buffers
-  __nv_bfloat16 *sx = reinterpret_cast<__nv_bfloat16 *>(smem);
-  __nv_bfloat16 *sh = sx + kTcRows * K1;
-  __nv_bfloat16 *sw = sh + kTcRows * kTcHidden;
-  float *partial = reinterpret_cast<float *>(sw + 2 * kTcHidden * kTcChunk);  // [128] second column half
-  uint64_t *bar = reinterpret_cast<uint64_t *>(partial + kTcRows);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int k1_tiles = K1 / kTcK, k2_tiles = kTcHidden / kTcK;
+  __nv_bfloat16 *sx = reinterpret_cast<__nv_bfloat16 *>(smem);         // k1_tiles x (128 x 32)
+  __nv_bfloat16 *sh = sx + kTcRows * K1;                                // 8 x (128 x 32)
+  __nv_bfloat16 *sw = sh + kTcRows * kTcHidden;                         // kStages x (256 x 32)
+  TcBars *bars = reinterpret_cast<TcBars *>(sw + kTcStages * kTcChunkElems);
+  volatile int *abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int row = (warp & 3) * 32 + lane, half = warp >> 2;
 
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(Smem(tmem_slot)),
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; ++i) {
+      BarInit(&bars->full[i], 1);
+      BarInit(&bars->empty[i], 1);
+    }
+    BarInit(&bars->x_full, 32);
+    BarInit(&bars->x_empty, 1);
+    BarInit(&bars->d1_full, 1);
+    BarInit(&bars->d1_empty, 8);
+    BarInit(&bars->h1_full, 8);
+    BarInit(&bars->h1_empty, 1);
+    BarInit(&bars->d2_full, 1);
+    BarInit(&bars->d2_empty, 8);
+    BarInit(&bars->part_full, 4);
+    BarInit(&bars->part_empty, 4);
+    BarInit(&bars->done, 1);
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(Smem(&bars->tmem)),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(Smem(bar)));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmem = bars->tmem;
   const uint32_t d1 = tmem, d2 = tmem + kTcHidden;
-  const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
-
-  uint32_t commits = 0;  // commits issued so far; commit j completes barrier phase j
-  bool failed = false;
-  const int chunks_per_member = k1_chunks + k2_chunks;
-  const int chunks = members * chunks_per_member;
-  const uint32_t sbo_w = kTcChunk * 16;  // 8-row group stride of a 64-wide operand tile
   const long long tiles = (n + kTcRows - 1) / kTcRows;
+  const int chunks_per_member = k1_tiles + k2_tiles;
 
-  auto chunk_src = [&](int q, const __nv_bfloat16 *&src, int &ld, int &k0) {
-    const int m = q / chunks_per_member, c = q % chunks_per_member;
-    if (c < k1_chunks) {
-      src = d.w1h + static_cast<long long>(m) * kTcHidden * K1;
-      ld = K1;
-      k0 = c * kTcChunk;
-    } else {
-      src = d.w2h + static_cast<long long>(m) * kTcHidden * kTcHidden;
-      ld = kTcHidden;
-      k0 = (c - k1_chunks) * kTcChunk;
-    }
-  };
-
-  for (long long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
-    const long long r0 = tile * kTcRows;
-    const int valid = static_cast<int>(n - r0 < kTcRows ? n - r0 : kTcRows);
-    // X tile (one 128 x 64 operand tile per K chunk) and the first weight chunk
-    for (int c = 0; c < k1_chunks; ++c)
-      LoadChunk(sx + c * kTcRows * kTcChunk, x + r0 * K1, K1, kTcRows, valid, c * kTcChunk);
-    {
-      const __nv_bfloat16 *src;
-      int ld, k0;
-      chunk_src(0, src, ld, k0);
-      LoadChunk(sw, src, ld, kTcHidden, kTcHidden, k0);
-    }
-    CpAsyncWaitAll();
-    FenceAsyncSmem();
-    __syncthreads();
-    float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
-    for (int q = 0; q < chunks && !failed; ++q) {
-      const int m = q / chunks_per_member, c = q % chunks_per_member;
-      // the buffer of chunk q + 1 was read by chunk q - 1: wait for it, then prefetch
-      // (the failure flag is made uniform over the CTA before anyone branches on it)
-      if (q >= 1) failed = __syncthreads_or(!WaitPhase(bar, (commits - 1) & 1));
-      if (q + 1 < chunks && !failed) {
-        const __nv_bfloat16 *src;
-        int ld, k0;
-        chunk_src(q + 1, src, ld, k0);
-        LoadChunk(sw + ((q + 1) & 1) * kTcHidden * kTcChunk, src, ld, kTcHidden, kTcHidden, k0);
+  if (warp == 0) {
+    // ---- producer: X tiles with cp.async (all lanes; fence, then arrive on x_full),
+    // weight blocks with one bulk copy each (lane 0; completes on the stage's full barrier) ----
+    long long g = 0;  // weight blocks issued
+    int t_local = 0;
+    bool stop = false;
+    for (long long tile = blockIdx.x; tile < tiles && !stop; tile += gridDim.x, ++t_local) {
+      const long long r0 = tile * kTcRows;
+      const int valid = static_cast<int>(n - r0 < kTcRows ? n - r0 : kTcRows);
+      if (t_local >= 1 && !Wait(&bars->x_empty, (t_local - 1) & 1, abort)) break;
+      for (int c = lane; c < kTcRows * (K1 / 8); c += 32) {
+        const int r = c / (K1 / 8), k = (c % (K1 / 8)) * 8;
+        char *to = reinterpret_cast<char *>(sx) + TileOffset(kTcRows, r, k);
+        if (r < valid) CpAsync16(to, x + (r0 + r) * K1 + k);
+        else *reinterpret_cast<uint4 *>(to) = make_uint4(0, 0, 0, 0);
       }
-      if (failed) break;
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t b = Smem(sw + (q & 1) * kTcHidden * kTcChunk);
-        const bool layer1 = c < k1_chunks;
-        const int kc = layer1 ? c : c - k1_chunks;
-        const uint32_t a = layer1 ? Smem(sx + kc * kTcRows * kTcChunk) : Smem(sh + kc * kTcRows * kTcChunk);
-#pragma unroll
-        for (int s = 0; s < kTcChunk / 16; ++s)
-          Mma(layer1 ? d1 : d2, OperandDesc(a + s * 256, sbo_w), OperandDesc(b + s * 256, sbo_w),
-              kc > 0 || s > 0);
-        Commit(bar);
-      }
-      ++commits;
-      const bool end1 = c == k1_chunks - 1, end2 = c == chunks_per_member - 1;
-      if (end1 || end2) {
-        failed = __syncthreads_or(!WaitPhase(bar, (commits - 1) & 1));
-        if (failed) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (end1) {
-          // H1 = GELU(D1 + b1): this thread's row, columns [128 half, 128 half + 128)
-          const float *b1 = d.b1 + m * kTcHidden;
-#pragma unroll 1
-          for (int j0 = 0; j0 < 128; j0 += 32) {
-            float v[32];
-            const int col0 = half * 128 + j0;
-            TmemLoad32(d1 + lane_base + col0, v);
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-              uint32_t packed[4];
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const int col = col0 + g * 8 + 2 * e;
-                const __nv_bfloat162 p = __floats2bfloat162_rn(MlpGelu(v[g * 8 + 2 * e] + __ldg(&b1[col])),
-                                                               MlpGelu(v[g * 8 + 2 * e + 1] + __ldg(&b1[col + 1])));
-                packed[e] = *reinterpret_cast<const uint32_t *>(&p);
-              }
-              const int col = col0 + g * 8;  // 8 consecutive columns: one 16-byte row of a core matrix
-              char *to = reinterpret_cast<char *>(sh + (col / kTcChunk) * kTcRows * kTcChunk) + (row >> 3) * sbo_w +
-                         ((col % kTcChunk) >> 3) * 128 + (row & 7) * 16;
-              *reinterpret_cast<uint4 *>(to) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+      CpAsyncCommit();
+      CpAsyncWait<0>();
+      FenceAsyncSmem();
+      Arrive(&bars->x_full);
+      if (lane == 0) {
+        for (int m = 0; m < members && !stop; ++m)
+          for (int c = 0; c < chunks_per_member; ++c, ++g) {
+            const int s = static_cast<int>(g % kTcStages);
+            const long long round = g / kTcStages;
+            if (round >= 1 && !Wait(&bars->empty[s], (round - 1) & 1, abort)) {
+              stop = true;
+              break;
             }
+            const __nv_bfloat16 *src =
+                c < k1_tiles ? d.w1_tiles + (static_cast<long long>(m) * k1_tiles + c) * kTcChunkElems
+                             : d.w2_tiles + (static_cast<long long>(m) * k2_tiles + (c - k1_tiles)) * kTcChunkElems;
+            ArriveExpectTx(&bars->full[s], kTcChunkElems * 2);
+            BulkCopy(sw + s * kTcChunkElems, src, kTcChunkElems * 2, &bars->full[s]);
           }
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-          FenceAsyncSmem();
-        } else {
-          // y_m = GELU(D2 + b2) . w3 + b3 over this thread's 128 columns
-          const float *b2 = d.b2 + m * kTcHidden, *w3 = d.w3 + m * kTcHidden;
-          float acc = 0.f;
-#pragma unroll 1
-          for (int j0 = 0; j0 < 128; j0 += 32) {
-            float v[32];
-            const int col0 = half * 128 + j0;
-            TmemLoad32(d2 + lane_base + col0, v);
-#pragma unroll
-            for (int e = 0; e < 32; ++e) acc += MlpGelu(v[e] + __ldg(&b2[col0 + e])) * __ldg(&w3[col0 + e]);
+      }
+      stop = __shfl_sync(0xffffffffu, stop ? 1 : 0, 0) != 0;
+    }
+    CpAsyncWait<0>();
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      long long g = 0;
+      int u = 0, t_local = 0;
+      bool ok = true;
+      for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t_local) {
+        ok = Wait(&bars->x_full, t_local & 1, abort);
+        for (int m = 0; m < members && ok; ++m, ++u) {
+          if (u >= 1 && !(ok = Wait(&bars->d1_empty, (u - 1) & 1, abort))) break;
+          for (int c = 0; c < k1_tiles && ok; ++c, ++g) {
+            const int s = static_cast<int>(g % kTcStages);
+            if (!(ok = Wait(&bars->full[s], (g / kTcStages) & 1, abort))) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a = Smem(sx + c * kTcTile), b = Smem(sw + s * kTcChunkElems);
+            Mma(d1, OperandDesc(a), OperandDesc(b), c > 0);
+            Mma(d1, OperandDesc(a + 256), OperandDesc(b + 256), true);
+            Commit(&bars->empty[s]);
           }
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-          if (half == 1) partial[row] = acc;
-          __syncthreads();
-          if (half == 0) {
-            const float y = acc + partial[row] + __ldg(&d.b3[m]);
-            ysum += y;
-            ymin = fminf(ymin, y);
-            ymax = fmaxf(ymax, y);
+          if (!ok) break;
+          Commit(&bars->d1_full);
+          if (m == members - 1) Commit(&bars->x_empty);
+          if (!(ok = Wait(&bars->h1_full, u & 1, abort))) break;
+          if (u >= 1 && !(ok = Wait(&bars->d2_empty, (u - 1) & 1, abort))) break;
+          for (int c = 0; c < k2_tiles && ok; ++c, ++g) {
+            const int s = static_cast<int>(g % kTcStages);
+            if (!(ok = Wait(&bars->full[s], (g / kTcStages) & 1, abort))) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a = Smem(sh + c * kTcTile), b = Smem(sw + s * kTcChunkElems);
+            Mma(d2, OperandDesc(a), OperandDesc(b), c > 0);
+            Mma(d2, OperandDesc(a + 256), OperandDesc(b + 256), true);
+            Commit(&bars->empty[s]);
           }
+          if (!ok) break;
+          Commit(&bars->d2_full);
+          Commit(&bars->h1_empty);
         }
       }
-      CpAsyncWaitAll();
-      FenceAsyncSmem();
-      __syncthreads();
+      // drain: the done barrier completes when every MMA issued so far has finished
+      Commit(&bars->done);
+      if (!WaitDrain(&bars->done, 0)) *abort = 1;
     }
-    if (!failed && half == 0 && row < valid) {
-      mean[r0 + row] = mean_label + std_label * ysum / members;
-      if (spread) spread[r0 + row] = std_label * (ymax - ymin);
+    __syncwarp();
+  } else {
+    // ---- epilogue warps ----
+    const int ew = warp - 2, half = ew >> 2;
+    const int row = (warp & 3) * 32 + lane;
+    const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
+    int u = 0;
+    bool ok = true;
+    for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+      const long long r0 = tile * kTcRows;
+      const int valid = static_cast<int>(n - r0 < kTcRows ? n - r0 : kTcRows);
+      float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
+      for (int m = 0; m < members && ok; ++m, ++u) {
+        // H1 = GELU(D1 + b1): this thread's row, columns [128 half, 128 half + 128)
+        if (!(ok = Wait(&bars->d1_full, u & 1, abort))) break;
+        if (u >= 1 && !(ok = Wait(&bars->h1_empty, (u - 1) & 1, abort))) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const float *b1 = d.b1 + m * kTcHidden;
+#pragma unroll 1
+        for (int j0 = 0; j0 < 128; j0 += 32) {
+          float v[32];
+          const int col0 = half * 128 + j0;
+          TmemLoad32(d1 + lane_base + col0, v);
+#pragma unroll
+          for (int g8 = 0; g8 < 4; ++g8) {
+            uint32_t packed[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int col = col0 + g8 * 8 + 2 * e;
+              const __nv_bfloat162 p = __floats2bfloat162_rn(MlpGelu(v[g8 * 8 + 2 * e] + __ldg(&b1[col])),
+                                                             MlpGelu(v[g8 * 8 + 2 * e + 1] + __ldg(&b1[col + 1])));
+              packed[e] = *reinterpret_cast<const uint32_t *>(&p);
+            }
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(sh) + TileOffset(kTcRows, row, col0 + g8 * 8)) =
+                make_uint4(packed[0], packed[1], packed[2], packed[3]);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        FenceAsyncSmem();
+        __syncwarp();
+        if (lane == 0) {
+          Arrive(&bars->d1_empty);
+          Arrive(&bars->h1_full);
+        }
+        // y_m = GELU(D2 + b2) . w3 + b3
+        if (!(ok = Wait(&bars->d2_full, u & 1, abort))) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const float *b2 = d.b2 + m * kTcHidden, *w3 = d.w3 + m * kTcHidden;
+        float acc = 0.f;
+#pragma unroll 1
+        for (int j0 = 0; j0 < 128; j0 += 32) {
+          float v[32];
+          const int col0 = half * 128 + j0;
+          TmemLoad32(d2 + lane_base + col0, v);
+#pragma unroll
+          for (int e = 0; e < 32; ++e) acc += MlpGelu(v[e] + __ldg(&b2[col0 + e])) * __ldg(&w3[col0 + e]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) Arrive(&bars->d2_empty);
+        // the two column halves of a row meet in shared memory: half 1 publishes
+        // (part_full), half 0 consumes and releases the slots (part_empty)
+        if (half == 1) {
+          if (u >= 1 && !(ok = Wait(&bars->part_empty, (u - 1) & 1, abort))) break;
+          bars->partial[row] = acc;
+          __syncwarp();
+          if (lane == 0) Arrive(&bars->part_full);
+        } else {
+          if (!(ok = Wait(&bars->part_full, u & 1, abort))) break;
+          const float y = acc + bars->partial[row] + __ldg(&d.b3[m]);
+          __syncwarp();
+          if (lane == 0) Arrive(&bars->part_empty);
+          ysum += y;
+          ymin = fminf(ymin, y);
+          ymax = fmaxf(ymax, y);
+        }
+      }
+      if (ok && half == 0 && row < valid) {
+        mean[r0 + row] = mean_label + std_label * ysum / members;
+        if (spread) spread[r0 + row] = std_label * (ymax - ymin);
+      }
     }
   }
-  if (failed) {
-    if (tid == 0) atomicOr(status, kMlpTimeout);
-    WaitPhase(bar, (commits - 1) & 1);  // the last commit, bounded
-  }
-  CpAsyncWaitAll();
+  __syncthreads();
+  if (tid == 0 && bars->abort) atomicOr(status, kMlpTimeout);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
 size_t MlpTcSharedBytes(int in) {
   return static_cast<size_t>(kTcRows) * in * 2 + static_cast<size_t>(kTcRows) * kTcHidden * 2 +
-         2ull * kTcHidden * kTcChunk * 2 + kTcRows * 4 + 16 + 1024;
+         static_cast<size_t>(kTcStages) * kTcChunkElems * 2 + sizeof(TcBars);
 }
 
 bool MlpTcSupported(const MlpDev &d) {
-  return d.hidden == kTcHidden && d.in % kTcChunk == 0 && d.in <= 256 && d.members >= 1 && d.members <= 16;
+  return d.hidden == kTcHidden && d.in % 64 == 0 && d.in <= 256 && d.members >= 1 && d.members <= 16 &&
+         MlpTcSharedBytes(d.in) <= 227 * 1024;
 }
 
 cudaError_t MlpTcPredict(const MlpDev &d, const __nv_bfloat16 *x, long long n, float mean_label, float std_label,
