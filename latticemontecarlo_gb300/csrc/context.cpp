@@ -19,6 +19,7 @@
 #include "kernels.cuh"
 #include "model.hpp"
 #include "abi_common.hpp"
+#include "mlp.cuh"
 
 namespace {
 using lmc::abi::CudaCheck;
@@ -1132,32 +1133,39 @@ int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, 
     ctx->s_fb_de.Ensure(sizeof(double) * mm);
     const auto *pairs = reinterpret_cast<const long long *>(pairs_dev);
     ctx->ClearStatus();
-    CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica], pairs, m, in,
-                                           ctx->s_feat.as<__nv_bfloat16>(), ctx->status.as<int>(), ctx->stream),
+    CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                           pairs, m, in, ctx->s_feat.as<__nv_bfloat16>(), ctx->status.as<int>(),
+                                           ctx->stream),
               "features kernel");
-    // the network runs on its own stream: order it after the features
-    ctx->Sync();
-    const int st = lmc_mlp_predict(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(),
-                                   ctx->s_spread.as<float>());
-    if (st != LMC_OK) throw LmcError(st, lmc_last_error());
+    // the network on the context stream when the fused kernel serves it, else on its own (synchronised)
+    if (!lmc::MlpPredictAsync(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(), ctx->s_spread.as<float>(),
+                               ctx->stream)) {
+      ctx->Sync();
+      const int st = lmc_mlp_predict(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(),
+                                     ctx->s_spread.as<float>());
+      if (st != LMC_OK) throw LmcError(st, lmc_last_error());
+    }
     int *d_count = ctx->s_fb_index.as<int>() + mm;
     CudaCheck(cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream), "memset");
     CudaCheck(lmc::LaunchFallbackCompact(pairs, ctx->s_mean.as<float>(), ctx->s_spread.as<float>(), m, threshold_ev,
                                          ctx->s_fb_pairs.as<long long>(), ctx->s_fb_index.as<int>(), d_count,
                                          fallback_dev, ctx->stream),
               "fallback kernel");
-    int count = 0;
-    CudaCheck(cudaMemcpyAsync(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    ctx->Sync();
-    if (count > 0)
-      CudaCheck(lmc::LaunchBarrierBatch(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
-                                        ctx->s_fb_pairs.as<long long>(), count, kind, ctx->s_fb_ea.as<double>(),
-                                        ctx->s_fb_de.as<double>(), nullptr, nullptr, ctx->status.as<int>(),
-                                        ctx->stream),
-                "barrier kernel");
+    // the plain predictor on the compacted pairs, sized by the device count (no host round trip)
+    CudaCheck(lmc::LaunchBarrierBatchCounted(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica],
+                                             ctx->n[replica], ctx->s_fb_pairs.as<long long>(), m, d_count, kind,
+                                             ctx->s_fb_ea.as<double>(), ctx->s_fb_de.as<double>(),
+                                             ctx->status.as<int>(), ctx->stream),
+              "barrier kernel");
     CudaCheck(lmc::LaunchFallbackMerge(ctx->s_mean.as<float>(), m, ctx->s_fb_ea.as<double>(), ctx->s_fb_index.as<int>(),
                                        d_count, ea_dev, ctx->stream),
               "merge kernel");
+    int count = 0, net_status = 0;
+    CudaCheck(cudaMemcpyAsync(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(&net_status, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
+    ctx->Sync();
+    Require(net_status == 0, LMC_ERR_STOPPED, "surrogate inference: a tensor-core wait expired");
     RaiseStatus(ctx->ReadStatus(), "surrogate barriers");
     if (num_fallback) *num_fallback = count;
   });

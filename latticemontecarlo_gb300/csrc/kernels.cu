@@ -17,6 +17,7 @@
 // (coherent) loads, never the read-only path.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -309,10 +310,12 @@ __device__ __forceinline__ void GatherJump(const DevTables &t, const int8_t *spe
   }
 }
 
+// m_dev (nullable): the number of pairs lives on the device (m is then its upper bound).
 __global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ species, int n,
-                                     const long long *__restrict__ pairs, int m, int kind, double *ea, double *de,
-                                     double *d_or_e0, double *ks, int *status) {
+                                     const long long *__restrict__ pairs, int m, const int *m_dev, int kind,
+                                     double *ea, double *de, double *d_or_e0, double *ks, int *status) {
   extern __shared__ __align__(16) unsigned char smem[];
+  if (m_dev) m = min(m, *m_dev);
   const JumpSmem s = CarveJumpSmem(t, smem);
   StageJump(t, s);
   __syncthreads();
@@ -1701,8 +1704,23 @@ cudaError_t LaunchBarrierBatch(const DevTables &t, const int8_t *species, int n,
                                cudaStream_t stream) {
   if (m <= 0) return cudaSuccess;
   const size_t sm = JumpSmemBytes(t, kJumpWarps);
-  barrier_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, kind, ea, de,
-                                                                              d_or_e0, ks, status);
+  barrier_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, nullptr, kind,
+                                                                              ea, de, d_or_e0, ks, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchBarrierBatchCounted(const DevTables &t, const int8_t *species, int n, const long long *pairs,
+                                      int m_max, const int *m_dev, int kind, double *ea, double *de, int *status,
+                                      cudaStream_t stream) {
+  if (m_max <= 0) return cudaSuccess;
+  const size_t sm = JumpSmemBytes(t, kJumpWarps);
+  // a grid for a few percent of the pairs: the warps stride over whatever the device count holds
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = std::max(1, std::min(Blocks(m_max, kJumpWarps), sms * 2));
+  barrier_batch_kernel<<<blocks, kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m_max, m_dev, kind, ea, de,
+                                                                nullptr, nullptr, status);
   return cudaGetLastError();
 }
 

@@ -130,6 +130,10 @@ struct SurrogateGen {
   int *status;
 };
 cudaError_t LaunchSurrogateDataset(const DevTables &t, const SurrogateGen &g, cudaStream_t stream);
+// lmc_barrier_batch with the pair count on the device (at most m_max pairs).
+cudaError_t LaunchBarrierBatchCounted(const DevTables &t, const int8_t *species, int n, const long long *pairs,
+                                      int m_max, const int *m_dev, int kind, double *ea, double *de, int *status,
+                                      cudaStream_t stream);
 // Surrogate fallback: compact the pairs whose ensemble spread exceeds `threshold`
 // (flag per pair, optional), then merge the plain barriers of those pairs into ea.
 cudaError_t LaunchFallbackCompact(const long long *pairs, const float *mean, const float *spread, int m,

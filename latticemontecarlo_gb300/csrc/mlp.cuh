@@ -4,6 +4,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 namespace lmc {
 
 // GELU, tanh form (Hendrycks & Gimpel, 2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
@@ -68,4 +70,12 @@ cudaError_t MlpTcPredict(const MlpDev &d, const __nv_bfloat16 *x, long long n, f
 cudaError_t MlpEnsemble(const float *y, int batch, int members, float mean_label, float std_label, float *mean,
                         float *spread, cudaStream_t s);
 
+}  // namespace lmc
+
+// Host-side hooks of the surrogate object (surrogate.cpp) for other translation units.
+struct lmc_mlp;
+namespace lmc {
+bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean_dev, float *spread_dev,
+                     cudaStream_t stream);
+const int *MlpStatusDev(const lmc_mlp *mlp);
 }  // namespace lmc

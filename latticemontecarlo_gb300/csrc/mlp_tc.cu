@@ -299,12 +299,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           TmemLoad32(d1 + lane_base + col0, v);
 #pragma unroll
           for (int g8 = 0; g8 < 4; ++g8) {
+            // the 8 biases of this 16-byte row (one broadcast load per 4 columns)
+            const float4 ba = __ldg(reinterpret_cast<const float4 *>(b1 + col0 + g8 * 8));
+            const float4 bb = __ldg(reinterpret_cast<const float4 *>(b1 + col0 + g8 * 8 + 4));
+            const float bias[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
             uint32_t packed[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const int col = col0 + g8 * 8 + 2 * e;
-              const __nv_bfloat162 p = __floats2bfloat162_rn(MlpGelu(v[g8 * 8 + 2 * e] + __ldg(&b1[col])),
-                                                             MlpGelu(v[g8 * 8 + 2 * e + 1] + __ldg(&b1[col + 1])));
+              const __nv_bfloat162 p = __floats2bfloat162_rn(MlpGelu(v[g8 * 8 + 2 * e] + bias[2 * e]),
+                                                             MlpGelu(v[g8 * 8 + 2 * e + 1] + bias[2 * e + 1]));
               packed[e] = *reinterpret_cast<const uint32_t *>(&p);
             }
             *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(sh) + TileOffset(kTcRows, row, col0 + g8 * 8)) =
@@ -329,7 +332,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const int col0 = half * 128 + j0;
           TmemLoad32(d2 + lane_base + col0, v);
 #pragma unroll
-          for (int e = 0; e < 32; ++e) acc += MlpGelu(v[e] + __ldg(&b2[col0 + e])) * __ldg(&w3[col0 + e]);
+          for (int e = 0; e < 32; e += 4) {
+            const float4 bb = __ldg(reinterpret_cast<const float4 *>(b2 + col0 + e));
+            const float4 ww = __ldg(reinterpret_cast<const float4 *>(w3 + col0 + e));
+            acc += MlpGelu(v[e] + bb.x) * ww.x + MlpGelu(v[e + 1] + bb.y) * ww.y + MlpGelu(v[e + 2] + bb.z) * ww.z +
+                   MlpGelu(v[e + 3] + bb.w) * ww.w;
+          }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();

@@ -93,6 +93,23 @@ struct lmc_mlp {
   }
 };
 
+namespace lmc {
+// Inference queued on `stream` (the tcgen05 kernel; its status word is checked by the
+// caller through lmc_mlp_status after synchronising). Returns false when the
+// fused kernel does not support this network.
+bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean_dev, float *spread_dev,
+                           cudaStream_t stream) {
+  if (mlp->path == 2 || !lmc::MlpTcSupported(mlp->d)) return false;
+  CudaCheck(cudaMemsetAsync(mlp->status, 0, sizeof(int), stream), "memset");
+  CudaCheck(lmc::MlpTcPredict(mlp->d, reinterpret_cast<const __nv_bfloat16 *>(x_dev), n, mlp->label_mean,
+                              mlp->label_std, mean_dev, spread_dev, mlp->status, stream),
+            "tcgen05 inference");
+  return true;
+}
+const int *MlpStatusDev(const lmc_mlp *mlp) { return mlp->status; }
+
+}  // namespace lmc
+
 extern "C" {
 
 int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_t seed, lmc_mlp **out) {
