@@ -381,7 +381,8 @@ def run_surrogate(args, device):
         "timing": "wall clock over 20 device-synchronised calls (two streams per surrogate call)",
         "training": {"samples": args.surrogate_samples, "epochs": args.surrogate_epochs, "dataset_s": t_data,
                      "train_s": t_train, "tflops": train_tflops},
-        "roofline": {"bound": "tensor", "kernel": "gemm_nt_kernel (mma.sync bf16)", "achieved": mlp_tflops,
+        "roofline": {"bound": "tensor", "kernel": "mlp_tc_infer_kernel (tcgen05, TMEM accumulators)",
+                     "achieved": mlp_tflops,
                      "peak": peak, "unit": "TFLOP/s", "frac": mlp_tflops / peak},
     }
 
