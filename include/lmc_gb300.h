@@ -303,6 +303,23 @@ int lmc_last_run_ms(lmc_ctx *ctx, double *ms);
  * autotuner and the benchmark record). Any output may be NULL. */
 int lmc_kmc_launch_info(lmc_ctx *ctx, int *warps_per_replica, int *replicas_per_block, int *blocks_per_sm,
                         int64_t *shared_bytes);
+/* Runs `launches` x `steps_per_launch` steps on every replica as one CUDA graph
+ * (status clear, the persistent KMC launches, status copy to pinned host memory),
+ * recorded on the first call and replayed while the launch arguments are
+ * unchanged. Same results as `launches` calls of lmc_kmc_run(steps_per_launch)
+ * without a trace. Replaces the per-step driver loop of
+ * KineticMcFirstAbstract::Simulate (KineticMcAbstract.cpp:182-190). */
+int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches);
+/* Picks the KMC launch shape (warps per replica, replicas per block, sparse or
+ * dense evaluation) by timing every shape the kernel accepts for `probe_steps`
+ * steps on a copy of this context's state (the state is restored), and stores
+ * the choice in the context's options. With a non-empty cache_path the choice is
+ * read from / written to that JSON file, keyed by the GPU, its SM count, the
+ * replica count and the histogram of supercell sizes (plus the options that
+ * change the kernel's work). All shapes give identical results. No reference
+ * counterpart (GPU launch tuning). Any output may be NULL. */
+int lmc_kmc_autotune(lmc_ctx *ctx, uint64_t probe_steps, const char *cache_path, int *warps_per_replica,
+                     int *replicas_per_block, int *evaluation, int *from_cache);
 
 /* ------------------------------------------------------------------------- */
 /* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */

@@ -150,6 +150,9 @@ SIGNATURES = {
     "lmc_kmc_get_escaped": (C.c_int, [_P, C.POINTER(C.c_uint8)]),
     "lmc_last_run_ms": (C.c_int, [_P, _DP]),
     "lmc_kmc_launch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _I64P]),
+    "lmc_kmc_run_graph": (C.c_int, [_P, C.c_uint64, C.c_int]),
+    "lmc_kmc_autotune": (C.c_int, [_P, C.c_uint64, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "lmc_cmc_run": (C.c_int, [_P, C.c_int, C.c_double, C.c_uint64, C.POINTER(CmcOptions), _DP, _U64P, _U64P]),
     "lmc_request_stop": (C.c_int, [_P, C.c_int]),
 }

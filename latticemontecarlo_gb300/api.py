@@ -7,6 +7,7 @@ fallback: a missing library or device raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import json
 from pathlib import Path
 
@@ -205,6 +206,19 @@ class Context:
         check(N.lib.lmc_kmc_launch_info(self._h, C.byref(g), C.byref(rpb), C.byref(per_sm), ptr(smem, C.c_int64)))
         return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "blocks_per_sm": per_sm.value,
                 "shared_bytes": int(smem[0])}
+
+    def kmc_run_graph(self, steps_per_launch: int, launches: int = 1):
+        """`launches` persistent launches of `steps_per_launch` steps as one CUDA graph (recorded once)."""
+        check(N.lib.lmc_kmc_run_graph(self._h, steps_per_launch, launches))
+
+    def kmc_autotune(self, probe_steps: int = 100, cache: str | os.PathLike | None = None) -> dict:
+        """Times every KMC launch shape on a copy of the state and keeps the fastest (cached in `cache`)."""
+        g, rpb, ev, hit = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        path = None if cache is None else os.fsencode(cache)
+        check(N.lib.lmc_kmc_autotune(self._h, probe_steps, path, C.byref(g), C.byref(rpb), C.byref(ev),
+                                     C.byref(hit)))
+        return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "evaluation": ev.value,
+                "from_cache": bool(hit.value)}
 
     def kmc_escaped(self) -> np.ndarray:
         """Per replica True when the early stop ended its trajectory."""

@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <sstream>
+#include <fstream>
 #include <cmath>
 #include <cstring>
 #include <ios>
@@ -16,6 +19,7 @@
 
 #include "../../include/lmc_gb300.h"
 #include "geometry.hpp"
+#include "json.hpp"
 #include "kernels.cuh"
 #include "model.hpp"
 #include "abi_common.hpp"
@@ -99,6 +103,11 @@ struct lmc_ctx {
   int *h_stop{nullptr};
   int *d_stop{nullptr};
   double last_ms{0};
+  // graph-captured KMC launches (lmc_kmc_run_graph): the executable graph and the
+  // kernel argument bytes it was recorded with; pinned word the graph copies the status into
+  cudaGraphExec_t kmc_graph{nullptr};
+  std::vector<unsigned char> kmc_graph_key;
+  int *h_status{nullptr};
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
@@ -110,6 +119,8 @@ struct lmc_ctx {
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
     if (h_stop) cudaFreeHost(h_stop);
+    if (kmc_graph) cudaGraphExecDestroy(kmc_graph);
+    if (h_status) cudaFreeHost(h_status);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -591,6 +602,214 @@ lmc::KmcLaunch KmcShape(const lmc_ctx *ctx) {
   l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
   l.sp = ctx->sparse;
   return l;
+}
+
+
+// Device state of the KMC kernel (pointers into the context's buffers).
+lmc::KmcDevState KmcState(const lmc_ctx *ctx) {
+  lmc::KmcDevState s{};
+  s.vacancy = ctx->k_vac.as<long long>();
+  s.steps = ctx->k_steps.as<unsigned long long>();
+  s.time = ctx->k_time.as<double>();
+  s.energy = ctx->k_energy.as<double>();
+  s.temperature = ctx->k_temp.as<double>();
+  s.corr_cvac = ctx->k_cvac.as<double>();
+  s.corr_csol = ctx->k_csol.as<double>();
+  s.early_stop = ctx->kmc_opt.early_stop ? 1 : 0;
+  s.solvent = ctx->k_solvent.as<int8_t>();
+  s.escaped = ctx->k_escaped.as<uint8_t>();
+  s.rng = ctx->k_rng.as<uint32_t>();
+  s.lat_off = ctx->lat_off.as<long long>();
+  s.lat_n = ctx->lat_n.as<int>();
+  s.num_replicas = ctx->num_replicas;
+  s.rng_kind = ctx->kmc_opt.rng;
+  s.barrier_kind = ctx->kmc_opt.barrier_kind;
+  s.tt_time = ctx->tt_len ? ctx->k_tt_time.as<double>() : nullptr;
+  s.tt_temp = ctx->tt_len ? ctx->k_tt_temp.as<double>() : nullptr;
+  s.tt_len = ctx->tt_len;
+  return s;
+}
+// ---- KMC launch-shape autotuner -------------------------------------------
+// Sweeps the (warps per replica, replicas per block, evaluation) shapes the
+// kernel accepts on a short probe of the context's own replicas, keeps the
+// fastest, and caches it in a JSON file keyed by the GPU, its SM count and the
+// histogram of supercell sizes. Every shape gives bit-identical trajectories
+// (integer cluster sums, per-replica RNG streams), so the choice is pure speed;
+// the probe runs on a copy of the state, which is put back afterwards.
+
+struct KmcTuneEntry {
+  int g{1}, rpb{1}, eval{LMC_EVAL_SPARSE};
+  double ms{0};
+  uint64_t probe_steps{0};
+};
+
+std::string KmcTuneKey(const lmc_ctx *ctx) {
+  cudaDeviceProp prop{};
+  CudaCheck(cudaGetDeviceProperties(&prop, ctx->device), "cudaGetDeviceProperties");
+  std::map<int, int> hist;
+  for (int v : ctx->n) ++hist[v];
+  std::string name = prop.name;
+  for (char &ch : name)
+    if (ch == '"' || ch == '\\' || static_cast<unsigned char>(ch) < 32) ch = '_';
+  std::string k = "kmc1|" + name + "|sm" + std::to_string(prop.major) + std::to_string(prop.minor) + "|sms=" +
+                  std::to_string(prop.multiProcessorCount) + "|R=" + std::to_string(ctx->num_replicas) + "|n=";
+  bool first = true;
+  for (const auto &kv : hist) {
+    k += (first ? "" : ",") + std::to_string(kv.first) + ":" + std::to_string(kv.second);
+    first = false;
+  }
+  k += "|E=" + std::to_string(ctx->fm.num_species) + "|kind=" + std::to_string(ctx->kmc_opt.barrier_kind) +
+       "|rng=" + std::to_string(ctx->kmc_opt.rng) + "|stop=" + std::to_string(ctx->kmc_opt.early_stop ? 1 : 0) +
+       "|tt=" + std::to_string(ctx->tt_len > 0 ? 1 : 0) + "|corr=" + std::to_string(ctx->kmc_opt.rate_corrector ? 1 : 0);
+  return k;
+}
+
+std::map<std::string, KmcTuneEntry> ReadTuneCache(const char *path) {
+  std::map<std::string, KmcTuneEntry> out;
+  std::ifstream f(path);
+  if (!f) return out;  // no cache yet
+  std::stringstream ss;
+  ss << f.rdbuf();
+  try {
+    const lmc::JsonValue v = lmc::JsonValue::Parse(ss.str());
+    if (!v.IsObject()) return out;
+    for (const auto &kv : v.Object()) {
+      const lmc::JsonValue &e = kv.second;
+      if (!e.Has("warps_per_replica") || !e.Has("replicas_per_block") || !e.Has("evaluation")) continue;
+      KmcTuneEntry t;
+      t.g = static_cast<int>(e.At("warps_per_replica").Number());
+      t.rpb = static_cast<int>(e.At("replicas_per_block").Number());
+      t.eval = static_cast<int>(e.At("evaluation").Number());
+      if (e.Has("ms")) t.ms = e.At("ms").Number();
+      if (e.Has("probe_steps")) t.probe_steps = static_cast<uint64_t>(e.At("probe_steps").Number());
+      out[kv.first] = t;
+    }
+  } catch (const std::exception &) {
+    out.clear();  // an unreadable cache is ignored and rewritten
+  }
+  return out;
+}
+
+void WriteTuneCache(const char *path, const std::map<std::string, KmcTuneEntry> &cache) {
+  const std::string tmp = std::string(path) + ".tmp";
+  {
+    std::ofstream f(tmp);
+    Require(static_cast<bool>(f), LMC_ERR_IO, std::string("Cannot open ") + tmp);
+    f << "{\n";
+    size_t i = 0;
+    for (const auto &kv : cache) {
+      char ms[64];
+      std::snprintf(ms, sizeof(ms), "%.6g", kv.second.ms);
+      f << "  \"" << kv.first << "\": {\"warps_per_replica\": " << kv.second.g
+        << ", \"replicas_per_block\": " << kv.second.rpb << ", \"evaluation\": " << kv.second.eval
+        << ", \"ms\": " << ms << ", \"probe_steps\": " << kv.second.probe_steps << "}"
+        << (++i < cache.size() ? ",\n" : "\n");
+    }
+    f << "}\n";
+    Require(static_cast<bool>(f), LMC_ERR_IO, std::string("Cannot write ") + tmp);
+  }
+  Require(std::rename(tmp.c_str(), path) == 0, LMC_ERR_IO, std::string("Cannot write ") + path);
+}
+
+// The mutable KMC state of a context (lattices and per-replica records).
+struct KmcSnapshot {
+  std::vector<std::pair<const DevBuf *, DevBuf>> bufs;
+  size_t species_bytes{0};
+  void Save(lmc_ctx *ctx) {
+    const size_t R = ctx->num_replicas;
+    species_bytes = static_cast<size_t>(ctx->total_sites);
+    const std::pair<const DevBuf *, size_t> src[] = {
+        {&ctx->species, species_bytes}, {&ctx->k_vac, 8 * R},    {&ctx->k_steps, 8 * R},
+        {&ctx->k_time, 8 * R},          {&ctx->k_energy, 8 * R}, {&ctx->k_temp, 8 * R},
+        {&ctx->k_rng, sizeof(uint32_t) * lmc::kRngWords * R},    {&ctx->k_escaped, R}};
+    for (const auto &p : src) {
+      DevBuf copy;
+      copy.Alloc(p.second);
+      CudaCheck(cudaMemcpyAsync(copy.p, p.first->p, p.second, cudaMemcpyDeviceToDevice, ctx->stream), "D2D save");
+      bufs.emplace_back(p.first, copy);
+    }
+  }
+  void Restore(lmc_ctx *ctx) {
+    for (auto &p : bufs)
+      CudaCheck(cudaMemcpyAsync(p.first->p, p.second.p, p.second.bytes, cudaMemcpyDeviceToDevice, ctx->stream),
+                "D2D restore");
+  }
+  ~KmcSnapshot() {
+    for (auto &p : bufs) p.second.Free();
+  }
+};
+
+KmcTuneEntry SweepKmcShapes(lmc_ctx *ctx, uint64_t probe_steps) {
+  const lmc_kmc_options saved = ctx->kmc_opt;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const int R = ctx->num_replicas;
+  std::vector<KmcTuneEntry> cands;
+  for (int eval : {LMC_EVAL_SPARSE, LMC_EVAL_DENSE}) {
+    std::vector<int> rpbs = {1, 2, 4, 8, 12, 16, 20, 24, 28};
+    const int wave = (R + sms - 1) / sms;  // one block per SM
+    if (wave >= 1 && wave <= 28) rpbs.push_back(wave);
+    std::sort(rpbs.begin(), rpbs.end());
+    rpbs.erase(std::unique(rpbs.begin(), rpbs.end()), rpbs.end());
+    for (int rpb : rpbs) cands.push_back({1, rpb, eval});
+    for (int g : {2, 3, 4, 6, 12})
+      for (int rpb = 1; g * rpb <= 12; rpb *= 2) cands.push_back({g, rpb, eval});
+  }
+  KmcSnapshot snap;
+  snap.Save(ctx);
+  const lmc::KmcDevState s = KmcState(ctx);
+  KmcTuneEntry best{};
+  best.ms = std::numeric_limits<double>::infinity();
+  try {
+    for (KmcTuneEntry c : cands) {
+      ctx->kmc_opt.warps_per_replica = c.g;
+      ctx->kmc_opt.replicas_per_block = c.rpb;
+      ctx->kmc_opt.evaluation = c.eval;
+      lmc::KmcLaunch l{};
+      try {
+        l = KmcShape(ctx);
+      } catch (const LmcError &) {
+        continue;  // shape the kernel does not accept
+      }
+      int per_sm = 0;
+      size_t bytes = 0;
+      if (lmc::KmcOccupancy(ctx->t, l, &per_sm, &bytes) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      l.steps = probe_steps;
+      l.trace_replica = -1;
+      l.stop_flag = ctx->d_stop;
+      l.status = ctx->status.as<int>();
+      double best_c = std::numeric_limits<double>::infinity();
+      for (int rep = 0; rep < 3; ++rep) {  // first repetition warms caches and the instruction stream
+        ctx->ClearStatus();
+        CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+        CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");
+        CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+        const int st = ctx->ReadStatus();
+        snap.Restore(ctx);
+        RaiseStatus(st, "KMC autotune probe");
+        float ms = 0;
+        CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+        if (rep > 0) best_c = std::min(best_c, static_cast<double>(ms));
+      }
+      if (best_c < best.ms) {
+        best = c;
+        best.ms = best_c;
+      }
+    }
+  } catch (...) {
+    snap.Restore(ctx);
+    ctx->Sync();
+    ctx->kmc_opt = saved;
+    throw;
+  }
+  ctx->Sync();
+  ctx->kmc_opt = saved;
+  Require(std::isfinite(best.ms), LMC_ERR_UNSUPPORTED, "no KMC launch shape fits this device");
+  best.probe_steps = probe_steps;
+  return best;
 }
 
 }  // namespace
@@ -1333,26 +1552,7 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (steps == 0) return;
     static_assert(sizeof(lmc_kmc_step) == sizeof(lmc::KmcTraceRec), "trace record layout");
-    lmc::KmcDevState s{};
-    s.vacancy = ctx->k_vac.as<long long>();
-    s.steps = ctx->k_steps.as<unsigned long long>();
-    s.time = ctx->k_time.as<double>();
-    s.energy = ctx->k_energy.as<double>();
-    s.temperature = ctx->k_temp.as<double>();
-    s.corr_cvac = ctx->k_cvac.as<double>();
-    s.corr_csol = ctx->k_csol.as<double>();
-    s.early_stop = ctx->kmc_opt.early_stop ? 1 : 0;
-    s.solvent = ctx->k_solvent.as<int8_t>();
-    s.escaped = ctx->k_escaped.as<uint8_t>();
-    s.rng = ctx->k_rng.as<uint32_t>();
-    s.lat_off = ctx->lat_off.as<long long>();
-    s.lat_n = ctx->lat_n.as<int>();
-    s.num_replicas = ctx->num_replicas;
-    s.rng_kind = ctx->kmc_opt.rng;
-    s.barrier_kind = ctx->kmc_opt.barrier_kind;
-    s.tt_time = ctx->tt_len ? ctx->k_tt_time.as<double>() : nullptr;
-    s.tt_temp = ctx->tt_len ? ctx->k_tt_temp.as<double>() : nullptr;
-    s.tt_len = ctx->tt_len;
+    const lmc::KmcDevState s = KmcState(ctx);
     lmc::KmcLaunch l = KmcShape(ctx);
     l.steps = steps;
     l.trace_replica = -1;
@@ -1385,6 +1585,114 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
     ctx->last_ms = ms;
     RaiseStatus(st, "KMC run");
+  });
+}
+
+int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    Require(steps_per_launch > 0 && launches > 0, LMC_ERR_INVALID_ARGUMENT, "steps_per_launch and launches must be > 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const lmc::KmcDevState s = KmcState(ctx);
+    lmc::KmcLaunch l = KmcShape(ctx);
+    l.steps = steps_per_launch;
+    l.trace_replica = -1;
+    l.stop_flag = ctx->d_stop;
+    l.status = ctx->status.as<int>();
+    int8_t *species = ctx->species.as<int8_t>();
+    // every byte the recorded launches depend on: a change re-records the graph
+    std::vector<unsigned char> key(sizeof(ctx->t) + sizeof(s) + sizeof(l) + sizeof(species) + sizeof(launches));
+    {
+      unsigned char *k = key.data();
+      std::memcpy(k, &ctx->t, sizeof(ctx->t));
+      k += sizeof(ctx->t);
+      std::memcpy(k, &s, sizeof(s));
+      k += sizeof(s);
+      std::memcpy(k, &l, sizeof(l));
+      k += sizeof(l);
+      std::memcpy(k, &species, sizeof(species));
+      k += sizeof(species);
+      std::memcpy(k, &launches, sizeof(launches));
+    }
+    if (!ctx->h_status) CudaCheck(cudaMallocHost(&ctx->h_status, sizeof(int)), "cudaMallocHost");
+    if (!ctx->kmc_graph || key != ctx->kmc_graph_key) {
+      if (ctx->kmc_graph) CudaCheck(cudaGraphExecDestroy(ctx->kmc_graph), "cudaGraphExecDestroy");
+      ctx->kmc_graph = nullptr;
+      ctx->kmc_graph_key.clear();
+      int per_sm = 0;
+      size_t bytes = 0;
+      CudaCheck(lmc::KmcOccupancy(ctx->t, l, &per_sm, &bytes), "KMC occupancy");  // sets the smem attribute
+      Require(per_sm >= 1, LMC_ERR_INVALID_ARGUMENT, "KMC launch shape does not fit on an SM");
+      CudaCheck(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+      cudaError_t err = cudaMemsetAsync(l.status, 0, sizeof(int), ctx->stream);
+      for (int i = 0; i < launches && err == cudaSuccess; ++i)
+        err = lmc::LaunchKmc(ctx->t, species, s, l, ctx->stream, /*prepare=*/false);
+      if (err == cudaSuccess)
+        err = cudaMemcpyAsync(ctx->h_status, l.status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t end = cudaStreamEndCapture(ctx->stream, &graph);  // always ends the capture
+      if (err == cudaSuccess) err = end;
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&ctx->kmc_graph, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      CudaCheck(err, "KMC graph capture");
+      ctx->kmc_graph_key = std::move(key);
+    }
+    *ctx->h_status = 0;
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(cudaGraphLaunch(ctx->kmc_graph, ctx->stream), "cudaGraphLaunch");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    ctx->Sync();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(*ctx->h_status, "KMC graph run");
+  });
+}
+
+int lmc_kmc_autotune(lmc_ctx *ctx, uint64_t probe_steps, const char *cache_path, int *warps_per_replica,
+                     int *replicas_per_block, int *evaluation, int *from_cache) {
+  return Guard([&] {
+    Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
+    Require(probe_steps > 0, LMC_ERR_INVALID_ARGUMENT, "probe_steps must be > 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const std::string key = KmcTuneKey(ctx);
+    std::map<std::string, KmcTuneEntry> cache;
+    if (cache_path && *cache_path) cache = ReadTuneCache(cache_path);
+    KmcTuneEntry best{};
+    bool cached = false;
+    auto hit = cache.find(key);
+    if (hit != cache.end()) {
+      lmc_kmc_options o = ctx->kmc_opt;
+      o.warps_per_replica = hit->second.g;
+      o.replicas_per_block = hit->second.rpb;
+      o.evaluation = hit->second.eval;
+      const lmc_kmc_options saved = ctx->kmc_opt;
+      ctx->kmc_opt = o;
+      try {
+        int per_sm = 0;
+        size_t bytes = 0;
+        CudaCheck(lmc::KmcOccupancy(ctx->t, KmcShape(ctx), &per_sm, &bytes), "KMC occupancy");
+        cached = per_sm >= 1;
+      } catch (const LmcError &) {
+        cached = false;
+      }
+      ctx->kmc_opt = saved;
+      if (cached) best = hit->second;
+    }
+    if (!cached) {
+      best = SweepKmcShapes(ctx, probe_steps);
+      if (cache_path && *cache_path) {
+        cache[key] = best;
+        WriteTuneCache(cache_path, cache);
+      }
+    }
+    ctx->kmc_opt.warps_per_replica = best.g;
+    ctx->kmc_opt.replicas_per_block = best.rpb;
+    ctx->kmc_opt.evaluation = best.eval;
+    if (warps_per_replica) *warps_per_replica = best.g;
+    if (replicas_per_block) *replicas_per_block = best.rpb;
+    if (evaluation) *evaluation = best.eval;
+    if (from_cache) *from_cache = cached ? 1 : 0;
   });
 }
 

@@ -1867,15 +1867,17 @@ cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per
 }
 
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, bool prepare) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
   if (threads > kShapeThreads[2] || (threads > kShapeThreads[1] && l.warps_per_replica != 1))
     return cudaErrorInvalidConfiguration;
   const int blocks = (s.num_replicas + l.replicas_per_block - 1) / l.replicas_per_block;
   const size_t sm = KmcSharedBytes(t, l);
   const KmcKernelFn kern = KmcKernelFor(l);
-  cudaError_t err = PrepareKmc(kern, sm);
-  if (err != cudaSuccess) return err;
+  if (prepare) {
+    cudaError_t err = PrepareKmc(kern, sm);
+    if (err != cudaSuccess) return err;
+  }
   kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
   return cudaGetLastError();
 }

@@ -112,8 +112,10 @@ cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, cons
                           int *status, cudaStream_t stream);
 cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
                          unsigned long long *counts, double *energy, cudaStream_t stream);
+// prepare = false skips the shared-memory attribute call (already made by
+// KmcOccupancy), so the launch can be recorded into a CUDA graph.
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
-                      cudaStream_t stream);
+                      cudaStream_t stream, bool prepare = true);
 size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
 
 // Surrogate training data (see surrogate_dataset_kernel).
