@@ -276,7 +276,7 @@ typedef struct lmc_kmc_step {
   int64_t vacancy;     /* vacancy site before the step */
   int64_t target;      /* selected neighbour (lattice id) */
   int32_t selected;    /* index in the id-sorted 1NN list */
-  int32_t pad;
+  int32_t slot;        /* vacancy slot that moved (multi-vacancy runs; 0 otherwise) */
   double ea, de;       /* barrier and energy change of the selected event */
   double total_rate;   /* sum of exp(-Ea beta) over the 12 events (no prefactor) */
   double time;         /* simulated time after the step */
@@ -320,6 +320,25 @@ int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches);
  * counterpart (GPU launch tuning). Any output may be NULL. */
 int lmc_kmc_autotune(lmc_ctx *ctx, uint64_t probe_steps, const char *cache_path, int *warps_per_replica,
                      int *replicas_per_block, int *evaluation, int *from_cache);
+
+/* Multi-vacancy KMC (no reference counterpart: KineticMcFirstOmp tracks the
+ * first vacancy only, Config.cpp:298-310, and its encodings throw when a second
+ * vacancy enters a jump environment, EnergyUtility.cpp:784). Every X site of a
+ * lattice is a tracked vacancy ("slot", ascending site id at init, 1 to 256 per
+ * lattice); each step chooses one event among all slots x 12 jumps by residence
+ * time (rates and clock as KineticMcFirstOmp, Philox stream per lattice) and
+ * moves that vacancy. A second vacancy inside a jump's neighbourhood
+ * contributes nothing to its encodings (clusters with two vacancies have no
+ * coefficients, a vacancy has no one-hot slot); a jump onto a vacancy has rate
+ * 0. One block per lattice; replaces KineticMcAbstract.cpp:140-190 for this case. */
+int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, int barrier_kind, int evaluation);
+/* Runs `steps` steps on every lattice; trace (NULL or `steps` records) receives
+ * lattice trace_replica's events, `slot` naming the vacancy that moved. */
+int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace);
+/* First slot of every lattice, R + 1 entries (the last is the slot count). */
+int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
+/* Vacancy site of every slot and per-lattice steps, time, energy (any may be NULL). */
+int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy);
 
 /* ------------------------------------------------------------------------- */
 /* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */

@@ -71,7 +71,7 @@ class KmcOptions(C.Structure):
 
 class KmcStep(C.Structure):
     _fields_ = [
-        ("vacancy", C.c_int64), ("target", C.c_int64), ("selected", C.c_int32), ("pad", C.c_int32),
+        ("vacancy", C.c_int64), ("target", C.c_int64), ("selected", C.c_int32), ("slot", C.c_int32),
         ("ea", C.c_double), ("de", C.c_double), ("total_rate", C.c_double), ("time", C.c_double),
         ("energy", C.c_double),
     ]
@@ -151,6 +151,10 @@ SIGNATURES = {
     "lmc_last_run_ms": (C.c_int, [_P, _DP]),
     "lmc_kmc_launch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _I64P]),
     "lmc_kmc_run_graph": (C.c_int, [_P, C.c_uint64, C.c_int]),
+    "lmc_kmc_multi_init": (C.c_int, [_P, _DP, C.c_uint64, C.c_int, C.c_int]),
+    "lmc_kmc_multi_run": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(KmcStep)]),
+    "lmc_kmc_multi_slots": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "lmc_kmc_multi_get_state": (C.c_int, [_P, _I64P, _U64P, _DP, _DP]),
     "lmc_kmc_autotune": (C.c_int, [_P, C.c_uint64, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "lmc_cmc_run": (C.c_int, [_P, C.c_int, C.c_double, C.c_uint64, C.POINTER(CmcOptions), _DP, _U64P, _U64P]),

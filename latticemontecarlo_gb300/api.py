@@ -98,7 +98,7 @@ class Model:
 class KmcTrace:
     """Per-step records of one replica (numpy structured view of lmc_kmc_step)."""
 
-    DTYPE = np.dtype([("vacancy", np.int64), ("target", np.int64), ("selected", np.int32), ("pad", np.int32),
+    DTYPE = np.dtype([("vacancy", np.int64), ("target", np.int64), ("selected", np.int32), ("slot", np.int32),
                       ("ea", np.float64), ("de", np.float64), ("total_rate", np.float64), ("time", np.float64),
                       ("energy", np.float64)])
 
@@ -219,6 +219,32 @@ class Context:
                                      C.byref(hit)))
         return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "evaluation": ev.value,
                 "from_cache": bool(hit.value)}
+
+    # multi-vacancy kinetic MC ---------------------------------------------
+    def kmc_multi_init(self, temperatures, seed: int = 0, kind: int = N.LMC_BARRIER_QUARTIC,
+                       evaluation: int = N.LMC_EVAL_SPARSE):
+        """Tracks every vacancy of every lattice (slots in ascending site order)."""
+        temps = np.ascontiguousarray(np.broadcast_to(np.asarray(temperatures, np.float64), (self.ns.size,)))
+        check(N.lib.lmc_kmc_multi_init(self._h, ptr(temps, C.c_double), seed, kind, evaluation))
+        off = np.zeros(self.ns.size + 1, np.int32)
+        check(N.lib.lmc_kmc_multi_slots(self._h, ptr(off, C.c_int32)))
+        self._multi_off = off
+
+    def kmc_multi_run(self, steps: int, trace_replica: int | None = None):
+        trace = np.zeros(steps, KmcTrace.DTYPE) if trace_replica is not None else None
+        check(N.lib.lmc_kmc_multi_run(self._h, steps, -1 if trace_replica is None else trace_replica,
+                                      trace.ctypes.data_as(C.POINTER(N.KmcStep)) if trace is not None else None))
+        return trace
+
+    def kmc_multi_state(self):
+        """(slot offsets [R + 1], vacancy site per slot, steps, time, energy per lattice)."""
+        off = self._multi_off
+        r = self.ns.size
+        vac = np.zeros(int(off[-1]), np.int64)
+        steps, time, energy = np.zeros(r, np.uint64), np.zeros(r), np.zeros(r)
+        check(N.lib.lmc_kmc_multi_get_state(self._h, ptr(vac, C.c_int64), ptr(steps, C.c_uint64),
+                                            ptr(time, C.c_double), ptr(energy, C.c_double)))
+        return off.copy(), vac, steps, time, energy
 
     def kmc_escaped(self) -> np.ndarray:
         """Per replica True when the early stop ended its trajectory."""

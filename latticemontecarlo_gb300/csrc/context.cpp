@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <sstream>
 #include <fstream>
@@ -108,6 +109,12 @@ struct lmc_ctx {
   cudaGraphExec_t kmc_graph{nullptr};
   std::vector<unsigned char> kmc_graph_key;
   int *h_status{nullptr};
+  // multi-vacancy KMC (every vacancy of a lattice tracked; slots per lattice)
+  bool multi_ready{false};
+  int multi_kind{0}, multi_eval{0};
+  std::vector<int> m_off_host;
+  DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_ea, m_de, m_tgt, m_trace;
+  std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
@@ -115,6 +122,8 @@ struct lmc_ctx {
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
                       &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &s_feat, &s_mean, &s_spread,
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+      b->Free();
+    for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_ea, &m_de, &m_tgt, &m_trace})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -254,6 +263,14 @@ void BuildTables(lmc_ctx *c) {
   std::vector<int8_t> local_off;
   for (const auto &s : local)
     for (int v : {s.x, s.y, s.z, 0}) local_off.push_back(Pack4(v));
+  // displacement bitmap of the neighbourhood (multi-vacancy KMC: which slots a changed site affects)
+  c->local_bits.fill(0);
+  for (const auto &s : local) {
+    Require(std::abs(s.x) <= 4 && std::abs(s.y) <= 4 && std::abs(s.z) <= 4, LMC_ERR_UNSUPPORTED,
+            "KMC neighbourhood wider than 4 half-units");
+    const int b = ((s.x + 4) * lmc::kLocalSpan + (s.y + 4)) * lmc::kLocalSpan + (s.z + 4);
+    c->local_bits[b >> 5] |= 1u << (b & 31);
+  }
   std::vector<uint8_t> l_st, l_mmm, l_mm2f, l_mm2b;
   for (int d = 0; d < lmc::kDirections; ++d) {
     const int db = lmc::DirectionIndex(lmc::I3{0, 0, 0} - pt.dir[d]);
@@ -1702,6 +1719,151 @@ int lmc_kmc_get_escaped(lmc_ctx *ctx, uint8_t *escaped) {
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     CudaCheck(cudaMemcpyAsync(escaped, ctx->k_escaped.p, ctx->num_replicas, cudaMemcpyDeviceToHost, ctx->stream),
               "D2H");
+    ctx->Sync();
+  });
+}
+
+int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, int barrier_kind, int evaluation) {
+  return Guard([&] {
+    Require(ctx && temperature && ctx->num_replicas > 0, LMC_ERR_INVALID_ARGUMENT, "bad argument");
+    Require(barrier_kind == LMC_BARRIER_QUARTIC || barrier_kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT,
+            "unknown barrier kind");
+    Require(evaluation == LMC_EVAL_SPARSE || evaluation == LMC_EVAL_DENSE, LMC_ERR_INVALID_ARGUMENT,
+            "unknown evaluation");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int R = ctx->num_replicas;
+    for (int r = 0; r < R; ++r)
+      Require(temperature[r] > 0 && std::isfinite(temperature[r]), LMC_ERR_INVALID_ARGUMENT, "temperature must be > 0");
+    ctx->multi_ready = false;
+    // vacancy slots of every lattice (ascending site id) and the species histogram
+    std::vector<int8_t> host(static_cast<size_t>(ctx->total_sites));
+    ctx->Sync();
+    CudaCheck(cudaMemcpy(host.data(), ctx->species.p, host.size(), cudaMemcpyDeviceToHost), "D2H species");
+    const int e = ctx->fm.num_species, x = ctx->fm.x_code;
+    std::vector<long long> pos;
+    std::vector<int> off(R + 1, 0);
+    std::vector<unsigned long long> tot(e, 0);
+    for (int r = 0; r < R; ++r) {
+      const long long nsites = 4LL * ctx->n[r] * ctx->n[r] * ctx->n[r];
+      const int8_t *sp = host.data() + ctx->offsets[r];
+      for (long long i = 0; i < nsites; ++i) {
+        const int c = sp[i];
+        Require(c >= 0 && c < e, LMC_ERR_INVALID_ARGUMENT, "species code out of range");
+        ++tot[c];
+        if (c == x) pos.push_back(i);
+      }
+      off[r + 1] = static_cast<int>(pos.size());
+      const int nv = off[r + 1] - off[r];
+      Require(nv >= 1 && nv <= lmc::kMaxMultiVac, LMC_ERR_UNSUPPORTED, "every lattice needs 1 to 256 vacancies");
+    }
+    int base = -1;
+    for (int c = 0; c < e; ++c)
+      if (c != x && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || tot[c] > tot[base])) base = c;
+    Require(base >= 0, LMC_ERR_INVALID_ARGUMENT, "no element of the barrier set in the lattices");
+    BuildSparse(ctx, base);
+    const size_t slots = pos.size();
+    ctx->m_pos.Ensure(8 * slots);
+    ctx->m_off.Ensure(sizeof(int) * (R + 1));
+    ctx->m_steps.Ensure(8 * R);
+    ctx->m_time.Ensure(8 * R);
+    ctx->m_energy.Ensure(8 * R);
+    ctx->m_temp.Ensure(8 * R);
+    ctx->m_key.Ensure(8 * R);
+    ctx->m_ea.Ensure(8 * 12 * slots);
+    ctx->m_de.Ensure(8 * 12 * slots);
+    ctx->m_tgt.Ensure(8 * 12 * slots);
+    std::vector<uint32_t> key(2 * R);
+    for (int r = 0; r < R; ++r) {
+      key[2 * r] = static_cast<uint32_t>(seed);
+      key[2 * r + 1] = static_cast<uint32_t>(seed >> 32);
+    }
+    std::vector<double> zeros(R, 0.0), temp(temperature, temperature + R);
+    std::vector<unsigned long long> zu(R, 0);
+    auto h2d = [&](DevBuf &d, const void *src, size_t bytes) {
+      CudaCheck(cudaMemcpyAsync(d.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    };
+    h2d(ctx->m_pos, pos.data(), 8 * slots);
+    h2d(ctx->m_off, off.data(), sizeof(int) * (R + 1));
+    h2d(ctx->m_steps, zu.data(), 8 * R);
+    h2d(ctx->m_time, zeros.data(), 8 * R);
+    h2d(ctx->m_energy, zeros.data(), 8 * R);
+    h2d(ctx->m_temp, temp.data(), 8 * R);
+    h2d(ctx->m_key, key.data(), 8 * R);
+    ctx->Sync();
+    ctx->m_off_host = off;
+    ctx->multi_kind = barrier_kind;
+    ctx->multi_eval = evaluation;
+    ctx->multi_ready = true;
+  });
+}
+
+int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace) {
+  return Guard([&] {
+    Require(ctx && ctx->multi_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_multi_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (steps == 0) return;
+    lmc::KmcMultiArgs a{};
+    a.vac_pos = ctx->m_pos.as<long long>();
+    a.vac_off = ctx->m_off.as<int>();
+    a.steps = ctx->m_steps.as<unsigned long long>();
+    a.time = ctx->m_time.as<double>();
+    a.energy = ctx->m_energy.as<double>();
+    a.temperature = ctx->m_temp.as<double>();
+    a.key = ctx->m_key.as<uint32_t>();
+    a.lat_off = ctx->lat_off.as<long long>();
+    a.lat_n = ctx->lat_n.as<int>();
+    a.num_replicas = ctx->num_replicas;
+    a.barrier_kind = ctx->multi_kind;
+    a.nsteps = steps;
+    a.ev_ea = ctx->m_ea.as<double>();
+    a.ev_de = ctx->m_de.as<double>();
+    a.ev_tgt = ctx->m_tgt.as<long long>();
+    a.trace_replica = -1;
+    if (trace) {
+      ctx->CheckReplica(trace_replica);
+      a.trace_replica = trace_replica;
+      ctx->m_trace.Ensure(sizeof(lmc::KmcTraceRec) * steps);
+      CudaCheck(cudaMemsetAsync(ctx->m_trace.p, 0, sizeof(lmc::KmcTraceRec) * steps, ctx->stream), "memset");
+      a.trace = ctx->m_trace.as<lmc::KmcTraceRec>();
+    }
+    a.stop_flag = ctx->d_stop;
+    a.status = ctx->status.as<int>();
+    a.sp = ctx->sparse;
+    std::copy(ctx->local_bits.begin(), ctx->local_bits.end(), a.local_bits);
+    ctx->ClearStatus();
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchKmcMulti(ctx->t, ctx->species.as<int8_t>(), a, ctx->multi_eval == LMC_EVAL_SPARSE,
+                                  ctx->stream),
+              "multi-vacancy KMC kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    if (trace)
+      CudaCheck(cudaMemcpyAsync(trace, a.trace, sizeof(lmc::KmcTraceRec) * steps, cudaMemcpyDeviceToHost, ctx->stream),
+                "D2H trace");
+    const int st = ctx->ReadStatus();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(st, "multi-vacancy KMC run");
+  });
+}
+
+int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets) {
+  return Guard([&] {
+    Require(ctx && ctx->multi_ready && slot_offsets, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_multi_init has not been called");
+    std::copy(ctx->m_off_host.begin(), ctx->m_off_host.end(), slot_offsets);
+  });
+}
+
+int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy) {
+  return Guard([&] {
+    Require(ctx && ctx->multi_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_multi_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t R = ctx->num_replicas, slots = ctx->m_off_host.back();
+    if (vacancies)
+      CudaCheck(cudaMemcpyAsync(vacancies, ctx->m_pos.p, 8 * slots, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (steps) CudaCheck(cudaMemcpyAsync(steps, ctx->m_steps.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (time) CudaCheck(cudaMemcpyAsync(time, ctx->m_time.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (energy) CudaCheck(cudaMemcpyAsync(energy, ctx->m_energy.p, 8 * R, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     ctx->Sync();
   });
 }

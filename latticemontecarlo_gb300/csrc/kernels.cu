@@ -577,20 +577,29 @@ __global__ void __launch_bounds__(kCensusThreads) census_kernel(DevTables t, con
       for (int q = 0; q < t.n_census_tri; ++q) base_count[s_tri[q] & 7] += 1;
       continue;
     }
+    // clusters whose multiset has no index (two or more vacancies) count nothing
     atomicAdd(&hist[s_idx[(0 * e + c0) * e * e]], 1u);
     for (int k = 0; k < kSiteSites; ++k) {
       const int l = s_label[k];
       if (l == 0) continue;
       const int c1 = sp[k];
-      if (c0 == base_code && c1 == base_code) base_count[l] += 1;
-      else atomicAdd(&hist[s_idx[((l * e + c0) * e + c1) * e]], 1u);
+      if (c0 == base_code && c1 == base_code) {
+        base_count[l] += 1;
+      } else {
+        const int idx = s_idx[((l * e + c0) * e + c1) * e];
+        if (idx >= 0) atomicAdd(&hist[idx], 1u);
+      }
     }
     for (int q = 0; q < t.n_census_tri; ++q) {
       const uint32_t w = s_tri[q];
       const int l = w & 7;
       const int c1 = sp[(w >> 3) & 63], c2 = sp[(w >> 9) & 63];
-      if (c0 == base_code && c1 == base_code && c2 == base_code) base_count[l] += 1;
-      else atomicAdd(&hist[s_idx[((l * e + c0) * e + c1) * e + c2]], 1u);
+      if (c0 == base_code && c1 == base_code && c2 == base_code) {
+        base_count[l] += 1;
+      } else {
+        const int idx = s_idx[((l * e + c0) * e + c1) * e + c2];
+        if (idx >= 0) atomicAdd(&hist[idx], 1u);
+      }
     }
   }
   // merge the per-label dominant-species counts
@@ -984,6 +993,159 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
   return {acc_a, acc_b, bad};
 }
 
+// Shared-memory layout of the KMC kernels: jump cluster tables, small tables,
+// local-index tables of the 12 jumps, the 135-site neighbourhood offsets, the
+// ExpFast table, one KmcShared per replica, per-warp sorted arrays, then the
+// sparse-evaluation tables (KmcSharedBytes gives the size).
+struct KmcSmem {
+  uint32_t *de, *mmm, *mm2;
+  SmallTables *small;
+  uint8_t *lst, *lmmm, *lmm2f, *lmm2b;  // [12][60], [12][58] x 3
+  int8_t *loff;                         // [135][4]
+  double *exp;                          // [kExpTableSize]
+  KmcShared *rep;                       // [replicas per block]
+  int8_t *arr;                          // [warps][kArr]
+  uint8_t *pos;                         // [4][12][136]
+  uint32_t *pxenv;                      // [2][kTriEnv + 1]
+  uint32_t *inter;                      // [135][kInterWords]
+  uint16_t *pxst;                       // [kTriState + 1]
+  unsigned char *end;
+};
+__device__ __forceinline__ KmcSmem CarveKmcSmem(const DevTables &t, unsigned char *smem, int rpb, int g_per) {
+  KmcSmem m;
+  m.de = reinterpret_cast<uint32_t *>(smem);
+  m.mmm = m.de + t.n_de_cl;
+  m.mm2 = m.mmm + t.n_mmm_cl;
+  m.small = reinterpret_cast<SmallTables *>(m.mm2 + t.n_mm2_cl);
+  m.lst = reinterpret_cast<uint8_t *>(m.small + 1);
+  m.lmmm = m.lst + 12 * kStateSites;
+  m.lmm2f = m.lmmm + 12 * kEnvSites;
+  m.lmm2b = m.lmm2f + 12 * kEnvSites;
+  m.loff = reinterpret_cast<int8_t *>(m.lmm2b + 12 * kEnvSites);
+  size_t off = reinterpret_cast<size_t>(m.loff + kLocalSites * 4);
+  off = (off + 15) & ~size_t(15);
+  m.exp = reinterpret_cast<double *>(off);
+  m.rep = reinterpret_cast<KmcShared *>(m.exp + kExpTableSize);
+  m.arr = reinterpret_cast<int8_t *>(m.rep + rpb);
+  m.pos = reinterpret_cast<uint8_t *>(m.arr + rpb * g_per * kArr);
+  m.pxenv = reinterpret_cast<uint32_t *>(m.pos + 4 * 12 * 136);
+  m.inter = m.pxenv + 2 * (kTriEnv + 1);
+  m.pxst = reinterpret_cast<uint16_t *>(m.inter + kLocalSites * kInterWords);
+  m.end = reinterpret_cast<unsigned char *>(m.pxst + kTriState + 1);
+  return m;
+}
+__device__ __forceinline__ void StageKmcSmem(const DevTables &t, const KmcSparse &sp, const KmcSmem &m, bool sparse) {
+  if (sparse) {
+    StageArray(sp.pos, m.pos, 4 * 12 * 136);
+    StageArray(sp.px_st, m.pxst, kTriState + 1);
+    StageArray(sp.px_env, m.pxenv, 2 * (kTriEnv + 1));
+    StageArray(sp.inter, m.inter, kLocalSites * kInterWords);
+  }
+  StageArray(t.de_cl, m.de, t.n_de_cl);
+  StageArray(t.mmm_cl, m.mmm, t.n_mmm_cl);
+  StageArray(t.mm2_cl, m.mm2, t.n_mm2_cl);
+  StageSmall(t, m.small);
+  StageArray(t.local_st, m.lst, 12 * kStateSites);
+  StageArray(t.local_mmm, m.lmmm, 12 * kEnvSites);
+  StageArray(t.local_mm2f, m.lmm2f, 12 * kEnvSites);
+  StageArray(t.local_mm2b, m.lmm2b, 12 * kEnvSites);
+  StageArray(t.local_off, m.loff, kLocalSites * 4);
+  StageArray(t.exp_tab, m.exp, kExpTableSize);
+}
+
+// Sparse evaluation, listing step (one warp): the non-base sites of the
+// neighbourhood in rs.local (except the centre) with their species, padded to
+// a multiple of 4, then the pairs of them that share a cluster in some jump
+// (interaction table rows), padded to a multiple of 4. rs.nbk / rs.npairs above
+// kMaxSparseSites / kMaxSparsePairs mean the lists are incomplete.
+__device__ __forceinline__ void SparseList(KmcShared &rs, const uint32_t *s_inter, const KmcSparse &sp, int lane) {
+  int k_sites = 0;
+#pragma unroll
+  for (int w = 0; w < 5; ++w) {
+    const int k = w * 32 + lane;
+    const int code = k < kLocalSites ? rs.local[k] : sp.base_code;
+    const bool nb = code != sp.base_code && k != sp.center;
+    const unsigned mk = __ballot_sync(0xffffffffu, nb);
+    const int idx = k_sites + __popc(mk & ((1u << lane) - 1u));
+    if (nb && idx < kMaxSparseSites) {
+      rs.nb_l[idx] = static_cast<uint8_t>(k);
+      rs.nb_code[idx] = static_cast<int8_t>(code);
+    }
+    k_sites += __popc(mk);
+  }
+  // padding up to the next multiple of 4 (and the fixed entry 32)
+  if (lane >= k_sites && lane < ((k_sites + 3) & ~3)) {
+    rs.nb_l[lane] = static_cast<uint8_t>(kLocalSites);
+    rs.nb_code[lane] = static_cast<int8_t>(sp.base_code);
+  }
+  if (lane == 0) {
+    rs.nb_l[kMaxSparseSites] = static_cast<uint8_t>(kLocalSites);
+    rs.nb_code[kMaxSparseSites] = static_cast<int8_t>(sp.base_code);
+  }
+  __syncwarp();
+  // interacting pairs (k2 < k): lane k tests its row of the interaction table
+  unsigned pm = 0;
+  if (k_sites <= kMaxSparseSites && lane < k_sites) {
+    const uint32_t *row = s_inter + rs.nb_l[lane] * kInterWords;
+    for (int k2 = 0; k2 < lane; ++k2) {
+      const int l2 = rs.nb_l[k2];
+      pm |= ((row[l2 >> 5] >> (l2 & 31)) & 1u) << k2;
+    }
+  }
+  const int cnt = __popc(pm);
+  int pre = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, pre, o);
+    if (lane >= o) pre += v;
+  }
+  const int n_pairs = __shfl_sync(0xffffffffu, pre, 31);
+  pre -= cnt;
+  if (n_pairs <= kMaxSparsePairs) {
+    while (pm) {
+      const int k2 = __ffs(pm) - 1;
+      pm &= pm - 1;
+      rs.pairs[pre++] = static_cast<uint16_t>(lane | (k2 << 8));
+    }
+    if (lane < ((n_pairs + 3) & ~3) - n_pairs)
+      rs.pairs[n_pairs + lane] = static_cast<uint16_t>(kMaxSparseSites | (kMaxSparseSites << 8));
+  }
+  if (lane == 0) {
+    rs.nbk = k_sites;
+    rs.npairs = n_pairs;
+  }
+}
+
+// Sparse evaluation, one lane's item (0..23; larger items idle): jump c =
+// item % 12, half item / 12 (0: energy change and the D / e0 sum, 1: the Ks
+// sums). Writes rs.acc / rs.slot of its jump; returns the warp's status bits.
+__device__ __forceinline__ unsigned SparseItem(const DevTables &t, const KmcSparse &sp, const uint8_t *s_lst,
+                                               const uint8_t *s_pos, const uint16_t *s_pxst, const uint32_t *s_pxenv,
+                                               const SmallTables *s_small, KmcShared &rs, int barrier_kind, int item) {
+  const int c = item % 12, part = item / 12;
+  LaneAcc la{0, 0, 0u};
+  if (item < 24) {
+    const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
+    const int slot = s_small->slot[mig];
+    const bool quartic = barrier_kind == 0;
+    const bool ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+    if (ok && (part == 0 || quartic))
+      la = EvalJumpPairs(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code, c, part, mig, slot,
+                         quartic);
+    if (ok) {
+      const long long *bf = sp.base_form + slot * 3;
+      if (part == 0) {
+        rs.acc[c][0] = sp.base_de[mig] + la.a;
+        rs.acc[c][1] = (quartic ? bf[0] : bf[2]) + la.b;
+      } else {
+        rs.acc[c][2] = bf[1] + la.a + la.b;
+      }
+    }
+    if (part == 0) rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+  }
+  return __reduce_or_sync(0xffffffffu, la.bad);
+}
+
 // Dense evaluation of the replica's 12 jumps (warp g takes jumps g, g + G, ...):
 // gathers each jump's sorted state / MMM / MM2 lists into the warp's arrays and
 // sums the cluster tables. Returns the status bits.
@@ -1064,45 +1226,18 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   extern __shared__ __align__(16) unsigned char smem[];
   const int g_per = l.warps_per_replica;
   const int rpb = l.replicas_per_block;
-  // carve: jump tables, small tables, local-index tables, per-replica state, per-warp arrays
-  uint32_t *s_de = reinterpret_cast<uint32_t *>(smem);
-  uint32_t *s_mmm = s_de + t.n_de_cl;
-  uint32_t *s_mm2 = s_mmm + t.n_mmm_cl;
-  SmallTables *s_small = reinterpret_cast<SmallTables *>(s_mm2 + t.n_mm2_cl);
-  uint8_t *s_lst = reinterpret_cast<uint8_t *>(s_small + 1);   // [12][60]
-  uint8_t *s_lmmm = s_lst + 12 * kStateSites;                    // [12][58]
-  uint8_t *s_lmm2f = s_lmmm + 12 * kEnvSites;
-  uint8_t *s_lmm2b = s_lmm2f + 12 * kEnvSites;
-  int8_t *s_loff = reinterpret_cast<int8_t *>(s_lmm2b + 12 * kEnvSites);  // [135][4]
-  size_t off = reinterpret_cast<size_t>(s_loff + kLocalSites * 4);
-  off = (off + 15) & ~size_t(15);
-  double *s_exp = reinterpret_cast<double *>(off);  // [256] ExpFast table
-  KmcShared *s_rep = reinterpret_cast<KmcShared *>(s_exp + kExpTableSize);
-  int8_t *s_arr = reinterpret_cast<int8_t *>(s_rep + rpb);
-  // sparse tables follow the per-warp arrays
-  uint8_t *s_pos = reinterpret_cast<uint8_t *>(s_arr + rpb * g_per * kArr);        // [4][12][136]
-  uint32_t *s_pxenv = reinterpret_cast<uint32_t *>(s_pos + 4 * 12 * 136);  // [2][kTriEnv + 1]
-  uint32_t *s_inter = s_pxenv + 2 * (kTriEnv + 1);                           // [135][5]
-  uint16_t *s_pxst = reinterpret_cast<uint16_t *>(s_inter + kLocalSites * kInterWords);  // [kTriState + 1]
-  if (kSparse) {
-    StageArray(l.sp.pos, s_pos, 4 * 12 * 136);
-    StageArray(l.sp.px_st, s_pxst, kTriState + 1);
-    StageArray(l.sp.px_env, s_pxenv, 2 * (kTriEnv + 1));
-    StageArray(l.sp.inter, s_inter, kLocalSites * kInterWords);
-  }
-
-  StageArray(t.de_cl, s_de, t.n_de_cl);
-  StageArray(t.mmm_cl, s_mmm, t.n_mmm_cl);
-  StageArray(t.mm2_cl, s_mm2, t.n_mm2_cl);
-  StageSmall(t, s_small);
-  StageArray(t.local_st, s_lst, 12 * kStateSites);
-  StageArray(t.local_mmm, s_lmmm, 12 * kEnvSites);
-  StageArray(t.local_mm2f, s_lmm2f, 12 * kEnvSites);
-  StageArray(t.local_mm2b, s_lmm2b, 12 * kEnvSites);
-  StageArray(t.local_off, s_loff, kLocalSites * 4);
-  StageArray(t.exp_tab, s_exp, kExpTableSize);
+  const KmcSmem sm = CarveKmcSmem(t, smem, rpb, g_per);
+  StageKmcSmem(t, l.sp, sm, kSparse);
   __syncthreads();
-  const ExpConsts ec{s_exp, t.exp_l1, t.exp_l2};
+  uint32_t *s_de = sm.de, *s_mmm = sm.mmm, *s_mm2 = sm.mm2;
+  SmallTables *s_small = sm.small;
+  uint8_t *s_lst = sm.lst, *s_lmmm = sm.lmmm, *s_lmm2f = sm.lmm2f, *s_lmm2b = sm.lmm2b;
+  int8_t *s_loff = sm.loff, *s_arr = sm.arr;
+  KmcShared *s_rep = sm.rep;
+  uint8_t *s_pos = sm.pos;
+  uint32_t *s_pxenv = sm.pxenv, *s_inter = sm.inter;
+  uint16_t *s_pxst = sm.pxst;
+  const ExpConsts ec{sm.exp, t.exp_l1, t.exp_l2};
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rl = warp / g_per;         // replica within block
@@ -1168,90 +1303,13 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     // ---- phase 2: the 12 jump evaluations ----
     if (kSparse) {
       // list the non-base sites of the neighbourhood (warp 0)
-      if (g == 0) {
-        int k_sites = 0;
-#pragma unroll
-        for (int w = 0; w < 5; ++w) {
-          const int k = w * 32 + lane;
-          const int code = k < kLocalSites ? rs.local[k] : l.sp.base_code;
-          const bool nb = code != l.sp.base_code && k != l.sp.center;
-          const unsigned mk = __ballot_sync(0xffffffffu, nb);
-          const int idx = k_sites + __popc(mk & ((1u << lane) - 1u));
-          if (nb && idx < kMaxSparseSites) {
-            rs.nb_l[idx] = static_cast<uint8_t>(k);
-            rs.nb_code[idx] = static_cast<int8_t>(code);
-          }
-          k_sites += __popc(mk);
-        }
-        // padding up to the next multiple of 4 (and the fixed entry 32)
-        if (lane >= k_sites && lane < ((k_sites + 3) & ~3)) {
-          rs.nb_l[lane] = static_cast<uint8_t>(kLocalSites);
-          rs.nb_code[lane] = static_cast<int8_t>(l.sp.base_code);
-        }
-        if (lane == 0) {
-          rs.nb_l[kMaxSparseSites] = static_cast<uint8_t>(kLocalSites);
-          rs.nb_code[kMaxSparseSites] = static_cast<int8_t>(l.sp.base_code);
-        }
-        __syncwarp();
-        // interacting pairs (k2 < k): lane k tests its row of the interaction table
-        unsigned pm = 0;
-        if (k_sites <= kMaxSparseSites && lane < k_sites) {
-          const uint32_t *row = s_inter + rs.nb_l[lane] * kInterWords;
-          for (int k2 = 0; k2 < lane; ++k2) {
-            const int l2 = rs.nb_l[k2];
-            pm |= ((row[l2 >> 5] >> (l2 & 31)) & 1u) << k2;
-          }
-        }
-        const int cnt = __popc(pm);
-        int pre = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int v = __shfl_up_sync(0xffffffffu, pre, o);
-          if (lane >= o) pre += v;
-        }
-        const int n_pairs = __shfl_sync(0xffffffffu, pre, 31);
-        pre -= cnt;
-        if (n_pairs <= kMaxSparsePairs) {
-          while (pm) {
-            const int k2 = __ffs(pm) - 1;
-            pm &= pm - 1;
-            rs.pairs[pre++] = static_cast<uint16_t>(lane | (k2 << 8));
-          }
-          if (lane < ((n_pairs + 3) & ~3) - n_pairs)
-            rs.pairs[n_pairs + lane] = static_cast<uint16_t>(kMaxSparseSites | (kMaxSparseSites << 8));
-        }
-        if (lane == 0) {
-          rs.nbk = k_sites;
-          rs.npairs = n_pairs;
-        }
-      }
+      if (g == 0) SparseList(rs, s_inter, l.sp, lane);
       ReplicaSync(g_per, rl);
     }
     const bool sparse_step = kSparse && rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
     if (sparse_step) {
       // one lane per (jump, half): item = lane * G + g, items 0..23
-      const int item = lane * g_per + g;
-      const int c = item % 12, part = item / 12;
-      LaneAcc la{0, 0, 0u};
-      if (item < 24) {
-        const int mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
-        const int slot = s_small->slot[mig];
-        const bool quartic = s.barrier_kind == 0;
-        const bool ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
-        if (ok && (part == 0 || quartic))
-          la = EvalJumpPairs(l.sp, s_pos, s_pxst, s_pxenv, s_small, rs, e, t.x_code, c, part, mig, slot, quartic);
-        if (ok) {
-          const long long *bf = l.sp.base_form + slot * 3;
-          if (part == 0) {
-            rs.acc[c][0] = l.sp.base_de[mig] + la.a;
-            rs.acc[c][1] = (quartic ? bf[0] : bf[2]) + la.b;
-          } else {
-            rs.acc[c][2] = bf[1] + la.a + la.b;
-          }
-        }
-        if (part == 0) rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
-      }
-      bad_all |= __reduce_or_sync(0xffffffffu, la.bad);
+      bad_all |= SparseItem(t, l.sp, s_lst, s_pos, s_pxst, s_pxenv, s_small, rs, s.barrier_kind, lane * g_per + g);
     }
     if (!sparse_step) {
       const DenseArgs da{s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_de, s_mmm, s_mm2, s_small, st, rm, rf, rb};
@@ -1358,7 +1416,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
           rec.vacancy = vac;
           rec.target = tgt;
           rec.selected = sel;
-          rec.pad = 0;
+          rec.slot = 0;
           rec.ea = ea_sel;
           rec.de = de_sel;
           rec.total_rate = total;
@@ -1406,6 +1464,298 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     s.steps[r] = step0 + steps_done;
   }
   if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
+// K4b: multi-vacancy KMC, one block of kMultiWarps warps per lattice.
+// Every vacancy of the lattice is tracked (slots 0..V-1). Per step:
+//  1. the warps re-evaluate the 12 events of each vacancy whose 135-site
+//     neighbourhood changed (one warp per vacancy, the sparse / dense
+//     evaluation of kmc_kernel). A neighbourhood holding a second vacancy takes
+//     the dense sums in which that vacancy contributes nothing: clusters with two
+//     vacancies have no coefficients and a vacancy has no one-hot slot (the
+//     reference throws there; this is the defined extension). A jump onto a
+//     vacancy has rate 0. Per slot: the 12 rates in id order and their inclusive
+//     scan in 4 shuffle steps (16 lanes, lanes 12-15 zero), K_v = scan[11];
+//  2. warp 0 forms the inclusive prefix of K_v over the slots, 32 slots at a time
+//     (inclusive scan in 5 shuffle steps, plus the running total of the previous
+//     chunks), draws (-log u1, u2) from the lattice's Philox stream (counter =
+//     step, lattice), takes x = u2 * total, the first slot v with prefix >= x and
+//     K_v > 0, then y = x - prefix(v - 1) and the first event with scan >= y and a
+//     positive rate (past the end: the last positive one); dt = -log(u1) / (total
+//     * prefactor); the vacancy moves and the slots whose neighbourhoods contain
+//     one of the two changed sites are marked for step 1.
+// The oracle restates exactly these operations (orc_kmc_multi).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool InLocal(const uint32_t *bits, int dx, int dy, int dz) {
+  if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) return false;
+  const int b = ((dx + 4) * kLocalSpan + (dy + 4)) * kLocalSpan + (dz + 4);
+  return (bits[b >> 5] >> (b & 31)) & 1u;
+}
+
+size_t MultiSharedBytes(const DevTables &t, bool sparse) {
+  KmcLaunch l{};
+  l.warps_per_replica = 1;
+  l.replicas_per_block = kMultiWarps;
+  l.sparse = sparse ? 1 : 0;
+  size_t b = KmcSharedBytes(t, l);
+  // sparse tables are always carved (the layout is shared); add them when not counted
+  if (!sparse) b += 4 * 12 * 136 + 4 * 2 * (kTriEnv + 1) + 4 * kLocalSites * kInterWords + 2 * (kTriState + 1);
+  b = (b + 15) & ~size_t(15);
+  b += sizeof(double) * kMaxMultiVac * 12;  // rate scans
+  b += sizeof(double) * kMaxMultiVac;       // slot prefix
+  b += sizeof(long long) * kMaxMultiVac;    // positions
+  b += sizeof(H3) * kMaxMultiVac;           // coordinates
+  b += sizeof(int) * kMaxMultiVac;          // dirty list
+  b += sizeof(uint16_t) * kMaxMultiVac;     // positive-rate masks
+  b += sizeof(int) * 4 + sizeof(uint32_t) * kLocalBitWords;
+  return (b + 15) & ~size_t(15);
+}
+
+template <bool kSparse>
+__global__ void __launch_bounds__(kMultiWarps * 32, 1)
+    kmc_multi_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcMultiArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const KmcSmem sm = CarveKmcSmem(t, smem, kMultiWarps, 1);
+  size_t off = (reinterpret_cast<size_t>(sm.end) + 15) & ~size_t(15);
+  double *s_cum = reinterpret_cast<double *>(off);                   // [kMaxMultiVac][12]
+  double *s_incl = s_cum + kMaxMultiVac * 12;                         // [kMaxMultiVac]
+  long long *s_pos = reinterpret_cast<long long *>(s_incl + kMaxMultiVac);
+  H3 *s_h = reinterpret_cast<H3 *>(s_pos + kMaxMultiVac);
+  int *s_list = reinterpret_cast<int *>(s_h + kMaxMultiVac);
+  uint16_t *s_kmask = reinterpret_cast<uint16_t *>(s_list + kMaxMultiVac);
+  int *s_ctl = reinterpret_cast<int *>(s_kmask + kMaxMultiVac);      // [0] dirty count, [1] stop
+  uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_ctl + 4);
+
+  const int r = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int v0 = a.vac_off[r], nv = a.vac_off[r + 1] - v0;
+  if (nv <= 0 || nv > kMaxMultiVac) return;  // block-uniform, before any barrier; the host rejects such lattices
+  StageKmcSmem(t, a.sp, sm, kSparse);
+  const int n = a.lat_n[r];
+  int8_t *lat = species + a.lat_off[r];
+  for (int i = threadIdx.x; i < kLocalBitWords; i += blockDim.x) s_bits[i] = a.local_bits[i];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const long long p = a.vac_pos[v0 + i];
+    s_pos[i] = p;
+    s_h[i] = SiteCoord(p, n);
+    s_list[i] = i;  // every slot is evaluated at the start of a launch
+  }
+  if (threadIdx.x == 0) {
+    s_ctl[0] = nv;
+    s_ctl[1] = 0;
+  }
+  __syncthreads();
+  const ExpConsts ec{sm.exp, t.exp_l1, t.exp_l2};
+  KmcShared &rs = sm.rep[warp];
+  int8_t *st = sm.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const int x_code = t.x_code;
+  const int center = sm.lst[t.pos_first];  // local index of the vacancy site itself
+  const double beta = 1.0 / kBoltzmannEv / a.temperature[r];
+  unsigned bad_all = 0;
+  double time = 0.0, energy = 0.0;
+  unsigned long long step0 = 0, steps_done = 0;
+  uint32_t key0 = 0, key1 = 0;
+  if (warp == 0) {
+    time = a.time[r];
+    energy = a.energy[r];
+    step0 = a.steps[r];
+    key0 = a.key[2 * r];
+    key1 = a.key[2 * r + 1];
+  }
+  double nlog_blk = 0.0, u2_blk = 0.0;
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    // ---- phase 1: re-evaluate the marked slots, one warp per slot ----
+    const int nd = s_ctl[0];
+    for (int q = warp; q < nd; q += kMultiWarps) {
+      const int v = s_list[q];
+      const H3 h = s_h[v];
+      bool other = false;  // a second vacancy in the neighbourhood
+      for (int k = lane; k < kLocalSites; k += 32) {
+        const int8_t *o = sm.loff + k * 4;
+        const int8_t c = lat[NeighborId(h, o[0], o[1], o[2], n)];
+        rs.local[k] = c;
+        other |= c == x_code && k != center;
+      }
+      if (lane < 12) {
+        const int8_t *o = t.dir + lane * 4;
+        rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
+      }
+      const bool extra_x = __any_sync(0xffffffffu, other);
+      __syncwarp();
+      bool sparse_v = false;
+      if (kSparse && !extra_x) {
+        SparseList(rs, sm.inter, a.sp, lane);
+        __syncwarp();
+        sparse_v = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
+      }
+      if (sparse_v) {
+        bad_all |= SparseItem(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, a.barrier_kind, lane);
+      } else {
+        const DenseArgs da{sm.lst, sm.lmmm, sm.lmm2f, sm.lmm2b, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb};
+        unsigned b = DenseJumpsCold(t, rs, da, a.barrier_kind, 0, 1, lane);
+        if (extra_x) b &= ~static_cast<unsigned>(kStatusXInEnv | kStatusBadCluster);
+        bad_all |= b;
+      }
+      __syncwarp();
+      double ea = 0.0, de = 0.0, k = 0.0;
+      long long id = 0x7fffffffffffffffLL;
+      if (lane < 12) {
+        const int slot = rs.slot[lane];
+        id = rs.ids[lane];
+        if (slot >= 0) {
+          const JumpOut o = JumpEpilogue(t, ec, a.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+          ea = o.ea;
+          de = o.de;
+          k = ExpFast(-ea * beta, ec);
+        } else if (slot == -1) {
+          bad_all |= kStatusNoCoefficients;
+        }
+      }
+      // events in id order (the sorted 1NN list), then their inclusive scan
+      int rank = 0;
+      for (int q2 = 0; q2 < 12; ++q2) {
+        const long long oid = __shfl_sync(0xffffffffu, id, q2);
+        rank += (q2 != lane) && (oid < id);
+      }
+      int src = 0;
+      for (int q2 = 0; q2 < 12; ++q2)
+        if (__shfl_sync(0xffffffffu, rank, q2) == lane) src = q2;
+      const double k_s = __shfl_sync(0xffffffffu, k, src);
+      const double ea_s = __shfl_sync(0xffffffffu, ea, src);
+      const double de_s = __shfl_sync(0xffffffffu, de, src);
+      const long long id_s = __shfl_sync(0xffffffffu, id, src);
+      double cum = lane < 12 ? k_s : 0.0;
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, cum, o);
+        if (lane >= o) cum += u;
+      }
+      const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
+      if (lane < 12) {
+        s_cum[v * 12 + lane] = cum;
+        const long long e = static_cast<long long>(v0 + v) * 12 + lane;
+        a.ev_ea[e] = ea_s;
+        a.ev_de[e] = de_s;
+        a.ev_tgt[e] = id_s;
+      }
+      if (lane == 0) s_kmask[v] = static_cast<uint16_t>(kpos);
+      __syncwarp();
+    }
+    __syncthreads();
+    // ---- phase 2: selection over all slots and the move (warp 0) ----
+    if (warp == 0) {
+      if (lane == 0) s_ctl[1] = (a.stop_flag && (it & 63) == 0 && *a.stop_flag) ? 1 : 0;
+      __syncwarp();
+      if (s_ctl[1] == 0) {
+        if ((it & 31) == 0) {
+          const unsigned long long ctr = step0 + it + lane;
+          const uint4 xr = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                         static_cast<uint32_t>(r), 0x4b4d43u, key0, key1);
+          nlog_blk = -log(U01Open(xr.x, xr.y));
+          u2_blk = U01(xr.z, xr.w);
+        }
+        const double nlog_u1 = __shfl_sync(0xffffffffu, nlog_blk, static_cast<int>(it & 31));
+        const double u2 = __shfl_sync(0xffffffffu, u2_blk, static_cast<int>(it & 31));
+        const int chunks = (nv + 31) >> 5;
+        double run = 0.0;
+        for (int c = 0; c < chunks; ++c) {
+          const int v = c * 32 + lane;
+          double sc = v < nv ? s_cum[v * 12 + 11] : 0.0;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, sc, o);
+            if (lane >= o) sc += u;
+          }
+          if (v < nv) s_incl[v] = run + sc;
+          run = run + __shfl_sync(0xffffffffu, sc, 31);
+        }
+        const double total = run;
+        __syncwarp();
+        const double xs = __dmul_rn(u2, total);  // not contracted with the subtraction below
+        int vsel = -1, vlast = -1;
+        for (int c = 0; c < chunks; ++c) {
+          const int v = c * 32 + lane;
+          const bool pos = v < nv && s_kmask[v] != 0;
+          const unsigned hit = __ballot_sync(0xffffffffu, pos && s_incl[v] >= xs);
+          const unsigned any = __ballot_sync(0xffffffffu, pos);
+          if (vsel < 0 && hit) vsel = c * 32 + __ffs(hit) - 1;
+          if (any) vlast = c * 32 + 31 - __clz(any);
+        }
+        if (vsel < 0) vsel = vlast;
+        if (vsel < 0 || !(total > 0.0) || !isfinite(total)) {
+          bad_all |= kStatusNumeric;
+          s_ctl[1] = 1;  // every lane writes the same value
+        } else {
+          const double y = __dsub_rn(xs, vsel > 0 ? s_incl[vsel - 1] : 0.0);
+          const unsigned km = s_kmask[vsel];
+          const bool pos = lane < 12 && ((km >> lane) & 1u);
+          const unsigned hit = __ballot_sync(0xffffffffu, pos && s_cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
+          const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
+          const long long e = static_cast<long long>(v0 + vsel) * 12 + sel;
+          const long long p_old = s_pos[vsel];
+          const long long tgt = a.ev_tgt[e];
+          const double ea_sel = a.ev_ea[e], de_sel = a.ev_de[e];
+          time += nlog_u1 * RcpFast(total * kPrefactor);
+          energy += de_sel;
+          const H3 h_old = s_h[vsel];
+          const H3 h_new = SiteCoord(tgt, n);
+          __syncwarp();
+          if (lane == 0) {
+            lat[p_old] = lat[tgt];  // Config::LatticeJump
+            lat[tgt] = static_cast<int8_t>(x_code);
+            s_pos[vsel] = tgt;
+            s_h[vsel] = h_new;
+            if (r == a.trace_replica && a.trace) {
+              KmcTraceRec rec;
+              rec.vacancy = p_old;
+              rec.target = tgt;
+              rec.selected = sel;
+              rec.slot = vsel;
+              rec.ea = ea_sel;
+              rec.de = de_sel;
+              rec.total_rate = total;
+              rec.time = time;
+              rec.energy = energy;
+              a.trace[it] = rec;
+            }
+          }
+          // slots to re-evaluate: the moved one and those whose neighbourhood holds a changed site
+          int nd2 = 0;
+          for (int c = 0; c < chunks; ++c) {
+            const int v = c * 32 + lane;
+            bool d = false;
+            if (v < nv) {
+              const H3 hv = v == vsel ? h_new : s_h[v];
+              d = v == vsel ||
+                  InLocal(s_bits, MinImage(h_old.x - hv.x, n), MinImage(h_old.y - hv.y, n),
+                          MinImage(h_old.z - hv.z, n)) ||
+                  InLocal(s_bits, MinImage(h_new.x - hv.x, n), MinImage(h_new.y - hv.y, n),
+                          MinImage(h_new.z - hv.z, n));
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, d);
+            if (d) s_list[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
+            nd2 += __popc(m);
+          }
+          if (lane == 0) s_ctl[0] = nd2;
+        }
+      }
+    }
+    __syncthreads();
+    if (s_ctl[1]) {
+      if (warp == 0 && !(bad_all & kStatusNumeric)) bad_all |= kStatusStopped;
+      break;
+    }
+    ++steps_done;
+  }
+  if (warp == 0 && lane == 0) {
+    a.time[r] = time;
+    a.energy[r] = energy;
+    a.steps[r] = step0 + steps_done;
+  }
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) a.vac_pos[v0 + i] = s_pos[i];
+  if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
 }
 
 // ---------------------------------------------------------------------------
@@ -1879,6 +2229,18 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
     if (err != cudaSuccess) return err;
   }
   kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  return cudaGetLastError();
+}
+
+size_t KmcMultiSharedBytes(const DevTables &t, bool sparse) { return MultiSharedBytes(t, sparse); }
+
+cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiArgs &a, bool sparse,
+                           cudaStream_t stream) {
+  const size_t sm = MultiSharedBytes(t, sparse);
+  auto kern = sparse ? kmc_multi_kernel<true> : kmc_multi_kernel<false>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  kern<<<a.num_replicas, kMultiWarps * 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

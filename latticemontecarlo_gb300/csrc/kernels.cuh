@@ -37,7 +37,7 @@ constexpr int kRngWords = 2 * 312 + 2;  // MT19937-64 state (312 x u64) + index;
 
 struct KmcTraceRec {
   long long vacancy, target;
-  int selected, pad;
+  int selected, slot;  // slot: the vacancy that moved (multi-vacancy kernel; 0 otherwise)
   double ea, de, total_rate, time, energy;
 };
 
@@ -112,6 +112,39 @@ cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, cons
                           int *status, cudaStream_t stream);
 cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
                          unsigned long long *counts, double *energy, cudaStream_t stream);
+// Multi-vacancy KMC: every vacancy of a lattice is tracked and one event is
+// chosen per step among all of them (residence-time selection over V x 12
+// events); one block per lattice. Vacancies are slots 0..V-1 (ascending site
+// id at initialisation), kept when they move.
+constexpr int kMaxMultiVac = 256;
+constexpr int kMultiWarps = 8;
+constexpr int kLocalSpan = 9;  // neighbourhood displacements lie in [-4, 4]^3 (half-lattice units)
+constexpr int kLocalBitWords = (kLocalSpan * kLocalSpan * kLocalSpan + 31) / 32;
+struct KmcMultiArgs {
+  long long *vac_pos;               // [slots] lattice id of each vacancy
+  const int *vac_off;               // [R + 1] first slot of each lattice
+  unsigned long long *steps;        // [R]
+  double *time, *energy;            // [R]
+  const double *temperature;        // [R]
+  const uint32_t *key;              // [R][2] Philox key
+  const long long *lat_off;
+  const int *lat_n;
+  int num_replicas;
+  int barrier_kind;
+  unsigned long long nsteps;        // steps per launch
+  double *ev_ea, *ev_de;            // [slots][12] scratch: events in id order
+  long long *ev_tgt;                // [slots][12]
+  int trace_replica;                // -1 = none
+  KmcTraceRec *trace;               // [nsteps] records of lattice trace_replica
+  volatile int *stop_flag;          // host-mapped, may be null
+  int *status;
+  KmcSparse sp;
+  uint32_t local_bits[kLocalBitWords];  // displacements (dx, dy, dz) + 4 of the 135-site neighbourhood
+};
+size_t KmcMultiSharedBytes(const DevTables &t, bool sparse);
+cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiArgs &a, bool sparse,
+                           cudaStream_t stream);
+
 // prepare = false skips the shared-memory attribute call (already made by
 // KmcOccupancy), so the launch can be recorded into a CUDA graph.
 cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,

@@ -649,6 +649,9 @@ struct orc_model {
   /* mapping cache for the lattice the model was last used with */
   const orc_lattice *map_lat;
   mappings maps;
+  /* multi-vacancy extension (orc_kmc_multi): a cluster with two vacancies or a
+   * vacancy in a one-hot environment contributes nothing instead of an error */
+  int x_zero;
 };
 
 static const char *kKnown[] = {"X", "Al", "Mg", "Zn", "Cu", "Sn"};
@@ -806,6 +809,7 @@ void orc_model_destroy(orc_model *m) {
 }
 
 int orc_model_num_species(const orc_model *m) { return m->E; }
+void orc_model_set_vacancy_zero(orc_model *m, int on) { m->x_zero = on ? 1 : 0; }
 int orc_model_num_theta(const orc_model *m) { return m->num_theta; }
 int orc_model_code(const orc_model *m, const char *name) {
   for (int c = 0; c < m->E; ++c)
@@ -921,11 +925,15 @@ static int onehot_counts(const orc_model *m, const mlist *l, const int *codes, i
       for (int z = 0; z < blk; ++z) out[off + z] = 0;
       last = c->group;
     }
-    int r[2];
+    int r[2], skip = 0;
     for (int z = 0; z < c->size; ++z) {
       r[z] = m->rank[codes[c->idx[z]]];
-      if (r[z] < 0) return -3; /* one_hot_encode_hashmap.at() throws */
+      if (r[z] < 0) {
+        if (!m->x_zero) return -3; /* one_hot_encode_hashmap.at() throws */
+        skip = 1;                  /* a vacancy: zero one-hot vector */
+      }
     }
+    if (skip) continue;
     int t;
     if (c->size == 1) t = r[0];
     else if (!c->sym) t = r[0] * m->eh + r[1];
@@ -990,9 +998,9 @@ static int de_from_ids(const orc_model *m, const mappings *mp, const int8_t *sp,
     }
     const int is = orc_model_cluster_index(m, c->group, c->size, st);
     const int ie = orc_model_cluster_index(m, c->group, c->size, en);
-    if (is < 0 || ie < 0) return -2;
-    s0[is]++;
-    e0[ie]++;
+    if ((is < 0 || ie < 0) && !m->x_zero) return -2;
+    if (is >= 0) s0[is]++; /* x_zero: a cluster outside the indexer counts nothing */
+    if (ie >= 0) e0[ie]++;
   }
   double acc = 0.0;
   for (int z = 0; z < m->num_theta; ++z) {
@@ -1216,13 +1224,13 @@ int orc_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int
     const int64_t *n1 = lat->nn[l1];
     int k[3] = {e1, 0, 0};
     int idx = orc_model_cluster_index(m, 0, 1, k);
-    if (idx < 0) return -2;
-    c[idx]++;
+    if (idx < 0 && !m->x_zero) return -2;
+    if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
     for (int a = 0; a < 12; ++a) {
       const int64_t l2 = n1[a];
       k[1] = sp[l2];
-      if ((idx = orc_model_cluster_index(m, 1, 2, k)) < 0) return -2;
-      c[idx]++;
+      if ((idx = orc_model_cluster_index(m, 1, 2, k)) < 0 && !m->x_zero) return -2;
+      if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
       for (int b = 0; b < 12; ++b) {
         const int64_t l3 = lat->nn[l2][b];
         int label = -1;
@@ -1234,8 +1242,8 @@ int orc_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int
           if (n1[q] == l3) label = 6;
         if (label < 0) continue;
         k[2] = sp[l3];
-        if ((idx = orc_model_cluster_index(m, label, 3, k)) < 0) return -2;
-        c[idx]++;
+        if ((idx = orc_model_cluster_index(m, label, 3, k)) < 0 && !m->x_zero) return -2;
+        if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
       }
       for (int b = 12; b < 18; ++b) {
         const int64_t l3 = lat->nn[l2][b];
@@ -1243,19 +1251,19 @@ int orc_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int
         for (int q = 18; q < 42; ++q) in3 |= n1[q] == l3;
         if (!in3) continue;
         k[2] = sp[l3];
-        if ((idx = orc_model_cluster_index(m, 7, 3, k)) < 0) return -2;
-        c[idx]++;
+        if ((idx = orc_model_cluster_index(m, 7, 3, k)) < 0 && !m->x_zero) return -2;
+        if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
       }
     }
     for (int a = 12; a < 18; ++a) {
       int kk[3] = {e1, sp[n1[a]], 0};
-      if ((idx = orc_model_cluster_index(m, 2, 2, kk)) < 0) return -2;
-      c[idx]++;
+      if ((idx = orc_model_cluster_index(m, 2, 2, kk)) < 0 && !m->x_zero) return -2;
+      if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
     }
     for (int a = 18; a < 42; ++a) {
       int kk[3] = {e1, sp[n1[a]], 0};
-      if ((idx = orc_model_cluster_index(m, 3, 2, kk)) < 0) return -2;
-      c[idx]++;
+      if ((idx = orc_model_cluster_index(m, 3, 2, kk)) < 0 && !m->x_zero) return -2;
+      if (idx >= 0) c[idx]++; /* x_zero: unindexed clusters count nothing */
     }
   }
   double acc = 0.0;
@@ -1608,4 +1616,147 @@ int64_t orc_cmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T
   *energy_io = energy;
   if (accepted) *accepted = acc;
   return done;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Multi-vacancy KMC (the project's extension, restated from its definition:  */
+/* the reference tracks one vacancy)                                          */
+/* ------------------------------------------------------------------------- */
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+ * as 1, 2, 3", SC'11): ten rounds of two 32x32->64 multiplies, key bumped by the
+ * Weyl constants after each round. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    c1 = (uint32_t)p1;
+    c3 = (uint32_t)p0;
+    c0 = n0;
+    c2 = n2;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+/* The production KMC draws of lattice r at step s: -log(u1), u1 in (0, 1], and
+ * u2 in [0, 1), 53 bits each, from Philox(counter = (s, r, "KMC"), key = seed). */
+static void philox_step_draws(uint64_t seed, uint64_t step, uint32_t r, double *nlog_u1, double *u2) {
+  const uint32_t ctr[4] = {(uint32_t)step, (uint32_t)(step >> 32), r, 0x4b4d43u};
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t x[4];
+  orc_philox4x32_10(ctr, key, x);
+  const uint64_t a = (((uint64_t)x[0] << 32) | x[1]) >> 11, b = (((uint64_t)x[2] << 32) | x[3]) >> 11;
+  *nlog_u1 = -log((double)(a + 1) * 1.1102230246251565404e-16);
+  *u2 = (double)b * 1.1102230246251565404e-16;
+}
+
+/* inclusive scan of n (16 or 32) values in log2(n) doubling steps:
+ * v[i] <- v[i] + v[i - o] for i >= o, o = 1, 2, 4, ... */
+static void doubling_scan(double *v, int n) {
+  double t[32];
+  for (int o = 1; o < n; o <<= 1) {
+    memcpy(t, v, sizeof(double) * n);
+    for (int i = o; i < n; ++i) v[i] = t[i] + t[i - o];
+  }
+}
+
+int orc_kmc_multi(orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, uint32_t replica,
+                  uint64_t step0, int64_t steps, int kind, int64_t *vac, int nv, double *time_io, double *energy_io,
+                  double *trace9) {
+  if (nv < 1 || nv > 256) return -1;
+  const mappings *mp = maps_for(m, lat);
+  const double beta = 1.0 / kBoltzmann / T;
+  double *cum = (double *)malloc(sizeof(double) * 16 * nv);
+  double *ea = (double *)malloc(sizeof(double) * 12 * nv), *de = (double *)malloc(sizeof(double) * 12 * nv);
+  double *kk = (double *)malloc(sizeof(double) * 12 * nv), *incl = (double *)malloc(sizeof(double) * nv);
+  double time = *time_io, energy = *energy_io;
+  int rc = 0;
+  const int saved = m->x_zero;
+  m->x_zero = 1;
+  for (int64_t s = 0; s < steps && !rc; ++s) {
+    /* every slot: its 12 events in id order, rates and their 16-wide scan */
+    for (int v = 0; v < nv && !rc; ++v) {
+      const int64_t *nb = lat->nn[vac[v]];
+      double *c = cum + 16 * v;
+      for (int j = 0; j < 12; ++j) {
+        ea[12 * v + j] = de[12 * v + j] = kk[12 * v + j] = 0.0;
+        if (sp[nb[j]] == m->x_code) continue; /* onto a vacancy: rate 0 */
+        pair_ids p;
+        double o[4];
+        if ((rc = make_pair_ids(lat, vac[v], nb[j], &p))) break;
+        if ((rc = barrier_from_ids(m, mp, sp, vac[v], nb[j], &p, kind, o))) break;
+        ea[12 * v + j] = o[0];
+        de[12 * v + j] = o[1];
+        kk[12 * v + j] = exp(-o[0] * beta);
+      }
+      for (int j = 0; j < 16; ++j) c[j] = j < 12 ? kk[12 * v + j] : 0.0;
+      doubling_scan(c, 16);
+    }
+    if (rc) break;
+    /* prefix of the slot totals, 32 slots at a time */
+    double run = 0.0;
+    for (int c0 = 0; c0 < nv; c0 += 32) {
+      double w[32];
+      for (int i = 0; i < 32; ++i) w[i] = c0 + i < nv ? cum[16 * (c0 + i) + 11] : 0.0;
+      doubling_scan(w, 32);
+      for (int i = 0; i < 32 && c0 + i < nv; ++i) incl[c0 + i] = run + w[i];
+      run = run + w[31];
+    }
+    const double total = run;
+    double nlog_u1, u2;
+    philox_step_draws(seed, step0 + (uint64_t)s, replica, &nlog_u1, &u2);
+    const double xs = u2 * total;
+    int vsel = -1, vlast = -1;
+    for (int v = 0; v < nv; ++v) {
+      if (!(cum[16 * v + 11] > 0.0)) continue;
+      vlast = v;
+      if (vsel < 0 && incl[v] >= xs) vsel = v;
+    }
+    if (vsel < 0) vsel = vlast;
+    if (vsel < 0 || !(total > 0.0) || !isfinite(total)) {
+      rc = -5;
+      break;
+    }
+    const double y = xs - (vsel > 0 ? incl[vsel - 1] : 0.0);
+    int sel = -1, jlast = -1;
+    for (int j = 0; j < 12; ++j) {
+      if (!(kk[12 * vsel + j] > 0.0)) continue;
+      jlast = j;
+      if (sel < 0 && cum[16 * vsel + j] >= y) sel = j;
+    }
+    if (sel < 0) sel = jlast;
+    const int64_t from = vac[vsel], to = lat->nn[from][sel];
+    time += nlog_u1 / (total * kPrefactor);
+    energy += de[12 * vsel + sel];
+    sp[from] = sp[to];
+    sp[to] = (int8_t)m->x_code;
+    vac[vsel] = to;
+    if (trace9) {
+      double *t = trace9 + 9 * s;
+      t[0] = vsel;
+      t[1] = (double)from;
+      t[2] = (double)to;
+      t[3] = sel;
+      t[4] = ea[12 * vsel + sel];
+      t[5] = de[12 * vsel + sel];
+      t[6] = total;
+      t[7] = time;
+      t[8] = energy;
+    }
+  }
+  m->x_zero = saved;
+  *time_io = time;
+  *energy_io = energy;
+  free(cum);
+  free(ea);
+  free(de);
+  free(kk);
+  free(incl);
+  return rc;
 }

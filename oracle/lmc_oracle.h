@@ -118,6 +118,26 @@ int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T,
 int64_t orc_cmc(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t attempts,
                 int batch, double *energy_io, double *energy_trace, int64_t cap, int64_t *accepted);
 
+/* Multi-vacancy extension switch: with on != 0 a cluster whose element multiset
+ * has no index (two or more vacancies) counts nothing and a vacancy inside a
+ * one-hot environment contributes a zero vector, instead of the reference's
+ * exceptions (ClusterIndexer::GetIndex, one_hot_encode_hashmap.at()). */
+void orc_model_set_vacancy_zero(orc_model *m, int on);
+
+/* Philox4x32-10 block (Salmon et al., SC'11): out = bijection(ctr) under key. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Multi-vacancy KMC as the GPU defines it (lmc_kmc_multi_run): the nv slots
+ * vac[] (site ids, updated in place) of lattice `replica`, steps step0 ..
+ * step0 + steps - 1 of its Philox stream. Every step re-evaluates all slots
+ * (a vacancy inside another's neighbourhood contributes nothing to the
+ * encodings), scans the rates as the kernel does, selects and moves one vacancy.
+ * trace9 (NULL or 9 doubles per step): slot, vacancy, target, selected, Ea, dE,
+ * total rate, time, energy. time_io / energy_io carry the clock and energy. */
+int orc_kmc_multi(orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, uint32_t replica,
+                  uint64_t step0, int64_t steps, int kind, int64_t *vac, int nv, double *time_io, double *energy_io,
+                  double *trace9);
+
 #ifdef __cplusplus
 }
 #endif

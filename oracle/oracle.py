@@ -72,6 +72,10 @@ def lib() -> C.CDLL:
             "orc_kmc_ex": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, DP, DP, DP, DP,
                                      C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]),
             "orc_cmc": (I64, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, DP, DP, I64, I64P]),
+            "orc_model_set_vacancy_zero": (None, [P, C.c_int]),
+            "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+            "orc_kmc_multi": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, I64, C.c_int,
+                                        I64P, C.c_int, DP, DP, DP]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -181,6 +185,11 @@ class Model:
     def code(self, name: str) -> int:
         return lib().orc_model_code(self.h, name.encode())
 
+    def set_vacancy_zero(self, on: bool = True):
+        """Multi-vacancy extension: clusters with two vacancies count nothing, a
+        vacancy in a one-hot environment is a zero vector (the reference throws)."""
+        lib().orc_model_set_vacancy_zero(self.h, int(on))
+
 
 def _sp(species: np.ndarray):
     assert species.dtype == np.int8 and species.flags.c_contiguous
@@ -266,3 +275,28 @@ def cmc(model: Model, lat: Lattice, species, T: float, seed: int, attempts: int,
     if done < 0:
         raise OracleError("orc_cmc failed")
     return done, e.value, acc.value, (tr[:done] if trace else None)
+
+
+def philox4x32_10(counter, key) -> np.ndarray:
+    """One Philox4x32-10 block (Salmon et al., SC'11)."""
+    c = np.ascontiguousarray(counter, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_p(c, C.c_uint32), _p(k, C.c_uint32), _p(out, C.c_uint32))
+    return out
+
+
+def kmc_multi(model: Model, lat: Lattice, species, T: float, seed: int, vacancies, steps: int, replica: int = 0,
+              step0: int = 0, kind: int = 0, time: float = 0.0, energy: float = 0.0):
+    """Multi-vacancy KMC as the GPU kernel defines it (every slot re-evaluated
+    every step). species and the returned slot positions are updated in place.
+    Returns (trace [steps x 9]: slot, vacancy, target, selected, Ea, dE, total,
+    time, energy), vacancies, time, energy)."""
+    vac = np.ascontiguousarray(vacancies, dtype=np.int64).copy()
+    trace = np.zeros((steps, 9))
+    t, e = C.c_double(time), C.c_double(energy)
+    rc = lib().orc_kmc_multi(model.h, lat.h, _sp(species), T, seed, replica, step0, steps, kind,
+                             _p(vac, C.c_int64), vac.size, C.byref(t), C.byref(e), _p(trace, C.c_double))
+    if rc:
+        raise OracleError(f"orc_kmc_multi rc={rc}")
+    return trace, vac, t.value, e.value
