@@ -236,6 +236,8 @@ def run_ours(args, rank, world, local):
         result["cmc"] = run_cmc(args, device, flush, barrier)
     if args.surrogate_samples > 0:
         result["surrogate"] = run_surrogate(args, device)
+    if not args.no_large:
+        result["large_lattice"] = run_large(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -270,6 +272,60 @@ def run_cmc(args, device, flush, barrier):
             "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+
+
+def run_large(args, device):
+    """Large-lattice workload: one n = 64 FCC supercell (2^20 sites), Al/Mg/Zn/Cu
+    .93/.03/.03/.01 with 64 vacancies, T = 500 K: one EnergyPredictor census,
+    CMC sweeps (throughput mode), and multi-vacancy KMC events (every vacancy
+    tracked, one event per step among 64 x 12)."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import _native as N
+    from latticemontecarlo_gb300 import synthetic as S
+
+    L = S.LARGE
+    el = L["elements"]
+    coeffs = S.make_coefficients(el, 64)
+    sp = S.make_lattice(L["n"], L["fractions"], L["vacancies"], 64, el)
+    ctx = Context(Model.from_coefficients(coeffs, list(el)), device=device)
+    ctx.set_lattices([L["n"]], sp)
+    T = 500.0
+    ctx.energy()
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e0, _ = ctx.energy()
+    census_ms = (time.perf_counter() - t0) / reps * 1e3
+    peak, _ = peaks()
+    out = {"workload": "n=64 FCC (1048576 sites), Al/Mg/Zn/Cu .93/.03/.03/.01, 64 vacancies, T=500 K",
+           "census": {"ms": census_ms, "sites_per_s": sp.size / (census_ms / 1e3),
+                      "note": "wall clock per lmc_energy call (launch, census, energy, counts copied back)"}}
+    if args.large_cmc_sweeps > 0:
+        attempts = args.large_cmc_sweeps * sp.size
+        ctx.cmc_run(T, sp.size, mode=N.LMC_CMC_THROUGHPUT, seed=1, energy=e0)  # warm-up sweep
+        ctx.set_lattices([L["n"]], sp)
+        e, done, acc = ctx.cmc_run(T, attempts, mode=N.LMC_CMC_THROUGHPUT, seed=2, energy=e0)
+        ms = ctx.last_run_ms()
+        v = done / (ms / 1e3)
+        out["cmc"] = {"sweeps": args.large_cmc_sweeps, "attempts": int(done), "accepted": int(acc), "ms": ms,
+                      "value": v, "unit": "swaps/s (Metropolis attempts)",
+                      "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * v / 1e9, "peak": peak,
+                                   "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * v / 1e9 / peak}}
+        ctx.set_lattices([L["n"]], sp)
+    if args.large_kmc_events > 0:
+        ctx.kmc_multi_init([T], seed=3)
+        ctx.kmc_multi_run(2000)  # warm-up
+        ctx.kmc_multi_run(args.large_kmc_events)
+        ms = ctx.last_run_ms()
+        off, vac, steps, tm, en = ctx.kmc_multi_state()
+        v = args.large_kmc_events / (ms / 1e3)
+        out["kmc_multi_vacancy"] = {
+            "events": args.large_kmc_events, "ms": ms, "value": v, "unit": "events/s",
+            "simulated_time_s": float(tm[0]), "vacancies": int(off[-1]),
+            "launch": "one block of 8 warps (a single lattice is one sequential trajectory)",
+            "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
+    return out
 
 
 def _vacancy_grid_lattice(n: int, spacing: int, fractions, seed: int, elements):
@@ -489,6 +545,9 @@ def main():
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
     ap.add_argument("--surrogate-epochs", type=int, default=30)
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
+    ap.add_argument("--large-cmc-sweeps", type=int, default=100, help="CMC sweeps on the n=64 lattice")
+    ap.add_argument("--large-kmc-events", type=int, default=1_000_000, help="multi-vacancy KMC events, n=64")
+    ap.add_argument("--no-large", action="store_true", help="skip the n=64, 64-vacancy block")
     ap.add_argument("--tune-probe-steps", type=int, default=100, help="KMC steps per autotuner probe")
     ap.add_argument("--tune-cache", default=os.environ.get("LMC_KMC_TUNE_CACHE", ""),
                     help="JSON cache of autotuned KMC launch shapes (empty: tune every run)")

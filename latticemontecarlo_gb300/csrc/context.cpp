@@ -113,7 +113,7 @@ struct lmc_ctx {
   bool multi_ready{false};
   int multi_kind{0}, multi_eval{0};
   std::vector<int> m_off_host;
-  DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_ea, m_de, m_tgt, m_trace;
+  DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_trace;
   std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
 
   ~lmc_ctx() {
@@ -123,7 +123,7 @@ struct lmc_ctx {
                       &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &s_feat, &s_mean, &s_spread,
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
-    for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_ea, &m_de, &m_tgt, &m_trace})
+    for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -1769,9 +1769,6 @@ int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, i
     ctx->m_energy.Ensure(8 * R);
     ctx->m_temp.Ensure(8 * R);
     ctx->m_key.Ensure(8 * R);
-    ctx->m_ea.Ensure(8 * 12 * slots);
-    ctx->m_de.Ensure(8 * 12 * slots);
-    ctx->m_tgt.Ensure(8 * 12 * slots);
     std::vector<uint32_t> key(2 * R);
     for (int r = 0; r < R; ++r) {
       key[2 * r] = static_cast<uint32_t>(seed);
@@ -1815,9 +1812,6 @@ int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_s
     a.num_replicas = ctx->num_replicas;
     a.barrier_kind = ctx->multi_kind;
     a.nsteps = steps;
-    a.ev_ea = ctx->m_ea.as<double>();
-    a.ev_de = ctx->m_de.as<double>();
-    a.ev_tgt = ctx->m_tgt.as<long long>();
     a.trace_replica = -1;
     if (trace) {
       ctx->CheckReplica(trace_replica);

@@ -1487,6 +1487,13 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
 //     one of the two changed sites are marked for step 1.
 // The oracle restates exactly these operations (orc_kmc_multi).
 // ---------------------------------------------------------------------------
+// Minimum image of a coordinate difference d in (-2n, 2n) (half units).
+__device__ __forceinline__ int WrapDelta(int d, int n) {
+  d += d < -n ? 2 * n : 0;
+  d -= d >= n ? 2 * n : 0;
+  return d;
+}
+
 __device__ __forceinline__ bool InLocal(const uint32_t *bits, int dx, int dy, int dz) {
   if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) return false;
   const int b = ((dx + 4) * kLocalSpan + (dy + 4)) * kLocalSpan + (dz + 4);
@@ -1503,6 +1510,7 @@ size_t MultiSharedBytes(const DevTables &t, bool sparse) {
   if (!sparse) b += 4 * 12 * 136 + 4 * 2 * (kTriEnv + 1) + 4 * kLocalSites * kInterWords + 2 * (kTriState + 1);
   b = (b + 15) & ~size_t(15);
   b += sizeof(double) * kMaxMultiVac * 12;  // rate scans
+  b += (2 * sizeof(double) + sizeof(long long)) * kMaxMultiVac * 12;  // Ea, dE, target of every event
   b += sizeof(double) * kMaxMultiVac;       // slot prefix
   b += sizeof(long long) * kMaxMultiVac;    // positions
   b += sizeof(H3) * kMaxMultiVac;           // coordinates
@@ -1519,7 +1527,10 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   const KmcSmem sm = CarveKmcSmem(t, smem, kMultiWarps, 1);
   size_t off = (reinterpret_cast<size_t>(sm.end) + 15) & ~size_t(15);
   double *s_cum = reinterpret_cast<double *>(off);                   // [kMaxMultiVac][12]
-  double *s_incl = s_cum + kMaxMultiVac * 12;                         // [kMaxMultiVac]
+  double *s_ea = s_cum + kMaxMultiVac * 12;                           // [kMaxMultiVac][12], id order
+  double *s_de = s_ea + kMaxMultiVac * 12;
+  long long *s_tgt = reinterpret_cast<long long *>(s_de + kMaxMultiVac * 12);
+  double *s_incl = reinterpret_cast<double *>(s_tgt + kMaxMultiVac * 12);  // [kMaxMultiVac]
   long long *s_pos = reinterpret_cast<long long *>(s_incl + kMaxMultiVac);
   H3 *s_h = reinterpret_cast<H3 *>(s_pos + kMaxMultiVac);
   int *s_list = reinterpret_cast<int *>(s_h + kMaxMultiVac);
@@ -1635,10 +1646,9 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
       const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
       if (lane < 12) {
         s_cum[v * 12 + lane] = cum;
-        const long long e = static_cast<long long>(v0 + v) * 12 + lane;
-        a.ev_ea[e] = ea_s;
-        a.ev_de[e] = de_s;
-        a.ev_tgt[e] = id_s;
+        s_ea[v * 12 + lane] = ea_s;
+        s_de[v * 12 + lane] = de_s;
+        s_tgt[v * 12 + lane] = id_s;
       }
       if (lane == 0) s_kmask[v] = static_cast<uint16_t>(kpos);
       __syncwarp();
@@ -1693,10 +1703,10 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
           const bool pos = lane < 12 && ((km >> lane) & 1u);
           const unsigned hit = __ballot_sync(0xffffffffu, pos && s_cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
           const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
-          const long long e = static_cast<long long>(v0 + vsel) * 12 + sel;
+          const int e = vsel * 12 + sel;
           const long long p_old = s_pos[vsel];
-          const long long tgt = a.ev_tgt[e];
-          const double ea_sel = a.ev_ea[e], de_sel = a.ev_de[e];
+          const long long tgt = s_tgt[e];
+          const double ea_sel = s_ea[e], de_sel = s_de[e];
           time += nlog_u1 * RcpFast(total * kPrefactor);
           energy += de_sel;
           const H3 h_old = s_h[vsel];
@@ -1729,10 +1739,10 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
             if (v < nv) {
               const H3 hv = v == vsel ? h_new : s_h[v];
               d = v == vsel ||
-                  InLocal(s_bits, MinImage(h_old.x - hv.x, n), MinImage(h_old.y - hv.y, n),
-                          MinImage(h_old.z - hv.z, n)) ||
-                  InLocal(s_bits, MinImage(h_new.x - hv.x, n), MinImage(h_new.y - hv.y, n),
-                          MinImage(h_new.z - hv.z, n));
+                  InLocal(s_bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
+                          WrapDelta(h_old.z - hv.z, n)) ||
+                  InLocal(s_bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
+                          WrapDelta(h_new.z - hv.z, n));
             }
             const unsigned m = __ballot_sync(0xffffffffu, d);
             if (d) s_list[nd2 + __popc(m & ((1u << lane) - 1u))] = v;

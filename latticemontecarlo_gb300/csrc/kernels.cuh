@@ -132,8 +132,6 @@ struct KmcMultiArgs {
   int num_replicas;
   int barrier_kind;
   unsigned long long nsteps;        // steps per launch
-  double *ev_ea, *ev_de;            // [slots][12] scratch: events in id order
-  long long *ev_tgt;                // [slots][12]
   int trace_replica;                // -1 = none
   KmcTraceRec *trace;               // [nsteps] records of lattice trace_replica
   volatile int *stop_flag;          // host-mapped, may be null
