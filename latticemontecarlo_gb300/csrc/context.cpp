@@ -1962,7 +1962,7 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
                   "D2H");
     } else if (opt->mode == LMC_CMC_THROUGHPUT) {
       int cand = opt->candidates;
-      if (cand <= 0) cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, nsites / 256)));
+      if (cand <= 0) cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, nsites / 64)));
       Require(cand <= 65535, LMC_ERR_INVALID_ARGUMENT, "at most 65535 candidates per round");
       ctx->c_claim.Ensure(sizeof(unsigned long long) * nsites);
       ctx->c_cand.Ensure(sizeof(long long) * 2 * cand);

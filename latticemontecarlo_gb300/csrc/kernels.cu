@@ -1930,32 +1930,40 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
       if (gtid == 0) atomicOr(a.status, kStatusNumeric);
       break;
     }
-    // phase A: candidates and claims
-    for (long long c = gtid; c < a.candidates; c += gthreads) {
+    // phase A: one warp per candidate (candidates spread over the blocks). The
+    // lanes make 32 draws at once; the first different-species draw in try
+    // order wins, exactly as a sequential search would. Then the lanes claim
+    // the 2 x 43 sites within 3NN of the pair.
+    for (long long c = static_cast<long long>(blockIdx.x) * warps + warp; c < a.candidates;
+         c += static_cast<long long>(gridDim.x) * warps) {
       long long l1 = -1, l2 = -1;
       uint32_t prio = 0;
-      for (uint32_t tr = 0; tr < 64; ++tr) {
+      for (uint32_t tr0 = 0; tr0 < 64; tr0 += 32) {
         const uint4 x = PhiloxRound10(static_cast<uint32_t>(round), static_cast<uint32_t>(round >> 32),
-                                      static_cast<uint32_t>(c), tr, k0, k1);
+                                      static_cast<uint32_t>(c), tr0 + lane, k0, k1);
         const long long c1 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.x) << 32) | x.y, nsites));
         const long long c2 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.z) << 32) | x.w, nsites));
-        if (c1 != c2 && species[c1] != species[c2]) {
-          l1 = c1;
-          l2 = c2;
-          prio = (x.x ^ x.w) & 0xFFFF0000u;
+        const bool ok = c1 != c2 && species[c1] != species[c2];
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (m) {
+          const int src = __ffs(m) - 1;
+          l1 = __shfl_sync(0xffffffffu, c1, src);
+          l2 = __shfl_sync(0xffffffffu, c2, src);
+          prio = __shfl_sync(0xffffffffu, (x.x ^ x.w) & 0xFFFF0000u, src);
           break;
         }
       }
-      a.cand[2 * c] = l1;
-      a.cand[2 * c + 1] = l2;
-      if (l1 < 0) continue;
+      if (lane == 0) {
+        a.cand[2 * c] = l1;
+        a.cand[2 * c + 1] = l2;
+      }
+      if (l1 < 0) continue;  // warp-uniform
       const unsigned long long key = (round << 32) | prio | static_cast<uint32_t>(c & 0xFFFF);
-      for (const long long e : {l1, l2}) {
-        const H3 h = SiteCoord(e, n);
-        for (int k = 0; k < kSiteSites; ++k) {
-          const int8_t *o = s.off + k * 4;
-          atomicMax(&a.claim[NeighborId(h, o[0], o[1], o[2], n)], key);
-        }
+      const H3 h1 = SiteCoord(l1, n), h2 = SiteCoord(l2, n);
+      for (int q = lane; q < 2 * kSiteSites; q += 32) {
+        const int k = q < kSiteSites ? q : q - kSiteSites;
+        const int8_t *o = s.off + k * 4;
+        atomicMax(&a.claim[NeighborId(q < kSiteSites ? h1 : h2, o[0], o[1], o[2], n)], key);
       }
     }
     grid.sync();
