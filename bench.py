@@ -539,8 +539,8 @@ def main():
     ap.add_argument("--kmc-steps-per-launch", type=int, default=KMC_STEPS_PER_BENCH_STEP)
     ap.add_argument("--cmc-steps", type=int, default=5)
     ap.add_argument("--cmc-sweeps-per-step", type=int, default=2)
-    ap.add_argument("--cpu-kmc-steps", type=int, default=1500)
-    ap.add_argument("--cpu-cmc-attempts", type=int, default=20000)
+    ap.add_argument("--cpu-kmc-steps", type=int, default=6000)
+    ap.add_argument("--cpu-cmc-attempts", type=int, default=1_500_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
     ap.add_argument("--surrogate-epochs", type=int, default=30)
@@ -568,6 +568,12 @@ def main():
                 "sample": f"{threads} independent KMC trajectories (n~U{{8..24}}, one per host thread), "
                           f"{args.cpu_kmc_steps} steps each, oracle C restatement with barrier memo, "
                           f"{w:.1f} s wall"}
+            if "cmc" in result:
+                cv, cw = cpu_cmc_baseline(threads, args.cpu_cmc_attempts)
+                result["cmc"]["cpu_baseline"] = {
+                    "value": cv, "unit": "swaps/s (Metropolis attempts)", "cores": threads, "kind": "port",
+                    "sample": f"{args.cpu_cmc_attempts} attempts of CanonicalMcOmp (batch = {threads} OpenMP "
+                              f"threads), same lattice, oracle C restatement, {cw:.1f} s wall"}
         print(json.dumps(result), flush=True)
 
 

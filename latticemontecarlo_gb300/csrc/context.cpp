@@ -1962,7 +1962,16 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
                   "D2H");
     } else if (opt->mode == LMC_CMC_THROUGHPUT) {
       int cand = opt->candidates;
-      if (cand <= 0) cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, nsites / 64)));
+      if (cand <= 0) {
+        // Surviving pairs per round grow with the candidates until the lattice
+        // is saturated (about N / 172 pairs fit 3NN apart); the round's latency
+        // grows once candidates outnumber the resident warps (measured on GB300:
+        // the optimum is near N / 80, capped at 3/5 of the resident warps).
+        const long long warps = lmc::CmcThroughputResidentWarps(ctx->t, ctx->device);
+        long long c = nsites / 80;
+        if (warps > 0) c = std::min(c, warps * 3 / 5);
+        cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, c)));
+      }
       Require(cand <= 65535, LMC_ERR_INVALID_ARGUMENT, "at most 65535 candidates per round");
       ctx->c_claim.Ensure(sizeof(unsigned long long) * nsites);
       ctx->c_cand.Ensure(sizeof(long long) * 2 * cand);

@@ -2269,6 +2269,17 @@ cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRef
   return cudaGetLastError();
 }
 
+int CmcThroughputResidentWarps(const DevTables &t, int device) {
+  const size_t sm = SiteSmemBytes(t, kCmcTpThreads / 32);
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cmc_tp_kernel, kCmcTpThreads, sm) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return sms * per_sm * (kCmcTpThreads / 32);
+}
+
 cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTpArgs &a, int device,
                                 cudaStream_t stream) {
   const size_t sm = SiteSmemBytes(t, kCmcTpThreads / 32);

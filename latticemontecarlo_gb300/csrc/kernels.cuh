@@ -215,6 +215,8 @@ struct CmcTpArgs {
   int *status;
   volatile int *stop_flag;
 };
+// Warps of the throughput CMC grid that fit on the device at once (0 on error).
+int CmcThroughputResidentWarps(const DevTables &t, int device);
 cudaError_t LaunchCmcThroughput(const DevTables &t, int8_t *species, const CmcTpArgs &a, int device,
                                 cudaStream_t stream);
 
