@@ -44,6 +44,22 @@ BYTES_PER_ATTEMPT = 100     # algorithmic HBM bytes per CMC attempt
 L2_BYTES = 129 * 1024 * 1024
 
 
+def rank_seed(rank: int) -> int:
+    """Each rank simulates its own replicas (replicas only: no exchange between ranks)."""
+    return 1234 + rank
+
+
+def max_over_ranks(value: float, device) -> float:
+    """The slowest rank's time (whole-job throughput = all ranks' units / this)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -145,7 +161,7 @@ def run_ours(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    seed = 1234 + rank
+    seed = rank_seed(rank)
     cfg, coeffs, ns, species, temps = kmc_inputs(seed, args.replicas)
     model = Model.from_coefficients(coeffs, list(cfg["elements"]))
     ctx = Context(model, device=device)
@@ -173,11 +189,7 @@ def run_ours(args, rank, world, local):
             ctx.kmc_run_graph(args.kmc_steps_per_launch)  # one recorded graph: the persistent launch
             kernel_ms.append(ctx.last_run_ms())
     barrier()
-    t_ms = float(np.sum(kernel_ms))
-    if world > 1:
-        t = torch.tensor([t_ms], device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+    t_ms = max_over_ranks(float(np.sum(kernel_ms)), f"cuda:{device}")
     total_events = events_per_step * args.steps * world
     value = total_events / (t_ms / 1e3)
     # end to end through the C ABI with host buffers (pinned host memory)
