@@ -290,14 +290,22 @@ __global__ void cast_weights_kernel(const float *w1, long long n1, const float *
 // Weights of [rows][k] row-major (blocks of 256 rows per member) in the operand-block
 // layout of the tcgen05 kernel: block (row / 256, k / 32), element (r, kk) at
 // (r / 8) * 256 + (kk / 8) * 64 + (r % 8) * 8 + kk % 8 (bf16 units).
-__global__ void tile_weights_kernel(const float *w, long long rows, int k, __nv_bfloat16 *out) {
+template <typename T>
+__device__ __forceinline__ T FromFloat(float v);
+template <>
+__device__ __forceinline__ __nv_bfloat16 FromFloat<__nv_bfloat16>(float v) { return __float2bfloat16(v); }
+template <>
+__device__ __forceinline__ __half FromFloat<__half>(float v) { return __float2half_rn(v); }
+
+template <typename T>
+__global__ void tile_weights_kernel(const float *w, long long rows, int k, T *out) {
   const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= rows * k) return;
   const long long r = i / k;
   const int kk = static_cast<int>(i % k);
   const long long block = (r / 256) * (k / 32) + kk / 32;
   const int rr = static_cast<int>(r % 256), kc = kk % 32;
-  out[block * 8192 + (rr >> 3) * 256 + (kc >> 3) * 64 + (rr & 7) * 8 + (kc & 7)] = __float2bfloat16(w[i]);
+  out[block * 8192 + (rr >> 3) * 256 + (kc >> 3) * 64 + (rr & 7) * 8 + (kc & 7)] = FromFloat<T>(w[i]);
 }
 
 // Transpose of a bf16 [rows][cols] matrix (32 x 32 tiles through shared memory).
@@ -476,9 +484,9 @@ cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s) {
   cast_weights_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, s>>>(d.w1, n1, d.w2, d.members, d.hidden, d.w1h,
                                                                         d.w2h, d.w2t);
   if (d.w1_tiles && d.hidden % 256 == 0 && d.in % 32 == 0) {
-    tile_weights_kernel<<<static_cast<int>((n1 + 255) / 256), 256, 0, s>>>(
+    tile_weights_kernel<__nv_bfloat16><<<static_cast<int>((n1 + 255) / 256), 256, 0, s>>>(
         d.w1, static_cast<long long>(d.members) * d.hidden, d.in, d.w1_tiles);
-    tile_weights_kernel<<<static_cast<int>((n2 + 255) / 256), 256, 0, s>>>(
+    tile_weights_kernel<__half><<<static_cast<int>((n2 + 255) / 256), 256, 0, s>>>(
         d.w2, static_cast<long long>(d.members) * d.hidden, d.hidden, d.w2_tiles);
   }
   return cudaGetLastError();

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -16,12 +17,14 @@ __device__ __forceinline__ float MlpTanh(float u) {
   asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
   return t;
 }
+// u = z (c0 + c1 z^2) with c0 = sqrt(2/pi), c1 = 0.044715 c0; GELU = h + h tanh(u), h = z / 2.
 __device__ __forceinline__ float MlpGelu(float z) {
-  const float t = MlpTanh(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
-  return 0.5f * z * (1.0f + t);
+  const float t = MlpTanh(z * fmaf(z * z, 0.0356774081363001f, 0.7978845608028654f));
+  const float h = 0.5f * z;
+  return fmaf(h, t, h);
 }
 __device__ __forceinline__ float MlpGeluGrad(float z) {
-  const float t = MlpTanh(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
+  const float t = MlpTanh(z * fmaf(z * z, 0.0356774081363001f, 0.7978845608028654f));
   return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f, z * z, 1.0f);
 }
 #endif
@@ -32,11 +35,13 @@ struct MlpDev {
   int in, hidden, members;
   float *w1, *b1, *w2, *b2, *w3, *b3;
   __nv_bfloat16 *w1h, *w2h, *w2t;
-  // W1 and W2 again, cut into 256-row x 32-K blocks stored contiguously in the
-  // tensor cores' shared-memory operand layout (see mlp_tc.cu), so one bulk copy
-  // moves a block: member m, block c of W1 at (m * in / 32 + c) * 8192 elements,
-  // of W2 at (m * hidden / 32 + c) * 8192 elements.
-  __nv_bfloat16 *w1_tiles, *w2_tiles;
+  // W1 (bf16) and W2 (IEEE half: layer 2 of the tensor-core inference runs in
+  // f16) again, cut into 256-row x 32-K blocks stored contiguously in the tensor
+  // cores' shared-memory operand layout (see mlp_tc.cu), so one bulk copy moves a
+  // block: member m, block c of W1 at (m * in / 32 + c) * 8192 elements, of W2 at
+  // (m * hidden / 32 + c) * 8192 elements.
+  __nv_bfloat16 *w1_tiles;
+  __half *w2_tiles;
 };
 
 // Activations of one batch (sizes for batch B, M members, H hidden).

@@ -1,9 +1,9 @@
-// Fused ensemble inference of the BF16 barrier surrogate on the 5th-generation
+// Fused ensemble inference of the barrier surrogate on the 5th-generation
 // tensor cores (tcgen05): one persistent CTA per SM walks tiles of 128 samples.
 // Per tile and member m:
-//   D1 (TMEM, 128 x 256 fp32) = X (smem) . W1[m]^T            tcgen05.mma kind::f16
-//   H1 (smem, bf16)            = GELU(D1 + b1[m])              epilogue warps (tcgen05.ld)
-//   D2 (TMEM)                  = H1 . W2[m]^T
+//   D1 (TMEM, 128 x 256 fp32) = X (smem, bf16) . W1[m]^T (bf16)   tcgen05.mma kind::f16
+//   H1 (smem, IEEE half)       = GELU(D1 + b1[m])   epilogue warps (tcgen05.ld, packed half GELU)
+//   D2 (TMEM)                  = H1 . W2[m]^T (half)               tcgen05.mma kind::f16
 //   y_m                        = GELU(D2 + b2[m]) . w3[m] + b3[m]
 // then the ensemble mean and spread.
 //
@@ -13,7 +13,7 @@
 //              mbarrier) per weight block of 256 rows x 32 K (16 KB, pre-tiled in
 //              global memory) into a ring of kStages buffers;
 //   warp 1     one thread issues the MMAs and the tcgen05.commit arrivals;
-//   warps 2-9  epilogue: TMEM lane group = warp % 4, column half = (warp - 2) / 4.
+//   warps 2-17 epilogue: TMEM lane group = warp % 4, column quarter = (warp - 2) / 4.
 // The layer-1 MMAs of member m + 1 overlap the layer-2 epilogue of member m.
 //
 // Operand layout in shared memory (K-major, no swizzle): 8-row x 16-byte core
@@ -39,7 +39,8 @@ constexpr int kTcK = 32;         // K per operand tile / weight chunk
 constexpr int kTcTile = kTcRows * kTcK;           // elements of a 128 x 32 operand tile
 constexpr int kTcChunkElems = kTcHidden * kTcK;   // elements of a 256 x 32 weight chunk (16 KB)
 constexpr int kTcStages = 6;
-constexpr int kTcThreads = 320;  // 10 warps
+constexpr int kEpiWarps = 16;    // 4 per TMEM lane group, 64 columns each
+constexpr int kTcThreads = 64 + 32 * kEpiWarps;  // producer, MMA issuer, epilogue
 constexpr uint32_t kTmemCols = 512;
 constexpr int kMlpTimeout = 1;
 constexpr long long kWaitLimit = 1LL << 26;
@@ -55,14 +56,29 @@ __device__ __forceinline__ uint64_t OperandDesc(uint32_t addr) {
   return d;                                    // base offset 0, no swizzle
 }
 
-// kind::f16 instruction descriptor: D fp32, A and B bf16, both K-major, N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((kTcHidden >> 3) << 17) | ((kTcRows >> 4) << 24);
+// kind::f16 instruction descriptors: D fp32, both operands K-major, N = 256, M = 128;
+// layer 1 reads bf16 A and B (features, W1), layer 2 IEEE half A and B (H1, W2).
+constexpr uint32_t kIdescBf16 =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((kTcHidden >> 3) << 17) | ((kTcRows >> 4) << 24);
+constexpr uint32_t kIdescF16 = (1u << 4) | ((kTcHidden >> 3) << 17) | ((kTcRows >> 4) << 24);
 
-__device__ __forceinline__ void Mma(uint32_t tmem, uint64_t a, uint64_t b, bool accumulate) {
+__device__ __forceinline__ void Mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate ? 1 : 0));
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1 : 0));
+}
+
+// GELU of two values in packed half precision (layer-1 epilogue: H1 is stored in
+// half for the layer-2 MMA): u = z (c0 + c1 z^2), GELU = h + h tanh(u), h = z / 2.
+__device__ __forceinline__ __half2 GeluHalf2(__half2 z) {
+  const __half2 u = __hmul2(z, __hfma2(__hmul2(z, z), __float2half2_rn(0.0356774081363001f),
+                                       __float2half2_rn(0.7978845608028654f)));
+  uint32_t ub = *reinterpret_cast<const uint32_t *>(&u), tb;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(tb) : "r"(ub));
+  const __half2 t = *reinterpret_cast<const __half2 *>(&tb);
+  const __half2 h = __hmul2(z, __float2half2_rn(0.5f));
+  return __hfma2(h, t, h);
 }
 __device__ __forceinline__ void Commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(Smem(bar)));
@@ -118,17 +134,17 @@ __device__ __forceinline__ void CpAsyncWait() {
 }
 __device__ __forceinline__ void FenceAsyncSmem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// 32 consecutive fp32 columns of this thread's TMEM lane. The wait carries the
+// 32 registers as operands (no memory clobber), so the compiler keeps their uses
+// after it while still free to issue independent loads (biases) earlier.
 __device__ __forceinline__ void TmemLoad32(uint32_t addr, float *v) {
   uint32_t r[32];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(addr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
 #pragma unroll
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
@@ -143,7 +159,7 @@ struct TcBars {
   uint64_t x_full, x_empty, d1_full, d1_empty, h1_full, h1_empty, d2_full, d2_empty, part_full, part_empty, done;
   int abort;
   uint32_t tmem;
-  float partial[kTcRows];
+  float partial[3][kTcRows];  // column quarters 1-3 of each row's output dot product
 };
 
 }  // namespace
@@ -155,8 +171,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int K1 = d.in, members = d.members;
   const int k1_tiles = K1 / kTcK, k2_tiles = kTcHidden / kTcK;
   __nv_bfloat16 *sx = reinterpret_cast<__nv_bfloat16 *>(smem);         // k1_tiles x (128 x 32)
-  __nv_bfloat16 *sh = sx + kTcRows * K1;                                // 8 x (128 x 32)
-  __nv_bfloat16 *sw = sh + kTcRows * kTcHidden;                         // kStages x (256 x 32)
+  __nv_bfloat16 *sh = sx + kTcRows * K1;                                // 8 x (128 x 32), IEEE half H1
+  __nv_bfloat16 *sw = sh + kTcRows * kTcHidden;                         // kStages x (256 x 32), W1 bf16 / W2 half
   TcBars *bars = reinterpret_cast<TcBars *>(sw + kTcStages * kTcChunkElems);
   volatile int *abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -169,12 +185,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     BarInit(&bars->x_full, 32);
     BarInit(&bars->x_empty, 1);
     BarInit(&bars->d1_full, 1);
-    BarInit(&bars->d1_empty, 8);
-    BarInit(&bars->h1_full, 8);
+    BarInit(&bars->d1_empty, kEpiWarps);
+    BarInit(&bars->h1_full, kEpiWarps);
     BarInit(&bars->h1_empty, 1);
     BarInit(&bars->d2_full, 1);
-    BarInit(&bars->d2_empty, 8);
-    BarInit(&bars->part_full, 4);
+    BarInit(&bars->d2_empty, kEpiWarps);
+    BarInit(&bars->part_full, 3 * 4);
     BarInit(&bars->part_empty, 4);
     BarInit(&bars->done, 1);
     bars->abort = 0;
@@ -222,9 +238,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               stop = true;
               break;
             }
-            const __nv_bfloat16 *src =
-                c < k1_tiles ? d.w1_tiles + (static_cast<long long>(m) * k1_tiles + c) * kTcChunkElems
-                             : d.w2_tiles + (static_cast<long long>(m) * k2_tiles + (c - k1_tiles)) * kTcChunkElems;
+            const void *src =
+                c < k1_tiles
+                    ? static_cast<const void *>(d.w1_tiles + (static_cast<long long>(m) * k1_tiles + c) * kTcChunkElems)
+                    : static_cast<const void *>(d.w2_tiles +
+                                                (static_cast<long long>(m) * k2_tiles + (c - k1_tiles)) * kTcChunkElems);
             ArriveExpectTx(&bars->full[s], kTcChunkElems * 2);
             BulkCopy(sw + s * kTcChunkElems, src, kTcChunkElems * 2, &bars->full[s]);
           }
@@ -247,8 +265,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!(ok = Wait(&bars->full[s], (g / kTcStages) & 1, abort))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a = Smem(sx + c * kTcTile), b = Smem(sw + s * kTcChunkElems);
-            Mma(d1, OperandDesc(a), OperandDesc(b), c > 0);
-            Mma(d1, OperandDesc(a + 256), OperandDesc(b + 256), true);
+            Mma(d1, OperandDesc(a), OperandDesc(b), kIdescBf16, c > 0);
+            Mma(d1, OperandDesc(a + 256), OperandDesc(b + 256), kIdescBf16, true);
             Commit(&bars->empty[s]);
           }
           if (!ok) break;
@@ -261,8 +279,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!(ok = Wait(&bars->full[s], (g / kTcStages) & 1, abort))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a = Smem(sh + c * kTcTile), b = Smem(sw + s * kTcChunkElems);
-            Mma(d2, OperandDesc(a), OperandDesc(b), c > 0);
-            Mma(d2, OperandDesc(a + 256), OperandDesc(b + 256), true);
+            Mma(d2, OperandDesc(a), OperandDesc(b), kIdescF16, c > 0);
+            Mma(d2, OperandDesc(a + 256), OperandDesc(b + 256), kIdescF16, true);
             Commit(&bars->empty[s]);
           }
           if (!ok) break;
@@ -277,7 +295,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncwarp();
   } else {
     // ---- epilogue warps ----
-    const int ew = warp - 2, half = ew >> 2;
+    const int ew = warp - 2, quarter = ew >> 2;  // columns [64 quarter, 64 quarter + 64)
     const int row = (warp & 3) * 32 + lane;
     const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
     int u = 0;
@@ -287,15 +305,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int valid = static_cast<int>(n - r0 < kTcRows ? n - r0 : kTcRows);
       float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
       for (int m = 0; m < members && ok; ++m, ++u) {
-        // H1 = GELU(D1 + b1): this thread's row, columns [128 half, 128 half + 128)
+        // H1 = GELU(D1 + b1): this thread's row, its column quarter
         if (!(ok = Wait(&bars->d1_full, u & 1, abort))) break;
         if (u >= 1 && !(ok = Wait(&bars->h1_empty, (u - 1) & 1, abort))) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const float *b1 = d.b1 + m * kTcHidden;
 #pragma unroll 1
-        for (int j0 = 0; j0 < 128; j0 += 32) {
+        for (int j0 = 0; j0 < 64; j0 += 32) {
           float v[32];
-          const int col0 = half * 128 + j0;
+          const int col0 = quarter * 64 + j0;
           TmemLoad32(d1 + lane_base + col0, v);
 #pragma unroll
           for (int g8 = 0; g8 < 4; ++g8) {
@@ -306,8 +324,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t packed[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const __nv_bfloat162 p = __floats2bfloat162_rn(MlpGelu(v[g8 * 8 + 2 * e] + bias[2 * e]),
-                                                             MlpGelu(v[g8 * 8 + 2 * e + 1] + bias[2 * e + 1]));
+              const __half2 p = GeluHalf2(
+                  __floats2half2_rn(v[g8 * 8 + 2 * e] + bias[2 * e], v[g8 * 8 + 2 * e + 1] + bias[2 * e + 1]));
               packed[e] = *reinterpret_cast<const uint32_t *>(&p);
             }
             *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(sh) + TileOffset(kTcRows, row, col0 + g8 * 8)) =
@@ -327,9 +345,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const float *b2 = d.b2 + m * kTcHidden, *w3 = d.w3 + m * kTcHidden;
         float acc = 0.f;
 #pragma unroll 1
-        for (int j0 = 0; j0 < 128; j0 += 32) {
+        for (int j0 = 0; j0 < 64; j0 += 32) {
           float v[32];
-          const int col0 = half * 128 + j0;
+          const int col0 = quarter * 64 + j0;
           TmemLoad32(d2 + lane_base + col0, v);
 #pragma unroll
           for (int e = 0; e < 32; e += 4) {
@@ -342,16 +360,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
         if (lane == 0) Arrive(&bars->d2_empty);
-        // the two column halves of a row meet in shared memory: half 1 publishes
-        // (part_full), half 0 consumes and releases the slots (part_empty)
-        if (half == 1) {
+        // the four column quarters of a row meet in shared memory: quarters 1-3
+        // publish (part_full), quarter 0 consumes and releases the slots (part_empty)
+        if (quarter != 0) {
           if (u >= 1 && !(ok = Wait(&bars->part_empty, (u - 1) & 1, abort))) break;
-          bars->partial[row] = acc;
+          bars->partial[quarter - 1][row] = acc;
           __syncwarp();
           if (lane == 0) Arrive(&bars->part_full);
         } else {
           if (!(ok = Wait(&bars->part_full, u & 1, abort))) break;
-          const float y = acc + bars->partial[row] + __ldg(&d.b3[m]);
+          const float y = acc + (bars->partial[0][row] + bars->partial[1][row] + bars->partial[2][row]) +
+                          __ldg(&d.b3[m]);
           __syncwarp();
           if (lane == 0) Arrive(&bars->part_empty);
           ysum += y;
@@ -359,7 +378,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           ymax = fmaxf(ymax, y);
         }
       }
-      if (ok && half == 0 && row < valid) {
+      if (ok && quarter == 0 && row < valid) {
         mean[r0 + row] = mean_label + std_label * ysum / members;
         if (spread) spread[r0 + row] = std_label * (ymax - ymin);
       }

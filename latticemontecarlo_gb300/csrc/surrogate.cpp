@@ -146,7 +146,7 @@ int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_
     m->d.w2h = DevAlloc<__nv_bfloat16>(M * H * H, &m->owned);
     m->d.w2t = DevAlloc<__nv_bfloat16>(M * H * H, &m->owned);
     m->d.w1_tiles = DevAlloc<__nv_bfloat16>(M * H * in_features, &m->owned);
-    m->d.w2_tiles = DevAlloc<__nv_bfloat16>(M * H * H, &m->owned);
+    m->d.w2_tiles = DevAlloc<__half>(M * H * H, &m->owned);
     // He initialisation (normal, std sqrt(2 / fan_in)), zero biases
     std::vector<float> p(m->num_params, 0.f);
     std::mt19937_64 gen(seed);
