@@ -151,6 +151,11 @@ struct lmc_ctx {
     return st;
   }
   void ClearStatus() { CudaCheck(cudaMemsetAsync(status.p, 0, sizeof(int), stream), "status clear"); }
+  // Four pinned host words for status / count copies that stay asynchronous.
+  int *Pinned() {
+    if (!h_status) CudaCheck(cudaMallocHost(&h_status, 4 * sizeof(int)), "cudaMallocHost");
+    return h_status;
+  }
   void CheckReplica(int r) const {
     Require(r >= 0 && r < num_replicas, LMC_ERR_OUT_OF_RANGE, "replica index out of range");
   }
@@ -1396,13 +1401,15 @@ int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, 
     CudaCheck(lmc::LaunchFallbackMerge(ctx->s_mean.as<float>(), m, ctx->s_fb_ea.as<double>(), ctx->s_fb_index.as<int>(),
                                        d_count, ea_dev, ctx->stream),
               "merge kernel");
-    int count = 0, net_status = 0;
-    CudaCheck(cudaMemcpyAsync(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    CudaCheck(cudaMemcpyAsync(&net_status, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
-              "D2H");
+    // one host round trip: fallback count, network status and kernel status into pinned words
+    int *h = ctx->Pinned();
+    CudaCheck(cudaMemcpyAsync(h, d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(h + 1, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(h + 2, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     ctx->Sync();
+    const int count = h[0], net_status = h[1], st = h[2];
     Require(net_status == 0, LMC_ERR_STOPPED, "surrogate inference: a tensor-core wait expired");
-    RaiseStatus(ctx->ReadStatus(), "surrogate barriers");
+    RaiseStatus(st, "surrogate barriers");
     if (num_fallback) *num_fallback = count;
   });
 }
@@ -1631,7 +1638,7 @@ int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches) {
       k += sizeof(species);
       std::memcpy(k, &launches, sizeof(launches));
     }
-    if (!ctx->h_status) CudaCheck(cudaMallocHost(&ctx->h_status, sizeof(int)), "cudaMallocHost");
+    ctx->Pinned();
     if (!ctx->kmc_graph || key != ctx->kmc_graph_key) {
       if (ctx->kmc_graph) CudaCheck(cudaGraphExecDestroy(ctx->kmc_graph), "cudaGraphExecDestroy");
       ctx->kmc_graph = nullptr;

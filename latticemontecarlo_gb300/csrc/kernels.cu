@@ -82,6 +82,13 @@ __device__ __forceinline__ int MinImage(int d, int n) {
   return d;
 }
 
+// Minimum image of a coordinate difference d in (-2n, 2n) (half units).
+__device__ __forceinline__ int WrapDelta(int d, int n) {
+  d += d < -n ? 2 * n : 0;
+  d -= d >= n ? 2 * n : 0;
+  return d;
+}
+
 // Direction index of a half-unit offset via the host-built 27-entry table
 // ((dx+1)*9 + (dy+1)*3 + (dz+1) -> index of the 1NN offset, -1 otherwise).
 __device__ __forceinline__ int DirIndex(const int8_t *dir_of, int dx, int dy, int dz) {
@@ -808,7 +815,78 @@ __global__ void surrogate_dataset_kernel(DevTables t, SurrogateGen g) {
   if (bad_all && lane == 0) atomicOr(g.status, static_cast<int>(bad_all));
 }
 
-// Features of lattice jumps (pairs first -> second), one warp per pair.
+// Features of lattice jumps, one thread per pair (alphabet size kEh known at
+// compile time): the 58 MMM-ordered sites are gathered with independent loads
+// and the row of in_pad bf16 values (a multiple of 8, 16-byte aligned) is
+// written as 16-byte stores, 8 features at a time. Same values as the warp
+// kernel below, which serves other row layouts.
+template <int kEh>
+__global__ void __launch_bounds__(256) surrogate_features_thread_kernel(
+    DevTables t, const int8_t *__restrict__ species, int n, const long long *__restrict__ pairs, int m, int in_pad,
+    __nv_bfloat16 *features, int *status) {
+  __shared__ int8_t s_off[12 * kEnvSites * 4];
+  __shared__ int8_t s_rank[8];
+  __shared__ int8_t s_dir_of[27];
+  StageArray(t.mmm_off, s_off, 12 * kEnvSites * 4);
+  if (threadIdx.x < 8) s_rank[threadIdx.x] = t.onehot_rank[threadIdx.x];
+  if (threadIdx.x < 27) s_dir_of[threadIdx.x] = t.dir_of[threadIdx.x];
+  __syncthreads();
+  const long long nsites = 4LL * n * n * n;
+  unsigned bad_all = 0;
+  for (long long p = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; p < m;
+       p += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long a = pairs[2 * p], b = pairs[2 * p + 1];
+    unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
+    int di = -1;
+    H3 hi{0, 0, 0};
+    if (!bad) {
+      hi = SiteCoord(a, n);
+      const H3 hj = SiteCoord(b, n);
+      const int dx = WrapDelta(hj.x - hi.x, n), dy = WrapDelta(hj.y - hi.y, n), dz = WrapDelta(hj.z - hi.z, n);
+      if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
+        di = s_dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)];
+      if (di < 0) bad = kStatusNotNeighbor;
+    }
+    bad_all |= bad;
+    int8_t rk[kEnvSites + 1];
+    if (!bad) {
+      const int8_t *o = s_off + di * kEnvSites * 4;
+#pragma unroll
+      for (int k = 0; k < kEnvSites; ++k) rk[k] = species[NeighborId(hi, o[4 * k], o[4 * k + 1], o[4 * k + 2], n)];
+      rk[kEnvSites] = species[b];
+#pragma unroll
+      for (int k = 0; k <= kEnvSites; ++k) rk[k] = s_rank[rk[k]];
+    } else {
+#pragma unroll
+      for (int k = 0; k <= kEnvSites; ++k) rk[k] = kMaxOnehot - 1;  // matches no rank: a zero row
+    }
+    uint4 *row = reinterpret_cast<uint4 *>(features + p * in_pad);
+    constexpr int kFeat = (kEnvSites + 1) * kEh;
+#pragma unroll
+    for (int c = 0; c < (kFeat + 7) / 8; ++c) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int idx = 8 * c + 2 * e + h;
+          if (idx < kFeat && rk[idx / kEh] == idx % kEh) word |= h ? 0x3F800000u : 0x3F80u;  // bf16 1.0
+        }
+        w[e] = word;
+      }
+      row[c] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    for (int c = (kFeat + 7) / 8; c < in_pad / 8; ++c) row[c] = make_uint4(0, 0, 0, 0);
+  }
+  if (bad_all) atomicOr(status, static_cast<int>(bad_all));
+}
+
+// Features of lattice jumps (pairs first -> second), one warp per pair. The
+// direction is found among the 12 neighbours of the first site (lanes 0-11),
+// the 58 MMM-ordered sites are gathered into shared memory, and lane l writes
+// features [8 l, 8 l + 8) as one 16-byte store (rows of a multiple of 8 values,
+// 16-byte aligned; other layouts take the scalar writer).
 __global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict__ species, int n,
                                           const long long *__restrict__ pairs, int m, int in_pad,
                                           __nv_bfloat16 *features, int *status) {
@@ -819,25 +897,63 @@ __global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict_
   __syncthreads();
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int8_t *rm = arr + warp * 64;
+  int8_t *rm = arr + warp * 64;  // [0, 58) environment ranks, [58] migrant rank, [59] padding (never matches)
+  const int eh = t.num_onehot;
+  const long long nsites = 4LL * n * n * n;
+  const bool vec = (in_pad % 8) == 0 && (reinterpret_cast<uintptr_t>(features) & 15) == 0 && in_pad <= 256;
+  // this lane's 8 features: (source slot in rm, one-hot rank)
+  int src[8], rk[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int idx = 8 * lane + j;
+    const int site = idx / eh;
+    src[j] = idx < (kEnvSites + 1) * eh ? site : kEnvSites + 1;
+    rk[j] = idx - site * eh;
+  }
+  const int8_t *dirs = t.dir;
   unsigned bad_all = 0;
   for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
-    H3 hi, hj;
-    int di = -1, db = -1;
-    const unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
-    int mig_rank = kMaxOnehot - 1;
+    const long long a = pairs[2 * p], b = pairs[2 * p + 1];
+    unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
+    int di = -1;
+    H3 hi{0, 0, 0};
+    if (!bad) {
+      hi = SiteCoord(a, n);
+      bool hit = false;
+      if (lane < 12) {
+        const int8_t *o = dirs + lane * 4;
+        hit = NeighborId(hi, o[0], o[1], o[2], n) == b;
+      }
+      const unsigned mk = __ballot_sync(0xffffffffu, hit);
+      di = mk ? __ffs(mk) - 1 : -1;
+      if (di < 0) bad = kStatusNotNeighbor;
+    }
     if (!bad) {
       for (int k = lane; k < kEnvSites; k += 32) {
-        const int8_t *a = t.mmm_off + (di * kEnvSites + k) * 4;
-        rm[k] = sm->rank[species[NeighborId(hi, a[0], a[1], a[2], n)]];
+        const int8_t *o = t.mmm_off + (di * kEnvSites + k) * 4;
+        rm[k] = sm->rank[species[NeighborId(hi, o[0], o[1], o[2], n)]];
       }
-      mig_rank = sm->rank[species[pairs[2 * p + 1]]];
+      if (lane == 0) rm[kEnvSites] = sm->rank[species[b]];
     } else {
-      for (int k = lane; k < kEnvSites; k += 32) rm[k] = kMaxOnehot - 1;
+      for (int k = lane; k <= kEnvSites; k += 32) rm[k] = kMaxOnehot - 1;
     }
+    if (lane == 0) rm[kEnvSites + 1] = -1;
     bad_all |= bad;
     __syncwarp();
-    WriteFeatures(rm, mig_rank, t.num_onehot, in_pad, features + static_cast<long long>(p) * in_pad, lane);
+    __nv_bfloat16 *row = features + static_cast<long long>(p) * in_pad;
+    if (vec) {
+      if (8 * lane < in_pad) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const bool lo = rm[src[2 * e]] == rk[2 * e], hi2 = rm[src[2 * e + 1]] == rk[2 * e + 1];
+          w[e] = (lo ? 0x3F80u : 0u) | (hi2 ? 0x3F800000u : 0u);  // bf16 1.0 in the low / high half
+        }
+        *reinterpret_cast<uint4 *>(row + 8 * lane) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    } else {
+      WriteFeatures(rm, rm[kEnvSites], eh, in_pad, row, lane);
+    }
     __syncwarp();
   }
   if (bad_all && lane == 0) atomicOr(status, static_cast<int>(bad_all));
@@ -1487,13 +1603,6 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
 //     one of the two changed sites are marked for step 1.
 // The oracle restates exactly these operations (orc_kmc_multi).
 // ---------------------------------------------------------------------------
-// Minimum image of a coordinate difference d in (-2n, 2n) (half units).
-__device__ __forceinline__ int WrapDelta(int d, int n) {
-  d += d < -n ? 2 * n : 0;
-  d -= d >= n ? 2 * n : 0;
-  return d;
-}
-
 __device__ __forceinline__ bool InLocal(const uint32_t *bits, int dx, int dy, int dz) {
   if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) return false;
   const int b = ((dx + 4) * kLocalSpan + (dy + 4)) * kLocalSpan + (dz + 4);
@@ -2112,6 +2221,16 @@ cudaError_t LaunchSurrogateFeatures(const DevTables &t, const int8_t *species, i
                                     int in_pad, __nv_bfloat16 *features, int *status, cudaStream_t stream) {
   if (m <= 0) return cudaSuccess;
   if (in_pad < (kEnvSites + 1) * t.num_onehot) return cudaErrorInvalidValue;
+  if (in_pad % 8 == 0 && (reinterpret_cast<uintptr_t>(features) & 15) == 0) {
+    const int blocks = static_cast<int>((m + 255) / 256);
+    switch (t.num_onehot) {
+      case 2: surrogate_features_thread_kernel<2><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
+      case 3: surrogate_features_thread_kernel<3><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
+      case 4: surrogate_features_thread_kernel<4><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
+      case 5: surrogate_features_thread_kernel<5><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
+      default: break;
+    }
+  }
   const size_t sm = sizeof(SmallTables) + kJumpWarps * 64;
   surrogate_features_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, in_pad,
                                                                                   features, status);

@@ -130,3 +130,51 @@ def test_tcgen05_inference(setup):
     y = R.predict(net.params(), R.bf16_bits_to_float(_bits(xs)), nin, 256, 4)
     mu, sd = float(np.float32(float(ea.mean()))), float(np.float32(float(ea.std())))
     np.testing.assert_allclose(m_tc, mu + sd * y.mean(0), rtol=0, atol=3e-3)
+
+
+@pytest.mark.parametrize("elements,pad", [(("Al", "Mg", "Zn"), 192), (("Al", "Mg", "Zn"), 180),
+                                          (("Al", "Cu", "Mg", "Zn"), 256), (("Al", "Cu", "Mg", "Zn"), 244)])
+def test_lattice_features_match_host_lists(native, elements, pad):
+    """Features of lattice jumps (both the thread-per-pair writer, rows of a
+    multiple of 8, and the warp writer) against the one-hot encoding built on the
+    host from the reference-pinned MMM site order."""
+    torch = pytest.importorskip("torch")
+    from latticemontecarlo_gb300 import api, synthetic as S
+    N = native
+    coeffs = S.make_coefficients(elements, 3)
+    n = 9
+    fr = {e: 1.0 / len(elements) for e in elements}
+    sp = S.make_lattice(n, fr, 5, 8, elements)
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(elements)))
+    ctx.set_lattices([n], sp)
+    rng = np.random.default_rng(1)
+    alpha = S.alphabet(elements)
+    rank = {c: (i if i < alpha.index("X") else i - 1) for i, c in enumerate(range(len(alpha))) if alpha[c] != "X"}
+    eh = len(elements)
+    m = 300
+    a = rng.integers(0, sp.size, m)
+    pairs = np.zeros((m, 2), np.int64)
+    for i in range(m):
+        nb = np.zeros(42, np.int64)
+        N.check(N.lib.lmc_geom_neighbors(n, int(a[i]), nb.ctypes.data_as(C.POINTER(C.c_int64))))
+        pairs[i] = (a[i], nb[rng.integers(0, 12)])
+    pd = torch.from_numpy(pairs).cuda()
+    out = torch.full((m, pad), 7, dtype=torch.int16, device="cuda")
+    N.check(N.lib.lmc_surrogate_features(ctx._h, 0, C.c_void_p(pd.data_ptr()), m, pad, C.c_void_p(out.data_ptr())))
+    got = out.cpu().numpy().view(np.uint16)
+    for i in range(m):
+        st, mmm, mm2 = np.zeros(60, np.int64), np.zeros(58, np.int64), np.zeros(58, np.int64)
+        N.check(N.lib.lmc_geom_pair_lists(n, int(pairs[i, 0]), int(pairs[i, 1]),
+                                          st.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          mmm.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          mm2.ctypes.data_as(C.POINTER(C.c_int64))))
+        want = np.zeros(pad, np.uint16)
+        for k, site in enumerate(list(mmm) + [pairs[i, 1]]):
+            c = int(sp[site])
+            if alpha[c] != "X":
+                want[k * eh + rank[c]] = 0x3F80  # bf16 1.0
+        assert np.array_equal(got[i], want), i
+    bad = torch.tensor([[0, 5]], dtype=torch.int64, device="cuda")  # not a 1NN pair
+    with pytest.raises(N.LmcError):
+        N.check(N.lib.lmc_surrogate_features(ctx._h, 0, C.c_void_p(bad.data_ptr()), 1, pad,
+                                             C.c_void_p(out.data_ptr())))
