@@ -263,6 +263,11 @@ typedef struct lmc_kmc_options {
   int early_stop;          /* IsEscaped (KineticMcAbstract.cpp:192-223): a replica whose vacancy has only
                               solvent (its most frequent element) in the 1-3NN shells completes that step
                               and takes no further steps */
+  int chain;               /* 1: second-order residence-time KMC of KineticMcChainOmpi
+                              (KineticMcChainOmpi.cpp:56-152): per step the 12 x 12 jumps after each
+                              first jump, deterministic second-order time, one uniform draw for the
+                              selection; one block of 12 warps per replica. Not combined with early_stop,
+                              lmc_kmc_run_graph or lmc_kmc_autotune; no events12 output. */
 } lmc_kmc_options;
 
 /* Jump evaluation inside the KMC kernel: both give bit-identical barriers.

@@ -91,7 +91,7 @@ struct lmc_ctx {
   bool kmc_ready{false};
   lmc_kmc_options kmc_opt{};
   DevBuf k_vac, k_steps, k_time, k_energy, k_temp, k_cvac, k_csol, k_rng, k_trace, k_events, k_tt_time, k_tt_temp;
-  DevBuf k_solvent, k_escaped, c_trace;
+  DevBuf k_solvent, k_escaped, k_prev, c_trace;
   DevBuf s_feat, s_mean, s_spread, s_fb_pairs, s_fb_index, s_fb_ea, s_fb_de;
   int tt_len{0};
   // sparse KMC tables (built for the dominant species at lmc_kmc_init)
@@ -120,7 +120,7 @@ struct lmc_ctx {
     for (auto &b : tables) b.Free();
     for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
-                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &c_trace, &s_feat, &s_mean, &s_spread,
+                      &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &k_prev, &c_trace, &s_feat, &s_mean, &s_spread,
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace})
@@ -649,6 +649,7 @@ lmc::KmcDevState KmcState(const lmc_ctx *ctx) {
   s.tt_time = ctx->tt_len ? ctx->k_tt_time.as<double>() : nullptr;
   s.tt_temp = ctx->tt_len ? ctx->k_tt_temp.as<double>() : nullptr;
   s.tt_len = ctx->tt_len;
+  s.prev = ctx->k_prev.as<long long>();
   return s;
 }
 // ---- KMC launch-shape autotuner -------------------------------------------
@@ -1455,8 +1456,10 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     ctx->k_cvac.Ensure(sizeof(double) * R);
     ctx->k_csol.Ensure(sizeof(double) * R);
     ctx->k_rng.Ensure(sizeof(uint32_t) * lmc::kRngWords * R);
+    Require(!(opt->chain && opt->early_stop), LMC_ERR_UNSUPPORTED, "the chain KMC has no early stop");
     ctx->k_solvent.Ensure(R);
     ctx->k_escaped.Ensure(R);
+    ctx->k_prev.Ensure(sizeof(long long) * R);
     CudaCheck(cudaMemsetAsync(ctx->k_escaped.p, 0, R, ctx->stream), "memset");
     // first vacancy and species histogram of every replica
     DevBuf hist;
@@ -1477,6 +1480,14 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     hist.Free();
     for (int r = 0; r < R; ++r)
       Require(first[r] != std::numeric_limits<long long>::max(), LMC_ERR_INVALID_ARGUMENT, "vacancy not found");
+    {
+      // previous_j_lattice_id_ of the chain KMC: the first (lowest-id) 1NN of the initial vacancy
+      // (KineticMcAbstract.cpp:255)
+      std::vector<long long> prev(R);
+      for (int r = 0; r < R; ++r) prev[r] = lmc::SortedNeighbors(lmc::Fcc{ctx->n[r]}, first[r], 1).front();
+      CudaCheck(cudaMemcpyAsync(ctx->k_prev.p, prev.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      ctx->Sync();
+    }
     // dominant species with a one-hot slot: the base of the sparse evaluation
     {
       std::vector<unsigned long long> tot(ctx->fm.num_species, 0);
@@ -1595,8 +1606,12 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
     l.stop_flag = ctx->d_stop;
     l.status = ctx->status.as<int>();
     ctx->ClearStatus();
+    Require(!(ctx->kmc_opt.chain && events12), LMC_ERR_UNSUPPORTED, "the chain KMC has no events12 output");
     CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
-    CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");
+    if (ctx->kmc_opt.chain)
+      CudaCheck(lmc::LaunchKmcChain(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "chain KMC kernel");
+    else
+      CudaCheck(lmc::LaunchKmc(ctx->t, ctx->species.as<int8_t>(), s, l, ctx->stream), "KMC kernel");
     CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
     if (trace)
       CudaCheck(cudaMemcpyAsync(trace, l.trace, sizeof(lmc::KmcTraceRec) * steps, cudaMemcpyDeviceToHost, ctx->stream),
@@ -1616,6 +1631,7 @@ int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches) {
   return Guard([&] {
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
     Require(steps_per_launch > 0 && launches > 0, LMC_ERR_INVALID_ARGUMENT, "steps_per_launch and launches must be > 0");
+    Require(!ctx->kmc_opt.chain, LMC_ERR_UNSUPPORTED, "graph runs cover the first-order KMC");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     const lmc::KmcDevState s = KmcState(ctx);
     lmc::KmcLaunch l = KmcShape(ctx);
@@ -1678,6 +1694,7 @@ int lmc_kmc_autotune(lmc_ctx *ctx, uint64_t probe_steps, const char *cache_path,
   return Guard([&] {
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
     Require(probe_steps > 0, LMC_ERR_INVALID_ARGUMENT, "probe_steps must be > 0");
+    Require(!ctx->kmc_opt.chain, LMC_ERR_UNSUPPORTED, "the chain KMC has a fixed launch shape");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     const std::string key = KmcTuneKey(ctx);
     std::map<std::string, KmcTuneEntry> cache;

@@ -1583,6 +1583,287 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
 }
 
 // ---------------------------------------------------------------------------
+// K4c: second-order "chain" KMC (KineticMcChainOmpi.cpp:56-152): one block of 12
+// warps per replica. Per step, warp d takes the neighbour i = k + dir[d] of the
+// vacancy k, builds the neighbourhood of i as it is after the jump k -> i (the
+// vacancy at i, the migrant at k) and evaluates the 12 jumps i -> l (the same
+// sparse / dense evaluation as kmc_kernel): their rate sum and the barrier and
+// energy change of i -> k. Warp 0 then forms, in the id order of the 12
+// neighbours, the reverse events k -> i (barrier Ea(i->k) - dE(i->k), energy
+// change -dE(i->k)), their rates and the second-order probabilities and time of
+// KineticMcChainOmpi::CalculateTime (sums sequential in that order), draws one
+// uniform (the time is deterministic), selects and moves the vacancy.
+// ---------------------------------------------------------------------------
+struct ChainShared {
+  double total_i[kChainWarps];  // per direction: rate sum of the 12 jumps out of i
+  double ea_ik[kChainWarps], de_ik[kChainWarps];
+  long long id_i[kChainWarps];
+  int opp[kChainWarps];  // local index of -dir[d] (where the migrant lands)
+  int sel_dir;
+  int stop;
+};
+
+size_t ChainSharedBytes(const DevTables &t, bool sparse) {
+  KmcLaunch l{};
+  l.warps_per_replica = 1;
+  l.replicas_per_block = kChainWarps;
+  l.sparse = sparse ? 1 : 0;
+  size_t b = KmcSharedBytes(t, l);
+  if (!sparse) b += 4 * 12 * 136 + 4 * 2 * (kTriEnv + 1) + 4 * kLocalSites * kInterWords + 2 * (kTriState + 1);
+  b = (b + 15) & ~size_t(15);
+  return b + ((sizeof(ChainShared) + 15) & ~size_t(15));
+}
+
+template <bool kSparse>
+__global__ void __launch_bounds__(kChainWarps * 32, 2)
+    kmc_chain_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcDevState s,
+                     const __grid_constant__ KmcLaunch l) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const KmcSmem sm = CarveKmcSmem(t, smem, kChainWarps, 1);
+  ChainShared *cs = reinterpret_cast<ChainShared *>((reinterpret_cast<size_t>(sm.end) + 15) & ~size_t(15));
+  const int r = blockIdx.x;
+  if (r >= s.num_replicas) return;  // block-uniform, before any barrier
+  StageKmcSmem(t, l.sp, sm, kSparse);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // local index of the offset opposite to each direction
+  {
+    const int8_t *o = t.dir + warp * 4;
+    __syncthreads();
+    int found = -1;
+    for (int k = lane; k < kLocalSites; k += 32) {
+      const int8_t *q = sm.loff + k * 4;
+      if (q[0] == -o[0] && q[1] == -o[1] && q[2] == -o[2]) found = k;
+    }
+    found = __reduce_max_sync(0xffffffffu, found);
+    if (lane == 0) cs->opp[warp] = found;
+  }
+  const ExpConsts ec{sm.exp, t.exp_l1, t.exp_l2};
+  KmcShared &rs = sm.rep[warp];
+  int8_t *st = sm.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const int n = s.lat_n[r];
+  int8_t *lat = species + s.lat_off[r];
+  const int center = sm.lst[t.pos_first];
+  long long vac = s.vacancy[r], prev = s.prev[r];
+  const bool leader = warp == 0 && lane == 0;
+  unsigned bad_all = 0;
+  double time = 0, energy = 0;
+  unsigned long long step0 = s.steps[r], steps_done = 0;
+  if (leader) {
+    time = s.time[r];
+    energy = s.energy[r];
+  }
+  uint32_t key0 = 0, key1 = 0;
+  if (s.rng_kind != 0) {
+    key0 = s.rng[r * kRngWords];
+    key1 = s.rng[r * kRngWords + 1];
+  }
+  double u_blk = 0.0;
+  Mt mt{nullptr, nullptr};
+  if (s.rng_kind == 0) {
+    uint32_t *w = s.rng + static_cast<long long>(r) * kRngWords;
+    mt.mt = reinterpret_cast<unsigned long long *>(w);
+    mt.idx = w + 2 * 312;
+  }
+  if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &sm.rep[0].beta, &sm.rep[0].corr);
+  __syncthreads();
+  H3 hk = SiteCoord(vac, n);
+  for (unsigned long long it = 0; it < l.steps; ++it) {
+    if (leader) {
+      if (s.tt_len > 0)
+        TemperatureFactors(s, r, InterpT(s.tt_time, s.tt_temp, s.tt_len, time), &sm.rep[0].beta, &sm.rep[0].corr);
+      cs->stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
+    }
+    __syncthreads();
+    if (cs->stop) {
+      bad_all |= kStatusStopped;
+      break;
+    }
+    const double beta = sm.rep[0].beta;
+    // ---- phase 1: warp d, the configuration after the jump k -> i ----
+    {
+      const int8_t *o = t.dir + warp * 4;
+      const H3 hi = WrapCoord(hk, o[0], o[1], o[2], n);
+      const long long id_i = NeighborId(hk, o[0], o[1], o[2], n);
+      const int8_t mig = lat[id_i];
+      for (int k = lane; k < kLocalSites; k += 32) {
+        const int8_t *q = sm.loff + k * 4;
+        rs.local[k] = lat[NeighborId(hi, q[0], q[1], q[2], n)];
+      }
+      __syncwarp();
+      if (lane == 0) {
+        rs.local[center] = static_cast<int8_t>(t.x_code);
+        rs.local[cs->opp[warp]] = mig;
+      }
+      if (lane < 12) {
+        const int8_t *q = t.dir + lane * 4;
+        rs.ids[lane] = NeighborId(hi, q[0], q[1], q[2], n);
+      }
+      __syncwarp();
+      bool sparse_v = false;
+      if (kSparse) {
+        SparseList(rs, sm.inter, l.sp, lane);
+        __syncwarp();
+        sparse_v = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
+      }
+      if (sparse_v) {
+        bad_all |= SparseItem(t, l.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, s.barrier_kind, lane);
+      } else {
+        const DenseArgs da{sm.lst, sm.lmmm, sm.lmm2f, sm.lmm2b, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb};
+        bad_all |= DenseJumpsCold(t, rs, da, s.barrier_kind, 0, 1, lane);
+      }
+      __syncwarp();
+      double ea = 0, de = 0, k = 0;
+      long long id = 0x7fffffffffffffffLL;
+      if (lane < 12) {
+        const int slot = rs.slot[lane];
+        id = rs.ids[lane];
+        if (slot >= 0) {
+          const JumpOut jo = JumpEpilogue(t, ec, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+          ea = jo.ea;
+          de = jo.de;
+          k = ExpFast(-ea * beta, ec);
+        } else if (slot == -1) {
+          bad_all |= kStatusNoCoefficients;
+        }
+      }
+      // rate sum in id order (sequential), and the jump back to k
+      int rank = 0;
+      for (int q = 0; q < 12; ++q) {
+        const long long oid = __shfl_sync(0xffffffffu, id, q);
+        rank += (q != lane) && (oid < id);
+      }
+      int src = 0;
+      for (int q = 0; q < 12; ++q)
+        if (__shfl_sync(0xffffffffu, rank, q) == lane) src = q;
+      const double k_s = __shfl_sync(0xffffffffu, k, src);
+      double total = 0.0;
+      for (int q = 0; q < 12; ++q) total += __shfl_sync(0xffffffffu, k_s, q);
+      const unsigned back = __ballot_sync(0xffffffffu, lane < 12 && id == vac);
+      const int bl = back ? __ffs(back) - 1 : 0;
+      const double ea_ik = __shfl_sync(0xffffffffu, ea, bl), de_ik = __shfl_sync(0xffffffffu, de, bl);
+      if (lane == 0) {
+        cs->total_i[warp] = total;
+        cs->ea_ik[warp] = ea_ik;
+        cs->de_ik[warp] = de_ik;
+        cs->id_i[warp] = id_i;
+      }
+    }
+    __syncthreads();
+    // ---- phase 2: second-order probabilities and time, selection, move (warp 0) ----
+    if (warp == 0) {
+      // lane q holds the neighbour of rank q in id order
+      long long idd = lane < 12 ? cs->id_i[lane] : 0x7fffffffffffffffLL;
+      int rank = 0;
+      for (int q = 0; q < 12; ++q) {
+        const long long oid = __shfl_sync(0xffffffffu, idd, q);
+        rank += (q != lane) && (oid < idd);
+      }
+      int src = 0;
+      for (int q = 0; q < 12; ++q)
+        if (__shfl_sync(0xffffffffu, rank, q) == lane) src = q;
+      const int d = lane < 12 ? src : 0;
+      const long long id_i = cs->id_i[d];
+      const double tot_i = cs->total_i[d];
+      const double barrier_ki = cs->ea_ik[d] - cs->de_ik[d];  // JumpEvent::GetReverseJumpEvent
+      const double de_ki = -cs->de_ik[d];
+      const double rate_ki = lane < 12 ? ExpFast(-barrier_ki * beta, ec) : 0.0;
+      const double back_ki = lane < 12 ? ExpFast((de_ki - barrier_ki) * beta, ec) : 0.0;
+      double total_k = 0.0;
+      for (int q = 0; q < 12; ++q) total_k += __shfl_sync(0xffffffffu, rate_ki, q);
+      const double t_1 = 1 / total_k / kPrefactor;
+      const double p_ki = rate_ki / total_k;
+      const double p_ik = lane < 12 ? back_ki / tot_i : 0.0;
+      const double bb = p_ki * p_ik, bk = p_ki * (1 - p_ik);
+      const bool is_prev = lane < 12 && id_i == prev;
+      const double t_i = lane < 12 ? 1 / tot_i / kPrefactor : 0.0;
+      double beta_bar_k = 0, beta_k = 0, gamma_bar_k_j = 0, gamma_k_j = 0, beta_k_j = 0, alpha_k_j = 0, ts_num = 0,
+             ts_j_num = 0;
+      for (int q = 0; q < 12; ++q) {
+        const double bbq = __shfl_sync(0xffffffffu, bb, q), bkq = __shfl_sync(0xffffffffu, bk, q);
+        const double pq = __shfl_sync(0xffffffffu, p_ki, q), tq = __shfl_sync(0xffffffffu, t_i, q);
+        const bool prq = __shfl_sync(0xffffffffu, is_prev ? 1 : 0, q) != 0;
+        beta_bar_k += bbq;
+        beta_k += bkq;
+        gamma_bar_k_j += prq ? 0.0 : bbq;
+        gamma_k_j += prq ? 0.0 : bkq;
+        beta_k_j += prq ? bkq : 0.0;
+        alpha_k_j += prq ? pq : 0.0;
+        ts_num += (t_1 + tq) * bbq;
+        ts_j_num += prq ? 0.0 : (t_1 + tq) * bbq;
+      }
+      const double ts = ts_num / beta_bar_k;
+      const double ts_j = ts_j_num / gamma_bar_k_j;
+      const double one_over = 1 / (1 - alpha_k_j);
+      const double t_2 = one_over * (gamma_k_j * t_1 + gamma_bar_k_j * (ts_j + t_1 + beta_bar_k / beta_k * ts));
+      const double pr = is_prev ? one_over * (gamma_bar_k_j / beta_k) * beta_k_j
+                                : one_over * (1 + gamma_bar_k_j / beta_k) * bk;
+      double cum = 0.0, mycum = 0.0;
+      for (int q = 0; q < 12; ++q) {
+        cum += __shfl_sync(0xffffffffu, pr, q);
+        if (lane == q) mycum = cum;
+      }
+      double u = 0.0;
+      if (s.rng_kind == 0) {
+        if (lane == 0) u = MtUniform(mt);
+        u = __shfl_sync(0xffffffffu, u, 0);
+      } else {
+        if ((it & 31) == 0) {
+          const unsigned long long ctr = step0 + it + lane;
+          const uint4 x = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                        static_cast<uint32_t>(r), 0x4b4d43u, key0, key1);
+          u_blk = U01(x.z, x.w);
+        }
+        u = __shfl_sync(0xffffffffu, u_blk, static_cast<int>(it & 31));
+      }
+      const unsigned hit = __ballot_sync(0xffffffffu, lane < 12 && !(mycum < u));
+      const int sel = hit ? __ffs(hit) - 1 : 11;
+      const int sel_dir = __shfl_sync(0xffffffffu, d, sel);
+      const long long tgt = __shfl_sync(0xffffffffu, id_i, sel);
+      const double b_sel = __shfl_sync(0xffffffffu, barrier_ki, sel), de_sel = __shfl_sync(0xffffffffu, de_ki, sel);
+      const double tot_sel = total_k;
+      if (lane == 0) {
+        if (!(total_k > 0.0) || !isfinite(total_k) || !isfinite(t_2) || !(t_2 >= 0.0)) bad_all |= kStatusNumeric;
+        time += t_2 * sm.rep[0].corr;
+        energy += de_sel;
+        lat[vac] = lat[tgt];
+        lat[tgt] = static_cast<int8_t>(t.x_code);
+        if (r == l.trace_replica && l.trace) {
+          KmcTraceRec rec;
+          rec.vacancy = vac;
+          rec.target = tgt;
+          rec.selected = sel;
+          rec.slot = 0;
+          rec.ea = b_sel;
+          rec.de = de_sel;
+          rec.total_rate = tot_sel;
+          rec.time = time;
+          rec.energy = energy;
+          l.trace[it] = rec;
+        }
+        cs->sel_dir = sel_dir;
+      }
+    }
+    __syncthreads();
+    {
+      const int8_t *o = t.dir + cs->sel_dir * 4;
+      prev = vac;
+      vac = NeighborId(hk, o[0], o[1], o[2], n);
+      hk = WrapCoord(hk, o[0], o[1], o[2], n);
+    }
+    ++steps_done;
+  }
+  if (leader) {
+    s.vacancy[r] = vac;
+    s.prev[r] = prev;
+    s.time[r] = time;
+    s.energy[r] = energy;
+    s.steps[r] = step0 + steps_done;
+  }
+  if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
 // K4b: multi-vacancy KMC, one block of kMultiWarps warps per lattice.
 // Every vacancy of the lattice is tracked (slots 0..V-1). Per step:
 //  1. the warps re-evaluate the 12 events of each vacancy whose 135-site
@@ -2366,6 +2647,18 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
     if (err != cudaSuccess) return err;
   }
   kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  return cudaGetLastError();
+}
+
+size_t KmcChainSharedBytes(const DevTables &t, bool sparse) { return ChainSharedBytes(t, sparse); }
+
+cudaError_t LaunchKmcChain(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
+                           cudaStream_t stream) {
+  const size_t sm = ChainSharedBytes(t, l.sparse != 0);
+  auto kern = l.sparse ? kmc_chain_kernel<true> : kmc_chain_kernel<false>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  kern<<<s.num_replicas, kChainWarps * 32, sm, stream>>>(t, species, s, l);
   return cudaGetLastError();
 }
 

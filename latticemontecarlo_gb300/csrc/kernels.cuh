@@ -31,6 +31,7 @@ struct KmcDevState {
   int early_stop;             // IsEscaped: stop a replica whose vacancy is surrounded by solvent
   const int8_t *solvent;      // per replica: most frequent species code
   uint8_t *escaped;           // per replica: 1 once the early stop ended the trajectory
+  long long *prev;            // per replica: previous vacancy site (second-order chain KMC)
 };
 
 constexpr int kRngWords = 2 * 312 + 2;  // MT19937-64 state (312 x u64) + index; Philox uses 4 words
@@ -141,6 +142,13 @@ struct KmcMultiArgs {
 };
 size_t KmcMultiSharedBytes(const DevTables &t, bool sparse);
 cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiArgs &a, bool sparse,
+                           cudaStream_t stream);
+
+// Second-order chain KMC (KineticMcChainOmpi semantics): one block of 12 warps
+// per replica, warp d evaluating the 12 jumps after the jump along direction d.
+constexpr int kChainWarps = 12;
+size_t KmcChainSharedBytes(const DevTables &t, bool sparse);
+cudaError_t LaunchKmcChain(const DevTables &t, int8_t *species, const KmcDevState &s, const KmcLaunch &l,
                            cudaStream_t stream);
 
 // prepare = false skips the shared-memory attribute call (already made by

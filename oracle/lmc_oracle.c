@@ -1760,3 +1760,124 @@ int orc_kmc_multi(orc_model *m, const orc_lattice *lat, int8_t *sp, double T, ui
   free(incl);
   return rc;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Second-order "chain" KMC (KineticMcChainOmpi.cpp:56-152, KineticMcAbstract.cpp:140-190,260-263) */
+/* ------------------------------------------------------------------------- */
+
+int orc_kmc_chain(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
+                  int kind, int rng, uint32_t replica, double *trace8) {
+  orc_mt g;
+  orc_mt_seed(&g, seed);
+  const mappings *mp = maps_for(m, lat);
+  const double beta = 1.0 / kBoltzmann / T;
+  int64_t vac = -1;
+  for (int64_t at = 0; at < lat->N && vac < 0; ++at)
+    if (sp[lat->atom_lattice[at]] == m->x_code) vac = lat->atom_lattice[at];
+  if (vac < 0) return -1;
+  int64_t prev = lat->nn[vac][0]; /* previous_j_lattice_id_: first 1NN of the initial vacancy */
+  double time = 0.0, energy = 0.0;
+  for (int64_t st = 0; st < steps; ++st) {
+    const int64_t k = vac;
+    const int64_t *nbk = lat->nn[k];
+    double total_i[12], barrier_ki[12], de_ki[12], rate_ki[12], back_ki[12];
+    /* BuildEventList: per neighbour i, the 12 jumps i -> l after the jump k -> i */
+    for (int r = 0; r < 12; ++r) {
+      const int64_t i = nbk[r];
+      sp[k] = sp[i];
+      sp[i] = (int8_t)m->x_code;
+      double tot = 0.0, ea_ik = 0.0, de_ik = 0.0;
+      for (int q = 0; q < 12; ++q) {
+        const int64_t l = lat->nn[i][q];
+        pair_ids p;
+        double o[4];
+        int rc;
+        if ((rc = make_pair_ids(lat, i, l, &p)) || (rc = barrier_from_ids(m, mp, sp, i, l, &p, kind, o))) {
+          sp[i] = sp[k];
+          sp[k] = (int8_t)m->x_code;
+          return rc;
+        }
+        tot += exp(-o[0] * beta);
+        if (l == k) {
+          ea_ik = o[0];
+          de_ik = o[1];
+        }
+      }
+      sp[i] = sp[k];
+      sp[k] = (int8_t)m->x_code;
+      /* event_k_i_ = event_i_l.GetReverseJumpEvent() (JumpEvent.cpp:54-57) */
+      barrier_ki[r] = ea_ik - de_ik;
+      de_ki[r] = -de_ik;
+      rate_ki[r] = exp(-barrier_ki[r] * beta);                 /* forward rate */
+      back_ki[r] = exp((de_ki[r] - barrier_ki[r]) * beta);      /* GetBackwardRate */
+      total_i[r] = tot;
+    }
+    double total_k = 0.0;
+    for (int r = 0; r < 12; ++r) total_k += rate_ki[r];
+    /* CalculateTime: sums over the 12 events in rank order */
+    const double t_1 = 1 / total_k / kPrefactor;
+    double beta_bar_k = 0, beta_k = 0, gamma_bar_k_j = 0, gamma_k_j = 0, beta_k_j = 0, alpha_k_j = 0, ts_num = 0,
+           ts_j_num = 0, bb[12], bk[12];
+    int is_prev[12];
+    for (int r = 0; r < 12; ++r) {
+      const double p_ki = rate_ki[r] / total_k;
+      const double p_ik = back_ki[r] / total_i[r];
+      bb[r] = p_ki * p_ik;
+      bk[r] = p_ki * (1 - p_ik);
+      is_prev[r] = nbk[r] == prev;
+      const double t_i = 1 / total_i[r] / kPrefactor;
+      beta_bar_k += bb[r];
+      beta_k += bk[r];
+      gamma_bar_k_j += is_prev[r] ? 0.0 : bb[r];
+      gamma_k_j += is_prev[r] ? 0.0 : bk[r];
+      beta_k_j += is_prev[r] ? bk[r] : 0.0;
+      alpha_k_j += is_prev[r] ? p_ki : 0.0;
+      ts_num += (t_1 + t_i) * bb[r];
+      ts_j_num += is_prev[r] ? 0.0 : (t_1 + t_i) * bb[r];
+    }
+    const double ts = ts_num / beta_bar_k;
+    const double ts_j = ts_j_num / gamma_bar_k_j;
+    const double one_over = 1 / (1 - alpha_k_j);
+    const double t_2 = one_over * (gamma_k_j * t_1 + gamma_bar_k_j * (ts_j + t_1 + beta_bar_k / beta_k * ts));
+    double cum[12], c = 0.0;
+    for (int r = 0; r < 12; ++r) {
+      const double pr = is_prev[r] ? one_over * (gamma_bar_k_j / beta_k) * beta_k_j
+                                   : one_over * (1 + gamma_bar_k_j / beta_k) * bk[r];
+      c += pr;
+      cum[r] = c;
+    }
+    /* SelectEvent: one draw (the time is deterministic) */
+    double u;
+    if (rng == 0) {
+      u = orc_mt_uniform(&g);
+    } else {
+      double nl;
+      philox_step_draws(seed, (uint64_t)st, replica, &nl, &u);
+    }
+    int sel = 11;
+    for (int r = 0; r < 12; ++r)
+      if (!(cum[r] < u)) {
+        sel = r;
+        break;
+      }
+    const int64_t j = nbk[sel];
+    time += t_2;
+    energy += de_ki[sel];
+    if (trace8) {
+      double *t = trace8 + st * 8;
+      t[0] = (double)k;
+      t[1] = (double)j;
+      t[2] = sel;
+      t[3] = barrier_ki[sel];
+      t[4] = de_ki[sel];
+      t[5] = total_k;
+      t[6] = time;
+      t[7] = energy;
+    }
+    sp[k] = sp[j];
+    sp[j] = (int8_t)m->x_code;
+    prev = k;
+    vac = j;
+  }
+  return 0;
+}

@@ -138,6 +138,14 @@ int orc_kmc_multi(orc_model *m, const orc_lattice *lat, int8_t *sp, double T, ui
                   uint64_t step0, int64_t steps, int kind, int64_t *vac, int nv, double *time_io, double *energy_io,
                   double *trace9);
 
+/* KineticMcChainOmpi (second-order residence time, KineticMcChainOmpi.cpp:56-152) on one
+ * lattice: per step the 12 x 12 barriers i -> l after each jump k -> i, the reverse events'
+ * rates and the second-order probabilities and time, sums in rank (id) order, one uniform
+ * draw per step for the selection (rng 0: mt19937_64 seeded with `seed`; rng 1: the Philox
+ * production stream of lattice `replica`). trace8 as orc_kmc, Ea = the chain event's barrier. */
+int orc_kmc_chain(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
+                  int kind, int rng, uint32_t replica, double *trace8);
+
 #ifdef __cplusplus
 }
 #endif

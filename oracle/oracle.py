@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
                                      C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]),
             "orc_cmc": (I64, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, DP, DP, I64, I64P]),
             "orc_model_set_vacancy_zero": (None, [P, C.c_int]),
+            "orc_kmc_chain": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, C.c_uint32, DP]),
             "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             "orc_kmc_multi": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, I64, C.c_int,
                                         I64P, C.c_int, DP, DP, DP]),
@@ -300,3 +301,13 @@ def kmc_multi(model: Model, lat: Lattice, species, T: float, seed: int, vacancie
     if rc:
         raise OracleError(f"orc_kmc_multi rc={rc}")
     return trace, vac, t.value, e.value
+
+
+def kmc_chain(model: Model, lat: Lattice, species, T: float, seed: int, steps: int, kind: int = 0, rng: int = 0,
+              replica: int = 0):
+    """Restated KineticMcChainOmpi loop (species modified in place); trace rows as kmc()."""
+    trace = np.zeros((steps, 8))
+    rc = lib().orc_kmc_chain(model.h, lat.h, _sp(species), T, seed, steps, kind, rng, replica, _p(trace, C.c_double))
+    if rc:
+        raise OracleError(f"orc_kmc_chain rc={rc}")
+    return trace
