@@ -250,6 +250,8 @@ def run_ours(args, rank, world, local):
         result["surrogate"] = run_surrogate(args, device)
     if not args.no_large:
         result["large_lattice"] = run_large(args, device)
+    if args.chain_steps > 0:
+        result["chain_kmc"] = run_chain(args, device, seed)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -284,6 +286,28 @@ def run_cmc(args, device, flush, barrier):
             "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+
+
+def run_chain(args, device, seed: int):
+    """Second-order chain KMC (KineticMcChainOmpi) on the batched-replica workload: per step the
+    12 x 12 jump barriers after each first jump, one block of 12 warps per replica."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import _native as N
+
+    cfg, coeffs, ns, species, temps = kmc_inputs(seed, args.replicas)
+    ctx = Context(Model.from_coefficients(coeffs, list(cfg["elements"])), device=device)
+    ctx.set_lattices(ns, species)
+    ctx.kmc_init(temps, seed=seed, rng=N.LMC_RNG_PHILOX, chain=True)
+    ctx.kmc_run(10)  # warm-up
+    ctx.kmc_run(args.chain_steps)
+    ms = ctx.last_run_ms()
+    ev = int(ns.size) * args.chain_steps
+    v = ev / (ms / 1e3)
+    peak, _ = peaks()
+    return {"workload": f"{int(ns.size)} replicas (the batched-KMC lattices), {args.chain_steps} chain steps each",
+            "value": v, "unit": "events/s", "ms": ms, "jump_evaluations_per_s": 144 * v,
+            "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
 
 
 def run_large(args, device):
@@ -557,6 +581,7 @@ def main():
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
     ap.add_argument("--surrogate-epochs", type=int, default=30)
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
+    ap.add_argument("--chain-steps", type=int, default=100, help="chain KMC steps per replica (0 skips)")
     ap.add_argument("--large-cmc-sweeps", type=int, default=100, help="CMC sweeps on the n=64 lattice")
     ap.add_argument("--large-kmc-events", type=int, default=1_000_000, help="multi-vacancy KMC events, n=64")
     ap.add_argument("--no-large", action="store_true", help="skip the n=64, 64-vacancy block")

@@ -669,6 +669,22 @@ KineticMcFirstOmp::KineticMcFirstOmp(cfg::Config config, unsigned long long log_
 
 KineticMcFirstOmp::~KineticMcFirstOmp() = default;
 
+KineticMcChainOmpi::KineticMcChainOmpi(cfg::Config config, unsigned long long log_dump_steps,
+                                       unsigned long long config_dump_steps, unsigned long long maximum_steps,
+                                       unsigned long long thermodynamic_averaging_steps,
+                                       unsigned long long restart_steps, double restart_energy, double restart_time,
+                                       double temperature, const std::set<Element> &element_set,
+                                       const std::string &json_coefficients_filename,
+                                       const std::string &time_temperature_filename, bool is_rate_corrector,
+                                       bool is_early_stop, bool is_solute_disp)
+    : KineticMcFirstOmp(std::move(config), log_dump_steps, config_dump_steps, maximum_steps,
+                        thermodynamic_averaging_steps, restart_steps, restart_energy, restart_time, temperature,
+                        element_set, json_coefficients_filename, time_temperature_filename, is_rate_corrector,
+                        is_early_stop, is_solute_disp) {
+  if (is_early_stop) throw std::invalid_argument("early_stop is not available with KineticMcChainOmpi here");
+  chain_ = true;
+}
+
 void KineticMcFirstOmp::Simulate() {
   pred::detail::Device dev(json_coefficients_filename_, element_set_);
   dev.Sync(config_);
@@ -686,6 +702,7 @@ void KineticMcFirstOmp::Simulate() {
   opt.tt_temp = is_time_temperature_interpolator_ ? tt_temp.data() : nullptr;
   opt.tt_len = is_time_temperature_interpolator_ ? static_cast<int>(tt_time.size()) : 0;
   opt.early_stop = is_early_stop_ ? 1 : 0;
+  opt.chain = chain_ ? 1 : 0;
   pred::detail::Check(lmc_kmc_init(dev.ctx(), &temperature_, &opt));
 
   const bool restarted = steps_ > 0;
@@ -917,7 +934,7 @@ void Parameter::ReadParam(const std::string &param_filename) {
 void Run(const Parameter &p) {
   std::set<Element> element_set;
   for (const auto &e : p.element_set_) element_set.insert(Element(e));
-  if (p.method != "KineticMcFirstOmp" && p.method != "CanonicalMcOmp") {
+  if (p.method != "KineticMcFirstOmp" && p.method != "KineticMcChainOmpi" && p.method != "CanonicalMcOmp") {
     std::cout << "No such method: " << p.method << std::endl;
     return;
   }
@@ -930,6 +947,14 @@ void Run(const Parameter &p) {
                               p.thermodynamic_averaging_steps_, p.restart_steps_, p.restart_energy_, p.restart_time_,
                               p.temperature_, element_set, p.json_coefficients_filename_,
                               p.time_temperature_filename_, p.rate_corrector_, p.early_stop_, p.solute_disp_);
+    if (p.has_seed_) kmc.SetSeed(p.seed_);
+    kmc.Simulate();
+  } else if (p.method == "KineticMcChainOmpi") {
+    std::cout << "Finish config reading. Start KMC." << std::endl;
+    mc::KineticMcChainOmpi kmc(config, p.log_dump_steps_, p.config_dump_steps_, p.maximum_steps_,
+                               p.thermodynamic_averaging_steps_, p.restart_steps_, p.restart_energy_,
+                               p.restart_time_, p.temperature_, element_set, p.json_coefficients_filename_,
+                               p.time_temperature_filename_, p.rate_corrector_, p.early_stop_, p.solute_disp_);
     if (p.has_seed_) kmc.SetSeed(p.seed_);
     kmc.Simulate();
   } else {

@@ -13,6 +13,7 @@
 //   pred::EnergyPredictor                     lmc/pred/include/EnergyPredictor.h:19
 //   pred::TimeTemperatureInterpolator         lmc/pred/include/TimeTemperatureInterpolator.h
 //   mc::KineticMcFirstOmp                     lmc/mc/include/KineticMcFirstOmp.h
+//   mc::KineticMcChainOmpi                    lmc/mc/include/KineticMcChainOmpi.h
 //   mc::CanonicalMcOmp                        lmc/mc/include/CanonicalMcOmp.h
 //   api::Parameter, api::Run                  lmc/api/include/Parameter.h, Home.h
 //
@@ -252,6 +253,9 @@ class KineticMcFirstOmp {
   void SetSeed(uint64_t seed) { seed_ = seed; }
   [[nodiscard]] const cfg::Config &GetConfig() const { return config_; }
 
+ protected:
+  bool chain_{false};  // second-order residence time (KineticMcChainOmpi)
+
  private:
   cfg::Config config_;
   unsigned long long log_dump_steps_, config_dump_steps_, maximum_steps_, steps_;
@@ -261,6 +265,21 @@ class KineticMcFirstOmp {
   pred::TimeTemperatureInterpolator time_temperature_interpolator_;
   bool is_time_temperature_interpolator_, is_rate_corrector_, is_early_stop_, is_solute_disp_;
   uint64_t seed_;
+};
+
+// KineticMcChainOmpi (KineticMcChainOmpi.cpp:56-152, KineticMcAbstract.cpp:225-263): the
+// second-order residence-time algorithm on one GPU (the reference runs 12 MPI ranks, one per
+// first jump): per step the 12 x 12 jumps after each first jump, deterministic second-order
+// time, one uniform draw for the selection. Same log and dumps as KineticMcFirstOmp; the early
+// stop is not available with it here.
+class KineticMcChainOmpi : public KineticMcFirstOmp {
+ public:
+  KineticMcChainOmpi(cfg::Config config, unsigned long long log_dump_steps, unsigned long long config_dump_steps,
+                     unsigned long long maximum_steps, unsigned long long thermodynamic_averaging_steps,
+                     unsigned long long restart_steps, double restart_energy, double restart_time, double temperature,
+                     const std::set<Element> &element_set, const std::string &json_coefficients_filename,
+                     const std::string &time_temperature_filename, bool is_rate_corrector, bool is_early_stop,
+                     bool is_solute_disp);
 };
 
 // CanonicalMcOmp (CanonicalMcOmp.cpp:40-92, CanonicalMcAbstract.cpp:43-101): batches
@@ -314,7 +333,8 @@ struct Parameter {
   int cmc_batch_{0};
 };
 
-// Run (Home.cpp:97-125) for the methods of this path: KineticMcFirstOmp and CanonicalMcOmp.
+// Run (Home.cpp:97-125) for the methods of this path: KineticMcFirstOmp, KineticMcChainOmpi and
+// CanonicalMcOmp.
 void Run(const Parameter &parameter);
 
 }  // namespace api

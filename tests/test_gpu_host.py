@@ -158,3 +158,28 @@ def test_cmc_executable(check, golden, oracle_mod, tmp_path):
         np.testing.assert_allclose(log[s, 3], ref_avg, rtol=1e-9, atol=1e-12)
     e0, _ = oracle_mod.energy(m, lat, sp)
     np.testing.assert_allclose(log[:, 4], e0 + trace, rtol=0, atol=1e-9)
+
+
+def test_chain_kmc_executable(check, golden, oracle_mod, tmp_path):
+    """simulation_method KineticMcChainOmpi: kmc_log.txt rows against the oracle's chain KMC."""
+    G, load = golden
+    el, coeffs, n, sp = G.case_inputs("kmc_ternary")
+    write_cfg(tmp_path / "start.cfg", n, sp, _alphabet(el))
+    (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
+    steps = 40
+    _run(tmp_path, {"simulation_method": "KineticMcChainOmpi", "config_filename": "start.cfg",
+                    "json_coefficients_filename": "coeffs.json", "log_dump_steps": 1, "config_dump_steps": 1000,
+                    "maximum_steps": steps, "thermodynamic_averaging_steps": 0, "temperature": G.KMC_T,
+                    "element_set": " ".join(el), "seed": G.KMC_SEED})
+    head, log = _read_log(tmp_path / "kmc_log.txt")
+    assert head[:6] == ["steps", "time", "temperature", "energy", "Ea", "dE"]
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    ref = oracle_mod.kmc_chain(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, steps + 1, rng=0)
+    assert log.shape[0] == steps + 1
+    t_before = np.concatenate([[0.0], ref[:-1, 6]])
+    e_before = np.concatenate([[0.0], ref[:-1, 7]])
+    np.testing.assert_allclose(log[:, 1], t_before, rtol=1e-9, atol=1e-300)
+    np.testing.assert_allclose(log[:, 3], e_before, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(log[:, 4], ref[:, 3], rtol=EA_RTOL)
+    np.testing.assert_allclose(log[:, 5], ref[:, 4], rtol=0, atol=DE_ATOL)
