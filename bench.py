@@ -252,6 +252,8 @@ def run_ours(args, rank, world, local):
         result["large_lattice"] = run_large(args, device)
     if args.chain_steps > 0:
         result["chain_kmc"] = run_chain(args, device, seed)
+    if args.single_steps > 0:
+        result["single_trajectory"] = run_single(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -286,6 +288,41 @@ def run_cmc(args, device, flush, barrier):
             "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+
+
+def run_single(args, device):
+    """One trajectory (KineticMcFirstOmp's own case: n = 10, 1 vacancy, Al/Mg/Zn .96/.02/.02, 400 K)
+    on the reference's mt19937_64 stream: the latency of a step, one replica on the GPU (12 warps,
+    one per jump), beside the oracle's restatement of the reference loop on one host core."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import _native as N
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    cfg = S.KMC_SINGLE
+    coeffs = S.make_coefficients(cfg["elements"], 11)
+    sp = S.make_lattice(cfg["n"], cfg["fractions"], 1, 11, cfg["elements"])
+    ctx = Context(Model.from_coefficients(coeffs, list(cfg["elements"])), device=device)
+    ctx.set_lattices([cfg["n"]], sp)
+    ctx.kmc_init([cfg["T"]], seed=5, rng=N.LMC_RNG_MT19937_64)
+    ctx.kmc_run(1000)
+    ctx.kmc_run(args.single_steps)
+    gpu = args.single_steps / (ctx.last_run_ms() / 1e3)
+    out = {"workload": f"n={cfg['n']} (4000 sites), 1 vacancy, T={cfg['T']} K, mt19937_64 stream, "
+                       f"{args.single_steps} steps", "value": gpu, "unit": "events/s",
+           "launch": ctx.kmc_launch_info()}
+    if not args.no_cpu_baseline:
+        O.build()
+        lat = O.Lattice(cfg["n"])
+        m = O.Model(cfg["elements"], coeffs, lat)
+        steps = max(1000, args.single_steps // 20)
+        t0 = time.perf_counter()
+        O.kmc(m, lat, sp.copy(), cfg["T"], 5, steps, memo=True)
+        w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": steps / w, "unit": "events/s", "cores": 1, "kind": "port",
+                               "sample": f"{steps} steps of the same trajectory, oracle C restatement with "
+                                         f"barrier memo, {w:.1f} s"}
+    return out
 
 
 def run_chain(args, device, seed: int):
@@ -582,6 +619,7 @@ def main():
     ap.add_argument("--surrogate-epochs", type=int, default=30)
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
     ap.add_argument("--chain-steps", type=int, default=100, help="chain KMC steps per replica (0 skips)")
+    ap.add_argument("--single-steps", type=int, default=100_000, help="steps of the one-trajectory case (0 skips)")
     ap.add_argument("--large-cmc-sweeps", type=int, default=100, help="CMC sweeps on the n=64 lattice")
     ap.add_argument("--large-kmc-events", type=int, default=1_000_000, help="multi-vacancy KMC events, n=64")
     ap.add_argument("--no-large", action="store_true", help="skip the n=64, 64-vacancy block")

@@ -346,6 +346,29 @@ int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
 int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy);
 
 /* ------------------------------------------------------------------------- */
+/* Simulated annealing (SimulatedAnnealing.cpp:99-185, a next row of the path) */
+/* ------------------------------------------------------------------------- */
+/* Per-step record: the trial pair, whether it was accepted, its dE, and the
+ * energy and temperature before the step (what Dump logs, SimulatedAnnealing.cpp:78-97). */
+typedef struct lmc_sa_step {
+  int64_t site1, site2;
+  int32_t accepted;
+  int32_t pad;
+  double de, energy, temperature;
+} lmc_sa_step;
+/* Starts an annealing run on lattice `replica`: mt19937_64 seeded with `seed` (the reference seeds
+ * from the clock, McAbstract.cpp:32), schedule lengths from maximum_steps (window 0.1 %, reheat
+ * trigger 5 %, cooldown 10 %), T = initial_temperature, energy = initial_energy (the reference's
+ * cluster energy relative to the dilute solution, SimulatedAnnealing.cpp:59-70, is the caller's). */
+int lmc_sa_init(lmc_ctx *ctx, int replica, uint64_t seed, uint64_t maximum_steps, double initial_temperature,
+                double initial_energy);
+/* Runs `steps` trial moves (one warp: pair redrawn until the species differ, PairSite dE, Metropolis,
+ * UpdateTemperature); trace (NULL or `steps` records). */
+int lmc_sa_run(lmc_ctx *ctx, uint64_t steps, lmc_sa_step *trace);
+/* Steps done, current temperature and energy, lowest energy seen by Dump's bookkeeping. */
+int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double *energy, double *lowest_energy);
+
+/* ------------------------------------------------------------------------- */
 /* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */
 /* ------------------------------------------------------------------------- */
 #define LMC_CMC_REFERENCE_BATCH 0 /* mt19937_64 stream, batch of `batch` pairs as the reference draws them */

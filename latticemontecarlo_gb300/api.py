@@ -220,6 +220,26 @@ class Context:
         return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "evaluation": ev.value,
                 "from_cache": bool(hit.value)}
 
+    # simulated annealing --------------------------------------------------
+    SA_DTYPE = np.dtype([("site1", np.int64), ("site2", np.int64), ("accepted", np.int32), ("pad", np.int32),
+                         ("de", np.float64), ("energy", np.float64), ("temperature", np.float64)])
+
+    def sa_init(self, initial_temperature: float, maximum_steps: int, seed: int = 0, energy: float = 0.0,
+                replica: int = 0):
+        check(N.lib.lmc_sa_init(self._h, replica, seed, maximum_steps, initial_temperature, energy))
+
+    def sa_run(self, steps: int, trace: bool = False):
+        tr = np.zeros(steps, self.SA_DTYPE) if trace else None
+        check(N.lib.lmc_sa_run(self._h, steps, tr.ctypes.data_as(C.c_void_p) if tr is not None else None))
+        return tr
+
+    def sa_state(self):
+        """(steps, temperature, energy, lowest energy)."""
+        st = C.c_uint64()
+        t, e, lo = C.c_double(), C.c_double(), C.c_double()
+        check(N.lib.lmc_sa_get_state(self._h, C.byref(st), C.byref(t), C.byref(e), C.byref(lo)))
+        return st.value, t.value, e.value, lo.value
+
     # multi-vacancy kinetic MC ---------------------------------------------
     def kmc_multi_init(self, temperatures, seed: int = 0, kind: int = N.LMC_BARRIER_QUARTIC,
                        evaluation: int = N.LMC_EVAL_SPARSE):

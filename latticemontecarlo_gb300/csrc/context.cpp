@@ -109,6 +109,10 @@ struct lmc_ctx {
   cudaGraphExec_t kmc_graph{nullptr};
   std::vector<unsigned char> kmc_graph_key;
   int *h_status{nullptr};
+  // simulated annealing on one lattice
+  bool sa_ready{false};
+  int sa_replica{0};
+  DevBuf sa_state, sa_rng, sa_trace;
   // multi-vacancy KMC (every vacancy of a lattice tracked; slots per lattice)
   bool multi_ready{false};
   int multi_kind{0}, multi_eval{0};
@@ -123,7 +127,8 @@ struct lmc_ctx {
                       &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &k_prev, &c_trace, &s_feat, &s_mean, &s_spread,
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
-    for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace})
+    for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace, &sa_state, &sa_rng,
+                      &sa_trace})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -833,6 +838,26 @@ KmcTuneEntry SweepKmcShapes(lmc_ctx *ctx, uint64_t probe_steps) {
   Require(std::isfinite(best.ms), LMC_ERR_UNSUPPORTED, "no KMC launch shape fits this device");
   best.probe_steps = probe_steps;
   return best;
+}
+
+// Number of distinct species in a replica's lattice (device scan).
+int SpeciesPresent(lmc_ctx *ctx, int replica) {
+  DevBuf hist, first;
+  hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1));
+  first.Alloc(sizeof(long long));
+  const long long big = std::numeric_limits<long long>::max();
+  CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+  CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>() + replica,
+                                   ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, ctx->fm.num_species,
+                                   first.as<long long>(), hist.as<unsigned long long>(), ctx->stream),
+            "scan kernel");
+  unsigned long long h[lmc::kMaxSpecies + 1];
+  CudaCheck(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  ctx->Sync();
+  int present = 0;
+  for (int c = 0; c < ctx->fm.num_species; ++c) present += h[c] > 0;
+  return present;
 }
 
 }  // namespace
@@ -1886,6 +1911,86 @@ int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, d
   });
 }
 
+int lmc_sa_init(lmc_ctx *ctx, int replica, uint64_t seed, uint64_t maximum_steps, double initial_temperature,
+                double initial_energy) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    ctx->CheckReplica(replica);
+    Require(initial_temperature > 0 && std::isfinite(initial_temperature), LMC_ERR_INVALID_ARGUMENT,
+            "initial_temperature must be > 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    Require(SpeciesPresent(ctx, replica) >= 2, LMC_ERR_INVALID_ARGUMENT,
+            "simulated annealing needs at least two species in the lattice");
+    lmc::SaState st{};
+    st.steps = 0;
+    st.maximum_steps = maximum_steps;
+    // SimulatedAnnealing constructor (SimulatedAnnealing.cpp:53-56): schedule lengths from maximum_steps
+    auto frac = [&](double r) {
+      return std::max<unsigned long long>(1ULL, static_cast<unsigned long long>(static_cast<double>(maximum_steps) * r));
+    };
+    st.reheat_trigger = frac(0.05);
+    st.reheat_cooldown = frac(0.10);
+    st.window_size = frac(0.001);
+    st.temperature = initial_temperature;
+    st.beta = 1.0 / 8.617333262145e-5 / initial_temperature;
+    st.energy = st.lowest = st.recent_best = initial_energy;
+    ctx->sa_state.Ensure(sizeof(lmc::SaState));
+    ctx->sa_rng.Ensure(sizeof(uint32_t) * lmc::kRngWords);
+    std::vector<uint32_t> w(lmc::kRngWords, 0);
+    lmc::MtSeed(seed, w.data());
+    CudaCheck(cudaMemcpy(ctx->sa_state.p, &st, sizeof(st), cudaMemcpyHostToDevice), "H2D");
+    CudaCheck(cudaMemcpy(ctx->sa_rng.p, w.data(), 4 * w.size(), cudaMemcpyHostToDevice), "H2D");
+    ctx->sa_replica = replica;
+    ctx->sa_ready = true;
+  });
+}
+
+int lmc_sa_run(lmc_ctx *ctx, uint64_t steps, lmc_sa_step *trace) {
+  return Guard([&] {
+    Require(ctx && ctx->sa_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_sa_init has not been called");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (steps == 0) return;
+    static_assert(sizeof(lmc_sa_step) == sizeof(lmc::SaStepRec), "trace record layout");
+    lmc::SaArgs a{};
+    a.n = ctx->n[ctx->sa_replica];
+    a.steps = steps;
+    a.rng = ctx->sa_rng.as<uint32_t>();
+    a.state = ctx->sa_state.as<lmc::SaState>();
+    if (trace) {
+      ctx->sa_trace.Ensure(sizeof(lmc::SaStepRec) * steps);
+      a.trace = ctx->sa_trace.as<lmc::SaStepRec>();
+    }
+    a.stop_flag = ctx->d_stop;
+    a.status = ctx->status.as<int>();
+    ctx->ClearStatus();
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchSa(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[ctx->sa_replica], a, ctx->stream),
+              "annealing kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    if (trace)
+      CudaCheck(cudaMemcpyAsync(trace, a.trace, sizeof(lmc::SaStepRec) * steps, cudaMemcpyDeviceToHost, ctx->stream),
+                "D2H trace");
+    const int st = ctx->ReadStatus();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(st, "simulated annealing");
+  });
+}
+
+int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double *energy, double *lowest_energy) {
+  return Guard([&] {
+    Require(ctx && ctx->sa_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_sa_init has not been called");
+    lmc::SaState st{};
+    CudaCheck(cudaMemcpyAsync(&st, ctx->sa_state.p, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    if (steps) *steps = st.steps;
+    if (temperature) *temperature = st.temperature;
+    if (energy) *energy = st.energy;
+    if (lowest_energy) *lowest_energy = st.lowest;
+  });
+}
+
 int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy) {
   return Guard([&] {
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
@@ -1921,26 +2026,10 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
     int *d_quit = reinterpret_cast<int *>(d_done + 2);
     double *d_energy = reinterpret_cast<double *>(d_done + 4);
     CudaCheck(cudaMemsetAsync(d_done, 0, sizeof(unsigned long long) * 4, ctx->stream), "memset");
-    {
-      // both CMC modes redraw pairs until the two species differ: refuse a
-      // lattice with a single species instead of spinning on it
-      DevBuf hist, first;
-      hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1));
-      first.Alloc(sizeof(long long));
-      const long long big = std::numeric_limits<long long>::max();
-      CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
-      CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
-      CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>() + replica,
-                                       ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, ctx->fm.num_species,
-                                       first.as<long long>(), hist.as<unsigned long long>(), ctx->stream),
-                "scan kernel");
-      unsigned long long h[lmc::kMaxSpecies + 1];
-      CudaCheck(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-      ctx->Sync();
-      int present = 0;
-      for (int c = 0; c < ctx->fm.num_species; ++c) present += h[c] > 0;
-      Require(present >= 2, LMC_ERR_INVALID_ARGUMENT, "canonical MC needs at least two species in the lattice");
-    }
+    // both CMC modes redraw pairs until the two species differ: refuse a
+    // lattice with a single species instead of spinning on it
+    Require(SpeciesPresent(ctx, replica) >= 2, LMC_ERR_INVALID_ARGUMENT,
+            "canonical MC needs at least two species in the lattice");
     CudaCheck(cudaMemcpyAsync(d_energy, energy_io, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
     ctx->ClearStatus();
     double e_out = *energy_io;

@@ -2278,6 +2278,125 @@ __global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// K5c: simulated annealing (SimulatedAnnealing.cpp:99-185), one warp. Per step:
+// Dump's lowest-energy bookkeeping on the state before the step (:83-97), a
+// trial pair redrawn until the species differ (:138-146), its PairSite dE (warp
+// cluster sums), Metropolis (:148-167), then UpdateTemperature (:99-137):
+// windowed acceptance cool-down, bounded reheats, the baseline exponential decay.
+// ---------------------------------------------------------------------------
+constexpr double kSaEpsilon = 1e-4;  // kEpsilon, lmc/cfg/include/VectorMatrix.hpp:65
+__global__ void sa_kernel(DevTables t, int8_t *species, SaArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  __shared__ unsigned long long s_mt[312];
+  __shared__ unsigned s_idx;
+  __shared__ long long s_pair[2];
+  __shared__ int s_stop;
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  const unsigned long long *gmt = reinterpret_cast<const unsigned long long *>(a.rng);
+  for (int i = threadIdx.x; i < 312; i += blockDim.x) s_mt[i] = gmt[i];
+  if (threadIdx.x == 0) s_idx = a.rng[2 * 312];
+  __syncthreads();
+  const int lane = threadIdx.x;
+  const Mt mt{s_mt, &s_idx};
+  const int n = a.n;
+  const unsigned long long nsites = 4ULL * n * n * n;
+  int8_t *sa = s.arr, *sb = sa + 44;
+  SaState st = *a.state;
+  unsigned bad = 0;
+  for (unsigned long long it = 0; it < a.steps; ++it) {
+    if (lane == 0) {
+      s_stop = (a.stop_flag && (it & 255) == 0 && *a.stop_flag) ? 1 : 0;
+      // Dump: lowest-energy bookkeeping on the state before this step
+      if (st.energy < st.lowest - kSaEpsilon) st.lowest = st.energy;
+      long long l1 = 0, l2 = 0;
+      unsigned draws = 0;
+      do {  // GenerateLatticeIdJumpPair (the host rejects single-species lattices; the cap is a safety net)
+        l1 = static_cast<long long>(MtBelow(mt, nsites));
+        l2 = static_cast<long long>(MtBelow(mt, nsites));
+      } while (species[l1] == species[l2] && ++draws < (1u << 24));
+      if (species[l1] == species[l2]) {
+        bad |= kStatusNumeric;
+        s_stop = 1;
+      }
+      s_pair[0] = l1;
+      s_pair[1] = l2;
+    }
+    __syncwarp();
+    if (s_stop) {
+      if (!(bad & kStatusNumeric)) bad |= kStatusStopped;
+      break;
+    }
+    int pa, pb;
+    GatherSwap(s.off, species, n, SiteCoord(s_pair[0], n), SiteCoord(s_pair[1], n), sa, sb, &pa, &pb, lane);
+    const long long acc_fx = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
+    if (lane == 0) {
+      const double dE = static_cast<double>(acc_fx) * t.de_scale;
+      const double e_before = st.energy, t_before = st.temperature;
+      bool accepted = dE < 0;
+      if (!accepted) accepted = MtUniform(mt) < exp(-dE * st.beta);
+      if (accepted) {
+        const long long l1 = s_pair[0], l2 = s_pair[1];
+        const int8_t v = species[l1];
+        species[l1] = species[l2];
+        species[l2] = v;
+        st.energy += dE;
+      }
+      // UpdateTemperature(accepted)
+      ++st.window_trials;
+      if (accepted) {
+        ++st.window_accepts;
+        if (st.energy < st.recent_best - kSaEpsilon) {
+          st.recent_best = st.energy;
+          st.last_improvement = st.steps;
+        }
+      }
+      if (st.window_trials >= st.window_size) {
+        const double accr = static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials);
+        if (accr > 0.50) st.temperature *= 0.99;
+        st.window_trials = 0;
+        st.window_accepts = 0;
+      }
+      const double acc_est = st.window_trials > 0u
+                                 ? static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials)
+                                 : 1.0;
+      if (st.reheats_done < 5 && st.steps - st.last_improvement >= st.reheat_trigger &&
+          st.steps - st.last_reheat >= st.reheat_cooldown && acc_est < 0.05) {
+        st.temperature *= 1.10;
+        st.last_improvement = st.steps;
+        st.last_reheat = st.steps;
+        st.recent_best = st.energy;
+        ++st.reheats_done;
+      }
+      st.temperature *= exp(-3.0 / static_cast<double>(st.maximum_steps > 1ULL ? st.maximum_steps : 1ULL));
+      st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
+      if (a.trace) {
+        SaStepRec rec;
+        rec.site1 = s_pair[0];
+        rec.site2 = s_pair[1];
+        rec.accepted = accepted ? 1 : 0;
+        rec.pad = 0;
+        rec.de = dE;
+        rec.energy = e_before;
+        rec.temperature = t_before;
+        a.trace[it] = rec;
+      }
+      ++st.steps;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    *a.state = st;
+    if (bad) atomicOr(a.status, static_cast<int>(bad));
+  }
+  __syncwarp();
+  unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
+  for (int i = lane; i < 312; i += 32) gw[i] = s_mt[i];
+  if (lane == 0) a.rng[2 * 312] = s_idx;
+}
+
+// ---------------------------------------------------------------------------
 // K5b: throughput CMC. Each round draws `candidates` different-species pairs
 // (Philox), resolves overlaps by random priority (a pair survives only if its
 // priority is the largest on every site within 3NN of both its sites, so two
@@ -2678,6 +2797,12 @@ cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRef
   if (a.batch < 1 || a.batch > kCmcRefMaxBatch) return cudaErrorInvalidValue;
   const size_t sm = SiteSmemBytes(t, 1);
   cmc_ref_kernel<<<1, 32, sm, stream>>>(t, species, a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSa(const DevTables &t, int8_t *species, const SaArgs &a, cudaStream_t stream) {
+  const size_t sm = SiteSmemBytes(t, 1);
+  sa_kernel<<<1, 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

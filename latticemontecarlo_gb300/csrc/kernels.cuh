@@ -207,6 +207,30 @@ struct CmcRefArgs {
 };
 cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream);
 
+// Simulated annealing (SimulatedAnnealing.cpp:99-185): one warp, the reference's
+// mt19937_64 stream, one trial pair per step and its adaptive temperature schedule.
+struct SaState {
+  unsigned long long steps, maximum_steps, last_improvement, last_reheat;
+  unsigned long long reheat_trigger, reheat_cooldown, window_size;
+  double temperature, beta, energy, lowest, recent_best;
+  unsigned int window_trials, window_accepts, reheats_done, pad;
+};
+struct SaStepRec {
+  long long site1, site2;
+  int accepted, pad;
+  double de, energy, temperature;  // dE of the trial; energy and temperature before the step
+};
+struct SaArgs {
+  int n;
+  unsigned long long steps;  // steps of this launch
+  uint32_t *rng;             // MT state
+  SaState *state;
+  SaStepRec *trace;          // nullable, `steps` records
+  volatile int *stop_flag;
+  int *status;
+};
+cudaError_t LaunchSa(const DevTables &t, int8_t *species, const SaArgs &a, cudaStream_t stream);
+
 // Throughput CMC (cooperative persistent grid, Philox, priority-resolved rounds).
 struct CmcTpArgs {
   int n;

@@ -1881,3 +1881,84 @@ int orc_kmc_chain(const orc_model *m, const orc_lattice *lat, int8_t *sp, double
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Simulated annealing (SimulatedAnnealing.cpp:78-185) on a given lattice      */
+/* ------------------------------------------------------------------------- */
+
+int orc_sa(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T0, uint64_t seed, uint64_t maximum_steps,
+           int64_t steps, double energy0, double *trace7, double *state4) {
+  const double eps = 1e-4; /* kEpsilon, VectorMatrix.hpp:65 */
+  orc_mt g;
+  orc_mt_seed(&g, seed);
+  const uint64_t N = (uint64_t)lat->N;
+#define SA_FRAC(r) ((uint64_t)((double)maximum_steps * (r)) > 1 ? (uint64_t)((double)maximum_steps * (r)) : 1)
+  const uint64_t reheat_trigger = SA_FRAC(0.05), reheat_cooldown = SA_FRAC(0.10), window_size = SA_FRAC(0.001);
+#undef SA_FRAC
+  double T = T0, beta = 1.0 / kBoltzmann / T0, energy = energy0, lowest = energy0, recent_best = energy0;
+  uint64_t last_improvement = 0, last_reheat = 0, st = 0;
+  unsigned window_trials = 0, window_accepts = 0, reheats_done = 0;
+  for (int64_t s = 0; s < steps; ++s, ++st) {
+    if (energy < lowest - eps) lowest = energy; /* Dump */
+    int64_t l1, l2;
+    do {
+      l1 = (int64_t)orc_mt_below(&g, N);
+      l2 = (int64_t)orc_mt_below(&g, N);
+    } while (sp[l1] == sp[l2]);
+    double dE;
+    int rc = orc_pair_site_de(m, lat, sp, l1, l2, &dE);
+    if (rc) return rc;
+    const double e_before = energy, t_before = T;
+    int accepted = dE < 0;
+    if (!accepted) accepted = orc_mt_uniform(&g) < exp(-dE * beta);
+    if (accepted) {
+      const int8_t v = sp[l1];
+      sp[l1] = sp[l2];
+      sp[l2] = v;
+      energy += dE;
+    }
+    /* UpdateTemperature (SimulatedAnnealing.cpp:99-137) */
+    ++window_trials;
+    if (accepted) {
+      ++window_accepts;
+      if (energy < recent_best - eps) {
+        recent_best = energy;
+        last_improvement = st;
+      }
+    }
+    if (window_trials >= window_size) {
+      const double acc = (double)window_accepts / (double)window_trials;
+      if (acc > 0.50) T *= 0.99;
+      window_trials = 0;
+      window_accepts = 0;
+    }
+    const double acc_est = window_trials > 0u ? (double)window_accepts / (double)window_trials : 1.0;
+    if (reheats_done < 5 && st - last_improvement >= reheat_trigger && st - last_reheat >= reheat_cooldown &&
+        acc_est < 0.05) {
+      T *= 1.10;
+      last_improvement = st;
+      last_reheat = st;
+      recent_best = energy;
+      ++reheats_done;
+    }
+    T *= exp(-3.0 / (double)(maximum_steps > 1 ? maximum_steps : 1));
+    beta = 1.0 / kBoltzmann / (T > 1e-12 ? T : 1e-12);
+    if (trace7) {
+      double *t = trace7 + 7 * s;
+      t[0] = (double)l1;
+      t[1] = (double)l2;
+      t[2] = accepted;
+      t[3] = dE;
+      t[4] = e_before;
+      t[5] = t_before;
+      t[6] = lowest;
+    }
+  }
+  if (state4) {
+    state4[0] = (double)st;
+    state4[1] = T;
+    state4[2] = energy;
+    state4[3] = lowest;
+  }
+  return 0;
+}

@@ -146,6 +146,14 @@ int orc_kmc_multi(orc_model *m, const orc_lattice *lat, int8_t *sp, double T, ui
 int orc_kmc_chain(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
                   int kind, int rng, uint32_t replica, double *trace8);
 
+/* SimulatedAnnealing's loop (SimulatedAnnealing.cpp:78-185) on lattice `sp` (modified in place):
+ * mt19937_64 seeded with `seed`, `steps` trial moves of a run planned for maximum_steps, energy
+ * starting at energy0. trace7 (NULL or 7 doubles per step): site1, site2, accepted, dE, energy and
+ * temperature before the step, lowest energy after Dump's bookkeeping. state4 (NULL or 4
+ * doubles): steps, temperature, energy, lowest energy at the end. */
+int orc_sa(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T0, uint64_t seed, uint64_t maximum_steps,
+           int64_t steps, double energy0, double *trace7, double *state4);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
                                      C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]),
             "orc_cmc": (I64, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, DP, DP, I64, I64P]),
             "orc_model_set_vacancy_zero": (None, [P, C.c_int]),
+            "orc_sa": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint64, I64, C.c_double, DP, DP]),
             "orc_kmc_chain": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, C.c_uint32, DP]),
             "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             "orc_kmc_multi": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, I64, C.c_int,
@@ -311,3 +312,17 @@ def kmc_chain(model: Model, lat: Lattice, species, T: float, seed: int, steps: i
     if rc:
         raise OracleError(f"orc_kmc_chain rc={rc}")
     return trace
+
+
+def sa(model: Model, lat: Lattice, species, T0: float, seed: int, maximum_steps: int, steps: int,
+       energy0: float = 0.0):
+    """Restated SimulatedAnnealing loop (species modified in place). Returns (trace [steps x 7]:
+    site1, site2, accepted, dE, energy and temperature before the step, lowest energy; state:
+    steps, temperature, energy, lowest)."""
+    trace = np.zeros((steps, 7))
+    state = np.zeros(4)
+    rc = lib().orc_sa(model.h, lat.h, _sp(species), T0, seed, maximum_steps, steps, energy0,
+                      _p(trace, C.c_double), _p(state, C.c_double))
+    if rc:
+        raise OracleError(f"orc_sa rc={rc}")
+    return trace, state
