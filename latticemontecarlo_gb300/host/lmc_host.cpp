@@ -412,6 +412,31 @@ void Config::SetSpeciesCodes(const std::vector<int8_t> &codes, const std::vector
   ++revision_;
 }
 
+Config GenerateSoluteConfig(int n, const Element &solvent, const std::map<Element, size_t> &solute_atom_count,
+                            uint64_t seed) {
+  Config config = Config::GenerateFCC(n, solvent);
+  std::mt19937_64 generator(seed);
+  std::set<size_t> available;
+  for (size_t i = 0; i < config.GetNumLattices(); ++i) available.insert(i);
+  for (const auto &[solute, count] : solute_atom_count) {
+    for (size_t it = 0; it < count; ++it) {
+      if (available.empty()) {
+        std::cerr << "Size is too small. Cannot generate correct config.\n";
+        return config;
+      }
+      std::uniform_int_distribution<size_t> dis(0, available.size() - 1);
+      auto pos = available.begin();
+      std::advance(pos, static_cast<long>(dis(generator)));
+      const size_t site = *pos;
+      config.SetElementAtLatticeId(site, solute);
+      available.erase(site);
+      for (int shell = 1; shell <= 3; ++shell)
+        for (size_t nb : config.GetNeighborLatticeIdVector(site, shell)) available.erase(nb);
+    }
+  }
+  return config;
+}
+
 }  // namespace cfg
 
 // ---------------------------------------------------------------------------
@@ -553,6 +578,20 @@ double EnergyPredictor::GetEnergy(const cfg::Config &config) const {
   return e;
 }
 
+std::map<Element, double> EnergyPredictor::GetChemicalPotential(const Element &solvent_element) const {
+  std::map<Element, double> potential;
+  const double solvent_energy = GetEnergy(cfg::Config::GenerateFCC(15, solvent_element));
+  potential[solvent_element] = 0;
+  for (const auto &name : device_->alphabet()) {  // the element set and X
+    const Element element(name);
+    if (element == solvent_element) continue;
+    cfg::Config config = cfg::Config::GenerateFCC(15, solvent_element);
+    config.SetElementAtLatticeId(config.GetLatticeIdFromAtomId(0), element);
+    potential[element] = GetEnergy(config) - solvent_energy;
+  }
+  return potential;
+}
+
 TimeTemperatureInterpolator::TimeTemperatureInterpolator(const std::string &filename) {
   if (filename.empty()) return;
   std::ifstream ifs(filename);
@@ -601,6 +640,11 @@ constexpr double kBoltzmann = 8.617333262145e-5;  // Constants.hpp:31
 uint64_t ClockSeed() {
   return static_cast<uint64_t>(std::chrono::system_clock::now().time_since_epoch().count());
 }
+}  // namespace
+
+uint64_t ClockSeedValue() { return ClockSeed(); }
+
+namespace {
 
 // Log cadence of McAbstract::Dump (KineticMcAbstract.cpp:82-90, CanonicalMcAbstract.cpp:72-79).
 bool LogThisStep(unsigned long long steps, unsigned long long log_dump_steps) {
@@ -873,6 +917,72 @@ void CanonicalMcOmp::Simulate() {
   config_.SetSpeciesCodes(species, dev.alphabet());
 }
 
+SimulatedAnnealing::SimulatedAnnealing(int factor, const Element &solvent_element,
+                                       const std::map<Element, size_t> &solute_atom_count,
+                                       unsigned long long log_dump_steps, unsigned long long config_dump_steps,
+                                       unsigned long long maximum_steps, double initial_temperature,
+                                       const std::string &json_coefficients_filename, uint64_t seed)
+    : config_(cfg::GenerateSoluteConfig(factor, solvent_element, solute_atom_count, seed + 1)),
+      solvent_(solvent_element),
+      solute_atom_count_(solute_atom_count),
+      log_dump_steps_(log_dump_steps),
+      maximum_steps_(maximum_steps),
+      initial_temperature_(initial_temperature),
+      json_coefficients_filename_(json_coefficients_filename),
+      seed_(seed) {
+  (void)config_dump_steps;  // the annealing log writes only lowest_energy.cfg.gz
+}
+
+void SimulatedAnnealing::Simulate() {
+  std::set<Element> element_set{solvent_};
+  for (const auto &kv : solute_atom_count_) element_set.insert(kv.first);
+  // SimulatedAnnealing constructor (SimulatedAnnealing.cpp:59-72): the cluster's energy relative
+  // to the same solutes dissolved in the solvent
+  const pred::EnergyPredictor energy_predictor(json_coefficients_filename_, element_set);
+  const auto chemical_potential = energy_predictor.GetChemicalPotential(solvent_);
+  double energy_change_solution_to_pure_solvent = 0;
+  for (const auto &[element, count] : solute_atom_count_)
+    energy_change_solution_to_pure_solvent += chemical_potential.at(element) * static_cast<double>(count);
+  const double absolute0 = energy_predictor.GetEnergy(config_);
+  const double energy_change_cluster_to_pure_solvent =
+      absolute0 - energy_predictor.GetEnergy(cfg::Config::GenerateFCC(config_.GetEdge(), solvent_));
+  double energy = energy_change_cluster_to_pure_solvent - energy_change_solution_to_pure_solvent;
+  std::cout << "initial_energy = " << energy << std::endl;
+  double lowest = energy, absolute = absolute0;
+
+  pred::detail::Device dev(json_coefficients_filename_, element_set);
+  dev.Sync(config_);
+  pred::detail::Check(lmc_sa_init(dev.ctx(), 0, seed_, maximum_steps_, initial_temperature_, energy));
+  std::ofstream ofs("sa_log.txt");
+  ofs.precision(16);
+  constexpr double kEps = 1e-4;  // kEpsilon (VectorMatrix.hpp:65)
+  constexpr unsigned long long kChunk = 1 << 16;
+  std::vector<lmc_sa_step> trace;
+  steps_ = 0;
+  while (steps_ <= maximum_steps_) {
+    const unsigned long long count = std::min(kChunk, maximum_steps_ + 1 - steps_);
+    trace.assign(count, lmc_sa_step{});
+    pred::detail::Check(lmc_sa_run(dev.ctx(), count, trace.data()));
+    for (const lmc_sa_step &s : trace) {
+      // Dump (SimulatedAnnealing.cpp:78-97): the state before this step's move
+      if (steps_ == 0) ofs << "steps\ttemperature\tenergy\tlowest_energy\tabsolute_energy" << std::endl;
+      if (energy < lowest - kEps) {
+        lowest = energy;
+        config_.WriteConfig("lowest_energy.cfg.gz");
+        ofs << steps_ << '\t' << s.temperature << '\t' << energy << '\t' << lowest << '\t' << absolute << std::endl;
+      }
+      if (steps_ % std::max(1ull, log_dump_steps_) == 0)
+        ofs << steps_ << '\t' << s.temperature << '\t' << energy << '\t' << lowest << '\t' << absolute << std::endl;
+      if (s.accepted) {
+        config_.LatticeJump({static_cast<size_t>(s.site1), static_cast<size_t>(s.site2)});
+        energy += s.de;
+        absolute += s.de;
+      }
+      ++steps_;
+    }
+  }
+}
+
 }  // namespace mc
 
 // ---------------------------------------------------------------------------
@@ -927,6 +1037,13 @@ void Parameter::ReadParam(const std::string &param_filename) {
       seed_ = std::stoull(v);
       has_seed_ = true;
     } else if (k == "cmc_batch") cmc_batch_ = std::stoi(v);
+    else if (k == "factor") factor_ = std::stoi(v);
+    else if (k == "solvent_element") solvent_element_ = v;
+    else if (k == "solute_element_set") solute_element_set_.assign(segs.begin() + 1, segs.end());
+    else if (k == "solute_number_set") {
+      solute_number_set_.clear();
+      for (size_t q = 1; q < segs.size(); ++q) solute_number_set_.push_back(std::stoull(segs[q]));
+    } else if (k == "initial_temperature") initial_temperature_ = std::stod(v);
     // other keys of the reference's grammar belong to methods outside this path
   }
 }
@@ -934,6 +1051,17 @@ void Parameter::ReadParam(const std::string &param_filename) {
 void Run(const Parameter &p) {
   std::set<Element> element_set;
   for (const auto &e : p.element_set_) element_set.insert(Element(e));
+  if (p.method == "SimulatedAnnealing") {
+    // BuildSimulatedAnnealingFromParameter (Home.cpp:223-240)
+    std::map<Element, size_t> solute_atom_count;
+    for (size_t i = 0; i < p.solute_element_set_.size() && i < p.solute_number_set_.size(); ++i)
+      solute_atom_count.emplace(Element(p.solute_element_set_[i]), p.solute_number_set_[i]);
+    mc::SimulatedAnnealing sa(p.factor_, Element(p.solvent_element_), solute_atom_count, p.log_dump_steps_,
+                              p.config_dump_steps_, p.maximum_steps_, p.initial_temperature_,
+                              p.json_coefficients_filename_, p.has_seed_ ? p.seed_ : mc::ClockSeedValue());
+    sa.Simulate();
+    return;
+  }
   if (p.method != "KineticMcFirstOmp" && p.method != "KineticMcChainOmpi" && p.method != "CanonicalMcOmp") {
     std::cout << "No such method: " << p.method << std::endl;
     return;

@@ -28,6 +28,7 @@
 #include <deque>
 #include <fstream>
 #include <map>
+#include <random>
 #include <memory>
 #include <mutex>
 #include <set>
@@ -119,6 +120,13 @@ class Config {
   friend class ConfigAccess;
 };
 
+// GenerateSoluteConfig (Config.cpp:1097-1143): a pure `solvent` box of n cells with the solutes
+// placed one at a time on uniformly drawn sites that are not within 3NN of an earlier solute. The
+// reference draws from a clock-seeded generator over an unordered set; here the draw is over the
+// sorted available sites with mt19937_64(seed) (the same distribution, reproducible).
+Config GenerateSoluteConfig(int n, const Element &solvent, const std::map<Element, size_t> &solute_atom_count,
+                            uint64_t seed);
+
 }  // namespace cfg
 
 namespace pred {
@@ -199,6 +207,9 @@ class EnergyPredictor {
  public:
   EnergyPredictor(const std::string &predictor_filename, const std::set<Element> &element_set);
   [[nodiscard]] double GetEnergy(const cfg::Config &config) const;
+  // GetChemicalPotential (EnergyPredictor.cpp:196-214): the energy of one atom of each element
+  // (and X) in a 15^3 solvent box relative to the pure box; 0 for the solvent.
+  [[nodiscard]] std::map<Element, double> GetChemicalPotential(const Element &solvent_element) const;
 
  private:
   std::shared_ptr<detail::Device> device_;
@@ -306,12 +317,38 @@ class CanonicalMcOmp {
   int batch_;
 };
 
+// Parameter (Parameter.cpp:8-130): the reference's keys, plus `seed` (fixed
+// mt19937_64 seed) and `cmc_batch` (pairs per CanonicalMcOmp batch).
+// Seed of the reference's clock-seeded generators (McAbstract.cpp:32).
+uint64_t ClockSeedValue();
+
+// SimulatedAnnealing (SimulatedAnnealing.cpp:31-185): trial swaps with the adaptive temperature
+// schedule on one warp of the GPU; sa_log.txt and lowest_energy.cfg.gz as the reference writes them.
+// `seed` (an extra trailing argument; the reference seeds from the clock) fixes both the solute
+// placement (mt19937_64(seed + 1)) and the annealing stream (mt19937_64(seed)).
+class SimulatedAnnealing {
+ public:
+  SimulatedAnnealing(int factor, const Element &solvent_element, const std::map<Element, size_t> &solute_atom_count,
+                     unsigned long long log_dump_steps, unsigned long long config_dump_steps,
+                     unsigned long long maximum_steps, double initial_temperature,
+                     const std::string &json_coefficients_filename, uint64_t seed);
+  void Simulate();
+  [[nodiscard]] const cfg::Config &GetConfig() const { return config_; }
+
+ private:
+  cfg::Config config_;
+  Element solvent_;
+  std::map<Element, size_t> solute_atom_count_;
+  unsigned long long log_dump_steps_, maximum_steps_, steps_{0};
+  double initial_temperature_;
+  std::string json_coefficients_filename_;
+  uint64_t seed_;
+};
+
 }  // namespace mc
 
 namespace api {
 
-// Parameter (Parameter.cpp:8-130): the reference's keys, plus `seed` (fixed
-// mt19937_64 seed) and `cmc_batch` (pairs per CanonicalMcOmp batch).
 struct Parameter {
   Parameter() = default;
   Parameter(int argc, char *argv[]);
@@ -331,6 +368,12 @@ struct Parameter {
   bool has_seed_{false};
   uint64_t seed_{0};
   int cmc_batch_{0};
+  // SimulatedAnnealing keys (Parameter.cpp:64-65,113-125)
+  int factor_{0};
+  std::string solvent_element_;
+  std::vector<std::string> solute_element_set_;
+  std::vector<size_t> solute_number_set_;
+  double initial_temperature_{0};
 };
 
 // Run (Home.cpp:97-125) for the methods of this path: KineticMcFirstOmp, KineticMcChainOmpi and

@@ -326,3 +326,23 @@ def sa(model: Model, lat: Lattice, species, T0: float, seed: int, maximum_steps:
     if rc:
         raise OracleError(f"orc_sa rc={rc}")
     return trace, state
+
+
+class Mt19937_64:
+    """std::mt19937_64 with libstdc++'s uniform_int_distribution (restated in the oracle)."""
+
+    class _State(C.Structure):
+        _fields_ = [("mt", C.c_uint64 * 312), ("idx", C.c_int)]
+
+    def __init__(self, seed: int):
+        self.s = self._State()
+        L = lib()
+        for name, res, args in (("orc_mt_seed", None, [C.c_void_p, C.c_uint64]),
+                                ("orc_mt_below", C.c_uint64, [C.c_void_p, C.c_uint64])):
+            getattr(L, name).restype = res
+            getattr(L, name).argtypes = args
+        L.orc_mt_seed(C.byref(self.s), seed)
+
+    def below(self, n: int) -> int:
+        """uniform_int_distribution<size_t>(0, n - 1)."""
+        return int(lib().orc_mt_below(C.byref(self.s), n))

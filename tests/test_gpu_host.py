@@ -183,3 +183,64 @@ def test_chain_kmc_executable(check, golden, oracle_mod, tmp_path):
     np.testing.assert_allclose(log[:, 3], e_before, rtol=0, atol=1e-10)
     np.testing.assert_allclose(log[:, 4], ref[:, 3], rtol=EA_RTOL)
     np.testing.assert_allclose(log[:, 5], ref[:, 4], rtol=0, atol=DE_ATOL)
+
+
+def _solute_config(n, solvent, solutes, seed, oracle_mod, alpha):
+    """GenerateSoluteConfig as the host mirror restates it: mt19937_64(seed + 1), uniform over the
+    sorted available sites, each placed solute removing itself and its 1-3NN sites."""
+    lat = oracle_mod.Lattice(n)
+    sp = np.full(4 * n ** 3, alpha.index(solvent), np.int8)
+    g = oracle_mod.Mt19937_64(seed + 1)
+    available = list(range(sp.size))
+    for el, count in sorted(solutes.items()):
+        for _ in range(count):
+            site = available[g.below(len(available))]
+            sp[site] = alpha.index(el)
+            gone = {site} | set(int(v) for v in lat.neighbors(site))
+            available = [v for v in available if v not in gone]
+    return sp
+
+
+def test_sa_executable(check, oracle_mod, tmp_path):
+    """simulation_method SimulatedAnnealing: the solute configuration, the initial energy from the
+    chemical potentials, and every sa_log.txt row against the oracle's annealing run."""
+    from latticemontecarlo_gb300 import synthetic as S
+    el = ("Al", "Mg", "Zn")
+    alpha = _alphabet(el)
+    coeffs = S.make_coefficients(el, 13)
+    (tmp_path / "coeffs.json").write_text(json.dumps(coeffs))
+    n, seed, max_steps, T0 = 8, 41, 1500, 700.0
+    solutes = {"Mg": 12, "Zn": 9}
+    r = _run(tmp_path, {"simulation_method": "SimulatedAnnealing", "json_coefficients_filename": "coeffs.json",
+                        "factor": n, "solvent_element": "Al", "solute_element_set": "Mg Zn",
+                        "solute_number_set": "12 9", "log_dump_steps": 10, "config_dump_steps": 1000,
+                        "maximum_steps": max_steps, "initial_temperature": T0, "seed": seed})
+    sp = _solute_config(n, "Al", solutes, seed, oracle_mod, alpha)
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    # initial energy: cluster vs pure solvent minus the solutes' chemical potentials (15^3 boxes)
+    lat15 = oracle_mod.Lattice(15)
+    m15 = oracle_mod.Model(el, coeffs, lat15)
+    pure15 = np.full(4 * 15 ** 3, alpha.index("Al"), np.int8)
+    e_pure15, _ = oracle_mod.energy(m15, lat15, pure15)
+    mu = {}
+    for e in ("Mg", "Zn"):
+        one = pure15.copy()
+        one[0] = alpha.index(e)
+        mu[e] = oracle_mod.energy(m15, lat15, one)[0] - e_pure15
+    e_abs0, _ = oracle_mod.energy(m, lat, sp)
+    e_pure, _ = oracle_mod.energy(m, lat, np.full_like(sp, alpha.index("Al")))
+    e0 = (e_abs0 - e_pure) - (12 * mu["Mg"] + 9 * mu["Zn"])
+    assert f"initial_energy = " in r.stdout
+    np.testing.assert_allclose(float(r.stdout.split("initial_energy = ")[1].split()[0]), e0, rtol=0, atol=1e-9)
+    ref, state = oracle_mod.sa(m, lat, sp.copy(), T0, seed, max_steps, max_steps + 1, e0)
+    lines = (tmp_path / "sa_log.txt").read_text().strip().splitlines()
+    assert lines[0].split("\t") == ["steps", "temperature", "energy", "lowest_energy", "absolute_energy"]
+    rows = np.array([[float(v) for v in ln.split("\t")] for ln in lines[1:]])
+    periodic = rows[np.isin(rows[:, 0], np.arange(0, max_steps + 1, 10))]
+    s = periodic[:, 0].astype(int)
+    # the same step can appear twice (an improvement line, then the periodic line): compare the last
+    np.testing.assert_allclose(periodic[:, 1], ref[s, 5], rtol=1e-12)
+    np.testing.assert_allclose(periodic[:, 2], ref[s, 4], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(periodic[:, 4] - periodic[:, 2], e_abs0 - e0, rtol=0, atol=1e-9)
+    assert (tmp_path / "lowest_energy.cfg.gz").exists() or np.all(ref[:, 4] >= e0 - 1e-4)
