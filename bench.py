@@ -254,6 +254,8 @@ def run_ours(args, rank, world, local):
         result["chain_kmc"] = run_chain(args, device, seed)
     if args.single_steps > 0:
         result["single_trajectory"] = run_single(args, device)
+    if args.sa_steps > 0:
+        result["simulated_annealing"] = run_sa(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -322,6 +324,38 @@ def run_single(args, device):
         out["cpu_baseline"] = {"value": steps / w, "unit": "events/s", "cores": 1, "kind": "port",
                                "sample": f"{steps} steps of the same trajectory, oracle C restatement with "
                                          f"barrier memo, {w:.1f} s"}
+    return out
+
+
+def run_sa(args, device):
+    """Simulated annealing (SimulatedAnnealing's sequential trial moves, one warp) on a 20^3 box with
+    200 Mg and 200 Zn solutes in Al, beside the oracle's restatement on one host core."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    el = ("Al", "Mg", "Zn")
+    coeffs = S.make_coefficients(el, 20)
+    n = 20
+    sp = S.make_lattice(n, {"Al": 0.9875, "Mg": 0.00625, "Zn": 0.00625}, 0, 20, el)
+    ctx = Context(Model.from_coefficients(coeffs, list(el)), device=device)
+    ctx.set_lattices([n], sp)
+    ctx.sa_init(600.0, args.sa_steps, seed=3)
+    ctx.sa_run(1000)
+    ctx.sa_run(args.sa_steps)
+    v = args.sa_steps / (ctx.last_run_ms() / 1e3)
+    out = {"workload": f"n={n} ({sp.size} sites), Al/Mg/Zn .9875/.00625/.00625, T0=600 K, {args.sa_steps} trial "
+                       "moves (one sequential chain)", "value": v, "unit": "trial moves/s"}
+    if not args.no_cpu_baseline:
+        O.build()
+        lat = O.Lattice(n)
+        m = O.Model(el, coeffs, lat)
+        steps = max(2000, args.sa_steps // 10)
+        t0 = time.perf_counter()
+        O.sa(m, lat, sp.copy(), 600.0, 3, args.sa_steps, steps)
+        w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": steps / w, "unit": "trial moves/s", "cores": 1, "kind": "port",
+                               "sample": f"the first {steps} moves of the same run, oracle C restatement, {w:.1f} s"}
     return out
 
 
@@ -620,6 +654,7 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
     ap.add_argument("--chain-steps", type=int, default=100, help="chain KMC steps per replica (0 skips)")
     ap.add_argument("--single-steps", type=int, default=100_000, help="steps of the one-trajectory case (0 skips)")
+    ap.add_argument("--sa-steps", type=int, default=200_000, help="simulated-annealing trial moves (0 skips)")
     ap.add_argument("--large-cmc-sweeps", type=int, default=100, help="CMC sweeps on the n=64 lattice")
     ap.add_argument("--large-kmc-events", type=int, default=1_000_000, help="multi-vacancy KMC events, n=64")
     ap.add_argument("--no-large", action="store_true", help="skip the n=64, 64-vacancy block")

@@ -2285,9 +2285,21 @@ __global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
 // windowed acceptance cool-down, bounded reheats, the baseline exponential decay.
 // ---------------------------------------------------------------------------
 constexpr double kSaEpsilon = 1e-4;  // kEpsilon, lmc/cfg/include/VectorMatrix.hpp:65
-__global__ void sa_kernel(DevTables t, int8_t *species, SaArgs a) {
+// Lattices up to this many sites are copied into shared memory for the launch:
+// the trial-pair redraws (one per same-species draw) then read species at
+// shared-memory latency instead of L2 latency.
+constexpr long long kSaSmemSites = 200 * 1024;
+__global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SiteSmem s = CarveSiteSmem(t, smem);
+  const long long nsites_ll = 4LL * a.n * a.n * a.n;
+  const bool local_lattice = nsites_ll <= kSaSmemSites;
+  int8_t *species = species_global;
+  if (local_lattice) {
+    // after the site tables and one warp's 2 x 44 arrays (the layout SiteSmemBytes(t, 1) sizes)
+    species = reinterpret_cast<int8_t *>((reinterpret_cast<size_t>(s.arr + 88) + 15) & ~size_t(15));
+    for (long long i = threadIdx.x; i < nsites_ll; i += blockDim.x) species[i] = species_global[i];
+  }
   __shared__ unsigned long long s_mt[312];
   __shared__ unsigned s_idx;
   __shared__ long long s_pair[2];
@@ -2391,6 +2403,8 @@ __global__ void sa_kernel(DevTables t, int8_t *species, SaArgs a) {
     if (bad) atomicOr(a.status, static_cast<int>(bad));
   }
   __syncwarp();
+  if (local_lattice)
+    for (long long i = lane; i < nsites_ll; i += 32) species_global[i] = species[i];
   unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
   for (int i = lane; i < 312; i += 32) gw[i] = s_mt[i];
   if (lane == 0) a.rng[2 * 312] = s_idx;
@@ -2801,7 +2815,10 @@ cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRef
 }
 
 cudaError_t LaunchSa(const DevTables &t, int8_t *species, const SaArgs &a, cudaStream_t stream) {
-  const size_t sm = SiteSmemBytes(t, 1);
+  const long long nsites = 4LL * a.n * a.n * a.n;
+  const size_t sm = SiteSmemBytes(t, 1) + (nsites <= kSaSmemSites ? static_cast<size_t>(nsites) : 0);
+  cudaError_t err = cudaFuncSetAttribute(sa_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
   sa_kernel<<<1, 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
