@@ -256,6 +256,8 @@ def run_ours(args, rank, world, local):
         result["single_trajectory"] = run_single(args, device)
     if args.sa_steps > 0:
         result["simulated_annealing"] = run_sa(args, device)
+    if not args.no_large:
+        result["exit_time_barriers"] = run_site_jumps(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -324,6 +326,51 @@ def run_single(args, device):
         out["cpu_baseline"] = {"value": steps / w, "unit": "events/s", "cores": 1, "kind": "port",
                                "sample": f"{steps} steps of the same trajectory, oracle C restatement with "
                                          f"barrier memo, {w:.1f} s"}
+    return out
+
+
+def run_site_jumps(args, device):
+    """ExitTime's barrier queries: the vacancy placed on each of the 2^20 sites of an n = 64 lattice
+    (Al/Mg/Zn/Cu .93/.03/.03/.01, one vacancy), 12 barriers per site, mean barrier and exit time;
+    beside the oracle's predictor on one host core for a sample of sites."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    L = S.LARGE
+    el = L["elements"]
+    coeffs = S.make_coefficients(el, 65)
+    sp = S.make_lattice(L["n"], L["fractions"], 1, 65, el)
+    alpha = S.alphabet(el)
+    ctx = Context(Model.from_coefficients(coeffs, list(el)), device=device)
+    ctx.set_lattices([L["n"]], sp)
+    ctx.site_jump_energetics(alpha.index("Al"), 600.0, sites=np.arange(1024))
+    t0 = time.perf_counter()
+    ea, _, _, _, ext = ctx.site_jump_energetics(alpha.index("Al"), 600.0)
+    wall = time.perf_counter() - t0
+    ms = ctx.last_run_ms()
+    out = {"workload": f"vacancy on each of the {sp.size} sites of an n=64 lattice, 12 barriers each",
+           "value": sp.size / (ms / 1e3), "unit": "sites/s", "kernel_ms": ms,
+           "wall_ms_with_host_copies": wall * 1e3, "barriers_per_s": 12 * sp.size / (ms / 1e3)}
+    if not args.no_cpu_baseline:
+        O.build()
+        lat = O.Lattice(L["n"])
+        m = O.Model(el, coeffs, lat)
+        x, al = alpha.index("X"), alpha.index("Al")
+        vac = int(np.flatnonzero(sp == x)[0])
+        mod = sp.copy()
+        mod[vac] = al
+        sites = np.random.default_rng(0).choice(sp.size, 40, replace=False)
+        t0 = time.perf_counter()
+        for s in sites:
+            keep = mod[s]
+            mod[s] = x
+            for t in lat.neighbors(int(s))[:12]:
+                O.quartic(m, lat, mod, int(s), int(t))
+            mod[s] = keep
+        w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(sites) / w, "unit": "sites/s", "cores": 1, "kind": "port",
+                               "sample": f"{len(sites)} sites x 12 barriers, oracle C restatement, {w:.1f} s"}
     return out
 
 

@@ -346,6 +346,20 @@ int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
 int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy);
 
 /* ------------------------------------------------------------------------- */
+/* Vacancy placed on every site: ExitTime's barrier queries (a next row)      */
+/* ------------------------------------------------------------------------- */
+/* ansys::ExitTime::GetJumpEnergetics (ExitTime.cpp:257-310) and GetBarrierListAndExitTime
+ * (:217-255) in one pass: the lattice's own vacancy (its first X) gets `solvent_code`, then for
+ * each listed site (sites NULL = every site, m ignored) the vacancy is put there and its 12 jumps
+ * are evaluated (Quartic or E0). Outputs, host pointers, any may be NULL: ea12 / de12 / nb12
+ * [m][12] in the id order of the neighbours (the adjacency-list order), average [m] = mean
+ * barrier, exit_time [m] = 1 / sum exp(-Ea / (kB T_escape)) / 1e13, both over the barriers in
+ * ascending order. No reference counterpart as one call; one warp per site. */
+int lmc_site_jump_energetics(lmc_ctx *ctx, int replica, int kind, int solvent_code, double escape_temperature,
+                             const int64_t *sites, int64_t m, double *ea12, double *de12, int64_t *nb12,
+                             double *average, double *exit_time);
+
+/* ------------------------------------------------------------------------- */
 /* Simulated annealing (SimulatedAnnealing.cpp:99-185, a next row of the path) */
 /* ------------------------------------------------------------------------- */
 /* Per-step record: the trial pair, whether it was accepted, its dE, and the

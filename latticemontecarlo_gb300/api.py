@@ -220,6 +220,23 @@ class Context:
         return {"warps_per_replica": g.value, "replicas_per_block": rpb.value, "evaluation": ev.value,
                 "from_cache": bool(hit.value)}
 
+    # vacancy on every site (ExitTime's barrier queries) -------------------
+    def site_jump_energetics(self, solvent: int, escape_temperature: float, sites=None, replica: int = 0,
+                             kind: int = N.LMC_BARRIER_QUARTIC):
+        """(ea [m,12], de [m,12], neighbours [m,12], mean barrier [m], exit time [m]) with the vacancy
+        placed on each site (every site when `sites` is None)."""
+        n = int(self.ns[replica])
+        s = None if sites is None else np.ascontiguousarray(sites, dtype=np.int64)
+        m = 4 * n ** 3 if s is None else s.size
+        ea, de = np.zeros((m, 12)), np.zeros((m, 12))
+        nb = np.zeros((m, 12), np.int64)
+        avg, ext = np.zeros(m), np.zeros(m)
+        check(N.lib.lmc_site_jump_energetics(self._h, replica, kind, solvent, escape_temperature,
+                                             ptr(s, C.c_int64) if s is not None else None, m,
+                                             ptr(ea, C.c_double), ptr(de, C.c_double), ptr(nb, C.c_int64),
+                                             ptr(avg, C.c_double), ptr(ext, C.c_double)))
+        return ea, de, nb, avg, ext
+
     # simulated annealing --------------------------------------------------
     SA_DTYPE = np.dtype([("site1", np.int64), ("site2", np.int64), ("accepted", np.int32), ("pad", np.int32),
                          ("de", np.float64), ("energy", np.float64), ("temperature", np.float64)])

@@ -1991,6 +1991,88 @@ int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double 
   });
 }
 
+int lmc_site_jump_energetics(lmc_ctx *ctx, int replica, int kind, int solvent_code, double escape_temperature,
+                             const int64_t *sites, int64_t m, double *ea12, double *de12, int64_t *nb12,
+                             double *average, double *exit_time) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    ctx->CheckReplica(replica);
+    Require(kind == LMC_BARRIER_QUARTIC || kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT, "unknown barrier kind");
+    Require(solvent_code >= 0 && solvent_code < ctx->fm.num_species && solvent_code != ctx->fm.x_code,
+            LMC_ERR_INVALID_ARGUMENT, "solvent code out of range");
+    Require(escape_temperature > 0, LMC_ERR_INVALID_ARGUMENT, "escape_temperature must be > 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int n = ctx->n[replica];
+    const long long nsites = 4LL * n * n * n;
+    if (!sites) m = nsites;
+    Require(m >= 0, LMC_ERR_INVALID_ARGUMENT, "m < 0");
+    if (m == 0) return;
+    if (sites)
+      for (long long i = 0; i < m; ++i)
+        Require(sites[i] >= 0 && sites[i] < nsites, LMC_ERR_OUT_OF_RANGE, "site out of range");
+    // the lattice's own vacancy (Config::GetVacancyAtomId: the first X) and the sparse base
+    DevBuf hist, first;
+    hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1));
+    first.Alloc(sizeof(long long));
+    const long long big = std::numeric_limits<long long>::max();
+    CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+    CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>() + replica,
+                                     ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, ctx->fm.num_species,
+                                     first.as<long long>(), hist.as<unsigned long long>(), ctx->stream),
+              "scan kernel");
+    unsigned long long h[lmc::kMaxSpecies + 1];
+    long long vac = big;
+    CudaCheck(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(&vac, first.p, sizeof(vac), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    int base = -1;
+    for (int c = 0; c < ctx->fm.num_species; ++c)
+      if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || h[c] > h[base])) base = c;
+    Require(base >= 0, LMC_ERR_INVALID_ARGUMENT, "no element of the barrier set in the lattice");
+    BuildSparse(ctx, base);
+    DevBuf d_sites, d_ea, d_de, d_nb, d_avg, d_exit;
+    lmc::SiteJumpArgs a{};
+    a.n = n;
+    if (sites) {
+      d_sites.Alloc(8 * m);
+      CudaCheck(cudaMemcpyAsync(d_sites.p, sites, 8 * m, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      a.sites = d_sites.as<long long>();
+    }
+    a.m = m;
+    a.vacancy = vac == big ? -1 : vac;
+    a.solvent = solvent_code;
+    a.barrier_kind = kind;
+    a.beta_escape = 1.0 / 8.617333262145e-5 / escape_temperature;
+    if (ea12) a.ea12 = (d_ea.Alloc(8 * 12 * m), d_ea.as<double>());
+    if (de12) a.de12 = (d_de.Alloc(8 * 12 * m), d_de.as<double>());
+    if (nb12) a.nb12 = (d_nb.Alloc(8 * 12 * m), d_nb.as<long long>());
+    if (average) a.average = (d_avg.Alloc(8 * m), d_avg.as<double>());
+    if (exit_time) a.exit_time = (d_exit.Alloc(8 * m), d_exit.as<double>());
+    a.status = ctx->status.as<int>();
+    a.sp = ctx->sparse;
+    a.sparse = 1;
+    ctx->ClearStatus();
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchSiteJumps(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], a, ctx->stream),
+              "site jumps kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    auto d2h = [&](void *dst, const DevBuf &src, size_t bytes) {
+      if (dst) CudaCheck(cudaMemcpyAsync(dst, src.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    };
+    d2h(ea12, d_ea, 8 * 12 * m);
+    d2h(de12, d_de, 8 * 12 * m);
+    d2h(nb12, d_nb, 8 * 12 * m);
+    d2h(average, d_avg, 8 * m);
+    d2h(exit_time, d_exit, 8 * m);
+    const int st = ctx->ReadStatus();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    RaiseStatus(st, "site jump energetics");
+  });
+}
+
 int lmc_kmc_get_state(lmc_ctx *ctx, int64_t *vacancy, uint64_t *steps, double *time, double *energy) {
   return Guard([&] {
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");

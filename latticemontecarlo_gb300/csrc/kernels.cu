@@ -1864,6 +1864,109 @@ __global__ void __launch_bounds__(kChainWarps * 32, 2)
 }
 
 // ---------------------------------------------------------------------------
+// K1b: jump energetics of a vacancy placed on each listed site, one warp per
+// site (ansys::ExitTime::GetJumpEnergetics, ExitTime.cpp:257-310, and
+// GetBarrierListAndExitTime, :217-255): the lattice's own vacancy becomes the
+// solvent, the site becomes X, and its 12 jumps are evaluated with the sparse /
+// dense code of kmc_kernel. Outputs per site: (Ea, dE, neighbour) in id order,
+// the mean barrier and the exit time 1 / sum exp(-Ea beta) / prefactor, both
+// summed over the barriers in ascending order as the reference does after its sort.
+// ---------------------------------------------------------------------------
+constexpr int kSiteJumpWarps = 8;
+template <bool kSparse>
+__global__ void __launch_bounds__(kSiteJumpWarps * 32)
+    site_jumps_kernel(const __grid_constant__ DevTables t, const int8_t *__restrict__ species,
+                      const __grid_constant__ SiteJumpArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const KmcSmem sm = CarveKmcSmem(t, smem, kSiteJumpWarps, 1);
+  StageKmcSmem(t, a.sp, sm, kSparse);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  KmcShared &rs = sm.rep[warp];
+  int8_t *st = sm.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const ExpConsts ec{sm.exp, t.exp_l1, t.exp_l2};
+  const int n = a.n;
+  const int center = sm.lst[t.pos_first];
+  unsigned bad_all = 0;
+  for (long long q = static_cast<long long>(blockIdx.x) * kSiteJumpWarps + warp; q < a.m;
+       q += static_cast<long long>(gridDim.x) * kSiteJumpWarps) {
+    const long long site = a.sites ? a.sites[q] : q;
+    const H3 h = SiteCoord(site, n);
+    for (int k = lane; k < kLocalSites; k += 32) {
+      const int8_t *o = sm.loff + k * 4;
+      const long long id = NeighborId(h, o[0], o[1], o[2], n);
+      rs.local[k] = k == center ? static_cast<int8_t>(t.x_code)
+                                : (id == a.vacancy ? static_cast<int8_t>(a.solvent) : species[id]);
+    }
+    if (lane < 12) {
+      const int8_t *o = t.dir + lane * 4;
+      rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
+    }
+    __syncwarp();
+    bool sparse_v = false;
+    if (kSparse) {
+      SparseList(rs, sm.inter, a.sp, lane);
+      __syncwarp();
+      sparse_v = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
+    }
+    if (sparse_v) {
+      bad_all |= SparseItem(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, a.barrier_kind, lane);
+    } else {
+      const DenseArgs da{sm.lst, sm.lmmm, sm.lmm2f, sm.lmm2b, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb};
+      bad_all |= DenseJumpsCold(t, rs, da, a.barrier_kind, 0, 1, lane);
+    }
+    __syncwarp();
+    double ea = 0, de = 0;
+    long long id = 0x7fffffffffffffffLL;
+    if (lane < 12) {
+      const int slot = rs.slot[lane];
+      id = rs.ids[lane];
+      if (slot >= 0) {
+        const JumpOut o = JumpEpilogue(t, ec, a.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+        ea = o.ea;
+        de = o.de;
+      } else {
+        bad_all |= slot == -1 ? kStatusNoCoefficients : kStatusXInEnv;
+      }
+    }
+    // id order (the reference's adjacency list) for the per-jump outputs
+    int rank = 0, rank_ea = 0;
+    for (int k2 = 0; k2 < 12; ++k2) {
+      const long long oid = __shfl_sync(0xffffffffu, id, k2);
+      const double oea = __shfl_sync(0xffffffffu, ea, k2);
+      rank += (k2 != lane) && (oid < id);
+      rank_ea += (k2 != lane) && (oea < ea || (oea == ea && k2 < lane));
+    }
+    if (lane < 12) {
+      const long long o = q * 12 + rank;
+      if (a.ea12) a.ea12[o] = ea;
+      if (a.de12) a.de12[o] = de;
+      if (a.nb12) a.nb12[o] = id;
+    }
+    // ascending barriers: sum and rate sum in that order (std::sort then the loop)
+    int src = 0;
+    for (int k2 = 0; k2 < 12; ++k2)
+      if (__shfl_sync(0xffffffffu, rank_ea, k2) == lane) src = k2;
+    const double ea_sorted = __shfl_sync(0xffffffffu, ea, src);
+    if (a.average || a.exit_time) {
+      double sum = 0.0, rate = 0.0;
+      for (int k2 = 0; k2 < 12; ++k2) {
+        const double b = __shfl_sync(0xffffffffu, ea_sorted, k2);
+        sum += b;
+        rate += exp(-b * a.beta_escape);
+      }
+      if (lane == 0) {
+        if (a.average) a.average[q] = sum / 12.0;
+        if (a.exit_time) a.exit_time[q] = 1.0 / rate / kPrefactor;
+      }
+    }
+    __syncwarp();
+  }
+  if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
 // K4b: multi-vacancy KMC, one block of kMultiWarps warps per lattice.
 // Every vacancy of the lattice is tracked (slots 0..V-1). Per step:
 //  1. the warps re-evaluate the 12 events of each vacancy whose 135-site
@@ -2780,6 +2883,25 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
     if (err != cudaSuccess) return err;
   }
   kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSiteJumps(const DevTables &t, const int8_t *species, const SiteJumpArgs &a, cudaStream_t stream) {
+  if (a.m <= 0) return cudaSuccess;
+  KmcLaunch l{};
+  l.warps_per_replica = 1;
+  l.replicas_per_block = kSiteJumpWarps;
+  l.sparse = 1;  // the carve always holds the sparse tables
+  const size_t sm = KmcSharedBytes(t, l);
+  auto kern = a.sparse ? site_jumps_kernel<true> : site_jumps_kernel<false>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long need = (a.m + kSiteJumpWarps - 1) / kSiteJumpWarps;
+  const int blocks = static_cast<int>(std::min<long long>(need, static_cast<long long>(sms) * 8));
+  kern<<<blocks, kSiteJumpWarps * 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

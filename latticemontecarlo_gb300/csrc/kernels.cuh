@@ -207,6 +207,25 @@ struct CmcRefArgs {
 };
 cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream);
 
+// Jump energetics with the vacancy placed on each of a list of sites
+// (ansys::ExitTime::GetJumpEnergetics / GetBarrierListAndExitTime).
+struct SiteJumpArgs {
+  int n;
+  const long long *sites;   // [m] or null: every site (m = 4 n^3)
+  long long m;
+  long long vacancy;        // the lattice's own vacancy (replaced by `solvent`), -1 none
+  int solvent;              // species code put on the own vacancy
+  int barrier_kind;
+  double beta_escape;       // 1 / kT of the exit-time rates
+  double *ea12, *de12;      // [m][12] in id order of the neighbours, nullable
+  long long *nb12;          // [m][12], nullable
+  double *average, *exit_time;  // [m], nullable
+  int *status;
+  KmcSparse sp;
+  int sparse;
+};
+cudaError_t LaunchSiteJumps(const DevTables &t, const int8_t *species, const SiteJumpArgs &a, cudaStream_t stream);
+
 // Simulated annealing (SimulatedAnnealing.cpp:99-185): one warp, the reference's
 // mt19937_64 stream, one trial pair per step and its adaptive temperature schedule.
 struct SaState {
