@@ -85,6 +85,9 @@ struct lmc_ctx {
   long long total_sites{0};
   DevBuf species, lat_off, lat_n, scan;
   std::vector<unsigned long long> scan_host;  // per replica species histogram + invalid count
+  std::vector<long long> first_host;          // per replica lowest X site (LLONG_MAX: none)
+  bool scan_fresh{false};                     // scan_host / first_host describe the current lattices
+  DevBuf scan_first;
   // batch scratch
   DevBuf pairs, out0, out1, out2, out3, status, counts, energy, enc;
   // KMC
@@ -96,6 +99,7 @@ struct lmc_ctx {
   int tt_len{0};
   // sparse KMC tables (built for the dominant species at lmc_kmc_init)
   std::vector<DevBuf> sparse_bufs;
+  int sparse_base{-1};  // base species the sparse tables were built for (-1: none)
   lmc::KmcSparse sparse{};
   // CMC
   DevBuf c_mark, c_mark_list, c_claim, c_cand, c_eacc, c_stats;
@@ -122,7 +126,7 @@ struct lmc_ctx {
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
-    for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
+    for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &scan_first, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
                       &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &k_prev, &c_trace, &s_feat, &s_mean, &s_spread,
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
@@ -421,6 +425,7 @@ std::vector<double> Vec(const double *p, int n, const char *what) {
 
 // Tables of the sparse KMC evaluation for dominant species `base` (see KmcSparse).
 void BuildSparse(lmc_ctx *c, int base) {
+  if (c->sparse_base == base) return;  // the tables depend only on the model and the base species
   const auto &pt = lmc::GetPairTables();
   const auto &fm = c->fm;
   const int e = fm.num_species, x = fm.x_code, eh = fm.num_onehot;
@@ -588,6 +593,7 @@ void BuildSparse(lmc_ctx *c, int base) {
   sp.dw_stride_mmm = off_mmm.back() + 64;
   sp.dw_stride_mm2 = off_mm2.back() + 64;
   c->sparse = sp;
+  c->sparse_base = base;
 }
 
 void KmcDefaults(const lmc_ctx *c, int *g, int *rpb) {
@@ -1135,12 +1141,22 @@ int lmc_ctx_set_lattices(lmc_ctx *ctx, int num_replicas, const int32_t *n, const
     CudaCheck(cudaMemsetAsync(ctx->scan.p, 0, sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * num_replicas,
                               ctx->stream),
               "memset");
+    ctx->scan_fresh = false;
+    ctx->first_host.assign(num_replicas, std::numeric_limits<long long>::max());
+    ctx->scan_first.Ensure(sizeof(long long) * num_replicas);
+    CudaCheck(cudaMemcpyAsync(ctx->scan_first.p, ctx->first_host.data(), sizeof(long long) * num_replicas,
+                              cudaMemcpyHostToDevice, ctx->stream),
+              "H2D");
     CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>(), ctx->lat_n.as<int>(),
-                                     num_replicas, ctx->fm.x_code, ctx->fm.num_species, nullptr,
-                                     ctx->scan.as<unsigned long long>(), ctx->stream),
+                                     num_replicas, ctx->fm.x_code, ctx->fm.num_species,
+                                     ctx->scan_first.as<long long>(), ctx->scan.as<unsigned long long>(),
+                                     ctx->stream),
               "scan kernel");
     ctx->scan_host.resize(static_cast<size_t>(lmc::kMaxSpecies + 1) * num_replicas);
     CudaCheck(cudaMemcpyAsync(ctx->scan_host.data(), ctx->scan.p, sizeof(unsigned long long) * ctx->scan_host.size(),
+                              cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
+    CudaCheck(cudaMemcpyAsync(ctx->first_host.data(), ctx->scan_first.p, sizeof(long long) * num_replicas,
                               cudaMemcpyDeviceToHost, ctx->stream),
               "D2H");
     ctx->Sync();
@@ -1152,6 +1168,7 @@ int lmc_ctx_set_lattices(lmc_ctx *ctx, int num_replicas, const int32_t *n, const
     ctx->offsets = off;
     ctx->total_sites = total;
     ctx->kmc_ready = false;
+    ctx->scan_fresh = true;
   });
 }
 
@@ -1486,26 +1503,38 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     ctx->k_escaped.Ensure(R);
     ctx->k_prev.Ensure(sizeof(long long) * R);
     CudaCheck(cudaMemsetAsync(ctx->k_escaped.p, 0, R, ctx->stream), "memset");
-    // first vacancy and species histogram of every replica
-    DevBuf hist;
-    hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * R);
-    std::vector<long long> first(R, std::numeric_limits<long long>::max());
-    CudaCheck(cudaMemcpyAsync(ctx->k_vac.p, first.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, ctx->stream),
-              "H2D");
-    CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
-    CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>(), ctx->lat_n.as<int>(), R,
-                                     ctx->fm.x_code, ctx->fm.num_species, ctx->k_vac.as<long long>(),
-                                     hist.as<unsigned long long>(), ctx->stream),
-              "scan kernel");
-    std::vector<unsigned long long> h((lmc::kMaxSpecies + 1) * R);
-    CudaCheck(cudaMemcpyAsync(first.data(), ctx->k_vac.p, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
-              "D2H");
-    CudaCheck(cudaMemcpyAsync(h.data(), hist.p, hist.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    ctx->Sync();
-    hist.Free();
+    // first vacancy and species histogram of every replica: from set_lattices' scan while no
+    // kernel has moved atoms since, else scanned again
+    std::vector<long long> first;
+    std::vector<unsigned long long> h;
+    if (ctx->scan_fresh) {
+      first = ctx->first_host;
+      h = ctx->scan_host;
+      CudaCheck(cudaMemcpyAsync(ctx->k_vac.p, first.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, ctx->stream),
+                "H2D");
+    } else {
+      DevBuf hist;
+      hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1) * R);
+      first.assign(R, std::numeric_limits<long long>::max());
+      CudaCheck(cudaMemcpyAsync(ctx->k_vac.p, first.data(), sizeof(long long) * R, cudaMemcpyHostToDevice,
+                                ctx->stream),
+                "H2D");
+      CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+      CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>(), ctx->lat_n.as<int>(),
+                                       R, ctx->fm.x_code, ctx->fm.num_species, ctx->k_vac.as<long long>(),
+                                       hist.as<unsigned long long>(), ctx->stream),
+                "scan kernel");
+      h.resize((lmc::kMaxSpecies + 1) * R);
+      CudaCheck(cudaMemcpyAsync(first.data(), ctx->k_vac.p, sizeof(long long) * R, cudaMemcpyDeviceToHost,
+                                ctx->stream),
+                "D2H");
+      CudaCheck(cudaMemcpyAsync(h.data(), hist.p, hist.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+      ctx->Sync();
+      hist.Free();
+    }
     for (int r = 0; r < R; ++r)
       Require(first[r] != std::numeric_limits<long long>::max(), LMC_ERR_INVALID_ARGUMENT, "vacancy not found");
-    {
+    if (opt->chain) {
       // previous_j_lattice_id_ of the chain KMC: the first (lowest-id) 1NN of the initial vacancy
       // (KineticMcAbstract.cpp:255)
       std::vector<long long> prev(R);
@@ -1546,14 +1575,16 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
         csol[r] = static_cast<double>(sol) / nsites;
       }
     }
-    std::vector<uint32_t> rng(static_cast<size_t>(lmc::kRngWords) * R, 0);
-    for (int r = 0; r < R; ++r) {
-      uint32_t *w = rng.data() + static_cast<size_t>(lmc::kRngWords) * r;
-      if (opt->rng == LMC_RNG_MT19937_64) {
-        lmc::MtSeed(opt->seed + static_cast<uint64_t>(r), w);
-      } else {
-        w[0] = static_cast<uint32_t>(opt->seed);
-        w[1] = static_cast<uint32_t>(opt->seed >> 32);
+    std::vector<uint32_t> rng;
+    if (opt->rng == LMC_RNG_MT19937_64) {
+      rng.assign(static_cast<size_t>(lmc::kRngWords) * R, 0);
+      for (int r = 0; r < R; ++r)
+        lmc::MtSeed(opt->seed + static_cast<uint64_t>(r), rng.data() + static_cast<size_t>(lmc::kRngWords) * r);
+    } else {
+      rng.resize(2 * static_cast<size_t>(R));  // Philox: the key words only
+      for (int r = 0; r < R; ++r) {
+        rng[2 * r] = static_cast<uint32_t>(opt->seed);
+        rng[2 * r + 1] = static_cast<uint32_t>(opt->seed >> 32);
       }
     }
     std::vector<unsigned long long> zeros_u(R, 0);
@@ -1564,7 +1595,12 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     CudaCheck(cudaMemcpyAsync(ctx->k_temp.p, temp.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
     CudaCheck(cudaMemcpyAsync(ctx->k_cvac.p, cvac.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
     CudaCheck(cudaMemcpyAsync(ctx->k_csol.p, csol.data(), 8 * R, cudaMemcpyHostToDevice, ctx->stream), "H2D");
-    CudaCheck(cudaMemcpyAsync(ctx->k_rng.p, rng.data(), rng.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    if (opt->rng == LMC_RNG_MT19937_64)
+      CudaCheck(cudaMemcpyAsync(ctx->k_rng.p, rng.data(), rng.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    else  // two words at the start of each replica's record
+      CudaCheck(cudaMemcpy2DAsync(ctx->k_rng.p, sizeof(uint32_t) * lmc::kRngWords, rng.data(), 8, 8, R,
+                                  cudaMemcpyHostToDevice, ctx->stream),
+                "H2D keys");
     ctx->tt_len = 0;
     if (opt->tt_len > 0) {
       Require(opt->tt_time && opt->tt_temp, LMC_ERR_INVALID_ARGUMENT, "T(t) table pointers are null");
@@ -1608,6 +1644,7 @@ int lmc_kmc_launch_info(lmc_ctx *ctx, int *warps_per_replica, int *replicas_per_
 
 int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace, double *events12) {
   return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (steps == 0) return;
@@ -1654,6 +1691,7 @@ int lmc_kmc_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *t
 
 int lmc_kmc_run_graph(lmc_ctx *ctx, uint64_t steps_per_launch, int launches) {
   return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
     Require(ctx && ctx->kmc_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_init has not been called");
     Require(steps_per_launch > 0 && launches > 0, LMC_ERR_INVALID_ARGUMENT, "steps_per_launch and launches must be > 0");
     Require(!ctx->kmc_opt.chain, LMC_ERR_UNSUPPORTED, "graph runs cover the first-order KMC");
@@ -1845,6 +1883,7 @@ int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, i
 
 int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace) {
   return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
     Require(ctx && ctx->multi_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_multi_init has not been called");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (steps == 0) return;
@@ -1947,6 +1986,7 @@ int lmc_sa_init(lmc_ctx *ctx, int replica, uint64_t seed, uint64_t maximum_steps
 
 int lmc_sa_run(lmc_ctx *ctx, uint64_t steps, lmc_sa_step *trace) {
   return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
     Require(ctx && ctx->sa_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_sa_init has not been called");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (steps == 0) return;
@@ -2095,6 +2135,7 @@ int lmc_last_run_ms(lmc_ctx *ctx, double *ms) {
 int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts, const lmc_cmc_options *opt,
                 double *energy_io, uint64_t *attempts_done, uint64_t *accepted) {
   return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
     Require(ctx && opt && energy_io, LMC_ERR_INVALID_ARGUMENT, "bad argument");
     ctx->CheckReplica(replica);
     Require(temperature > 0 && std::isfinite(temperature), LMC_ERR_INVALID_ARGUMENT, "temperature must be > 0");

@@ -102,6 +102,12 @@ __device__ __forceinline__ long long WarpSum(long long v) {
   return v;
 }
 
+__device__ __forceinline__ unsigned long long WarpSumU(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __device__ __forceinline__ double WarpSumD(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -2663,10 +2669,22 @@ __global__ void replica_scan_kernel(const int8_t *__restrict__ species, const lo
     if (c >= 0 && c < num_species) local[c] += 1;
     else invalid += 1;
   }
-  if (first_x) atomicMin(&first_x[r], best);
-  for (int c = 0; c < num_species; ++c)
-    if (local[c]) atomicAdd(&hist[r * (kMaxSpecies + 1) + c], local[c]);
-  if (invalid) atomicAdd(&hist[r * (kMaxSpecies + 1) + kMaxSpecies], invalid);
+  // warp totals first: one atomic per warp instead of one per thread
+  const int lane = threadIdx.x & 31;
+  if (first_x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long v = __shfl_xor_sync(0xffffffffu, best, o);
+      best = v < best ? v : best;
+    }
+    if (lane == 0 && best != 0x7fffffffffffffffLL) atomicMin(&first_x[r], best);
+  }
+  for (int c = 0; c < num_species; ++c) {
+    const unsigned long long v = WarpSumU(local[c]);
+    if (lane == 0 && v) atomicAdd(&hist[r * (kMaxSpecies + 1) + c], v);
+  }
+  const unsigned long long bad = WarpSumU(invalid);
+  if (lane == 0 && bad) atomicAdd(&hist[r * (kMaxSpecies + 1) + kMaxSpecies], bad);
 }
 
 }  // namespace
