@@ -633,6 +633,7 @@ lmc::KmcLaunch KmcShape(const lmc_ctx *ctx) {
   l.warps_per_replica = g;
   l.replicas_per_block = rpb;
   l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
+  l.mt = ctx->kmc_opt.rng == LMC_RNG_MT19937_64 ? 1 : 0;
   l.sp = ctx->sparse;
   return l;
 }

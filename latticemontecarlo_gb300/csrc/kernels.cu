@@ -1341,7 +1341,7 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
 // copy of the staged tables per SM, 72 registers per thread).
 constexpr int kShapeThreads[3] = {256, 384, 896};
 constexpr int kShapeBlocks[3] = {4, 2, 1};
-template <bool kSparse, int kShape>
+template <bool kSparse, int kShape, bool kMt>
 __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     kmc_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcDevState s,
                const __grid_constant__ KmcLaunch l) {
@@ -1382,7 +1382,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   }
   if (active && g == 0) step0 = s.steps[r];
   uint32_t key0 = 0, key1 = 0;  // Philox key of the replica
-  if (active && g == 0 && s.rng_kind != 0) {
+  if (active && g == 0 && !kMt) {
     key0 = s.rng[r * kRngWords];
     key1 = s.rng[r * kRngWords + 1];
   }
@@ -1390,7 +1390,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   // step (it & ~31) + j, so the FP64 logarithm runs once per 32 steps
   double nlog_blk = 0.0, u2_blk = 0.0;
   Mt mt{nullptr, nullptr};
-  if (active && s.rng_kind == 0) {
+  if (active && kMt) {
     uint32_t *w = s.rng + static_cast<long long>(r) * kRngWords;
     mt.mt = reinterpret_cast<unsigned long long *>(w);
     mt.idx = w + 2 * 312;
@@ -1472,7 +1472,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       // total rate and prefix sums, sequential in id order (the reference's
       // single-thread reduction, KineticMcFirstOmp.cpp:55-68)
       double total = 0.0, mycum = 0.0;
-      if (s.rng_kind == 0) {
+      if (kMt) {
         for (int q = 0; q < 12; ++q) {
           total += __shfl_sync(0xffffffffu, k_s, q);
           if (lane == q) mycum = total;
@@ -1488,7 +1488,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
         total = __shfl_sync(0xffffffffu, mycum, 11);
       }
       double nlog_u1 = 0, u2 = 0;  // -log(u1) for the clock, u2 for the selection
-      if (s.rng_kind == 0) {
+      if (kMt) {
         if (lane == 0) {
           const double2 d = MtStepDraws(mt);
           nlog_u1 = d.x;
@@ -1507,7 +1507,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
         u2 = __shfl_sync(0xffffffffu, u2_blk, static_cast<int>(it & 31));
       }
       bool hit;
-      if (s.rng_kind == 0) {
+      if (kMt) {
         // cumulative probabilities k_i / total summed in order, first one >= u2
         // (std::lower_bound in KineticMcFirstAbstract::SelectEvent)
         const double p = k_s / total;
@@ -2872,8 +2872,15 @@ using KmcKernelFn = void (*)(DevTables, int8_t *, KmcDevState, KmcLaunch);
 static KmcKernelFn KmcKernelFor(const KmcLaunch &l) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
   const int shape = threads <= kShapeThreads[0] ? 0 : (threads <= kShapeThreads[1] ? 1 : 2);
-  if (l.sparse) return shape == 0 ? kmc_kernel<true, 0> : (shape == 1 ? kmc_kernel<true, 1> : kmc_kernel<true, 2>);
-  return shape == 0 ? kmc_kernel<false, 0> : (shape == 1 ? kmc_kernel<false, 1> : kmc_kernel<false, 2>);
+  // the RNG kind is a template parameter so the Philox instances carry no mt19937_64 code (and back)
+  if (l.mt) {
+    if (l.sparse)
+      return shape == 0 ? kmc_kernel<true, 0, true> : (shape == 1 ? kmc_kernel<true, 1, true> : kmc_kernel<true, 2, true>);
+    return shape == 0 ? kmc_kernel<false, 0, true> : (shape == 1 ? kmc_kernel<false, 1, true> : kmc_kernel<false, 2, true>);
+  }
+  if (l.sparse)
+    return shape == 0 ? kmc_kernel<true, 0, false> : (shape == 1 ? kmc_kernel<true, 1, false> : kmc_kernel<true, 2, false>);
+  return shape == 0 ? kmc_kernel<false, 0, false> : (shape == 1 ? kmc_kernel<false, 1, false> : kmc_kernel<false, 2, false>);
 }
 
 cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes) {

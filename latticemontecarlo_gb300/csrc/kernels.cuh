@@ -91,6 +91,7 @@ struct KmcLaunch {
   volatile int *stop_flag;       // host-mapped, may be null
   int *status;                   // device status word (bit flags)
   int sparse;                    // 1: sparse solute corrections, 0: dense cluster sums
+  int mt;                        // 1: mt19937_64 stream (KmcDevState::rng_kind 0), 0: Philox
   KmcSparse sp;
 };
 
