@@ -2386,6 +2386,107 @@ __global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
   if (lane == 0) a.rng[2 * 312] = s_idx;
 }
 
+// The reference's mt19937_64 stream read by a whole warp: the current block of
+// 312 raw state words and the next one (twisted ahead, warp-parallel) sit in
+// shared memory, so any lane can read any of the next 312 or more outputs;
+// positions are consumed in order, as the serial generator would. Every lane
+// holds the same copy of this struct (warp-uniform calls only).
+struct MtWarp {
+  unsigned long long *cur, *nxt;  // raw words of the current and the following block
+  unsigned idx;                   // next unread position in cur (0..311)
+};
+__device__ __forceinline__ unsigned long long MtTemper(unsigned long long y) {
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  return y ^ (y >> 43);
+}
+// dst = the block after src (the serial in-place twist, split into its two
+// dependency-free halves: words 0-155 read only src, words 156-311 read dst 0-155).
+__device__ __forceinline__ void MtTwistWarp(const unsigned long long *src, unsigned long long *dst, int lane) {
+  constexpr unsigned long long kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL;
+  constexpr unsigned long long kA = 0xB5026F5AA96619E9ULL;
+  for (int k = lane; k < 156; k += 32) {
+    const unsigned long long x = (src[k] & kUpper) | (src[k + 1] & kLower);
+    dst[k] = src[k + 156] ^ (x >> 1) ^ ((x & 1ULL) ? kA : 0ULL);
+  }
+  __syncwarp();
+  for (int k = 156 + lane; k < 312; k += 32) {
+    const unsigned long long x = (src[k] & kUpper) | ((k + 1 < 312 ? src[k + 1] : dst[0]) & kLower);
+    dst[k] = dst[k - 156] ^ (x >> 1) ^ ((x & 1ULL) ? kA : 0ULL);
+  }
+  __syncwarp();
+}
+__device__ __forceinline__ unsigned long long MtWarpOut(const MtWarp &w, unsigned p) {
+  const unsigned q = w.idx + p;  // p < 312
+  return MtTemper(q < 312 ? w.cur[q] : w.nxt[q - 312]);
+}
+__device__ __forceinline__ void MtWarpAdvance(MtWarp &w, unsigned count, int lane) {
+  w.idx += count;  // count <= 312
+  if (w.idx >= 312) {
+    unsigned long long *tmp = w.cur;
+    w.cur = w.nxt;
+    w.nxt = tmp;
+    w.idx -= 312;
+    __syncwarp();
+    MtTwistWarp(w.cur, w.nxt, lane);
+  }
+}
+// uniform_int_distribution<size_t>(0, range - 1), one draw at a time (Lemire's rejection).
+__device__ __forceinline__ unsigned long long MtWarpBelow(MtWarp &w, unsigned long long range, int lane) {
+  unsigned long long x = MtWarpOut(w, 0);
+  MtWarpAdvance(w, 1, lane);
+  unsigned long long low = x * range;
+  if (low < range) {
+    const unsigned long long threshold = (0ULL - range) % range;
+    while (low < threshold) {
+      x = MtWarpOut(w, 0);
+      MtWarpAdvance(w, 1, lane);
+      low = x * range;
+    }
+  }
+  return __umul64hi(x, range);
+}
+// GenerateLatticeIdJumpPair on the stream: pairs of draws until the species differ.
+// Lanes 0-15 test the next 16 candidate pairs at once; the first different-species
+// candidate wins and exactly its draws and those before it are consumed. A draw that
+// Lemire's method would reject (probability below range / 2^64) shifts the pairing,
+// so from the first such candidate on the draws are taken one by one.
+__device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, unsigned long long range, int lane,
+                                           long long *l1, long long *l2) {
+  const unsigned long long threshold = (0ULL - range) % range;
+  const int k = lane & 15;
+  for (unsigned round = 0; round < (1u << 20); ++round) {
+    const unsigned long long x1 = MtWarpOut(w, 2 * k), x2 = MtWarpOut(w, 2 * k + 1);
+    const bool rej = x1 * range < threshold || x2 * range < threshold;
+    const long long a = static_cast<long long>(__umul64hi(x1, range)), b = static_cast<long long>(__umul64hi(x2, range));
+    const bool diff = species[a] != species[b];
+    const unsigned mrej = __ballot_sync(0xffffffffu, lane < 16 && rej);
+    const int r0 = mrej ? __ffs(mrej) - 1 : 16;
+    const unsigned mdiff = __ballot_sync(0xffffffffu, lane < 16 && diff) & ((1u << r0) - 1u);
+    if (mdiff) {
+      const int g = __ffs(mdiff) - 1;
+      *l1 = __shfl_sync(0xffffffffu, a, g);
+      *l2 = __shfl_sync(0xffffffffu, b, g);
+      MtWarpAdvance(w, 2 * (g + 1), lane);
+      return true;
+    }
+    if (r0 < 16) {
+      MtWarpAdvance(w, 2 * r0, lane);
+      const long long c1 = static_cast<long long>(MtWarpBelow(w, range, lane));
+      const long long c2 = static_cast<long long>(MtWarpBelow(w, range, lane));
+      if (species[c1] != species[c2]) {
+        *l1 = c1;
+        *l2 = c2;
+        return true;
+      }
+      continue;
+    }
+    MtWarpAdvance(w, 32, lane);
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------
 // K5c: simulated annealing (SimulatedAnnealing.cpp:99-185), one warp. Per step:
 // Dump's lowest-energy bookkeeping on the state before the step (:83-97), a
@@ -2409,102 +2510,103 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
     species = reinterpret_cast<int8_t *>((reinterpret_cast<size_t>(s.arr + 88) + 15) & ~size_t(15));
     for (long long i = threadIdx.x; i < nsites_ll; i += blockDim.x) species[i] = species_global[i];
   }
-  __shared__ unsigned long long s_mt[312];
-  __shared__ unsigned s_idx;
-  __shared__ long long s_pair[2];
-  __shared__ int s_stop;
+  __shared__ unsigned long long s_mt[2][312];
   StageArray(t.site_cl, s.cl, t.n_site_cl);
   StageArray(t.site_off, s.off, kSiteSites * 4);
   const unsigned long long *gmt = reinterpret_cast<const unsigned long long *>(a.rng);
-  for (int i = threadIdx.x; i < 312; i += blockDim.x) s_mt[i] = gmt[i];
-  if (threadIdx.x == 0) s_idx = a.rng[2 * 312];
+  for (int i = threadIdx.x; i < 312; i += blockDim.x) s_mt[0][i] = gmt[i];
   __syncthreads();
   const int lane = threadIdx.x;
-  const Mt mt{s_mt, &s_idx};
+  MtWarp mw{s_mt[0], s_mt[1], a.rng[2 * 312]};
+  if (mw.idx >= 312) {  // the serial generator twists on its next draw
+    MtTwistWarp(mw.cur, mw.nxt, lane);
+    unsigned long long *tmp = mw.cur;
+    mw.cur = mw.nxt;
+    mw.nxt = tmp;
+    mw.idx = 0;
+  }
+  MtTwistWarp(mw.cur, mw.nxt, lane);  // the following block, ready for reads past the current one
   const int n = a.n;
   const unsigned long long nsites = 4ULL * n * n * n;
   int8_t *sa = s.arr, *sb = sa + 44;
-  SaState st = *a.state;
+  SaState st = *a.state;  // every lane keeps the same copy; lane 0 writes memory
   unsigned bad = 0;
   for (unsigned long long it = 0; it < a.steps; ++it) {
-    if (lane == 0) {
-      s_stop = (a.stop_flag && (it & 255) == 0 && *a.stop_flag) ? 1 : 0;
-      // Dump: lowest-energy bookkeeping on the state before this step
-      if (st.energy < st.lowest - kSaEpsilon) st.lowest = st.energy;
-      long long l1 = 0, l2 = 0;
-      unsigned draws = 0;
-      do {  // GenerateLatticeIdJumpPair (the host rejects single-species lattices; the cap is a safety net)
-        l1 = static_cast<long long>(MtBelow(mt, nsites));
-        l2 = static_cast<long long>(MtBelow(mt, nsites));
-      } while (species[l1] == species[l2] && ++draws < (1u << 24));
-      if (species[l1] == species[l2]) {
-        bad |= kStatusNumeric;
-        s_stop = 1;
-      }
-      s_pair[0] = l1;
-      s_pair[1] = l2;
+    int stop = 0;
+    if (lane == 0) stop = (a.stop_flag && (it & 255) == 0 && *a.stop_flag) ? 1 : 0;
+    if (__shfl_sync(0xffffffffu, stop, 0)) {
+      bad |= kStatusStopped;
+      break;
     }
-    __syncwarp();
-    if (s_stop) {
-      if (!(bad & kStatusNumeric)) bad |= kStatusStopped;
+    // Dump: lowest-energy bookkeeping on the state before this step
+    if (st.energy < st.lowest - kSaEpsilon) st.lowest = st.energy;
+    long long l1 = 0, l2 = 0;
+    if (!MtWarpPair(mw, species, nsites, lane, &l1, &l2)) {  // the host rejects single-species lattices
+      bad |= kStatusNumeric;
       break;
     }
     int pa, pb;
-    GatherSwap(s.off, species, n, SiteCoord(s_pair[0], n), SiteCoord(s_pair[1], n), sa, sb, &pa, &pb, lane);
+    GatherSwap(s.off, species, n, SiteCoord(l1, n), SiteCoord(l2, n), sa, sb, &pa, &pb, lane);
     const long long acc_fx = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
-    if (lane == 0) {
-      const double dE = static_cast<double>(acc_fx) * t.de_scale;
-      const double e_before = st.energy, t_before = st.temperature;
-      bool accepted = dE < 0;
-      if (!accepted) accepted = MtUniform(mt) < exp(-dE * st.beta);
-      if (accepted) {
-        const long long l1 = s_pair[0], l2 = s_pair[1];
+    const double dE = static_cast<double>(acc_fx) * t.de_scale;
+    const double e_before = st.energy, t_before = st.temperature;
+    bool accepted = dE < 0;
+    if (!accepted) {
+      // generate_canonical<double, 53>: one draw scaled by 2^-64, 1 rounded down
+      const double u0 = __ull2double_rn(MtWarpOut(mw, 0)) * 5.421010862427522170e-20;
+      MtWarpAdvance(mw, 1, lane);
+      const double u = u0 >= 1.0 ? 0.99999999999999988898 : u0;
+      accepted = u < exp(-dE * st.beta);
+    }
+    __syncwarp();
+    if (accepted) {
+      if (lane == 0) {
         const int8_t v = species[l1];
         species[l1] = species[l2];
         species[l2] = v;
-        st.energy += dE;
       }
-      // UpdateTemperature(accepted)
-      ++st.window_trials;
-      if (accepted) {
-        ++st.window_accepts;
-        if (st.energy < st.recent_best - kSaEpsilon) {
-          st.recent_best = st.energy;
-          st.last_improvement = st.steps;
-        }
-      }
-      if (st.window_trials >= st.window_size) {
-        const double accr = static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials);
-        if (accr > 0.50) st.temperature *= 0.99;
-        st.window_trials = 0;
-        st.window_accepts = 0;
-      }
-      const double acc_est = st.window_trials > 0u
-                                 ? static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials)
-                                 : 1.0;
-      if (st.reheats_done < 5 && st.steps - st.last_improvement >= st.reheat_trigger &&
-          st.steps - st.last_reheat >= st.reheat_cooldown && acc_est < 0.05) {
-        st.temperature *= 1.10;
-        st.last_improvement = st.steps;
-        st.last_reheat = st.steps;
-        st.recent_best = st.energy;
-        ++st.reheats_done;
-      }
-      st.temperature *= exp(-3.0 / static_cast<double>(st.maximum_steps > 1ULL ? st.maximum_steps : 1ULL));
-      st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
-      if (a.trace) {
-        SaStepRec rec;
-        rec.site1 = s_pair[0];
-        rec.site2 = s_pair[1];
-        rec.accepted = accepted ? 1 : 0;
-        rec.pad = 0;
-        rec.de = dE;
-        rec.energy = e_before;
-        rec.temperature = t_before;
-        a.trace[it] = rec;
-      }
-      ++st.steps;
+      st.energy += dE;
     }
+    // UpdateTemperature(accepted)
+    ++st.window_trials;
+    if (accepted) {
+      ++st.window_accepts;
+      if (st.energy < st.recent_best - kSaEpsilon) {
+        st.recent_best = st.energy;
+        st.last_improvement = st.steps;
+      }
+    }
+    if (st.window_trials >= st.window_size) {
+      const double accr = static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials);
+      if (accr > 0.50) st.temperature *= 0.99;
+      st.window_trials = 0;
+      st.window_accepts = 0;
+    }
+    const double acc_est = st.window_trials > 0u
+                               ? static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials)
+                               : 1.0;
+    if (st.reheats_done < 5 && st.steps - st.last_improvement >= st.reheat_trigger &&
+        st.steps - st.last_reheat >= st.reheat_cooldown && acc_est < 0.05) {
+      st.temperature *= 1.10;
+      st.last_improvement = st.steps;
+      st.last_reheat = st.steps;
+      st.recent_best = st.energy;
+      ++st.reheats_done;
+    }
+    st.temperature *= exp(-3.0 / static_cast<double>(st.maximum_steps > 1ULL ? st.maximum_steps : 1ULL));
+    st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
+    if (a.trace && lane == 0) {
+      SaStepRec rec;
+      rec.site1 = l1;
+      rec.site2 = l2;
+      rec.accepted = accepted ? 1 : 0;
+      rec.pad = 0;
+      rec.de = dE;
+      rec.energy = e_before;
+      rec.temperature = t_before;
+      a.trace[it] = rec;
+    }
+    ++st.steps;
     __syncwarp();
   }
   if (lane == 0) {
@@ -2515,8 +2617,8 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
   if (local_lattice)
     for (long long i = lane; i < nsites_ll; i += 32) species_global[i] = species[i];
   unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
-  for (int i = lane; i < 312; i += 32) gw[i] = s_mt[i];
-  if (lane == 0) a.rng[2 * 312] = s_idx;
+  for (int i = lane; i < 312; i += 32) gw[i] = mw.cur[i];
+  if (lane == 0) a.rng[2 * 312] = mw.idx;
 }
 
 // ---------------------------------------------------------------------------
