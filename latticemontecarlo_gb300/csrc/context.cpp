@@ -102,7 +102,7 @@ struct lmc_ctx {
   int sparse_base{-1};  // base species the sparse tables were built for (-1: none)
   lmc::KmcSparse sparse{};
   // CMC
-  DevBuf c_mark, c_mark_list, c_claim, c_cand, c_eacc, c_stats;
+  DevBuf c_claim, c_cand, c_eacc, c_stats;
   std::map<int, std::pair<uint64_t, DevBuf>> c_mt;  // per replica: seed and MT state
   // host-mapped stop flag
   int *h_stop{nullptr};
@@ -129,7 +129,7 @@ struct lmc_ctx {
     for (DevBuf *b : {&species, &lat_off, &lat_n, &scan, &scan_first, &pairs, &out0, &out1, &out2, &out3, &status, &counts, &energy, &enc,
                       &k_vac, &k_steps, &k_time, &k_energy, &k_temp, &k_cvac, &k_csol, &k_rng, &k_trace, &k_events,
                       &k_tt_time, &k_tt_temp, &k_solvent, &k_escaped, &k_prev, &c_trace, &s_feat, &s_mean, &s_spread,
-                      &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_mark, &c_mark_list, &c_claim, &c_cand, &c_eacc, &c_stats})
+                      &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace, &sa_state, &sa_rng,
                       &sa_trace})
@@ -2167,19 +2167,12 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
         CudaCheck(cudaMemcpy(slot.second.p, w.data(), sizeof(uint32_t) * lmc::kRngWords, cudaMemcpyHostToDevice), "H2D");
         slot.first = opt->seed;
       }
-      if (ctx->c_mark.bytes < static_cast<size_t>(nsites)) {
-        ctx->c_mark.Alloc(nsites);
-        CudaCheck(cudaMemset(ctx->c_mark.p, 0, nsites), "memset");
-      }
-      ctx->c_mark_list.Ensure(sizeof(long long) * 86 * opt->batch);
       lmc::CmcRefArgs a{};
       a.n = n;
       a.beta = beta;
       a.attempts = attempts;
       a.batch = opt->batch;
       a.rng = slot.second.as<uint32_t>();
-      a.mark = ctx->c_mark.as<unsigned char>();
-      a.mark_list = ctx->c_mark_list.as<long long>();
       a.energy = d_energy;
       a.done = d_done;
       a.accepted = d_done + 1;

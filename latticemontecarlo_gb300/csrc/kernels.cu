@@ -40,12 +40,14 @@ struct H3 {
 };
 
 __device__ __forceinline__ H3 SiteCoord(long long id, int n) {
-  const long long plane = 2LL * n * n;
-  const int hx = static_cast<int>(id / plane);
-  const long long r = id - static_cast<long long>(hx) * plane;
-  const int hy = static_cast<int>(r / n);
-  const int k = static_cast<int>(r - static_cast<long long>(hy) * n);
-  return {hx, hy, 2 * k + ((hx + hy) & 1)};
+  // 32-bit unsigned arithmetic: supercells have n <= 1000, so 4 n^3 < 2^32
+  const unsigned u = static_cast<unsigned>(id), nn = static_cast<unsigned>(n);
+  const unsigned plane = 2u * nn * nn;
+  const unsigned hx = u / plane;
+  const unsigned r = u - hx * plane;
+  const unsigned hy = r / nn;
+  const unsigned k = r - hy * nn;
+  return {static_cast<int>(hx), static_cast<int>(hy), static_cast<int>(2 * k + ((hx + hy) & 1u))};
 }
 
 // Id of h + (dx, dy, dz) with periodic wrap; |offset| <= 4 < 2n.
@@ -2267,125 +2269,7 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
 }
 
-// ---------------------------------------------------------------------------
-// K5a: CanonicalMcOmp batch semantics on the reference's RNG stream (one warp).
-// Batch build (CanonicalMcOmp.cpp:40-79): up to `batch` pairs; each pair is
-// redrawn until both sites are outside the exclusion set (1-3NN of chosen
-// sites), giving up the batch after 50 tries; pair draws repeat until the two
-// species differ (CanonicalMcAbstract.cpp:43-51). dE of all pairs on the
-// unchanged lattice, then sequential Metropolis (CanonicalMcAbstract.cpp:86-101).
-// ---------------------------------------------------------------------------
 constexpr int kCmcRefMaxBatch = 256;
-__global__ void cmc_ref_kernel(DevTables t, int8_t *species, CmcRefArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const SiteSmem s = CarveSiteSmem(t, smem);
-  __shared__ unsigned long long s_mt[312];
-  __shared__ unsigned s_idx;
-  __shared__ long long s_pair[kCmcRefMaxBatch][2];
-  __shared__ double s_de[kCmcRefMaxBatch];
-  __shared__ int s_nb;
-  StageArray(t.site_cl, s.cl, t.n_site_cl);
-  StageArray(t.site_off, s.off, kSiteSites * 4);
-  const unsigned long long *gmt = reinterpret_cast<const unsigned long long *>(a.rng);
-  for (int i = threadIdx.x; i < 312; i += blockDim.x) s_mt[i] = gmt[i];
-  if (threadIdx.x == 0) s_idx = a.rng[2 * 312];
-  __syncthreads();
-  const int lane = threadIdx.x;
-  const Mt mt{s_mt, &s_idx};
-  const int n = a.n;
-  const unsigned long long nsites = 4ULL * n * n * n;
-  int8_t *sa = s.arr, *sb = sa + 44;
-  double energy = *a.energy;
-  unsigned long long done = 0, accepted = 0;
-  long long nmark = 0;
-  while (done < a.attempts) {
-    if (lane == 0) {
-      int nb = 0;
-      nmark = 0;
-      for (int i = 0; i < a.batch; ++i) {
-        int ct = 0;
-        long long l1, l2;
-        bool exhausted = false;
-        for (;;) {
-          // GenerateLatticeIdJumpPair: redraw until the species differ (bounded:
-          // the host rejects single-species lattices, the cap is a safety net)
-          unsigned draws = 0;
-          do {
-            l1 = static_cast<long long>(MtBelow(mt, nsites));
-            l2 = static_cast<long long>(MtBelow(mt, nsites));
-          } while (species[l1] == species[l2] && ++draws < (1u << 24));
-          if (species[l1] == species[l2]) {
-            exhausted = true;
-            break;
-          }
-          ++ct;
-          if (ct == 50) break;
-          if (!a.mark[l1] && !a.mark[l2]) break;
-        }
-        if (exhausted) {
-          atomicOr(a.status, kStatusNumeric);
-          break;
-        }
-        if (ct == 50) break;
-        for (const long long c : {l1, l2}) {
-          const H3 h = SiteCoord(c, n);
-          for (int k = 0; k < kSiteSites; ++k) {
-            const int8_t *o = s.off + k * 4;
-            const long long id = NeighborId(h, o[0], o[1], o[2], n);
-            if (!a.mark[id]) {
-              a.mark[id] = 1;
-              a.mark_list[nmark++] = id;
-            }
-          }
-        }
-        s_pair[nb][0] = l1;
-        s_pair[nb][1] = l2;
-        ++nb;
-      }
-      s_nb = nb;
-    }
-    __syncwarp();
-    const int nb = s_nb;
-    for (int i = 0; i < nb; ++i) {
-      int pa, pb;
-      GatherSwap(s.off, species, n, SiteCoord(s_pair[i][0], n), SiteCoord(s_pair[i][1], n), sa, sb, &pa, &pb, lane);
-      const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
-      if (lane == 0) s_de[i] = static_cast<double>(acc) * t.de_scale;
-      __syncwarp();
-    }
-    if (lane == 0) {
-      for (int i = 0; i < nb; ++i) {
-        const double dE = s_de[i];
-        if (a.energy_trace) a.energy_trace[done] = energy;
-        bool acc = dE < 0;
-        if (!acc) acc = MtUniform(mt) < exp(-dE * a.beta);
-        if (acc) {
-          const long long l1 = s_pair[i][0], l2 = s_pair[i][1];
-          const int8_t v = species[l1];
-          species[l1] = species[l2];
-          species[l2] = v;
-          energy += dE;
-          ++accepted;
-        }
-        ++done;
-      }
-      for (long long q = 0; q < nmark; ++q) a.mark[a.mark_list[q]] = 0;
-      if (nb == 0) done = a.attempts;  // no pair could be placed: stop rather than spin
-    }
-    done = __shfl_sync(0xffffffffu, done, 0);
-    __syncwarp();
-  }
-  if (lane == 0) {
-    *a.energy = energy;
-    *a.done = done;
-    *a.accepted = accepted;
-  }
-  __syncwarp();
-  unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
-  for (int i = lane; i < 312; i += 32) gw[i] = s_mt[i];
-  if (lane == 0) a.rng[2 * 312] = s_idx;
-}
-
 // The reference's mt19937_64 stream read by a whole warp: the current block of
 // 312 raw state words and the next one (twisted ahead, warp-parallel) sit in
 // shared memory, so any lane can read any of the next 312 or more outputs;
@@ -2452,9 +2336,9 @@ __device__ __forceinline__ unsigned long long MtWarpBelow(MtWarp &w, unsigned lo
 // candidate wins and exactly its draws and those before it are consumed. A draw that
 // Lemire's method would reject (probability below range / 2^64) shifts the pairing,
 // so from the first such candidate on the draws are taken one by one.
-__device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, unsigned long long range, int lane,
-                                           long long *l1, long long *l2) {
-  const unsigned long long threshold = (0ULL - range) % range;
+// `threshold` = (2^64 - range) mod range, Lemire's rejection bound (hoisted out of the loops).
+__device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, unsigned long long range,
+                                           unsigned long long threshold, int lane, long long *l1, long long *l2) {
   const int k = lane & 15;
   for (unsigned round = 0; round < (1u << 20); ++round) {
     const unsigned long long x1 = MtWarpOut(w, 2 * k), x2 = MtWarpOut(w, 2 * k + 1);
@@ -2485,6 +2369,161 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
     MtWarpAdvance(w, 32, lane);
   }
   return false;
+}
+
+// ---------------------------------------------------------------------------
+// K5a: CanonicalMcOmp (CanonicalMcOmp.cpp:40-92, CanonicalMcAbstract.cpp:43-101)
+// in its exact order, one block. Warp 0 reads the mt19937_64 stream as a warp and
+// builds the batch: each pair is redrawn until both sites lie outside the 1-3NN
+// shells (site included) of the sites already chosen, the batch given up after 50
+// tries. The shells are not marked on a lattice-sized array: on an FCC supercell
+// with n >= 6 a site lies in the shell of c exactly when its minimum-image
+// displacement from c has squared length <= 6 (half units: 1NN 2, 2NN 4, 3NN 6,
+// 4NN 8), so the lanes test the candidates against the chosen sites directly.
+// The block's warps then compute the batch's dE values (and the Metropolis
+// factors) on the unchanged lattice, one pair per warp, as the reference's OpenMP
+// threads do; warp 0 runs the Metropolis tests in batch order.
+// ---------------------------------------------------------------------------
+constexpr int kCmcRefWarps = 8;
+// Lattices up to this many sites are copied into shared memory for the launch.
+constexpr long long kCmcRefSmemSites = 192 * 1024;
+__device__ __forceinline__ bool CmcRefNear(H3 a, H3 b, int n) {
+  const int dx = WrapDelta(a.x - b.x, n), dy = WrapDelta(a.y - b.y, n), dz = WrapDelta(a.z - b.z, n);
+  return dx * dx + dy * dy + dz * dz <= 6;
+}
+__global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables t, int8_t *species_global, CmcRefArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  __shared__ unsigned long long s_mt[2][312];
+  __shared__ long long s_pair[kCmcRefMaxBatch][2];
+  __shared__ H3 s_h[2 * kCmcRefMaxBatch];
+  __shared__ double s_de[kCmcRefMaxBatch], s_p[kCmcRefMaxBatch];
+  __shared__ int s_nb, s_fail, s_stop;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = a.n;
+  const long long nsites_ll = 4LL * n * n * n;
+  const unsigned long long nsites = static_cast<unsigned long long>(nsites_ll);
+  const unsigned long long threshold = (0ULL - nsites) % nsites;
+  const bool local_lattice = nsites_ll <= kCmcRefSmemSites;
+  int8_t *species = species_global;
+  if (local_lattice) {
+    // after the site tables and the warps' 2 x 44 arrays (the layout SiteSmemBytes(t, kCmcRefWarps) sizes)
+    species = reinterpret_cast<int8_t *>((reinterpret_cast<size_t>(s.arr + 88 * kCmcRefWarps) + 15) & ~size_t(15));
+    for (long long k = threadIdx.x; k < nsites_ll; k += blockDim.x) species[k] = species_global[k];
+  }
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  const unsigned long long *gmt = reinterpret_cast<const unsigned long long *>(a.rng);
+  for (int k = threadIdx.x; k < 312; k += blockDim.x) s_mt[0][k] = gmt[k];
+  __syncthreads();
+  MtWarp mw{s_mt[0], s_mt[1], a.rng[2 * 312]};
+  if (warp == 0) {
+    if (mw.idx >= 312) {  // the serial generator twists on its next draw
+      MtTwistWarp(mw.cur, mw.nxt, lane);
+      unsigned long long *tmp = mw.cur;
+      mw.cur = mw.nxt;
+      mw.nxt = tmp;
+      mw.idx = 0;
+    }
+    MtTwistWarp(mw.cur, mw.nxt, lane);
+  }
+  int8_t *sa = s.arr + warp * 88, *sb = sa + 44;
+  double energy = *a.energy;  // kept by warp 0, every lane the same copy
+  unsigned long long done = 0, accepted = 0;
+  bool stop = a.attempts == 0;
+  while (!stop) {
+    if (warp == 0) {
+      int nb = 0;
+      bool failed = false;
+      for (int i = 0; i < a.batch; ++i) {
+        long long l1 = 0, l2 = 0;
+        H3 h1{}, h2{};
+        int ct = 0;
+        for (;;) {
+          // GenerateLatticeIdJumpPair (the host rejects single-species lattices)
+          if (!MtWarpPair(mw, species, nsites, threshold, lane, &l1, &l2)) {
+            failed = true;
+            break;
+          }
+          ++ct;
+          if (ct == 50) break;
+          h1 = SiteCoord(l1, n);
+          h2 = SiteCoord(l2, n);
+          bool hit = false;
+          for (int j = lane; j < 2 * nb; j += 32) hit |= CmcRefNear(h1, s_h[j], n) || CmcRefNear(h2, s_h[j], n);
+          if (!__any_sync(0xffffffffu, hit)) break;
+        }
+        if (failed || ct == 50) break;
+        if (lane == 0) {
+          s_pair[nb][0] = l1;
+          s_pair[nb][1] = l2;
+          s_h[2 * nb] = h1;
+          s_h[2 * nb + 1] = h2;
+        }
+        __syncwarp();
+        ++nb;
+      }
+      if (lane == 0) {
+        s_nb = nb;
+        s_fail = failed;
+        if (failed) atomicOr(a.status, kStatusNumeric);
+      }
+    }
+    __syncthreads();
+    if (s_fail) break;
+    const int nb = s_nb;
+    for (int i = warp; i < nb; i += kCmcRefWarps) {
+      int pa, pb;
+      GatherSwap(s.off, species, n, s_h[2 * i], s_h[2 * i + 1], sa, sb, &pa, &pb, lane);
+      const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
+      if (lane == 0) {
+        const double dE = static_cast<double>(acc) * t.de_scale;
+        s_de[i] = dE;
+        s_p[i] = dE < 0 ? 1.0 : exp(-dE * a.beta);
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int i = 0; i < nb; ++i) {
+        const double dE = s_de[i];
+        if (a.energy_trace && lane == 0) a.energy_trace[done] = energy;
+        bool acc = dE < 0;
+        if (!acc) {
+          const double u0 = __ull2double_rn(MtWarpOut(mw, 0)) * 5.421010862427522170e-20;  // 2^-64
+          MtWarpAdvance(mw, 1, lane);
+          acc = (u0 >= 1.0 ? 0.99999999999999988898 : u0) < s_p[i];
+        }
+        if (acc) {
+          if (lane == 0) {
+            const long long l1 = s_pair[i][0], l2 = s_pair[i][1];
+            const int8_t v = species[l1];
+            species[l1] = species[l2];
+            species[l2] = v;
+          }
+          energy += dE;
+          ++accepted;
+        }
+        ++done;
+      }
+      if (nb == 0) done = a.attempts;  // no pair could be placed: stop rather than spin
+      if (lane == 0) s_stop = done >= a.attempts;
+    }
+    __syncthreads();
+    stop = s_stop;
+  }
+  if (threadIdx.x == 0) {
+    *a.energy = energy;
+    *a.done = done;
+    *a.accepted = accepted;
+  }
+  __syncthreads();
+  if (local_lattice)
+    for (long long k = threadIdx.x; k < nsites_ll; k += blockDim.x) species_global[k] = species[k];
+  if (warp == 0) {
+    unsigned long long *gw = reinterpret_cast<unsigned long long *>(a.rng);
+    for (int k = lane; k < 312; k += 32) gw[k] = mw.cur[k];
+    if (lane == 0) a.rng[2 * 312] = mw.idx;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2528,6 +2567,7 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
   MtTwistWarp(mw.cur, mw.nxt, lane);  // the following block, ready for reads past the current one
   const int n = a.n;
   const unsigned long long nsites = 4ULL * n * n * n;
+  const unsigned long long threshold = (0ULL - nsites) % nsites;
   int8_t *sa = s.arr, *sb = sa + 44;
   SaState st = *a.state;  // every lane keeps the same copy; lane 0 writes memory
   unsigned bad = 0;
@@ -2541,7 +2581,7 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
     // Dump: lowest-energy bookkeeping on the state before this step
     if (st.energy < st.lowest - kSaEpsilon) st.lowest = st.energy;
     long long l1 = 0, l2 = 0;
-    if (!MtWarpPair(mw, species, nsites, lane, &l1, &l2)) {  // the host rejects single-species lattices
+    if (!MtWarpPair(mw, species, nsites, threshold, lane, &l1, &l2)) {  // the host rejects single-species lattices
       bad |= kStatusNumeric;
       break;
     }
@@ -3057,9 +3097,13 @@ cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiAr
 }
 
 cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream) {
-  if (a.batch < 1 || a.batch > kCmcRefMaxBatch) return cudaErrorInvalidValue;
-  const size_t sm = SiteSmemBytes(t, 1);
-  cmc_ref_kernel<<<1, 32, sm, stream>>>(t, species, a);
+  if (a.batch < 1 || a.batch > kCmcRefMaxBatch || a.n < 6) return cudaErrorInvalidValue;
+  const long long nsites = 4LL * a.n * a.n * a.n;
+  const size_t sm = SiteSmemBytes(t, kCmcRefWarps) + (nsites <= kCmcRefSmemSites ? static_cast<size_t>(nsites) : 0);
+  cudaError_t err = cudaFuncSetAttribute(cmc_ref_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  cmc_ref_kernel<<<1, kCmcRefWarps * 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

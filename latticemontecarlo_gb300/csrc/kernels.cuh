@@ -191,15 +191,13 @@ cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, lon
 // Resident blocks per SM and dynamic shared memory of the KMC launch `l`.
 cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes);
 
-// Reference-batch CMC (one warp, mt19937_64 stream, batch = `batch` pairs).
+// Reference-batch CMC (one block, mt19937_64 stream, batch = `batch` pairs, n >= 6).
 struct CmcRefArgs {
   int n;
   double beta;
   unsigned long long attempts;
   int batch;
   uint32_t *rng;             // MT state
-  unsigned char *mark;       // N bytes scratch, zero on entry and on exit
-  long long *mark_list;      // batch * 86 entries scratch
   double *energy;            // in/out
   double *energy_trace;      // optional: energy before every test (attempts + batch entries)
   unsigned long long *done;  // attempts done
