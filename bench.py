@@ -286,12 +286,24 @@ def run_cmc(args, device, flush, barrier):
     barrier()
     value = done_total / (np.sum(ms) / 1e3)
     peak, _ = peaks()
-    return {"value": value, "unit": "swaps/s (Metropolis attempts)",
-            "workload": "CMC 30^3 FCC (108000 sites), Al/Mg/Zn/Cu .94/.02/.02/.02, T=500 K, "
-                        f"{args.cmc_sweeps_per_step} sweeps per step, non-overlapping pairs per round",
-            "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
-            "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
-                         "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+    out = {"value": value, "unit": "swaps/s (Metropolis attempts)",
+           "workload": "CMC 30^3 FCC (108000 sites), Al/Mg/Zn/Cu .94/.02/.02/.02, T=500 K, "
+                       f"{args.cmc_sweeps_per_step} sweeps per step, non-overlapping pairs per round",
+           "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
+           "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
+    if args.cmc_ref_attempts > 0:
+        # CanonicalMcOmp's own order on its mt19937_64 stream (what the host executable runs), with the
+        # batch the CPU baseline's OpenMP threads give
+        batch = min(256, os.cpu_count() or 1)
+        e, _, _ = ctx.cmc_run(cfg["T"], 20_000, mode=N.LMC_CMC_REFERENCE_BATCH, seed=1, batch=batch, energy=e)
+        e, done, _ = ctx.cmc_run(cfg["T"], args.cmc_ref_attempts, mode=N.LMC_CMC_REFERENCE_BATCH, seed=2,
+                                 batch=batch, energy=e)
+        ms_ref = ctx.last_run_ms()
+        out["reference_batch"] = {"value": done / (ms_ref / 1e3), "unit": "swaps/s (Metropolis attempts)",
+                                  "batch": batch, "attempts": int(done), "ms": ms_ref,
+                                  "workload": "the same lattice, CanonicalMcOmp batch order and RNG stream"}
+    return out
 
 
 def run_single(args, device):
@@ -695,6 +707,8 @@ def main():
     ap.add_argument("--cmc-sweeps-per-step", type=int, default=2)
     ap.add_argument("--cpu-kmc-steps", type=int, default=6000)
     ap.add_argument("--cpu-cmc-attempts", type=int, default=1_500_000)
+    ap.add_argument("--cmc-ref-attempts", type=int, default=400_000,
+                    help="attempts of the reference-order CMC kernel (0 skips)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
     ap.add_argument("--surrogate-epochs", type=int, default=30)
