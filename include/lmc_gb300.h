@@ -196,7 +196,7 @@ int lmc_fastmath_check(lmc_ctx *ctx, int fn, const double *x, int64_t n, double 
 
 /* ------------------------------------------------------------------------- */
 /* Learned barrier surrogate (no reference counterpart: the plain predictor    */
-/* above is its fallback and the judge of its error)                          */
+/* above is its fallback and the yardstick of its error)                      */
 /* ------------------------------------------------------------------------- */
 /* Ensemble of `members` MLPs in -> hidden -> hidden -> 1 (GELU), BF16 weights and
  * activations on the tensor cores, FP32 accumulation, FP32 master weights, Adam.
@@ -386,7 +386,7 @@ int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double 
 /* Canonical MC (CanonicalMcOmp semantics, CanonicalMcOmp.cpp:40-92)          */
 /* ------------------------------------------------------------------------- */
 #define LMC_CMC_REFERENCE_BATCH 0 /* mt19937_64 stream, batch of `batch` pairs as the reference draws them */
-#define LMC_CMC_THROUGHPUT 1      /* Philox, many non-overlapping pairs per round (see DESIGN) */
+#define LMC_CMC_THROUGHPUT 1      /* Philox, many pairs per round, kept when more than 3NN apart */
 
 typedef struct lmc_cmc_options {
   int mode;          /* LMC_CMC_* */
