@@ -346,7 +346,7 @@ int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
 int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy);
 
 /* ------------------------------------------------------------------------- */
-/* Vacancy placed on every site: ExitTime's barrier queries (a next row)      */
+/* Vacancy placed on every site: ExitTime's barrier queries (ansys)          */
 /* ------------------------------------------------------------------------- */
 /* ansys::ExitTime::GetJumpEnergetics (ExitTime.cpp:257-310) and GetBarrierListAndExitTime
  * (:217-255) in one pass: the lattice's own vacancy (its first X) gets `solvent_code`, then for
@@ -358,6 +358,30 @@ int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, d
 int lmc_site_jump_energetics(lmc_ctx *ctx, int replica, int kind, int solvent_code, double escape_temperature,
                              const int64_t *sites, int64_t m, double *ea12, double *de12, int64_t *nb12,
                              double *average, double *exit_time);
+
+/* ------------------------------------------------------------------------- */
+/* Solute clusters (ansys::SoluteCluster)                                     */
+/* ------------------------------------------------------------------------- */
+/* ansys::SoluteCluster::FindAtomListOfClusters (SoluteCluster.cpp:277-373) on lattice `replica`:
+ * the 1NN-connected components of the sites whose species is not `solvent_code` (vacancies
+ * included), those with fewer than `smallest` sites dropped; a component of more than
+ * `solvent_bond` sites gains every site of its 1NN shell that has more than `solvent_bond` 1NN
+ * bonds to its non-solvent sites (such a solvent site may join several clusters). Clusters are
+ * ordered by size, larger first, equal sizes by their smallest site id (the reference leaves
+ * that order to std::sort over hash-set order); members are sorted by id. With
+ * `chemical_potential` (per species code, as EnergyPredictor::GetChemicalPotential; NULL skips
+ * it) each cluster also gets SoluteCluster::GetFormationEnergy (:395-410): GetEnergyOfCluster
+ * (EnergyPredictor.cpp:97-184) with the members' species on a solvent background minus that of
+ * the pure solvent, minus the members' chemical potentials (a cluster of the census holding two
+ * vacancies counts nothing, where the reference's ClusterIndexer throws). The results are kept in the context:
+ * num_clusters and num_members size the buffers of lmc_solute_cluster_get. Components are found
+ * by union-find on the GPU, the energies by one GPU block per cluster. */
+int lmc_solute_clusters(lmc_ctx *ctx, int replica, int solvent_code, int64_t smallest, int64_t solvent_bond,
+                        const double *chemical_potential, int64_t *num_clusters, int64_t *num_members);
+/* Copies the last lmc_solute_clusters result (host pointers, any may be NULL): offsets
+ * [num_clusters + 1], members [num_members], formation_energy [num_clusters] (NaN without
+ * chemical potentials). */
+int lmc_solute_cluster_get(lmc_ctx *ctx, int64_t *offsets, int64_t *members, double *formation_energy);
 
 /* ------------------------------------------------------------------------- */
 /* Simulated annealing (SimulatedAnnealing.cpp:99-185, a next row of the path) */

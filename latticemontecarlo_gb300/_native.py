@@ -154,6 +154,8 @@ SIGNATURES = {
     "lmc_sa_init": (C.c_int, [_P, C.c_int, C.c_uint64, C.c_uint64, C.c_double, C.c_double]),
     "lmc_site_jump_energetics": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_double, _I64P, C.c_int64, _DP, _DP,
                                            _I64P, _DP, _DP]),
+    "lmc_solute_clusters": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64, C.c_int64, _DP, _I64P, _I64P]),
+    "lmc_solute_cluster_get": (C.c_int, [_P, _I64P, _I64P, _DP]),
     "lmc_sa_run": (C.c_int, [_P, C.c_uint64, _P]),
     "lmc_sa_get_state": (C.c_int, [_P, _U64P, _DP, _DP, _DP]),
     "lmc_kmc_multi_init": (C.c_int, [_P, _DP, C.c_uint64, C.c_int, C.c_int]),

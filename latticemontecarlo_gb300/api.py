@@ -237,6 +237,37 @@ class Context:
                                              ptr(avg, C.c_double), ptr(ext, C.c_double)))
         return ea, de, nb, avg, ext
 
+    # solute clusters ------------------------------------------------------
+    def chemical_potential(self, solvent: int):
+        """EnergyPredictor::GetChemicalPotential (EnergyPredictor.cpp:196-214): per species code, the
+        energy of a 15^3-cell solvent lattice with one site of that species minus the pure
+        solvent's (0 for the solvent), from the GPU census."""
+        alpha = self.model.alphabet
+        side = Context(self.model, device=self.device)
+        lat = np.full(4 * 15 ** 3, solvent, np.int8)
+        lats = []
+        for code in range(len(alpha)):
+            one = lat.copy()
+            one[0] = code
+            lats.append(one)
+        side.set_lattices([15] * len(alpha), np.concatenate(lats))
+        pure = side.energy(solvent)[0]
+        return np.array([0.0 if c == solvent else side.energy(c)[0] - pure for c in range(len(alpha))])
+
+    def solute_clusters(self, solvent: int, smallest: int = 1, solvent_bond: int = 12, chemical_potential=None,
+                        replica: int = 0):
+        """ansys::SoluteCluster's clusters of lattice `replica` (sorted site-id arrays, larger clusters
+        first) and their formation energies (NaN without chemical potentials)."""
+        k, nm = C.c_int64(), C.c_int64()
+        mu = None if chemical_potential is None else np.ascontiguousarray(chemical_potential, np.float64)
+        check(N.lib.lmc_solute_clusters(self._h, replica, solvent, smallest, solvent_bond,
+                                        ptr(mu, C.c_double) if mu is not None else None, C.byref(k), C.byref(nm)))
+        off = np.zeros(k.value + 1, np.int64)
+        mem = np.zeros(max(nm.value, 1), np.int64)
+        ef = np.zeros(max(k.value, 1))
+        check(N.lib.lmc_solute_cluster_get(self._h, ptr(off, C.c_int64), ptr(mem, C.c_int64), ptr(ef, C.c_double)))
+        return [mem[off[i]:off[i + 1]].copy() for i in range(k.value)], ef[:k.value].copy()
+
     # simulated annealing --------------------------------------------------
     SA_DTYPE = np.dtype([("site1", np.int64), ("site2", np.int64), ("accepted", np.int32), ("pad", np.int32),
                          ("de", np.float64), ("energy", np.float64), ("temperature", np.float64)])

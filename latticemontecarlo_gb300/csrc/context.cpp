@@ -113,6 +113,9 @@ struct lmc_ctx {
   cudaGraphExec_t kmc_graph{nullptr};
   std::vector<unsigned char> kmc_graph_key;
   int *h_status{nullptr};
+  // solute clusters of the last lmc_solute_clusters call (CSR lists, formation energies)
+  std::vector<int64_t> cl_offsets, cl_members;
+  std::vector<double> cl_energy;
   // simulated annealing on one lattice
   bool sa_ready{false};
   int sa_replica{0};
@@ -2029,6 +2032,148 @@ int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double 
     if (temperature) *temperature = st.temperature;
     if (energy) *energy = st.energy;
     if (lowest_energy) *lowest_energy = st.lowest;
+  });
+}
+
+int lmc_solute_clusters(lmc_ctx *ctx, int replica, int solvent_code, int64_t smallest, int64_t solvent_bond,
+                        const double *chemical_potential, int64_t *num_clusters, int64_t *num_members) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    ctx->CheckReplica(replica);
+    Require(solvent_code >= 0 && solvent_code < ctx->fm.num_species && solvent_code != ctx->fm.x_code,
+            LMC_ERR_INVALID_ARGUMENT, "solvent code out of range");
+    Require(smallest >= 0 && solvent_bond >= 0, LMC_ERR_INVALID_ARGUMENT, "criteria must be >= 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int n = ctx->n[replica];
+    const long long nsites = 4LL * n * n * n;
+    const int8_t *d_sp = ctx->species.as<int8_t>() + ctx->offsets[replica];
+    // components of the non-solvent sites on the GPU
+    DevBuf parent;
+    parent.Alloc(sizeof(uint32_t) * nsites);
+    ctx->ClearStatus();
+    CudaCheck(lmc::LaunchSoluteLabels(ctx->t, d_sp, n, solvent_code, parent.as<uint32_t>(), ctx->status.as<int>(),
+                                      ctx->stream),
+              "cluster label kernels");
+    std::vector<uint32_t> root(nsites);
+    std::vector<int8_t> sp(nsites);
+    CudaCheck(cudaMemcpyAsync(root.data(), parent.p, sizeof(uint32_t) * nsites, cudaMemcpyDeviceToHost, ctx->stream),
+              "D2H");
+    CudaCheck(cudaMemcpyAsync(sp.data(), d_sp, nsites, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    RaiseStatus(ctx->ReadStatus(), "solute clusters");
+    // SoluteCluster::FindAtomListOfClusters (SoluteCluster.cpp:324-372): the components, those
+    // smaller than `smallest` dropped; a component of more than `solvent_bond` sites gains every
+    // 1NN-shell site with more than `solvent_bond` bonds to it
+    std::vector<std::pair<uint32_t, uint32_t>> by_root;
+    for (long long i = 0; i < nsites; ++i)
+      if (root[i] != 0xFFFFFFFFu) by_root.emplace_back(root[i], static_cast<uint32_t>(i));
+    std::sort(by_root.begin(), by_root.end());
+    lmc::Fcc fcc{n};
+    const auto &nn1 = lmc::ShellOffsets(1);
+    std::vector<std::vector<int64_t>> clusters;
+    std::vector<int> mark(nsites, -1);
+    for (size_t a = 0; a < by_root.size();) {
+      size_t b = a;
+      while (b < by_root.size() && by_root[b].first == by_root[a].first) ++b;
+      const int64_t size = static_cast<int64_t>(b - a);
+      if (size >= smallest) {
+        const int id = static_cast<int>(clusters.size());
+        std::vector<int64_t> c;
+        for (size_t q = a; q < b; ++q) c.push_back(by_root[q].second), mark[by_root[q].second] = id;
+        if (size > solvent_bond) {
+          for (int64_t q = 0; q < size; ++q) {
+            const lmc::I3 h = fcc.Coord(c[q]);
+            for (const auto &o : nn1) {
+              const int64_t x = fcc.Id(fcc.Wrap(h + o));
+              if (mark[x] == id) continue;
+              const lmc::I3 hx = fcc.Coord(x);
+              int64_t bonds = 0;
+              for (const auto &o2 : nn1) {
+                const int64_t y = fcc.Id(fcc.Wrap(hx + o2));
+                bonds += mark[y] == id && sp[y] != solvent_code;
+              }
+              if (bonds > solvent_bond) {
+                c.push_back(x);
+                mark[x] = id;
+              }
+            }
+          }
+          for (int64_t x : c)
+            if (sp[x] == solvent_code) mark[x] = -1;  // solvent sites may join several clusters
+        }
+        std::sort(c.begin(), c.end());
+        clusters.push_back(std::move(c));
+      }
+      a = b;
+    }
+    // larger clusters first; equal sizes by their first site id
+    std::sort(clusters.begin(), clusters.end(), [](const std::vector<int64_t> &x, const std::vector<int64_t> &y) {
+      return x.size() != y.size() ? x.size() > y.size() : x[0] < y[0];
+    });
+    const long long K = static_cast<long long>(clusters.size());
+    ctx->cl_offsets.assign(1, 0);
+    ctx->cl_members.clear();
+    for (const auto &c : clusters) {
+      ctx->cl_members.insert(ctx->cl_members.end(), c.begin(), c.end());
+      ctx->cl_offsets.push_back(static_cast<int64_t>(ctx->cl_members.size()));
+    }
+    ctx->cl_energy.assign(K, std::numeric_limits<double>::quiet_NaN());
+    if (chemical_potential && K > 0) {
+      // SoluteCluster::GetFormationEnergy (SoluteCluster.cpp:395-410): GetEnergyOfCluster on the
+      // members' species over a solvent background minus that of the pure solvent, on the set of
+      // the members and their 1-3NN shells (one GPU block per cluster), minus the members'
+      // chemical potentials
+      std::vector<long long> s_off(1, 0), s_ids;
+      std::vector<int64_t> shell;
+      for (const auto &c : clusters) {
+        shell.clear();
+        for (int64_t x : c) {
+          shell.push_back(x);
+          const lmc::I3 h = fcc.Coord(x);
+          for (int sh = 1; sh <= 3; ++sh)
+            for (const auto &o : lmc::ShellOffsets(sh)) shell.push_back(fcc.Id(fcc.Wrap(h + o)));
+        }
+        std::sort(shell.begin(), shell.end());
+        shell.erase(std::unique(shell.begin(), shell.end()), shell.end());
+        s_ids.insert(s_ids.end(), shell.begin(), shell.end());
+        s_off.push_back(static_cast<long long>(s_ids.size()));
+      }
+      DevBuf d_soff, d_sids, d_loff, d_lids, d_e;
+      d_soff.Alloc(sizeof(long long) * s_off.size());
+      d_sids.Alloc(sizeof(long long) * s_ids.size());
+      d_loff.Alloc(sizeof(long long) * ctx->cl_offsets.size());
+      d_lids.Alloc(sizeof(long long) * ctx->cl_members.size());
+      d_e.Alloc(sizeof(double) * 2 * K);
+      CudaCheck(cudaMemcpyAsync(d_soff.p, s_off.data(), d_soff.bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      CudaCheck(cudaMemcpyAsync(d_sids.p, s_ids.data(), d_sids.bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+      CudaCheck(cudaMemcpyAsync(d_loff.p, ctx->cl_offsets.data(), d_loff.bytes, cudaMemcpyHostToDevice, ctx->stream),
+                "H2D");
+      CudaCheck(cudaMemcpyAsync(d_lids.p, ctx->cl_members.data(), d_lids.bytes, cudaMemcpyHostToDevice, ctx->stream),
+                "H2D");
+      CudaCheck(lmc::LaunchClusterCensus(ctx->t, d_sp, n, solvent_code, K, d_soff.as<long long>(),
+                                         d_sids.as<long long>(), d_loff.as<long long>(), d_lids.as<long long>(),
+                                         d_e.as<double>(), ctx->stream),
+                "cluster census kernel");
+      std::vector<double> e(2 * K);
+      CudaCheck(cudaMemcpyAsync(e.data(), d_e.p, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+      ctx->Sync();
+      for (long long k = 0; k < K; ++k) {
+        double mu = 0.0;
+        for (int64_t q = ctx->cl_offsets[k]; q < ctx->cl_offsets[k + 1]; ++q) mu += chemical_potential[sp[ctx->cl_members[q]]];
+        ctx->cl_energy[k] = (e[2 * k] - e[2 * k + 1]) - mu;
+      }
+    }
+    if (num_clusters) *num_clusters = K;
+    if (num_members) *num_members = static_cast<int64_t>(ctx->cl_members.size());
+  });
+}
+
+int lmc_solute_cluster_get(lmc_ctx *ctx, int64_t *offsets, int64_t *members, double *formation_energy) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    if (offsets) std::copy(ctx->cl_offsets.begin(), ctx->cl_offsets.end(), offsets);
+    if (members) std::copy(ctx->cl_members.begin(), ctx->cl_members.end(), members);
+    if (formation_energy) std::copy(ctx->cl_energy.begin(), ctx->cl_energy.end(), formation_energy);
   });
 }
 

@@ -1975,6 +1975,164 @@ __global__ void __launch_bounds__(kSiteJumpWarps * 32)
 }
 
 // ---------------------------------------------------------------------------
+// K3b: solute clusters (ansys::SoluteCluster, SoluteCluster.cpp:277-410).
+// Connected components of the non-solvent sites under 1NN bonds by lock-free
+// union-find: every root is hooked under a smaller root (so a parent id never
+// exceeds its child's and every chain ends), finds halve their paths; a final
+// read-only pass stores each site's root. Then one block per cluster evaluates
+// EnergyPredictor::GetEnergyOfCluster (EnergyPredictor.cpp:97-184) on the
+// cluster's sorted site set S (members and their 1-3NN shells) twice: with the
+// members' own species on a solvent background, and with the solvent everywhere.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoCluster = 0xFFFFFFFFu;
+constexpr int kUnionLimit = 1 << 22;  // retries of one union (bounded; each retry follows progress elsewhere)
+
+__global__ void solute_label_init_kernel(const int8_t *__restrict__ species, long long nsites, int solvent,
+                                         uint32_t *parent) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nsites;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    parent[i] = species[i] != solvent ? static_cast<uint32_t>(i) : kNoCluster;
+}
+// Root of x while unions run: parent[x] < x below the root, so at most x + 1 steps; path halving
+// (g is an ancestor of x in the same tree, and only non-roots are written).
+__device__ __forceinline__ uint32_t ClusterRoot(uint32_t *parent, uint32_t x) {
+  volatile uint32_t *vp = parent;
+  for (uint32_t it = 0, x0 = x; it <= x0; ++it) {
+    const uint32_t p = vp[x];
+    if (p == x) return x;
+    const uint32_t g = vp[p];
+    if (g != p) vp[x] = g;
+    x = p;
+  }
+  return x;
+}
+// Root of x once the forest is final (read-only: a concurrent flatten writes only roots).
+__device__ __forceinline__ uint32_t ClusterRootRead(const uint32_t *parent, uint32_t x) {
+  const volatile uint32_t *vp = parent;
+  for (uint32_t it = 0, x0 = x; it <= x0; ++it) {
+    const uint32_t p = vp[x];
+    if (p == x) return x;
+    x = p;
+  }
+  return x;
+}
+__global__ void solute_hook_kernel(DevTables t, const int8_t *__restrict__ species, int n, int solvent,
+                                   uint32_t *parent, int *status) {
+  __shared__ int8_t s_dir[12 * 4];
+  StageArray(t.dir, s_dir, 12 * 4);
+  __syncthreads();
+  const long long nsites = 4LL * n * n * n;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nsites;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    if (species[i] == solvent) continue;
+    const H3 h = SiteCoord(i, n);
+    for (int d = 0; d < 12; ++d) {
+      const long long j = NeighborId(h, s_dir[d * 4], s_dir[d * 4 + 1], s_dir[d * 4 + 2], n);
+      if (j < i || species[j] == solvent) continue;  // each bond once, from its smaller end
+      int it = 0;
+      for (; it < kUnionLimit; ++it) {
+        uint32_t ra = ClusterRoot(parent, static_cast<uint32_t>(i)), rb = ClusterRoot(parent, static_cast<uint32_t>(j));
+        if (ra == rb) break;
+        if (ra < rb) {
+          const uint32_t tmp = ra;
+          ra = rb;
+          rb = tmp;
+        }
+        if (atomicCAS(&parent[ra], ra, rb) == ra) break;
+      }
+      if (it == kUnionLimit) atomicOr(status, kStatusNumeric);
+    }
+  }
+}
+__global__ void solute_flatten_kernel(long long nsites, uint32_t *parent) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nsites;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    if (parent[i] != kNoCluster) parent[i] = ClusterRootRead(parent, static_cast<uint32_t>(i));
+}
+
+__device__ __forceinline__ bool SortedHas(const long long *a, long long len, long long v) {
+  long long lo = 0, hi = len;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < len && a[lo] == v;
+}
+constexpr int kClusterThreads = 128;
+__global__ void __launch_bounds__(kClusterThreads) cluster_census_kernel(DevTables t, const int8_t *__restrict__ species,
+                                                                          int n, int solvent, const long long *s_off,
+                                                                          const long long *s_ids, const long long *l_off,
+                                                                          const long long *l_ids, double *de) {
+  __shared__ unsigned int hist[2][512];  // solute configuration, solvent configuration
+  __shared__ uint32_t s_tri[160];
+  __shared__ int8_t s_off4[kSiteSites * 4];
+  __shared__ int8_t s_label[kSiteSites];
+  __shared__ int16_t s_idx[8 * 6 * 6 * 6];
+  const int e = t.num_species;
+  const int k = blockIdx.x;
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) (&hist[0][0])[i] = 0;
+  StageArray(t.census_tri, s_tri, t.n_census_tri);
+  StageArray(t.site_off, s_off4, kSiteSites * 4);
+  StageArray(t.cluster_index, s_idx, 8 * e * e * e);
+  __syncthreads();
+  for (int q = threadIdx.x; q < kSiteSites; q += blockDim.x) {
+    const int x = s_off4[q * 4], y = s_off4[q * 4 + 1], z = s_off4[q * 4 + 2];
+    const int n2 = x * x + y * y + z * z;
+    s_label[q] = n2 == 2 ? 1 : (n2 == 4 ? 2 : (n2 == 6 ? 3 : 0));
+  }
+  __syncthreads();
+  const long long *S = s_ids + s_off[k], *L = l_ids + l_off[k];
+  const long long ns = s_off[k + 1] - s_off[k], nl = l_off[k + 1] - l_off[k];
+  const int8_t sv = static_cast<int8_t>(solvent);
+  for (long long t1 = threadIdx.x; t1 < ns; t1 += blockDim.x) {
+    const long long site = S[t1];
+    const H3 h = SiteCoord(site, n);
+    int8_t sp[kSiteSites];
+    uint64_t in_s = 0;  // bit q: neighbour q lies in S
+    for (int q = 0; q < kSiteSites; ++q) {
+      const long long j = NeighborId(h, s_off4[q * 4], s_off4[q * 4 + 1], s_off4[q * 4 + 2], n);
+      const bool ins = q == t.site_center || SortedHas(S, ns, j);
+      in_s |= static_cast<uint64_t>(ins) << q;
+      sp[q] = ins && SortedHas(L, nl, j) ? species[j] : sv;
+    }
+    const int c0 = sp[t.site_center];
+    int idx = s_idx[(0 * e + c0) * e * e];
+    if (idx >= 0) atomicAdd(&hist[0][idx], 1u);
+    const int i0 = s_idx[(0 * e + sv) * e * e];
+    if (i0 >= 0) atomicAdd(&hist[1][i0], 1u);
+    for (int q = 0; q < kSiteSites; ++q) {
+      const int l = s_label[q];
+      if (l == 0 || !((in_s >> q) & 1)) continue;
+      idx = s_idx[((l * e + c0) * e + sp[q]) * e];
+      if (idx >= 0) atomicAdd(&hist[0][idx], 1u);
+      const int i1 = s_idx[((l * e + sv) * e + sv) * e];
+      if (i1 >= 0) atomicAdd(&hist[1][i1], 1u);
+    }
+    for (int q = 0; q < t.n_census_tri; ++q) {
+      const uint32_t w = s_tri[q];
+      const int l = w & 7, o1 = (w >> 3) & 63, o2 = (w >> 9) & 63;
+      if (!((in_s >> o1) & 1) || !((in_s >> o2) & 1)) continue;
+      idx = s_idx[((l * e + c0) * e + sp[o1]) * e + sp[o2]];
+      if (idx >= 0) atomicAdd(&hist[0][idx], 1u);
+      const int i2 = s_idx[((l * e + sv) * e + sv) * e + sv];
+      if (i2 >= 0) atomicAdd(&hist[1][i2], 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // sequential in index order without contraction, as GetEncodeOfCluster + dot
+    double ea = 0.0, eb = 0.0;
+    for (int i = 0; i < t.num_theta; ++i) {
+      ea = __dadd_rn(ea, __dmul_rn(t.theta[i], __ddiv_rn(static_cast<double>(hist[0][i]), t.census_bonds[i])));
+      eb = __dadd_rn(eb, __dmul_rn(t.theta[i], __ddiv_rn(static_cast<double>(hist[1][i]), t.census_bonds[i])));
+    }
+    de[2 * k] = ea;
+    de[2 * k + 1] = eb;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K4b: multi-vacancy KMC, one block of kMultiWarps warps per lattice.
 // Every vacancy of the lattice is tracked (slots 0..V-1). Per step:
 //  1. the warps re-evaluate the 12 events of each vacancy whose 135-site
@@ -3050,6 +3208,30 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
     if (err != cudaSuccess) return err;
   }
   kern<<<blocks, threads, sm, stream>>>(t, species, s, l);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSoluteLabels(const DevTables &t, const int8_t *species, int n, int solvent, uint32_t *parent,
+                               int *status, cudaStream_t stream) {
+  const long long nsites = 4LL * n * n * n;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = static_cast<int>(std::min<long long>((nsites + 255) / 256, 8LL * sms));
+  solute_label_init_kernel<<<blocks, 256, 0, stream>>>(species, nsites, solvent, parent);
+  solute_hook_kernel<<<blocks, 256, 0, stream>>>(t, species, n, solvent, parent, status);
+  solute_flatten_kernel<<<blocks, 256, 0, stream>>>(nsites, parent);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchClusterCensus(const DevTables &t, const int8_t *species, int n, int solvent, long long clusters,
+                                const long long *s_off, const long long *s_ids, const long long *l_off,
+                                const long long *l_ids, double *energies, cudaStream_t stream) {
+  if (clusters <= 0) return cudaSuccess;
+  if (clusters > 0x7FFFFFFFLL || t.num_theta > 512 || t.n_census_tri > 160 || t.num_species > 6)
+    return cudaErrorInvalidValue;
+  cluster_census_kernel<<<static_cast<int>(clusters), kClusterThreads, 0, stream>>>(t, species, n, solvent, s_off,
+                                                                                    s_ids, l_off, l_ids, energies);
   return cudaGetLastError();
 }
 

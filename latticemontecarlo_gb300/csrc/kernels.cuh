@@ -206,6 +206,17 @@ struct CmcRefArgs {
 };
 cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream);
 
+// Solute clusters (ansys::SoluteCluster): parent[i] = root site of i's 1NN-connected component
+// of non-solvent sites (0xFFFFFFFF for solvent sites); n <= 1000 keeps ids below 2^32 - 1.
+cudaError_t LaunchSoluteLabels(const DevTables &t, const int8_t *species, int n, int solvent, uint32_t *parent,
+                               int *status, cudaStream_t stream);
+// GetEnergyOfCluster of every cluster k on its sorted site set s_ids[s_off[k]..s_off[k+1]) (members
+// and their 1-3NN shells) with the sorted members l_ids[l_off[k]..): energies[2k] with the members'
+// species on a solvent background, energies[2k+1] with the solvent everywhere.
+cudaError_t LaunchClusterCensus(const DevTables &t, const int8_t *species, int n, int solvent, long long clusters,
+                                const long long *s_off, const long long *s_ids, const long long *l_off,
+                                const long long *l_ids, double *energies, cudaStream_t stream);
+
 // Jump energetics with the vacancy placed on each of a list of sites
 // (ansys::ExitTime::GetJumpEnergetics / GetBarrierListAndExitTime).
 struct SiteJumpArgs {

@@ -1278,6 +1278,189 @@ int orc_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int
 }
 
 /* ------------------------------------------------------------------------- */
+/* solute clusters (ansys::SoluteCluster, SoluteCluster.cpp:277-410)          */
+/* ------------------------------------------------------------------------- */
+/* EnergyPredictor::GetEncodeOfCluster + GetEnergyOfCluster (EnergyPredictor.cpp:97-184): the census
+ * restricted to S = the listed sites and their 1-3NN neighbours (every site of a counted cluster in
+ * S), species taken from sp, or the solvent everywhere except at the listed sites (mode 1), or the
+ * solvent everywhere (mode 2). */
+int orc_cluster_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int solvent, int mode,
+                       const int64_t *sites, int64_t count, double *energy) {
+  unsigned char *in_s = (unsigned char *)calloc((size_t)lat->N, 1);
+  unsigned char *in_l = (unsigned char *)calloc((size_t)lat->N, 1);
+  int64_t *list = (int64_t *)malloc(sizeof(int64_t) * (size_t)(count * 43 + 1));
+  if (!in_s || !in_l || !list) {
+    free(in_s);
+    free(in_l);
+    free(list);
+    return -5;
+  }
+  int64_t ns = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const int64_t a = sites[i];
+    in_l[a] = 1;
+    if (!in_s[a]) in_s[a] = 1, list[ns++] = a;
+    for (int q = 0; q < 42; ++q) {
+      const int64_t b = lat->nn[a][q];
+      if (!in_s[b]) in_s[b] = 1, list[ns++] = b;
+    }
+  }
+#define ORC_SP(x) (mode == 0 ? sp[x] : (mode == 1 && in_l[x] ? sp[x] : solvent))
+  int64_t c[512];
+  int rc = 0;
+  for (int z = 0; z < m->num_theta; ++z) c[z] = 0;
+  for (int64_t t = 0; t < ns && rc == 0; ++t) {
+    const int64_t l1 = list[t];
+    const int64_t *n1 = lat->nn[l1];
+    int k[3] = {ORC_SP(l1), 0, 0};
+    int idx = orc_model_cluster_index(m, 0, 1, k);
+    if (idx < 0 && !m->x_zero) { rc = -2; break; }
+    if (idx >= 0) c[idx]++;
+    for (int a = 0; a < 12 && rc == 0; ++a) {
+      const int64_t l2 = n1[a];
+      if (!in_s[l2]) continue;
+      k[1] = ORC_SP(l2);
+      if ((idx = orc_model_cluster_index(m, 1, 2, k)) < 0 && !m->x_zero) { rc = -2; break; }
+      if (idx >= 0) c[idx]++;
+      for (int b = 0; b < 12; ++b) {
+        const int64_t l3 = lat->nn[l2][b];
+        if (!in_s[l3]) continue;
+        int label = -1;
+        for (int q = 0; q < 12 && label < 0; ++q)
+          if (n1[q] == l3) label = 4;
+        for (int q = 12; q < 18 && label < 0; ++q)
+          if (n1[q] == l3) label = 5;
+        for (int q = 18; q < 42 && label < 0; ++q)
+          if (n1[q] == l3) label = 6;
+        if (label < 0) continue;
+        k[2] = ORC_SP(l3);
+        if ((idx = orc_model_cluster_index(m, label, 3, k)) < 0 && !m->x_zero) { rc = -2; break; }
+        if (idx >= 0) c[idx]++;
+      }
+      for (int b = 12; b < 18 && rc == 0; ++b) {
+        const int64_t l3 = lat->nn[l2][b];
+        if (!in_s[l3]) continue;
+        int in3 = 0;
+        for (int q = 18; q < 42; ++q) in3 |= n1[q] == l3;
+        if (!in3) continue;
+        k[2] = ORC_SP(l3);
+        if ((idx = orc_model_cluster_index(m, 7, 3, k)) < 0 && !m->x_zero) { rc = -2; break; }
+        if (idx >= 0) c[idx]++;
+      }
+    }
+    for (int a = 12; a < 42 && rc == 0; ++a) {
+      if (!in_s[n1[a]]) continue;
+      int kk[3] = {ORC_SP(l1), ORC_SP(n1[a]), 0};
+      if ((idx = orc_model_cluster_index(m, a < 18 ? 2 : 3, 2, kk)) < 0 && !m->x_zero) { rc = -2; break; }
+      if (idx >= 0) c[idx]++;
+    }
+  }
+#undef ORC_SP
+  free(in_s);
+  free(in_l);
+  free(list);
+  if (rc) return rc;
+  double acc = 0.0;
+  for (int z = 0; z < m->num_theta; ++z) {
+    const double enc = (double)c[z] / kCensusCounter[m->key_label[z]];
+    const double p = m->theta[z] * enc;
+    acc = acc + p;
+  }
+  *energy = acc;
+  return 0;
+}
+
+static int cmp_id(const void *a, const void *b) {
+  const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+  return x < y ? -1 : x > y;
+}
+typedef struct {
+  int64_t *ids;
+  int64_t size;
+} orc_cl;
+static int cmp_cluster(const void *a, const void *b) {
+  const orc_cl *x = (const orc_cl *)a, *y = (const orc_cl *)b;
+  if (x->size != y->size) return x->size > y->size ? -1 : 1;
+  return x->ids[0] < y->ids[0] ? -1 : x->ids[0] > y->ids[0];
+}
+
+/* SoluteCluster::FindAtomListOfClusters (SoluteCluster.cpp:277-373): connected components of the
+ * non-solvent sites under 1NN bonds (breadth-first, as FindAtomListOfClustersBFSHelper), components
+ * smaller than `smallest` dropped; a component of more than `bond` sites gains every site of its 1NN
+ * shell with more than `bond` 1NN bonds to it. Clusters sorted by size, larger first (ties: smaller
+ * first site id first; the reference leaves their order to std::sort over hash-set order), members
+ * sorted by id. offsets (K + 1) and members (capacity `cap`) receive the CSR lists; returns K or a
+ * negative error. */
+int64_t orc_solute_clusters(const orc_lattice *lat, const int8_t *sp, int solvent, int64_t smallest, int64_t bond,
+                            int64_t *offsets, int64_t *members, int64_t cap) {
+  const int64_t N = lat->N;
+  unsigned char *seen = (unsigned char *)calloc((size_t)N, 1);
+  int64_t *queue = (int64_t *)malloc(sizeof(int64_t) * (size_t)N);
+  orc_cl *cl = (orc_cl *)malloc(sizeof(orc_cl) * (size_t)(N + 1));
+  int64_t *mark = (int64_t *)malloc(sizeof(int64_t) * (size_t)N);
+  if (!seen || !queue || !cl || !mark) {
+    free(seen), free(queue), free(cl), free(mark);
+    return -5;
+  }
+  for (int64_t i = 0; i < N; ++i) mark[i] = -1;
+  int64_t K = 0;
+  for (int64_t s0 = 0; s0 < N; ++s0) {
+    if (sp[s0] == solvent || seen[s0]) continue;
+    int64_t head = 0, tail = 0;
+    queue[tail++] = s0;
+    seen[s0] = 1;
+    while (head < tail) {
+      const int64_t a = queue[head++];
+      for (int q = 0; q < 12; ++q) {
+        const int64_t b = lat->nn[a][q];
+        if (sp[b] != solvent && !seen[b]) seen[b] = 1, queue[tail++] = b;
+      }
+    }
+    if (tail < smallest) continue;
+    /* the component, then its qualifying solvent shell */
+    int64_t cap_k = tail * 13;
+    int64_t *ids = (int64_t *)malloc(sizeof(int64_t) * (size_t)cap_k);
+    int64_t size = 0;
+    for (int64_t i = 0; i < tail; ++i) ids[size++] = queue[i], mark[queue[i]] = K;
+    if (tail > bond) {
+      for (int64_t i = 0; i < tail; ++i) {
+        for (int q = 0; q < 12; ++q) {
+          const int64_t c = lat->nn[queue[i]][q];
+          if (mark[c] == K) continue; /* already a member */
+          int64_t bonds = 0;
+          for (int r = 0; r < 12; ++r) {
+            const int64_t d = lat->nn[c][r];
+            bonds += mark[d] == K && sp[d] != solvent;
+          }
+          if (bonds > bond) {
+            ids[size++] = c;
+            mark[c] = K;
+          }
+        }
+      }
+    }
+    for (int64_t i = 0; i < size; ++i)
+      if (sp[ids[i]] == solvent) mark[ids[i]] = -1; /* solvent sites may join several clusters */
+    qsort(ids, (size_t)size, sizeof(int64_t), cmp_id);
+    cl[K].ids = ids;
+    cl[K].size = size;
+    ++K;
+  }
+  qsort(cl, (size_t)K, sizeof(orc_cl), cmp_cluster);
+  int64_t off = 0, rc = K;
+  offsets[0] = 0;
+  for (int64_t k = 0; k < K; ++k) {
+    if (off + cl[k].size > cap) rc = -1;
+    for (int64_t i = 0; i < cl[k].size && off + i < cap; ++i) members[off + i] = cl[k].ids[i];
+    off += cl[k].size;
+    offsets[k + 1] = off;
+    free(cl[k].ids);
+  }
+  free(seen), free(queue), free(cl), free(mark);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------- */
 /* random numbers                                                             */
 /* ------------------------------------------------------------------------- */
 void orc_mt_seed(orc_mt *g, uint64_t seed) {

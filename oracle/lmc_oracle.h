@@ -154,6 +154,15 @@ int orc_kmc_chain(const orc_model *m, const orc_lattice *lat, int8_t *sp, double
 int orc_sa(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T0, uint64_t seed, uint64_t maximum_steps,
            int64_t steps, double energy0, double *trace7, double *state4);
 
+/* EnergyPredictor::GetEnergyOfCluster (EnergyPredictor.cpp:97-184) over the listed sites and their
+ * 1-3NN shells; mode 0: species sp, 1: solvent except at the listed sites, 2: solvent everywhere. */
+int orc_cluster_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int solvent, int mode,
+                       const int64_t *sites, int64_t count, double *energy);
+/* SoluteCluster::FindAtomListOfClusters (SoluteCluster.cpp:277-373): CSR cluster lists (members sorted,
+ * clusters by size, larger first, ties by first id). Returns the cluster count, -1 if `cap` is short. */
+int64_t orc_solute_clusters(const orc_lattice *lat, const int8_t *sp, int solvent, int64_t smallest, int64_t bond,
+                            int64_t *offsets, int64_t *members, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

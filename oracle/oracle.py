@@ -78,6 +78,8 @@ def lib() -> C.CDLL:
             "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             "orc_kmc_multi": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, I64, C.c_int,
                                         I64P, C.c_int, DP, DP, DP]),
+            "orc_cluster_energy": (C.c_int, [P, P, I8P, C.c_int, C.c_int, I64P, I64, DP]),
+            "orc_solute_clusters": (I64, [P, I8P, C.c_int, I64, I64, I64P, I64P, I64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -239,6 +241,30 @@ def energy(model: Model, lat: Lattice, species):
     if rc:
         raise OracleError(f"orc_energy rc={rc}")
     return e.value, counts
+
+
+def cluster_energy(model: Model, lat: Lattice, species, solvent: int, sites, mode: int = 0) -> float:
+    """GetEnergyOfCluster over the sites and their 1-3NN shells; mode 0 the lattice's species, 1 the
+    solvent except at the sites, 2 the solvent everywhere."""
+    ids = np.ascontiguousarray(sites, np.int64)
+    e = C.c_double()
+    rc = lib().orc_cluster_energy(model.h, lat.h, _sp(species), solvent, mode, _p(ids, C.c_int64), ids.size,
+                                  C.byref(e))
+    if rc:
+        raise OracleError(f"orc_cluster_energy rc={rc}")
+    return e.value
+
+
+def solute_clusters(lat: Lattice, species, solvent: int, smallest: int, bond: int):
+    """SoluteCluster::FindAtomListOfClusters restated: a list of sorted id arrays, larger clusters first."""
+    sp = np.ascontiguousarray(species, np.int8)
+    offsets = np.zeros(sp.size + 1, np.int64)
+    members = np.zeros(13 * sp.size, np.int64)
+    k = lib().orc_solute_clusters(lat.h, _sp(sp), solvent, smallest, bond, _p(offsets, C.c_int64),
+                                  _p(members, C.c_int64), members.size)
+    if k < 0:
+        raise OracleError(f"orc_solute_clusters rc={k}")
+    return [members[offsets[i]:offsets[i + 1]].copy() for i in range(k)]
 
 
 def kmc(model: Model, lat: Lattice, species, T: float, seed: int, steps: int, kind: int = 0, memo: bool = False,

@@ -24,6 +24,12 @@
 //       CanonicalMcOmp run (batch = OMP thread count) with the seeded generator
 //       (lmc/mc/src/CanonicalMcOmp.cpp:40-92); prints per-step energies
 //       read back from cmc_log.txt and the final lattice.
+//   cluster <n> <species_file> <json> <elements> <solvent> <lists_file>
+//       per line of lists_file (lattice ids of one cluster): EnergyPredictor::GetEnergyOfCluster
+//       on the lattice, on the solvent lattice carrying the listed sites' species (the solute_config
+//       of SoluteCluster::GetFormationEnergy) and on the pure solvent lattice (EnergyPredictor.cpp:
+//       97-184, SoluteCluster.cpp:395-410); then GetChemicalPotential(solvent) (EnergyPredictor.cpp:
+//       196-214).
 //   rng    <seed> <count> <range>
 //       raw mt19937_64 outputs, uniform_real_distribution<double>(0,1) and
 //       uniform_int_distribution<size_t>(0, range-1) draws from libstdc++.
@@ -301,6 +307,35 @@ int CmdRng(unsigned long long seed, size_t count, size_t range) {
 }
 }  // namespace
 
+int CmdCluster(size_t n, const std::string &species_file, const std::string &json, const std::string &elements,
+               const std::string &solvent, const std::string &lists_file) {
+  auto config = MakeConfig(n);
+  LoadSpecies(config, species_file);
+  const pred::EnergyPredictor energy(json, ParseElements(elements));
+  const Element solvent_element(solvent);
+  auto solvent_config = config;
+  for (size_t a = 0; a < solvent_config.GetNumAtoms(); ++a) solvent_config.SetAtomElementTypeAtAtom(a, solvent_element);
+  std::cout.precision(17);
+  std::ifstream ifs(lists_file);
+  if (!ifs) throw std::runtime_error("cannot open " + lists_file);
+  std::string line;
+  while (std::getline(ifs, line)) {
+    std::stringstream ss(line);
+    std::vector<size_t> atoms;
+    size_t l;
+    while (ss >> l) atoms.push_back(config.GetAtomIdFromLatticeId(l));
+    if (atoms.empty()) continue;
+    auto solute_config = solvent_config;
+    for (size_t a : atoms) solute_config.SetAtomElementTypeAtAtom(a, config.GetElementAtAtomId(a));
+    std::cout << "cluster " << energy.GetEnergyOfCluster(config, atoms) << ' '
+              << energy.GetEnergyOfCluster(solute_config, atoms) << ' '
+              << energy.GetEnergyOfCluster(solvent_config, atoms) << '\n';
+  }
+  for (const auto &[element, mu] : energy.GetChemicalPotential(solvent_element))
+    std::cout << "mu " << element.GetString() << ' ' << mu << '\n';
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::cerr << "usage: ref_harness <geom|pred|kmc|cmc|rng> ...\n";
@@ -316,6 +351,7 @@ int main(int argc, char **argv) {
     if (cmd == "cmc" && argc == 9)
       return CmdCmc(std::stoul(argv[2]), argv[3], argv[4], argv[5], std::stod(argv[6]), std::stoull(argv[7]),
                     std::stoull(argv[8]));
+    if (cmd == "cluster" && argc == 8) return CmdCluster(std::stoul(argv[2]), argv[3], argv[4], argv[5], argv[6], argv[7]);
     if (cmd == "rng" && argc == 5) return CmdRng(std::stoull(argv[2]), std::stoul(argv[3]), std::stoul(argv[4]));
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << '\n';

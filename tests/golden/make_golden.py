@@ -6,7 +6,8 @@ and stores its outputs as compressed .npz files. Inputs are regenerated by the
 tests from the same seeds (numpy PCG64, platform independent), so only the
 outputs are committed.
 
-    python tests/golden/make_golden.py        # needs the reference sources at /root/reference
+    python tests/golden/make_golden.py            # needs the reference sources at /root/reference
+    python tests/golden/make_golden.py clusters   # only clusters_quaternary.npz
 
 The fixtures pin the oracle restatement (oracle/lmc_oracle.c); the product is
 then tested against the oracle and against these fixtures directly.
@@ -38,7 +39,9 @@ CASES = {
     "pred_quaternary": (QUATERNARY, 11, 8, {"Al": 0.70, "Cu": 0.10, "Mg": 0.10, "Zn": 0.10}, 1, 202),
     "kmc_ternary": (TERNARY, 7, 10, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 1, 303),
     "cmc_quaternary": (QUATERNARY, 11, 8, {"Al": 0.94, "Cu": 0.02, "Mg": 0.02, "Zn": 0.02}, 0, 404),
+    "clusters_quaternary": (QUATERNARY, 11, 10, {"Al": 0.84, "Cu": 0.04, "Mg": 0.06, "Zn": 0.06}, 2, 505),
 }
+CLUSTER_SMALLEST, CLUSTER_BOND = 2, 3
 KMC_T, KMC_SEED, KMC_STEPS, KMC_DETAIL = 400.0, 12345, 3000, 200
 CMC_T, CMC_SEED, CMC_STEPS, CMC_BATCH = 500.0, 777, 6000, 4
 
@@ -203,7 +206,43 @@ def make_geom(tmp: Path) -> dict:
     return fx
 
 
+def cluster_lists(n: int, species: np.ndarray, elements):
+    """The oracle's solute clusters of the case (solvent Al), the clusters of single sites, and the
+    two vacancies as lists of their own: the lists whose energies the reference evaluates."""
+    from oracle import oracle as O
+    lat = O.Lattice(n)
+    solvent = S.alphabet(elements).index("Al")
+    lists = O.solute_clusters(lat, species, solvent, CLUSTER_SMALLEST, CLUSTER_BOND)
+    singles = O.solute_clusters(lat, species, solvent, 1, 12)
+    x = S.alphabet(elements).index("X")
+    extra = [c for c in singles if len(c) == 1][:4] + [np.flatnonzero(species == x)[:1]]
+    return lists + extra
+
+
+def make_clusters(tmp: Path) -> dict:
+    elements, coeffs, n, species = case_inputs("clusters_quaternary")
+    els = write_inputs(tmp, elements, coeffs, species)
+    lists = cluster_lists(n, species, elements)
+    (tmp / "lists.txt").write_text("\n".join(" ".join(str(int(v)) for v in c) for c in lists))
+    lines = run(["cluster", n, tmp / "species.txt", tmp / "coeffs.json", els, "Al", tmp / "lists.txt"], tmp)
+    energies, mu = [], {}
+    for ln in lines:
+        f = ln.split()
+        if f[0] == "cluster":
+            energies.append([float(v) for v in f[1:]])
+        elif f[0] == "mu":
+            mu[f[1]] = float(f[2])
+    alpha = S.alphabet(elements)
+    offsets = np.concatenate([[0], np.cumsum([len(c) for c in lists])]).astype(np.int64)
+    return {"offsets": offsets, "members": np.concatenate(lists).astype(np.int64), "energies": np.asarray(energies),
+            "mu": np.asarray([mu[a] for a in alpha])}
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "clusters":
+        with tempfile.TemporaryDirectory() as td:
+            np.savez_compressed(HERE / "clusters_quaternary.npz", **make_clusters(Path(td)))
+        return
     if not HARNESS.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
     env = dict(os.environ)
@@ -262,6 +301,7 @@ def main():
                 f = ln.split()
                 rng_fx[f"{f[0]}_{seed}_{rng_range}"] = np.asarray(f[1:], dtype=np.uint64 if f[0] != "real" else float)
         np.savez_compressed(HERE / "rng.npz", **rng_fx)
+        np.savez_compressed(HERE / "clusters_quaternary.npz", **make_clusters(tmp))
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

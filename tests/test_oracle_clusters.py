@@ -1,0 +1,95 @@
+"""The oracle's restatement of ansys::SoluteCluster on the CPU.
+
+* GetEnergyOfCluster (EnergyPredictor.cpp:97-184) on the lattice, on the solute
+  configuration of SoluteCluster::GetFormationEnergy and on the pure solvent equals
+  the reference's own values (tests/golden/clusters_quaternary.npz, from the
+  reference sources compiled by oracle/build_ref.sh) for 84 site lists: the
+  oracle's clusters of the case, single solute sites and a vacancy.
+* GetChemicalPotential (EnergyPredictor.cpp:196-214) from the oracle's census
+  equals the reference's.
+* The cluster search (SoluteCluster.cpp:277-373) equals an independent
+  breadth-first restatement written here over the oracle's neighbour lists."""
+from collections import deque
+
+import numpy as np
+import pytest
+
+from latticemontecarlo_gb300 import synthetic as S
+
+from tests.golden.make_golden import CLUSTER_BOND, CLUSTER_SMALLEST, case_inputs
+
+
+@pytest.fixture(scope="module")
+def case(oracle_mod):
+    elements, coeffs, n, species = case_inputs("clusters_quaternary")
+    g = np.load("tests/golden/clusters_quaternary.npz")
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(elements, coeffs, lat)
+    return elements, coeffs, n, species, g, lat, m
+
+
+def test_cluster_energies_match_reference(oracle_mod, case):
+    elements, coeffs, n, species, g, lat, m = case
+    solvent = S.alphabet(elements).index("Al")
+    off, mem, ref = g["offsets"], g["members"], g["energies"]
+    assert len(off) - 1 == ref.shape[0] == 84
+    for k in range(ref.shape[0]):
+        ids = mem[off[k]:off[k + 1]]
+        got = [oracle_mod.cluster_energy(m, lat, species, solvent, ids, mode) for mode in (0, 1, 2)]
+        np.testing.assert_allclose(got, ref[k], rtol=1e-14, atol=1e-17, err_msg=f"list {k}")
+
+
+def test_chemical_potential_matches_reference(oracle_mod, case):
+    elements, coeffs, n, species, g, lat, m = case
+    alpha = S.alphabet(elements)
+    solvent = alpha.index("Al")
+    lat15 = oracle_mod.Lattice(15)
+    m15 = oracle_mod.Model(elements, coeffs, lat15)
+    pure = np.full(4 * 15 ** 3, solvent, np.int8)
+    e_pure, _ = oracle_mod.energy(m15, lat15, pure)
+    mu = []
+    for c in range(len(alpha)):
+        one = pure.copy()
+        one[0] = c
+        mu.append(0.0 if c == solvent else oracle_mod.energy(m15, lat15, one)[0] - e_pure)
+    np.testing.assert_allclose(mu, g["mu"], rtol=1e-12, atol=1e-15)
+
+
+def _bfs_clusters(lat, sp, solvent, smallest, bond):
+    nb = [lat.neighbors(i)[:12] for i in range(sp.size)]
+    seen = np.zeros(sp.size, bool)
+    out = []
+    for s0 in range(sp.size):
+        if sp[s0] == solvent or seen[s0]:
+            continue
+        comp, q = [], deque([s0])
+        seen[s0] = True
+        while q:
+            a = q.popleft()
+            comp.append(a)
+            for b in nb[a]:
+                if sp[b] != solvent and not seen[b]:
+                    seen[b] = True
+                    q.append(int(b))
+        if len(comp) < smallest:
+            continue
+        members = set(comp)
+        if len(comp) > bond:
+            shell = {int(b) for a in comp for b in nb[a]} - members
+            for c in shell:
+                if sum(1 for d in nb[c] if int(d) in members and sp[d] != solvent) > bond:
+                    members.add(c)
+        out.append(sorted(members))
+    out.sort(key=lambda c: (-len(c), c[0]))
+    return out
+
+
+@pytest.mark.parametrize("smallest,bond", [(1, 12), (2, 3), (3, 2), (1, 0)])
+def test_cluster_search_matches_breadth_first(oracle_mod, smallest, bond):
+    el = ("Al", "Mg", "Zn")
+    sp = S.make_lattice(8, {"Al": 0.78, "Mg": 0.12, "Zn": 0.10}, 2, 91, el)
+    lat = oracle_mod.Lattice(8)
+    got = oracle_mod.solute_clusters(lat, sp, 0, smallest, bond)
+    want = _bfs_clusters(lat, sp, 0, smallest, bond)
+    assert [c.tolist() for c in got] == want
+    assert len(got) > 3
