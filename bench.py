@@ -258,6 +258,7 @@ def run_ours(args, rank, world, local):
         result["simulated_annealing"] = run_sa(args, device)
     if not args.no_large:
         result["exit_time_barriers"] = run_site_jumps(args, device)
+        result["solute_clusters"] = run_solute_clusters(args, device)
     return result, (cfg, coeffs, ns, species, temps)
 
 
@@ -383,6 +384,46 @@ def run_site_jumps(args, device):
         w = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": len(sites) / w, "unit": "sites/s", "cores": 1, "kind": "port",
                                "sample": f"{len(sites)} sites x 12 barriers, oracle C restatement, {w:.1f} s"}
+    return out
+
+
+def run_solute_clusters(args, device):
+    """SoluteCluster's analysis of one frame: the solute clusters of the n = 64 lattice (Al/Mg/Zn/Cu
+    .93/.03/.03/.01, 64 vacancies; clusters of at least 2 sites, solvent shells above 3 bonds) with
+    their formation energies; beside the oracle's restatement on one host core."""
+    from latticemontecarlo_gb300 import Context, Model
+    from latticemontecarlo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    L = S.LARGE
+    el = L["elements"]
+    coeffs = S.make_coefficients(el, 31)
+    sp = S.make_lattice(L["n"], L["fractions"], L["vacancies"], 31, el)
+    solvent = S.alphabet(el).index("Al")
+    ctx = Context(Model.from_coefficients(coeffs, list(el)), device=device)
+    ctx.set_lattices([L["n"]], sp)
+    mu = ctx.chemical_potential(solvent)
+    ctx.solute_clusters(solvent, 2, 3, chemical_potential=mu)  # warm-up
+    t0 = time.perf_counter()
+    clusters, ef = ctx.solute_clusters(solvent, 2, 3, chemical_potential=mu)
+    wall = time.perf_counter() - t0
+    sizes = np.array([len(c) for c in clusters])
+    out = {"workload": f"solute clusters of an n=64 lattice ({sp.size} sites, 64 vacancies), clusters >= 2 sites, "
+                       "solvent shells above 3 bonds, formation energies",
+           "value": sp.size / wall, "unit": "sites/s", "wall_ms": wall * 1e3, "clusters": len(clusters),
+           "largest": int(sizes.max()) if sizes.size else 0, "members": int(sizes.sum())}
+    if not args.no_cpu_baseline:
+        O.build()
+        lat = O.Lattice(L["n"])
+        m = O.Model(el, coeffs, lat)
+        m.set_vacancy_zero(True)
+        t0 = time.perf_counter()
+        ref = O.solute_clusters(lat, sp, solvent, 2, 3)
+        for c in ref:
+            O.cluster_energy(m, lat, sp, solvent, c, 1) - O.cluster_energy(m, lat, sp, solvent, c, 2)
+        w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sp.size / w, "unit": "sites/s", "cores": 1, "kind": "port",
+                               "sample": f"the same frame, oracle C restatement, {w:.1f} s"}
     return out
 
 
