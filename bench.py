@@ -39,7 +39,7 @@ BYTES_PER_EVENT = 225       # algorithmic HBM bytes per KMC event
 # DRAM bytes (read + write) of one full-size kmc_kernel launch (4096 replicas x 1000 steps), one ncu
 # capture with the L2 flushed before the launch; the command and figures are in the kmc_kernel
 # summary under profiles/. The lattices and tables stay in L2, hence far below the algorithmic bytes.
-KMC_TRAFFIC_PER_LAUNCH = 53.52e6 + 4.68e6
+KMC_TRAFFIC_PER_LAUNCH = 53.16e6 + 2.57e6
 BYTES_PER_ATTEMPT = 100     # algorithmic HBM bytes per CMC attempt
 L2_BYTES = 129 * 1024 * 1024
 
@@ -230,8 +230,9 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "int64 fixed-point cluster sums + f64 rates/clock",
         "data": "synthetic (seeded lattices and coefficients; the reference ships none)",
-        "config": {"workload": "batched replica KMC: 4096 FCC supercells n~U{8..24}, 1 vacancy, "
-                               "Al/Mg/Zn .96/.02/.02, T~U(350,550) K, 1e3 KMC steps per replica per step",
+        "config": {"workload": f"batched replica KMC: {args.replicas} FCC supercells n~U{{8..24}}, 1 vacancy, "
+                               f"Al/Mg/Zn .96/.02/.02, T~U(350,550) K, {args.kmc_steps_per_launch} KMC steps per "
+                               "replica per step",
                    "replicas": int(ns.size), "sites_total": int(species.size),
                    "kmc_steps_per_step": args.kmc_steps_per_launch, "rng": "philox4x32-10",
                    "l2": "flushed between timed steps (2x L2 write)", "parallelism": f"replicas x{world}",
