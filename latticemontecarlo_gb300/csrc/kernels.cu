@@ -2542,7 +2542,7 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
 // factors) on the unchanged lattice, one pair per warp, as the reference's OpenMP
 // threads do; warp 0 runs the Metropolis tests in batch order.
 // ---------------------------------------------------------------------------
-constexpr int kCmcRefWarps = 8;
+constexpr int kCmcRefWarps = 16;
 // Lattices up to this many sites are copied into shared memory for the launch.
 constexpr long long kCmcRefSmemSites = 192 * 1024;
 __device__ __forceinline__ bool CmcRefNear(H3 a, H3 b, int n) {
