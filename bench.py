@@ -40,6 +40,10 @@ BYTES_PER_EVENT = 225       # algorithmic HBM bytes per KMC event
 # capture with the L2 flushed before the launch; the command and figures are in the kmc_kernel
 # summary under profiles/. The lattices and tables stay in L2, hence far below the algorithmic bytes.
 KMC_TRAFFIC_PER_LAUNCH = 53.16e6 + 2.57e6
+# What bounds kmc_kernel instead of HBM (the ncu --set full capture summarised under profiles/): the
+# lattices sit in L2 and the per-event work is a dependent chain of gathers and FP64 arithmetic.
+KMC_LIMITER = ("latency and FP64: issue active 50 % and FP64 pipe 55 % of active cycles, 27 of 64 warps "
+               "resident (72 registers), DRAM 6 % of the algorithmic bytes")
 BYTES_PER_ATTEMPT = 100     # algorithmic HBM bytes per CMC attempt
 L2_BYTES = 129 * 1024 * 1024
 
@@ -241,7 +245,8 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "kmc_kernel", "bytes_per_event": BYTES_PER_EVENT},
+                     "kernel": "kmc_kernel", "bytes_per_event": BYTES_PER_EVENT,
+                     "limiter": KMC_LIMITER},
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
     }
