@@ -485,6 +485,33 @@ def run_chain(args, device, seed: int):
             "value": v, "unit": "events/s", "ms": ms, "jump_evaluations_per_s": 144 * v,
             "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
+    if not args.no_cpu_baseline:
+        # the oracle's EnergyPredictor census (serial, as the reference's) and CanonicalMcOmp on all
+        # host cores, on the same lattice; clusters holding two vacancies count nothing, as on the GPU
+        from oracle import oracle as O
+        O.build()
+        lat = O.Lattice(L["n"])
+        m = O.Model(el, coeffs, lat)
+        m.set_vacancy_zero(True)
+        t0 = time.perf_counter()
+        O.energy(m, lat, sp)
+        w = time.perf_counter() - t0
+        out["census"]["cpu_baseline"] = {"value": sp.size / w, "unit": "sites/s", "cores": 1, "kind": "port",
+                                         "sample": f"one census of the same lattice, oracle C restatement, {w:.2f} s"}
+        if args.large_cmc_sweeps > 0:
+            threads = os.cpu_count() or 1
+            os.environ["OMP_NUM_THREADS"] = str(threads)
+            attempts = min(args.cpu_cmc_attempts, sp.size)
+            filled = sp.copy()  # the restated CanonicalMcOmp takes lattices without vacancies
+            filled[filled == S.alphabet(el).index("X")] = S.alphabet(el).index("Al")
+            t0 = time.perf_counter()
+            done, _, _, _ = O.cmc(m, lat, filled, T, 1, attempts, threads)
+            w = time.perf_counter() - t0
+            out["cmc"]["cpu_baseline"] = {"value": done / w, "unit": "swaps/s (Metropolis attempts)", "cores": threads,
+                                          "kind": "port",
+                                          "sample": f"{done} attempts of CanonicalMcOmp (batch = {threads}) on the "
+                                                    f"lattice with its vacancies filled by Al, oracle C restatement, "
+                                                    f"{w:.1f} s"}
 
 
 def run_large(args, device):
@@ -538,6 +565,33 @@ def run_large(args, device):
             "launch": "one block of 8 warps (a single lattice is one sequential trajectory)",
             "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
+    if not args.no_cpu_baseline:
+        # the oracle's EnergyPredictor census (serial, as the reference's) and CanonicalMcOmp on all
+        # host cores, on the same lattice; clusters holding two vacancies count nothing, as on the GPU
+        from oracle import oracle as O
+        O.build()
+        lat = O.Lattice(L["n"])
+        m = O.Model(el, coeffs, lat)
+        m.set_vacancy_zero(True)
+        t0 = time.perf_counter()
+        O.energy(m, lat, sp)
+        w = time.perf_counter() - t0
+        out["census"]["cpu_baseline"] = {"value": sp.size / w, "unit": "sites/s", "cores": 1, "kind": "port",
+                                         "sample": f"one census of the same lattice, oracle C restatement, {w:.2f} s"}
+        if args.large_cmc_sweeps > 0:
+            threads = os.cpu_count() or 1
+            os.environ["OMP_NUM_THREADS"] = str(threads)
+            attempts = min(args.cpu_cmc_attempts, sp.size)
+            filled = sp.copy()  # the restated CanonicalMcOmp takes lattices without vacancies
+            filled[filled == S.alphabet(el).index("X")] = S.alphabet(el).index("Al")
+            t0 = time.perf_counter()
+            done, _, _, _ = O.cmc(m, lat, filled, T, 1, attempts, threads)
+            w = time.perf_counter() - t0
+            out["cmc"]["cpu_baseline"] = {"value": done / w, "unit": "swaps/s (Metropolis attempts)", "cores": threads,
+                                          "kind": "port",
+                                          "sample": f"{done} attempts of CanonicalMcOmp (batch = {threads}) on the "
+                                                    f"lattice with its vacancies filled by Al, oracle C restatement, "
+                                                    f"{w:.1f} s"}
     return out
 
 
