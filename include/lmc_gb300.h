@@ -359,6 +359,15 @@ int lmc_site_jump_energetics(lmc_ctx *ctx, int replica, int kind, int solvent_co
                              const int64_t *sites, int64_t m, double *ea12, double *de12, int64_t *nb12,
                              double *average, double *exit_time);
 
+/* EnergyChangePredictorPairSite::GetDeFromAtomIdSite / GetDeFromLatticeIdSite
+ * (EnergyChangePredictorPairSite.cpp:148-192) for m queries on lattice `replica`: the energy change
+ * of replacing the species at sites[q] (taken as from_codes[q], or the lattice's own when
+ * from_codes is NULL) by to_codes[q], the lattice read as if fill_site (when >= 0) held fill_code.
+ * Host arrays; one GPU warp per query. The building block of ExitTime::GetBindingEnergy and
+ * GetProfileEnergy (ExitTime.cpp:401-511): fill_site = the vacancy, fill_code = the solvent. */
+int lmc_site_de_batch(lmc_ctx *ctx, int replica, const int64_t *sites, const int8_t *from_codes,
+                      const int8_t *to_codes, int64_t m, int64_t fill_site, int fill_code, double *de);
+
 /* ------------------------------------------------------------------------- */
 /* Solute clusters (ansys::SoluteCluster)                                     */
 /* ------------------------------------------------------------------------- */

@@ -154,6 +154,8 @@ SIGNATURES = {
     "lmc_sa_init": (C.c_int, [_P, C.c_int, C.c_uint64, C.c_uint64, C.c_double, C.c_double]),
     "lmc_site_jump_energetics": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_double, _I64P, C.c_int64, _DP, _DP,
                                            _I64P, _DP, _DP]),
+    "lmc_site_de_batch": (C.c_int, [_P, C.c_int, _I64P, C.POINTER(C.c_int8), C.POINTER(C.c_int8), C.c_int64,
+                                    C.c_int64, C.c_int, _DP]),
     "lmc_solute_clusters": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64, C.c_int64, _DP, _I64P, _I64P]),
     "lmc_solute_cluster_get": (C.c_int, [_P, _I64P, _I64P, _DP]),
     "lmc_sa_run": (C.c_int, [_P, C.c_uint64, _P]),

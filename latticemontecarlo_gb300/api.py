@@ -237,6 +237,45 @@ class Context:
                                              ptr(avg, C.c_double), ptr(ext, C.c_double)))
         return ea, de, nb, avg, ext
 
+    # single-site energies (ExitTime's binding and profile energies) -----------
+    def site_de(self, sites, to_codes, from_codes=None, fill_site: int = -1, fill_code: int = 0, replica: int = 0):
+        """GetDeFromLatticeIdSite for each query: the species at sites[q] (from_codes[q], or the lattice's
+        own) replaced by to_codes[q], the lattice read as if fill_site held fill_code."""
+        s = np.ascontiguousarray(sites, np.int64)
+        to = np.ascontiguousarray(np.broadcast_to(np.asarray(to_codes, np.int8), s.shape))
+        fr = None if from_codes is None else np.ascontiguousarray(np.broadcast_to(np.asarray(from_codes, np.int8),
+                                                                                  s.shape))
+        de = np.zeros(s.size)
+        check(N.lib.lmc_site_de_batch(self._h, replica, ptr(s, C.c_int64), ptr(fr, C.c_int8) if fr is not None else None,
+                                      ptr(to, C.c_int8), s.size, fill_site, fill_code, ptr(de, C.c_double)))
+        return de
+
+    def exit_time_energies(self, solvent: int, chemical_potential, replica: int = 0):
+        """ExitTime::GetBindingEnergy and GetProfileEnergy (ExitTime.cpp:401-511) per lattice site, with
+        the lattice's vacancy (its lowest-id X) filled by the solvent: binding[e][i] = dE(i: e -> X) -
+        (mu_X - mu_e) for every element e, profile[i] = dE(i: own -> X) + mu_own - mu_X, and at the
+        vacancy the largest dE(e -> X) + mu_e - mu_X. Returns ({element name: array}, profile)."""
+        alpha = self.model.alphabet
+        x = alpha.index("X")
+        mu = np.asarray(chemical_potential, np.float64)
+        off = self.replica_offset(replica)
+        nsites = 4 * int(self.ns[replica]) ** 3
+        sp = self.get_lattices()[off:off + nsites]
+        xs = np.flatnonzero(sp == x)
+        vac = int(xs[0]) if xs.size else -1
+        elems = [c for c in range(len(alpha)) if c != x]
+        idx = np.arange(nsites, dtype=np.int64)
+        de = self.site_de(np.tile(idx, len(elems)), x, np.repeat(np.asarray(elems, np.int8), nsites), vac, solvent,
+                          replica)
+        binding = {alpha[c]: de[k * nsites:(k + 1) * nsites] - (mu[x] - mu[c]) for k, c in enumerate(elems)}
+        own = sp.copy()
+        if vac >= 0:
+            own[vac] = solvent
+        profile = self.site_de(idx, x, None, vac, solvent, replica) + mu[own] - mu[x]
+        if vac >= 0:
+            profile[vac] = max(de[k * nsites + vac] + mu[c] - mu[x] for k, c in enumerate(elems))
+        return binding, profile
+
     # solute clusters ------------------------------------------------------
     def chemical_potential(self, solvent: int):
         """EnergyPredictor::GetChemicalPotential (EnergyPredictor.cpp:196-214): per species code, the

@@ -2035,6 +2035,49 @@ int lmc_sa_get_state(lmc_ctx *ctx, uint64_t *steps, double *temperature, double 
   });
 }
 
+int lmc_site_de_batch(lmc_ctx *ctx, int replica, const int64_t *sites, const int8_t *from_codes,
+                      const int8_t *to_codes, int64_t m, int64_t fill_site, int fill_code, double *de) {
+  return Guard([&] {
+    Require(ctx && sites && to_codes && de, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    ctx->CheckReplica(replica);
+    Require(m >= 0, LMC_ERR_INVALID_ARGUMENT, "m < 0");
+    if (m == 0) return;
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int n = ctx->n[replica];
+    const long long nsites = 4LL * n * n * n;
+    const int e = ctx->fm.num_species;
+    Require(fill_site < nsites, LMC_ERR_OUT_OF_RANGE, "fill_site out of range");
+    Require(fill_site < 0 || (fill_code >= 0 && fill_code < e), LMC_ERR_INVALID_ARGUMENT, "fill_code out of range");
+    for (int64_t q = 0; q < m; ++q) {
+      Require(sites[q] >= 0 && sites[q] < nsites, LMC_ERR_OUT_OF_RANGE, "site out of range");
+      Require(to_codes[q] >= 0 && to_codes[q] < e, LMC_ERR_INVALID_ARGUMENT, "species code out of range");
+      Require(!from_codes || (from_codes[q] >= 0 && from_codes[q] < e), LMC_ERR_INVALID_ARGUMENT,
+              "species code out of range");
+    }
+    DevBuf d_sites, d_from, d_to, d_de;
+    d_sites.Alloc(sizeof(long long) * m);
+    d_to.Alloc(m);
+    d_de.Alloc(sizeof(double) * m);
+    CudaCheck(cudaMemcpyAsync(d_sites.p, sites, sizeof(long long) * m, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemcpyAsync(d_to.p, to_codes, m, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    if (from_codes) {
+      d_from.Alloc(m);
+      CudaCheck(cudaMemcpyAsync(d_from.p, from_codes, m, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    }
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchSiteDe(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], n, d_sites.as<long long>(),
+                                from_codes ? d_from.as<int8_t>() : nullptr, d_to.as<int8_t>(), m, fill_site, fill_code,
+                                d_de.as<double>(), ctx->stream),
+              "site dE kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    CudaCheck(cudaMemcpyAsync(de, d_de.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+  });
+}
+
 int lmc_solute_clusters(lmc_ctx *ctx, int replica, int solvent_code, int64_t smallest, int64_t solvent_bond,
                         const double *chemical_potential, int64_t *num_clusters, int64_t *num_members) {
   return Guard([&] {

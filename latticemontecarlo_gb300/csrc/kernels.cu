@@ -513,6 +513,51 @@ __device__ __forceinline__ void GatherSwap(const int8_t *off, const int8_t *spec
   __syncwarp();
 }
 
+// Single-site substitution dE (EnergyChangePredictorPairSite::GetDeFromLatticeIdSite,
+// EnergyChangePredictorPairSite.cpp:154-192), one warp per query: the species at `site`
+// taken as from[q] (the lattice's own when from is null) and replaced by to[q]; the
+// lattice read with `fill_site` (if >= 0) holding fill_code. Folded int64 weights over
+// the site's clusters: sum W(c; centre -> to) - W(c; centre = from).
+__global__ void site_de_kernel(DevTables t, const int8_t *__restrict__ species, int n,
+                               const long long *__restrict__ sites, const int8_t *__restrict__ from,
+                               const int8_t *__restrict__ to, long long m, long long fill_site, int fill_code,
+                               double *de) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *sa = s.arr + warp * 88;
+  const int e = t.num_species;
+  for (long long q = static_cast<long long>(blockIdx.x) * warps + warp; q < m;
+       q += static_cast<long long>(gridDim.x) * warps) {
+    const long long site = sites[q];
+    const H3 h = SiteCoord(site, n);
+    for (int k = lane; k < kSiteSites; k += 32) {
+      const int8_t *o = s.off + k * 4;
+      const long long id = NeighborId(h, o[0], o[1], o[2], n);
+      sa[k] = id == fill_site ? static_cast<int8_t>(fill_code) : species[id];
+    }
+    __syncwarp();
+    const int ca = from ? from[q] : sa[t.site_center], cb = to[q];
+    long long acc = 0;
+    if (ca != cb) {
+      const long long *__restrict__ w = t.w_de;
+      for (int c = lane; c < t.n_site_cl; c += 32) {
+        const uint32_t d = s.cl[c];
+        const int label = d & 7, o1 = (d >> 3) & 63, o2 = (d >> 9) & 63;
+        const int tail = (o1 == 63 ? 0 : sa[o1]) * e + (o2 == 63 ? 0 : sa[o2]);
+        acc += __ldg(&w[(label * e + cb) * e * e + tail]) - __ldg(&w[(label * e + ca) * e * e + tail]);
+      }
+    }
+    acc = WarpSum(acc);
+    if (lane == 0) de[q] = static_cast<double>(acc) * t.de_scale;
+    __syncwarp();
+  }
+}
+
 __global__ void de_pairs_kernel(DevTables t, const int8_t *__restrict__ species, int n,
                                 const long long *__restrict__ pairs, int m, double *de, int *status) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -3122,6 +3167,20 @@ cudaError_t LaunchEncodeBatch(const DevTables &t, const int8_t *species, int n, 
   const size_t sm = JumpSmemBytes(t, kJumpWarps);
   encode_batch_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, state_start,
                                                                              state_end, mmm, mm2f, mm2b, status);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSiteDe(const DevTables &t, const int8_t *species, int n, const long long *sites, const int8_t *from,
+                         const int8_t *to, long long m, long long fill_site, int fill_code, double *de,
+                         cudaStream_t stream) {
+  if (m <= 0) return cudaSuccess;
+  const size_t sm = SiteSmemBytes(t, kJumpWarps);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (m + kJumpWarps - 1) / kJumpWarps;
+  const int blocks = static_cast<int>(std::min<long long>(want, 32LL * sms));
+  site_de_kernel<<<blocks, kJumpWarps * 32, sm, stream>>>(t, species, n, sites, from, to, m, fill_site, fill_code, de);
   return cudaGetLastError();
 }
 

@@ -112,6 +112,11 @@ cudaError_t LaunchEncodeBatch(const DevTables &t, const int8_t *species, int n, 
                               cudaStream_t stream);
 cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m, double *de,
                           int *status, cudaStream_t stream);
+// GetDeFromLatticeIdSite for m queries: species at sites[q] (from[q], or the lattice's own when from
+// is null) replaced by to[q], the lattice read with fill_site (>= 0) holding fill_code.
+cudaError_t LaunchSiteDe(const DevTables &t, const int8_t *species, int n, const long long *sites, const int8_t *from,
+                         const int8_t *to, long long m, long long fill_site, int fill_code, double *de,
+                         cudaStream_t stream);
 cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
                          unsigned long long *counts, double *energy, cudaStream_t stream);
 // Multi-vacancy KMC: every vacancy of a lattice is tracked and one event is

@@ -1165,6 +1165,11 @@ static int site_de(const orc_model *m, const orc_lattice *lat, const int8_t *sp,
   return 0;
 }
 
+/* EnergyChangePredictorPairSite::GetDeFromLatticeIdSite (EnergyChangePredictorPairSite.cpp:154-192). */
+int orc_site_de(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t site, int new_code, double *de) {
+  return site_de(m, lat, sp, site, new_code, de);
+}
+
 int orc_pair_site_de(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t a, int64_t b,
                      double *de) {
   const int ca = sp[a], cb = sp[b];

@@ -81,6 +81,8 @@ int orc_e0(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t
 /* PairSite swap dE (EnergyChangePredictorPairSite.cpp:69-192). */
 int orc_pair_site_de(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t a, int64_t b,
                      double *de);
+/* Single-site substitution dE (EnergyChangePredictorPairSite.cpp:154-192): species at `site` -> new_code. */
+int orc_site_de(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t site, int new_code, double *de);
 /* EnergyPredictor census counts (num_theta) and energy (EnergyPredictor.cpp:40-96,173-177). */
 int orc_energy(const orc_model *m, const orc_lattice *lat, const int8_t *sp, int64_t *counts, double *energy);
 

@@ -79,6 +79,7 @@ def lib() -> C.CDLL:
             "orc_kmc_multi": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, I64, C.c_int,
                                         I64P, C.c_int, DP, DP, DP]),
             "orc_cluster_energy": (C.c_int, [P, P, I8P, C.c_int, C.c_int, I64P, I64, DP]),
+            "orc_site_de": (C.c_int, [P, P, I8P, I64, C.c_int, DP]),
             "orc_solute_clusters": (I64, [P, I8P, C.c_int, I64, I64, I64P, I64P, I64]),
         }
         for name, (res, args) in sig.items():
@@ -241,6 +242,15 @@ def energy(model: Model, lat: Lattice, species):
     if rc:
         raise OracleError(f"orc_energy rc={rc}")
     return e.value, counts
+
+
+def site_de(model: Model, lat: Lattice, species, site: int, new_code: int) -> float:
+    """GetDeFromLatticeIdSite: dE of changing the species at `site` to new_code."""
+    out = C.c_double()
+    rc = lib().orc_site_de(model.h, lat.h, _sp(species), site, new_code, C.byref(out))
+    if rc:
+        raise OracleError(f"orc_site_de rc={rc}")
+    return out.value
 
 
 def cluster_energy(model: Model, lat: Lattice, species, solvent: int, sites, mode: int = 0) -> float:

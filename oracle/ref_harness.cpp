@@ -30,6 +30,10 @@
 //       of SoluteCluster::GetFormationEnergy) and on the pure solvent lattice (EnergyPredictor.cpp:
 //       97-184, SoluteCluster.cpp:395-410); then GetChemicalPotential(solvent) (EnergyPredictor.cpp:
 //       196-214).
+//   sitede <n> <species_file> <json> <elements> <queries_file>
+//       per line "lattice_id from to" of queries_file: the site set to `from`, then
+//       EnergyChangePredictorPairSite::GetDeFromAtomIdSite(config, atom, to)
+//       (EnergyChangePredictorPairSite.cpp:148-192), the site restored.
 //   rng    <seed> <count> <range>
 //       raw mt19937_64 outputs, uniform_real_distribution<double>(0,1) and
 //       uniform_int_distribution<size_t>(0, range-1) draws from libstdc++.
@@ -336,6 +340,27 @@ int CmdCluster(size_t n, const std::string &species_file, const std::string &jso
   return 0;
 }
 
+int CmdSiteDe(size_t n, const std::string &species_file, const std::string &json, const std::string &elements,
+              const std::string &queries_file) {
+  auto config = MakeConfig(n);
+  LoadSpecies(config, species_file);
+  const auto element_set = ParseElements(elements);
+  const pred::EnergyChangePredictorPairSite pair_site(json, config, element_set);
+  std::cout.precision(17);
+  std::ifstream ifs(queries_file);
+  if (!ifs) throw std::runtime_error("cannot open " + queries_file);
+  size_t l;
+  std::string from, to;
+  while (ifs >> l >> from >> to) {
+    const size_t atom = config.GetAtomIdFromLatticeId(l);
+    const Element keep = config.GetElementAtAtomId(atom);
+    config.SetAtomElementTypeAtAtom(atom, Element(from));
+    std::cout << "sitede " << pair_site.GetDeFromAtomIdSite(config, atom, Element(to)) << '\n';
+    config.SetAtomElementTypeAtAtom(atom, keep);
+  }
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::cerr << "usage: ref_harness <geom|pred|kmc|cmc|rng> ...\n";
@@ -352,6 +377,7 @@ int main(int argc, char **argv) {
       return CmdCmc(std::stoul(argv[2]), argv[3], argv[4], argv[5], std::stod(argv[6]), std::stoull(argv[7]),
                     std::stoull(argv[8]));
     if (cmd == "cluster" && argc == 8) return CmdCluster(std::stoul(argv[2]), argv[3], argv[4], argv[5], argv[6], argv[7]);
+    if (cmd == "sitede" && argc == 7) return CmdSiteDe(std::stoul(argv[2]), argv[3], argv[4], argv[5], argv[6]);
     if (cmd == "rng" && argc == 5) return CmdRng(std::stoull(argv[2]), std::stoul(argv[3]), std::stoul(argv[4]));
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << '\n';

@@ -8,6 +8,7 @@ outputs are committed.
 
     python tests/golden/make_golden.py            # needs the reference sources at /root/reference
     python tests/golden/make_golden.py clusters   # only clusters_quaternary.npz
+    python tests/golden/make_golden.py sitede     # only site_de_quaternary.npz
 
 The fixtures pin the oracle restatement (oracle/lmc_oracle.c); the product is
 then tested against the oracle and against these fixtures directly.
@@ -238,7 +239,48 @@ def make_clusters(tmp: Path) -> dict:
             "mu": np.asarray([mu[a] for a in alpha])}
 
 
+def site_de_lattice():
+    """The clusters_quaternary lattice with its vacancies filled by Al (ExitTime's this_config): one
+    X at a time keeps every cluster indexable."""
+    elements, coeffs, n, species = case_inputs("clusters_quaternary")
+    alpha = S.alphabet(elements)
+    vac = np.flatnonzero(species == alpha.index("X"))
+    filled = species.copy()
+    filled[vac] = alpha.index("Al")
+    return elements, coeffs, n, filled, vac
+
+
+def site_de_queries(n: int, species: np.ndarray, elements, vac, seed: int = 9):
+    """(site, from, to) codes: random sites, every element to the vacancy and some element swaps,
+    plus every element at the two former vacancies."""
+    rng = np.random.default_rng(seed)
+    alpha = S.alphabet(elements)
+    x = alpha.index("X")
+    sites = np.concatenate([rng.choice(species.size, 60, replace=False), vac])
+    q = []
+    for s in sites:
+        for f in range(len(alpha)):
+            if f != x:
+                q.append((int(s), f, x))
+        q.append((int(s), int(species[s]), int(rng.integers(len(alpha)))))
+    return np.asarray(q, np.int64)
+
+
+def make_site_de(tmp: Path) -> dict:
+    elements, coeffs, n, species, vac = site_de_lattice()
+    els = write_inputs(tmp, elements, coeffs, species)
+    q = site_de_queries(n, species, elements, vac)
+    alpha = S.alphabet(elements)
+    (tmp / "queries.txt").write_text("\n".join(f"{s} {alpha[f]} {alpha[t]}" for s, f, t in q))
+    lines = run(["sitede", n, tmp / "species.txt", tmp / "coeffs.json", els, tmp / "queries.txt"], tmp)
+    return {"queries": q, "de": np.asarray([float(ln.split()[1]) for ln in lines if ln.startswith("sitede")])}
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "sitede":
+        with tempfile.TemporaryDirectory() as td:
+            np.savez_compressed(HERE / "site_de_quaternary.npz", **make_site_de(Path(td)))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "clusters":
         with tempfile.TemporaryDirectory() as td:
             np.savez_compressed(HERE / "clusters_quaternary.npz", **make_clusters(Path(td)))
@@ -302,6 +344,7 @@ def main():
                 rng_fx[f"{f[0]}_{seed}_{rng_range}"] = np.asarray(f[1:], dtype=np.uint64 if f[0] != "real" else float)
         np.savez_compressed(HERE / "rng.npz", **rng_fx)
         np.savez_compressed(HERE / "clusters_quaternary.npz", **make_clusters(tmp))
+        np.savez_compressed(HERE / "site_de_quaternary.npz", **make_site_de(tmp))
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -93,3 +93,21 @@ def test_cluster_search_matches_breadth_first(oracle_mod, smallest, bond):
     want = _bfs_clusters(lat, sp, 0, smallest, bond)
     assert [c.tolist() for c in got] == want
     assert len(got) > 3
+
+
+def test_site_de_matches_reference(oracle_mod):
+    """GetDeFromAtomIdSite (EnergyChangePredictorPairSite.cpp:148-192), the building block of
+    ExitTime's binding and profile energies, against the reference's own values
+    (tests/golden/site_de_quaternary.npz): 310 (site, from, to) queries on the case lattice with its
+    vacancies filled by the solvent."""
+    from tests.golden.make_golden import site_de_lattice
+    elements, coeffs, n, sp, vac = site_de_lattice()
+    g = np.load("tests/golden/site_de_quaternary.npz")
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(elements, coeffs, lat)
+    got = []
+    for site, f, t in g["queries"]:
+        x = sp.copy()
+        x[site] = f
+        got.append(oracle_mod.site_de(m, lat, x, int(site), int(t)))
+    np.testing.assert_array_equal(np.asarray(got), g["de"])
