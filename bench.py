@@ -390,6 +390,30 @@ def run_site_jumps(args, device):
         w = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": len(sites) / w, "unit": "sites/s", "cores": 1, "kind": "port",
                                "sample": f"{len(sites)} sites x 12 barriers, oracle C restatement, {w:.1f} s"}
+    # GetBindingEnergy + GetProfileEnergy: a site substitution dE per (site, element) and per site
+    al = alpha.index("Al")
+    mu = ctx.chemical_potential(al)
+    ctx.exit_time_energies(al, mu)
+    t0 = time.perf_counter()
+    ctx.exit_time_energies(al, mu)
+    w_be = time.perf_counter() - t0
+    queries = sp.size * (len(alpha) - 1) + sp.size
+    out["binding_profile_energies"] = {"value": queries / w_be, "unit": "site substitutions/s",
+                                       "wall_ms": w_be * 1e3, "queries": queries,
+                                       "note": "wall clock of Context.exit_time_energies: host query arrays, "
+                                               "copies and two lmc_site_de_batch calls"}
+    if not args.no_cpu_baseline:
+        x = alpha.index("X")
+        this = sp.copy()
+        this[this == x] = al
+        sites = np.random.default_rng(1).choice(sp.size, 2000, replace=False)
+        t0 = time.perf_counter()
+        for s in sites:
+            O.site_de(m, lat, this, int(s), x)
+        w = time.perf_counter() - t0
+        out["binding_profile_energies"]["cpu_baseline"] = {
+            "value": len(sites) / w, "unit": "site substitutions/s", "cores": 1, "kind": "port",
+            "sample": f"{len(sites)} site substitutions, oracle C restatement, {w:.2f} s"}
     return out
 
 
