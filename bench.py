@@ -400,8 +400,10 @@ def run_site_jumps(args, device):
     queries = sp.size * (len(alpha) - 1) + sp.size
     out["binding_profile_energies"] = {"value": queries / w_be, "unit": "site substitutions/s",
                                        "wall_ms": w_be * 1e3, "queries": queries,
-                                       "note": "wall clock of Context.exit_time_energies: host query arrays, "
-                                               "copies and two lmc_site_de_batch calls"}
+                                       "kernel_ms": ctx.last_run_ms(),
+                                       "note": "wall clock of one lmc_exit_time_energies call (vacancy scan, "
+                                               "one warp per site, every element in one pass, results copied "
+                                               "back); kernel_ms is the kernel alone"}
     if not args.no_cpu_baseline:
         x = alpha.index("X")
         this = sp.copy()

@@ -368,6 +368,16 @@ int lmc_site_jump_energetics(lmc_ctx *ctx, int replica, int kind, int solvent_co
 int lmc_site_de_batch(lmc_ctx *ctx, int replica, const int64_t *sites, const int8_t *from_codes,
                       const int8_t *to_codes, int64_t m, int64_t fill_site, int fill_code, double *de);
 
+/* ExitTime::GetBindingEnergy and GetProfileEnergy (ExitTime.cpp:401-511) for every site of lattice
+ * `replica`, the lattice's vacancy (its first X) read as `solvent_code`: binding [E - 1][N] (rows in
+ * ascending order of the non-X species codes) = dE(site: e -> X) - (mu_X - mu_e); profile [N] =
+ * dE(site: own -> X) + mu_own - mu_X, at the vacancy the largest dE(e -> X) + mu_e - mu_X.
+ * chemical_potential per species code (EnergyPredictor::GetChemicalPotential); host outputs, either
+ * may be NULL. One GPU warp per site, every element's sum from one pass over the site's clusters;
+ * at most 5 elements besides X. */
+int lmc_exit_time_energies(lmc_ctx *ctx, int replica, int solvent_code, const double *chemical_potential,
+                           double *binding, double *profile);
+
 /* ------------------------------------------------------------------------- */
 /* Solute clusters (ansys::SoluteCluster)                                     */
 /* ------------------------------------------------------------------------- */

@@ -257,24 +257,14 @@ class Context:
         vacancy the largest dE(e -> X) + mu_e - mu_X. Returns ({element name: array}, profile)."""
         alpha = self.model.alphabet
         x = alpha.index("X")
-        mu = np.asarray(chemical_potential, np.float64)
-        off = self.replica_offset(replica)
         nsites = 4 * int(self.ns[replica]) ** 3
-        sp = self.get_lattices()[off:off + nsites]
-        xs = np.flatnonzero(sp == x)
-        vac = int(xs[0]) if xs.size else -1
-        elems = [c for c in range(len(alpha)) if c != x]
-        idx = np.arange(nsites, dtype=np.int64)
-        de = self.site_de(np.tile(idx, len(elems)), x, np.repeat(np.asarray(elems, np.int8), nsites), vac, solvent,
-                          replica)
-        binding = {alpha[c]: de[k * nsites:(k + 1) * nsites] - (mu[x] - mu[c]) for k, c in enumerate(elems)}
-        own = sp.copy()
-        if vac >= 0:
-            own[vac] = solvent
-        profile = self.site_de(idx, x, None, vac, solvent, replica) + mu[own] - mu[x]
-        if vac >= 0:
-            profile[vac] = max(de[k * nsites + vac] + mu[c] - mu[x] for k, c in enumerate(elems))
-        return binding, profile
+        mu = np.ascontiguousarray(chemical_potential, np.float64)
+        binding = np.zeros((len(alpha) - 1, nsites))
+        profile = np.zeros(nsites)
+        check(N.lib.lmc_exit_time_energies(self._h, replica, solvent, ptr(mu, C.c_double), ptr(binding, C.c_double),
+                                           ptr(profile, C.c_double)))
+        names = [alpha[c] for c in range(len(alpha)) if c != x]
+        return {nm: binding[k] for k, nm in enumerate(names)}, profile
 
     # solute clusters ------------------------------------------------------
     def chemical_potential(self, solvent: int):

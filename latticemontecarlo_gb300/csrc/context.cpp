@@ -2078,6 +2078,54 @@ int lmc_site_de_batch(lmc_ctx *ctx, int replica, const int64_t *sites, const int
   });
 }
 
+int lmc_exit_time_energies(lmc_ctx *ctx, int replica, int solvent_code, const double *chemical_potential,
+                           double *binding, double *profile) {
+  return Guard([&] {
+    Require(ctx && chemical_potential, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    ctx->CheckReplica(replica);
+    Require(solvent_code >= 0 && solvent_code < ctx->fm.num_species && solvent_code != ctx->fm.x_code,
+            LMC_ERR_INVALID_ARGUMENT, "solvent code out of range");
+    Require(ctx->fm.num_species - 1 <= 5, LMC_ERR_UNSUPPORTED, "at most 5 elements besides X");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int n = ctx->n[replica];
+    const long long nsites = 4LL * n * n * n;
+    const int e = ctx->fm.num_species;
+    // the lattice's vacancy (Config::GetVacancyAtomId: its first X), from the replica scan
+    DevBuf hist, first, d_mu, d_bind, d_prof;
+    hist.Alloc(sizeof(unsigned long long) * (lmc::kMaxSpecies + 1));
+    first.Alloc(sizeof(long long));
+    const long long big = std::numeric_limits<long long>::max();
+    CudaCheck(cudaMemcpyAsync(first.p, &big, sizeof(big), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    CudaCheck(cudaMemsetAsync(hist.p, 0, hist.bytes, ctx->stream), "memset");
+    CudaCheck(lmc::LaunchReplicaScan(ctx->species.as<int8_t>(), ctx->lat_off.as<long long>() + replica,
+                                     ctx->lat_n.as<int>() + replica, 1, ctx->fm.x_code, e, first.as<long long>(),
+                                     hist.as<unsigned long long>(), ctx->stream),
+              "scan kernel");
+    d_mu.Alloc(sizeof(double) * e);
+    d_bind.Alloc(sizeof(double) * (e - 1) * nsites);
+    d_prof.Alloc(sizeof(double) * nsites);
+    CudaCheck(cudaMemcpyAsync(d_mu.p, chemical_potential, sizeof(double) * e, cudaMemcpyHostToDevice, ctx->stream),
+              "H2D");
+    long long vac = big;
+    CudaCheck(cudaMemcpyAsync(&vac, first.p, sizeof(vac), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    if (vac == big) vac = -1;
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    CudaCheck(lmc::LaunchExitEnergies(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], n, vac, solvent_code,
+                                      d_mu.as<double>(), d_bind.as<double>(), d_prof.as<double>(), ctx->stream),
+              "exit energy kernel");
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    if (binding)
+      CudaCheck(cudaMemcpyAsync(binding, d_bind.p, d_bind.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    if (profile)
+      CudaCheck(cudaMemcpyAsync(profile, d_prof.p, d_prof.bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+  });
+}
+
 int lmc_solute_clusters(lmc_ctx *ctx, int replica, int solvent_code, int64_t smallest, int64_t solvent_bond,
                         const double *chemical_potential, int64_t *num_clusters, int64_t *num_members) {
   return Guard([&] {

@@ -558,6 +558,63 @@ __global__ void site_de_kernel(DevTables t, const int8_t *__restrict__ species, 
   }
 }
 
+// ExitTime::GetBindingEnergy and GetProfileEnergy (ExitTime.cpp:401-511) for every site, one warp
+// per site: the neighbourhood gathered once (the vacancy `vac`, if >= 0, read as the solvent), then in
+// one pass over the site's clusters the substitution sums of every element e -> X; binding[k][i] =
+// dE(e_k -> X) - (mu_X - mu_e_k) over the non-X codes e_k in ascending order, profile[i] = dE(own ->
+// X) + mu_own - mu_X, and at the vacancy the largest dE(e -> X) + mu_e - mu_X.
+constexpr int kExitMaxElements = 5;
+__global__ void exit_energy_kernel(DevTables t, const int8_t *__restrict__ species, int n, long long vac, int solvent,
+                                   const double *__restrict__ mu, double *binding, double *profile) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SiteSmem s = CarveSiteSmem(t, smem);
+  StageArray(t.site_cl, s.cl, t.n_site_cl);
+  StageArray(t.site_off, s.off, kSiteSites * 4);
+  __syncthreads();
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t *sa = s.arr + warp * 88;
+  const int e = t.num_species, x = t.x_code;
+  const long long nsites = 4LL * n * n * n;
+  for (long long site = static_cast<long long>(blockIdx.x) * warps + warp; site < nsites;
+       site += static_cast<long long>(gridDim.x) * warps) {
+    const H3 h = SiteCoord(site, n);
+    for (int k = lane; k < kSiteSites; k += 32) {
+      const int8_t *o = s.off + k * 4;
+      const long long id = NeighborId(h, o[0], o[1], o[2], n);
+      sa[k] = id == vac ? static_cast<int8_t>(solvent) : species[id];
+    }
+    __syncwarp();
+    long long acc[kExitMaxElements] = {0, 0, 0, 0, 0};  // indexed by the element's rank among non-X codes
+    const long long *__restrict__ w = t.w_de;
+    for (int c = lane; c < t.n_site_cl; c += 32) {
+      const uint32_t d = s.cl[c];
+      const int label = d & 7, o1 = (d >> 3) & 63, o2 = (d >> 9) & 63;
+      const int tail = (o1 == 63 ? 0 : sa[o1]) * e + (o2 == 63 ? 0 : sa[o2]);
+      const long long wx = __ldg(&w[(label * e + x) * e * e + tail]);
+#pragma unroll
+      for (int k = 0; k < kExitMaxElements; ++k) {
+        const int code = k < x ? k : k + 1;
+        if (code < e) acc[k] += wx - __ldg(&w[(label * e + code) * e * e + tail]);
+      }
+    }
+    double best = -1e300;
+    const int own = sa[t.site_center];
+#pragma unroll
+    for (int k = 0; k < kExitMaxElements; ++k) {
+      const int code = k < x ? k : k + 1;
+      if (code >= e) continue;
+      const double de = static_cast<double>(WarpSum(acc[k])) * t.de_scale;
+      if (lane == 0) binding[k * nsites + site] = de - (mu[x] - mu[code]);
+      best = fmax(best, de + mu[code] - mu[x]);
+      if (code == own && lane == 0 && site != vac) profile[site] = de + mu[code] - mu[x];
+    }
+    if (lane == 0 && site != vac && own == x) profile[site] = 0.0;  // another vacancy: X -> X
+    if (lane == 0 && site == vac) profile[site] = best;
+    __syncwarp();
+  }
+}
+
 __global__ void de_pairs_kernel(DevTables t, const int8_t *__restrict__ species, int n,
                                 const long long *__restrict__ pairs, int m, double *de, int *status) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -3181,6 +3238,19 @@ cudaError_t LaunchSiteDe(const DevTables &t, const int8_t *species, int n, const
   const long long want = (m + kJumpWarps - 1) / kJumpWarps;
   const int blocks = static_cast<int>(std::min<long long>(want, 32LL * sms));
   site_de_kernel<<<blocks, kJumpWarps * 32, sm, stream>>>(t, species, n, sites, from, to, m, fill_site, fill_code, de);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchExitEnergies(const DevTables &t, const int8_t *species, int n, long long vac, int solvent,
+                               const double *mu, double *binding, double *profile, cudaStream_t stream) {
+  if (t.num_species - 1 > kExitMaxElements || t.x_code < 0) return cudaErrorInvalidValue;
+  const long long nsites = 4LL * n * n * n;
+  const size_t sm = SiteSmemBytes(t, kJumpWarps);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = static_cast<int>(std::min<long long>((nsites + kJumpWarps - 1) / kJumpWarps, 32LL * sms));
+  exit_energy_kernel<<<blocks, kJumpWarps * 32, sm, stream>>>(t, species, n, vac, solvent, mu, binding, profile);
   return cudaGetLastError();
 }
 

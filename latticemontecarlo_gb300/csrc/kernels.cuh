@@ -117,6 +117,10 @@ cudaError_t LaunchDePairs(const DevTables &t, const int8_t *species, int n, cons
 cudaError_t LaunchSiteDe(const DevTables &t, const int8_t *species, int n, const long long *sites, const int8_t *from,
                          const int8_t *to, long long m, long long fill_site, int fill_code, double *de,
                          cudaStream_t stream);
+// ExitTime's binding energies binding[k][i] (k = rank of the element among the non-X codes) and
+// profile energies profile[i] of every site, the vacancy `vac` (>= 0) read as the solvent.
+cudaError_t LaunchExitEnergies(const DevTables &t, const int8_t *species, int n, long long vac, int solvent,
+                               const double *mu, double *binding, double *profile, cudaStream_t stream);
 cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int base_code,
                          unsigned long long *counts, double *energy, cudaStream_t stream);
 // Multi-vacancy KMC: every vacancy of a lattice is tracked and one event is

@@ -3,8 +3,9 @@
 * lmc_site_de_batch (GetDeFromLatticeIdSite) against the reference's own values
   (tests/golden/site_de_quaternary.npz) within the folded-weight tolerance.
 * The fill option equals running on a lattice with that site changed, bit for bit.
-* Context.exit_time_energies against a restatement of ExitTime::GetBindingEnergy /
-  GetProfileEnergy (ExitTime.cpp:401-511) over the oracle's site dE."""
+* Context.exit_time_energies (lmc_exit_time_energies, one warp per site) against a restatement of
+  ExitTime::GetBindingEnergy / GetProfileEnergy (ExitTime.cpp:401-511) over the oracle's site dE,
+  and bit for bit against the same lists composed from lmc_site_de_batch queries."""
 import numpy as np
 import pytest
 
@@ -95,3 +96,30 @@ def test_site_de_checks_arguments(native):
     with pytest.raises(N.LmcError) as e:
         ctx.site_de([0], [9])
     assert e.value.code == N.LMC_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("vacancies", [1, 3])
+def test_exit_time_energies_equal_site_de_queries(native, vacancies):
+    el = ("Al", "Cu", "Mg", "Zn")
+    coeffs = S.make_coefficients(el, 21)
+    n = 10
+    sp = S.make_lattice(n, {"Al": 0.8, "Cu": 0.05, "Mg": 0.08, "Zn": 0.07}, vacancies, 21, el)
+    alpha = S.alphabet(el)
+    x, al = alpha.index("X"), alpha.index("Al")
+    ctx = _ctx(el, coeffs, n, sp)
+    mu = ctx.chemical_potential(al)
+    binding, profile = ctx.exit_time_energies(al, mu)
+    vac = int(np.flatnonzero(sp == x)[0])
+    idx = np.arange(sp.size)
+    elems = [c for c in range(len(alpha)) if c != x]
+    best = np.full(sp.size, -np.inf)
+    for c in elems:
+        de = ctx.site_de(idx, x, np.full(sp.size, c, np.int8), vac, al)
+        assert np.array_equal(binding[alpha[c]], de - (mu[x] - mu[c]))
+        best = np.maximum(best, de + mu[c] - mu[x])
+    own = sp.copy()
+    own[vac] = al
+    want = ctx.site_de(idx, x, None, vac, al) + mu[own] - mu[x]
+    want[vac] = best[vac]
+    assert np.array_equal(profile, want)
+
