@@ -111,3 +111,12 @@ def test_site_de_matches_reference(oracle_mod):
         x[site] = f
         got.append(oracle_mod.site_de(m, lat, x, int(site), int(t)))
     np.testing.assert_array_equal(np.asarray(got), g["de"])
+
+
+def test_cluster_energy_over_every_site_is_the_census(oracle_mod, case):
+    """GetEncodeOfCluster restricted to the whole lattice enumerates exactly GetEncode's clusters: the
+    cluster energy of the list of every site equals the census energy, bit for bit."""
+    elements, coeffs, n, species, g, lat, m = case
+    solvent = S.alphabet(elements).index("Al")
+    e_census, _ = oracle_mod.energy(m, lat, species)
+    assert oracle_mod.cluster_energy(m, lat, species, solvent, np.arange(species.size), 0) == e_census
