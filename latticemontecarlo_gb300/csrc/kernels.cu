@@ -110,12 +110,6 @@ __device__ __forceinline__ unsigned long long WarpSumU(unsigned long long v) {
   return v;
 }
 
-__device__ __forceinline__ double WarpSumD(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // Shared-memory copies of the small model tables.
 struct SmallTables {
   int8_t rank[8];
@@ -784,19 +778,6 @@ __device__ __forceinline__ unsigned long long MtNext(Mt s) {
 __device__ __forceinline__ double MtUniform(Mt s) {
   const double u = __ull2double_rn(MtNext(s)) * 5.421010862427522170e-20;  // 2^-64
   return u >= 1.0 ? 0.99999999999999988898 : u;
-}
-// uniform_int_distribution<size_t>(0, range - 1) on a 64-bit engine.
-__device__ __forceinline__ unsigned long long MtBelow(Mt s, unsigned long long range) {
-  unsigned long long x = MtNext(s);
-  unsigned long long low = x * range;
-  if (low < range) {
-    const unsigned long long threshold = (0ULL - range) % range;
-    while (low < threshold) {
-      x = MtNext(s);
-      low = x * range;
-    }
-  }
-  return __umul64hi(x, range);
 }
 
 struct Philox {
@@ -1499,7 +1480,6 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     mt.mt = reinterpret_cast<unsigned long long *>(w);
     mt.idx = w + 2 * 312;
   }
-  const int e = t.num_species;
   if (!active || (s.early_stop && s.escaped[r])) return;  // no block-wide barrier below this point
   if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
   H3 hv = SiteCoord(vac, n);  // vacancy coordinates, advanced by the selected direction each step
@@ -2949,7 +2929,6 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int8_t *sa = s.arr + warp * 88, *sb = sa + 44;
   const long long gtid = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
-  const long long gthreads = static_cast<long long>(gridDim.x) * blockDim.x;
   const uint32_t k0 = static_cast<uint32_t>(a.seed), k1 = static_cast<uint32_t>(a.seed >> 32);
   unsigned long long prev_done = 0;
   int empty_rounds = 0;
