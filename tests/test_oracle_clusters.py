@@ -16,7 +16,7 @@ import pytest
 
 from latticemontecarlo_gb300 import synthetic as S
 
-from tests.golden.make_golden import CLUSTER_BOND, CLUSTER_SMALLEST, case_inputs
+from tests.golden.make_golden import case_inputs
 
 
 @pytest.fixture(scope="module")
