@@ -5,6 +5,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <fstream>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -300,6 +301,96 @@ void Config::WriteConfig(const std::string &filename) const {
     PutVector(fos, map_shift_[atom]) << '\n';
   }
   WriteText(filename, fos.str());
+}
+
+Config Config::ReadMap(const std::string &lattice_filename, const std::string &element_filename,
+                       const std::string &map_filename) {
+  std::ifstream ifs_lattice(lattice_filename);
+  if (!ifs_lattice.is_open()) throw std::runtime_error("Cannot open " + lattice_filename);
+  size_t num_atoms = 0;
+  ifs_lattice >> num_atoms;
+  ifs_lattice.ignore(std::numeric_limits<std::streamsize>::max(), '\n');
+  double basis[9];
+  for (double &b : basis) ifs_lattice >> b;
+  if (!ifs_lattice || num_atoms == 0) throw std::runtime_error("Cannot read " + lattice_filename);
+  const int n = static_cast<int>(std::llround(std::cbrt(static_cast<double>(num_atoms) / 4.0)));
+  if (4ull * n * n * n != num_atoms) throw std::invalid_argument(lattice_filename + ": not a cubic FCC supercell");
+  if (basis[1] != 0 || basis[2] != 0 || basis[3] != 0 || basis[5] != 0 || basis[6] != 0 || basis[7] != 0 ||
+      basis[0] != basis[4] || basis[0] != basis[8])
+    throw std::invalid_argument(lattice_filename + ": only cubic boxes are supported");
+  Config c = GenerateFCC(n, Element(ElementName::X));
+  const int m = 2 * n;
+  for (size_t lattice_id = 0; lattice_id < num_atoms; ++lattice_id) {
+    Vector_d r{};
+    ifs_lattice >> r[0] >> r[1] >> r[2];
+    if (!ifs_lattice) throw std::runtime_error("Cannot read " + lattice_filename);
+    ifs_lattice.ignore(std::numeric_limits<std::streamsize>::max(), '\n');  // the neighbour lists
+    int h[3];
+    for (int d = 0; d < 3; ++d) {
+      const double v = r[d] * m;
+      const long long k = std::llround(v);
+      if (std::fabs(v - static_cast<double>(k)) > 1e-3) throw std::invalid_argument(lattice_filename + ": off-lattice site");
+      h[d] = static_cast<int>(((k % m) + m) % m);
+    }
+    if ((h[0] + h[1] + h[2]) & 1) throw std::invalid_argument(lattice_filename + ": off-lattice site");
+    const size_t id = static_cast<size_t>(h[0]) * 2 * n * n + static_cast<size_t>(h[1]) * n + h[2] / 2;
+    if (id != lattice_id)
+      throw std::invalid_argument(lattice_filename + ": lattice ids are not in ReassignLatticeVector order");
+  }
+  std::ifstream ifs_element(element_filename);
+  if (!ifs_element.is_open()) throw std::runtime_error("Cannot open " + element_filename);
+  std::string type;
+  for (size_t atom = 0; atom < num_atoms; ++atom) {
+    if (!(ifs_element >> type)) throw std::runtime_error("Cannot read " + element_filename);
+    c.atom_element_[atom] = Element(type);
+    ifs_element.ignore(std::numeric_limits<std::streamsize>::max(), '\n');
+  }
+  std::ifstream ifs_map(map_filename);
+  if (!ifs_map.is_open()) throw std::runtime_error("Cannot open " + map_filename);
+  constexpr uint32_t kUnset = std::numeric_limits<uint32_t>::max();
+  c.lattice_to_atom_.assign(num_atoms, kUnset);
+  c.atom_to_lattice_.assign(num_atoms, kUnset);
+  for (size_t atom = 0; atom < num_atoms; ++atom) {
+    size_t lattice_id = 0;
+    if (!(ifs_map >> lattice_id)) throw std::runtime_error("Cannot read " + map_filename);
+    if (lattice_id >= num_atoms)
+      throw std::runtime_error("Lattice id out of bounds in map file: " + std::to_string(lattice_id));
+    if (c.lattice_to_atom_[lattice_id] != kUnset)
+      throw std::runtime_error("Duplicate lattice id in map file: " + std::to_string(lattice_id));
+    c.lattice_to_atom_[lattice_id] = static_cast<uint32_t>(atom);
+    c.atom_to_lattice_[atom] = static_cast<uint32_t>(lattice_id);
+    ifs_map.ignore(std::numeric_limits<std::streamsize>::max(), '\n');
+  }
+  return c;
+}
+
+void Config::WriteLattice(const std::string &filename) const {
+  std::ofstream ofs(filename);
+  ofs.precision(16);
+  const double L = kLatticeConstant * static_cast<double>(n_);
+  ofs << GetNumAtoms() << " positions in total" << '\n';
+  PutVector(ofs, Vector_d{L, 0, 0}) << '\n';
+  PutVector(ofs, Vector_d{0, L, 0}) << '\n';
+  PutVector(ofs, Vector_d{0, 0, L}) << std::endl;
+  for (size_t id = 0; id < GetNumLattices(); ++id) {
+    PutVector(ofs, GetRelativePositionOfLattice(id));
+    ofs << " # ";
+    for (int shell = 1; shell <= 3; ++shell)
+      for (size_t nb : GetNeighborLatticeIdVector(id, shell)) ofs << nb << ' ';
+    ofs << std::endl;
+  }
+}
+
+void Config::WriteElement(const std::string &filename) const {
+  std::ofstream ofs(filename);
+  ofs.precision(16);
+  for (const auto &e : atom_element_) ofs << e.GetString() << std::endl;
+}
+
+void Config::WriteMap(const std::string &filename) const {
+  std::ofstream ofs(filename);
+  ofs.precision(16);
+  for (size_t atom = 0; atom < atom_to_lattice_.size(); ++atom) ofs << atom_to_lattice_[atom] << std::endl;
 }
 
 Vector_d Config::GetRelativePositionOfLattice(size_t id) const {
@@ -1066,9 +1157,14 @@ void Run(const Parameter &p) {
     std::cout << "No such method: " << p.method << std::endl;
     return;
   }
-  if (!p.map_filename_.empty()) throw std::runtime_error("map_filename input is not supported; use config_filename");
-  cfg::Config config = cfg::Config::ReadConfig(p.config_filename_);
-  config.ReassignLatticeVector();
+  // Home.cpp:165-170: a CFG file (reassigned), or the map files lattice.txt / element.txt / map_filename
+  cfg::Config config;
+  if (p.map_filename_.empty()) {
+    config = cfg::Config::ReadConfig(p.config_filename_);
+    config.ReassignLatticeVector();
+  } else {
+    config = cfg::Config::ReadMap("lattice.txt", "element.txt", p.map_filename_);
+  }
   if (p.method == "KineticMcFirstOmp") {
     std::cout << "Finish config reading. Start KMC." << std::endl;
     mc::KineticMcFirstOmp kmc(config, p.log_dump_steps_, p.config_dump_steps_, p.maximum_steps_,

@@ -79,6 +79,16 @@ class Config {
   static Config GenerateFCC(int n, const Element &element);
   // Config::WriteConfig (Config.cpp:651-692).
   void WriteConfig(const std::string &filename) const;
+  // Config::ReadMap (Config.cpp:814-885): lattice file (site count, basis, per lattice id its
+  // relative position and 1-3NN lists), element file (one element per atom id), map file (the
+  // lattice id of every atom id). The lattice ids must be in ReassignLatticeVector order (what
+  // WriteLattice writes for a configuration read from a CFG file and reassigned).
+  static Config ReadMap(const std::string &lattice_filename, const std::string &element_filename,
+                        const std::string &map_filename);
+  // Config::WriteLattice / WriteElement / WriteMap (Config.cpp:887-922).
+  void WriteLattice(const std::string &filename) const;
+  void WriteElement(const std::string &filename) const;
+  void WriteMap(const std::string &filename) const;
   // Lattice ids are already in ReassignLatticeVector order.
   void ReassignLatticeVector() {}
 

@@ -34,6 +34,9 @@
 //       per line "lattice_id from to" of queries_file: the site set to `from`, then
 //       EnergyChangePredictorPairSite::GetDeFromAtomIdSite(config, atom, to)
 //       (EnergyChangePredictorPairSite.cpp:148-192), the site restored.
+//   writemap <n> <species_file> <outdir>
+//       the configuration written by Config::WriteConfig (start.cfg) and by WriteLattice /
+//       WriteElement / WriteMap (lattice.txt, element.txt, map.txt; Config.cpp:651-692,887-922).
 //   rng    <seed> <count> <range>
 //       raw mt19937_64 outputs, uniform_real_distribution<double>(0,1) and
 //       uniform_int_distribution<size_t>(0, range-1) draws from libstdc++.
@@ -361,6 +364,16 @@ int CmdSiteDe(size_t n, const std::string &species_file, const std::string &json
   return 0;
 }
 
+int CmdWriteMap(size_t n, const std::string &species_file, const std::string &outdir) {
+  auto config = MakeConfig(n);
+  LoadSpecies(config, species_file);
+  config.WriteConfig(outdir + "/start.cfg");
+  config.WriteLattice(outdir + "/lattice.txt");
+  config.WriteElement(outdir + "/element.txt");
+  config.WriteMap(outdir + "/map.txt");
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     std::cerr << "usage: ref_harness <geom|pred|kmc|cmc|rng> ...\n";
@@ -378,6 +391,7 @@ int main(int argc, char **argv) {
                     std::stoull(argv[8]));
     if (cmd == "cluster" && argc == 8) return CmdCluster(std::stoul(argv[2]), argv[3], argv[4], argv[5], argv[6], argv[7]);
     if (cmd == "sitede" && argc == 7) return CmdSiteDe(std::stoul(argv[2]), argv[3], argv[4], argv[5], argv[6]);
+    if (cmd == "writemap" && argc == 5) return CmdWriteMap(std::stoul(argv[2]), argv[3], argv[4]);
     if (cmd == "rng" && argc == 5) return CmdRng(std::stoull(argv[2]), std::stoul(argv[3]), std::stoul(argv[4]));
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << '\n';

@@ -9,6 +9,7 @@ outputs are committed.
     python tests/golden/make_golden.py            # needs the reference sources at /root/reference
     python tests/golden/make_golden.py clusters   # only clusters_quaternary.npz
     python tests/golden/make_golden.py sitede     # only site_de_quaternary.npz
+    python tests/golden/make_golden.py maps       # only map_quaternary.npz
 
 The fixtures pin the oracle restatement (oracle/lmc_oracle.c); the product is
 then tested against the oracle and against these fixtures directly.
@@ -41,6 +42,7 @@ CASES = {
     "kmc_ternary": (TERNARY, 7, 10, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 1, 303),
     "cmc_quaternary": (QUATERNARY, 11, 8, {"Al": 0.94, "Cu": 0.02, "Mg": 0.02, "Zn": 0.02}, 0, 404),
     "clusters_quaternary": (QUATERNARY, 11, 10, {"Al": 0.84, "Cu": 0.04, "Mg": 0.06, "Zn": 0.06}, 2, 505),
+    "map_quaternary": (QUATERNARY, 11, 6, {"Al": 0.85, "Cu": 0.05, "Mg": 0.05, "Zn": 0.05}, 1, 606),
 }
 CLUSTER_SMALLEST, CLUSTER_BOND = 2, 3
 KMC_T, KMC_SEED, KMC_STEPS, KMC_DETAIL = 400.0, 12345, 3000, 200
@@ -276,7 +278,24 @@ def make_site_de(tmp: Path) -> dict:
     return {"queries": q, "de": np.asarray([float(ln.split()[1]) for ln in lines if ln.startswith("sitede")])}
 
 
+def make_map_files(tmp: Path) -> dict:
+    """The reference's own CFG and map files (WriteConfig / WriteLattice / WriteElement / WriteMap)
+    of a 6^3-cell quaternary lattice: the CFG is the input of the host mirror's tests, the three map
+    files are compared byte for byte with what the mirror writes."""
+    elements, coeffs, n, species = case_inputs("map_quaternary")
+    write_inputs(tmp, elements, coeffs, species)
+    out = tmp / "maps"
+    out.mkdir()
+    run(["writemap", n, tmp / "species.txt", out], tmp)
+    return {name: np.frombuffer((out / name).read_bytes(), np.uint8)
+            for name in ("start.cfg", "lattice.txt", "element.txt", "map.txt")}
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "maps":
+        with tempfile.TemporaryDirectory() as td:
+            np.savez_compressed(HERE / "map_quaternary.npz", **make_map_files(Path(td)))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "sitede":
         with tempfile.TemporaryDirectory() as td:
             np.savez_compressed(HERE / "site_de_quaternary.npz", **make_site_de(Path(td)))
@@ -345,6 +364,7 @@ def main():
         np.savez_compressed(HERE / "rng.npz", **rng_fx)
         np.savez_compressed(HERE / "clusters_quaternary.npz", **make_clusters(tmp))
         np.savez_compressed(HERE / "site_de_quaternary.npz", **make_site_de(tmp))
+        np.savez_compressed(HERE / "map_quaternary.npz", **make_map_files(tmp))
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

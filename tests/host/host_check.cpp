@@ -1,5 +1,7 @@
 // Test driver for the C++ host mirror (lmc_host.hpp), used by tests/test_host.py.
 //   host_check cfg-roundtrip <dir>              CFG write/read (plain and gzip) with atom tracking
+//   host_check map-write <cfg> <dir>            Config::WriteLattice / WriteElement / WriteMap of a CFG
+//   host_check map-read <dir> <cfg>             Config::ReadMap of <dir>'s map files against the CFG
 //   host_check param <file>                     parsed api::Parameter keys
 //   host_check predict <json> <cfg> <elements,comma> <m> <a b> x m <a b> ...
 //                                               Ea dE (Quartic) and Ea (E0) for the m jump pairs, swap dE
@@ -52,6 +54,28 @@ int main(int argc, char **argv) {
       std::cout.precision(17);
       std::cout << "OK " << vac << ' ' << u[0] << ' ' << u[1] << ' ' << u[2] << ' '
                 << c.GetSolventElement().GetString() << std::endl;
+      return 0;
+    }
+    if (cmd == "map-write" && argc == 4) {
+      cfg::Config c = cfg::Config::ReadConfig(argv[2]);
+      c.ReassignLatticeVector();
+      const std::string dir = argv[3];
+      c.WriteLattice(dir + "/lattice.txt");
+      c.WriteElement(dir + "/element.txt");
+      c.WriteMap(dir + "/map.txt");
+      std::cout << "OK" << std::endl;
+      return 0;
+    }
+    if (cmd == "map-read" && argc == 4) {
+      const std::string dir = argv[2];
+      const cfg::Config m = cfg::Config::ReadMap(dir + "/lattice.txt", dir + "/element.txt", dir + "/map.txt");
+      const cfg::Config c = cfg::Config::ReadConfig(argv[3]);
+      if (m.GetNumAtoms() != c.GetNumAtoms()) return Fail("atom count");
+      for (size_t id = 0; id < c.GetNumLattices(); ++id) {
+        if (m.GetElementAtLatticeId(id) != c.GetElementAtLatticeId(id)) return Fail("element at " + std::to_string(id));
+        if (m.GetAtomIdFromLatticeId(id) != c.GetAtomIdFromLatticeId(id)) return Fail("atom id at " + std::to_string(id));
+      }
+      std::cout << "OK " << m.GetVacancyLatticeId() << std::endl;
       return 0;
     }
     if (cmd == "param") {

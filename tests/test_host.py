@@ -4,7 +4,7 @@ import subprocess
 
 import pytest
 
-from host_util import EXE, build_check
+from host_util import EXE, ROOT, build_check
 
 
 @pytest.fixture(scope="module")
@@ -45,3 +45,41 @@ def test_parameter_keys(check, tmp_path):
                  "seed 42\nunknown_key 7\n")
     r = subprocess.run([str(check), "param", str(p)], capture_output=True, text=True)
     assert r.stdout.strip() == "KineticMcFirstOmp|start.cfg|c.json|10|100|1000|400|101|42|Al,Mg,Zn,"
+
+
+def _golden_maps(tmp_path):
+    import numpy as np
+    g = np.load(ROOT / "tests" / "golden" / "map_quaternary.npz")
+    files = {k: bytes(g[k]) for k in g.files}
+    ref = tmp_path / "ref"
+    ref.mkdir()
+    for name, data in files.items():
+        (ref / name).write_bytes(data)
+    return files, ref
+
+
+def test_map_files_match_reference(check, tmp_path):
+    """Config::WriteLattice / WriteElement / WriteMap (Config.cpp:887-922) of the reference's own CFG
+    file equal the files the reference wrote, byte for byte (tests/golden/map_quaternary.npz)."""
+    files, ref = _golden_maps(tmp_path)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(check), "map-write", str(ref / "start.cfg"), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for name in ("lattice.txt", "element.txt", "map.txt"):
+        assert (out / name).read_bytes() == files[name], name
+
+
+def test_map_read(check, tmp_path):
+    """Config::ReadMap (Config.cpp:814-885) of the reference's map files gives the CFG's configuration
+    (species and atom ids per lattice id); malformed map files fail with the reference's messages."""
+    files, ref = _golden_maps(tmp_path)
+    r = subprocess.run([str(check), "map-read", str(ref), str(ref / "start.cfg")], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
+    ids = files["map.txt"].decode().split()
+    for bad, msg in (([ids[1]] + ids[1:], f"Duplicate lattice id in map file: {ids[1]}"),
+                     (["864"] + ids[1:], "Lattice id out of bounds in map file: 864")):
+        (ref / "map.txt").write_text("\n".join(bad) + "\n")
+        r = subprocess.run([str(check), "map-read", str(ref), str(ref / "start.cfg")], capture_output=True, text=True)
+        assert r.returncode != 0 and msg in r.stdout + r.stderr, (msg, r.stdout + r.stderr)
+
