@@ -1135,7 +1135,14 @@ void Parameter::ReadParam(const std::string &param_filename) {
       solute_number_set_.clear();
       for (size_t q = 1; q < segs.size(); ++q) solute_number_set_.push_back(std::stoull(segs[q]));
     } else if (k == "initial_temperature") initial_temperature_ = std::stod(v);
-    // other keys of the reference's grammar belong to methods outside this path
+    else if (k == "decrement_temperature") decrement_temperature_ = std::stod(v);
+    else if (k == "escape_temperature") escape_temperature_ = std::stod(v);
+    else if (k == "initial_steps") initial_steps_ = std::stoull(v);
+    else if (k == "increment_steps") increment_steps_ = std::stoull(v);
+    else if (k == "early_stop_steps") early_stop_steps_ = std::stoull(v);
+    else if (k == "smallest_cluster_criteria") smallest_cluster_criteria_ = std::stoul(v);
+    else if (k == "solvent_bond_criteria") solvent_bond_criteria_ = std::stoul(v);
+    // the remaining keys of the reference's grammar (vacancy_trajectory) are commented out there
   }
 }
 

@@ -378,6 +378,11 @@ struct Parameter {
   bool has_seed_{false};
   uint64_t seed_{0};
   int cmc_batch_{0};
+  // keys of the analysis (Traverse / ExitTime / SoluteCluster) and annealing schedules, kept for
+  // callers that read them (Parameter.cpp:66-80,125-126)
+  double decrement_temperature_{0}, escape_temperature_{0};
+  unsigned long long initial_steps_{0}, increment_steps_{0}, early_stop_steps_{0};
+  size_t smallest_cluster_criteria_{0}, solvent_bond_criteria_{0};
   // SimulatedAnnealing keys (Parameter.cpp:64-65,113-125)
   int factor_{0};
   std::string solvent_element_;
@@ -386,8 +391,8 @@ struct Parameter {
   double initial_temperature_{0};
 };
 
-// Run (Home.cpp:97-125) for the methods of this path: KineticMcFirstOmp, KineticMcChainOmpi and
-// CanonicalMcOmp.
+// Run (Home.cpp:97-125) for the methods of this path: KineticMcFirstOmp, KineticMcChainOmpi,
+// CanonicalMcOmp and SimulatedAnnealing.
 void Run(const Parameter &parameter);
 
 }  // namespace api

@@ -3,6 +3,7 @@
 //   host_check map-write <cfg> <dir>            Config::WriteLattice / WriteElement / WriteMap of a CFG
 //   host_check map-read <dir> <cfg>             Config::ReadMap of <dir>'s map files against the CFG
 //   host_check param <file>                     parsed api::Parameter keys
+//   host_check param-analysis <file>            the analysis / schedule keys of api::Parameter
 //   host_check predict <json> <cfg> <elements,comma> <m> <a b> x m <a b> ...
 //                                               Ea dE (Quartic) and Ea (E0) for the m jump pairs, swap dE
 //                                               for the remaining pairs, then the energy
@@ -85,6 +86,13 @@ int main(int argc, char **argv) {
                 << '|' << p.rate_corrector_ << p.early_stop_ << p.solute_disp_ << '|' << p.seed_ << '|';
       for (const auto &e : p.element_set_) std::cout << e << ',';
       std::cout << std::endl;
+      return 0;
+    }
+    if (cmd == "param-analysis") {
+      const api::Parameter p(argv[2]);
+      std::cout << p.initial_steps_ << '|' << p.increment_steps_ << '|' << p.smallest_cluster_criteria_ << '|'
+                << p.solvent_bond_criteria_ << '|' << p.escape_temperature_ << '|' << p.decrement_temperature_ << '|'
+                << p.early_stop_steps_ << '|' << p.map_filename_ << std::endl;
       return 0;
     }
     if (cmd == "predict") {

@@ -47,6 +47,16 @@ def test_parameter_keys(check, tmp_path):
     assert r.stdout.strip() == "KineticMcFirstOmp|start.cfg|c.json|10|100|1000|400|101|42|Al,Mg,Zn,"
 
 
+def test_parameter_analysis_keys(check, tmp_path):
+    """The reference's remaining keys (Parameter.cpp:66-80,125-126) are parsed into its field names."""
+    p = tmp_path / "param.txt"
+    p.write_text("simulation_method Ansys\ninitial_steps 100\nincrement_steps 50\nsmallest_cluster_criteria 3\n"
+                 "solvent_bond_criteria 4\nescape_temperature 600\ndecrement_temperature 10\n"
+                 "early_stop_steps 7\nmap_filename map9.txt\n")
+    r = subprocess.run([str(check), "param-analysis", str(p)], capture_output=True, text=True)
+    assert r.stdout.strip() == "100|50|3|4|600|10|7|map9.txt"
+
+
 def _golden_maps(tmp_path):
     import numpy as np
     g = np.load(ROOT / "tests" / "golden" / "map_quaternary.npz")
