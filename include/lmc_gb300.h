@@ -288,10 +288,12 @@ typedef struct lmc_kmc_step {
   double energy;       /* energy after the step */
 } lmc_kmc_step;
 
-/* Initialises KMC state for every replica: temperature[r] (K), vacancy = the
- * lowest-id X site, time = 0, energy = 0. */
+/* Initialises KMC state for every replica (the KineticMcFirstAbstract constructor,
+ * KineticMcAbstract.cpp:5-50): temperature[r] (K), vacancy = the lowest-id X site, time = 0,
+ * energy = 0. */
 int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options *opt);
-/* Runs `steps` steps on every replica in one persistent launch. If trace is
+/* KineticMcFirstAbstract::Simulate's step loop (KineticMcAbstract.cpp:140-190,
+ * KineticMcFirstOmp.cpp:52-82): runs `steps` steps on every replica in one persistent launch. If trace is
  * non-NULL it receives `steps` records of replica trace_replica; events12
  * (NULL or 12 * 3 * steps doubles: target id, Ea, dE per id-sorted event)
  * receives the full event lists of that replica. */
@@ -441,7 +443,8 @@ typedef struct lmc_cmc_options {
                            ThermodynamicAveraging::AddEnergy and Dump, CanonicalMcOmp.cpp:82-90) */
 } lmc_cmc_options;
 
-/* Runs CMC on one replica until at least `attempts` Metropolis tests were made.
+/* CanonicalMcOmp::Simulate (CanonicalMcOmp.cpp:40-92, CanonicalMcAbstract.cpp:43-101): runs CMC
+ * on one replica until at least `attempts` Metropolis tests were made.
  * energy_io: in = current energy, out = energy after the run.
  * attempts_done / accepted: totals of this call. */
 int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts, const lmc_cmc_options *opt,
