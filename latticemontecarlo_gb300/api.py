@@ -466,6 +466,48 @@ def surrogate_barriers(ctx: "Context", model: Surrogate, pairs_dev, threshold_ev
     return ea, flag, nfb.value
 
 
+LATTICE_CONSTANT = 4.046  # Angstrom (lmc/cfg/include/Constants.hpp:6)
+
+
+def site_relative_positions(n: int, sites) -> np.ndarray:
+    """Relative positions (fractions of the cubic box) of lattice ids of an n^3-cell FCC supercell,
+    in the id order of Config::ReassignLatticeVector."""
+    ids = np.asarray(sites, np.int64)
+    plane = 2 * n * n
+    hx = ids // plane
+    rem = ids - hx * plane
+    hy = rem // n
+    hz = 2 * (rem - hy * n) + ((hx + hy) & 1)
+    return np.stack([hx, hy, hz], axis=-1) / (2.0 * n)
+
+
+def cluster_info(clusters, formation_energy, species, n: int, alphabet):
+    """The fields of SoluteCluster::GetClustersInfo (SoluteCluster.cpp:110-275) that need no element
+    masses, per cluster (lists from Context.solute_clusters): cluster_id (1-based), cluster_size
+    (sites other than vacancies), elements_number (every element and X), effective_radius (of a
+    sphere of the cluster's atomic volume), cluster_energy (formation energy per non-vacancy site,
+    0 for a cluster of vacancies only) and geometry_center (periodic circular mean of the relative
+    positions, GetGeometryCenter :412-433, in Angstrom)."""
+    sp = np.asarray(species)
+    x = alphabet.index("X")
+    box = n * LATTICE_CONSTANT
+    out = []
+    for k, (c, ef) in enumerate(zip(clusters, formation_energy)):
+        codes = sp[c]
+        counts = {name: int(np.count_nonzero(codes == code)) for code, name in enumerate(alphabet)}
+        size = len(c)
+        size_wo_x = size - counts["X"]
+        volume = size * LATTICE_CONSTANT ** 3 / 4
+        theta = site_relative_positions(n, c) * 2 * np.pi
+        cbar, sbar = np.cos(theta).sum(0) / size, np.sin(theta).sum(0) / size
+        center = (np.arctan2(-sbar, -cbar) + np.pi) / (2 * np.pi) * box
+        out.append({"cluster_id": k + 1, "cluster_size": size_wo_x, "elements_number": counts,
+                    "effective_radius": (3 * volume / (4 * np.pi)) ** (1.0 / 3.0),
+                    "cluster_energy": 0.0 if size_wo_x == 0 else float(ef) / size_wo_x,
+                    "geometry_center": center, "vacancies": int(np.count_nonzero(codes == x))})
+    return out
+
+
 def load_coefficients(path) -> dict:
     with open(path) as f:
         return json.load(f)

@@ -120,3 +120,31 @@ def test_cluster_energy_over_every_site_is_the_census(oracle_mod, case):
     solvent = S.alphabet(elements).index("Al")
     e_census, _ = oracle_mod.energy(m, lat, species)
     assert oracle_mod.cluster_energy(m, lat, species, solvent, np.arange(species.size), 0) == e_census
+
+
+def test_cluster_info_fields(oracle_mod):
+    """api.cluster_info: the mass-free fields of GetClustersInfo for the oracle's clusters; positions
+    from the closed-form ids equal the oracle's restated GenerateFCC + ReassignLatticeVector
+    positions, and a cluster straddling the periodic boundary gets its centre across the boundary."""
+    from latticemontecarlo_gb300 import api
+    el = ("Al", "Mg", "Zn")
+    alpha = S.alphabet(el)
+    n = 8
+    sp = S.make_lattice(n, {"Al": 0.8, "Mg": 0.1, "Zn": 0.1}, 1, 5, el)
+    lat = oracle_mod.Lattice(n)
+    ids = np.arange(sp.size)
+    np.testing.assert_allclose(api.site_relative_positions(n, ids), [lat.position(int(i)) for i in ids], atol=1e-15)
+    clusters = oracle_mod.solute_clusters(lat, sp, alpha.index("Al"), 2, 3)
+    ef = np.linspace(-0.1, 0.1, len(clusters))
+    info = api.cluster_info(clusters, ef, sp, n, alpha)
+    for k, (c, d) in enumerate(zip(clusters, info)):
+        counts = np.bincount(sp[c], minlength=len(alpha))
+        assert d["cluster_id"] == k + 1 and d["elements_number"]["Mg"] == counts[alpha.index("Mg")]
+        assert d["cluster_size"] == len(c) - counts[alpha.index("X")]
+        np.testing.assert_allclose(d["effective_radius"], (3 * len(c) * 4.046 ** 3 / 4 / (4 * np.pi)) ** (1 / 3))
+        np.testing.assert_allclose(d["cluster_energy"], ef[k] / d["cluster_size"])
+    # two neighbouring sites across the x boundary: the centre sits at the boundary, not mid-box
+    a = 0                                   # h = (0, 0, 0)
+    b = (2 * n - 1) * 2 * n * n + n * 0 + 0  # h = (2n - 1, 0, 1): a 1NN of site 0 across x
+    (d,) = api.cluster_info([np.array([a, b])], [0.0], np.array([1] * (4 * n ** 3), np.int8), n, alpha)
+    assert d["geometry_center"][0] > 0.9 * n * 4.046 or d["geometry_center"][0] < 0.1 * n * 4.046
