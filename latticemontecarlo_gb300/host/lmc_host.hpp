@@ -40,7 +40,8 @@
 
 enum class ElementName { X, Al, Mg, Zn, Cu, Sn };
 
-// Element (Element.hpp): ordered by ElementName like the reference's std::set<Element>.
+// Element (Element.hpp): ordered by name string (Element.hpp:44-46), so a std::set<Element> or
+// std::map<Element, ...> iterates Al, Cu, Mg, Sn, X, Zn as the reference's does.
 class Element {
  public:
   Element() = default;
@@ -49,7 +50,7 @@ class Element {
   [[nodiscard]] std::string GetString() const;
   [[nodiscard]] double GetMass() const;
   [[nodiscard]] ElementName GetElementName() const { return name_; }
-  bool operator<(const Element &o) const { return name_ < o.name_; }
+  bool operator<(const Element &o) const { return GetString() < o.GetString(); }
   bool operator==(const Element &o) const { return name_ == o.name_; }
   bool operator!=(const Element &o) const { return name_ != o.name_; }
 

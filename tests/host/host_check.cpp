@@ -2,6 +2,7 @@
 //   host_check cfg-roundtrip <dir>              CFG write/read (plain and gzip) with atom tracking
 //   host_check map-write <cfg> <dir>            Config::WriteLattice / WriteElement / WriteMap of a CFG
 //   host_check map-read <dir> <cfg>             Config::ReadMap of <dir>'s map files against the CFG
+//   host_check element-order <e1,e2,...>         the names in std::set<Element> iteration order
 //   host_check param <file>                     parsed api::Parameter keys
 //   host_check param-analysis <file>            the analysis / schedule keys of api::Parameter
 //   host_check predict <json> <cfg> <elements,comma> <m> <a b> x m <a b> ...
@@ -93,6 +94,15 @@ int main(int argc, char **argv) {
       std::cout << p.initial_steps_ << '|' << p.increment_steps_ << '|' << p.smallest_cluster_criteria_ << '|'
                 << p.solvent_bond_criteria_ << '|' << p.escape_temperature_ << '|' << p.decrement_temperature_ << '|'
                 << p.early_stop_steps_ << '|' << p.map_filename_ << std::endl;
+      return 0;
+    }
+    if (cmd == "element-order") {
+      std::set<Element> els;
+      std::stringstream ss(argv[2]);
+      std::string e;
+      while (std::getline(ss, e, ',')) els.insert(Element(e));
+      for (const auto &el : els) std::cout << el.GetString() << ' ';
+      std::cout << std::endl;
       return 0;
     }
     if (cmd == "predict") {

@@ -37,6 +37,13 @@ def test_cfg_roundtrip(check, tmp_path):
     assert gz[:2] == b"\x1f\x8b"
 
 
+def test_element_set_order(check):
+    """std::set<Element> iterates in name order (Element.hpp:44-46), as the reference's does."""
+    r = subprocess.run([str(check), "element-order", "Zn,Al,X,Mg,Cu,Sn"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split() == ["Al", "Cu", "Mg", "Sn", "X", "Zn"]
+
+
 def test_parameter_keys(check, tmp_path):
     p = tmp_path / "param.txt"
     p.write_text("# comment\n\nsimulation_method KineticMcFirstOmp\nconfig_filename start.cfg\n"
