@@ -170,22 +170,29 @@ int lmc_de_pairs(lmc_ctx *ctx, int replica, const int64_t *pairs, int m, double 
  * cluster census behind it. */
 int lmc_energy(lmc_ctx *ctx, int replica, double *energy, int64_t *counts);
 
-/* Allocation-free variant of lmc_energy, for callers that must not allocate
- * device memory: code that runs while a CUDA stream is being captured (where
- * cudaMalloc is not allowed) or hosts that hand the library a fixed memory
- * budget. It has no counterpart in the reference.
+/* Allocation-free variant of lmc_energy. It has no counterpart in the
+ * reference. It serves callers that cannot allocate device memory at the call
+ * site: a host application whose own pool allocator already owns the GPU's
+ * memory and forbids other cudaMalloc calls, a plugin run under a fixed memory
+ * budget, or a stepping loop where cudaMalloc / cudaFree would synchronise the
+ * device and stall its other streams.
  * species_dev: the caller's device array of 4 n^3 species codes (lattice ids
  * as above); energy_dev: the caller's device double that receives the energy.
  * The call allocates nothing: the cluster counters live in one static device
- * array of 512 entries per GPU (4 KiB, held by every GPU that loads the library
- * until the process exits); models with more cluster types are rejected with
- * LMC_ERR_UNSUPPORTED. The first call on a device looks the array up
- * (cudaGetSymbolAddress) with that device current: make that first call before
- * any stream capture. The work is queued on the context's stream and the call
- * returns without waiting (lmc_ctx_synchronize before reading energy_dev).
- * Every call shares the array and clears it first, so calls that overlap on the
- * GPU (other streams, other contexts on the same device) race and must be
- * serialised by the caller. */
+ * array of 512 counters plus one status word per GPU (about 4 KiB, held by
+ * every GPU that loads the library until the process exits); models with more
+ * cluster types are rejected with LMC_ERR_UNSUPPORTED, edges outside [6, 1000]
+ * likewise. The first call on a device looks the array up
+ * (cudaGetSymbolAddress) with that device current and keeps the address for
+ * the life of the process: make that first call before any stream capture,
+ * and do not call it again on a device after cudaDeviceReset. The species
+ * codes are checked on the device: if any code lies outside [0, number of
+ * species), energy_dev receives NaN (no status is returned, because the call
+ * does not wait for the GPU). The work is queued on the context's stream and
+ * the call returns without waiting (lmc_ctx_synchronize before reading
+ * energy_dev). Every call shares the array and clears it first, so calls that
+ * overlap on the GPU (other streams, other contexts on the same device) race
+ * and must be serialised by the caller. */
 int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *energy_dev);
 
 /* Self-check of the device FP64 helpers the barrier epilogue, the rates and the

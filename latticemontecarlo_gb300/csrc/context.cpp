@@ -1322,8 +1322,9 @@ int lmc_energy_noalloc(lmc_ctx *ctx, const int8_t *species_dev, int n, double *e
     int base = ctx->fm.x_code == 0 ? 1 : 0;
     for (int c = 0; c < ctx->fm.num_species; ++c)
       if (ctx->model.alphabet[c] == "Al") base = c;
-    // LaunchCensus clears the counters it uses before the census kernel runs.
-    CudaCheck(lmc::LaunchCensus(ctx->t, species_dev, n, base, scratch, energy_dev, ctx->stream), "census kernel");
+    // clears the scratch, range-checks every species code on the device (NaN energy on a bad one)
+    CudaCheck(lmc::LaunchCensusCheckedNoAlloc(ctx->t, species_dev, n, base, scratch, energy_dev, ctx->stream),
+              "census kernel");
   });
 }
 

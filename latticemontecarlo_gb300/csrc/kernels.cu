@@ -646,9 +646,15 @@ __global__ void de_pairs_kernel(DevTables t, const int8_t *__restrict__ species,
 // histogram; clusters made only of the dominant species are counted in
 // registers per label and merged once per warp (they are most of the lattice).
 // ---------------------------------------------------------------------------
+// kCheckCodes: the species array comes straight from the caller (lmc_energy_noalloc) rather than
+// from a context lattice validated at upload, so every code is range-checked before it indexes
+// the shared tables; a site whose 43-site neighbourhood holds a code outside [0, e) is skipped
+// and counted in *bad_codes.
 constexpr int kCensusThreads = 256;
+template <bool kCheckCodes>
 __global__ void __launch_bounds__(kCensusThreads) census_kernel(DevTables t, const int8_t *__restrict__ species, int n,
-                                                                int base_code, unsigned long long *counts) {
+                                                                int base_code, unsigned long long *counts,
+                                                                unsigned long long *bad_codes) {
   __shared__ unsigned int hist[512];
   __shared__ uint32_t s_tri[160];
   __shared__ int8_t s_off[kSiteSites * 4];
@@ -687,6 +693,14 @@ __global__ void __launch_bounds__(kCensusThreads) census_kernel(DevTables t, con
       base_count[3] += 24;
       for (int q = 0; q < t.n_census_tri; ++q) base_count[s_tri[q] & 7] += 1;
       continue;
+    }
+    if constexpr (kCheckCodes) {
+      bool ok = true;
+      for (int k = 0; k < kSiteSites; ++k) ok &= static_cast<unsigned>(static_cast<int>(sp[k])) < static_cast<unsigned>(e);
+      if (!ok) {
+        atomicAdd(bad_codes, 1ull);
+        continue;
+      }
     }
     // clusters whose multiset has no index (two or more vacancies) count nothing
     atomicAdd(&hist[s_idx[(0 * e + c0) * e * e]], 1u);
@@ -732,8 +746,14 @@ __global__ void __launch_bounds__(kCensusThreads) census_kernel(DevTables t, con
 // Energy = sum_idx theta_idx * (count_idx / bonds_idx), sequential in index
 // order without contraction, as the reference's GetEncode + dot
 // (EnergyPredictor.cpp:87-95,173-177).
-__global__ void census_energy_kernel(DevTables t, const unsigned long long *counts, double *energy) {
+// With bad_codes set, a nonzero count of skipped sites gives NaN instead of an energy.
+__global__ void census_energy_kernel(DevTables t, const unsigned long long *counts, double *energy,
+                                     const unsigned long long *bad_codes) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (bad_codes != nullptr && *bad_codes != 0) {
+    *energy = nan("");
+    return;
+  }
   double s = 0.0;
   for (int i = 0; i < t.num_theta; ++i) {
     const double enc = __ddiv_rn(static_cast<double>(counts[i]), t.census_bonds[i]);
@@ -3252,10 +3272,35 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
   long long blocks = (nsites + kCensusThreads - 1) / kCensusThreads;
   const long long cap = static_cast<long long>(sms) * 8;
   if (blocks > cap) blocks = cap;
-  census_kernel<<<static_cast<int>(blocks), kCensusThreads, 0, stream>>>(t, species, n, base_code, counts);
+  census_kernel<false><<<static_cast<int>(blocks), kCensusThreads, 0, stream>>>(t, species, n, base_code, counts,
+                                                                                nullptr);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  census_energy_kernel<<<1, 32, 0, stream>>>(t, counts, energy);
+  census_energy_kernel<<<1, 32, 0, stream>>>(t, counts, energy, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchCensusCheckedNoAlloc(const DevTables &t, const int8_t *species, int n, int base_code,
+                                       unsigned long long *scratch, double *energy, cudaStream_t stream) {
+  if (t.num_theta > kNoAllocMaxTheta) return cudaErrorInvalidValue;
+  // every call starts from zero: the counters and the bad-code word after them
+  cudaError_t err = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * kNoAllocScratchWords, stream);
+  if (err != cudaSuccess) return err;
+  unsigned long long *bad = scratch + kNoAllocMaxTheta;
+  const long long nsites = 4LL * n * n * n;
+  int dev = 0, sms = 0;
+  err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (err != cudaSuccess) return err;
+  long long blocks = (nsites + kCensusThreads - 1) / kCensusThreads;
+  const long long cap = static_cast<long long>(sms) * 8;
+  if (blocks > cap) blocks = cap;
+  census_kernel<true><<<static_cast<int>(blocks), kCensusThreads, 0, stream>>>(t, species, n, base_code, scratch,
+                                                                               bad);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  census_energy_kernel<<<1, 32, 0, stream>>>(t, scratch, energy, bad);
   return cudaGetLastError();
 }
 
@@ -3460,7 +3505,7 @@ cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, lon
 // array shared by every call on a device (see lmc_energy_noalloc).
 // ---------------------------------------------------------------------------
 namespace {
-static __device__ __align__(256) unsigned long long g_noalloc_census_counts[kNoAllocMaxTheta];
+static __device__ __align__(256) unsigned long long g_noalloc_census_counts[kNoAllocScratchWords];
 }  // namespace
 
 cudaError_t NoAllocCensusScratch(int device, unsigned long long **ptr) {

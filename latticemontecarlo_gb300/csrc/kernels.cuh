@@ -297,11 +297,20 @@ cudaError_t LaunchReplicaScan(const int8_t *species, const long long *lat_off, c
                               cudaStream_t stream);
 
 // Scratch of the allocation-free census: a file-scope device array of
-// kNoAllocMaxTheta counters. Returns its device address for `device`, which
-// must be the current device; the lookup happens on the first call per device.
+// kNoAllocMaxTheta counters followed by one word that counts sites skipped for
+// species codes outside the alphabet. Returns its device address for `device`,
+// which must be the current device; the lookup happens on the first call per
+// device.
 constexpr int kNoAllocMaxTheta = 512;
+constexpr int kNoAllocScratchWords = kNoAllocMaxTheta + 1;
 constexpr int kNoAllocMaxDevices = 64;
 cudaError_t NoAllocCensusScratch(int device, unsigned long long **ptr);
+// The census of LaunchCensus on a caller-owned species array whose codes are not
+// trusted: clears the kNoAllocScratchWords words of `scratch` (from
+// NoAllocCensusScratch), skips sites whose neighbourhood holds a code outside
+// [0, num_species) and writes NaN to *energy when any site was skipped.
+cudaError_t LaunchCensusCheckedNoAlloc(const DevTables &t, const int8_t *species, int n, int base_code,
+                                       unsigned long long *scratch, double *energy, cudaStream_t stream);
 
 // Host-side reference seeding of std::mt19937_64 (state words for the device).
 void MtSeed(uint64_t seed, uint32_t *words);
