@@ -7,9 +7,10 @@
 # -ffp-contract=fast, replaced by -ffp-contract=off so x86-64 and aarch64 builds
 # round identically.
 #
-# usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# usage: oracle/build_ref.sh [reference_root]
+#   reference_root defaults to $LMC_REFERENCE_ROOT, else /root/reference
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${LMC_REFERENCE_ROOT:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/lmc" ]; then

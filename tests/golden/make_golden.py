@@ -6,7 +6,7 @@ and stores its outputs as compressed .npz files. Inputs are regenerated by the
 tests from the same seeds (numpy PCG64, platform independent), so only the
 outputs are committed.
 
-    python tests/golden/make_golden.py            # needs the reference sources at /root/reference
+    python tests/golden/make_golden.py            # needs the reference sources (oracle/build_ref.sh)
     python tests/golden/make_golden.py clusters   # only clusters_quaternary.npz
     python tests/golden/make_golden.py sitede     # only site_de_quaternary.npz
     python tests/golden/make_golden.py maps       # only map_quaternary.npz
