@@ -137,6 +137,16 @@ def peaks():
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
+def kmc_config(args, world: int, sites_total: int) -> dict:
+    """The batched-KMC workload's description; both arms print the same dict."""
+    return {"workload": f"batched replica KMC: {args.replicas} FCC supercells n~U{{8..24}}, 1 vacancy, "
+                        f"Al/Mg/Zn .96/.02/.02, T~U(350,550) K, {args.kmc_steps_per_launch} KMC steps per "
+                        "replica per step",
+            "replicas": int(args.replicas), "sites_total": int(sites_total),
+            "kmc_steps_per_step": args.kmc_steps_per_launch, "seed": rank_seed(0),
+            "l2": "flushed between timed steps (2x L2 write)", "parallelism": f"replicas x{world}"}
+
+
 def kmc_inputs(seed: int, replicas: int):
     from latticemontecarlo_gb300 import synthetic as S
     cfg = S.KMC_BATCHED
@@ -234,13 +244,9 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "int64 fixed-point cluster sums + f64 rates/clock",
         "data": "synthetic (seeded lattices and coefficients; the reference ships none)",
-        "config": {"workload": f"batched replica KMC: {args.replicas} FCC supercells n~U{{8..24}}, 1 vacancy, "
-                               f"Al/Mg/Zn .96/.02/.02, T~U(350,550) K, {args.kmc_steps_per_launch} KMC steps per "
-                               "replica per step",
-                   "replicas": int(ns.size), "sites_total": int(species.size),
-                   "kmc_steps_per_step": args.kmc_steps_per_launch, "rng": "philox4x32-10",
-                   "l2": "flushed between timed steps (2x L2 write)", "parallelism": f"replicas x{world}",
-                   "launch": dict(shape, autotuned=True, from_cache=tune["from_cache"], cuda_graph=True)},
+        "config": kmc_config(args, world, int(species.size)),
+        "rng": "philox4x32-10",
+        "launch": dict(shape, autotuned=True, from_cache=tune["from_cache"], cuda_graph=True),
         "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -511,33 +517,6 @@ def run_chain(args, device, seed: int):
             "value": v, "unit": "events/s", "ms": ms, "jump_evaluations_per_s": 144 * v,
             "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
-    if not args.no_cpu_baseline:
-        # the oracle's EnergyPredictor census (serial, as the reference's) and CanonicalMcOmp on all
-        # host cores, on the same lattice; clusters holding two vacancies count nothing, as on the GPU
-        from oracle import oracle as O
-        O.build()
-        lat = O.Lattice(L["n"])
-        m = O.Model(el, coeffs, lat)
-        m.set_vacancy_zero(True)
-        t0 = time.perf_counter()
-        O.energy(m, lat, sp)
-        w = time.perf_counter() - t0
-        out["census"]["cpu_baseline"] = {"value": sp.size / w, "unit": "sites/s", "cores": 1, "kind": "port",
-                                         "sample": f"one census of the same lattice, oracle C restatement, {w:.2f} s"}
-        if args.large_cmc_sweeps > 0:
-            threads = os.cpu_count() or 1
-            os.environ["OMP_NUM_THREADS"] = str(threads)
-            attempts = min(args.cpu_cmc_attempts, sp.size)
-            filled = sp.copy()  # the restated CanonicalMcOmp takes lattices without vacancies
-            filled[filled == S.alphabet(el).index("X")] = S.alphabet(el).index("Al")
-            t0 = time.perf_counter()
-            done, _, _, _ = O.cmc(m, lat, filled, T, 1, attempts, threads)
-            w = time.perf_counter() - t0
-            out["cmc"]["cpu_baseline"] = {"value": done / w, "unit": "swaps/s (Metropolis attempts)", "cores": threads,
-                                          "kind": "port",
-                                          "sample": f"{done} attempts of CanonicalMcOmp (batch = {threads}) on the "
-                                                    f"lattice with its vacancies filled by Al, oracle C restatement, "
-                                                    f"{w:.1f} s"}
 
 
 def run_large(args, device):
@@ -743,46 +722,59 @@ def run_surrogate(args, device):
 # ---------------------------------------------------------------------------
 # CPU restatement of the reference path (baseline)
 # ---------------------------------------------------------------------------
-def cpu_kmc_baseline(seed: int, threads: int, steps_per_replica: int):
-    """Independent trajectories, one per host thread (the reference's own advice
-    for many trajectories, KineticMcAbstract.cpp:188-189), with the barrier memo
-    that plays the role of its LRU cache. Returns events/s over all threads."""
-    from concurrent.futures import ThreadPoolExecutor
+class CpuKmcSampler:
+    """The batched-KMC workload on the host cores: independent trajectories, one per thread (the
+    reference's own advice for many trajectories, KineticMcAbstract.cpp:188-189), each a replica of
+    the GPU arm's replica set (same seed, edges, temperatures and lattices) advanced by the GPU arm's
+    steps per bench step, with the barrier memo that plays the role of the reference's LRU cache.
+    Built from oracle/ alone (inputs from oracle/workload.py), so the timed process never loads the
+    product library. Successive samples take successive replicas of the set."""
 
-    from latticemontecarlo_gb300 import synthetic as S
-    from oracle import oracle as O
+    def __init__(self, seed: int, replicas: int, threads: int, steps_per_replica: int):
+        from oracle import oracle as O
+        from oracle import workload as W
+        self.O, self.W = O, W
+        cfg = W.KMC_BATCHED
+        self.elements = cfg["elements"]
+        coeffs = W.make_coefficients(self.elements, seed)
+        self.coeffs = {k: {kk: np.asarray(vv) if isinstance(vv, list) else vv for kk, vv in blk.items()}
+                       for k, blk in coeffs.items()}
+        self.seed, self.threads, self.steps = seed, threads, steps_per_replica
+        self.ns, self.temps = W.batched_edges_and_temperatures(seed, replicas, cfg["n_range"], cfg["T_range"])
+        self.next = 0
 
-    cfg = S.KMC_BATCHED
-    coeffs = S.make_coefficients(cfg["elements"], seed)
-    ns, species, temps = S.batched_replicas(seed, threads, cfg["n_range"], cfg["fractions"], cfg["T_range"],
-                                            cfg["elements"])
-    offs = np.concatenate([[0], np.cumsum(4 * ns.astype(np.int64) ** 3)])
-    jobs = []
-    for r in range(threads):
-        lat = O.Lattice(int(ns[r]))
-        m = O.Model(cfg["elements"], coeffs, lat)
-        jobs.append((lat, m, species[offs[r]:offs[r + 1]].copy(), float(temps[r])))
+    def sample(self):
+        """Runs one sample; returns (events/s over all threads, wall seconds, replica ids)."""
+        from concurrent.futures import ThreadPoolExecutor
+        O, W = self.O, self.W
+        ids = [(self.next + i) % self.ns.size for i in range(self.threads)]
+        self.next += self.threads
+        jobs = []
+        for r in ids:  # set-up outside the timed region
+            n = int(self.ns[r])
+            lat = O.Lattice(n)
+            jobs.append((lat, O.Model(self.elements, self.coeffs, lat), W.batched_replica_lattice(self.seed, r, n),
+                         float(self.temps[r])))
 
-    def one(job):
-        lat, m, sp, T = job
+        def one(job):
+            lat, m, sp, T = job
+            O.kmc(m, lat, sp, T, self.seed, self.steps, memo=True)
+
         t0 = time.perf_counter()
-        O.kmc(m, lat, sp, T, seed, steps_per_replica, memo=True)
-        return time.perf_counter() - t0
-
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes releases the GIL in the C call
-        list(ex.map(one, jobs))
-    wall = time.perf_counter() - t0
-    return threads * steps_per_replica / wall, wall
+        with ThreadPoolExecutor(max_workers=self.threads) as ex:  # ctypes releases the GIL in the C call
+            list(ex.map(one, jobs))
+        wall = time.perf_counter() - t0
+        return self.threads * self.steps / wall, wall, ids
 
 
 def cpu_cmc_baseline(threads: int, attempts: int):
-    from latticemontecarlo_gb300 import synthetic as S
+    """CanonicalMcOmp restated (batch = threads) on the CMC workload's lattice, inputs from oracle/."""
     from oracle import oracle as O
+    from oracle import workload as W
 
-    cfg = S.CMC_SINGLE
-    coeffs = S.make_coefficients(cfg["elements"], 4321)
-    sp = S.make_lattice(cfg["n"], cfg["fractions"], 0, 4321, cfg["elements"])
+    cfg = W.CMC_SINGLE
+    coeffs = W.make_coefficients(cfg["elements"], 4321)
+    sp = W.make_lattice(cfg["n"], cfg["fractions"], 0, 4321, cfg["elements"])
     lat = O.Lattice(cfg["n"])
     m = O.Model(cfg["elements"], coeffs, lat)
     os.environ["OMP_NUM_THREADS"] = str(threads)
@@ -793,32 +785,37 @@ def cpu_cmc_baseline(threads: int, attempts: int):
 
 
 def run_reference(args, rank, world):
+    """The reference's algorithm on the host cores for the GPU arm's workload and config: the oracle's
+    C restatement of KineticMcFirstOmp (the reference's own build cannot run here: see the CPU
+    baseline section of the design notes). Every step is a bounded sample of the same replica set."""
     from oracle import oracle as O
+    from oracle import workload as W
 
     O.build()
     threads = os.cpu_count() or 1
-    kmc_vals, walls = [], []
+    sampler = CpuKmcSampler(rank_seed(0), args.replicas, threads, args.kmc_steps_per_launch)
     for _ in range(args.warmup):
-        cpu_kmc_baseline(99, threads, max(50, args.cpu_kmc_steps // 10))
-    for k in range(args.steps):
-        v, w = cpu_kmc_baseline(7 + k, threads, args.cpu_kmc_steps)
-        kmc_vals.append(v)
-        walls.append(w)
-    value = float(np.mean(kmc_vals))
+        sampler.sample()
+    walls = []
+    for _ in range(args.steps):
+        walls.append(sampler.sample()[1])
+    events = threads * args.kmc_steps_per_launch * args.steps
+    value = events / float(np.sum(walls))
     cmc_v, cmc_w = cpu_cmc_baseline(threads, args.cpu_cmc_attempts)
-    sample = (f"{threads} independent KMC trajectories (one per host thread, n~U{{8..24}}), "
-              f"{args.cpu_kmc_steps} steps each per step, barrier memo on")
+    sites_total = int(np.sum(4 * sampler.ns.astype(np.int64) ** 3))
+    sample = (f"per step {threads} of the {args.replicas} replicas (one per host thread, the next {threads} each "
+              f"step), {args.kmc_steps_per_launch} KMC steps each, oracle C restatement of KineticMcFirstOmp with "
+              "barrier memo; inputs from oracle/workload.py")
     return {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(np.mean(walls) * 1e3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference algorithm)",
-        "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": "batched replica KMC (same distribution of supercells, compositions and "
-                               "temperatures), CPU sample", "threads": threads},
+        "data": "synthetic (seeded lattices and coefficients; the reference ships none)", "impl": "reference",
+        "config": kmc_config(args, world, sites_total),
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "cmc": {"value": cmc_v, "unit": "swaps/s (Metropolis attempts)", "cores": threads,
-                "sample": f"{args.cpu_cmc_attempts} attempts, batch = {threads} (CanonicalMcOmp)"},
+                "sample": f"{args.cpu_cmc_attempts} attempts, batch = {threads} (CanonicalMcOmp), {cmc_w:.1f} s"},
     }
 
 
@@ -832,7 +829,6 @@ def main():
     ap.add_argument("--kmc-steps-per-launch", type=int, default=KMC_STEPS_PER_BENCH_STEP)
     ap.add_argument("--cmc-steps", type=int, default=5)
     ap.add_argument("--cmc-sweeps-per-step", type=int, default=2)
-    ap.add_argument("--cpu-kmc-steps", type=int, default=6000)
     ap.add_argument("--cpu-cmc-attempts", type=int, default=1_500_000)
     ap.add_argument("--cmc-ref-attempts", type=int, default=400_000,
                     help="attempts of the reference-order CMC kernel (0 skips)")
@@ -860,12 +856,13 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            v, w = cpu_kmc_baseline(7, threads, args.cpu_kmc_steps)
+            sampler = CpuKmcSampler(rank_seed(0), args.replicas, threads, args.kmc_steps_per_launch)
+            v, w, ids = sampler.sample()
             result["cpu_baseline"] = {
                 "value": v, "unit": "events/s", "cores": threads, "kind": "port",
-                "sample": f"{threads} independent KMC trajectories (n~U{{8..24}}, one per host thread), "
-                          f"{args.cpu_kmc_steps} steps each, oracle C restatement with barrier memo, "
-                          f"{w:.1f} s wall"}
+                "sample": f"replicas {ids[0]}..{ids[-1]} of the same replica set (one per host thread), "
+                          f"{args.kmc_steps_per_launch} KMC steps each, oracle C restatement of KineticMcFirstOmp "
+                          f"with barrier memo, {w:.1f} s wall"}
             if "cmc" in result:
                 cv, cw = cpu_cmc_baseline(threads, args.cpu_cmc_attempts)
                 result["cmc"]["cpu_baseline"] = {

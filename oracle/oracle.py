@@ -167,7 +167,8 @@ class Model:
             code = self.code(name)
             if code < 0:
                 continue
-            arr = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in blk.items() if isinstance(v, list)}
+            arr = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in blk.items()
+                   if isinstance(v, (list, np.ndarray))}
             self._keep.append(arr)
             if "U_mm2" in arr:
                 lib().orc_model_set_quartic(

@@ -10,6 +10,9 @@ outputs are committed.
     python tests/golden/make_golden.py clusters   # only clusters_quaternary.npz
     python tests/golden/make_golden.py sitede     # only site_de_quaternary.npz
     python tests/golden/make_golden.py maps       # only map_quaternary.npz
+    python tests/golden/make_golden.py pred       # only pred_ternary.npz / pred_quaternary.npz
+    python tests/golden/make_golden.py baseline   # the benchmark configurations (KMC n=10 1e5 steps,
+                                                  # CMC n=30 batch 16), see BASELINE_CASES
 
 The fixtures pin the oracle restatement (oracle/lmc_oracle.c); the product is
 then tested against the oracle and against these fixtures directly.
@@ -47,6 +50,41 @@ CASES = {
 CLUSTER_SMALLEST, CLUSTER_BOND = 2, 3
 KMC_T, KMC_SEED, KMC_STEPS, KMC_DETAIL = 400.0, 12345, 3000, 200
 CMC_T, CMC_SEED, CMC_STEPS, CMC_BATCH = 500.0, 777, 6000, 4
+
+# The benchmark configurations at their own sizes, generated from the same seeds as bench.py. The
+# "strong" variants multiply "Base".theta by STRONG_ECI_SCALE: the synthetic pair ECIs, after the
+# reference's division by the cluster counts, give a median |dE| of about 1e-3 kT, so almost every
+# Metropolis test accepts; x800 gives a median |dE| of about kT and 40-50 % acceptance at 500 K, so
+# the rejection branch and the energy dependence of the rates are exercised.
+STRONG_ECI_SCALE = 800.0
+BASELINE_CASES = {
+    # name: (kind, elements, coeff_seed, eci_scale, n, fractions, vacancies, lattice_seed, T, rng_seed, steps)
+    "kmc_config1": ("kmc", TERNARY, 11, 1.0, 10, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 1, 11, 400.0, 5, 100_000),
+    "kmc_config1_strong": ("kmc", TERNARY, 11, STRONG_ECI_SCALE, 10, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 1, 11,
+                           400.0, 5, 100_000),
+    "cmc_config2_strong": ("cmc", QUATERNARY, 4321, STRONG_ECI_SCALE, 30,
+                           {"Al": 0.94, "Mg": 0.02, "Zn": 0.02, "Cu": 0.02}, 0, 4321, 500.0, 777, 120_000),
+}
+BASELINE_CMC_BATCH = 16
+BASELINE_SAMPLE = 50  # every 50th step's scalars are stored (the event sequence is stored in full)
+
+
+def scaled_eci(coeffs: dict, factor: float) -> dict:
+    """The coefficients with "Base".theta multiplied by `factor` (barrier blocks unchanged)."""
+    out = dict(coeffs)
+    out["Base"] = {"theta": (np.asarray(coeffs["Base"]["theta"]) * factor).tolist()}
+    return out
+
+
+def baseline_inputs(name: str):
+    """Inputs of a benchmark-configuration case: the calibrated coefficients bench.py uses, "Base".theta
+    scaled by the case's factor, and the lattice of the same seed."""
+    kind, elements, cseed, scale, n, fractions, vac, lseed, T, rseed, steps = BASELINE_CASES[name]
+    coeffs = S.make_coefficients(elements, cseed)
+    if scale != 1.0:
+        coeffs = scaled_eci(coeffs, scale)
+    species = S.make_lattice(n, fractions, vac, lseed, elements)
+    return elements, coeffs, n, species
 
 
 def case_inputs(name: str):
@@ -119,7 +157,7 @@ def parse_pred(lines, elements, coeffs):
     model = Model.create(list(elements))
     sz_mmm, sz_mm2 = model.orbit_sizes(0), model.orbit_sizes(1)
     res = {k: [] for k in ("pair", "quartic", "state_start", "state_end", "enc_mmm", "enc_mm2_fwd", "enc_mm2_bwd",
-                           "e0", "jump_ok", "pairsite")}
+                           "enc_mmm_fp", "enc_mm2_fwd_fp", "enc_mm2_bwd_fp", "e0", "jump_ok", "pairsite")}
     cur_ok = None
     for ln in lines:
         f = ln.split()
@@ -135,8 +173,10 @@ def parse_pred(lines, elements, coeffs):
         elif key in ("state_start", "state_end"):
             res[key].append([int(v) for v in vals])
         elif key == "enc_mmm":
+            res[key + "_fp"].append(np.asarray(vals, float))  # the reference's own FP vector, as printed
             res[key].append(np.rint(np.asarray(vals, float) * sz_mmm).astype(np.int32))
         elif key in ("enc_mm2_fwd", "enc_mm2_bwd"):
+            res[key + "_fp"].append(np.asarray(vals, float))
             res[key].append(np.rint(np.asarray(vals, float) * sz_mm2).astype(np.int32))
         elif key == "e0":
             res[key].append([float(v) for v in vals])
@@ -291,7 +331,75 @@ def make_map_files(tmp: Path) -> dict:
             for name in ("start.cfg", "lattice.txt", "element.txt", "map.txt")}
 
 
+def make_pred(tmp: Path, name: str) -> dict:
+    elements, coeffs, n, species = case_inputs(name)
+    els = write_inputs(tmp, elements, coeffs, species)
+    jumps, swaps = case_pairs(name, n, species)
+    allp = np.concatenate([jumps, swaps])
+    (tmp / "pairs.txt").write_text("\n".join(f"{a} {b}" for a, b in allp))
+    res = parse_pred(run(["pred", n, tmp / "species.txt", tmp / "coeffs.json", els, tmp / "pairs.txt"], tmp),
+                     elements, coeffs)
+    res["jumps"], res["swaps"] = jumps, swaps
+    return res
+
+
+def make_baseline_kmc(tmp: Path, name: str) -> dict:
+    """KineticMcFirstOmp on its mt19937_64 stream for the whole run: the selected event of every
+    step (index among the 12 jumps in id order, and the target site), every BASELINE_SAMPLE-th
+    step's barrier, energy change, total rate, time and energy, and the final state."""
+    kind, elements, *_ , T, rseed, steps = BASELINE_CASES[name]
+    _, coeffs, n, species = baseline_inputs(name)
+    els = write_inputs(tmp, elements, coeffs, species)
+    env = dict(os.environ, OMP_NUM_THREADS=str(min(12, os.cpu_count() or 1)))
+    lines = run(["kmc", n, tmp / "species.txt", tmp / "coeffs.json", els, T, rseed, steps, 0], tmp, env)
+    rows = np.asarray([[float(v) for v in ln.split()[1:]] for ln in lines if ln.startswith("step ")])
+    assert rows.shape == (steps, 9)  # steps vacancy target selected Ea dE total time energy
+    k = np.arange(0, steps, BASELINE_SAMPLE)
+    return {"target": rows[:, 2].astype(np.int32), "selected": rows[:, 3].astype(np.uint8),
+            "sample_steps": k, "sample": rows[k][:, 4:9], "final": rows[-1, 4:9],
+            "final_vacancy": int(rows[-1, 2])}
+
+
+def make_baseline_cmc(tmp: Path, name: str) -> dict:
+    """CanonicalMcOmp with a batch of BASELINE_CMC_BATCH (OpenMP threads) on its mt19937_64 stream:
+    the final lattice, the energy before every BASELINE_SAMPLE-th Metropolis test and at the end."""
+    kind, elements, *_ , T, rseed, steps = BASELINE_CASES[name]
+    _, coeffs, n, species = baseline_inputs(name)
+    els = write_inputs(tmp, elements, coeffs, species)
+    env = dict(os.environ, OMP_NUM_THREADS=str(BASELINE_CMC_BATCH))
+    lines = run(["cmc", n, tmp / "species.txt", tmp / "coeffs.json", els, T, rseed, steps], tmp, env)
+    alpha = S.alphabet(elements)
+    log = []
+    for ln in lines:
+        f = ln.split()
+        if f[0] == "log":
+            log.append(float(f[3]))  # energy column of cmc_log.txt
+        elif f[0] == "final_species":
+            final = np.asarray([alpha.index(t) for t in f[1:]], np.int8)
+        elif f[0] == "final_steps":
+            fsteps = int(f[1])
+        elif f[0] == "final_energy":
+            fenergy = [float(v) for v in f[1:]]
+    log = np.asarray(log)
+    k = np.arange(0, log.size, BASELINE_SAMPLE)
+    return {"final_species": final, "final_steps": fsteps, "final_energy": np.asarray(fenergy),
+            "sample_steps": k, "sample_energy": log[k]}
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "baseline":
+        names = sys.argv[2:] or list(BASELINE_CASES)
+        with tempfile.TemporaryDirectory() as td:
+            for name in names:
+                make = make_baseline_kmc if BASELINE_CASES[name][0] == "kmc" else make_baseline_cmc
+                np.savez_compressed(HERE / f"{name}.npz", **make(Path(td), name))
+                print(name, (HERE / f"{name}.npz").stat().st_size)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "pred":
+        with tempfile.TemporaryDirectory() as td:
+            for name in ("pred_ternary", "pred_quaternary"):
+                np.savez_compressed(HERE / f"{name}.npz", **make_pred(Path(td), name))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "maps":
         with tempfile.TemporaryDirectory() as td:
             np.savez_compressed(HERE / "map_quaternary.npz", **make_map_files(Path(td)))
@@ -311,15 +419,7 @@ def main():
         tmp = Path(td)
         np.savez_compressed(HERE / "geometry.npz", **make_geom(tmp))
         for name in ("pred_ternary", "pred_quaternary"):
-            elements, coeffs, n, species = case_inputs(name)
-            els = write_inputs(tmp, elements, coeffs, species)
-            jumps, swaps = case_pairs(name, n, species)
-            allp = np.concatenate([jumps, swaps])
-            (tmp / "pairs.txt").write_text("\n".join(f"{a} {b}" for a, b in allp))
-            res = parse_pred(run(["pred", n, tmp / "species.txt", tmp / "coeffs.json", els, tmp / "pairs.txt"], tmp),
-                             elements, coeffs)
-            res["jumps"], res["swaps"] = jumps, swaps
-            np.savez_compressed(HERE / f"{name}.npz", **res)
+            np.savez_compressed(HERE / f"{name}.npz", **make_pred(tmp, name))
         elements, coeffs, n, species = case_inputs("kmc_ternary")
         els = write_inputs(tmp, elements, coeffs, species)
         lines = run(["kmc", n, tmp / "species.txt", tmp / "coeffs.json", els, KMC_T, KMC_SEED, KMC_STEPS,

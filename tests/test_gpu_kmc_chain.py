@@ -29,9 +29,12 @@ def _compare(tr, ref):
     np.testing.assert_allclose(tr["energy"], ref[:, 7], rtol=0, atol=1e-10)
 
 
-def test_chain_reference_stream(native, oracle_mod):
+@pytest.mark.parametrize("eci_scale", [1.0, 800.0])
+def test_chain_reference_stream(native, oracle_mod, golden, eci_scale):
+    """eci_scale 800: "Base".theta scaled so |dE| ~ kT (the golden cases' STRONG_ECI_SCALE)."""
     from latticemontecarlo_gb300 import api
-    coeffs = S.make_coefficients(EL, 17)
+    G, _ = golden
+    coeffs = G.scaled_eci(S.make_coefficients(EL, 17), eci_scale)
     n = 8
     sp = S.make_lattice(n, FRAC, 1, 4, EL)
     lat = oracle_mod.Lattice(n)

@@ -114,6 +114,52 @@ def test_cmc_reference_batch(api, golden):
     np.testing.assert_allclose(e, fx["final_energy"][0], rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("name", ["kmc_config1", "kmc_config1_strong"])
+@pytest.mark.parametrize("warps,evaluation", [(1, 1), (12, 0)])
+def test_kmc_baseline_config_stream(api, golden, name, warps, evaluation):
+    """The benchmark's one-trajectory KMC configuration (n = 10, Al/Mg/Zn .96/.02/.02, 400 K) for
+    its full 1e5 steps on the reference's mt19937_64 stream: the event selected at every step is
+    the reference's (plain coefficients, and ECIs scaled so |dE| ~ kT), sparse and dense evaluation."""
+    G, load = golden
+    fx = load(name)
+    kind, el, *_, T, rseed, steps = G.BASELINE_CASES[name]
+    _, coeffs, n, sp = G.baseline_inputs(name)
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+    ctx.set_lattices([n], sp)
+    ctx.kmc_init([T], seed=rseed, rng=0, warps_per_replica=warps, replicas_per_block=1, evaluation=evaluation)
+    tr, _ = ctx.kmc_run(steps, trace_replica=0)
+    first_diff = np.flatnonzero(tr["target"] != fx["target"])
+    assert first_diff.size == 0, f"first differing step {first_diff[:1]}"
+    assert np.array_equal(tr["selected"], fx["selected"].astype(np.int32))
+    k = fx["sample_steps"]
+    ref = fx["sample"]  # Ea dE total time energy
+    np.testing.assert_allclose(tr["ea"][k], ref[:, 0], rtol=EA_RTOL)
+    np.testing.assert_allclose(tr["de"][k], ref[:, 1], rtol=0, atol=DE_ATOL * 1e3 * abs(ref[:, 1]).max())
+    np.testing.assert_allclose(tr["total_rate"][k], ref[:, 2], rtol=1e-8)
+    np.testing.assert_allclose(tr["time"][k], ref[:, 3], rtol=TIME_RTOL)
+    np.testing.assert_allclose(tr["energy"][k], ref[:, 4], rtol=0, atol=1e-8)
+    vac, nsteps, time, energy = ctx.kmc_state()
+    assert nsteps[0] == steps and vac[0] == int(fx["final_vacancy"])
+
+
+def test_cmc_baseline_config_reference_batch(api, golden):
+    """CanonicalMcOmp at the benchmark's CMC size (n = 30, 108000 sites, Al/Mg/Zn/Cu .94/.02/.02/.02,
+    500 K, batch 16) with ECIs scaled for 40-50 % acceptance, 1.2e5 attempts on the reference's
+    mt19937_64 stream: the final lattice is the reference's, and the Metropolis test rejects often."""
+    G, load = golden
+    name = "cmc_config2_strong"
+    fx = load(name)
+    kind, el, *_, T, rseed, steps = G.BASELINE_CASES[name]
+    _, coeffs, n, sp = G.baseline_inputs(name)
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+    ctx.set_lattices([n], sp)
+    e, done, acc = ctx.cmc_run(T, steps + 1, mode=0, seed=rseed, batch=G.BASELINE_CMC_BATCH)
+    assert done == int(fx["final_steps"])
+    assert np.array_equal(ctx.get_lattices(), fx["final_species"])
+    np.testing.assert_allclose(e, fx["final_energy"][0], rtol=0, atol=1e-9)
+    assert 0.3 < acc / done < 0.7, acc / done
+
+
 def _replay_check(api, oracle_mod, G, el, coeffs, ns, species, replica, trace, ev, every=7):
     """Replays a traced replica on the host and checks the traced events of
     every `every`-th step against the oracle's barriers for that lattice."""

@@ -12,11 +12,15 @@ pytestmark = pytest.mark.gpu
 EL = ("Al", "Mg", "Zn")
 
 
-@pytest.mark.parametrize("T0,fractions", [(800.0, {"Al": 0.9, "Mg": 0.05, "Zn": 0.05}),
-                                          (150.0, {"Al": 0.8, "Mg": 0.1, "Zn": 0.1})])
-def test_sa_against_oracle(native, oracle_mod, T0, fractions):
+# eci_scale 800: "Base".theta scaled so |dE| ~ kT (STRONG_ECI_SCALE of the golden cases), so the
+# Metropolis test rejects often and the reheat / cool-down schedule sees real energy changes
+@pytest.mark.parametrize("T0,fractions,eci_scale", [(800.0, {"Al": 0.9, "Mg": 0.05, "Zn": 0.05}, 1.0),
+                                                    (150.0, {"Al": 0.8, "Mg": 0.1, "Zn": 0.1}, 1.0),
+                                                    (600.0, {"Al": 0.9, "Mg": 0.05, "Zn": 0.05}, 800.0)])
+def test_sa_against_oracle(native, oracle_mod, golden, T0, fractions, eci_scale):
     from latticemontecarlo_gb300 import api
-    coeffs = S.make_coefficients(EL, 9)
+    G, _ = golden
+    coeffs = G.scaled_eci(S.make_coefficients(EL, 9), eci_scale)
     n = 8
     sp = S.make_lattice(n, fractions, 0, 3, EL)
     lat = oracle_mod.Lattice(n)
@@ -39,6 +43,8 @@ def test_sa_against_oracle(native, oracle_mod, T0, fractions):
     np.testing.assert_allclose([T, e, lowest], ref_state[1:], rtol=1e-12, atol=1e-10)
     assert np.array_equal(ctx.get_lattices(), ref_sp)
     assert 0.05 < tr["accepted"].mean() < 0.999 and T < T0
+    if eci_scale > 1:
+        assert tr["accepted"].mean() < 0.7
 
 
 def test_sa_single_species_rejected(native):

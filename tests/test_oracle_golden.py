@@ -82,6 +82,36 @@ def test_predictors(oracle_mod, golden, name):
     assert np.array_equal(counts / bonds[labels], fx["census_encode"])
 
 
+def _feature_orbit_sizes(records, e: int) -> np.ndarray:
+    """Per one-hot feature, the size of its orbit, from the reference's own MMM / MM2 mapping
+    (GetOneHotParametersFromMap, EnergyUtility.cpp:753-792): an orbit of singlets has e features,
+    of ordered pairs e^2, of symmetric pairs (flag -1) e(e+1)/2; each feature is the orbit's summed
+    one-hot vector divided by the number of clusters in the orbit."""
+    sizes = []
+    for o in range(int(records[:, 0].max()) + 1):
+        r = records[records[:, 0] == o]
+        if r[0, 1] == -1:
+            width = e * (e + 1) // 2
+        else:
+            width = e ** int(np.sum(r[0, 1:] >= 0))
+        sizes += [len(r)] * width
+    return np.asarray(sizes, float)
+
+
+@pytest.mark.parametrize("name", ["pred_ternary", "pred_quaternary"])
+def test_onehot_vectors_are_the_references(golden, name):
+    """The integer one-hot numerators the GPU tests compare against are the reference's own FP
+    vectors times orbit sizes taken from the reference's own mapping: numerator / size reproduces
+    every printed FP feature exactly."""
+    G, load = golden
+    fx, gz = load(name), load("geometry")
+    e = len(G.CASES[name][0])
+    for key, mkey in (("enc_mmm", "map_mmm"), ("enc_mm2_fwd", "map_mm2"), ("enc_mm2_bwd", "map_mm2")):
+        sizes = _feature_orbit_sizes(gz[mkey], e)
+        assert sizes.size == fx[key].shape[1] == fx[key + "_fp"].shape[1]
+        assert np.array_equal(fx[key] / sizes, fx[key + "_fp"]), key
+
+
 def test_mt19937_and_distributions(oracle_mod, golden):
     G, load = golden
     fx = load("rng")
@@ -134,3 +164,54 @@ def test_cmc_trajectory(oracle_mod, golden):
     assert np.array_equal(sp2, fx["final_species"])
     np.testing.assert_allclose(trace, fx["log"][:, 2], rtol=0, atol=1e-15)
     np.testing.assert_allclose(e, fx["final_energy"][0], rtol=0, atol=1e-15)
+
+
+def _baseline_kmc_check(oracle_mod, G, fx, name):
+    """The oracle's KineticMcFirstOmp over the whole run of a benchmark-configuration fixture."""
+    kind, el, *_, T, rseed, steps = G.BASELINE_CASES[name]
+    _, coeffs, n, sp = G.baseline_inputs(name)
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    tr, _ = oracle_mod.kmc(m, lat, sp, T, rseed, steps, memo=True)
+    return tr
+
+
+def test_baseline_kmc_trajectories(oracle_mod, golden):
+    """KMC of the benchmark's one-trajectory configuration (n = 10, Al/Mg/Zn .96/.02/.02, 400 K) for
+    its full 1e5 steps, with the benchmark's coefficients and with the ECIs scaled so |dE| ~ kT: the
+    oracle selects the reference's event at every step (the two runs in parallel threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+    G, load = golden
+    names = ["kmc_config1", "kmc_config1_strong"]
+    with ThreadPoolExecutor(2) as ex:
+        trs = list(ex.map(lambda nm: _baseline_kmc_check(oracle_mod, G, load(nm), nm), names))
+    for name, tr in zip(names, trs):
+        fx = load(name)
+        assert np.array_equal(tr[:, 1], fx["target"]), name
+        assert np.array_equal(tr[:, 2], fx["selected"]), name
+        k = fx["sample_steps"]
+        got, ref = tr[k][:, 3:8], fx["sample"]  # Ea dE total time energy
+        # barriers, energy changes and energies bit for bit; the total rate and the clock to the last
+        # bit or two (the reference's OpenMP reduction order of the 12 rates is not sequential)
+        assert np.array_equal(got[:, [0, 1, 4]], ref[:, [0, 1, 4]]), name
+        np.testing.assert_allclose(got[:, 2:4], ref[:, 2:4], rtol=1e-15, atol=0)
+
+
+def test_baseline_cmc_trajectory(oracle_mod, golden):
+    """CanonicalMcOmp at the benchmark's CMC size (n = 30, 108000 sites, batch 16) with ECIs scaled
+    for 40-50 % acceptance at 500 K, 1.2e5 attempts: the oracle's final lattice and energies are the
+    reference's."""
+    G, load = golden
+    name = "cmc_config2_strong"
+    fx = load(name)
+    kind, el, *_, T, rseed, steps = G.BASELINE_CASES[name]
+    _, coeffs, n, sp = G.baseline_inputs(name)
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    done, e, acc, trace = oracle_mod.cmc(m, lat, sp, T, rseed, steps + 1, G.BASELINE_CMC_BATCH, 0.0, trace=True)
+    assert done == int(fx["final_steps"])
+    assert np.array_equal(sp, fx["final_species"])
+    # the running energy to rounding (its dE terms are summed in the restatement's order)
+    np.testing.assert_allclose(trace[fx["sample_steps"]], fx["sample_energy"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(e, fx["final_energy"][0], rtol=0, atol=1e-12)
+    assert 0.3 < acc / done < 0.7, acc / done
