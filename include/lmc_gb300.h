@@ -275,7 +275,14 @@ typedef struct lmc_kmc_options {
                               first jump, deterministic second-order time, one uniform draw for the
                               selection; one block of 12 warps per replica. Not combined with early_stop,
                               lmc_kmc_run_graph or lmc_kmc_autotune; no events12 output. */
+  int rates;               /* LMC_RATES_FP32 (default) or LMC_RATES_FP64, for the first-order KMC on
+                              LMC_RNG_PHILOX streams: FP32 barriers and rates (within 1e-6 relative of the
+                              FP64 ones), FP64 rate sum and clock, exact energy sums. The reference's
+                              mt19937_64 stream, the chain KMC and the multi-vacancy KMC always use FP64. */
 } lmc_kmc_options;
+
+#define LMC_RATES_FP32 0
+#define LMC_RATES_FP64 1
 
 /* Jump evaluation inside the KMC kernel: both give bit-identical barriers.
  * Sparse: constant all-solvent sums plus corrections for the clusters that touch

@@ -28,6 +28,8 @@ LMC_RNG_MT19937_64 = 0
 LMC_RNG_PHILOX = 1
 LMC_EVAL_SPARSE = 0
 LMC_EVAL_DENSE = 1
+LMC_RATES_FP32 = 0
+LMC_RATES_FP64 = 1
 LMC_CMC_REFERENCE_BATCH = 0
 LMC_CMC_THROUGHPUT = 1
 
@@ -65,7 +67,7 @@ class KmcOptions(C.Structure):
         ("rng", C.c_int), ("seed", C.c_uint64), ("barrier_kind", C.c_int), ("rate_corrector", C.c_int),
         ("tt_time", C.POINTER(C.c_double)), ("tt_temp", C.POINTER(C.c_double)), ("tt_len", C.c_int),
         ("warps_per_replica", C.c_int), ("replicas_per_block", C.c_int), ("evaluation", C.c_int),
-        ("early_stop", C.c_int), ("chain", C.c_int),
+        ("early_stop", C.c_int), ("chain", C.c_int), ("rates", C.c_int),
     ]
 
 

@@ -172,11 +172,12 @@ class Context:
     # kinetic MC -----------------------------------------------------------
     def kmc_init(self, temperatures, seed: int = 0, rng: int = N.LMC_RNG_PHILOX, kind: int = N.LMC_BARRIER_QUARTIC,
                  rate_corrector: bool = False, tt=None, warps_per_replica: int = 0, replicas_per_block: int = 0,
-                 evaluation: int = N.LMC_EVAL_SPARSE, early_stop: bool = False, chain: bool = False):
+                 evaluation: int = N.LMC_EVAL_SPARSE, early_stop: bool = False, chain: bool = False,
+                 rates: int = N.LMC_RATES_FP32):
         temps = np.ascontiguousarray(np.broadcast_to(np.asarray(temperatures, np.float64), (self.ns.size,)))
         self._tt = None
         opt = N.KmcOptions(rng, seed, kind, int(rate_corrector), None, None, 0, warps_per_replica,
-                           replicas_per_block, evaluation, int(early_stop), int(chain))
+                           replicas_per_block, evaluation, int(early_stop), int(chain), rates)
         if tt is not None:
             t0, t1 = _f64(tt[0]), _f64(tt[1])
             self._tt = (t0, t1)

@@ -387,6 +387,34 @@ void BuildTables(lmc_ctx *c) {
   t.w_ks = c->Upload(wks);
   t.w_e0 = c->Upload(we0);
   t.form = c->Upload(form);
+  {
+    // FP32 epilogue tables: the sums' integer centres C = round(c / scale) (exact integer
+    // deviations S - C on the device) and the folded constants, from extended precision
+    std::vector<long long> fc(lmc::kMaxSlots * 3, 0);
+    std::vector<float> f32(lmc::kMaxSlots * 8, 0.0f);
+    Require(fm.de_shift < 126, LMC_ERR_UNSUPPORTED, "energy-change scale outside the FP32 range");
+    for (int sidx = 0; sidx < slots; ++sidx) {
+      const lmc::FoldedForm *forms[3] = {&fm.quartic_d[sidx], &fm.quartic_ks[sidx], &fm.e0[sidx]};
+      long double lc[3];  // mu - sigma * (c - C scale): the form's value at S = C
+      for (int q = 0; q < 3; ++q) {
+        const long double sc = std::ldexp(1.0L, -forms[q]->shift);
+        const long double centre = std::nearbyint(static_cast<long double>(forms[q]->c) / sc);
+        Require(std::fabs(centre) < 9.0e18L, LMC_ERR_UNSUPPORTED, "linear-form centre outside int64");
+        fc[sidx * 3 + q] = static_cast<long long>(centre);
+        lc[q] = forms[q]->mu - forms[q]->sigma * (forms[q]->c - centre * sc);
+      }
+      f32[sidx * 8 + 0] = static_cast<float>(2.0L * forms[0]->sigma * std::ldexp(1.0L, -forms[0]->shift));
+      f32[sidx * 8 + 1] = static_cast<float>(forms[1]->sigma * std::ldexp(1.0L, -forms[1]->shift));
+      f32[sidx * 8 + 2] = static_cast<float>(std::exp(2.0L * lc[0] + lc[1]));
+      f32[sidx * 8 + 3] = static_cast<float>(forms[2]->sigma * std::ldexp(1.0L, -forms[2]->shift));
+      f32[sidx * 8 + 4] = static_cast<float>(std::exp(lc[2]));
+      f32[sidx * 8 + 7] = std::ldexp(1.0f, -fm.de_shift);
+      for (int q = 0; q < 8; ++q)
+        Require(std::isfinite(f32[sidx * 8 + q]), LMC_ERR_UNSUPPORTED, "barrier constants outside the FP32 range");
+    }
+    t.form32_c = c->Upload(fc);
+    t.form32 = c->Upload(f32);
+  }
   // ExpFast constants: 2^(j/256) rounded from extended precision; ln2/256
   // split into a 34-bit head (exact products with |n| < 2^18) and a tail
   {
@@ -637,6 +665,7 @@ lmc::KmcLaunch KmcShape(const lmc_ctx *ctx) {
   l.replicas_per_block = rpb;
   l.sparse = ctx->kmc_opt.evaluation == LMC_EVAL_DENSE ? 0 : 1;
   l.mt = ctx->kmc_opt.rng == LMC_RNG_MT19937_64 ? 1 : 0;
+  l.f32 = !l.mt && ctx->kmc_opt.rates == LMC_RATES_FP32 ? 1 : 0;
   l.sp = ctx->sparse;
   return l;
 }
@@ -698,7 +727,8 @@ std::string KmcTuneKey(const lmc_ctx *ctx) {
   }
   k += "|E=" + std::to_string(ctx->fm.num_species) + "|kind=" + std::to_string(ctx->kmc_opt.barrier_kind) +
        "|rng=" + std::to_string(ctx->kmc_opt.rng) + "|stop=" + std::to_string(ctx->kmc_opt.early_stop ? 1 : 0) +
-       "|tt=" + std::to_string(ctx->tt_len > 0 ? 1 : 0) + "|corr=" + std::to_string(ctx->kmc_opt.rate_corrector ? 1 : 0);
+       "|tt=" + std::to_string(ctx->tt_len > 0 ? 1 : 0) + "|corr=" + std::to_string(ctx->kmc_opt.rate_corrector ? 1 : 0) +
+       "|rates=" + std::to_string(ctx->kmc_opt.rates);
   return k;
 }
 
@@ -1490,6 +1520,8 @@ int lmc_kmc_init(lmc_ctx *ctx, const double *temperature, const lmc_kmc_options 
     Require(opt->rng == LMC_RNG_MT19937_64 || opt->rng == LMC_RNG_PHILOX, LMC_ERR_INVALID_ARGUMENT, "unknown rng");
     Require(opt->barrier_kind == LMC_BARRIER_QUARTIC || opt->barrier_kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT,
             "unknown barrier kind");
+    Require(opt->rates == LMC_RATES_FP32 || opt->rates == LMC_RATES_FP64, LMC_ERR_INVALID_ARGUMENT,
+            "unknown rate precision");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     const int R = ctx->num_replicas;
     for (int r = 0; r < R; ++r)

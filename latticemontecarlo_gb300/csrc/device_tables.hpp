@@ -59,6 +59,12 @@ struct DevTables {
   const long long *w_ks;         // [slot][f_mm2]
   const long long *w_e0;         // [slot][f_mmm]
   const double *form;            // [kMaxSlots][12]: {d: scale, c, sigma, mu}, {ks: ...}, {e0: ...}
+  // FP32 epilogue (production KMC streams): per slot the integer centres of the three sums and
+  //   [0] 2 sigma_D scale_D, [1] sigma_Ks scale_Ks, [2] P0 = Ks D^2 at the centres,
+  //   [3] sigma_e0 scale_e0, [4] e0 at the centre, [7] the energy-change scale
+  // so that P = P0 exp([0] (S_D - C_D) + [1] (S_Ks - C_Ks)) and e0 = [4] exp([3] (S_e0 - C_e0)).
+  const long long *form32_c;     // [kMaxSlots][3]
+  const float *form32;           // [kMaxSlots][8]
   const double *exp_tab;         // [256] 2^(j/256) for ExpFast
   double exp_l1, exp_l2;         // ln2/256 split for ExpFast
   const double *theta;           // [num_theta]

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "fastmath.cuh"
@@ -255,6 +256,41 @@ __device__ __forceinline__ JumpOut JumpEpilogue(const DevTables &t, const ExpCon
     o.ea = fmax(0.0, v + o.de / 2);
     o.d_or_e0 = v;
     o.ks = 0.0;
+  }
+  return o;
+}
+
+// Exact-to-rounding int64 -> float on the FP32 / integer pipes: v = hi 2^32 + lo with a signed
+// low half (|lo| <= 2^31), so small values convert exactly and large ones within 1.5 ulp.
+__device__ __forceinline__ float I64ToFloat(long long v) {
+  const int lo = static_cast<int>(static_cast<unsigned>(v));
+  const int hi = static_cast<int>((v - lo) >> 32);
+  return fmaf(static_cast<float>(hi), 4294967296.0f, static_cast<float>(lo));
+}
+
+// FP32 epilogue of one jump for the production streams (barriers within 1e-6 relative of the
+// FP64 epilogue): the integer sums are centred exactly (S - C), so only the small deviations
+// are rounded, and P = Ks D^2 = P0 exp(a_D (S_D - C_D) + a_Ks (S_Ks - C_Ks)). With x = dE / P
+// the closed form above is Ea = P / 64 (1 + 12 x)^2 (1 + 8 x - 48 x^2).
+struct JumpOutF {
+  float ea, de;
+};
+__device__ __forceinline__ JumpOutF JumpEpilogueF32(const DevTables &t, int kind, int slot, long long acc_de,
+                                                    long long acc_d, long long acc_ks) {
+  const float *f = t.form32 + slot * 8;
+  const long long *c = t.form32_c + slot * 3;
+  JumpOutF o;
+  o.de = I64ToFloat(acc_de) * f[7];
+  if (kind == 0) {
+    const float dev = fmaf(f[0], I64ToFloat(acc_d - c[0]), f[1] * I64ToFloat(acc_ks - c[1]));
+    const float p = f[2] * expf(dev);
+    const float x = o.de * __frcp_rn(p);
+    const float a = fmaf(12.0f, x, 1.0f);
+    const float b = fmaf(x, fmaf(-48.0f, x, 8.0f), 1.0f);
+    o.ea = p * 0.015625f * a * a * b;
+  } else {
+    const float e0 = f[4] * expf(f[3] * I64ToFloat(acc_d - c[2]));
+    o.ea = fmaxf(0.0f, fmaf(0.5f, o.de, e0));  // VacancyMigrationPredictorE0.cpp:153-159
   }
   return o;
 }
@@ -1085,6 +1121,7 @@ struct KmcShared {
   long long ids[12];
   double beta;
   double corr;
+  float beta_f;                     // beta rounded to FP32 (FP32 rates)
   int stop;
   int dsel;                         // direction index of the selected jump
   int escaped;                      // early stop: this step's vacancy had only solvent in its 1-3NN shells
@@ -1429,6 +1466,22 @@ __device__ __noinline__ double2 MtStepDraws(Mt mt) {
   return make_double2(nlog, u2);
 }
 
+// Time increment of a step with FP32 rates: the 12 rates are exp(lmin - Ea_i beta), relative to
+// the fastest event (lmin = min Ea_i beta), and `total` is their FP64 sum, so
+//   dt = -log(u1) / (total exp(-lmin) 1e13) * corr,
+// with exp(lmin) = 2^yi 2^(y - yi), y = lmin log2(e): 2^yi exact in FP64, the rest in FP32.
+__device__ __noinline__ double KmcDtWide(double nlog_u1, double total, float lmin, double corr) {
+  return nlog_u1 * exp(static_cast<double>(lmin)) / (total * kPrefactor) * corr;
+}
+__device__ __forceinline__ double KmcDtF32(double nlog_u1, double total, float lmin, double corr) {
+  const float y = lmin * 1.44269504088896341f;
+  if (!(fabsf(y) < 1000.0f)) return KmcDtWide(nlog_u1, total, lmin, corr);
+  const float yi = floorf(y);
+  const float f = exp2f(y - yi) * __frcp_rn(__double2float_rn(total) * 1e13f);
+  const double p2 = __hiloint2double((static_cast<int>(yi) + 1023) << 20, 0);
+  return nlog_u1 * static_cast<double>(f) * p2 * corr;
+}
+
 // Synchronises the warps of one replica only: nothing for a single warp
 // (beyond the warp itself), a named barrier (id 1 + replica slot) otherwise,
 // so replicas sharing a block never wait for one another.
@@ -1444,9 +1497,13 @@ __device__ __forceinline__ void ReplicaSync(int g_per, int rl) {
 // resident blocks per SM; 1 up to 384 threads (12 warps per replica), 2
 // resident blocks; 2 one block per SM of up to 28 single-warp replicas (one
 // copy of the staged tables per SM, 72 registers per thread).
+// kF32 (production Philox streams only): barriers and rates in FP32 (JumpEpilogueF32, rates
+// relative to the fastest event), the rate sum and the clock in FP64, the energy in exact
+// fixed point. Without it (and always on the reference's mt19937_64 stream) the epilogue,
+// rates, sum and clock are FP64 as in the reference.
 constexpr int kShapeThreads[3] = {256, 384, 896};
 constexpr int kShapeBlocks[3] = {4, 2, 1};
-template <bool kSparse, int kShape, bool kMt>
+template <bool kSparse, int kShape, bool kMt, bool kF32>
 __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     kmc_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcDevState s,
                const __grid_constant__ KmcLaunch l) {
@@ -1478,8 +1535,11 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   int8_t *lat = species + (active ? s.lat_off[r] : 0);
   long long vac = active ? s.vacancy[r] : 0;
   const bool leader = g == 0 && lane == 0;
+  static_assert(!(kMt && kF32), "the reference's stream keeps the FP64 epilogue");
+  using Real = typename std::conditional<kF32, float, double>::type;
   unsigned bad_all = 0;
   double time = 0, energy = 0;
+  long long energy_fix = 0;  // FP32 mode: this launch's energy change in the dE fixed point (exact)
   unsigned long long step0 = 0, steps_done = 0;
   if (active && leader) {
     time = s.time[r];
@@ -1501,7 +1561,10 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     mt.idx = w + 2 * 312;
   }
   if (!active || (s.early_stop && s.escaped[r])) return;  // no block-wide barrier below this point
-  if (leader && s.tt_len == 0) TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
+  if (leader && s.tt_len == 0) {
+    TemperatureFactors(s, r, s.temperature[r], &rs.beta, &rs.corr);
+    rs.beta_f = static_cast<float>(rs.beta);
+  }
   H3 hv = SiteCoord(vac, n);  // vacancy coordinates, advanced by the selected direction each step
   for (unsigned long long it = 0; it < l.steps; ++it) {
     // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
@@ -1516,8 +1579,10 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
         rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
       }
       if (leader) {
-        if (s.tt_len > 0)
+        if (s.tt_len > 0) {
           TemperatureFactors(s, r, InterpT(s.tt_time, s.tt_temp, s.tt_len, time), &rs.beta, &rs.corr);
+          rs.beta_f = static_cast<float>(rs.beta);
+        }
         rs.stop = (l.stop_flag && (it & 63) == 0 && *l.stop_flag) ? 1 : 0;
       }
     }
@@ -1545,19 +1610,45 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     ReplicaSync(g_per, rl);
     // ---- phase 3: rates, selection, update (warp 0 of the replica) ----
     if (active && g == 0) {
-      double ea = 0, de = 0, k = 0;
+      Real ea = 0, de = 0;
+      double k = 0;
+      float lmin = 0.0f;  // FP32 mode: min Ea beta over the 12 events
       long long id = 0x7fffffffffffffffLL;
-      if (lane < 12) {
-        const int slot = rs.slot[lane];
-        id = rs.ids[lane];
-        if (slot >= 0) {
-          const JumpOut o =
-              JumpEpilogue(t, ec, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
-          ea = o.ea;
-          de = o.de;
-          k = ExpFast(-ea * rs.beta, ec);  // JumpEvent forward rate (JumpEvent.cpp:6-13)
-        } else if (slot == -1) {
-          bad_all |= kStatusNoCoefficients;
+      if constexpr (kF32) {
+        bool ok = false;
+        if (lane < 12) {
+          const int slot = rs.slot[lane];
+          id = rs.ids[lane];
+          if (slot >= 0) {
+            const JumpOutF o =
+                JumpEpilogueF32(t, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+            ea = o.ea;
+            de = o.de;
+            ok = true;
+          } else if (slot == -1) {
+            bad_all |= kStatusNoCoefficients;
+          }
+        }
+        const float lb = ok ? ea * rs.beta_f : INFINITY;
+        lmin = lb;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+        lmin = __shfl_sync(0xffffffffu, lmin, 0);
+        // JumpEvent forward rate (JumpEvent.cpp:6-13), relative to exp(-lmin)
+        k = ok ? static_cast<double>(expf(lmin - lb)) : 0.0;
+      } else {
+        if (lane < 12) {
+          const int slot = rs.slot[lane];
+          id = rs.ids[lane];
+          if (slot >= 0) {
+            const JumpOut o =
+                JumpEpilogue(t, ec, s.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
+            ea = o.ea;
+            de = o.de;
+            k = ExpFast(-ea * rs.beta, ec);  // JumpEvent forward rate (JumpEvent.cpp:6-13)
+          } else if (slot == -1) {
+            bad_all |= kStatusNoCoefficients;
+          }
         }
       }
       // lane q takes the event of rank q in the id-sorted 1NN list
@@ -1570,8 +1661,8 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       for (int q = 0; q < 12; ++q)
         if (__shfl_sync(0xffffffffu, rank, q) == lane) src = q;
       const double k_s = __shfl_sync(0xffffffffu, k, src);
-      const double ea_s = __shfl_sync(0xffffffffu, ea, src);
-      const double de_s = __shfl_sync(0xffffffffu, de, src);
+      const Real ea_s = __shfl_sync(0xffffffffu, ea, src);
+      const Real de_s = __shfl_sync(0xffffffffu, de, src);
       const long long id_s = __shfl_sync(0xffffffffu, id, src);
       // total rate and prefix sums, sequential in id order (the reference's
       // single-thread reduction, KineticMcFirstOmp.cpp:55-68)
@@ -1628,13 +1719,19 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       const int sel = ballot ? __ffs(ballot) - 1 : 11;  // past the end: the last event
       const int dsel = __shfl_sync(0xffffffffu, src, sel);
       const long long tgt = __shfl_sync(0xffffffffu, id_s, sel);
-      const double ea_sel = __shfl_sync(0xffffffffu, ea_s, sel);
-      const double de_sel = __shfl_sync(0xffffffffu, de_s, sel);
+      const Real ea_sel = __shfl_sync(0xffffffffu, ea_s, sel);
+      const Real de_sel = __shfl_sync(0xffffffffu, de_s, sel);
       if (lane == 0) {
         if (!(total > 0.0) || !isfinite(total)) bad_all |= kStatusNumeric;
-        const double dt = nlog_u1 * RcpFast(total * kPrefactor) * rs.corr;
+        double dt;
+        if constexpr (kF32) {
+          dt = KmcDtF32(nlog_u1, total, lmin, rs.corr);
+          energy_fix += rs.acc[dsel][0];
+        } else {
+          dt = nlog_u1 * RcpFast(total * kPrefactor) * rs.corr;
+          energy += de_sel;
+        }
         time += dt;
-        energy += de_sel;
         lat[vac] = lat[tgt];  // Config::LatticeJump: the migrating atom takes the vacancy site
         lat[tgt] = static_cast<int8_t>(t.x_code);
         if (r == l.trace_replica && l.trace) {
@@ -1645,9 +1742,9 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
           rec.slot = 0;
           rec.ea = ea_sel;
           rec.de = de_sel;
-          rec.total_rate = total;
+          rec.total_rate = kF32 ? total * exp(-static_cast<double>(lmin)) : total;
           rec.time = time;
-          rec.energy = energy;
+          rec.energy = kF32 ? energy + static_cast<double>(energy_fix) * t.de_scale : energy;
           l.trace[it] = rec;
         }
         rs.ids[0] = tgt;
@@ -1686,7 +1783,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   if (active && leader) {
     s.vacancy[r] = vac;
     s.time[r] = time;
-    s.energy[r] = energy;
+    s.energy[r] = kF32 ? energy + static_cast<double>(energy_fix) * t.de_scale : energy;
     s.steps[r] = step0 + steps_done;
   }
   if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
@@ -3325,15 +3422,27 @@ using KmcKernelFn = void (*)(DevTables, int8_t *, KmcDevState, KmcLaunch);
 static KmcKernelFn KmcKernelFor(const KmcLaunch &l) {
   const int threads = l.warps_per_replica * l.replicas_per_block * 32;
   const int shape = threads <= kShapeThreads[0] ? 0 : (threads <= kShapeThreads[1] ? 1 : 2);
-  // the RNG kind is a template parameter so the Philox instances carry no mt19937_64 code (and back)
+  // the RNG kind and the epilogue precision are template parameters so the Philox instances carry
+  // no mt19937_64 code (and back) and the FP32 instances no FP64 epilogue
   if (l.mt) {
     if (l.sparse)
-      return shape == 0 ? kmc_kernel<true, 0, true> : (shape == 1 ? kmc_kernel<true, 1, true> : kmc_kernel<true, 2, true>);
-    return shape == 0 ? kmc_kernel<false, 0, true> : (shape == 1 ? kmc_kernel<false, 1, true> : kmc_kernel<false, 2, true>);
+      return shape == 0 ? kmc_kernel<true, 0, true, false>
+                        : (shape == 1 ? kmc_kernel<true, 1, true, false> : kmc_kernel<true, 2, true, false>);
+    return shape == 0 ? kmc_kernel<false, 0, true, false>
+                      : (shape == 1 ? kmc_kernel<false, 1, true, false> : kmc_kernel<false, 2, true, false>);
+  }
+  if (l.f32) {
+    if (l.sparse)
+      return shape == 0 ? kmc_kernel<true, 0, false, true>
+                        : (shape == 1 ? kmc_kernel<true, 1, false, true> : kmc_kernel<true, 2, false, true>);
+    return shape == 0 ? kmc_kernel<false, 0, false, true>
+                      : (shape == 1 ? kmc_kernel<false, 1, false, true> : kmc_kernel<false, 2, false, true>);
   }
   if (l.sparse)
-    return shape == 0 ? kmc_kernel<true, 0, false> : (shape == 1 ? kmc_kernel<true, 1, false> : kmc_kernel<true, 2, false>);
-  return shape == 0 ? kmc_kernel<false, 0, false> : (shape == 1 ? kmc_kernel<false, 1, false> : kmc_kernel<false, 2, false>);
+    return shape == 0 ? kmc_kernel<true, 0, false, false>
+                      : (shape == 1 ? kmc_kernel<true, 1, false, false> : kmc_kernel<true, 2, false, false>);
+  return shape == 0 ? kmc_kernel<false, 0, false, false>
+                    : (shape == 1 ? kmc_kernel<false, 1, false, false> : kmc_kernel<false, 2, false, false>);
 }
 
 cudaError_t KmcOccupancy(const DevTables &t, const KmcLaunch &l, int *blocks_per_sm, size_t *shared_bytes) {

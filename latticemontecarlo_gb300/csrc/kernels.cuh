@@ -92,6 +92,7 @@ struct KmcLaunch {
   int *status;                   // device status word (bit flags)
   int sparse;                    // 1: sparse solute corrections, 0: dense cluster sums
   int mt;                        // 1: mt19937_64 stream (KmcDevState::rng_kind 0), 0: Philox
+  int f32;                       // 1 (Philox only): FP32 barriers and rates, FP64 rate sum and clock
   KmcSparse sp;
 };
 

@@ -88,7 +88,7 @@ def test_single_vacancy_equals_kmc_kernel(native):
     ns, sp, temps = S.batched_replicas(6, 40, n_range=(8, 12), fractions=FRAC)
     single = api.Context(api.Model.from_coefficients(coeffs, list(EL)))
     single.set_lattices(ns, sp)
-    single.kmc_init(temps, seed=5, rng=native.LMC_RNG_PHILOX)
+    single.kmc_init(temps, seed=5, rng=native.LMC_RNG_PHILOX, rates=native.LMC_RATES_FP64)
     single.kmc_run(200)
     multi = api.Context(api.Model.from_coefficients(coeffs, list(EL)))
     multi.set_lattices(ns, sp)
