@@ -394,6 +394,24 @@ int lmc_site_de_batch(lmc_ctx *ctx, int replica, const int64_t *sites, const int
 int lmc_exit_time_energies(lmc_ctx *ctx, int replica, int solvent_code, const double *chemical_potential,
                            double *binding, double *profile);
 
+/* ExitTime::GetExitTimeInfo's per-cluster quantities (ExitTime.cpp:53-128) for `num_clusters`
+ * clusters of lattice `replica` given as CSR lattice-id lists (offsets [num_clusters + 1],
+ * members; e.g. from lmc_solute_cluster_get). For each cluster S and its first-neighbour shell T:
+ * markov_escape_time = ExitTime::BuildMarkovChain (ExitTime.cpp:165-216) over the states S u T
+ * (start probabilities ~ exp(-profile_energy beta_escape), rates 1e13 exp(-Ea beta_escape), jumps
+ * out of S u T absorbing), neighbor_size = |T|, barriers [num_clusters][8] = the mean and the
+ * population standard deviation of Ea - dE / 2 over the jumps in / to / on / off the cluster
+ * (GetAverageBarriers, ExitTime.cpp:311-399; NaN when a category is empty) and
+ * effective_binding_energy = -ln(escape_time 1e13) / beta_escape + mean_off (ExitTime.cpp:121).
+ * profile_energy: the lattice's per-site profile energies (lmc_exit_time_energies). The barriers
+ * are the Quartic ones of lmc_site_jump_energetics (the lattice's vacancy read as solvent_code) on
+ * the GPU; each chain's linear system is solved on the host (at most 4096 states). Any output may
+ * be NULL. */
+int lmc_exit_time_clusters(lmc_ctx *ctx, int replica, int solvent_code, double escape_temperature,
+                           const int64_t *offsets, const int64_t *members, int64_t num_clusters,
+                           const double *profile_energy, double *markov_escape_time, int64_t *neighbor_size,
+                           double *barriers, double *effective_binding_energy);
+
 /* ------------------------------------------------------------------------- */
 /* Solute clusters (ansys::SoluteCluster)                                     */
 /* ------------------------------------------------------------------------- */

@@ -267,6 +267,24 @@ class Context:
         names = [alpha[c] for c in range(len(alpha)) if c != x]
         return {nm: binding[k] for k, nm in enumerate(names)}, profile
 
+    def exit_time_clusters(self, clusters, solvent: int, escape_temperature: float, profile, replica: int = 0):
+        """ExitTime's per-cluster quantities (ExitTime.cpp:72-128) for the given clusters (site-id
+        arrays, e.g. from solute_clusters): Markov-chain escape time (BuildMarkovChain), neighbour-
+        shell size, barriers [mean in/to/on/off, std in/to/on/off] (GetAverageBarriers) and the
+        effective binding energy; `profile` is exit_time_energies' profile array."""
+        k = len(clusters)
+        off = np.concatenate([[0], np.cumsum([len(c) for c in clusters])]).astype(np.int64)
+        mem = np.ascontiguousarray(np.concatenate(clusters) if k else np.zeros(1), np.int64)
+        prof = np.ascontiguousarray(profile, np.float64)
+        esc, eff = np.zeros(max(k, 1)), np.zeros(max(k, 1))
+        nsz = np.zeros(max(k, 1), np.int64)
+        bar = np.zeros((max(k, 1), 8))
+        check(N.lib.lmc_exit_time_clusters(self._h, replica, solvent, escape_temperature, ptr(off, C.c_int64),
+                                           ptr(mem, C.c_int64), k, ptr(prof, C.c_double), ptr(esc, C.c_double),
+                                           ptr(nsz, C.c_int64), ptr(bar, C.c_double), ptr(eff, C.c_double)))
+        return {"markov_escape_time": esc[:k], "neighbor_size": nsz[:k], "barriers": bar[:k],
+                "effective_binding_energy": eff[:k]}
+
     # solute clusters ------------------------------------------------------
     def chemical_potential(self, solvent: int):
         """EnergyPredictor::GetChemicalPotential (EnergyPredictor.cpp:196-214): per species code, the
@@ -482,16 +500,40 @@ def site_relative_positions(n: int, sites) -> np.ndarray:
     return np.stack([hx, hy, hz], axis=-1) / (2.0 * n)
 
 
+# Atomic masses as the reference tabulates them (lmc/cfg/include/Element.hpp:71-87).
+ELEMENT_MASS = {"X": 0.00, "Al": 26.98, "Mg": 24.31, "Zn": 65.38, "Cu": 63.55, "Sn": 118.71}
+
+
+def _periodic_mean(rel, weights):
+    """Circular mean of relative positions per dimension (SoluteCluster::GetGeometryCenter /
+    GetMassCenter, SoluteCluster.cpp:412-455): theta = 2 pi r, atan2 of the weighted mean sine
+    and cosine, mapped to [0, 1)."""
+    theta = rel * 2 * np.pi
+    w = np.asarray(weights, np.float64)[:, None]
+    cbar = (np.cos(theta) * w).sum(0) / w.sum()
+    sbar = (np.sin(theta) * w).sum(0) / w.sum()
+    return (np.arctan2(-sbar, -cbar) + np.pi) / (2 * np.pi)
+
+
+def _wrapped(rel, centre_rel):
+    d = rel - centre_rel
+    return d - np.floor(d + 0.5)  # into [-0.5, 0.5), as the reference's while loops
+
+
 def cluster_info(clusters, formation_energy, species, n: int, alphabet):
-    """The fields of SoluteCluster::GetClustersInfo (SoluteCluster.cpp:110-275) that need no element
-    masses, per cluster (lists from Context.solute_clusters): cluster_id (1-based), cluster_size
-    (sites other than vacancies), elements_number (every element and X), effective_radius (of a
-    sphere of the cluster's atomic volume), cluster_energy (formation energy per non-vacancy site,
-    0 for a cluster of vacancies only) and geometry_center (periodic circular mean of the relative
-    positions, GetGeometryCenter :412-433, in Angstrom)."""
+    """The per-cluster fields of SoluteCluster::GetClustersInfo (SoluteCluster.cpp:110-257) for the
+    lists of Context.solute_clusters: cluster_atom_id_list (lattice ids), cluster_id (1-based),
+    cluster_size (sites other than vacancies), elements_number (every element and X),
+    effective_radius (of a sphere of the cluster's atomic volume), cluster_mass, cluster_energy
+    (formation energy per non-vacancy site, 0 for a cluster of vacancies only), geometry_center
+    and mass_center (periodic circular means, Angstrom), mass_gyration_tensor (Angstrom^2,
+    GetMassGyrationTensor :457-492) with its eigenvalue measures mass_gyration_radius,
+    asphericity, acylindricity and anisotropy (NaN for single-site clusters), and
+    mass_inertia_tensor (GetMassInertiaTensor :494-528)."""
     sp = np.asarray(species)
     x = alphabet.index("X")
     box = n * LATTICE_CONSTANT
+    mass_of = np.array([ELEMENT_MASS[a] for a in alphabet])
     out = []
     for k, (c, ef) in enumerate(zip(clusters, formation_energy)):
         codes = sp[c]
@@ -499,14 +541,45 @@ def cluster_info(clusters, formation_energy, species, n: int, alphabet):
         size = len(c)
         size_wo_x = size - counts["X"]
         volume = size * LATTICE_CONSTANT ** 3 / 4
-        theta = site_relative_positions(n, c) * 2 * np.pi
-        cbar, sbar = np.cos(theta).sum(0) / size, np.sin(theta).sum(0) / size
-        center = (np.arctan2(-sbar, -cbar) + np.pi) / (2 * np.pi) * box
-        out.append({"cluster_id": k + 1, "cluster_size": size_wo_x, "elements_number": counts,
-                    "effective_radius": (3 * volume / (4 * np.pi)) ** (1.0 / 3.0),
+        rel = site_relative_positions(n, c)
+        masses = mass_of[codes]
+        total_mass = float(masses.sum())
+        centre = _periodic_mean(rel, np.ones(size))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mcentre = _periodic_mean(rel, masses)
+            d = _wrapped(rel, mcentre)
+            gyr = (d[:, :, None] * d[:, None, :] * masses[:, None, None]).sum(0) / total_mass * box * box
+        ev = np.linalg.eigvalsh(gyr) if size > 1 and np.all(np.isfinite(gyr)) else np.full(3, np.nan)
+        cart = d * box
+        inertia = np.zeros((3, 3))
+        for a in range(3):
+            for b in range(3):
+                inertia[a, b] = -(masses * cart[:, a] * cart[:, b]).sum()
+            inertia[a, a] = (masses * ((cart ** 2).sum(1) - cart[:, a] ** 2)).sum()
+        out.append({"cluster_atom_id_list": np.asarray(c, np.int64), "cluster_id": k + 1,
+                    "cluster_size": size_wo_x, "elements_number": counts,
+                    "effective_radius": (3 * volume / (4 * np.pi)) ** (1.0 / 3.0), "cluster_mass": total_mass,
                     "cluster_energy": 0.0 if size_wo_x == 0 else float(ef) / size_wo_x,
-                    "geometry_center": center, "vacancies": int(np.count_nonzero(codes == x))})
+                    "geometry_center": centre * box, "mass_center": mcentre * box,
+                    "mass_gyration_tensor": gyr, "mass_gyration_radius": float(np.sqrt(ev.sum())),
+                    "asphericity": float(ev[2] - 0.5 * (ev[0] + ev[1])), "acylindricity": float(ev[1] - ev[0]),
+                    "anisotropy": float(1.5 * (ev ** 2).sum() / ev.sum() ** 2 - 0.5),
+                    "mass_inertia_tensor": inertia, "vacancies": int(np.count_nonzero(codes == x))})
     return out
+
+
+def clusters_frame_info(clusters, formation_energy, species, n: int, alphabet):
+    """SoluteCluster::GetClustersInfo's frame record (SoluteCluster.cpp:254-275): the per-cluster
+    records of cluster_info under "clusters", and num_cluster, num_atom (summed cluster_size),
+    num_<element> for every element of the element set (the alphabet without X) and
+    cluster_size_list (strings, as the reference writes them)."""
+    info = cluster_info(clusters, formation_energy, species, n, alphabet)
+    frame = {"clusters": info, "num_cluster": len(info), "num_atom": int(sum(d["cluster_size"] for d in info)),
+             "cluster_size_list": [str(d["cluster_size"]) for d in info]}
+    for name in alphabet:
+        if name != "X":
+            frame["num_" + name] = int(sum(d["elements_number"][name] for d in info))
+    return frame
 
 
 def load_coefficients(path) -> dict:

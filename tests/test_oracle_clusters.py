@@ -148,3 +148,80 @@ def test_cluster_info_fields(oracle_mod):
     b = (2 * n - 1) * 2 * n * n + n * 0 + 0  # h = (2n - 1, 0, 1): a 1NN of site 0 across x
     (d,) = api.cluster_info([np.array([a, b])], [0.0], np.array([1] * (4 * n ** 3), np.int8), n, alpha)
     assert d["geometry_center"][0] > 0.9 * n * 4.046 or d["geometry_center"][0] < 0.1 * n * 4.046
+
+
+def _ref_circular(rel, w):
+    """GetGeometryCenter / GetMassCenter (SoluteCluster.cpp:412-455), restated with loops."""
+    out = []
+    for dim in range(3):
+        sc = ss = sw = 0.0
+        for r, m in zip(rel, w):
+            sc += np.cos(r[dim] * 2 * np.pi) * m
+            ss += np.sin(r[dim] * 2 * np.pi) * m
+            sw += m
+        out.append((np.arctan2(-ss / sw, -sc / sw) + np.pi) / (2 * np.pi))
+    return np.array(out)
+
+
+def _ref_wrap(v):
+    while v >= 0.5:
+        v -= 1
+    while v < -0.5:
+        v += 1
+    return v
+
+
+def test_cluster_info_geometry_and_mass_fields(oracle_mod):
+    """Every field of GetClustersInfo against a loop-for-loop restatement of the reference's
+    formulas on the oracle's positions (GenerateFCC + ReassignLatticeVector restated): the geometry
+    and mass centres in all three coordinates, the full elements_number dict (X included), the mass,
+    the gyration tensor and its eigenvalue measures (SelfAdjointEigenSolver's ascending order),
+    the inertia tensor, and the frame-level aggregates (SoluteCluster.cpp:254-275)."""
+    from latticemontecarlo_gb300 import api
+    el = ("Al", "Cu", "Mg", "Zn")
+    alpha = S.alphabet(el)
+    mass = {"X": 0.0, "Al": 26.98, "Mg": 24.31, "Zn": 65.38, "Cu": 63.55}  # Element.hpp:71-87
+    n = 8
+    sp = S.make_lattice(n, {"Al": 0.8, "Cu": 0.05, "Mg": 0.08, "Zn": 0.07}, 3, 8, el)
+    lat = oracle_mod.Lattice(n)
+    clusters = oracle_mod.solute_clusters(lat, sp, alpha.index("Al"), 1, 3)
+    ef = np.linspace(-0.2, 0.2, len(clusters))
+    frame = api.clusters_frame_info(clusters, ef, sp, n, alpha)
+    box = n * 4.046
+    for c, d in zip(clusters, frame["clusters"]):
+        rel = np.array([lat.position(int(i)) for i in c])
+        w = np.array([mass[alpha[sp[i]]] for i in c])
+        assert d["elements_number"] == {a: int(np.count_nonzero(sp[c] == k)) for k, a in enumerate(alpha)}
+        assert np.array_equal(d["cluster_atom_id_list"], c)
+        np.testing.assert_allclose(d["geometry_center"], _ref_circular(rel, np.ones(len(c))) * box, atol=1e-12)
+        np.testing.assert_allclose(d["cluster_mass"], w.sum(), rtol=1e-15)
+        if w.sum() == 0:
+            continue  # a cluster of vacancies has no mass centre (0 / 0 in the reference too)
+        mc = _ref_circular(rel, w)
+        np.testing.assert_allclose(d["mass_center"], mc * box, atol=1e-12)
+        gyr = np.zeros((3, 3))
+        inertia = np.zeros((3, 3))
+        for r, m in zip(rel, w):
+            dr = np.array([_ref_wrap(r[k] - mc[k]) for k in range(3)])
+            gyr += np.outer(dr, dr) * m
+            cd = dr * box
+            inertia += m * (np.dot(cd, cd) * np.eye(3) - np.outer(cd, cd))
+        gyr = gyr / w.sum() * box * box
+        np.testing.assert_allclose(d["mass_gyration_tensor"], gyr, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(d["mass_inertia_tensor"], inertia, rtol=1e-12, atol=1e-9)
+        if len(c) > 1:
+            l1, l2, l3 = np.linalg.eigvalsh(gyr)
+            np.testing.assert_allclose(d["mass_gyration_radius"], np.sqrt(l1 + l2 + l3), rtol=1e-12)
+            np.testing.assert_allclose(d["asphericity"], l3 - 0.5 * (l1 + l2), atol=1e-10)
+            np.testing.assert_allclose(d["acylindricity"], l2 - l1, atol=1e-10)
+            np.testing.assert_allclose(d["anisotropy"], 1.5 * (l1 ** 2 + l2 ** 2 + l3 ** 2) / (l1 + l2 + l3) ** 2 - 0.5,
+                                       atol=1e-10)
+        else:
+            assert np.isnan(d["mass_gyration_radius"])
+    sizes = [len(c) - int(np.count_nonzero(sp[c] == alpha.index("X"))) for c in clusters]
+    assert frame["num_cluster"] == len(clusters) and frame["num_atom"] == sum(sizes)
+    assert frame["cluster_size_list"] == [str(v) for v in sizes]
+    for k, a in enumerate(alpha):
+        if a != "X":
+            assert frame["num_" + a] == sum(int(np.count_nonzero(sp[c] == k)) for c in clusters)
+    assert "num_X" not in frame
