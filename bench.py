@@ -39,7 +39,7 @@ BYTES_PER_EVENT = 225       # algorithmic HBM bytes per KMC event
 # DRAM bytes (read + write) of one full-size kmc_kernel launch (4096 replicas x 1e4 steps), one ncu
 # capture with the L2 flushed before the launch; the command and figures are in the kmc_kernel
 # summary under profiles/. The lattices and tables stay in L2, hence far below the algorithmic bytes.
-KMC_TRAFFIC_PER_LAUNCH = None
+KMC_TRAFFIC_PER_LAUNCH = 102_407_936 + 70_376_704
 # What bounds kmc_kernel instead of HBM (the ncu --set full capture summarised under profiles/): the
 # lattices sit in L2 and the per-event work is a dependent chain of gathers and integer table sums.
 KMC_LIMITER = ("issue and latency: issue active 61 % of active cycles, FP64 pipe 20 %, ALU 44 %, 27 of 64 warps "
