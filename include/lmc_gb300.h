@@ -155,6 +155,12 @@ int lmc_barrier_batch(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs,
 /* Device-resident variant: pairs/outputs are device pointers, asynchronous on the context stream. */
 int lmc_barrier_batch_device(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs_dev, int m, double *ea_dev,
                              double *de_dev);
+/* Evaluation used by the barrier batch entry points (and the surrogate's fallback), identical
+ * results either way: LMC_EVAL_SPARSE (default) evaluates each run of consecutive pairs that
+ * share a vacancy as first site once, with the solvent-relative sparse sums (the way
+ * KineticMcFirstOmp::BuildEventList asks for a vacancy's 12 jumps, KineticMcFirstOmp.cpp:57-64);
+ * LMC_EVAL_DENSE sums every cluster of every pair. No reference counterpart (a GPU choice). */
+int lmc_ctx_set_barrier_evaluation(lmc_ctx *ctx, int evaluation);
 
 /* Integer encodings of a batch of 1NN jump pairs computed on the device (same
  * layout as lmc_host_encode_pair, m consecutive records per array). */

@@ -159,6 +159,7 @@ SIGNATURES = {
     "lmc_site_de_batch": (C.c_int, [_P, C.c_int, _I64P, C.POINTER(C.c_int8), C.POINTER(C.c_int8), C.c_int64,
                                     C.c_int64, C.c_int, _DP]),
     "lmc_exit_time_energies": (C.c_int, [_P, C.c_int, C.c_int, _DP, _DP, _DP]),
+    "lmc_ctx_set_barrier_evaluation": (C.c_int, [_P, C.c_int]),
     "lmc_exit_time_clusters": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, _I64P, _I64P, C.c_int64, _DP, _DP, _I64P,
                                          _DP, _DP]),
     "lmc_solute_clusters": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64, C.c_int64, _DP, _I64P, _I64P]),

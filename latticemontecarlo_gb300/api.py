@@ -147,6 +147,10 @@ class Context:
                                       ptr(de, C.c_double), ptr(x, C.c_double), ptr(ks, C.c_double)))
         return ea, de, x, ks
 
+    def set_barrier_evaluation(self, evaluation: int) -> None:
+        """LMC_EVAL_SPARSE (default) or LMC_EVAL_DENSE for barrier_batch and the surrogate's fallback."""
+        check(N.lib.lmc_ctx_set_barrier_evaluation(self._h, evaluation))
+
     def encode_batch(self, pairs, replica: int = 0):
         p = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
         m, mo = p.shape[0], self.model

@@ -87,6 +87,7 @@ struct lmc_ctx {
   std::vector<unsigned long long> scan_host;  // per replica species histogram + invalid count
   std::vector<long long> first_host;          // per replica lowest X site (LLONG_MAX: none)
   bool scan_fresh{false};                     // scan_host / first_host describe the current lattices
+  int barrier_eval{LMC_EVAL_SPARSE};          // evaluation of the barrier batch entry points
   DevBuf scan_first;
   // batch scratch
   DevBuf pairs, out0, out1, out2, out3, status, counts, energy, enc;
@@ -1221,14 +1222,65 @@ int64_t lmc_ctx_replica_offset(const lmc_ctx *ctx, int replica) {
 }
 void *lmc_ctx_species_device_ptr(lmc_ctx *ctx) { return ctx ? ctx->species.p : nullptr; }
 
+// Dominant species of replica r with a one-hot slot (the base of the sparse evaluation), from the
+// histogram of the last lmc_ctx_set_lattices (the kernels conserve every replica's composition);
+// -1 if none.
+static int SparseBaseOf(const lmc_ctx *ctx, int replica) {
+  if (ctx->scan_host.size() < static_cast<size_t>(replica + 1) * (lmc::kMaxSpecies + 1)) return -1;
+  const unsigned long long *h = &ctx->scan_host[static_cast<size_t>(replica) * (lmc::kMaxSpecies + 1)];
+  int base = -1;
+  for (int c = 0; c < ctx->fm.num_species; ++c)
+    if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || h[c] > h[base])) base = c;
+  return base;
+}
+
+// The barrier kernels of the batch entry points: the sparse evaluation for runs of pairs that
+// share a vacancy (LMC_EVAL_SPARSE, the default) or the dense per-pair sums; identical results.
+static void LaunchBarriers(lmc_ctx *ctx, int replica, int kind, const long long *d_pairs, int m, const int *m_dev,
+                           double *d_ea, double *d_de, double *d_x, double *d_ks) {
+  const int8_t *sp = ctx->species.as<int8_t>() + ctx->offsets[replica];
+  const int base = ctx->barrier_eval == LMC_EVAL_SPARSE ? SparseBaseOf(ctx, replica) : -1;
+  if (base >= 0) {
+    BuildSparse(ctx, base);
+    lmc::BarrierGroupArgs a{};
+    a.n = ctx->n[replica];
+    a.pairs = d_pairs;
+    a.m = m;
+    a.m_dev = m_dev;
+    a.kind = kind;
+    a.ea = d_ea;
+    a.de = d_de;
+    a.d_or_e0 = d_x;
+    a.ks = d_ks;
+    a.status = ctx->status.as<int>();
+    a.sp = ctx->sparse;
+    CudaCheck(lmc::LaunchBarrierGroup(ctx->t, sp, a, ctx->stream), "barrier kernel");
+  } else if (m_dev) {
+    CudaCheck(lmc::LaunchBarrierBatchCounted(ctx->t, sp, ctx->n[replica], d_pairs, m, m_dev, kind, d_ea, d_de,
+                                             ctx->status.as<int>(), ctx->stream),
+              "barrier kernel");
+  } else {
+    CudaCheck(lmc::LaunchBarrierBatch(ctx->t, sp, ctx->n[replica], d_pairs, m, kind, d_ea, d_de, d_x, d_ks,
+                                      ctx->status.as<int>(), ctx->stream),
+              "barrier kernel");
+  }
+}
+
 static void BarrierBatchImpl(lmc_ctx *ctx, int replica, int kind, const long long *d_pairs, int m, double *d_ea,
                              double *d_de, double *d_x, double *d_ks) {
   ctx->CheckReplica(replica);
   Require(kind == LMC_BARRIER_QUARTIC || kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT, "unknown barrier kind");
   ctx->ClearStatus();
-  CudaCheck(lmc::LaunchBarrierBatch(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
-                                    d_pairs, m, kind, d_ea, d_de, d_x, d_ks, ctx->status.as<int>(), ctx->stream),
-            "barrier kernel");
+  LaunchBarriers(ctx, replica, kind, d_pairs, m, nullptr, d_ea, d_de, d_x, d_ks);
+}
+
+int lmc_ctx_set_barrier_evaluation(lmc_ctx *ctx, int evaluation) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    Require(evaluation == LMC_EVAL_SPARSE || evaluation == LMC_EVAL_DENSE, LMC_ERR_INVALID_ARGUMENT,
+            "unknown evaluation");
+    ctx->barrier_eval = evaluation;
+  });
 }
 
 int lmc_barrier_batch(lmc_ctx *ctx, int replica, int kind, const int64_t *pairs, int m, double *ea, double *de,
@@ -1471,11 +1523,8 @@ int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, 
                                          fallback_dev, ctx->stream),
               "fallback kernel");
     // the plain predictor on the compacted pairs, sized by the device count (no host round trip)
-    CudaCheck(lmc::LaunchBarrierBatchCounted(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica],
-                                             ctx->n[replica], ctx->s_fb_pairs.as<long long>(), m, d_count, kind,
-                                             ctx->s_fb_ea.as<double>(), ctx->s_fb_de.as<double>(),
-                                             ctx->status.as<int>(), ctx->stream),
-              "barrier kernel");
+    LaunchBarriers(ctx, replica, kind, ctx->s_fb_pairs.as<long long>(), m, d_count, ctx->s_fb_ea.as<double>(),
+                   ctx->s_fb_de.as<double>(), nullptr, nullptr);
     CudaCheck(lmc::LaunchFallbackMerge(ctx->s_mean.as<float>(), m, ctx->s_fb_ea.as<double>(), ctx->s_fb_index.as<int>(),
                                        d_count, ea_dev, ctx->stream),
               "merge kernel");

@@ -356,6 +356,48 @@ __device__ __forceinline__ void GatherJump(const DevTables &t, const int8_t *spe
 }
 
 // m_dev (nullable): the number of pairs lives on the device (m is then its upper bound).
+// One jump pair by the whole warp over the sorted state / MMM / MM2 lists (the
+// dense cluster sums); writes pair p's outputs and returns its status bits.
+__device__ __forceinline__ unsigned DensePairBarrier(const DevTables &t, const int8_t *__restrict__ species, int n,
+                                                     const long long *__restrict__ pairs, long long p, int kind,
+                                                     const uint32_t *s_de, const uint32_t *s_mmm,
+                                                     const uint32_t *s_mm2, const SmallTables *small, int8_t *st,
+                                                     int8_t *rm, int8_t *rf, int8_t *rb, double *ea, double *de,
+                                                     double *d_or_e0, double *ks, int lane) {
+  H3 hi, hj;
+  int di = -1, db = -1;
+  unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
+  int slot = -1;
+  if (!bad) {
+    GatherJump(t, species, n, hi, hj, di, db, small, st, rm, rf, rb, lane);
+    __syncwarp();
+    slot = small->slot[st[t.pos_second]];
+    if (slot < 0 || (kind == 0 ? !small->has_quartic[slot] : !small->has_e0[slot])) bad = kStatusNoCoefficients;
+  }
+  if (bad) {
+    if (lane == 0) {
+      ea[p] = nan("");
+      de[p] = nan("");
+    }
+    __syncwarp();
+    return bad;
+  }
+  JumpAcc a = kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, small->pairtype, lane)
+                        : EvalJump<false>(t, slot, st, rm, rf, rb, s_de, s_mmm, s_mm2, small->pairtype, lane);
+  const long long acc_de = WarpSum(a.de), acc_d = WarpSum(a.d), acc_ks = WarpSum(a.ks);
+  unsigned b = __reduce_or_sync(0xffffffffu, a.bad);
+  if (lane == 0) {
+    const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
+    ea[p] = o.ea;
+    de[p] = o.de;
+    if (d_or_e0) d_or_e0[p] = kind == 0 ? exp(o.d_or_e0) : o.d_or_e0;
+    if (ks) ks[p] = kind == 0 ? exp(o.ks) : 0.0;
+    if (!isfinite(o.ea)) b |= kStatusNumeric;
+  }
+  __syncwarp();
+  return b;
+}
+
 __global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ species, int n,
                                      const long long *__restrict__ pairs, int m, const int *m_dev, int kind,
                                      double *ea, double *de, double *d_or_e0, double *ks, int *status) {
@@ -369,41 +411,9 @@ __global__ void barrier_batch_kernel(DevTables t, const int8_t *__restrict__ spe
   int8_t *st = s.arr + warp * kArr;
   int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
   unsigned bad_all = 0;
-  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps) {
-    H3 hi, hj;
-    int di = -1, db = -1;
-    unsigned bad = ResolvePair(t.dir_of, pairs[2 * p], pairs[2 * p + 1], n, &hi, &hj, &di, &db);
-    int slot = -1;
-    if (!bad) {
-      GatherJump(t, species, n, hi, hj, di, db, s.small, st, rm, rf, rb, lane);
-      __syncwarp();
-      slot = s.small->slot[st[t.pos_second]];
-      if (slot < 0 || (kind == 0 ? !s.small->has_quartic[slot] : !s.small->has_e0[slot])) bad = kStatusNoCoefficients;
-    }
-    if (bad) {
-      if (lane == 0) {
-        ea[p] = nan("");
-        de[p] = nan("");
-      }
-      bad_all |= bad;
-      __syncwarp();
-      continue;
-    }
-    JumpAcc a = kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane)
-                          : EvalJump<false>(t, slot, st, rm, rf, rb, s.de, s.mmm, s.mm2, s.small->pairtype, lane);
-    const long long acc_de = WarpSum(a.de), acc_d = WarpSum(a.d), acc_ks = WarpSum(a.ks);
-    const unsigned b = __reduce_or_sync(0xffffffffu, a.bad);
-    if (lane == 0) {
-      const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
-      ea[p] = o.ea;
-      de[p] = o.de;
-      if (d_or_e0) d_or_e0[p] = kind == 0 ? exp(o.d_or_e0) : o.d_or_e0;
-      if (ks) ks[p] = kind == 0 ? exp(o.ks) : 0.0;
-      if (!isfinite(o.ea)) bad_all |= kStatusNumeric;
-    }
-    bad_all |= b;
-    __syncwarp();
-  }
+  for (int p = blockIdx.x * warps + warp; p < m; p += gridDim.x * warps)
+    bad_all |= DensePairBarrier(t, species, n, pairs, p, kind, s.de, s.mmm, s.mm2, s.small, st, rm, rf, rb, ea, de,
+                                d_or_e0, ks, lane);
   if (bad_all && lane == 0) atomicOr(status, static_cast<int>(bad_all));
 }
 
@@ -2174,6 +2184,91 @@ __global__ void __launch_bounds__(kSiteJumpWarps * 32)
 }
 
 // ---------------------------------------------------------------------------
+// K1s: batched barriers with the sparse evaluation. A vacancy's jumps are usually
+// asked together (KineticMcFirstOmp::BuildEventList asks for all 12,
+// KineticMcFirstOmp.cpp:57-64), so each warp takes 12 consecutive pairs and, for
+// every run of pairs that share a first site holding a vacancy, gathers that
+// site's 135-site neighbourhood once and evaluates its 12 jumps with the sparse
+// sums of the KMC kernel (bit-identical to the dense sums); every other pair, a
+// run whose neighbourhood is too rich for the sparse lists, or a run whose
+// sparse items report anything, takes the dense per-pair path.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSiteJumpWarps * 32)
+    barrier_group_kernel(const __grid_constant__ DevTables t, const int8_t *__restrict__ species,
+                         const __grid_constant__ BarrierGroupArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const KmcSmem sm = CarveKmcSmem(t, smem, kSiteJumpWarps, 1);
+  StageKmcSmem(t, a.sp, sm, true);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  KmcShared &rs = sm.rep[warp];
+  int8_t *st = sm.arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  const ExpConsts ec{sm.exp, t.exp_l1, t.exp_l2};
+  const int n = a.n;
+  const long long nsites = 4LL * n * n * n;
+  const long long m = a.m_dev ? min(a.m, static_cast<long long>(*a.m_dev)) : a.m;
+  const long long *__restrict__ pairs = a.pairs;
+  unsigned bad_all = 0;
+  for (long long c0 = (static_cast<long long>(blockIdx.x) * kSiteJumpWarps + warp) * 12; c0 < m;
+       c0 += static_cast<long long>(gridDim.x) * kSiteJumpWarps * 12) {
+    const long long cend = min(c0 + 12, m);
+    long long p = c0;
+    while (p < cend) {
+      const long long i = pairs[2 * p];
+      long long q = p + 1;
+      while (q < cend && pairs[2 * q] == i) ++q;
+      bool group = i >= 0 && i < nsites && species[i] == t.x_code;
+      if (group) {
+        const H3 h = SiteCoord(i, n);
+        for (int k = lane; k < kLocalSites; k += 32) {
+          const int8_t *o = sm.loff + k * 4;
+          rs.local[k] = species[NeighborId(h, o[0], o[1], o[2], n)];
+        }
+        __syncwarp();
+        SparseList(rs, sm.inter, a.sp, lane);
+        __syncwarp();
+        group = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs &&
+                SparseItem(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, a.kind, lane) == 0u;
+        __syncwarp();
+      }
+      if (group) {
+        // lane k writes pair p + k from the jump of its direction
+        if (lane < q - p) {
+          const long long pk = p + lane;
+          H3 hi, hj;
+          int di = -1, db = -1;
+          unsigned bad = ResolvePair(t.dir_of, pairs[2 * pk], pairs[2 * pk + 1], n, &hi, &hj, &di, &db);
+          const int slot = bad ? -1 : rs.slot[di];
+          if (!bad && (slot < 0 || (a.kind == 0 ? !sm.small->has_quartic[slot] : !sm.small->has_e0[slot])))
+            bad = kStatusNoCoefficients;
+          if (bad) {
+            a.ea[pk] = nan("");
+            a.de[pk] = nan("");
+            bad_all |= bad;
+          } else {
+            const JumpOut o = JumpEpilogue(t, ec, a.kind, slot, rs.acc[di][0], rs.acc[di][1], rs.acc[di][2]);
+            a.ea[pk] = o.ea;
+            a.de[pk] = o.de;
+            if (a.d_or_e0) a.d_or_e0[pk] = a.kind == 0 ? exp(o.d_or_e0) : o.d_or_e0;
+            if (a.ks) a.ks[pk] = a.kind == 0 ? exp(o.ks) : 0.0;
+            if (!isfinite(o.ea)) bad_all |= kStatusNumeric;
+          }
+        }
+        __syncwarp();
+      } else {
+        for (long long r = p; r < q; ++r)
+          bad_all |= DensePairBarrier(t, species, n, pairs, r, a.kind, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb,
+                                      a.ea, a.de, a.d_or_e0, a.ks, lane);
+      }
+      p = q;
+    }
+  }
+  bad_all = __reduce_or_sync(0xffffffffu, bad_all);
+  if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
+}
+
+// ---------------------------------------------------------------------------
 // K3b: solute clusters (ansys::SoluteCluster, SoluteCluster.cpp:277-410).
 // Connected components of the non-solvent sites under 1NN bonds by lock-free
 // union-find: every root is hooked under a smaller root (so a parent id never
@@ -3513,6 +3608,29 @@ cudaError_t LaunchSiteJumps(const DevTables &t, const int8_t *species, const Sit
   const long long need = (a.m + kSiteJumpWarps - 1) / kSiteJumpWarps;
   const int blocks = static_cast<int>(std::min<long long>(need, static_cast<long long>(sms) * 8));
   kern<<<blocks, kSiteJumpWarps * 32, sm, stream>>>(t, species, a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchBarrierGroup(const DevTables &t, const int8_t *species, const BarrierGroupArgs &a,
+                               cudaStream_t stream) {
+  if (a.m <= 0) return cudaSuccess;
+  KmcLaunch l{};
+  l.warps_per_replica = 1;
+  l.replicas_per_block = kSiteJumpWarps;
+  l.sparse = 1;
+  const size_t sm = KmcSharedBytes(t, l);
+  cudaError_t err =
+      cudaFuncSetAttribute(barrier_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0;
+  err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (err != cudaSuccess) return err;
+  // one warp per 12 pairs; a device-side count (m_dev) only shrinks the work, so the grid covers m
+  const long long need = (a.m + 12LL * kSiteJumpWarps - 1) / (12LL * kSiteJumpWarps);
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>(need, static_cast<long long>(sms) * 8)));
+  barrier_group_kernel<<<blocks, kSiteJumpWarps * 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

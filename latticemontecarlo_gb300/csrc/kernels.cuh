@@ -246,6 +246,22 @@ struct SiteJumpArgs {
 };
 cudaError_t LaunchSiteJumps(const DevTables &t, const int8_t *species, const SiteJumpArgs &a, cudaStream_t stream);
 
+// Batched barriers with the sparse evaluation for runs of pairs that share a vacancy as first
+// site (identical results to LaunchBarrierBatch; `sp` built for the lattice's dominant species).
+struct BarrierGroupArgs {
+  int n;
+  const long long *pairs;  // [m][2] (device)
+  long long m;
+  const int *m_dev;        // device count that caps m, or null
+  int kind;
+  double *ea, *de;         // [m]
+  double *d_or_e0, *ks;    // [m], nullable
+  int *status;
+  KmcSparse sp;
+};
+cudaError_t LaunchBarrierGroup(const DevTables &t, const int8_t *species, const BarrierGroupArgs &a,
+                               cudaStream_t stream);
+
 // Simulated annealing (SimulatedAnnealing.cpp:99-185): one warp, the reference's
 // mt19937_64 stream, one trial pair per step and its adaptive temperature schedule.
 struct SaState {

@@ -282,6 +282,50 @@ def test_sparse_equals_dense_bitwise(api, base_fraction, warps):
     assert np.array_equal(t0, t1) and np.array_equal(e0, e1)
 
 
+@pytest.mark.parametrize("base_fraction", [0.96, 0.8, 0.6])
+def test_barrier_batch_sparse_equals_dense(api, oracle_mod, base_fraction):
+    """lmc_barrier_batch's sparse path (runs of jumps that share a vacancy, evaluated once with the
+    solvent-relative sums) gives the dense per-pair results bit for bit: the 12 jumps of every
+    vacancy of a vacancy grid, jumps asked singly and in a shuffled order, and pairs whose first
+    site is not a vacancy; a vacancy with a second vacancy in its environments raises on both."""
+    from latticemontecarlo_gb300 import synthetic as S
+    el = ("Al", "Mg", "Zn")
+    coeffs = S.make_coefficients(el, 8)
+    n = 16
+    rest = (1.0 - base_fraction) / 2
+    sp = S.make_lattice(n, {"Al": base_fraction, "Mg": rest, "Zn": rest}, 0, 12, el)
+    x = S.alphabet(el).index("X")
+    m2 = 2 * n
+    grid = [(a, b, c) for a in range(0, m2, 8) for b in range(0, m2, 8) for c in range(0, m2, 8)]
+    vac = np.array([a * 2 * n * n + b * n + c // 2 for a, b, c in grid])
+    sp[vac] = x
+    sp[vac[0] + 1] = x  # a second vacancy inside vac[0]'s environments
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+    ctx.set_lattices([n], sp)
+    lat = oracle_mod.Lattice(n)
+    grouped = np.array([[v, j] for v in vac[1:] for j in lat.neighbors(int(v))[:12]], np.int64)
+    rng = np.random.default_rng(3)
+    shuffled = grouped[rng.permutation(len(grouped))[:200]]
+    others = []
+    while len(others) < 40:  # non-vacancy first sites whose environments hold no vacancy
+        a = int(rng.choice(np.flatnonzero(sp != x)))
+        b = int(lat.neighbors(a)[rng.integers(12)])
+        if sp[b] != x and not any(np.any(sp[v] == x) for v in lat.pair_lists(a, b)):
+            others.append([a, b])
+    pairs = np.concatenate([grouped, shuffled, np.array(others, np.int64)])
+    out = []
+    for evaluation in (0, 1):
+        ctx.set_barrier_evaluation(evaluation)
+        out.append(ctx.barrier_batch(pairs))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    bad = np.array([[vac[0], j] for j in lat.neighbors(int(vac[0]))[:12]], np.int64)
+    for evaluation in (0, 1):
+        ctx.set_barrier_evaluation(evaluation)
+        with pytest.raises(Exception):  # X inside an environment, as the reference's encoder throws
+            ctx.barrier_batch(bad)
+
+
 def test_invalid_species_rejected(api, golden):
     from latticemontecarlo_gb300 import LmcError
     G, load = golden
