@@ -233,6 +233,10 @@ int lmc_mlp_gradients(lmc_mlp *mlp, const uint16_t *features, const float *label
  * (nullable, per member) is the mean loss of the last epoch in standardised units. */
 int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *features_dev, const float *labels_dev, int64_t n, int batch,
                   int epochs, float lr, uint64_t seed, float *loss);
+/* Training GEMM kernels: 0 (default) the tcgen05 kernel (BF16 operands, FP32 accumulators in
+ * TMEM) for every GEMM whose rows are a multiple of 128 (batch and hidden widths), the mma.sync
+ * kernel otherwise; 1 the mma.sync kernel for all. Same arithmetic (BF16 products, FP32 sums). */
+int lmc_mlp_set_train_path(lmc_mlp *mlp, int path);
 /* Inference kernels: 0 automatic (the fused tcgen05 kernel when hidden = 256 and
  * in_features <= 256), 1 tcgen05, 2 the mma.sync GEMMs of training. */
 int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path);

@@ -140,6 +140,7 @@ SIGNATURES = {
                                 C.POINTER(C.c_float)]),
     "lmc_mlp_predict": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "lmc_mlp_set_inference_path": (C.c_int, [_P, C.c_int]),
+    "lmc_mlp_set_train_path": (C.c_int, [_P, C.c_int]),
     "lmc_surrogate_feature_count": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "lmc_surrogate_dataset": (C.c_int, [_P, C.c_uint64, C.c_int64, C.c_double, C.c_double, C.c_int, C.c_int, _P, _P,
                                         _P, _P]),

@@ -439,6 +439,10 @@ class Surrogate:
                                   features.shape[0], batch, epochs, lr, seed, ptr(loss, C.c_float)))
         return loss
 
+    def set_train_path(self, path: int) -> None:
+        """0 the tcgen05 training GEMMs where the shapes allow (default), 1 mma.sync only."""
+        check(N.lib.lmc_mlp_set_train_path(self._h, path))
+
     def set_inference_path(self, path: int) -> None:
         """0 automatic (tcgen05 when supported), 1 tcgen05, 2 mma.sync."""
         check(N.lib.lmc_mlp_set_inference_path(self._h, path))

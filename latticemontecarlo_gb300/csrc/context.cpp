@@ -1224,13 +1224,18 @@ void *lmc_ctx_species_device_ptr(lmc_ctx *ctx) { return ctx ? ctx->species.p : n
 
 // Dominant species of replica r with a one-hot slot (the base of the sparse evaluation), from the
 // histogram of the last lmc_ctx_set_lattices (the kernels conserve every replica's composition);
-// -1 if none.
+// -1 if none, or if it fills less than 7/8 of the lattice: a 135-site neighbourhood then holds
+// more than about 17 other sites on average, and the dense sums are cheaper than the lists.
 static int SparseBaseOf(const lmc_ctx *ctx, int replica) {
   if (ctx->scan_host.size() < static_cast<size_t>(replica + 1) * (lmc::kMaxSpecies + 1)) return -1;
   const unsigned long long *h = &ctx->scan_host[static_cast<size_t>(replica) * (lmc::kMaxSpecies + 1)];
   int base = -1;
-  for (int c = 0; c < ctx->fm.num_species; ++c)
+  unsigned long long total = 0;
+  for (int c = 0; c < ctx->fm.num_species; ++c) {
+    total += h[c];
     if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0 && (base < 0 || h[c] > h[base])) base = c;
+  }
+  if (base < 0 || 8 * h[base] < 7 * total) return -1;
   return base;
 }
 
@@ -1239,7 +1244,8 @@ static int SparseBaseOf(const lmc_ctx *ctx, int replica) {
 static void LaunchBarriers(lmc_ctx *ctx, int replica, int kind, const long long *d_pairs, int m, const int *m_dev,
                            double *d_ea, double *d_de, double *d_x, double *d_ks) {
   const int8_t *sp = ctx->species.as<int8_t>() + ctx->offsets[replica];
-  const int base = ctx->barrier_eval == LMC_EVAL_SPARSE ? SparseBaseOf(ctx, replica) : -1;
+  // a device-side count (the surrogate's fallback list: few, scattered pairs) takes the dense sums
+  const int base = ctx->barrier_eval == LMC_EVAL_SPARSE && !m_dev ? SparseBaseOf(ctx, replica) : -1;
   if (base >= 0) {
     BuildSparse(ctx, base);
     lmc::BarrierGroupArgs a{};

@@ -3627,9 +3627,14 @@ cudaError_t LaunchBarrierGroup(const DevTables &t, const int8_t *species, const 
   if (err != cudaSuccess) return err;
   err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (err != cudaSuccess) return err;
-  // one warp per 12 pairs; a device-side count (m_dev) only shrinks the work, so the grid covers m
+  // one warp per 12 pairs, at most one wave of resident blocks (each block stages the tables once
+  // and strides over the runs); a device-side count (m_dev) only shrinks the work
+  int resident = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, barrier_group_kernel, kSiteJumpWarps * 32, sm);
+  if (err != cudaSuccess) return err;
   const long long need = (a.m + 12LL * kSiteJumpWarps - 1) / (12LL * kSiteJumpWarps);
-  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>(need, static_cast<long long>(sms) * 8)));
+  const long long wave = static_cast<long long>(sms) * std::max(1, resident);
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>(need, wave)));
   barrier_group_kernel<<<blocks, kSiteJumpWarps * 32, sm, stream>>>(t, species, a);
   return cudaGetLastError();
 }

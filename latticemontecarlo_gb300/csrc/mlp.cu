@@ -48,28 +48,6 @@ __device__ __forceinline__ void Mma16816(float *c, const uint32_t *a, const uint
 __device__ __forceinline__ float Gelu(float z) { return MlpGelu(z); }
 __device__ __forceinline__ float GeluGrad(float z) { return MlpGeluGrad(z); }
 
-// Epilogues.
-enum Epi : int {
-  kEpiStoreF32 = 0,     // C fp32 = acc                                   (weight gradients)
-  kEpiBiasGelu = 1,     // Z = acc + bias (fp32), H = GELU(Z) (bf16), optional Ht (bf16, [n][m])
-  kEpiGeluGrad = 2,     // D = acc * GELU'(Z) (bf16), optional Dt (bf16, [n][m])
-};
-
-struct GemmArgs {
-  const __nv_bfloat16 *a;  // [M][K], lda
-  const __nv_bfloat16 *b;  // [N][K], ldb
-  int m, n, k, lda, ldb;
-  long long stride_a, stride_b;  // per grid.z
-  // epilogue
-  float *c;              // kEpiStoreF32: [M][N] ldc; kEpiBiasGelu: Z; kEpiGeluGrad: Z (input)
-  const float *bias;     // kEpiBiasGelu
-  __nv_bfloat16 *h;      // kEpiBiasGelu: H; kEpiGeluGrad: D
-  __nv_bfloat16 *ht;     // optional transposed copy, [N][M] with ld ldt
-  int ldc, ldh, ldt;
-  long long stride_c, stride_bias, stride_h, stride_ht;
-  float alpha;           // scales acc (kEpiStoreF32)
-};
-
 // C tile (kBM x kBN) per block, 4 warps of 32 x 32; K in steps of kBK with a
 // two-stage cp.async pipeline. M, N multiples of 64 and K of 32 (checked on the host).
 template <int kEpi>
@@ -171,8 +149,27 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_nt_kernel(GemmArgs g) {
       }
 }
 
+// The training GEMMs go to the tcgen05 kernel where the shape fits (unless the ensemble is set
+// to mma.sync), else to the mma.sync kernel above.
 template <int kEpi>
-cudaError_t Gemm(const GemmArgs &g, int batch, cudaStream_t s) {
+cudaError_t Gemm(const MlpDev &d, const GemmArgs &g, int batch, cudaStream_t s) {
+  if (!d.gemm_mma_sync && d.gemm_status && GemmTcFits(g)) {
+    GemmArgs t = g;
+    t.splits = 1;
+    if (kEpi == kEpiStoreF32 && d.gemm_ws) {
+      // weight gradients (K = the batch): split K until the grid fills the GPU, at least 4 K
+      // tiles per split, the partials within the workspace
+      const int bn = g.n % 256 == 0 ? 256 : (g.n % 128 == 0 ? 128 : 64);
+      const long long ctas = static_cast<long long>(g.n / bn) * (g.m / 128) * batch;
+      const int ktiles = g.k / 32;
+      while (t.splits < 16 && ctas * t.splits < 256 && ktiles % (2 * t.splits) == 0 &&
+             ktiles / (2 * t.splits) >= 4 &&
+             2LL * t.splits * batch * g.m * g.n <= d.gemm_ws_floats)
+        t.splits *= 2;
+      t.ws = d.gemm_ws;
+    }
+    return GemmTc(t, kEpi, batch, d.gemm_status, s);
+  }
   if (g.m % kBM || g.n % kBN || g.k % kBK || g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaErrorInvalidValue;
   const dim3 grid(g.n / kBN, g.m / kBM, batch);
   gemm_nt_kernel<kEpi><<<grid, kGemmThreads, 0, s>>>(g);
@@ -369,7 +366,7 @@ cudaError_t MlpForward(const MlpDev &d, const __nv_bfloat16 *x, int batch, MlpWo
   g.ht = keep_ht ? w.h1t : nullptr;
   g.ldc = g.ldh = M * H;
   g.ldt = batch;
-  cudaError_t err = Gemm<kEpiBiasGelu>(g, 1, s);
+  cudaError_t err = Gemm<kEpiBiasGelu>(d, g, 1, s);
   if (err != cudaSuccess) return err;
   // layer 2, member z: Z2[:, zH:(z+1)H] = H1[:, zH:(z+1)H] W2[z]^T + b2[z]
   GemmArgs g2{};
@@ -388,7 +385,7 @@ cudaError_t MlpForward(const MlpDev &d, const __nv_bfloat16 *x, int batch, MlpWo
   g2.ldc = g2.ldh = M * H;
   g2.stride_c = g2.stride_h = H;
   g2.stride_bias = H;
-  err = Gemm<kEpiBiasGelu>(g2, M, s);
+  err = Gemm<kEpiBiasGelu>(d, g2, M, s);
   if (err != cudaSuccess) return err;
   const int warps = batch * M;
   output_kernel<<<(warps * 32 + 255) / 256, 256, 0, s>>>(w.h2, d.w3, d.b3, batch, M, H, w.y);
@@ -418,7 +415,7 @@ cudaError_t MlpBackward(const MlpDev &d, const __nv_bfloat16 *x, const __nv_bflo
   g.ldc = H;
   g.stride_c = static_cast<long long>(H) * H;
   g.alpha = 1.f;
-  cudaError_t err = Gemm<kEpiStoreF32>(g, M, s);
+  cudaError_t err = Gemm<kEpiStoreF32>(d, g, M, s);
   if (err != cudaSuccess) return err;
   column_sum_kernel<<<M * H, 256, 0, s>>>(w.dz2t, batch, gb2);
   // dZ1[:, z] = (dZ2[:, z] W2[z]) * GELU'(Z1): B operand W2[z]^T stored [in][out]
@@ -439,7 +436,7 @@ cudaError_t MlpBackward(const MlpDev &d, const __nv_bfloat16 *x, const __nv_bflo
   g2.ldt = batch;
   g2.stride_c = g2.stride_h = H;
   g2.stride_ht = static_cast<long long>(H) * batch;
-  err = Gemm<kEpiGeluGrad>(g2, M, s);
+  err = Gemm<kEpiGeluGrad>(d, g2, M, s);
   if (err != cudaSuccess) return err;
   column_sum_kernel<<<M * H, 256, 0, s>>>(w.dz1t, batch, gb1);
   // gW1 = dZ1^T X  ([M*H][B] x [K][B]^T)
@@ -453,7 +450,7 @@ cudaError_t MlpBackward(const MlpDev &d, const __nv_bfloat16 *x, const __nv_bflo
   g3.c = gw1;
   g3.ldc = d.in;
   g3.alpha = 1.f;
-  return Gemm<kEpiStoreF32>(g3, 1, s);
+  return Gemm<kEpiStoreF32>(d, g3, 1, s);
 }
 
 cudaError_t MlpGather(const __nv_bfloat16 *x, const float *labels, const int *idx, int batch, int in, float mean,

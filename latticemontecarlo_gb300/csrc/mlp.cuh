@@ -29,10 +29,47 @@ __device__ __forceinline__ float MlpGeluGrad(float z) {
 }
 #endif
 
+// Training GEMMs: C[m][n] = sum_k A[m][k] B[n][k] (both operands K-major, BF16, FP32
+// accumulate), batched over grid.z, with one of three fused epilogues.
+enum Epi : int {
+  kEpiStoreF32 = 0,     // C fp32 = alpha acc                            (weight gradients)
+  kEpiBiasGelu = 1,     // Z = acc + bias (fp32), H = GELU(Z) (bf16), optional Ht (bf16, [n][m])
+  kEpiGeluGrad = 2,     // D = acc * GELU'(Z) (bf16), optional Dt (bf16, [n][m])
+};
+
+struct GemmArgs {
+  const __nv_bfloat16 *a;  // [M][K], lda
+  const __nv_bfloat16 *b;  // [N][K], ldb
+  int m, n, k, lda, ldb;
+  long long stride_a, stride_b;  // per grid.z
+  // epilogue
+  float *c;              // kEpiStoreF32: [M][N] ldc; kEpiBiasGelu: Z; kEpiGeluGrad: Z (input)
+  const float *bias;     // kEpiBiasGelu
+  __nv_bfloat16 *h;      // kEpiBiasGelu: H; kEpiGeluGrad: D
+  __nv_bfloat16 *ht;     // optional transposed copy, [N][M] with ld ldt
+  int ldc, ldh, ldt;
+  long long stride_c, stride_bias, stride_h, stride_ht;
+  float alpha;           // scales acc (kEpiStoreF32)
+  // kEpiStoreF32 on the tcgen05 path: K split over `splits` CTAs (1 = none), whose partial tiles
+  // go to ws ([splits][batch][m][n]) and are summed in split order by a second kernel
+  int splits;
+  float *ws;
+};
+
+// The tcgen05 version of the training GEMMs (mlp_gemm_tc.cu): 128-row tiles, N tiles of 64 /
+// 128 / 256, accumulators in TMEM. GemmTcFits: M a multiple of 128, N of 64, K of 32, the
+// leading dimensions and epilogue strides multiples of 8. An expired wait sets *status.
+bool GemmTcFits(const GemmArgs &g);
+cudaError_t GemmTc(const GemmArgs &g, int epi, int batch, int *status, cudaStream_t s);
+
 // Parameters of an ensemble (FP32 master copy, flat: W1, b1, W2, b2, w3, b3) and
 // the BF16 copies the GEMMs read.
 struct MlpDev {
   int in, hidden, members;
+  int gemm_mma_sync;   // 1: training GEMMs on mma.sync only; 0: tcgen05 where GemmTcFits
+  int *gemm_status;    // device word set by an expired tcgen05 wait
+  float *gemm_ws;      // split-K partials of the weight-gradient GEMMs
+  long long gemm_ws_floats;
   float *w1, *b1, *w2, *b2, *w3, *b3;
   __nv_bfloat16 *w1h, *w2h, *w2t;
   // W1 (bf16) and W2 (IEEE half: layer 2 of the tensor-core inference runs in

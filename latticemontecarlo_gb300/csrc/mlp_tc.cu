@@ -29,9 +29,26 @@
 #include <cstdint>
 
 #include "mlp.cuh"
+#include "tcgen05.cuh"
 
 namespace lmc {
 namespace {
+
+using tc::Arrive;
+using tc::ArriveExpectTx;
+using tc::BarInit;
+using tc::BulkCopy;
+using tc::Commit;
+using tc::CpAsync16;
+using tc::CpAsyncCommit;
+using tc::CpAsyncWait;
+using tc::FenceAsyncSmem;
+using tc::Mma;
+using tc::OperandDesc;
+using tc::Smem;
+using tc::TmemLoad32;
+using tc::Wait;
+using tc::WaitDrain;
 
 constexpr int kTcRows = 128;     // samples per tile (MMA M)
 constexpr int kTcHidden = 256;   // MMA N and the hidden width
@@ -43,31 +60,13 @@ constexpr int kEpiWarps = 16;    // 4 per TMEM lane group, 64 columns each
 constexpr int kTcThreads = 64 + 32 * kEpiWarps;  // producer, MMA issuer, epilogue
 constexpr uint32_t kTmemCols = 512;
 constexpr int kMlpTimeout = 1;
-constexpr long long kWaitLimit = 1LL << 26;
 constexpr uint32_t kSbo = kTcK * 16;  // 8-row group stride of a 32-wide operand tile
-
-__device__ __forceinline__ uint32_t Smem(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ uint64_t OperandDesc(uint32_t addr) {
-  uint64_t d = static_cast<uint64_t>((addr & 0x3FFFF) >> 4);
-  d |= static_cast<uint64_t>(128 >> 4) << 16;  // leading (K) byte offset between core matrices
-  d |= static_cast<uint64_t>(kSbo >> 4) << 32; // stride byte offset between 8-row groups
-  d |= static_cast<uint64_t>(1) << 46;         // descriptor version of sm_100 and later
-  return d;                                    // base offset 0, no swizzle
-}
 
 // kind::f16 instruction descriptors: D fp32, both operands K-major, N = 256, M = 128;
 // layer 1 reads bf16 A and B (features, W1), layer 2 IEEE half A and B (H1, W2).
 constexpr uint32_t kIdescBf16 =
     (1u << 4) | (1u << 7) | (1u << 10) | ((kTcHidden >> 3) << 17) | ((kTcRows >> 4) << 24);
 constexpr uint32_t kIdescF16 = (1u << 4) | ((kTcHidden >> 3) << 17) | ((kTcRows >> 4) << 24);
-
-__device__ __forceinline__ void Mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1 : 0));
-}
 
 // GELU of two values in packed half precision (layer-1 epilogue: H1 is stored in
 // half for the layer-2 MMA): u = z (c0 + c1 z^2), GELU = h + h tanh(u), h = z / 2.
@@ -79,74 +78,6 @@ __device__ __forceinline__ __half2 GeluHalf2(__half2 z) {
   const __half2 t = *reinterpret_cast<const __half2 *>(&tb);
   const __half2 h = __hmul2(z, __float2half2_rn(0.5f));
   return __hfma2(h, t, h);
-}
-__device__ __forceinline__ void Commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(Smem(bar)));
-}
-__device__ __forceinline__ void Arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(Smem(bar)) : "memory");
-}
-__device__ __forceinline__ void BarInit(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(Smem(bar)), "r"(count));
-}
-__device__ __forceinline__ bool TryWait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(Smem(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Waits for the completion of the barrier phase with the given parity. False
-// when it expires or another warp gave up (the abort flag), which it then sets.
-__device__ __forceinline__ bool Wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
-  for (long long it = 0; it < kWaitLimit; ++it) {
-    if (TryWait(bar, parity)) return true;
-    if ((it & 63) == 0 && *abort) return false;
-  }
-  *abort = 1;
-  return false;
-}
-// Bounded wait that ignores the abort flag (draining work already issued).
-__device__ __forceinline__ bool WaitDrain(uint64_t *bar, uint32_t parity) {
-  for (long long it = 0; it < kWaitLimit; ++it)
-    if (TryWait(bar, parity)) return true;
-  return false;
-}
-__device__ __forceinline__ void ArriveExpectTx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(Smem(bar)), "r"(bytes) : "memory");
-}
-// Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on `bar`.
-__device__ __forceinline__ void BulkCopy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(Smem(dst)),
-      "l"(src), "r"(bytes), "r"(Smem(bar))
-      : "memory");
-}
-__device__ __forceinline__ void CpAsync16(void *smem, const void *gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(Smem(smem)), "l"(gmem));
-}
-__device__ __forceinline__ void CpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int kPending>
-__device__ __forceinline__ void CpAsyncWait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
-}
-__device__ __forceinline__ void FenceAsyncSmem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// 32 consecutive fp32 columns of this thread's TMEM lane. The wait carries the
-// 32 registers as operands (no memory clobber), so the compiler keeps their uses
-// after it while still free to issue independent loads (biases) earlier.
-__device__ __forceinline__ void TmemLoad32(uint32_t addr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(addr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;"
-               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
-#pragma unroll
-  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 // Byte offset of element (r, k) in a sequence of 32-wide operand tiles of `rows` rows.

@@ -82,6 +82,16 @@ struct lmc_mlp {
 
   void Cast() { CudaCheck(lmc::MlpCastWeights(d, stream), "cast weights"); }
 
+  // A tcgen05 training GEMM whose bounded wait expired leaves its outputs unwritten.
+  void CheckGemmStatus() {
+    int st = 0;
+    CudaCheck(cudaMemcpy(&st, d.gemm_status, sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    if (st != 0) {
+      CudaCheck(cudaMemset(d.gemm_status, 0, sizeof(int)), "memset");
+      throw lmc::abi::LmcError(LMC_ERR_STOPPED, "surrogate training: a tensor-core wait expired");
+    }
+  }
+
   // One optimisation step on the batch already in xb / tb.
   void TrainStep(int batch, float lr) {
     CudaCheck(lmc::MlpTranspose(xb, batch, d.in, xt, stream), "transpose");
@@ -135,6 +145,12 @@ int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_
     m->m2 = DevAlloc<float>(m->num_params, &m->owned);
     m->loss = DevAlloc<float>(members, &m->owned);
     m->status = DevAlloc<int>(1, &m->owned);
+    m->d.gemm_status = DevAlloc<int>(1, &m->owned);
+    CudaCheck(cudaMemset(m->d.gemm_status, 0, sizeof(int)), "memset");
+    m->d.gemm_mma_sync = 0;
+    // split-K partials of the weight-gradient GEMMs: up to 16 splits of the largest gradient
+    m->d.gemm_ws_floats = 16LL * members * hidden * std::max(hidden, in_features);
+    m->d.gemm_ws = DevAlloc<float>(static_cast<size_t>(m->d.gemm_ws_floats), &m->owned);
     const long long H = hidden, M = members;
     m->d.w1 = m->params;
     m->d.b1 = m->d.w1 + M * H * in_features;
@@ -233,6 +249,7 @@ int lmc_mlp_gradients(lmc_mlp *mlp, const uint16_t *x, const float *labels, int 
       CudaCheck(cudaMemcpyAsync(loss, mlp->loss, sizeof(float) * mlp->d.members, cudaMemcpyDeviceToHost, mlp->stream),
                 "D2H");
     CudaCheck(cudaStreamSynchronize(mlp->stream), "sync");
+    mlp->CheckGemmStatus();
   });
 }
 
@@ -277,9 +294,18 @@ int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *x_dev, const float *labels_dev, 
       throw;
     }
     cudaFree(dperm);
+    mlp->CheckGemmStatus();
     // mean loss per member over the last epoch, in standardised label units
     if (loss)
       for (int m = 0; m < mlp->d.members; ++m) loss[m] = host_loss[m] / static_cast<float>(steps_per_epoch);
+  });
+}
+
+int lmc_mlp_set_train_path(lmc_mlp *mlp, int path) {
+  return Guard([&] {
+    Require(mlp != nullptr, LMC_ERR_INVALID_ARGUMENT, "mlp is null");
+    Require(path == 0 || path == 1, LMC_ERR_INVALID_ARGUMENT, "path must be 0 (tcgen05) or 1 (mma.sync)");
+    mlp->d.gemm_mma_sync = path;
   });
 }
 

@@ -282,12 +282,14 @@ def test_sparse_equals_dense_bitwise(api, base_fraction, warps):
     assert np.array_equal(t0, t1) and np.array_equal(e0, e1)
 
 
-@pytest.mark.parametrize("base_fraction", [0.96, 0.8, 0.6])
+@pytest.mark.parametrize("base_fraction", [0.96, 0.9])
 def test_barrier_batch_sparse_equals_dense(api, oracle_mod, base_fraction):
     """lmc_barrier_batch's sparse path (runs of jumps that share a vacancy, evaluated once with the
     solvent-relative sums) gives the dense per-pair results bit for bit: the 12 jumps of every
-    vacancy of a vacancy grid, jumps asked singly and in a shuffled order, and pairs whose first
-    site is not a vacancy; a vacancy with a second vacancy in its environments raises on both."""
+    vacancy of a vacancy grid, a vacancy whose 1-3NN shells are all solute (more non-solvent sites
+    than the sparse lists hold: its run falls back to the dense pairs), jumps asked singly and in a
+    shuffled order, and pairs whose first site is not a vacancy; a vacancy with a second vacancy in
+    its environments raises on both."""
     from latticemontecarlo_gb300 import synthetic as S
     el = ("Al", "Mg", "Zn")
     coeffs = S.make_coefficients(el, 8)
@@ -300,9 +302,10 @@ def test_barrier_batch_sparse_equals_dense(api, oracle_mod, base_fraction):
     vac = np.array([a * 2 * n * n + b * n + c // 2 for a, b, c in grid])
     sp[vac] = x
     sp[vac[0] + 1] = x  # a second vacancy inside vac[0]'s environments
+    lat = oracle_mod.Lattice(n)
+    sp[lat.neighbors(int(vac[1]))] = S.alphabet(el).index("Mg")  # a solute-rich neighbourhood
     ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
     ctx.set_lattices([n], sp)
-    lat = oracle_mod.Lattice(n)
     grouped = np.array([[v, j] for v in vac[1:] for j in lat.neighbors(int(v))[:12]], np.int64)
     rng = np.random.default_rng(3)
     shuffled = grouped[rng.permutation(len(grouped))[:200]]

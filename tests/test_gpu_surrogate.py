@@ -33,11 +33,14 @@ def _bits(x_bf16):
     return x_bf16.contiguous().view(torch.int16).cpu().numpy().view(np.uint16)
 
 
-def test_gradients_against_float64(setup):
+@pytest.mark.parametrize("train_path", [0, 1])
+def test_gradients_against_float64(setup, train_path):
+    """Both training-GEMM paths (0: tcgen05 with TMEM accumulators, 1: mma.sync) against float64."""
     torch, api, ctx, el, coeffs, nin = setup
     from oracle import mlp as R
     hidden, members, batch = 128, 2, 128
     net = api.Surrogate(nin, hidden, members, seed=5)
+    net.set_train_path(train_path)
     x, ea, _, _ = api.surrogate_dataset(ctx, 11, batch, 0.0, 0.3, nin)
     ea_h = ea.cpu().numpy()
     net.set_label_scale(float(ea_h.mean()), float(ea_h.std()))
@@ -57,6 +60,32 @@ def test_gradients_against_float64(setup):
         cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
         assert rel < 3e-2 and cos > 0.999, (name, rel, cos)
         off += sz
+
+
+def test_tcgen05_training_gemms_match_mma_sync(setup):
+    """The tcgen05 training GEMMs and the mma.sync ones give the same gradients to the rounding of
+    their FP32 sums (the BF16 activations they store may differ by one BF16 step), on the
+    workload's own shapes (hidden 256, 4 members, a batch of 512), and one training epoch from
+    the same start reaches the same loss."""
+    torch, api, ctx, el, coeffs, nin = setup
+    hidden, members, batch = 256, 4, 512
+    x, ea, _, _ = api.surrogate_dataset(ctx, 13, batch, 0.0, 0.3, nin)
+    ea_h = ea.cpu().numpy()
+    bits = _bits(x)
+    grads, losses = [], []
+    for path in (0, 1):
+        net = api.Surrogate(nin, hidden, members, seed=9)
+        net.set_label_scale(float(ea_h.mean()), float(ea_h.std()))
+        net.set_train_path(path)
+        g, _ = net.gradients(bits, ea_h)
+        grads.append(g.astype(np.float64))
+        xt, et, _, _ = api.surrogate_dataset(ctx, 21, 8192, 0.0, 0.3, nin)
+        losses.append(net.train(xt, et, batch=1024, epochs=1, lr=2e-3, seed=4))
+    a, b = grads
+    rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+    cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+    assert rel < 1e-2 and cos > 0.9999, (rel, cos)
+    np.testing.assert_allclose(losses[0], losses[1], rtol=2e-2)
 
 
 def test_dataset_labels_match_oracle(setup, oracle_mod):
