@@ -334,6 +334,32 @@ void BuildTables(lmc_ctx *c) {
   for (int d = 0; d < lmc::kDirections; ++d)
     dir_of[(pt.dir[d].x + 1) * 9 + (pt.dir[d].y + 1) * 3 + (pt.dir[d].z + 1)] = static_cast<int8_t>(d);
   t.dir = c->Upload(dir);
+  {
+    // Id order of a site's 12 first neighbours. Ids are lexicographic in the wrapped half-lattice
+    // coordinates, and a +-1 step wraps only at coordinate 0 (-1 becomes the largest) or 2n - 1
+    // (+1 becomes the smallest), so the order depends only on which axes sit on a boundary:
+    // per axis 0 interior, 1 at 0, 2 at 2n - 1; case = 9 s_x + 3 s_y + s_z; entry q = the
+    // direction of rank q.
+    std::vector<int8_t> order(27 * lmc::kDirections);
+    for (int cs = 0; cs < 27; ++cs) {
+      const int st[3] = {cs / 9, (cs / 3) % 3, cs % 3};
+      auto key = [&](int d) {
+        const int v[3] = {pt.dir[d].x, pt.dir[d].y, pt.dir[d].z};
+        std::array<int, 3> k{};
+        for (int a = 0; a < 3; ++a) {
+          // the step's value relative to the site on an axis of width 8, site at 4 / 0 / 7
+          const int h = st[a] == 0 ? 4 : (st[a] == 1 ? 0 : 7);
+          k[a] = ((h + v[a]) % 8 + 8) % 8;
+        }
+        return k;
+      };
+      std::vector<int> ds(lmc::kDirections);
+      for (int d = 0; d < lmc::kDirections; ++d) ds[d] = d;
+      std::sort(ds.begin(), ds.end(), [&](int a, int b) { return key(a) < key(b); });
+      for (int q = 0; q < lmc::kDirections; ++q) order[cs * lmc::kDirections + q] = static_cast<int8_t>(ds[q]);
+    }
+    t.id_order = c->Upload(order);
+  }
   t.dir_of = c->Upload(dir_of);
   t.state_off = c->Upload(st_off);
   t.mmm_off = c->Upload(mmm_off);

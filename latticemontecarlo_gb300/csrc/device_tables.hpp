@@ -28,6 +28,7 @@ struct DevTables {
   const int8_t *site_off;    // [43][4]
   const int8_t *local_off;   // [135][4] KMC neighbourhood of a vacancy
   const uint8_t *shell_local;  // [42] local indices of the vacancy's 1NN, 2NN, 3NN shells
+  const int8_t *id_order;    // [27][12] direction of id rank q, per boundary case (context.cpp)
   const uint8_t *local_st;   // [12][60] state list of jump c as indices into the local list
   const uint8_t *local_mmm;  // [12][58]
   const uint8_t *local_mm2f; // [12][58]

@@ -1661,15 +1661,12 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
           }
         }
       }
-      // lane q takes the event of rank q in the id-sorted 1NN list
-      int rank = 0;
-      for (int q = 0; q < 12; ++q) {
-        const long long oid = __shfl_sync(0xffffffffu, id, q);
-        rank += (q != lane) && (oid < id);
-      }
-      int src = 0;
-      for (int q = 0; q < 12; ++q)
-        if (__shfl_sync(0xffffffffu, rank, q) == lane) src = q;
+      // lane q takes the event of rank q in the id-sorted 1NN list: the order depends only on
+      // which axes of the vacancy lie on the periodic boundary (t.id_order)
+      const int m2 = 2 * n - 1;
+      const int bcase = (hv.x == 0 ? 9 : (hv.x == m2 ? 18 : 0)) + (hv.y == 0 ? 3 : (hv.y == m2 ? 6 : 0)) +
+                        (hv.z == 0 ? 1 : (hv.z == m2 ? 2 : 0));
+      const int src = lane < 12 ? __ldg(&t.id_order[bcase * 12 + lane]) : lane;
       const double k_s = __shfl_sync(0xffffffffu, k, src);
       const Real ea_s = __shfl_sync(0xffffffffu, ea, src);
       const Real de_s = __shfl_sync(0xffffffffu, de, src);
