@@ -493,6 +493,7 @@ void BuildSparse(lmc_ctx *c, int base) {
   c->sparse_bufs.clear();
   lmc::KmcSparse sp{};
   sp.base_code = base;
+  sp.x_code = fm.x_code;
   auto w = [&](int label, int c0, int c1, int c2) {
     return static_cast<long long>(fm.w_de[((label * e + c0) * e + c1) * e + c2]);
   };

@@ -51,7 +51,8 @@ __device__ __forceinline__ H3 SiteCoord(long long id, int n) {
   return {static_cast<int>(hx), static_cast<int>(hy), static_cast<int>(2 * k + ((hx + hy) & 1u))};
 }
 
-// Id of h + (dx, dy, dz) with periodic wrap; |offset| <= 4 < 2n.
+// Id of h + (dx, dy, dz) with periodic wrap; |offset| <= 4 < 2n. 32-bit unsigned
+// arithmetic: (x 2n + y) n + z / 2 < 4 n^3 < 2^32 for n <= 1000.
 __device__ __forceinline__ long long NeighborId(H3 h, int dx, int dy, int dz, int n) {
   const int m = 2 * n;
   int x = h.x + dx, y = h.y + dy, z = h.z + dz;
@@ -61,7 +62,9 @@ __device__ __forceinline__ long long NeighborId(H3 h, int dx, int dy, int dz, in
   y -= (y >= m) ? m : 0;
   z += (z < 0) ? m : 0;
   z -= (z >= m) ? m : 0;
-  return static_cast<long long>(x) * 2 * n * n + static_cast<long long>(y) * n + (z >> 1);
+  const unsigned nn = static_cast<unsigned>(n);
+  return static_cast<long long>((static_cast<unsigned>(x) * 2u * nn + static_cast<unsigned>(y)) * nn +
+                                (static_cast<unsigned>(z) >> 1));
 }
 
 // h + (dx, dy, dz) with periodic wrap (half units); |offset| <= 4 < 2n.
@@ -1136,6 +1139,7 @@ struct KmcShared {
   int dsel;                         // direction index of the selected jump
   int escaped;                      // early stop: this step's vacancy had only solvent in its 1-3NN shells
   int nbk;                          // non-base sites in the neighbourhood (sparse evaluation)
+  int has_x;                        // one of them is a vacancy (the checked sparse sums)
   int npairs;                       // pairs of them that share a cluster in some jump
   uint8_t nb_l[kMaxSparseSites + 1];    // their local indices; padding: kLocalSites (in no list)
   int8_t nb_code[kMaxSparseSites + 1];  // and species; padding: the base species
@@ -1199,7 +1203,10 @@ struct LaneAcc {
 // forward (A) and backward (B). Branch-free, four entries at a time, so the
 // table loads of independent entries overlap. Returns the corrections to the
 // all-base constants.
-__device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint8_t *s_pos, const uint16_t *s_pxst,
+// kCheckX: a listed site may be a vacancy (then the status bits of the reference's exceptions are
+// formed); without one, no site lacks a one-hot rank and the checks are skipped.
+template <bool kCheckX>
+__device__ __forceinline__ LaneAcc EvalJumpPairsT(const KmcSparse &sp, const uint8_t *s_pos, const uint16_t *s_pxst,
                                                  const uint32_t *s_pxenv, const SmallTables *sm, const KmcShared &rs,
                                                  int e, int x, int c, int part, int mig, int slot, bool quartic) {
   long long acc_a = 0, acc_b = 0;
@@ -1230,9 +1237,11 @@ __device__ __forceinline__ LaneAcc EvalJumpPairs(const KmcSparse &sp, const uint
       const bool in_a = pa != 255, in_b = pb != 255;
       va[u] = __ldg(&sg_a[(in_a ? pa : zero_a) * stride_a + (part == 0 ? code : rp)]);
       vb[u] = __ldg(&sg_b[(in_b ? pb : kEnvSites) * 8 + rp]);
-      const bool bad_rank = rp == kMaxOnehot - 1;
-      bad |= (part == 0 && in_a && code == x) ? kStatusBadCluster : 0u;
-      bad |= (((part == 1 && in_a) || in_b) && bad_rank) ? kStatusXInEnv : 0u;
+      if constexpr (kCheckX) {  // only a vacancy lacks a one-hot rank
+        const bool bad_rank = rp == kMaxOnehot - 1;
+        bad |= (part == 0 && in_a && code == x) ? kStatusBadCluster : 0u;
+        bad |= (((part == 1 && in_a) || in_b) && bad_rank) ? kStatusXInEnv : 0u;
+      }
     }
     acc_a += (va[0] + va[1]) + (va[2] + va[3]);
     acc_b += (vb[0] + vb[1]) + (vb[2] + vb[3]);
@@ -1334,11 +1343,13 @@ __device__ __forceinline__ void StageKmcSmem(const DevTables &t, const KmcSparse
 // kMaxSparseSites / kMaxSparsePairs mean the lists are incomplete.
 __device__ __forceinline__ void SparseList(KmcShared &rs, const uint32_t *s_inter, const KmcSparse &sp, int lane) {
   int k_sites = 0;
+  bool any_x = false;
 #pragma unroll
   for (int w = 0; w < 5; ++w) {
     const int k = w * 32 + lane;
     const int code = k < kLocalSites ? rs.local[k] : sp.base_code;
     const bool nb = code != sp.base_code && k != sp.center;
+    any_x |= nb && code == sp.x_code;
     const unsigned mk = __ballot_sync(0xffffffffu, nb);
     const int idx = k_sites + __popc(mk & ((1u << lane) - 1u));
     if (nb && idx < kMaxSparseSites) {
@@ -1384,9 +1395,11 @@ __device__ __forceinline__ void SparseList(KmcShared &rs, const uint32_t *s_inte
     if (lane < ((n_pairs + 3) & ~3) - n_pairs)
       rs.pairs[n_pairs + lane] = static_cast<uint16_t>(kMaxSparseSites | (kMaxSparseSites << 8));
   }
+  const bool has_x = __any_sync(0xffffffffu, any_x);
   if (lane == 0) {
     rs.nbk = k_sites;
     rs.npairs = n_pairs;
+    rs.has_x = has_x ? 1 : 0;
   }
 }
 
@@ -1404,8 +1417,10 @@ __device__ __forceinline__ unsigned SparseItem(const DevTables &t, const KmcSpar
     const bool quartic = barrier_kind == 0;
     const bool ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
     if (ok && (part == 0 || quartic))
-      la = EvalJumpPairs(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code, c, part, mig, slot,
-                         quartic);
+      la = rs.has_x ? EvalJumpPairsT<true>(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code, c,
+                                           part, mig, slot, quartic)
+                    : EvalJumpPairsT<false>(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code, c,
+                                            part, mig, slot, quartic);
     if (ok) {
       const long long *bf = sp.base_form + slot * 3;
       if (part == 0) {

@@ -79,6 +79,7 @@ struct KmcSparse {
   int dw_stride_mmm, dw_stride_mm2;
   int base_code;
   int center;  // local index of the vacancy site
+  int x_code;  // species code of the vacancy
 };
 
 struct KmcLaunch {
