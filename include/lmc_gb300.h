@@ -213,9 +213,10 @@ int lmc_fastmath_check(lmc_ctx *ctx, int fn, const double *x, int64_t n, double 
 /* ------------------------------------------------------------------------- */
 /* Ensemble of `members` MLPs in -> hidden -> hidden -> 1 (GELU), BF16 weights and
  * activations on the tensor cores, FP32 accumulation, FP32 master weights, Adam.
- * Features (bf16 rows, passed as uint16_t): the one-hot rank of the 58 MMM-ordered
+ * Features (bf16 rows, passed as uint16_t): channels of the 58 MMM-ordered
  * environment sites of a jump (VacancyMigrationPredictorQuartic's MMM list), then of
- * the migrant, zero padded to in_features (a multiple of 64). */
+ * the migrant, zero padded to in_features (a multiple of 64); the context's encoding
+ * (lmc_surrogate_set_encoding) sets the channels. */
 typedef struct lmc_mlp lmc_mlp;
 int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_t seed, lmc_mlp **out);
 void lmc_mlp_destroy(lmc_mlp *mlp);
@@ -237,13 +238,26 @@ int lmc_mlp_train(lmc_mlp *mlp, const uint16_t *features_dev, const float *label
  * TMEM) for every GEMM whose rows are a multiple of 128 (batch and hidden widths), the mma.sync
  * kernel otherwise; 1 the mma.sync kernel for all. Same arithmetic (BF16 products, FP32 sums). */
 int lmc_mlp_set_train_path(lmc_mlp *mlp, int path);
-/* Inference kernels: 0 automatic (the fused tcgen05 kernel when hidden = 256 and
- * in_features <= 256), 1 tcgen05, 2 the mma.sync GEMMs of training. */
+/* Inference kernels: 0 automatic (tcgen05 where a kernel serves the network: feature rows
+ * for hidden = 256 and in_features <= 256; lattice jumps, features gathered inside the
+ * kernel, for 2 members of 128 -> 128 -> 128 with solute-channel features of a
+ * three-species alphabet), 1 tcgen05, 2 the mma.sync GEMMs of training. */
 int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path);
 /* Ensemble mean and spread (max - min over members), eV, for n feature rows (device arrays). */
 int lmc_mlp_predict(lmc_mlp *mlp, const uint16_t *features_dev, int64_t n, float *mean_dev, float *spread_dev);
 
-/* Feature row length of a context's model: at least 59 x one-hot alphabet, padded to 64. */
+/* Feature encodings of the surrogate (per site, one channel set to 1):
+ * ONEHOT  the one-hot rank of the species (E' channels, E' = one-hot alphabet size);
+ * SOLUTE  one channel per species other than the base (the solvent, Al when present):
+ *         E' - 1 channels, a base site is all zero. A network's first-layer bias absorbs
+ *         the base, so both encodings describe the same function class. */
+#define LMC_FEATURES_ONEHOT 0
+#define LMC_FEATURES_SOLUTE 1
+/* Encoding of the context's surrogate features, datasets and lattice-jump inference
+ * (default ONEHOT). A network must be used with the encoding it was trained on. */
+int lmc_surrogate_set_encoding(lmc_ctx *ctx, int encoding);
+/* Feature row length of a context's model and encoding: at least 59 x the channels per
+ * site, padded to 64. */
 int lmc_surrogate_feature_count(const lmc_ctx *ctx, int *min_features, int *padded_features);
 /* Training data: `count` seeded random neighbourhoods (solute fraction ~ U(solute_lo, solute_hi),
  * solutes equally likely, the rest the base element), their features and the plain
@@ -253,6 +267,11 @@ int lmc_surrogate_dataset(lmc_ctx *ctx, uint64_t seed, int64_t count, double sol
 /* Features of lattice jumps (pairs first -> second, device arrays). */
 int lmc_surrogate_features(lmc_ctx *ctx, int replica, const int64_t *pairs_dev, int m, int in_features,
                            uint16_t *features_dev);
+/* The network alone on m lattice jumps (device arrays): ensemble mean and spread (max - min
+ * over members), eV. Rows that the network cannot describe (a pair that is not a 1NN jump,
+ * an environment with a second vacancy) get spread +inf in the fused kernel. */
+int lmc_surrogate_predict_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, const int64_t *pairs_dev, int m,
+                                 float *mean_dev, float *spread_dev);
 /* Surrogate barriers of m jumps (device arrays): the ensemble mean, or the plain predictor
  * (lmc_barrier_batch) where the ensemble spread exceeds threshold_ev; fallback_dev (nullable)
  * flags those pairs and num_fallback (nullable) counts them. */

@@ -27,6 +27,8 @@ LMC_BARRIER_E0 = 1
 LMC_RNG_MT19937_64 = 0
 LMC_RNG_PHILOX = 1
 LMC_EVAL_SPARSE = 0
+LMC_FEATURES_ONEHOT = 0
+LMC_FEATURES_SOLUTE = 1
 LMC_EVAL_DENSE = 1
 LMC_RATES_FP32 = 0
 LMC_RATES_FP64 = 1
@@ -141,10 +143,12 @@ SIGNATURES = {
     "lmc_mlp_predict": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "lmc_mlp_set_inference_path": (C.c_int, [_P, C.c_int]),
     "lmc_mlp_set_train_path": (C.c_int, [_P, C.c_int]),
+    "lmc_surrogate_set_encoding": (C.c_int, [_P, C.c_int]),
     "lmc_surrogate_feature_count": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "lmc_surrogate_dataset": (C.c_int, [_P, C.c_uint64, C.c_int64, C.c_double, C.c_double, C.c_int, C.c_int, _P, _P,
                                         _P, _P]),
     "lmc_surrogate_features": (C.c_int, [_P, C.c_int, _P, C.c_int, C.c_int, _P]),
+    "lmc_surrogate_predict_device": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P]),
     "lmc_surrogate_barrier_batch_device": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.c_float, _P, _P,
                                                      C.POINTER(C.c_int)]),
     "lmc_kmc_init": (C.c_int, [_P, _DP, C.POINTER(KmcOptions)]),

@@ -151,6 +151,11 @@ class Context:
         """LMC_EVAL_SPARSE (default) or LMC_EVAL_DENSE for barrier_batch and the surrogate's fallback."""
         check(N.lib.lmc_ctx_set_barrier_evaluation(self._h, evaluation))
 
+    def set_surrogate_encoding(self, encoding: int) -> None:
+        """LMC_FEATURES_ONEHOT (default) or LMC_FEATURES_SOLUTE for the surrogate's features,
+        datasets and lattice-jump inference."""
+        check(N.lib.lmc_surrogate_set_encoding(self._h, encoding))
+
     def encode_batch(self, pairs, replica: int = 0):
         p = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
         m, mo = p.shape[0], self.model
@@ -401,6 +406,7 @@ class Surrogate:
         check(N.lib.lmc_mlp_create(device, in_features, hidden, members, seed, C.byref(h)))
         self._h = h
         self.in_features, self.hidden, self.members = in_features, hidden, members
+        self.label_scale = (0.0, 1.0)
         n = np.zeros(1, np.int64)
         check(N.lib.lmc_mlp_layout(h, None, None, None, ptr(n, C.c_int64)))
         self.num_params = int(n[0])
@@ -423,6 +429,7 @@ class Surrogate:
 
     def set_label_scale(self, mean: float, std: float) -> None:
         check(N.lib.lmc_mlp_set_label_scale(self._h, float(mean), float(std)))
+        self.label_scale = (float(mean), float(std))
 
     def gradients(self, features_bf16_bits: np.ndarray, labels: np.ndarray):
         x = np.ascontiguousarray(features_bf16_bits, np.uint16)
@@ -477,6 +484,27 @@ def surrogate_dataset(ctx: "Context", seed: int, count: int, solute_lo: float, s
                                       C.c_void_p(ea64.data_ptr()),
                                       C.c_void_p(de64.data_ptr()) if de64 is not None else None))
     return x, ea, ea64, de64
+
+
+def surrogate_predict(ctx: "Context", model: Surrogate, pairs_dev, replica: int = 0):
+    """The network alone on lattice jumps: ensemble mean and spread, eV (torch tensors)."""
+    import torch
+    m = pairs_dev.shape[0]
+    mean = torch.empty(m, dtype=torch.float32, device=pairs_dev.device)
+    spread = torch.empty(m, dtype=torch.float32, device=pairs_dev.device)
+    check(N.lib.lmc_surrogate_predict_device(ctx._h, model._h, replica, C.c_void_p(pairs_dev.data_ptr()), m,
+                                             C.c_void_p(mean.data_ptr()), C.c_void_p(spread.data_ptr())))
+    return mean, spread
+
+
+def surrogate_features(ctx: "Context", pairs_dev, in_features: int, replica: int = 0):
+    """Feature rows of lattice jumps in the context's encoding (bfloat16 torch tensor)."""
+    import torch
+    m = pairs_dev.shape[0]
+    x = torch.empty((m, in_features), dtype=torch.bfloat16, device=pairs_dev.device)
+    check(N.lib.lmc_surrogate_features(ctx._h, replica, C.c_void_p(pairs_dev.data_ptr()), m, in_features,
+                                       C.c_void_p(x.data_ptr())))
+    return x
 
 
 def surrogate_barriers(ctx: "Context", model: Surrogate, pairs_dev, threshold_ev: float = 0.010, replica: int = 0,

@@ -88,6 +88,7 @@ struct lmc_ctx {
   std::vector<long long> first_host;          // per replica lowest X site (LLONG_MAX: none)
   bool scan_fresh{false};                     // scan_host / first_host describe the current lattices
   int barrier_eval{LMC_EVAL_SPARSE};          // evaluation of the barrier batch entry points
+  int feat_encoding{LMC_FEATURES_ONEHOT};     // surrogate feature rows (lmc_surrogate_set_encoding)
   DevBuf scan_first;
   // batch scratch
   DevBuf pairs, out0, out1, out2, out3, status, counts, energy, enc;
@@ -1451,12 +1452,68 @@ int SurrogateBase(const lmc_ctx *ctx) {
     if (c != ctx->fm.x_code && ctx->fm.onehot_rank[c] >= 0) return c;
   return -1;
 }
+
+// Channels of a site for the context's feature encoding: the one-hot rank, or (solute
+// channels) the ranks other than the base species' in their order.
+lmc::FeatEnc FeatEncOf(const lmc_ctx *ctx) {
+  const int eh = ctx->fm.num_onehot;
+  lmc::FeatEnc f{~0ull, eh};
+  const int base = SurrogateBase(ctx);
+  const int rb = (ctx->feat_encoding == LMC_FEATURES_SOLUTE && base >= 0) ? ctx->fm.onehot_rank[base] : -1;
+  if (rb >= 0) f.width = eh - 1;
+  for (int r = 0; r < eh && r < lmc::kMaxOnehot - 1; ++r) {
+    const int ch = rb < 0 ? r : (r == rb ? -1 : (r < rb ? r : r - 1));
+    if (ch >= 0) {
+      f.rank_ch &= ~(0xFFull << (8 * r));
+      f.rank_ch |= static_cast<unsigned long long>(ch) << (8 * r);
+    }
+  }
+  return f;
+}
+
+int FeatureCount(const lmc_ctx *ctx) { return (lmc::kEnvSites + 1) * FeatEncOf(ctx).width; }
+
+// The fused jump kernel's description of the replica's lattice and the encoding (solute
+// channels of a three-species alphabet: two bf16 channels per site, one word).
+bool FusedJumpsFor(const lmc_ctx *ctx, int replica, const long long *pairs, long long m, float *mean, float *spread,
+                   lmc::FusedJumps *j) {
+  const lmc::FeatEnc f = FeatEncOf(ctx);
+  if (ctx->feat_encoding != LMC_FEATURES_SOLUTE || f.width != 2) return false;
+  *j = lmc::FusedJumps{};
+  j->species = ctx->species.as<int8_t>() + ctx->offsets[replica];
+  j->n = ctx->n[replica];
+  j->pairs = pairs;
+  j->m = m;
+  j->mmm_off = ctx->t.mmm_off;
+  j->dir_of = ctx->t.dir_of;
+  for (int c = 0; c < 8; ++c) {
+    const int rank = c < ctx->fm.num_species ? ctx->fm.onehot_rank[c] : -1;
+    const int ch = rank >= 0 ? lmc::FeatChannel(f, rank) : -1;
+    j->site_word[c] = ch == 0 ? 0x3F80u : (ch == 1 ? 0x3F800000u : 0u);  // bf16 1.0 in the low / high half
+    if (rank < 0) j->fallback_codes |= 1u << c;
+  }
+  j->mean = mean;
+  j->spread = spread;
+  j->pair_status = ctx->status.as<int>();
+  return true;
+}
 }  // namespace
+
+int lmc_surrogate_set_encoding(lmc_ctx *ctx, int encoding) {
+  return Guard([&] {
+    Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
+    Require(encoding == LMC_FEATURES_ONEHOT || encoding == LMC_FEATURES_SOLUTE, LMC_ERR_INVALID_ARGUMENT,
+            "unknown feature encoding");
+    Require(encoding == LMC_FEATURES_ONEHOT || SurrogateBase(ctx) >= 0, LMC_ERR_INVALID_ARGUMENT,
+            "no base species with a one-hot slot");
+    ctx->feat_encoding = encoding;
+  });
+}
 
 int lmc_surrogate_feature_count(const lmc_ctx *ctx, int *min_features, int *padded_features) {
   return Guard([&] {
     Require(ctx != nullptr, LMC_ERR_INVALID_ARGUMENT, "ctx is null");
-    const int need = (lmc::kEnvSites + 1) * ctx->fm.num_onehot;
+    const int need = FeatureCount(ctx);
     if (min_features) *min_features = need;
     if (padded_features) *padded_features = (need + 63) / 64 * 64;
   });
@@ -1470,10 +1527,10 @@ int lmc_surrogate_dataset(lmc_ctx *ctx, uint64_t seed, int64_t count, double sol
     Require(0.0 <= solute_lo && solute_lo <= solute_hi && solute_hi <= 1.0, LMC_ERR_INVALID_ARGUMENT,
             "need 0 <= solute_lo <= solute_hi <= 1");
     Require(kind == LMC_BARRIER_QUARTIC || kind == LMC_BARRIER_E0, LMC_ERR_INVALID_ARGUMENT, "unknown barrier kind");
-    Require(in_features >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
-            "in_features below 59 x the one-hot alphabet");
+    Require(in_features >= FeatureCount(ctx), LMC_ERR_INVALID_ARGUMENT, "in_features below 59 x the site channels");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     lmc::SurrogateGen g{};
+    g.enc = FeatEncOf(ctx);
     g.seed = seed;
     g.count = count;
     g.solute_lo = static_cast<float>(solute_lo);
@@ -1498,16 +1555,61 @@ int lmc_surrogate_features(lmc_ctx *ctx, int replica, const int64_t *pairs_dev, 
   return Guard([&] {
     Require(ctx && pairs_dev && features_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
     ctx->CheckReplica(replica);
-    Require(in_features >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
-            "in_features below 59 x the one-hot alphabet");
+    Require(in_features >= FeatureCount(ctx), LMC_ERR_INVALID_ARGUMENT, "in_features below 59 x the site channels");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
     ctx->ClearStatus();
     CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
                                            reinterpret_cast<const long long *>(pairs_dev), m, in_features,
-                                           reinterpret_cast<__nv_bfloat16 *>(features_dev), ctx->status.as<int>(),
-                                           ctx->stream),
+                                           FeatEncOf(ctx), reinterpret_cast<__nv_bfloat16 *>(features_dev),
+                                           ctx->status.as<int>(), ctx->stream),
               "features kernel");
     RaiseStatus(ctx->ReadStatus(), "surrogate features");
+  });
+}
+
+namespace {
+// The ensemble's mean and spread for m lattice jumps (device arrays) on the context stream:
+// the fused jump kernel where the network and the encoding allow it (features gathered
+// inside), else the feature kernel and then the feature-row inference (tcgen05 kernel on the
+// context stream, or the mma.sync GEMMs on the network's stream, synchronised).
+void NetworkOnJumps(lmc_ctx *ctx, lmc_mlp *mlp, int replica, const long long *pairs, int m, float *mean,
+                    float *spread) {
+  const int in = lmc::MlpInputs(mlp);
+  Require(in >= FeatureCount(ctx), LMC_ERR_INVALID_ARGUMENT,
+          "the network's input is narrower than the features of this model and encoding");
+  lmc::FusedJumps j;
+  if (in == 128 && FusedJumpsFor(ctx, replica, pairs, m, mean, spread, &j) && lmc::MlpFusedJumpsAsync(mlp, j, ctx->stream))
+    return;
+  ctx->s_feat.Ensure(sizeof(uint16_t) * static_cast<size_t>(m) * in);
+  CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
+                                         pairs, m, in, FeatEncOf(ctx), ctx->s_feat.as<__nv_bfloat16>(),
+                                         ctx->status.as<int>(), ctx->stream),
+            "features kernel");
+  if (!lmc::MlpPredictAsync(mlp, ctx->s_feat.as<uint16_t>(), m, mean, spread, ctx->stream)) {
+    ctx->Sync();
+    const int st = lmc_mlp_predict(mlp, ctx->s_feat.as<uint16_t>(), m, mean, spread);
+    if (st != LMC_OK) throw LmcError(st, lmc_last_error());
+  }
+}
+}  // namespace
+
+int lmc_surrogate_predict_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, const int64_t *pairs_dev, int m,
+                                 float *mean_dev, float *spread_dev) {
+  return Guard([&] {
+    Require(ctx && mlp && pairs_dev && mean_dev && spread_dev, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    Require(m >= 0, LMC_ERR_INVALID_ARGUMENT, "m < 0");
+    ctx->CheckReplica(replica);
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (m == 0) return;
+    ctx->ClearStatus();
+    NetworkOnJumps(ctx, mlp, replica, reinterpret_cast<const long long *>(pairs_dev), m, mean_dev, spread_dev);
+    int *h = ctx->Pinned();
+    CudaCheck(cudaMemcpyAsync(h, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(h + 1, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ctx->Sync();
+    const int net_status = h[0], st = h[1];
+    Require(net_status == 0, LMC_ERR_STOPPED, "surrogate inference: a tensor-core wait expired");
+    RaiseStatus(st, "surrogate network");
   });
 }
 
@@ -1519,16 +1621,11 @@ int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, 
     Require(m >= 0, LMC_ERR_INVALID_ARGUMENT, "m < 0");
     ctx->CheckReplica(replica);
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
-    int in = 0;
-    Require(lmc_mlp_layout(mlp, &in, nullptr, nullptr, nullptr) == LMC_OK, LMC_ERR_INVALID_ARGUMENT, "bad mlp");
-    Require(in >= (lmc::kEnvSites + 1) * ctx->fm.num_onehot, LMC_ERR_INVALID_ARGUMENT,
-            "the network's input is narrower than the features of this model");
     if (m == 0) {
       if (num_fallback) *num_fallback = 0;
       return;
     }
     const size_t mm = static_cast<size_t>(m);
-    ctx->s_feat.Ensure(sizeof(uint16_t) * mm * in);
     ctx->s_mean.Ensure(sizeof(float) * mm);
     ctx->s_spread.Ensure(sizeof(float) * mm);
     ctx->s_fb_pairs.Ensure(sizeof(long long) * 2 * mm);
@@ -1537,18 +1634,7 @@ int lmc_surrogate_barrier_batch_device(lmc_ctx *ctx, lmc_mlp *mlp, int replica, 
     ctx->s_fb_de.Ensure(sizeof(double) * mm);
     const auto *pairs = reinterpret_cast<const long long *>(pairs_dev);
     ctx->ClearStatus();
-    CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],
-                                           pairs, m, in, ctx->s_feat.as<__nv_bfloat16>(), ctx->status.as<int>(),
-                                           ctx->stream),
-              "features kernel");
-    // the network on the context stream when the fused kernel serves it, else on its own (synchronised)
-    if (!lmc::MlpPredictAsync(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(), ctx->s_spread.as<float>(),
-                               ctx->stream)) {
-      ctx->Sync();
-      const int st = lmc_mlp_predict(mlp, ctx->s_feat.as<uint16_t>(), m, ctx->s_mean.as<float>(),
-                                     ctx->s_spread.as<float>());
-      if (st != LMC_OK) throw LmcError(st, lmc_last_error());
-    }
+    NetworkOnJumps(ctx, mlp, replica, pairs, m, ctx->s_mean.as<float>(), ctx->s_spread.as<float>());
     int *d_count = ctx->s_fb_index.as<int>() + mm;
     CudaCheck(cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream), "memset");
     CudaCheck(lmc::LaunchFallbackCompact(pairs, ctx->s_mean.as<float>(), ctx->s_spread.as<float>(), m, threshold_ev,

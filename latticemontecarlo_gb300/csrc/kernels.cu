@@ -25,6 +25,7 @@
 
 #include "kernels.cuh"
 #include "fastmath.cuh"
+#include "lattice_index.cuh"
 #include <cuda_bf16.h>
 
 namespace cg = cooperative_groups;
@@ -35,65 +36,6 @@ namespace {
 constexpr double kBoltzmannEv = 8.617333262145e-5;  // lmc/cfg/include/Constants.hpp:31
 constexpr double kPrefactor = 1e13;                 // lmc/cfg/include/Constants.hpp:32
 constexpr int kArr = 240;                           // per-warp sorted arrays: 60 + 3 * 58 (+pad)
-
-struct H3 {
-  int x, y, z;
-};
-
-__device__ __forceinline__ H3 SiteCoord(long long id, int n) {
-  // 32-bit unsigned arithmetic: supercells have n <= 1000, so 4 n^3 < 2^32
-  const unsigned u = static_cast<unsigned>(id), nn = static_cast<unsigned>(n);
-  const unsigned plane = 2u * nn * nn;
-  const unsigned hx = u / plane;
-  const unsigned r = u - hx * plane;
-  const unsigned hy = r / nn;
-  const unsigned k = r - hy * nn;
-  return {static_cast<int>(hx), static_cast<int>(hy), static_cast<int>(2 * k + ((hx + hy) & 1u))};
-}
-
-// Id of h + (dx, dy, dz) with periodic wrap; |offset| <= 4 < 2n. 32-bit unsigned
-// arithmetic: (x 2n + y) n + z / 2 < 4 n^3 < 2^32 for n <= 1000.
-__device__ __forceinline__ long long NeighborId(H3 h, int dx, int dy, int dz, int n) {
-  const int m = 2 * n;
-  int x = h.x + dx, y = h.y + dy, z = h.z + dz;
-  x += (x < 0) ? m : 0;
-  x -= (x >= m) ? m : 0;
-  y += (y < 0) ? m : 0;
-  y -= (y >= m) ? m : 0;
-  z += (z < 0) ? m : 0;
-  z -= (z >= m) ? m : 0;
-  const unsigned nn = static_cast<unsigned>(n);
-  return static_cast<long long>((static_cast<unsigned>(x) * 2u * nn + static_cast<unsigned>(y)) * nn +
-                                (static_cast<unsigned>(z) >> 1));
-}
-
-// h + (dx, dy, dz) with periodic wrap (half units); |offset| <= 4 < 2n.
-__device__ __forceinline__ H3 WrapCoord(H3 h, int dx, int dy, int dz, int n) {
-  const int m = 2 * n;
-  int x = h.x + dx, y = h.y + dy, z = h.z + dz;
-  x += (x < 0) ? m : 0;
-  x -= (x >= m) ? m : 0;
-  y += (y < 0) ? m : 0;
-  y -= (y >= m) ? m : 0;
-  z += (z < 0) ? m : 0;
-  z -= (z >= m) ? m : 0;
-  return {x, y, z};
-}
-
-__device__ __forceinline__ int MinImage(int d, int n) {
-  const int m = 2 * n;
-  d %= m;
-  if (d < -n) d += m;
-  if (d >= n) d -= m;
-  return d;
-}
-
-// Minimum image of a coordinate difference d in (-2n, 2n) (half units).
-__device__ __forceinline__ int WrapDelta(int d, int n) {
-  d += d < -n ? 2 * n : 0;
-  d -= d >= n ? 2 * n : 0;
-  return d;
-}
 
 // Direction index of a half-unit offset via the host-built 27-entry table
 // ((dx+1)*9 + (dy+1)*3 + (dz+1) -> index of the 1NN offset, -1 otherwise).
@@ -881,18 +823,18 @@ __device__ __forceinline__ double U01Open(uint32_t hi, uint32_t lo) {
 // ---------------------------------------------------------------------------
 // K6: surrogate training data and features.
 //
-// Features of a jump (MLP input, bf16 row of in_pad values): the one-hot rank
-// of each of the 58 MMM-ordered environment sites (58 x E' values, E' = one-hot
-// alphabet size, vacancies excluded), then the one-hot rank of the migrant
-// (E' values), zero padded.
+// Features of a jump (MLP input, bf16 row of in_pad values): for each of the 58
+// MMM-ordered environment sites, then the migrant, `width` channels, one of which
+// is 1 (FeatEnc: the one-hot rank, or a solute channel with the base species as
+// the all-zero site); zero padded.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void WriteFeatures(const int8_t *rm, int mig_rank, int eh, int in_pad,
+__device__ __forceinline__ void WriteFeatures(const int8_t *rm, int mig_rank, const FeatEnc &f, int in_pad,
                                               __nv_bfloat16 *row, int lane) {
-  const int env = kEnvSites * eh;
+  const int w = f.width, env = kEnvSites * w;
   for (int idx = lane; idx < in_pad; idx += 32) {
     bool one = false;
-    if (idx < env) one = rm[idx / eh] == idx % eh;
-    else if (idx < env + eh) one = mig_rank == idx - env;
+    if (idx < env) one = FeatChannel(f, rm[idx / w]) == idx % w;
+    else if (idx < env + w) one = FeatChannel(f, mig_rank) == idx - env;
     row[idx] = __float2bfloat16(one ? 1.0f : 0.0f);
   }
 }
@@ -913,7 +855,7 @@ __global__ void surrogate_dataset_kernel(DevTables t, SurrogateGen g) {
   int8_t *st = s.arr + warp * kArr;
   int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
   int8_t *local = locals + warp * 144;
-  const int e = t.num_species, eh = t.num_onehot;
+  const int e = t.num_species;
   // solutes: every non-vacancy species other than the base
   int solutes[8], ns = 0;
   for (int c = 0; c < e; ++c)
@@ -969,13 +911,13 @@ __global__ void surrogate_dataset_kernel(DevTables t, SurrogateGen g) {
       if (g.ea64) g.ea64[i] = ea;
       if (g.de64) g.de64[i] = de;
     }
-    WriteFeatures(rm, s.small->rank[mig], eh, g.in_pad, g.features + i * g.in_pad, lane);
+    WriteFeatures(rm, s.small->rank[mig], g.enc, g.in_pad, g.features + i * g.in_pad, lane);
     __syncwarp();
   }
   if (bad_all && lane == 0) atomicOr(g.status, static_cast<int>(bad_all));
 }
 
-// Features of lattice jumps, one thread per pair (alphabet size kEh known at
+// Features of lattice jumps, one thread per pair (channels per site kEh known at
 // compile time): the 58 MMM-ordered sites are gathered with independent loads
 // and the row of in_pad bf16 values (a multiple of 8, 16-byte aligned) is
 // written as 16-byte stores, 8 features at a time. Same values as the warp
@@ -983,12 +925,12 @@ __global__ void surrogate_dataset_kernel(DevTables t, SurrogateGen g) {
 template <int kEh>
 __global__ void __launch_bounds__(256) surrogate_features_thread_kernel(
     DevTables t, const int8_t *__restrict__ species, int n, const long long *__restrict__ pairs, int m, int in_pad,
-    __nv_bfloat16 *features, int *status) {
+    FeatEnc enc, __nv_bfloat16 *features, int *status) {
   __shared__ int8_t s_off[12 * kEnvSites * 4];
   __shared__ int8_t s_rank[8];
   __shared__ int8_t s_dir_of[27];
   StageArray(t.mmm_off, s_off, 12 * kEnvSites * 4);
-  if (threadIdx.x < 8) s_rank[threadIdx.x] = t.onehot_rank[threadIdx.x];
+  if (threadIdx.x < 8) s_rank[threadIdx.x] = static_cast<int8_t>(FeatChannel(enc, t.onehot_rank[threadIdx.x]));
   if (threadIdx.x < 27) s_dir_of[threadIdx.x] = t.dir_of[threadIdx.x];
   __syncthreads();
   const long long nsites = 4LL * n * n * n;
@@ -1048,17 +990,17 @@ __global__ void __launch_bounds__(256) surrogate_features_thread_kernel(
 // features [8 l, 8 l + 8) as one 16-byte store (rows of a multiple of 8 values,
 // 16-byte aligned; other layouts take the scalar writer).
 __global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict__ species, int n,
-                                          const long long *__restrict__ pairs, int m, int in_pad,
+                                          const long long *__restrict__ pairs, int m, int in_pad, FeatEnc enc,
                                           __nv_bfloat16 *features, int *status) {
   extern __shared__ __align__(16) unsigned char smem[];
-  SmallTables *sm = reinterpret_cast<SmallTables *>(smem);
-  int8_t *arr = reinterpret_cast<int8_t *>(sm + 1);
-  StageSmall(t, sm);
+  __shared__ int8_t s_ch[8];  // feature channel of each species code (-1: none)
+  int8_t *arr = reinterpret_cast<int8_t *>(smem);
+  if (threadIdx.x < 8) s_ch[threadIdx.x] = static_cast<int8_t>(FeatChannel(enc, t.onehot_rank[threadIdx.x]));
   __syncthreads();
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int8_t *rm = arr + warp * 64;  // [0, 58) environment ranks, [58] migrant rank, [59] padding (never matches)
-  const int eh = t.num_onehot;
+  int8_t *rm = arr + warp * 64;  // [0, 58) environment channels, [58] migrant channel, [59] padding (never matches)
+  const int eh = enc.width;
   const long long nsites = 4LL * n * n * n;
   const bool vec = (in_pad % 8) == 0 && (reinterpret_cast<uintptr_t>(features) & 15) == 0 && in_pad <= 256;
   // this lane's 8 features: (source slot in rm, one-hot rank)
@@ -1091,11 +1033,11 @@ __global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict_
     if (!bad) {
       for (int k = lane; k < kEnvSites; k += 32) {
         const int8_t *o = t.mmm_off + (di * kEnvSites + k) * 4;
-        rm[k] = sm->rank[species[NeighborId(hi, o[0], o[1], o[2], n)]];
+        rm[k] = s_ch[species[NeighborId(hi, o[0], o[1], o[2], n)]];
       }
-      if (lane == 0) rm[kEnvSites] = sm->rank[species[b]];
+      if (lane == 0) rm[kEnvSites] = s_ch[species[b]];
     } else {
-      for (int k = lane; k <= kEnvSites; k += 32) rm[k] = kMaxOnehot - 1;
+      for (int k = lane; k <= kEnvSites; k += 32) rm[k] = -1;
     }
     if (lane == 0) rm[kEnvSites + 1] = -1;
     bad_all |= bad;
@@ -1112,7 +1054,9 @@ __global__ void surrogate_features_kernel(DevTables t, const int8_t *__restrict_
         *reinterpret_cast<uint4 *>(row + 8 * lane) = make_uint4(w[0], w[1], w[2], w[3]);
       }
     } else {
-      WriteFeatures(rm, rm[kEnvSites], eh, in_pad, row, lane);
+      // rm already holds channels: write them through the identity encoding of this width
+      const FeatEnc id{0x0706050403020100ull, eh};
+      WriteFeatures(rm, rm[kEnvSites], id, in_pad, row, lane);
     }
     __syncwarp();
   }
@@ -3343,7 +3287,7 @@ cudaError_t LaunchBarrierBatchCounted(const DevTables &t, const int8_t *species,
 
 cudaError_t LaunchSurrogateDataset(const DevTables &t, const SurrogateGen &g, cudaStream_t stream) {
   if (g.count <= 0) return cudaSuccess;
-  if (g.in_pad < (kEnvSites + 1) * t.num_onehot) return cudaErrorInvalidValue;
+  if (g.enc.width < 1 || g.in_pad < (kEnvSites + 1) * g.enc.width) return cudaErrorInvalidValue;
   const size_t sm = JumpSmemBytes(t, kJumpWarps) + kJumpWarps * 144;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -3358,21 +3302,23 @@ cudaError_t LaunchSurrogateDataset(const DevTables &t, const SurrogateGen &g, cu
 }
 
 cudaError_t LaunchSurrogateFeatures(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
-                                    int in_pad, __nv_bfloat16 *features, int *status, cudaStream_t stream) {
+                                    int in_pad, const FeatEnc &enc, __nv_bfloat16 *features, int *status,
+                                    cudaStream_t stream) {
   if (m <= 0) return cudaSuccess;
-  if (in_pad < (kEnvSites + 1) * t.num_onehot) return cudaErrorInvalidValue;
+  if (enc.width < 1 || in_pad < (kEnvSites + 1) * enc.width) return cudaErrorInvalidValue;
   if (in_pad % 8 == 0 && (reinterpret_cast<uintptr_t>(features) & 15) == 0) {
     const int blocks = static_cast<int>((m + 255) / 256);
-    switch (t.num_onehot) {
-      case 2: surrogate_features_thread_kernel<2><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
-      case 3: surrogate_features_thread_kernel<3><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
-      case 4: surrogate_features_thread_kernel<4><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
-      case 5: surrogate_features_thread_kernel<5><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, features, status); return cudaGetLastError();
+    switch (enc.width) {
+      case 1: surrogate_features_thread_kernel<1><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, enc, features, status); return cudaGetLastError();
+      case 2: surrogate_features_thread_kernel<2><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, enc, features, status); return cudaGetLastError();
+      case 3: surrogate_features_thread_kernel<3><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, enc, features, status); return cudaGetLastError();
+      case 4: surrogate_features_thread_kernel<4><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, enc, features, status); return cudaGetLastError();
+      case 5: surrogate_features_thread_kernel<5><<<blocks, 256, 0, stream>>>(t, species, n, pairs, m, in_pad, enc, features, status); return cudaGetLastError();
       default: break;
     }
   }
-  const size_t sm = sizeof(SmallTables) + kJumpWarps * 64;
-  surrogate_features_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, in_pad,
+  const size_t sm = kJumpWarps * 64;
+  surrogate_features_kernel<<<Blocks(m, kJumpWarps), kJumpWarps * 32, sm, stream>>>(t, species, n, pairs, m, in_pad, enc,
                                                                                   features, status);
   return cudaGetLastError();
 }

@@ -170,13 +170,27 @@ cudaError_t LaunchKmc(const DevTables &t, int8_t *species, const KmcDevState &s,
 size_t KmcSharedBytes(const DevTables &t, const KmcLaunch &l);
 
 // Surrogate training data (see surrogate_dataset_kernel).
+// Feature encoding of the surrogate: each site's species becomes `width` channels, one of
+// them 1. One-hot: the channel is the one-hot rank (width E'). Solute channels: the base
+// species has no channel (its site is all zero) and the other ranks keep their order
+// (width E' - 1); a network's first-layer bias absorbs the base, so both encodings give
+// the same function class with E' - 1 / E' of the inputs.
+struct FeatEnc {
+  unsigned long long rank_ch;  // byte r: channel of one-hot rank r, 0xFF none
+  int width;                   // channels per site
+};
+__host__ __device__ __forceinline__ int FeatChannel(const FeatEnc &f, int rank) {
+  return static_cast<int>(static_cast<signed char>((f.rank_ch >> (8 * (rank & 7))) & 0xFFu));
+}
+
 struct SurrogateGen {
   unsigned long long seed;
   long long count;
   float solute_lo, solute_hi;  // per-sample solute fraction range
   int base_code;               // species filling the non-solute sites
   int kind;                    // 0 Quartic, 1 E0
-  int in_pad;                  // feature row length (>= 59 x one-hot alphabet)
+  int in_pad;                  // feature row length (>= 59 x enc.width)
+  FeatEnc enc;
   __nv_bfloat16 *features;     // [count][in_pad]
   float *ea;                   // [count]
   double *ea64, *de64;         // optional [count]
@@ -195,7 +209,8 @@ cudaError_t LaunchFallbackCompact(const long long *pairs, const float *mean, con
 cudaError_t LaunchFallbackMerge(const float *mean, int m, const double *fb_ea, const int *fb_index, const int *count,
                                 double *ea, cudaStream_t stream);
 cudaError_t LaunchSurrogateFeatures(const DevTables &t, const int8_t *species, int n, const long long *pairs, int m,
-                                    int in_pad, __nv_bfloat16 *features, int *status, cudaStream_t stream);
+                                    int in_pad, const FeatEnc &enc, __nv_bfloat16 *features, int *status,
+                                    cudaStream_t stream);
 // fn 0: ExpFast and exp; fn 1: RcpFast and 1 / x, over n device doubles.
 cudaError_t LaunchFastmathCheck(const DevTables &t, int fn, const double *x, long long n, double *fast, double *ref,
                                 cudaStream_t stream);

@@ -73,12 +73,17 @@ struct MlpDev {
   float *w1, *b1, *w2, *b2, *w3, *b3;
   __nv_bfloat16 *w1h, *w2h, *w2t;
   // W1 (bf16) and W2 (IEEE half: layer 2 of the tensor-core inference runs in
-  // f16) again, cut into 256-row x 32-K blocks stored contiguously in the tensor
+  // f16) again, cut into R-row x 32-K blocks stored contiguously in the tensor
   // cores' shared-memory operand layout (see mlp_tc.cu), so one bulk copy moves a
-  // block: member m, block c of W1 at (m * in / 32 + c) * 8192 elements, of W2 at
-  // (m * hidden / 32 + c) * 8192 elements.
+  // block. R = 256 for hidden 256 (member m, block c of W1 at (m * in / 32 + c) *
+  // 8192 elements, of W2 at (m * hidden / 32 + c) * 8192) and R = 128 for hidden 128
+  // (blocks of 4096 elements, same order).
   __nv_bfloat16 *w1_tiles;
   __half *w2_tiles;
+  // b2 and w3 in IEEE half (the fused jump kernel's packed layer-2 epilogue). For in = 128
+  // and hidden = 128 the last input column of w1_tiles holds b1 instead of W1's (unused)
+  // column 127: that kernel sets feature 127 to 1, so the layer-1 MMA adds the bias.
+  __half *b2h, *w3h;
 };
 
 // Activations of one batch (sizes for batch B, M members, H hidden).
@@ -104,13 +109,33 @@ cudaError_t MlpGather(const __nv_bfloat16 *x, const float *labels, const int *id
 cudaError_t MlpTranspose(const __nv_bfloat16 *in, int rows, int cols, __nv_bfloat16 *out, cudaStream_t s);
 cudaError_t MlpAdam(float *p, const float *grad, float *m1, float *m2, long long n, float lr, int step, cudaStream_t s);
 cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s);
-// Fused tcgen05 inference (mlp_tc.cu): hidden 256, in <= 256 and a multiple of 64.
+// Fused tcgen05 inference of feature rows (mlp_tc.cu): hidden 256, in <= 256 and a multiple of 64.
 bool MlpTcSupported(const MlpDev &d);
 size_t MlpTcSharedBytes(int in);
 cudaError_t MlpTcPredict(const MlpDev &d, const __nv_bfloat16 *x, long long n, float mean_label, float std_label,
                          float *mean, float *spread, int *status, cudaStream_t s);
 cudaError_t MlpEnsemble(const float *y, int batch, int members, float mean_label, float std_label, float *mean,
                         float *spread, cudaStream_t s);
+
+// Lattice jumps for the fused kernel (mlp_fused.cu), which gathers the solute-channel
+// features itself (two channels per site: one-hot alphabets of three species).
+struct FusedJumps {
+  const int8_t *species;     // the lattice (one replica), n^3 cells
+  int n;
+  const long long *pairs;    // [m][2] (vacancy site, migrant site)
+  long long m;
+  const int8_t *mmm_off;     // [12][58][4] MMM-ordered offsets per jump direction (half units)
+  const int8_t *dir_of;      // [27] 1NN direction of an offset, -1 none
+  uint32_t site_word[8];     // per species code: its two bf16 channels as one word (0 for the base species)
+  uint32_t fallback_codes;   // bit c: species code c in the environment sends the row to the plain predictor
+  float *mean, *spread;      // [m] ensemble mean (eV) and spread (+inf: plain predictor)
+  int *pair_status;          // kStatusBadSite / kStatusNotNeighbor of rejected pairs
+};
+// The fused kernel serves ensembles of 2 members, 128 inputs, hidden 128 (weights kept in
+// shared memory); an expired wait sets *status.
+bool MlpFusedSupported(const MlpDev &d);
+cudaError_t MlpFusedPredict(const MlpDev &d, const FusedJumps &j, float mean_label, float std_label, int *status,
+                            cudaStream_t s);
 
 }  // namespace lmc
 
@@ -119,5 +144,9 @@ struct lmc_mlp;
 namespace lmc {
 bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean_dev, float *spread_dev,
                      cudaStream_t stream);
+// The fused jump kernel queued on `stream` (status word as above); false when this network
+// or the inference path setting does not allow it.
+bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream);
+int MlpInputs(const lmc_mlp *mlp);
 const int *MlpStatusDev(const lmc_mlp *mlp);
 }  // namespace lmc

@@ -1,0 +1,432 @@
+// Fused surrogate barriers of lattice jumps for a compact ensemble whose weights
+// stay in shared memory: 2 members of 128 -> 128 -> 128 -> 1 (GELU) over the
+// solute-channel features (two channels per site, the base species all zero:
+// 59 sites x 2 = 118 inputs, padded to 128). One persistent CTA per SM loads
+// both members' weights once (128 KB, two bulk copies) and walks tiles of 128
+// jumps. Per tile:
+//   X  (smem, bf16)        the features, gathered from the lattice by the producer warps
+//   D1 (TMEM, fp32)        = X . W1[m]^T + b1[m]             tcgen05.mma kind::f16, M = N = 128
+//   H1 (smem, IEEE half)   = GELU(D1)                        epilogue warps, packed half
+//   D2 (TMEM, same columns)= H1 . W2[m]^T (half)             tcgen05.mma kind::f16
+//   y_m                    = GELU(D2 + b2[m]) . w3[m] + b3[m] packed half, FP32 sums of 8 terms
+// then the ensemble mean and spread. The layer-1 bias is the last input column: the
+// producer sets feature 127 (padding in the solute encoding) to 1 and the weight tiles
+// hold b1 there. A row whose pair is not a 1NN jump inside the lattice, or whose
+// environment holds a species without a one-hot slot (a second vacancy), gets
+// spread = +inf, so the caller's fallback sends it to the plain predictor.
+//
+// Warp roles (mbarriers only, no block-wide barrier inside the loop):
+//   warps 0-3   producer: thread r of the tile gathers row r (the pair's direction,
+//               its 58 MMM-ordered sites and the migrant: independent loads issued
+//               before the wait for the X buffer), then writes the row into the
+//               operand layout; warp 0 lane 0 also issues the weight copies;
+//   warp 4      lane 0 issues the MMAs and the tcgen05.commit arrivals; it
+//               issues tile t's layer-1 MMAs before tile t-1's layer-2 MMAs, so
+//               the tensor pipe works on the next tile while the epilogue
+//               finishes the current one;
+//   warps 5-20  epilogue: TMEM lane group = warp % 4, 32-column quarter =
+//               (warp - 5) / 4.
+// TMEM: 512 columns = 4 slots of 128 (tile parity x member); a slot holds D1 and
+// then D2 of the same tile and member (D2 is issued only after the epilogue has
+// read D1 and written H1).
+//
+// Operand layout in shared memory: K-major 8-row x 16-byte core matrices, 32-wide
+// K tiles of 128 rows (tcgen05.cuh). Every wait is bounded and polls a shared
+// abort flag: on expiry the kernel records kMlpFusedTimeout, drains its MMAs and
+// copies, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+#include "lattice_index.cuh"
+#include "mlp.cuh"
+#include "tcgen05.cuh"
+
+namespace lmc {
+namespace {
+
+using tc::Arrive;
+using tc::ArriveExpectTx;
+using tc::BarInit;
+using tc::BulkCopy;
+using tc::Commit;
+using tc::FenceAfterSync;
+using tc::FenceAsyncSmem;
+using tc::FenceBarrierInit;
+using tc::FenceBeforeSync;
+using tc::IdescBf16;
+using tc::Mma;
+using tc::OperandDesc;
+using tc::Smem;
+using tc::TmemAlloc;
+using tc::TmemFree;
+using tc::TmemLoad32;
+using tc::WaitDrain;
+using tc::WaitSleep;
+
+constexpr int kRows = 128;      // jumps per tile (MMA M)
+constexpr int kHid = 128;       // hidden width (MMA N of both layers)
+constexpr int kIn = 128;        // padded features (layer-1 K)
+constexpr int kMembers = 2;
+constexpr int kSites = kEnvSites + 1;  // 58 environment sites and the migrant
+constexpr int kTileBytes = kRows * 32 * 2;  // one 128 x 32 operand tile (8 KB)
+constexpr int kProdWarps = 4;
+constexpr int kMmaWarp = kProdWarps;
+constexpr int kFirstEpi = kProdWarps + 1;
+constexpr int kEpiWarps = 16;
+constexpr int kThreads = 32 * (kFirstEpi + kEpiWarps);
+constexpr uint32_t kCols = 512;
+constexpr int kFlagRing = 4;
+constexpr uint32_t kIdescL1 = IdescBf16(kRows, kHid);                                    // bf16 x bf16
+constexpr uint32_t kIdescL2 = (1u << 4) | ((kHid >> 3) << 17) | ((kRows >> 4) << 24);  // f16 x f16
+
+constexpr int kW1Bytes = kMembers * kHid * kIn * 2;
+constexpr int kW2Bytes = kMembers * kHid * kHid * 2;
+constexpr int kXBytes = kRows * kIn * 2;
+constexpr int kH1Bytes = kMembers * kRows * kHid * 2;
+
+struct FusedBars {
+  uint64_t w_full, x_full, x_empty;
+  uint64_t acc_full[4], acc_empty[4];  // TMEM slot (tile parity * 2 + member)
+  uint64_t h1_full[kMembers], h1_empty[kMembers];
+  uint64_t flag_full[kFlagRing];
+  uint64_t part_full, part_empty, done;
+  int abort;
+  uint32_t tmem;
+  uint32_t site_word[8];               // per species code: the row word of a site (two bf16 channels)
+  float partial[3][kRows];             // column quarters 1-3 of each row's output dot product
+  uint8_t flag[kFlagRing][kRows];      // per tile (ring): the row goes to the plain predictor
+};
+
+constexpr size_t kSmemBytes = static_cast<size_t>(kW1Bytes) + kW2Bytes + kXBytes + kH1Bytes + sizeof(FusedBars);
+static_assert(kSmemBytes <= 232448, "the fused kernel's shared memory exceeds 227 KB");
+static_assert(kSites <= 64, "a row holds 16 x 4 site words");
+
+// GELU of two values in packed half precision: u = z (c0 + c1 z^2), GELU = h + h tanh(u), h = z / 2.
+__device__ __forceinline__ __half2 GeluHalf2(__half2 z) {
+  const __half2 u = __hmul2(z, __hfma2(__hmul2(z, z), __float2half2_rn(0.0356774081363001f),
+                                       __float2half2_rn(0.7978845608028654f)));
+  uint32_t ub = *reinterpret_cast<const uint32_t *>(&u), tb;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(tb) : "r"(ub));
+  const __half2 t = *reinterpret_cast<const __half2 *>(&tb);
+  const __half2 h = __hmul2(z, __float2half2_rn(0.5f));
+  return __hfma2(h, t, h);
+}
+
+// Byte offset of row r, 16-byte chunk c (columns 8c .. 8c + 7) in a sequence of 32-wide operand tiles.
+__device__ __forceinline__ uint32_t ChunkOffset(int r, int c) {
+  return static_cast<uint32_t>((c >> 2) * kTileBytes + (r >> 3) * 512 + (c & 3) * 128 + (r & 7) * 16);
+}
+
+// Bounded wait by lane 0 (sleeping probes), its outcome broadcast to the warp.
+__device__ __forceinline__ bool WarpWait(uint64_t *bar, uint32_t parity, volatile int *abort, int lane) {
+  int ok = 1;
+  if (lane == 0) ok = WaitSleep(bar, parity, abort) ? 1 : 0;
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// Packed half GELU(z + b) . w over 32 columns, summed in FP32 per 8 columns.
+__device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, const __half *w) {
+  float acc = 0.f;
+#pragma unroll
+  for (int g8 = 0; g8 < 4; ++g8) {
+    const uint4 bb = __ldg(reinterpret_cast<const uint4 *>(b + g8 * 8));
+    const uint4 ww = __ldg(reinterpret_cast<const uint4 *>(w + g8 * 8));
+    const uint32_t bw[4] = {bb.x, bb.y, bb.z, bb.w}, wv[4] = {ww.x, ww.y, ww.z, ww.w};
+    __half2 s2 = __float2half2_rn(0.f);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __half2 z = __hadd2(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]),
+                                *reinterpret_cast<const __half2 *>(&bw[e]));
+      s2 = __hfma2(GeluHalf2(z), *reinterpret_cast<const __half2 *>(&wv[e]), s2);
+    }
+    const float2 f = __half22float2(s2);
+    acc += f.x + f.y;
+  }
+  return acc;
+}
+
+}  // namespace
+
+constexpr int kMlpFusedTimeout = 1;
+
+__global__ void __launch_bounds__(kThreads, 1)
+    mlp_fused_jump_kernel(const __grid_constant__ MlpDev d, const __grid_constant__ FusedJumps j, float mean_label,
+                          float std_label, int *status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char *sw1 = smem, *sw2 = sw1 + kW1Bytes, *sx = sw2 + kW2Bytes, *sh = sx + kXBytes;
+  FusedBars *bars = reinterpret_cast<FusedBars *>(sh + kH1Bytes);
+  volatile int *abort = &bars->abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    BarInit(&bars->w_full, 1);
+    BarInit(&bars->x_full, kProdWarps);
+    BarInit(&bars->x_empty, 1);
+    for (int i = 0; i < 4; ++i) {
+      BarInit(&bars->acc_full[i], 1);
+      BarInit(&bars->acc_empty[i], kEpiWarps);
+    }
+    for (int m = 0; m < kMembers; ++m) {
+      BarInit(&bars->h1_full[m], kEpiWarps);
+      BarInit(&bars->h1_empty[m], 1);
+    }
+    for (int i = 0; i < kFlagRing; ++i) BarInit(&bars->flag_full[i], kProdWarps);
+    BarInit(&bars->part_full, 3 * 4);
+    BarInit(&bars->part_empty, 4);
+    BarInit(&bars->done, 1);
+    bars->abort = 0;
+    FenceBarrierInit();
+  }
+  if (tid < 8) bars->site_word[tid] = j.site_word[tid];
+  if (warp == kMmaWarp) TmemAlloc(&bars->tmem, kCols);
+  FenceBeforeSync();
+  __syncthreads();
+  FenceAfterSync();
+  const uint32_t tmem = bars->tmem;
+  const long long tiles = (j.m + kRows - 1) / kRows;
+
+  if (warp < kProdWarps) {
+    // ---- producer: weights once, then one row per thread and tile ----
+    if (warp == 0 && lane == 0) {
+      ArriveExpectTx(&bars->w_full, kW1Bytes + kW2Bytes);
+      BulkCopy(sw1, d.w1_tiles, kW1Bytes, &bars->w_full);
+      BulkCopy(sw2, d.w2_tiles, kW2Bytes, &bars->w_full);
+    }
+    const int r = warp * 32 + lane;
+    const int n = j.n;
+    const long long nsites = 4LL * n * n * n;
+    unsigned bad_all = 0;
+    int t_local = 0;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
+      const long long row = tile * kRows + r;
+      int code[kSites];
+      bool fallback = true;
+      if (row < j.m) {
+        const long long a = __ldg(&j.pairs[2 * row]), b = __ldg(&j.pairs[2 * row + 1]);
+        unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
+        int di = -1;
+        H3 hi{0, 0, 0};
+        if (!bad) {
+          hi = SiteCoord(a, n);
+          const H3 hj = SiteCoord(b, n);
+          const int dx = WrapDelta(hj.x - hi.x, n), dy = WrapDelta(hj.y - hi.y, n), dz = WrapDelta(hj.z - hi.z, n);
+          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
+            di = __ldg(&j.dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
+          if (di < 0) bad = kStatusNotNeighbor;
+        }
+        bad_all |= bad;
+        if (!bad) {
+          // the 58 offsets of this direction, 4 bytes (dx, dy, dz, 0) each (|offset| <= 4)
+          const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
+          const int m2 = 2 * n;
+          if (hi.x >= 4 && hi.x < m2 - 4 && hi.y >= 4 && hi.y < m2 - 4 && hi.z >= 4 && hi.z < m2 - 4) {
+            // no wrap: id(h + o) = id(h) + dx 2n^2 + dy n + floor((hz % 2 + dz) / 2)
+            const unsigned base = static_cast<unsigned>(a), plane = 2u * static_cast<unsigned>(n) * n;
+            const int p = hi.z & 1;
+#pragma unroll
+            for (int k = 0; k < kEnvSites; ++k) {
+              const int o = __ldg(off + k);
+              const int dx = static_cast<int8_t>(o), dy = static_cast<int8_t>(o >> 8), dz = static_cast<int8_t>(o >> 16);
+              const unsigned id = base + static_cast<unsigned>(dx) * plane + static_cast<unsigned>(dy * n) +
+                                  static_cast<unsigned>((p + dz) >> 1);
+              code[k] = __ldg(&j.species[id]);
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < kEnvSites; ++k) {
+              const int o = __ldg(off + k);
+              code[k] = __ldg(&j.species[NeighborId(hi, static_cast<int8_t>(o), static_cast<int8_t>(o >> 8),
+                                                    static_cast<int8_t>(o >> 16), n)]);
+            }
+          }
+          code[kEnvSites] = __ldg(&j.species[b]);
+          unsigned seen = 0;
+#pragma unroll
+          for (int k = 0; k < kSites; ++k) seen |= 1u << (code[k] & 7);
+          fallback = (seen & j.fallback_codes) != 0;
+        }
+      }
+      if (fallback) {
+#pragma unroll
+        for (int k = 0; k < kSites; ++k) code[k] = -1;
+      }
+      // the X buffer is free once the previous tile's layer-1 MMAs have completed
+      if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
+#pragma unroll
+      for (int c = 0; c < kIn / 8; ++c) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int s = 4 * c + e;  // word s holds features 2s, 2s + 1
+          w[e] = (s < kSites && code[s] >= 0) ? bars->site_word[code[s] & 7] : 0u;
+          if (s == kIn / 2 - 1) w[e] |= 0x3F800000u;  // feature 127 = 1: the bias column
+        }
+        *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+      bars->flag[t_local % kFlagRing][r] = fallback ? 1 : 0;
+      FenceAsyncSmem();
+      __syncwarp();
+      if (lane == 0) {
+        Arrive(&bars->x_full);
+        Arrive(&bars->flag_full[t_local % kFlagRing]);
+      }
+    }
+    if (bad_all) atomicOr(j.pair_status, static_cast<int>(bad_all));
+    // the weight copies must land before the CTA exits
+    if (warp == 0 && lane == 0 && !WaitDrain(&bars->w_full, 0)) *abort = 1;
+  } else if (warp == kMmaWarp) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      const uint32_t a1 = Smem(sx), b1 = Smem(sw1), a2 = Smem(sh), b2 = Smem(sw2);
+      // layer 2 of tile tp (both members), once the epilogue has written its H1
+      const auto layer2 = [&](int tp) -> bool {
+        for (int m = 0; m < kMembers; ++m) {
+          if (!WaitSleep(&bars->h1_full[m], tp & 1, abort)) return false;
+          FenceAfterSync();
+          const int slot = (tp & 1) * 2 + m;
+          const uint32_t dcol = tmem + slot * kHid;
+          for (int c = 0; c < kHid / 32; ++c) {
+            const uint32_t a = a2 + m * (kRows * kHid * 2) + c * kTileBytes, b = b2 + (m * (kHid / 32) + c) * kTileBytes;
+            Mma(dcol, OperandDesc(a), OperandDesc(b), kIdescL2, c > 0);
+            Mma(dcol, OperandDesc(a + 256), OperandDesc(b + 256), kIdescL2, true);
+          }
+          Commit(&bars->acc_full[slot]);
+          Commit(&bars->h1_empty[m]);
+        }
+        return true;
+      };
+      bool ok = WaitSleep(&bars->w_full, 0, abort);
+      int t_local = 0;
+      for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t_local) {
+        if (!(ok = WaitSleep(&bars->x_full, t_local & 1, abort))) break;
+        FenceAfterSync();
+        for (int m = 0; m < kMembers && ok; ++m) {
+          const int slot = (t_local & 1) * 2 + m;
+          if (t_local >= 2 && !(ok = WaitSleep(&bars->acc_empty[slot], ((t_local >> 1) - 1) & 1, abort))) break;
+          FenceAfterSync();
+          const uint32_t dcol = tmem + slot * kHid;
+          for (int c = 0; c < kIn / 32; ++c) {
+            const uint32_t a = a1 + c * kTileBytes, b = b1 + (m * (kIn / 32) + c) * kTileBytes;
+            Mma(dcol, OperandDesc(a), OperandDesc(b), kIdescL1, c > 0);
+            Mma(dcol, OperandDesc(a + 256), OperandDesc(b + 256), kIdescL1, true);
+          }
+          Commit(&bars->acc_full[slot]);
+        }
+        if (!ok) break;
+        Commit(&bars->x_empty);
+        if (t_local >= 1) ok = layer2(t_local - 1);
+      }
+      if (ok && t_local >= 1) layer2(t_local - 1);
+      // drain: `done` completes once every MMA issued so far has finished
+      Commit(&bars->done);
+      if (!WaitDrain(&bars->done, 0)) *abort = 1;
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue warps ----
+    const int ew = warp - kFirstEpi, q = ew >> 2, lg = warp & 3;
+    const int r = lg * 32 + lane;
+    const uint32_t lane_base = static_cast<uint32_t>(lg * 32) << 16;
+    bool ok = true;
+    int t_local = 0;
+    for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t_local) {
+      const long long row = tile * kRows + r;
+      const int par = t_local & 1;
+      bool fallback = false;
+      if (q == 0) {
+        if (!(ok = WarpWait(&bars->flag_full[t_local % kFlagRing], (t_local / kFlagRing) & 1, abort, lane))) break;
+        fallback = bars->flag[t_local % kFlagRing][r] != 0;
+      }
+      // H1 = GELU(D1) (D1 includes b1): this thread's row, its 32 columns (K tile q of H1)
+      for (int m = 0; m < kMembers && ok; ++m) {
+        const int slot = par * 2 + m;
+        if (!(ok = WarpWait(&bars->acc_full[slot], 0, abort, lane))) break;
+        if (t_local >= 1 && !(ok = WarpWait(&bars->h1_empty[m], (t_local - 1) & 1, abort, lane))) break;
+        FenceAfterSync();
+        float v[32];
+        TmemLoad32(tmem + lane_base + slot * kHid + q * 32, v);
+        unsigned char *hrow = sh + m * (kRows * kHid * 2);
+#pragma unroll
+        for (int g8 = 0; g8 < 4; ++g8) {
+          uint32_t packed[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const __half2 p = GeluHalf2(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]));
+            packed[e] = *reinterpret_cast<const uint32_t *>(&p);
+          }
+          *reinterpret_cast<uint4 *>(hrow + ChunkOffset(r, q * 4 + g8)) =
+              make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        }
+        FenceBeforeSync();
+        FenceAsyncSmem();
+        __syncwarp();
+        if (lane == 0) Arrive(&bars->h1_full[m]);
+      }
+      // y_m = GELU(D2 + b2) . w3 + b3
+      float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
+      for (int m = 0; m < kMembers && ok; ++m) {
+        const int slot = par * 2 + m;
+        if (!(ok = WarpWait(&bars->acc_full[slot], 1, abort, lane))) break;
+        FenceAfterSync();
+        float v[32];
+        TmemLoad32(tmem + lane_base + slot * kHid + q * 32, v);
+        const float acc = GeluDotHalf(v, d.b2h + m * kHid + q * 32, d.w3h + m * kHid + q * 32);
+        FenceBeforeSync();
+        __syncwarp();
+        if (lane == 0) Arrive(&bars->acc_empty[slot]);
+        // the four column quarters of a row meet in shared memory
+        const int u = 2 * t_local + m;
+        if (q != 0) {
+          if (u >= 1 && !(ok = WarpWait(&bars->part_empty, (u - 1) & 1, abort, lane))) break;
+          bars->partial[q - 1][r] = acc;
+          __syncwarp();
+          if (lane == 0) Arrive(&bars->part_full);
+        } else {
+          if (!(ok = WarpWait(&bars->part_full, u & 1, abort, lane))) break;
+          const float y = acc + (bars->partial[0][r] + bars->partial[1][r] + bars->partial[2][r]) + __ldg(&d.b3[m]);
+          __syncwarp();
+          if (lane == 0) Arrive(&bars->part_empty);
+          ysum += y;
+          ymin = fminf(ymin, y);
+          ymax = fmaxf(ymax, y);
+        }
+      }
+      if (ok && q == 0 && row < j.m) {
+        j.mean[row] = mean_label + std_label * ysum * (1.0f / kMembers);
+        j.spread[row] = fallback ? __int_as_float(0x7f800000) : std_label * (ymax - ymin);
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && bars->abort) atomicOr(status, kMlpFusedTimeout);
+  FenceBeforeSync();
+  __syncthreads();
+  if (warp == kMmaWarp) TmemFree(tmem, kCols);
+}
+
+bool MlpFusedSupported(const MlpDev &d) {
+  return d.in == kIn && d.hidden == kHid && d.members == kMembers && d.w1_tiles != nullptr && d.w2_tiles != nullptr &&
+         d.b2h != nullptr && d.w3h != nullptr;
+}
+
+cudaError_t MlpFusedPredict(const MlpDev &d, const FusedJumps &j, float mean_label, float std_label, int *status,
+                            cudaStream_t s) {
+  if (!MlpFusedSupported(d)) return cudaErrorInvalidValue;
+  if (j.m <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (j.m + kRows - 1) / kRows;
+  const int grid = static_cast<int>(tiles < sms ? tiles : sms);
+  cudaError_t err = cudaFuncSetAttribute(mlp_fused_jump_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kSmemBytes));
+  if (err != cudaSuccess) return err;
+  mlp_fused_jump_kernel<<<grid, kThreads, kSmemBytes, s>>>(d, j, mean_label, std_label, status);
+  return cudaGetLastError();
+}
+
+}  // namespace lmc

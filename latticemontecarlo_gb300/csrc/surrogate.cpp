@@ -116,6 +116,14 @@ bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean
             "tcgen05 inference");
   return true;
 }
+bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream) {
+  if (mlp->path == 2 || !lmc::MlpFusedSupported(mlp->d)) return false;
+  CudaCheck(cudaMemsetAsync(mlp->status, 0, sizeof(int), stream), "memset");
+  CudaCheck(lmc::MlpFusedPredict(mlp->d, j, mlp->label_mean, mlp->label_std, mlp->status, stream),
+            "fused surrogate kernel");
+  return true;
+}
+int MlpInputs(const lmc_mlp *mlp) { return mlp->d.in; }
 const int *MlpStatusDev(const lmc_mlp *mlp) { return mlp->status; }
 
 }  // namespace lmc
@@ -163,6 +171,8 @@ int lmc_mlp_create(int device, int in_features, int hidden, int members, uint64_
     m->d.w2t = DevAlloc<__nv_bfloat16>(M * H * H, &m->owned);
     m->d.w1_tiles = DevAlloc<__nv_bfloat16>(M * H * in_features, &m->owned);
     m->d.w2_tiles = DevAlloc<__half>(M * H * H, &m->owned);
+    m->d.b2h = DevAlloc<__half>(M * H, &m->owned);
+    m->d.w3h = DevAlloc<__half>(M * H, &m->owned);
     // He initialisation (normal, std sqrt(2 / fan_in)), zero biases
     std::vector<float> p(m->num_params, 0.f);
     std::mt19937_64 gen(seed);
@@ -313,8 +323,8 @@ int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path) {
   return Guard([&] {
     Require(mlp != nullptr, LMC_ERR_INVALID_ARGUMENT, "mlp is null");
     Require(path >= 0 && path <= 2, LMC_ERR_INVALID_ARGUMENT, "path must be 0, 1 or 2");
-    Require(path != 1 || lmc::MlpTcSupported(mlp->d), LMC_ERR_UNSUPPORTED,
-            "the tcgen05 path needs hidden = 256 and in_features <= 256");
+    Require(path != 1 || lmc::MlpTcSupported(mlp->d) || lmc::MlpFusedSupported(mlp->d), LMC_ERR_UNSUPPORTED,
+            "the tcgen05 kernels serve hidden 256 with in_features <= 256, or 2 members of 128 -> 128");
     mlp->path = path;
   });
 }

@@ -82,6 +82,37 @@ __device__ __forceinline__ bool Wait(uint64_t *bar, uint32_t parity, volatile in
   *abort = 1;
   return false;
 }
+// try_wait with a suspend-time hint (ns): the thread sleeps until the phase completes or
+// the hint expires, so waiting warps take few issue slots.
+__device__ __forceinline__ bool TryWaitSleep(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(Smem(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t GlobalTimerNs() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+// Wait as above with sleeping probes, bounded by kWaitLimitNs of wall time.
+__device__ __forceinline__ bool WaitSleep(uint64_t *bar, uint32_t parity, volatile int *abort) {
+  if (TryWaitSleep(bar, parity, 1000)) return true;
+  const uint64_t t0 = GlobalTimerNs();
+  for (;;) {
+    if (TryWaitSleep(bar, parity, 20000)) return true;
+    if (*abort) return false;
+    if (GlobalTimerNs() - t0 > kWaitLimitNs) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
 // Bounded wait that ignores the abort flag (draining work already issued).
 __device__ __forceinline__ bool WaitDrain(uint64_t *bar, uint32_t parity) {
   for (long long it = 0; it < kWaitLimit; ++it)

@@ -1,0 +1,152 @@
+"""Solute-channel features and the fused jump kernel of the barrier surrogate:
+
+* lattice-jump features in the solute encoding (both writers) against the
+  encoding built on the host from the reference-pinned MMM site order;
+* the training data in the solute encoding against the one-hot data of the
+  same seed (same environments, same labels);
+* the fused kernel (features gathered inside, weights in shared memory, tcgen05)
+  against the unfused path (feature rows, then the mma.sync GEMMs) and the
+  float64 network, over several tiles per CTA, with the rows it hands to the
+  plain predictor (a second vacancy in the environment) and a rejected pair."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EL = ("Al", "Mg", "Zn")
+
+
+def _pair_sites(N, n, a, b):
+    st, mmm, mm2 = np.zeros(60, np.int64), np.zeros(58, np.int64), np.zeros(58, np.int64)
+    N.check(N.lib.lmc_geom_pair_lists(n, int(a), int(b), st.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      mmm.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      mm2.ctypes.data_as(C.POINTER(C.c_int64))))
+    return list(mmm) + [int(b)]
+
+
+def _jumps_of(N, n, sites):
+    pairs = []
+    for v in sites:
+        nb = np.zeros(42, np.int64)
+        N.check(N.lib.lmc_geom_neighbors(n, int(v), nb.ctypes.data_as(C.POINTER(C.c_int64))))
+        pairs += [(int(v), int(j)) for j in nb[:12]]
+    return np.array(pairs, np.int64)
+
+
+def _solute_row(sp, sites, alpha, pad):
+    """Solute channels of one jump: per site, channel 0 for Mg, 1 for Zn, Al (base) and X all zero."""
+    ch = {alpha.index("Mg"): 0, alpha.index("Zn"): 1}
+    row = np.zeros(pad, np.uint16)
+    for k, s in enumerate(sites):
+        c = int(sp[s])
+        if c in ch:
+            row[2 * k + ch[c]] = 0x3F80  # bf16 1.0
+    return row
+
+
+@pytest.mark.parametrize("pad", [128, 122])
+def test_solute_features_match_host_lists(native, pad):
+    torch = pytest.importorskip("torch")
+    from latticemontecarlo_gb300 import api, synthetic as S
+    N = native
+    n = 9
+    sp = S.make_lattice(n, {"Al": 0.5, "Mg": 0.25, "Zn": 0.25}, 5, 8, EL)
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 3), list(EL)))
+    ctx.set_lattices([n], sp)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
+    assert api.surrogate_feature_count(ctx) == 128
+    alpha = S.alphabet(EL)
+    rng = np.random.default_rng(2)
+    pairs = _jumps_of(N, n, rng.integers(0, sp.size, 25))
+    got = api.surrogate_features(ctx, torch.from_numpy(pairs).cuda(), pad)
+    got = got.contiguous().view(torch.int16).cpu().numpy().view(np.uint16)
+    for i, (a, b) in enumerate(pairs):
+        assert np.array_equal(got[i], _solute_row(sp, _pair_sites(N, n, a, b), alpha, pad)), i
+
+
+def test_solute_dataset_is_the_onehot_dataset(native):
+    """Same seed, same environments and labels; the solute rows are the one-hot rows without
+    the base (Al) channel."""
+    pytest.importorskip("torch")
+    from latticemontecarlo_gb300 import api, synthetic as S
+    N = native
+    n = 10
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 7), list(EL)))
+    ctx.set_lattices([n], S.make_lattice(n, {"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, 1, 3, EL))
+    x1, ea1, e64_1, _ = api.surrogate_dataset(ctx, 17, 4096, 0.0, 0.5, 192)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
+    x2, ea2, e64_2, _ = api.surrogate_dataset(ctx, 17, 4096, 0.0, 0.5, 128)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_ONEHOT)
+    assert np.array_equal(e64_1.cpu().numpy(), e64_2.cpu().numpy())
+    oh = x1.float().cpu().numpy()[:, :177].reshape(-1, 59, 3)   # ranks Al, Mg, Zn
+    so = x2.float().cpu().numpy()
+    assert np.array_equal(so[:, :118].reshape(-1, 59, 2), oh[:, :, 1:])
+    assert not so[:, 118:].any()
+
+
+@pytest.fixture(scope="module")
+def trained(native):
+    """A compact ensemble (2 members, 128 -> 128 -> 128) trained briefly on solute features."""
+    torch = pytest.importorskip("torch")
+    from latticemontecarlo_gb300 import api, synthetic as S
+    N = native
+    n = 12
+    el_frac = {"Al": 0.7, "Mg": 0.15, "Zn": 0.15}
+    sp = S.make_lattice(n, el_frac, 9, 0, EL)
+    alpha = S.alphabet(EL)
+    x_code = alpha.index("X")
+    rng = np.random.default_rng(4)
+    vac = rng.choice(sp.size, 40, replace=False)
+    sp[vac] = x_code
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 1234), list(EL)))
+    ctx.set_lattices([n], sp)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
+    x, ea, _, _ = api.surrogate_dataset(ctx, 1, 1 << 17, 0.1, 0.4, 128)
+    net = api.Surrogate(128, 128, 2, seed=3)
+    net.set_label_scale(float(ea.mean()), float(ea.std()))
+    net.train(x, ea, batch=4096, epochs=3, lr=2e-3, seed=4)
+    return torch, api, N, ctx, net, sp, n, vac, alpha
+
+
+def test_fused_kernel_matches_unfused_and_float64(trained):
+    torch, api, N, ctx, net, sp, n, vac, alpha = trained
+    from oracle import mlp as R
+    pairs = _jumps_of(N, n, vac)                      # 480 jumps, several with a second vacancy nearby
+    x_code = alpha.index("X")
+    has_x = np.array([any(int(sp[s]) == x_code for s in _pair_sites(N, n, a, b)) for a, b in pairs])
+    assert has_x.any() and not has_x.all()
+    reps = 100                                        # 48 000 rows: several tiles per CTA, a partial last tile
+    pd = torch.from_numpy(np.tile(pairs, (reps, 1))).cuda()
+    net.set_inference_path(0)
+    m_f, s_f = api.surrogate_predict(ctx, net, pd)
+    net.set_inference_path(2)
+    m_r, s_r = api.surrogate_predict(ctx, net, pd)
+    net.set_inference_path(0)
+    m_f, s_f, m_r, s_r = (t.double().cpu().numpy() for t in (m_f, s_f, m_r, s_r))
+    flag = np.tile(has_x, reps)
+    assert np.all(np.isinf(s_f[flag])) and np.all(np.isfinite(s_f[~flag]))
+    assert np.all(np.isfinite(m_f))
+    np.testing.assert_allclose(m_f[~flag], m_r[~flag], rtol=0, atol=2e-3)
+    np.testing.assert_allclose(s_f[~flag], s_r[~flag], rtol=0, atol=3e-3)
+    # every repetition of a jump gives the same bits
+    assert np.array_equal(m_f.reshape(reps, -1), np.broadcast_to(m_f[:len(pairs)], (reps, len(pairs))))
+    # the float64 network on the same feature rows
+    xs = api.surrogate_features(ctx, pd[:len(pairs)], 128)
+    bits = xs.contiguous().view(torch.int16).cpu().numpy().view(np.uint16)
+    y = R.predict(net.params(), R.bf16_bits_to_float(bits), 128, 128, 2)
+    mu, sd = (float(np.float32(v)) for v in net.label_scale)
+    ok = ~has_x
+    np.testing.assert_allclose(m_f[:len(pairs)][ok], (mu + sd * y.mean(0))[ok], rtol=0, atol=3e-3)
+
+
+def test_fused_kernel_rejects_non_jumps(trained):
+    torch, api, N, ctx, net, sp, n, vac, alpha = trained
+    bad = torch.tensor([[0, 5]], dtype=torch.int64, device="cuda")
+    with pytest.raises(N.LmcError):
+        api.surrogate_predict(ctx, net, bad)
+    # the context stays usable
+    pd = torch.from_numpy(_jumps_of(N, n, vac[:2])).cuda()
+    m, s = api.surrogate_predict(ctx, net, pd)
+    assert torch.isfinite(m).all()
