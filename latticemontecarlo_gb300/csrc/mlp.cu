@@ -295,28 +295,28 @@ template <>
 __device__ __forceinline__ __half FromFloat<__half>(float v) { return __float2half_rn(v); }
 
 template <typename T>
-__global__ void tile_weights_kernel(const float *w, long long rows, int k, int block_rows, T *out) {
+__global__ void tile_weights_kernel(const float *w, long long rows, int k, int block_rows, float scale, T *out) {
   const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= rows * k) return;
   const long long r = i / k;
   const int kk = static_cast<int>(i % k);
   const long long block = (r / block_rows) * (k / 32) + kk / 32;
   const int rr = static_cast<int>(r % block_rows), kc = kk % 32;
-  out[block * block_rows * 32 + (rr >> 3) * 256 + (kc >> 3) * 64 + (rr & 7) * 8 + (kc & 7)] = FromFloat<T>(w[i]);
+  out[block * block_rows * 32 + (rr >> 3) * 256 + (kc >> 3) * 64 + (rr & 7) * 8 + (kc & 7)] = FromFloat<T>(scale * w[i]);
 }
 
-// Half copies of b2 and w3; for in = hidden = 128, b1 into the last input column of the W1
-// tiles (row r = m * 128 + h: block m * 4 + 3, column 31 of the block).
+// Half copies of `scale` b2 and of w3; for in = hidden = 128, `scale` b1 into the last input
+// column of the W1 tiles (row r = m * 128 + h: block m * 4 + 3, column 31 of the block).
 __global__ void fused_extras_kernel(const float *b1, const float *b2, const float *w3, int n, bool bias_col,
-                                    __half *b2h, __half *w3h, __nv_bfloat16 *w1_tiles) {
+                                    float scale, __half *b2h, __half *w3h, __nv_bfloat16 *w1_tiles) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  b2h[i] = __float2half_rn(b2[i]);
+  b2h[i] = __float2half_rn(scale * b2[i]);
   w3h[i] = __float2half_rn(w3[i]);
   if (bias_col) {
     const int m = i / 128, h = i % 128;
     w1_tiles[static_cast<long long>(m * 4 + 3) * 4096 + (h >> 3) * 256 + 3 * 64 + (h & 7) * 8 + 7] =
-        __float2bfloat16(b1[i]);
+        __float2bfloat16(scale * b1[i]);
   }
 }
 
@@ -495,17 +495,20 @@ cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s) {
   const long long n = n1 > n2 ? n1 : n2;
   cast_weights_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, s>>>(d.w1, n1, d.w2, d.members, d.hidden, d.w1h,
                                                                         d.w2h, d.w2t);
+  // hidden 128 with 128 inputs: the fused jump kernel's tiles, W1, b1, W2 and b2 halved (exact)
+  const bool fused_shape = d.in == 128 && d.hidden == 128;
+  const float scale = fused_shape ? 0.5f : 1.0f;
   if (d.w1_tiles && (d.hidden % 256 == 0 || d.hidden == 128) && d.in % 32 == 0) {
     const int block_rows = d.hidden == 128 ? 128 : 256;
     tile_weights_kernel<__nv_bfloat16><<<static_cast<int>((n1 + 255) / 256), 256, 0, s>>>(
-        d.w1, static_cast<long long>(d.members) * d.hidden, d.in, block_rows, d.w1_tiles);
+        d.w1, static_cast<long long>(d.members) * d.hidden, d.in, block_rows, scale, d.w1_tiles);
     tile_weights_kernel<__half><<<static_cast<int>((n2 + 255) / 256), 256, 0, s>>>(
-        d.w2, static_cast<long long>(d.members) * d.hidden, d.hidden, block_rows, d.w2_tiles);
+        d.w2, static_cast<long long>(d.members) * d.hidden, d.hidden, block_rows, scale, d.w2_tiles);
   }
   if (d.b2h && d.w3h) {
     const int nh = d.members * d.hidden;
-    const bool bias_col = d.w1_tiles && d.in == 128 && d.hidden == 128;
-    fused_extras_kernel<<<(nh + 255) / 256, 256, 0, s>>>(d.b1, d.b2, d.w3, nh, bias_col, d.b2h, d.w3h, d.w1_tiles);
+    fused_extras_kernel<<<(nh + 255) / 256, 256, 0, s>>>(d.b1, d.b2, d.w3, nh, fused_shape && d.w1_tiles, scale,
+                                                         d.b2h, d.w3h, d.w1_tiles);
   }
   return cudaGetLastError();
 }

@@ -81,8 +81,9 @@ struct MlpDev {
   __nv_bfloat16 *w1_tiles;
   __half *w2_tiles;
   // b2 and w3 in IEEE half (the fused jump kernel's packed layer-2 epilogue). For in = 128
-  // and hidden = 128 the last input column of w1_tiles holds b1 instead of W1's (unused)
-  // column 127: that kernel sets feature 127 to 1, so the layer-1 MMA adds the bias.
+  // and hidden = 128 (that kernel's shape) the tiles and b2h hold W1, W2 and b2 halved, and
+  // the last input column of w1_tiles holds b1 / 2 instead of W1's (unused) column 127: the
+  // kernel sets feature 127 to 1, so the layer-1 MMA adds the bias.
   __half *b2h, *w3h;
 };
 

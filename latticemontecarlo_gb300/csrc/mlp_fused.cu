@@ -5,27 +5,31 @@
 // both members' weights once (128 KB, two bulk copies) and walks tiles of 128
 // jumps. Per tile:
 //   X  (smem, bf16)        the features, gathered from the lattice by the producer warps
-//   D1 (TMEM, fp32)        = X . W1[m]^T + b1[m]             tcgen05.mma kind::f16, M = N = 128
-//   H1 (smem, IEEE half)   = GELU(D1)                        epilogue warps, packed half
-//   D2 (TMEM, same columns)= H1 . W2[m]^T (half)             tcgen05.mma kind::f16
-//   y_m                    = GELU(D2 + b2[m]) . w3[m] + b3[m] packed half, FP32 sums of 8 terms
+//   D1 (TMEM, fp32)        = (X . W1[m]^T + b1[m]) / 2       tcgen05.mma kind::f16, M = N = 128
+//   H1 (smem, IEEE half)   = GELU(2 D1)                      epilogue warps, packed half
+//   D2 (TMEM, same columns)= H1 . W2[m]^T / 2 (half)         tcgen05.mma kind::f16
+//   y_m                    = GELU(2 (D2 + b2[m] / 2)) . w3[m] + b3[m]   packed half, FP32 sums of 8 terms
 // then the ensemble mean and spread. The layer-1 bias is the last input column: the
 // producer sets feature 127 (padding in the solute encoding) to 1 and the weight tiles
-// hold b1 there. A row whose pair is not a 1NN jump inside the lattice, or whose
+// hold b1 there. W1, b1, W2 and b2 are stored halved (exact in binary floating point), so
+// the MMAs produce h = z / 2 and GELU(z) = h + h tanh(h (2 c0 + 8 c1 h^2)) takes one
+// multiply less. A row whose pair is not a 1NN jump inside the lattice, or whose
 // environment holds a species without a one-hot slot (a second vacancy), gets
 // spread = +inf, so the caller's fallback sends it to the plain predictor.
 //
 // Warp roles (mbarriers only, no block-wide barrier inside the loop):
-//   warps 0-3   producer: thread r of the tile gathers row r (the pair's direction,
-//               its 58 MMM-ordered sites and the migrant: independent loads issued
-//               before the wait for the X buffer), then writes the row into the
-//               operand layout; warp 0 lane 0 also issues the weight copies;
-//   warp 4      lane 0 issues the MMAs and the tcgen05.commit arrivals; it
+//   warps 0-7   producer: row r of the tile is gathered by threads r of warps 0-3
+//               (sites 0-31 of the row: its direction and 32 MMM-ordered sites) and
+//               of warps 4-7 (sites 32-58, the migrant being site 58), with
+//               independent loads issued before the wait for the X buffer; each
+//               writes its half of the row into the operand layout; warp 0 lane 0
+//               also issues the weight copies;
+//   warp 8      lane 0 issues the MMAs and the tcgen05.commit arrivals; it
 //               issues tile t's layer-1 MMAs before tile t-1's layer-2 MMAs, so
 //               the tensor pipe works on the next tile while the epilogue
 //               finishes the current one;
-//   warps 5-20  epilogue: TMEM lane group = warp % 4, 32-column quarter =
-//               (warp - 5) / 4.
+//   warps 9-24  epilogue: TMEM lane group = warp % 4, 32-column quarter =
+//               (warp - 9) / 4.
 // TMEM: 512 columns = 4 slots of 128 (tile parity x member); a slot holds D1 and
 // then D2 of the same tile and member (D2 is issued only after the epilogue has
 // read D1 and written H1).
@@ -73,7 +77,8 @@ constexpr int kIn = 128;        // padded features (layer-1 K)
 constexpr int kMembers = 2;
 constexpr int kSites = kEnvSites + 1;  // 58 environment sites and the migrant
 constexpr int kTileBytes = kRows * 32 * 2;  // one 128 x 32 operand tile (8 KB)
-constexpr int kProdWarps = 4;
+constexpr int kProdWarps = 8;     // two per row: sites [0, 32) and [32, 64)
+constexpr int kHalfSites = 32;
 constexpr int kMmaWarp = kProdWarps;
 constexpr int kFirstEpi = kProdWarps + 1;
 constexpr int kEpiWarps = 16;
@@ -98,21 +103,22 @@ struct FusedBars {
   uint32_t tmem;
   uint32_t site_word[8];               // per species code: the row word of a site (two bf16 channels)
   float partial[3][kRows];             // column quarters 1-3 of each row's output dot product
-  uint8_t flag[kFlagRing][kRows];      // per tile (ring): the row goes to the plain predictor
+  uint32_t flag[kFlagRing][kProdWarps];  // per tile (ring) and producer warp: bit l, row (warp % 4) 32 + l
+                                         // goes to the plain predictor
 };
 
 constexpr size_t kSmemBytes = static_cast<size_t>(kW1Bytes) + kW2Bytes + kXBytes + kH1Bytes + sizeof(FusedBars);
 static_assert(kSmemBytes <= 232448, "the fused kernel's shared memory exceeds 227 KB");
 static_assert(kSites <= 64, "a row holds 16 x 4 site words");
 
-// GELU of two values in packed half precision: u = z (c0 + c1 z^2), GELU = h + h tanh(u), h = z / 2.
-__device__ __forceinline__ __half2 GeluHalf2(__half2 z) {
-  const __half2 u = __hmul2(z, __hfma2(__hmul2(z, z), __float2half2_rn(0.0356774081363001f),
-                                       __float2half2_rn(0.7978845608028654f)));
+// GELU(z) of two values in packed half precision from h = z / 2:
+// u = z (c0 + c1 z^2) = h (2 c0 + 8 c1 h^2), GELU = h + h tanh(u).
+__device__ __forceinline__ __half2 GeluHalf2FromHalfZ(__half2 h) {
+  const __half2 u = __hmul2(h, __hfma2(__hmul2(h, h), __float2half2_rn(8.0f * 0.0356774081363001f),
+                                       __float2half2_rn(2.0f * 0.7978845608028654f)));
   uint32_t ub = *reinterpret_cast<const uint32_t *>(&u), tb;
   asm("tanh.approx.f16x2 %0, %1;" : "=r"(tb) : "r"(ub));
   const __half2 t = *reinterpret_cast<const __half2 *>(&tb);
-  const __half2 h = __hmul2(z, __float2half2_rn(0.5f));
   return __hfma2(h, t, h);
 }
 
@@ -128,7 +134,7 @@ __device__ __forceinline__ bool WarpWait(uint64_t *bar, uint32_t parity, volatil
   return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
-// Packed half GELU(z + b) . w over 32 columns, summed in FP32 per 8 columns.
+// Packed half GELU(2 (v + b)) . w over 32 columns (v and b halved), summed in FP32 per 8 columns.
 __device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, const __half *w) {
   float acc = 0.f;
 #pragma unroll
@@ -141,12 +147,94 @@ __device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, co
     for (int e = 0; e < 4; ++e) {
       const __half2 z = __hadd2(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]),
                                 *reinterpret_cast<const __half2 *>(&bw[e]));
-      s2 = __hfma2(GeluHalf2(z), *reinterpret_cast<const __half2 *>(&wv[e]), s2);
+      s2 = __hfma2(GeluHalf2FromHalfZ(z), *reinterpret_cast<const __half2 *>(&wv[e]), s2);
     }
     const float2 f = __half22float2(s2);
     acc += f.x + f.y;
   }
   return acc;
+}
+
+// Producer of half kHalf of every row of the CTA's tiles: sites [32 kHalf, 32 kHalf + 32)
+// of the row (MMM-ordered environment, then the migrant; past site 58 nothing), written
+// as words 32 kHalf .. 32 kHalf + 31 of the row (word s = features 2 s, 2 s + 1). Returns
+// the status bits of rejected pairs.
+template <int kHalf>
+__device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *bars, unsigned char *sx,
+                                                long long tiles, int warp, int lane, volatile int *abort) {
+  const int r = (warp & 3) * 32 + lane;
+  const int n = j.n;
+  const long long nsites = 4LL * n * n * n;
+  unsigned bad_all = 0;
+  int t_local = 0;
+  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
+    const long long row = tile * kRows + r;
+    int code[kHalfSites];
+    bool fallback = true;
+    if (row < j.m) {
+      const long long a = __ldg(&j.pairs[2 * row]), b = __ldg(&j.pairs[2 * row + 1]);
+      unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
+      int di = -1;
+      H3 hi{0, 0, 0};
+      if (!bad) {
+        hi = SiteCoord(a, n);
+        const H3 hj = SiteCoord(b, n);
+        const int dx = WrapDelta(hj.x - hi.x, n), dy = WrapDelta(hj.y - hi.y, n), dz = WrapDelta(hj.z - hi.z, n);
+        if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
+          di = __ldg(&j.dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
+        if (di < 0) bad = kStatusNotNeighbor;
+      }
+      if (kHalf == 0) bad_all |= bad;
+      if (!bad) {
+        // the offsets of this direction, 4 bytes (dx, dy, dz, 0) per site
+        const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
+        unsigned seen = 0;
+#pragma unroll
+        for (int k = 0; k < kHalfSites; ++k) {
+          const int site = kHalf * kHalfSites + k;
+          int c = -1;
+          if (site < kEnvSites) {
+            const int o = __ldg(off + site);
+            c = __ldg(&j.species[NeighborId(hi, static_cast<int8_t>(o), static_cast<int8_t>(o >> 8),
+                                            static_cast<int8_t>(o >> 16), n)]);
+          } else if (site == kEnvSites) {
+            c = __ldg(&j.species[b]);
+          }
+          code[k] = c;
+        }
+#pragma unroll
+        for (int k = 0; k < kHalfSites; ++k)
+          if (kHalf * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
+        fallback = (seen & j.fallback_codes) != 0;
+      }
+    }
+    if (fallback) {
+#pragma unroll
+      for (int k = 0; k < kHalfSites; ++k) code[k] = -1;
+    }
+    // the X buffer is free once the previous tile's layer-1 MMAs have completed
+    if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
+#pragma unroll
+    for (int c = 0; c < kHalfSites / 4; ++c) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int k = 4 * c + e, word = kHalf * kHalfSites + k;
+        w[e] = code[k] >= 0 ? bars->site_word[code[k] & 7] : 0u;
+        if (word == kIn / 2 - 1) w[e] |= 0x3F800000u;  // feature 127 = 1: the bias column
+      }
+      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, kHalf * (kHalfSites / 4) + c)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    const unsigned fb = __ballot_sync(0xffffffffu, fallback);
+    if (lane == 0) bars->flag[t_local % kFlagRing][warp] = fb;
+    FenceAsyncSmem();
+    __syncwarp();
+    if (lane == 0) {
+      Arrive(&bars->x_full);
+      Arrive(&bars->flag_full[t_local % kFlagRing]);
+    }
+  }
+  return bad_all;
 }
 
 }  // namespace
@@ -190,91 +278,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   const long long tiles = (j.m + kRows - 1) / kRows;
 
   if (warp < kProdWarps) {
-    // ---- producer: weights once, then one row per thread and tile ----
+    // ---- producer: weights once, then half a row per thread and tile ----
     if (warp == 0 && lane == 0) {
       ArriveExpectTx(&bars->w_full, kW1Bytes + kW2Bytes);
       BulkCopy(sw1, d.w1_tiles, kW1Bytes, &bars->w_full);
       BulkCopy(sw2, d.w2_tiles, kW2Bytes, &bars->w_full);
     }
-    const int r = warp * 32 + lane;
-    const int n = j.n;
-    const long long nsites = 4LL * n * n * n;
-    unsigned bad_all = 0;
-    int t_local = 0;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
-      const long long row = tile * kRows + r;
-      int code[kSites];
-      bool fallback = true;
-      if (row < j.m) {
-        const long long a = __ldg(&j.pairs[2 * row]), b = __ldg(&j.pairs[2 * row + 1]);
-        unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
-        int di = -1;
-        H3 hi{0, 0, 0};
-        if (!bad) {
-          hi = SiteCoord(a, n);
-          const H3 hj = SiteCoord(b, n);
-          const int dx = WrapDelta(hj.x - hi.x, n), dy = WrapDelta(hj.y - hi.y, n), dz = WrapDelta(hj.z - hi.z, n);
-          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
-            di = __ldg(&j.dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
-          if (di < 0) bad = kStatusNotNeighbor;
-        }
-        bad_all |= bad;
-        if (!bad) {
-          // the 58 offsets of this direction, 4 bytes (dx, dy, dz, 0) each (|offset| <= 4)
-          const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
-          const int m2 = 2 * n;
-          if (hi.x >= 4 && hi.x < m2 - 4 && hi.y >= 4 && hi.y < m2 - 4 && hi.z >= 4 && hi.z < m2 - 4) {
-            // no wrap: id(h + o) = id(h) + dx 2n^2 + dy n + floor((hz % 2 + dz) / 2)
-            const unsigned base = static_cast<unsigned>(a), plane = 2u * static_cast<unsigned>(n) * n;
-            const int p = hi.z & 1;
-#pragma unroll
-            for (int k = 0; k < kEnvSites; ++k) {
-              const int o = __ldg(off + k);
-              const int dx = static_cast<int8_t>(o), dy = static_cast<int8_t>(o >> 8), dz = static_cast<int8_t>(o >> 16);
-              const unsigned id = base + static_cast<unsigned>(dx) * plane + static_cast<unsigned>(dy * n) +
-                                  static_cast<unsigned>((p + dz) >> 1);
-              code[k] = __ldg(&j.species[id]);
-            }
-          } else {
-#pragma unroll
-            for (int k = 0; k < kEnvSites; ++k) {
-              const int o = __ldg(off + k);
-              code[k] = __ldg(&j.species[NeighborId(hi, static_cast<int8_t>(o), static_cast<int8_t>(o >> 8),
-                                                    static_cast<int8_t>(o >> 16), n)]);
-            }
-          }
-          code[kEnvSites] = __ldg(&j.species[b]);
-          unsigned seen = 0;
-#pragma unroll
-          for (int k = 0; k < kSites; ++k) seen |= 1u << (code[k] & 7);
-          fallback = (seen & j.fallback_codes) != 0;
-        }
-      }
-      if (fallback) {
-#pragma unroll
-        for (int k = 0; k < kSites; ++k) code[k] = -1;
-      }
-      // the X buffer is free once the previous tile's layer-1 MMAs have completed
-      if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
-#pragma unroll
-      for (int c = 0; c < kIn / 8; ++c) {
-        uint32_t w[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int s = 4 * c + e;  // word s holds features 2s, 2s + 1
-          w[e] = (s < kSites && code[s] >= 0) ? bars->site_word[code[s] & 7] : 0u;
-          if (s == kIn / 2 - 1) w[e] |= 0x3F800000u;  // feature 127 = 1: the bias column
-        }
-        *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
-      }
-      bars->flag[t_local % kFlagRing][r] = fallback ? 1 : 0;
-      FenceAsyncSmem();
-      __syncwarp();
-      if (lane == 0) {
-        Arrive(&bars->x_full);
-        Arrive(&bars->flag_full[t_local % kFlagRing]);
-      }
-    }
+    const unsigned bad_all = warp < 4 ? ProduceRows<0>(j, bars, sx, tiles, warp, lane, abort)
+                                      : ProduceRows<1>(j, bars, sx, tiles, warp, lane, abort);
     if (bad_all) atomicOr(j.pair_status, static_cast<int>(bad_all));
     // the weight copies must land before the CTA exits
     if (warp == 0 && lane == 0 && !WaitDrain(&bars->w_full, 0)) *abort = 1;
@@ -339,9 +350,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool fallback = false;
       if (q == 0) {
         if (!(ok = WarpWait(&bars->flag_full[t_local % kFlagRing], (t_local / kFlagRing) & 1, abort, lane))) break;
-        fallback = bars->flag[t_local % kFlagRing][r] != 0;
+        const uint32_t *fw = bars->flag[t_local % kFlagRing];
+        fallback = (((fw[lg] | fw[4 + lg]) >> lane) & 1u) != 0;
       }
-      // H1 = GELU(D1) (D1 includes b1): this thread's row, its 32 columns (K tile q of H1)
+      // H1 = GELU(2 D1) (D1 includes b1 / 2): this thread's row, its 32 columns (K tile q of H1)
       for (int m = 0; m < kMembers && ok; ++m) {
         const int slot = par * 2 + m;
         if (!(ok = WarpWait(&bars->acc_full[slot], 0, abort, lane))) break;
@@ -355,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           uint32_t packed[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const __half2 p = GeluHalf2(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]));
+            const __half2 p = GeluHalf2FromHalfZ(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]));
             packed[e] = *reinterpret_cast<const uint32_t *>(&p);
           }
           *reinterpret_cast<uint4 *>(hrow + ChunkOffset(r, q * 4 + g8)) =
@@ -366,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         if (lane == 0) Arrive(&bars->h1_full[m]);
       }
-      // y_m = GELU(D2 + b2) . w3 + b3
+      // y_m = GELU(2 (D2 + b2 / 2)) . w3 + b3
       float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
       for (int m = 0; m < kMembers && ok; ++m) {
         const int slot = par * 2 + m;
