@@ -1474,12 +1474,13 @@ lmc::FeatEnc FeatEncOf(const lmc_ctx *ctx) {
 int FeatureCount(const lmc_ctx *ctx) { return (lmc::kEnvSites + 1) * FeatEncOf(ctx).width; }
 
 // The fused jump kernel's description of the replica's lattice and the encoding (solute
-// channels of a three-species alphabet: two bf16 channels per site, one word).
+// channels of a three- or four-species alphabet: two or three channels per site).
 bool FusedJumpsFor(const lmc_ctx *ctx, int replica, const long long *pairs, long long m, float *mean, float *spread,
                    lmc::FusedJumps *j) {
   const lmc::FeatEnc f = FeatEncOf(ctx);
-  if (ctx->feat_encoding != LMC_FEATURES_SOLUTE || f.width != 2) return false;
+  if (ctx->feat_encoding != LMC_FEATURES_SOLUTE || (f.width != 2 && f.width != 3)) return false;
   *j = lmc::FusedJumps{};
+  j->channels = f.width;
   j->species = ctx->species.as<int8_t>() + ctx->offsets[replica];
   j->n = ctx->n[replica];
   j->pairs = pairs;
@@ -1490,6 +1491,7 @@ bool FusedJumpsFor(const lmc_ctx *ctx, int replica, const long long *pairs, long
     const int rank = c < ctx->fm.num_species ? ctx->fm.onehot_rank[c] : -1;
     const int ch = rank >= 0 ? lmc::FeatChannel(f, rank) : -1;
     j->site_word[c] = ch == 0 ? 0x3F80u : (ch == 1 ? 0x3F800000u : 0u);  // bf16 1.0 in the low / high half
+    j->chan[c] = static_cast<int8_t>(ch);
     if (rank < 0) j->fallback_codes |= 1u << c;
   }
   j->mean = mean;
@@ -1578,7 +1580,7 @@ void NetworkOnJumps(lmc_ctx *ctx, lmc_mlp *mlp, int replica, const long long *pa
   Require(in >= FeatureCount(ctx), LMC_ERR_INVALID_ARGUMENT,
           "the network's input is narrower than the features of this model and encoding");
   lmc::FusedJumps j;
-  if (in == 128 && FusedJumpsFor(ctx, replica, pairs, m, mean, spread, &j) && lmc::MlpFusedJumpsAsync(mlp, j, ctx->stream))
+  if (FusedJumpsFor(ctx, replica, pairs, m, mean, spread, &j) && lmc::MlpFusedJumpsAsync(mlp, j, ctx->stream))
     return;
   ctx->s_feat.Ensure(sizeof(uint16_t) * static_cast<size_t>(m) * in);
   CudaCheck(lmc::LaunchSurrogateFeatures(ctx->t, ctx->species.as<int8_t>() + ctx->offsets[replica], ctx->n[replica],

@@ -305,17 +305,18 @@ __global__ void tile_weights_kernel(const float *w, long long rows, int k, int b
   out[block * block_rows * 32 + (rr >> 3) * 256 + (kc >> 3) * 64 + (rr & 7) * 8 + (kc & 7)] = FromFloat<T>(scale * w[i]);
 }
 
-// Half copies of `scale` b2 and of w3; for in = hidden = 128, `scale` b1 into the last input
-// column of the W1 tiles (row r = m * 128 + h: block m * 4 + 3, column 31 of the block).
-__global__ void fused_extras_kernel(const float *b1, const float *b2, const float *w3, int n, bool bias_col,
-                                    float scale, __half *b2h, __half *w3h, __nv_bfloat16 *w1_tiles) {
+// Half copies of `scale` b2 and of w3; with kt > 0 (hidden 128, kt = in / 32 K tiles),
+// `scale` b1 into the last input column of the W1 tiles (row r = m * 128 + h: block
+// m * kt + kt - 1, column 31 of the block).
+__global__ void fused_extras_kernel(const float *b1, const float *b2, const float *w3, int n, int kt, float scale,
+                                    __half *b2h, __half *w3h, __nv_bfloat16 *w1_tiles) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   b2h[i] = __float2half_rn(scale * b2[i]);
   w3h[i] = __float2half_rn(w3[i]);
-  if (bias_col) {
+  if (kt > 0) {
     const int m = i / 128, h = i % 128;
-    w1_tiles[static_cast<long long>(m * 4 + 3) * 4096 + (h >> 3) * 256 + 3 * 64 + (h & 7) * 8 + 7] =
+    w1_tiles[static_cast<long long>(m * kt + kt - 1) * 4096 + (h >> 3) * 256 + 3 * 64 + (h & 7) * 8 + 7] =
         __float2bfloat16(scale * b1[i]);
   }
 }
@@ -495,8 +496,8 @@ cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s) {
   const long long n = n1 > n2 ? n1 : n2;
   cast_weights_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, s>>>(d.w1, n1, d.w2, d.members, d.hidden, d.w1h,
                                                                         d.w2h, d.w2t);
-  // hidden 128 with 128 inputs: the fused jump kernel's tiles, W1, b1, W2 and b2 halved (exact)
-  const bool fused_shape = d.in == 128 && d.hidden == 128;
+  // hidden 128 with 128 or 192 inputs: the fused jump kernel's tiles, W1, b1, W2 and b2 halved (exact)
+  const bool fused_shape = (d.in == 128 || d.in == 192) && d.hidden == 128;
   const float scale = fused_shape ? 0.5f : 1.0f;
   if (d.w1_tiles && (d.hidden % 256 == 0 || d.hidden == 128) && d.in % 32 == 0) {
     const int block_rows = d.hidden == 128 ? 128 : 256;
@@ -507,8 +508,9 @@ cudaError_t MlpCastWeights(const MlpDev &d, cudaStream_t s) {
   }
   if (d.b2h && d.w3h) {
     const int nh = d.members * d.hidden;
-    fused_extras_kernel<<<(nh + 255) / 256, 256, 0, s>>>(d.b1, d.b2, d.w3, nh, fused_shape && d.w1_tiles, scale,
-                                                         d.b2h, d.w3h, d.w1_tiles);
+    fused_extras_kernel<<<(nh + 255) / 256, 256, 0, s>>>(d.b1, d.b2, d.w3, nh,
+                                                         fused_shape && d.w1_tiles ? d.in / 32 : 0, scale, d.b2h,
+                                                         d.w3h, d.w1_tiles);
   }
   return cudaGetLastError();
 }

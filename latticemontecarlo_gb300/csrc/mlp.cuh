@@ -81,9 +81,9 @@ struct MlpDev {
   __nv_bfloat16 *w1_tiles;
   __half *w2_tiles;
   // b2 and w3 in IEEE half (the fused jump kernel's packed layer-2 epilogue). For in = 128
-  // and hidden = 128 (that kernel's shape) the tiles and b2h hold W1, W2 and b2 halved, and
-  // the last input column of w1_tiles holds b1 / 2 instead of W1's (unused) column 127: the
-  // kernel sets feature 127 to 1, so the layer-1 MMA adds the bias.
+  // or 192 and hidden = 128 (that kernel's shapes) the tiles and b2h hold W1, W2 and b2
+  // halved, and the last input column of w1_tiles holds b1 / 2 instead of W1's (unused)
+  // last column: the kernel sets that feature to 1, so the layer-1 MMA adds the bias.
   __half *b2h, *w3h;
 };
 
@@ -119,7 +119,8 @@ cudaError_t MlpEnsemble(const float *y, int batch, int members, float mean_label
                         float *spread, cudaStream_t s);
 
 // Lattice jumps for the fused kernel (mlp_fused.cu), which gathers the solute-channel
-// features itself (two channels per site: one-hot alphabets of three species).
+// features itself (two channels per site for one-hot alphabets of three species, three
+// for four).
 struct FusedJumps {
   const int8_t *species;     // the lattice (one replica), n^3 cells
   int n;
@@ -127,14 +128,17 @@ struct FusedJumps {
   long long m;
   const int8_t *mmm_off;     // [12][58][4] MMM-ordered offsets per jump direction (half units)
   const int8_t *dir_of;      // [27] 1NN direction of an offset, -1 none
-  uint32_t site_word[8];     // per species code: its two bf16 channels as one word (0 for the base species)
+  int channels;              // channels per site (2 or 3)
+  uint32_t site_word[8];     // two channels: per species code, both bf16 channels as one word (0: base)
+  int8_t chan[8];            // per species code: its channel, -1 none (the base, a vacancy)
   uint32_t fallback_codes;   // bit c: species code c in the environment sends the row to the plain predictor
   float *mean, *spread;      // [m] ensemble mean (eV) and spread (+inf: plain predictor)
   int *pair_status;          // kStatusBadSite / kStatusNotNeighbor of rejected pairs
 };
-// The fused kernel serves ensembles of 2 members, 128 inputs, hidden 128 (weights kept in
-// shared memory); an expired wait sets *status.
+// The fused kernel serves ensembles of 2 members, 128 or 192 inputs (2 or 3 channels per
+// site), hidden 128 (weights kept in shared memory); an expired wait sets *status.
 bool MlpFusedSupported(const MlpDev &d);
+int MlpFusedChannels(const MlpDev &d);  // 2, 3, or 0 when the kernel does not serve the network
 cudaError_t MlpFusedPredict(const MlpDev &d, const FusedJumps &j, float mean_label, float std_label, int *status,
                             cudaStream_t s);
 

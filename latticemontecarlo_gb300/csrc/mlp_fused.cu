@@ -1,43 +1,43 @@
 // Fused surrogate barriers of lattice jumps for a compact ensemble whose weights
-// stay in shared memory: 2 members of 128 -> 128 -> 128 -> 1 (GELU) over the
-// solute-channel features (two channels per site, the base species all zero:
-// 59 sites x 2 = 118 inputs, padded to 128). One persistent CTA per SM loads
-// both members' weights once (128 KB, two bulk copies) and walks tiles of 128
-// jumps. Per tile:
+// stay in shared memory: 2 members of in -> 128 -> 128 -> 1 (GELU) over the
+// solute-channel features (kC channels per site, the base species all zero:
+// 59 sites x kC inputs, padded to in = 128 for three-species alphabets, kC = 2,
+// and to 192 for four, kC = 3). One persistent CTA per SM loads both members'
+// weights once (128 / 160 KB, two bulk copies) and walks tiles of 128 jumps.
+// Per tile and member m:
 //   X  (smem, bf16)        the features, gathered from the lattice by the producer warps
-//   D1 (TMEM, fp32)        = (X . W1[m]^T + b1[m]) / 2       tcgen05.mma kind::f16, M = N = 128
-//   H1 (smem, IEEE half)   = GELU(2 D1)                      epilogue warps, packed half
-//   D2 (TMEM, same columns)= H1 . W2[m]^T / 2 (half)         tcgen05.mma kind::f16
-//   y_m                    = GELU(2 (D2 + b2[m] / 2)) . w3[m] + b3[m]   packed half, FP32 sums of 8 terms
+//   D  (TMEM, fp32)        = (X . W1[m]^T + b1[m]) / 2     tcgen05.mma kind::f16, A and B in smem
+//   H1 (TMEM, IEEE half)   = GELU(2 D)                     epilogue warps (tcgen05.ld, tcgen05.st)
+//   D  (TMEM, same columns)= H1 . W2[m]^T / 2 (half)       tcgen05.mma kind::f16, A in TMEM
+//   y_m                    = GELU(2 (D + b2[m] / 2)) . w3[m] + b3[m]   packed half, FP32 sums of 8
 // then the ensemble mean and spread. The layer-1 bias is the last input column: the
-// producer sets feature 127 (padding in the solute encoding) to 1 and the weight tiles
-// hold b1 there. W1, b1, W2 and b2 are stored halved (exact in binary floating point), so
-// the MMAs produce h = z / 2 and GELU(z) = h + h tanh(h (2 c0 + 8 c1 h^2)) takes one
-// multiply less. A row whose pair is not a 1NN jump inside the lattice, or whose
-// environment holds a species without a one-hot slot (a second vacancy), gets
+// producer sets feature in - 1 (padding in the solute encoding) to 1 and the weight
+// tiles hold b1 there. W1, b1, W2 and b2 are stored halved (exact in binary floating
+// point), so the MMAs produce h = z / 2 and GELU(z) = h + h tanh(h (2 c0 + 8 c1 h^2))
+// takes one multiply less. A row whose pair is not a 1NN jump inside the lattice, or
+// whose environment holds a species without a one-hot slot (a second vacancy), gets
 // spread = +inf, so the caller's fallback sends it to the plain predictor.
 //
 // Warp roles (mbarriers only, no block-wide barrier inside the loop):
 //   warps 0-7   producer: row r of the tile is gathered by threads r of warps 0-3
-//               (sites 0-31 of the row: its direction and 32 MMM-ordered sites) and
-//               of warps 4-7 (sites 32-58, the migrant being site 58), with
+//               (its direction and sites 0-31: the first half of the row) and of
+//               warps 4-7 (sites 32-58, the migrant being site 58), with
 //               independent loads issued before the wait for the X buffer; each
 //               writes its half of the row into the operand layout; warp 0 lane 0
 //               also issues the weight copies;
-//   warp 8      lane 0 issues the MMAs and the tcgen05.commit arrivals; it
-//               issues tile t's layer-1 MMAs before tile t-1's layer-2 MMAs, so
-//               the tensor pipe works on the next tile while the epilogue
-//               finishes the current one;
+//   warp 8      lane 0 issues the MMAs and the tcgen05.commit arrivals;
 //   warps 9-24  epilogue: TMEM lane group = warp % 4, 32-column quarter =
 //               (warp - 9) / 4.
-// TMEM: 512 columns = 4 slots of 128 (tile parity x member); a slot holds D1 and
-// then D2 of the same tile and member (D2 is issued only after the epilogue has
-// read D1 and written H1).
+// TMEM (512 columns allocated): member m owns columns [192 m, 192 m + 192): D in the
+// first 128 (layer 1, then layer 2 once H1 is written), H1 in the last 64 (128 half
+// values per row). The members give the pipeline its overlap: the layer-1 MMAs of the
+// next tile's member m start once the epilogue has read member m's layer-2 result,
+// while it works on the other member.
 //
-// Operand layout in shared memory: K-major 8-row x 16-byte core matrices, 32-wide
-// K tiles of 128 rows (tcgen05.cuh). Every wait is bounded and polls a shared
-// abort flag: on expiry the kernel records kMlpFusedTimeout, drains its MMAs and
-// copies, frees its TMEM and returns.
+// Operand layout in shared memory: K-major 8-row x 16-byte core matrices, 32-wide K
+// tiles of 128 rows (tcgen05.cuh). Every wait is bounded (sleeping probes, 2 s of wall
+// time) and polls a shared abort flag: on expiry the kernel records kMlpFusedTimeout,
+// drains its MMAs and copies, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -63,53 +63,65 @@ using tc::FenceBarrierInit;
 using tc::FenceBeforeSync;
 using tc::IdescBf16;
 using tc::Mma;
+using tc::MmaTmemA;
 using tc::OperandDesc;
 using tc::Smem;
 using tc::TmemAlloc;
 using tc::TmemFree;
 using tc::TmemLoad32;
+using tc::TmemStore16;
 using tc::WaitDrain;
 using tc::WaitSleep;
 
 constexpr int kRows = 128;      // jumps per tile (MMA M)
 constexpr int kHid = 128;       // hidden width (MMA N of both layers)
-constexpr int kIn = 128;        // padded features (layer-1 K)
 constexpr int kMembers = 2;
-constexpr int kSites = kEnvSites + 1;  // 58 environment sites and the migrant
+constexpr int kSites = kEnvSites + 1;       // 58 environment sites and the migrant
 constexpr int kTileBytes = kRows * 32 * 2;  // one 128 x 32 operand tile (8 KB)
-constexpr int kProdWarps = 8;     // two per row: sites [0, 32) and [32, 64)
+constexpr int kProdWarps = 8;               // two per row: sites [0, 32) and [32, 64)
 constexpr int kHalfSites = 32;
 constexpr int kMmaWarp = kProdWarps;
 constexpr int kFirstEpi = kProdWarps + 1;
 constexpr int kEpiWarps = 16;
 constexpr int kThreads = 32 * (kFirstEpi + kEpiWarps);
 constexpr uint32_t kCols = 512;
+constexpr uint32_t kMemberCols = 192;       // D (128) and H1 (64) of one member
 constexpr int kFlagRing = 4;
 constexpr uint32_t kIdescL1 = IdescBf16(kRows, kHid);                                    // bf16 x bf16
 constexpr uint32_t kIdescL2 = (1u << 4) | ((kHid >> 3) << 17) | ((kRows >> 4) << 24);  // f16 x f16
-
-constexpr int kW1Bytes = kMembers * kHid * kIn * 2;
 constexpr int kW2Bytes = kMembers * kHid * kHid * 2;
-constexpr int kXBytes = kRows * kIn * 2;
-constexpr int kH1Bytes = kMembers * kRows * kHid * 2;
+
+template <int kC>
+struct Shape {
+  static constexpr int kIn = (kSites * kC + 63) / 64 * 64;  // 128 (kC = 2) or 192 (kC = 3)
+  static constexpr int kKt = kIn / 32;                      // layer-1 K tiles
+  static constexpr int kW1Bytes = kMembers * kHid * kIn * 2;
+  static constexpr int kXBytes = kRows * kIn * 2;
+};
 
 struct FusedBars {
   uint64_t w_full, x_full, x_empty;
-  uint64_t acc_full[4], acc_empty[4];  // TMEM slot (tile parity * 2 + member)
-  uint64_t h1_full[kMembers], h1_empty[kMembers];
+  uint64_t acc_full[kMembers];   // phases 2t (layer 1 of tile t) and 2t + 1 (layer 2)
+  uint64_t acc_empty[kMembers];  // the epilogue has read layer 2 of the member's tile
+  uint64_t h1_full[kMembers];
   uint64_t flag_full[kFlagRing];
   uint64_t part_full, part_empty, done;
   int abort;
   uint32_t tmem;
-  uint32_t site_word[8];               // per species code: the row word of a site (two bf16 channels)
-  float partial[3][kRows];             // column quarters 1-3 of each row's output dot product
-  uint32_t flag[kFlagRing][kProdWarps];  // per tile (ring) and producer warp: bit l, row (warp % 4) 32 + l
-                                         // goes to the plain predictor
+  uint32_t site_word[8];                 // kC = 2: per species code, the row word of a site
+  int8_t chan[8];                        // per species code: its channel, -1 none
+  float partial[3][kRows];               // column quarters 1-3 of each row's output dot product
+  uint32_t flag[kFlagRing][kProdWarps];  // per tile (ring) and producer warp: bit l set when row
+                                         // (warp % 4) 32 + l goes to the plain predictor
 };
 
-constexpr size_t kSmemBytes = static_cast<size_t>(kW1Bytes) + kW2Bytes + kXBytes + kH1Bytes + sizeof(FusedBars);
-static_assert(kSmemBytes <= 232448, "the fused kernel's shared memory exceeds 227 KB");
-static_assert(kSites <= 64, "a row holds 16 x 4 site words");
+template <int kC>
+constexpr size_t SmemBytes() {
+  return static_cast<size_t>(Shape<kC>::kW1Bytes) + kW2Bytes + Shape<kC>::kXBytes + sizeof(FusedBars);
+}
+static_assert(SmemBytes<3>() <= 232448, "the fused kernel's shared memory exceeds 227 KB");
+static_assert(kSites <= 2 * kHalfSites, "a row is gathered in two halves of 32 sites");
+static_assert(2 * kMemberCols <= kCols, "both members' TMEM columns");
 
 // GELU(z) of two values in packed half precision from h = z / 2:
 // u = z (c0 + c1 z^2) = h (2 c0 + 8 c1 h^2), GELU = h + h tanh(u).
@@ -156,12 +168,15 @@ __device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, co
 }
 
 // Producer of half kHalf of every row of the CTA's tiles: sites [32 kHalf, 32 kHalf + 32)
-// of the row (MMM-ordered environment, then the migrant; past site 58 nothing), written
-// as words 32 kHalf .. 32 kHalf + 31 of the row (word s = features 2 s, 2 s + 1). Returns
-// the status bits of rejected pairs.
-template <int kHalf>
+// of the row (MMM-ordered environment, then the migrant; past site 58 nothing), i.e.
+// features [kIn / 2 kHalf, kIn / 2 (kHalf + 1)) (feature kC s + c is channel c of site s).
+// Returns the status bits of rejected pairs.
+template <int kC, int kHalf>
 __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *bars, unsigned char *sx,
                                                 long long tiles, int warp, int lane, volatile int *abort) {
+  constexpr int kIn = Shape<kC>::kIn;
+  constexpr int kHalfFeat = kIn / 2;
+  static_assert(kHalfFeat == kC * kHalfSites, "a half row is 32 sites");
   const int r = (warp & 3) * 32 + lane;
   const int n = j.n;
   const long long nsites = 4LL * n * n * n;
@@ -188,7 +203,6 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
       if (!bad) {
         // the offsets of this direction, 4 bytes (dx, dy, dz, 0) per site
         const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
-        unsigned seen = 0;
 #pragma unroll
         for (int k = 0; k < kHalfSites; ++k) {
           const int site = kHalf * kHalfSites + k;
@@ -202,6 +216,7 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
           }
           code[k] = c;
         }
+        unsigned seen = 0;
 #pragma unroll
         for (int k = 0; k < kHalfSites; ++k)
           if (kHalf * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
@@ -215,15 +230,26 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
     // the X buffer is free once the previous tile's layer-1 MMAs have completed
     if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
 #pragma unroll
-    for (int c = 0; c < kHalfSites / 4; ++c) {
+    for (int c = 0; c < kHalfFeat / 8; ++c) {
       uint32_t w[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int k = 4 * c + e, word = kHalf * kHalfSites + k;
-        w[e] = code[k] >= 0 ? bars->site_word[code[k] & 7] : 0u;
-        if (word == kIn / 2 - 1) w[e] |= 0x3F800000u;  // feature 127 = 1: the bias column
+        const int f = kHalf * kHalfFeat + 8 * c + 2 * e;  // features f (low half), f + 1 (high half)
+        uint32_t word;
+        if constexpr (kC == 2) {
+          const int k = (f - kHalf * kHalfFeat) / 2;  // site of features f, f + 1 in this half
+          word = code[k] >= 0 ? bars->site_word[code[k] & 7] : 0u;
+        } else {
+          const int k0 = (f - kHalf * kHalfFeat) / kC, k1 = (f + 1 - kHalf * kHalfFeat) / kC;
+          const int ch0 = bars->chan[code[k0] & 7], ch1 = bars->chan[code[k1] & 7];
+          word = ((code[k0] >= 0 && ch0 == f % kC) ? 0x3F80u : 0u) |
+                 ((code[k1] >= 0 && ch1 == (f + 1) % kC) ? 0x3F800000u : 0u);
+        }
+        if (f + 1 == kIn - 1) word |= 0x3F800000u;  // the last feature is 1: the bias column
+        w[e] = word;
       }
-      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, kHalf * (kHalfSites / 4) + c)) = make_uint4(w[0], w[1], w[2], w[3]);
+      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, kHalf * (kHalfFeat / 8) + c)) =
+          make_uint4(w[0], w[1], w[2], w[3]);
     }
     const unsigned fb = __ballot_sync(0xffffffffu, fallback);
     if (lane == 0) bars->flag[t_local % kFlagRing][warp] = fb;
@@ -241,12 +267,14 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
 
 constexpr int kMlpFusedTimeout = 1;
 
+template <int kC>
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_fused_jump_kernel(const __grid_constant__ MlpDev d, const __grid_constant__ FusedJumps j, float mean_label,
                           float std_label, int *status) {
+  using S = Shape<kC>;
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char *sw1 = smem, *sw2 = sw1 + kW1Bytes, *sx = sw2 + kW2Bytes, *sh = sx + kXBytes;
-  FusedBars *bars = reinterpret_cast<FusedBars *>(sh + kH1Bytes);
+  unsigned char *sw1 = smem, *sw2 = sw1 + S::kW1Bytes, *sx = sw2 + kW2Bytes;
+  FusedBars *bars = reinterpret_cast<FusedBars *>(sx + S::kXBytes);
   volatile int *abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -254,13 +282,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     BarInit(&bars->w_full, 1);
     BarInit(&bars->x_full, kProdWarps);
     BarInit(&bars->x_empty, 1);
-    for (int i = 0; i < 4; ++i) {
-      BarInit(&bars->acc_full[i], 1);
-      BarInit(&bars->acc_empty[i], kEpiWarps);
-    }
     for (int m = 0; m < kMembers; ++m) {
+      BarInit(&bars->acc_full[m], 1);
+      BarInit(&bars->acc_empty[m], kEpiWarps);
       BarInit(&bars->h1_full[m], kEpiWarps);
-      BarInit(&bars->h1_empty[m], 1);
     }
     for (int i = 0; i < kFlagRing; ++i) BarInit(&bars->flag_full[i], kProdWarps);
     BarInit(&bars->part_full, 3 * 4);
@@ -269,7 +294,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     bars->abort = 0;
     FenceBarrierInit();
   }
-  if (tid < 8) bars->site_word[tid] = j.site_word[tid];
+  if (tid < 8) {
+    bars->site_word[tid] = j.site_word[tid];
+    bars->chan[tid] = j.chan[tid];
+  }
   if (warp == kMmaWarp) TmemAlloc(&bars->tmem, kCols);
   FenceBeforeSync();
   __syncthreads();
@@ -280,58 +308,50 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp < kProdWarps) {
     // ---- producer: weights once, then half a row per thread and tile ----
     if (warp == 0 && lane == 0) {
-      ArriveExpectTx(&bars->w_full, kW1Bytes + kW2Bytes);
-      BulkCopy(sw1, d.w1_tiles, kW1Bytes, &bars->w_full);
+      ArriveExpectTx(&bars->w_full, S::kW1Bytes + kW2Bytes);
+      BulkCopy(sw1, d.w1_tiles, S::kW1Bytes, &bars->w_full);
       BulkCopy(sw2, d.w2_tiles, kW2Bytes, &bars->w_full);
     }
-    const unsigned bad_all = warp < 4 ? ProduceRows<0>(j, bars, sx, tiles, warp, lane, abort)
-                                      : ProduceRows<1>(j, bars, sx, tiles, warp, lane, abort);
+    const unsigned bad_all = warp < 4 ? ProduceRows<kC, 0>(j, bars, sx, tiles, warp, lane, abort)
+                                      : ProduceRows<kC, 1>(j, bars, sx, tiles, warp, lane, abort);
     if (bad_all) atomicOr(j.pair_status, static_cast<int>(bad_all));
     // the weight copies must land before the CTA exits
     if (warp == 0 && lane == 0 && !WaitDrain(&bars->w_full, 0)) *abort = 1;
   } else if (warp == kMmaWarp) {
     // ---- MMA issuer ----
     if (lane == 0) {
-      const uint32_t a1 = Smem(sx), b1 = Smem(sw1), a2 = Smem(sh), b2 = Smem(sw2);
-      // layer 2 of tile tp (both members), once the epilogue has written its H1
-      const auto layer2 = [&](int tp) -> bool {
-        for (int m = 0; m < kMembers; ++m) {
-          if (!WaitSleep(&bars->h1_full[m], tp & 1, abort)) return false;
-          FenceAfterSync();
-          const int slot = (tp & 1) * 2 + m;
-          const uint32_t dcol = tmem + slot * kHid;
-          for (int c = 0; c < kHid / 32; ++c) {
-            const uint32_t a = a2 + m * (kRows * kHid * 2) + c * kTileBytes, b = b2 + (m * (kHid / 32) + c) * kTileBytes;
-            Mma(dcol, OperandDesc(a), OperandDesc(b), kIdescL2, c > 0);
-            Mma(dcol, OperandDesc(a + 256), OperandDesc(b + 256), kIdescL2, true);
-          }
-          Commit(&bars->acc_full[slot]);
-          Commit(&bars->h1_empty[m]);
-        }
-        return true;
-      };
+      const uint32_t a1 = Smem(sx), b1 = Smem(sw1), b2 = Smem(sw2);
       bool ok = WaitSleep(&bars->w_full, 0, abort);
       int t_local = 0;
       for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t_local) {
         if (!(ok = WaitSleep(&bars->x_full, t_local & 1, abort))) break;
         FenceAfterSync();
+        // layer 1 of both members, as each member's columns are released
         for (int m = 0; m < kMembers && ok; ++m) {
-          const int slot = (t_local & 1) * 2 + m;
-          if (t_local >= 2 && !(ok = WaitSleep(&bars->acc_empty[slot], ((t_local >> 1) - 1) & 1, abort))) break;
+          if (t_local >= 1 && !(ok = WaitSleep(&bars->acc_empty[m], (t_local - 1) & 1, abort))) break;
           FenceAfterSync();
-          const uint32_t dcol = tmem + slot * kHid;
-          for (int c = 0; c < kIn / 32; ++c) {
-            const uint32_t a = a1 + c * kTileBytes, b = b1 + (m * (kIn / 32) + c) * kTileBytes;
+          const uint32_t dcol = tmem + m * kMemberCols;
+          for (int c = 0; c < S::kKt; ++c) {
+            const uint32_t a = a1 + c * kTileBytes, b = b1 + (m * S::kKt + c) * kTileBytes;
             Mma(dcol, OperandDesc(a), OperandDesc(b), kIdescL1, c > 0);
             Mma(dcol, OperandDesc(a + 256), OperandDesc(b + 256), kIdescL1, true);
           }
-          Commit(&bars->acc_full[slot]);
+          Commit(&bars->acc_full[m]);
         }
         if (!ok) break;
         Commit(&bars->x_empty);
-        if (t_local >= 1) ok = layer2(t_local - 1);
+        // layer 2, A = H1 in TMEM (16 K per MMA = 8 columns), once the epilogue has written it
+        for (int m = 0; m < kMembers && ok; ++m) {
+          if (!(ok = WaitSleep(&bars->h1_full[m], t_local & 1, abort))) break;
+          FenceAfterSync();
+          const uint32_t dcol = tmem + m * kMemberCols, hcol = dcol + kHid;
+          for (int c = 0; c < kHid / 16; ++c) {
+            const uint32_t b = b2 + (m * (kHid / 32) + (c >> 1)) * kTileBytes + (c & 1) * 256;
+            MmaTmemA(dcol, hcol + c * 8, OperandDesc(b), kIdescL2, c > 0);
+          }
+          Commit(&bars->acc_full[m]);
+        }
       }
-      if (ok && t_local >= 1) layer2(t_local - 1);
       // drain: `done` completes once every MMA issued so far has finished
       Commit(&bars->done);
       if (!WaitDrain(&bars->done, 0)) *abort = 1;
@@ -346,50 +366,42 @@ __global__ void __launch_bounds__(kThreads, 1)
     int t_local = 0;
     for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t_local) {
       const long long row = tile * kRows + r;
-      const int par = t_local & 1;
       bool fallback = false;
       if (q == 0) {
         if (!(ok = WarpWait(&bars->flag_full[t_local % kFlagRing], (t_local / kFlagRing) & 1, abort, lane))) break;
         const uint32_t *fw = bars->flag[t_local % kFlagRing];
         fallback = (((fw[lg] | fw[4 + lg]) >> lane) & 1u) != 0;
       }
-      // H1 = GELU(2 D1) (D1 includes b1 / 2): this thread's row, its 32 columns (K tile q of H1)
+      // H1 = GELU(2 D) (D holds layer 1 with b1, halved): this thread's row, its 32 columns,
+      // as 16 packed-half columns of the member's H1
       for (int m = 0; m < kMembers && ok; ++m) {
-        const int slot = par * 2 + m;
-        if (!(ok = WarpWait(&bars->acc_full[slot], 0, abort, lane))) break;
-        if (t_local >= 1 && !(ok = WarpWait(&bars->h1_empty[m], (t_local - 1) & 1, abort, lane))) break;
+        if (!(ok = WarpWait(&bars->acc_full[m], 0, abort, lane))) break;
         FenceAfterSync();
+        const uint32_t dcol = tmem + lane_base + m * kMemberCols;
         float v[32];
-        TmemLoad32(tmem + lane_base + slot * kHid + q * 32, v);
-        unsigned char *hrow = sh + m * (kRows * kHid * 2);
+        TmemLoad32(dcol + q * 32, v);
+        uint32_t packed[16];
 #pragma unroll
-        for (int g8 = 0; g8 < 4; ++g8) {
-          uint32_t packed[4];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const __half2 p = GeluHalf2FromHalfZ(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]));
-            packed[e] = *reinterpret_cast<const uint32_t *>(&p);
-          }
-          *reinterpret_cast<uint4 *>(hrow + ChunkOffset(r, q * 4 + g8)) =
-              make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        for (int e = 0; e < 16; ++e) {
+          const __half2 p = GeluHalf2FromHalfZ(__floats2half2_rn(v[2 * e], v[2 * e + 1]));
+          packed[e] = *reinterpret_cast<const uint32_t *>(&p);
         }
+        TmemStore16(dcol + kHid + q * 16, packed);
         FenceBeforeSync();
-        FenceAsyncSmem();
         __syncwarp();
         if (lane == 0) Arrive(&bars->h1_full[m]);
       }
-      // y_m = GELU(2 (D2 + b2 / 2)) . w3 + b3
+      // y_m = GELU(2 (D + b2 / 2)) . w3 + b3
       float ysum = 0.f, ymin = 3.4e38f, ymax = -3.4e38f;
       for (int m = 0; m < kMembers && ok; ++m) {
-        const int slot = par * 2 + m;
-        if (!(ok = WarpWait(&bars->acc_full[slot], 1, abort, lane))) break;
+        if (!(ok = WarpWait(&bars->acc_full[m], 1, abort, lane))) break;
         FenceAfterSync();
         float v[32];
-        TmemLoad32(tmem + lane_base + slot * kHid + q * 32, v);
+        TmemLoad32(tmem + lane_base + m * kMemberCols + q * 32, v);
         const float acc = GeluDotHalf(v, d.b2h + m * kHid + q * 32, d.w3h + m * kHid + q * 32);
         FenceBeforeSync();
         __syncwarp();
-        if (lane == 0) Arrive(&bars->acc_empty[slot]);
+        if (lane == 0) Arrive(&bars->acc_empty[m]);
         // the four column quarters of a row meet in shared memory
         const int u = 2 * t_local + m;
         if (q != 0) {
@@ -421,24 +433,40 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 bool MlpFusedSupported(const MlpDev &d) {
-  return d.in == kIn && d.hidden == kHid && d.members == kMembers && d.w1_tiles != nullptr && d.w2_tiles != nullptr &&
-         d.b2h != nullptr && d.w3h != nullptr;
+  return (d.in == Shape<2>::kIn || d.in == Shape<3>::kIn) && d.hidden == kHid && d.members == kMembers &&
+         d.w1_tiles != nullptr && d.w2_tiles != nullptr && d.b2h != nullptr && d.w3h != nullptr;
+}
+
+int MlpFusedChannels(const MlpDev &d) {
+  if (!MlpFusedSupported(d)) return 0;
+  return d.in == Shape<2>::kIn ? 2 : 3;
+}
+
+template <int kC>
+static cudaError_t LaunchFused(const MlpDev &d, const FusedJumps &j, float mean_label, float std_label, int *status,
+                               cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (err != cudaSuccess) return err;
+  const long long tiles = (j.m + kRows - 1) / kRows;
+  const int grid = static_cast<int>(tiles < sms ? tiles : sms);
+  constexpr size_t smem = SmemBytes<kC>();
+  err = cudaFuncSetAttribute(mlp_fused_jump_kernel<kC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+  if (err != cudaSuccess) return err;
+  mlp_fused_jump_kernel<kC><<<grid, kThreads, smem, s>>>(d, j, mean_label, std_label, status);
+  return cudaGetLastError();
 }
 
 cudaError_t MlpFusedPredict(const MlpDev &d, const FusedJumps &j, float mean_label, float std_label, int *status,
                             cudaStream_t s) {
-  if (!MlpFusedSupported(d)) return cudaErrorInvalidValue;
+  const int kc = MlpFusedChannels(d);
+  if (kc == 0 || j.channels != kc) return cudaErrorInvalidValue;
   if (j.m <= 0) return cudaSuccess;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (j.m + kRows - 1) / kRows;
-  const int grid = static_cast<int>(tiles < sms ? tiles : sms);
-  cudaError_t err = cudaFuncSetAttribute(mlp_fused_jump_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(kSmemBytes));
-  if (err != cudaSuccess) return err;
-  mlp_fused_jump_kernel<<<grid, kThreads, kSmemBytes, s>>>(d, j, mean_label, std_label, status);
-  return cudaGetLastError();
+  return kc == 2 ? LaunchFused<2>(d, j, mean_label, std_label, status, s)
+                 : LaunchFused<3>(d, j, mean_label, std_label, status, s);
 }
 
 }  // namespace lmc

@@ -117,7 +117,7 @@ bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean
   return true;
 }
 bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream) {
-  if (mlp->path == 2 || !lmc::MlpFusedSupported(mlp->d)) return false;
+  if (mlp->path == 2 || lmc::MlpFusedChannels(mlp->d) != j.channels) return false;
   CudaCheck(cudaMemsetAsync(mlp->status, 0, sizeof(int), stream), "memset");
   CudaCheck(lmc::MlpFusedPredict(mlp->d, j, mlp->label_mean, mlp->label_std, mlp->status, stream),
             "fused surrogate kernel");
@@ -324,7 +324,7 @@ int lmc_mlp_set_inference_path(lmc_mlp *mlp, int path) {
     Require(mlp != nullptr, LMC_ERR_INVALID_ARGUMENT, "mlp is null");
     Require(path >= 0 && path <= 2, LMC_ERR_INVALID_ARGUMENT, "path must be 0, 1 or 2");
     Require(path != 1 || lmc::MlpTcSupported(mlp->d) || lmc::MlpFusedSupported(mlp->d), LMC_ERR_UNSUPPORTED,
-            "the tcgen05 kernels serve hidden 256 with in_features <= 256, or 2 members of 128 -> 128");
+            "the tcgen05 kernels serve hidden 256 with in_features <= 256, or 2 members of 128 / 192 -> 128");
     mlp->path = path;
   });
 }

@@ -16,6 +16,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 EL = ("Al", "Mg", "Zn")
+EL4 = ("Al", "Cu", "Mg", "Zn")
 
 
 def _pair_sites(N, n, a, b):
@@ -35,35 +36,37 @@ def _jumps_of(N, n, sites):
     return np.array(pairs, np.int64)
 
 
-def _solute_row(sp, sites, alpha, pad):
-    """Solute channels of one jump: per site, channel 0 for Mg, 1 for Zn, Al (base) and X all zero."""
-    ch = {alpha.index("Mg"): 0, alpha.index("Zn"): 1}
+def _solute_row(sp, sites, alpha, el, pad):
+    """Solute channels of one jump: per site one channel per element other than the base (Al),
+    in element order; Al and X sites all zero."""
+    ch = {alpha.index(e): i for i, e in enumerate(el[1:])}
+    w = len(el) - 1
     row = np.zeros(pad, np.uint16)
     for k, s in enumerate(sites):
         c = int(sp[s])
         if c in ch:
-            row[2 * k + ch[c]] = 0x3F80  # bf16 1.0
+            row[w * k + ch[c]] = 0x3F80  # bf16 1.0
     return row
 
 
-@pytest.mark.parametrize("pad", [128, 122])
-def test_solute_features_match_host_lists(native, pad):
+@pytest.mark.parametrize("el,pad", [(EL, 128), (EL, 122), (EL4, 192), (EL4, 180)])
+def test_solute_features_match_host_lists(native, el, pad):
     torch = pytest.importorskip("torch")
     from latticemontecarlo_gb300 import api, synthetic as S
     N = native
     n = 9
-    sp = S.make_lattice(n, {"Al": 0.5, "Mg": 0.25, "Zn": 0.25}, 5, 8, EL)
-    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 3), list(EL)))
+    sp = S.make_lattice(n, {e: 1.0 / len(el) for e in el}, 5, 8, el)
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(el, 3), list(el)))
     ctx.set_lattices([n], sp)
     ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
-    assert api.surrogate_feature_count(ctx) == 128
-    alpha = S.alphabet(EL)
+    assert api.surrogate_feature_count(ctx) == (128 if len(el) == 3 else 192)
+    alpha = S.alphabet(el)
     rng = np.random.default_rng(2)
     pairs = _jumps_of(N, n, rng.integers(0, sp.size, 25))
     got = api.surrogate_features(ctx, torch.from_numpy(pairs).cuda(), pad)
     got = got.contiguous().view(torch.int16).cpu().numpy().view(np.uint16)
     for i, (a, b) in enumerate(pairs):
-        assert np.array_equal(got[i], _solute_row(sp, _pair_sites(N, n, a, b), alpha, pad)), i
+        assert np.array_equal(got[i], _solute_row(sp, _pair_sites(N, n, a, b), alpha, el, pad)), i
 
 
 def test_solute_dataset_is_the_onehot_dataset(native):
@@ -86,25 +89,28 @@ def test_solute_dataset_is_the_onehot_dataset(native):
     assert not so[:, 118:].any()
 
 
-@pytest.fixture(scope="module")
-def trained(native):
-    """A compact ensemble (2 members, 128 -> 128 -> 128) trained briefly on solute features."""
+@pytest.fixture(scope="module", params=[EL, EL4], ids=["ternary", "quaternary"])
+def trained(native, request):
+    """A compact ensemble (2 members, in -> 128 -> 128, in = 128 / 192 for three / four
+    species) trained briefly on solute features."""
     torch = pytest.importorskip("torch")
     from latticemontecarlo_gb300 import api, synthetic as S
     N = native
+    el = request.param
     n = 12
-    el_frac = {"Al": 0.7, "Mg": 0.15, "Zn": 0.15}
-    sp = S.make_lattice(n, el_frac, 9, 0, EL)
-    alpha = S.alphabet(EL)
+    el_frac = {e: (0.7 if e == "Al" else 0.3 / (len(el) - 1)) for e in el}
+    sp = S.make_lattice(n, el_frac, 9, 0, el)
+    alpha = S.alphabet(el)
     x_code = alpha.index("X")
     rng = np.random.default_rng(4)
     vac = rng.choice(sp.size, 40, replace=False)
     sp[vac] = x_code
-    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 1234), list(EL)))
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(el, 1234), list(el)))
     ctx.set_lattices([n], sp)
     ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
-    x, ea, _, _ = api.surrogate_dataset(ctx, 1, 1 << 17, 0.1, 0.4, 128)
-    net = api.Surrogate(128, 128, 2, seed=3)
+    nin = api.surrogate_feature_count(ctx)
+    x, ea, _, _ = api.surrogate_dataset(ctx, 1, 1 << 17, 0.1, 0.4, nin)
+    net = api.Surrogate(nin, 128, 2, seed=3)
     net.set_label_scale(float(ea.mean()), float(ea.std()))
     net.train(x, ea, batch=4096, epochs=3, lr=2e-3, seed=4)
     return torch, api, N, ctx, net, sp, n, vac, alpha
@@ -133,9 +139,10 @@ def test_fused_kernel_matches_unfused_and_float64(trained):
     # every repetition of a jump gives the same bits
     assert np.array_equal(m_f.reshape(reps, -1), np.broadcast_to(m_f[:len(pairs)], (reps, len(pairs))))
     # the float64 network on the same feature rows
-    xs = api.surrogate_features(ctx, pd[:len(pairs)], 128)
+    nin = net.in_features
+    xs = api.surrogate_features(ctx, pd[:len(pairs)], nin)
     bits = xs.contiguous().view(torch.int16).cpu().numpy().view(np.uint16)
-    y = R.predict(net.params(), R.bf16_bits_to_float(bits), 128, 128, 2)
+    y = R.predict(net.params(), R.bf16_bits_to_float(bits), nin, 128, 2)
     mu, sd = (float(np.float32(v)) for v in net.label_scale)
     ok = ~has_x
     np.testing.assert_allclose(m_f[:len(pairs)][ok], (mu + sd * y.mean(0))[ok], rtol=0, atol=3e-3)
