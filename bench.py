@@ -630,14 +630,21 @@ def _vacancy_grid_lattice(n: int, spacing: int, fractions, seed: int, elements):
 
 
 def run_surrogate(args, device):
-    """Learned barrier surrogate (BF16 MLP ensembles on the tensor cores, plain-predictor fallback)
-    against the plain barrier predictor on the same lattice jumps: the 12 jumps of every vacancy of
-    a vacancy grid in a 96^3-cell lattice, in a dilute alloy (Al .96) and a solute-rich one (Al .70),
-    each with ensembles trained on barriers of random environments of that composition range. The
-    plain path is timed with its sparse evaluation (a vacancy's jumps evaluated once from the
-    solvent-relative sums; used for dilute lattices) and with the dense cluster sums; the surrogate
-    with the 4-member ensemble of the workload and with a 2-member one. Accuracy: MAE against the
-    plain predictor's FP64 barriers on the same jumps (fallback merged) and on held-out random
+    """Learned barrier surrogate against the plain barrier predictor on the same lattice jumps: the
+    12 jumps of every vacancy of a vacancy grid in a 192^3-cell lattice (1.33e6 jumps), in a dilute
+    alloy (Al .96) and a solute-rich one (Al .70), each with ensembles trained on 2e6 barriers of
+    random environments of that composition range:
+
+    * the workload's ensemble: 4 members of 256-256 GELU over the one-hot features (the streaming
+      tcgen05 inference kernel on feature rows written by a separate gather kernel);
+    * a compact ensemble: 2 members of 128-128 GELU over the solute-channel features, run by the
+      fused jump kernel (the lattice gather in its producer warps, both members' weights resident
+      in shared memory, tcgen05 with the hidden layer in tensor memory).
+
+    The plain path is timed with its sparse evaluation (a vacancy's jumps from the solvent-relative
+    sums) and with the dense cluster sums; the surrogate path includes the fallback (the plain dense
+    predictor on the jumps whose ensemble spread exceeds 10 meV). Accuracy: MAE against the plain
+    predictor's FP64 barriers on the same jumps (fallback merged) and on held-out random
     environments (network alone)."""
     import ctypes as C
 
@@ -651,12 +658,15 @@ def run_surrogate(args, device):
     coeffs = S.make_coefficients(el, 1234)
     model = api.Model.from_coefficients(coeffs, list(el))
     ctx = api.Context(model, device=device)
-    n, spacing = 96, 8
+    n, spacing = 192, 8
     # composition of the lattice, solute-fraction range of the training environments
     cases = {"dilute": ({"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, (0.0, 0.1)),
              "solute_rich": ({"Al": 0.70, "Mg": 0.15, "Zn": 0.15}, (0.2, 0.4))}
     peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] \
         if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
+    # networks: (encoding, hidden, members, epochs, lr, batch)
+    nets_spec = {"ensemble_4x256_onehot": (N.LMC_FEATURES_ONEHOT, 256, 4, args.surrogate_epochs, 2e-3, 4096),
+                 "ensemble_2x128_fused": (N.LMC_FEATURES_SOLUTE, 128, 2, args.surrogate_epochs_compact, 3e-3, 2048)}
 
     def timed(fn, reps):
         for _ in range(3):
@@ -668,40 +678,10 @@ def run_surrogate(args, device):
         torch.cuda.synchronize()
         return (time.perf_counter() - t) / reps
 
-    out_cases, roofline = {}, None
+    out_cases, roofline = {}, {}
     for case, (frac, (lo, hi)) in cases.items():
         sp, pairs = _vacancy_grid_lattice(n, spacing, frac, 77, el)
         ctx.set_lattices([n], sp)
-        nin = api.surrogate_feature_count(ctx)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        x, ea, _, _ = api.surrogate_dataset(ctx, 1, args.surrogate_samples, lo, hi, nin)
-        torch.cuda.synchronize()
-        rec = {"training_solute_range": [lo, hi], "dataset_s": time.perf_counter() - t0}
-        xt, _, eat, _ = api.surrogate_dataset(ctx, 99, 1 << 17, lo, hi, nin)
-        nets = {}
-        for members in (4, 2):
-            net = api.Surrogate(nin, 256, members, seed=1, device=device)
-            net.set_label_scale(float(ea.mean()), float(ea.std()))
-            t0 = time.perf_counter()
-            net.train(x, ea, batch=4096, epochs=args.surrogate_epochs, lr=2e-3, seed=2)
-            torch.cuda.synchronize()
-            t_train = time.perf_counter() - t0
-            flop_fwd = 2 * members * (nin * 256 + 256 * 256 + 256)
-            nets[members] = net
-            rec[f"ensemble_{members}"] = {
-                "train_s": t_train,
-                "train_tflops": 3 * flop_fwd * args.surrogate_samples * args.surrogate_epochs / t_train / 1e12,
-                "mae_mev_heldout_network_only": 1e3 * float((net.predict(xt)[0].double() - eat).abs().mean())}
-            if roofline is None and members == 4:
-                xb, _, _, _ = api.surrogate_dataset(ctx, 5, 1 << 20, lo, hi, nin)
-                t_mlp = timed(lambda: net.predict(xb), 5)
-                tf = flop_fwd * xb.shape[0] / t_mlp / 1e12
-                roofline = {"bound": "tensor", "kernel": "mlp_tc_infer_kernel (tcgen05, TMEM accumulators)",
-                            "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
-                            "network_barriers_per_s": xb.shape[0] / t_mlp}
-                del xb
-        del x, ea
         pd = torch.from_numpy(pairs).to(f"cuda:{device}")
         m = pd.shape[0]
         ea_plain = torch.empty(m, dtype=torch.float64, device=pd.device)
@@ -713,34 +693,71 @@ def run_surrogate(args, device):
             N.check(N.lib.lmc_ctx_synchronize(ctx._h))
 
         ctx.set_barrier_evaluation(N.LMC_EVAL_DENSE)
-        t_dense = timed(plain, 20)
+        t_dense = timed(plain, 10)
         ctx.set_barrier_evaluation(N.LMC_EVAL_SPARSE)
-        t_sparse = timed(plain, 20)
+        t_sparse = timed(plain, 10)
         t_plain = min(t_dense, t_sparse)
-        rec.update({"jumps": m, "plain_sparse_barriers_per_s": m / t_sparse,
-                    "plain_dense_barriers_per_s": m / t_dense})
-        for members, net in nets.items():
+        rec = {"training_solute_range": [lo, hi], "jumps": m, "plain_sparse_barriers_per_s": m / t_sparse,
+               "plain_dense_barriers_per_s": m / t_dense}
+        for name, (enc, hidden, members, epochs, lr, batch) in nets_spec.items():
+            ctx.set_surrogate_encoding(enc)
+            nin = api.surrogate_feature_count(ctx)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            x, ea, _, _ = api.surrogate_dataset(ctx, 1, args.surrogate_samples, lo, hi, nin)
+            torch.cuda.synchronize()
+            t_data = time.perf_counter() - t0
+            xt, _, eat, _ = api.surrogate_dataset(ctx, 99, 1 << 17, lo, hi, nin)
+            net = api.Surrogate(nin, hidden, members, seed=1, device=device)
+            net.set_label_scale(float(ea.mean()), float(ea.std()))
+            t0 = time.perf_counter()
+            net.train(x, ea, batch=batch, epochs=epochs, lr=lr, seed=2)
+            torch.cuda.synchronize()
+            t_train = time.perf_counter() - t0
+            flop_fwd = 2 * members * (nin * hidden + hidden * hidden + hidden)
+            r = {"features": nin, "hidden": hidden, "members": members, "epochs": epochs, "dataset_s": t_data,
+                 "train_s": t_train,
+                 "train_tflops": 3 * flop_fwd * args.surrogate_samples * epochs / t_train / 1e12,
+                 "mae_mev_heldout_network_only": 1e3 * float((net.predict(xt)[0].double() - eat).abs().mean())}
+            del x, ea, xt, eat
             res = {}
 
-            def surrogate():
-                res["out"] = api.surrogate_barriers(ctx, net, pd, 0.010)
+            def network():
+                res["n"] = api.surrogate_predict(ctx, net, pd)
 
-            t_sur = timed(surrogate, 20)
-            ea_sur, flag, nfb = res["out"]
-            rec[f"ensemble_{members}"].update({
-                "surrogate_barriers_per_s": m / t_sur, "over_best_plain": t_plain / t_sur,
-                "over_dense_plain": t_dense / t_sur, "fallback_fraction": nfb / m,
-                "mae_mev_with_fallback": 1e3 * float((ea_sur - ea_plain).abs().mean())})
+            t_net = timed(network, 10)
+
+            def surrogate():
+                res["s"] = api.surrogate_barriers(ctx, net, pd, 0.010)
+
+            t_sur = timed(surrogate, 10)
+            ea_sur, flag, nfb = res["s"]
+            r.update({"network_barriers_per_s": m / t_net, "network_tflops": flop_fwd * m / t_net / 1e12,
+                      "surrogate_barriers_per_s": m / t_sur, "over_best_plain": t_plain / t_sur,
+                      "over_dense_plain": t_dense / t_sur, "fallback_fraction": nfb / m,
+                      "mae_mev_with_fallback": 1e3 * float((ea_sur - ea_plain).abs().mean())})
+            rec[name] = r
+            if case == "solute_rich":
+                kernel = ("mlp_fused_jump_kernel (tcgen05, features gathered in the kernel)"
+                          if enc == N.LMC_FEATURES_SOLUTE else
+                          "surrogate_features_thread_kernel + mlp_tc_infer_kernel (tcgen05)")
+                tf = flop_fwd * m / t_net / 1e12
+                roofline[name] = {"bound": "tensor", "kernel": kernel, "achieved": tf, "peak": peak,
+                                  "unit": "TFLOP/s", "frac": tf / peak,
+                                  "flop_per_jump": flop_fwd, "timing": "wall clock per synchronised call"}
+            del net
+        ctx.set_surrogate_encoding(N.LMC_FEATURES_ONEHOT)
         out_cases[case] = rec
-    best = max(((c, k) for c in out_cases for k in ("ensemble_4", "ensemble_2")),
-               key=lambda ck: out_cases[ck[0]][ck[1]]["over_best_plain"])
+    cands = [(c, k) for c in out_cases for k in nets_spec
+             if out_cases[c][k]["mae_mev_with_fallback"] <= 5.0]
+    best = max(cands, key=lambda ck: out_cases[ck[0]][ck[1]]["over_best_plain"]) if cands else None
     return {
         "workload": f"the 12 jumps of each of {out_cases['dilute']['jumps'] // 12} vacancies in a {n}^3-cell FCC "
-                    "lattice per composition; surrogate MLP 192-256-256-1 GELU (bf16, fp32 accumulate), ensembles "
-                    "of 4 and 2 trained on 2e6 barriers of that composition range, fallback spread > 10 meV",
+                    f"lattice per composition; ensembles trained on {args.surrogate_samples:.0e} barriers of that "
+                    "composition range; fallback to the plain predictor where the ensemble spread exceeds 10 meV",
         "compositions": out_cases,
-        "best": {"composition": best[0], "ensemble": best[1], **out_cases[best[0]][best[1]]},
-        "timing": "wall clock over 20 device-synchronised calls",
+        "best": ({"composition": best[0], "ensemble": best[1], **out_cases[best[0]][best[1]]} if best else None),
+        "timing": "wall clock over 10 device-synchronised calls",
         "roofline": roofline,
     }
 
@@ -862,7 +879,9 @@ def main():
                     help="attempts of the reference-order CMC kernel (0 skips)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
-    ap.add_argument("--surrogate-epochs", type=int, default=30)
+    ap.add_argument("--surrogate-epochs", type=int, default=30, help="epochs of the 4 x 256 one-hot ensemble")
+    ap.add_argument("--surrogate-epochs-compact", type=int, default=80,
+                    help="epochs of the 2 x 128 solute-channel ensemble (fused jump kernel)")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")
     ap.add_argument("--chain-steps", type=int, default=100, help="chain KMC steps per replica (0 skips)")
     ap.add_argument("--single-steps", type=int, default=100_000, help="steps of the one-trajectory case (0 skips)")

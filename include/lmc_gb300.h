@@ -389,6 +389,19 @@ int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_s
 int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
 /* Vacancy site of every slot and per-lattice steps, time, energy (any may be NULL). */
 int lmc_kmc_multi_get_state(lmc_ctx *ctx, int64_t *vacancies, uint64_t *steps, double *time, double *energy);
+/* Surrogate-assisted multi-vacancy KMC: `steps` steps of lmc_kmc_multi_run on a context holding
+ * one lattice (lmc_kmc_multi_init with the Quartic barrier), with the barriers of the jumps whose
+ * environment changed taken from the ensemble `mlp` (the fused jump kernel: the context's
+ * solute-channel encoding, 2 members of hidden 128), and from the plain predictor where the
+ * ensemble spread exceeds threshold_ev or the network does not describe the jump. The energy
+ * change of each selected jump is the plain predictor's, so the energy sums stay exact; with
+ * threshold_ev = 0 the trajectory is lmc_kmc_multi_run's. trace (nullable, `steps` records)
+ * receives the events with the barrier used; plain_barrier (nullable, `steps` values) the plain
+ * predictor's barrier of each selected event; num_fallback (nullable) the jumps that took the
+ * plain predictor. No reference counterpart for the network (KineticMcAbstract.cpp:140-190 for
+ * the step loop). */
+int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, float threshold_ev,
+                                lmc_kmc_step *trace, double *plain_barrier, uint64_t *num_fallback);
 
 /* ------------------------------------------------------------------------- */
 /* Vacancy placed on every site: ExitTime's barrier queries (ansys)          */

@@ -361,6 +361,19 @@ class Context:
                                       trace.ctypes.data_as(C.POINTER(N.KmcStep)) if trace is not None else None))
         return trace
 
+    def kmc_multi_surrogate_run(self, model: "Surrogate", steps: int, threshold_ev: float = 0.010,
+                                trace: bool = False):
+        """Surrogate-assisted multi-vacancy KMC on the context's one lattice: (trace or None,
+        plain barrier of each selected event or None, jumps that took the plain predictor)."""
+        tr = np.zeros(steps, KmcTrace.DTYPE) if trace else None
+        plain = np.zeros(steps) if trace else None
+        nfb = np.zeros(1, np.uint64)
+        check(N.lib.lmc_kmc_multi_surrogate_run(
+            self._h, model._h, steps, threshold_ev,
+            tr.ctypes.data_as(C.POINTER(N.KmcStep)) if tr is not None else None,
+            ptr(plain, C.c_double) if plain is not None else None, ptr(nfb, C.c_uint64)))
+        return tr, plain, int(nfb[0])
+
     def kmc_multi_state(self):
         """(slot offsets [R + 1], vacancy site per slot, steps, time, energy per lattice)."""
         off = self._multi_off

@@ -128,6 +128,9 @@ struct lmc_ctx {
   std::vector<int> m_off_host;
   DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_trace;
   std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
+  // surrogate-assisted multi-vacancy KMC (lmc_kmc_multi_surrogate_run)
+  DevBuf su_pairs, su_dirty, su_rows, su_mean, su_spread, su_cum, su_ea, su_tgt, su_kmask, su_pair_ea, su_pair_de,
+      su_sel, su_fb, su_halt, su_trace, su_plain;
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
@@ -137,7 +140,8 @@ struct lmc_ctx {
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace, &sa_state, &sa_rng,
-                      &sa_trace})
+                      &sa_trace, &su_pairs, &su_dirty, &su_rows, &su_mean, &su_spread, &su_cum, &su_ea, &su_tgt,
+                      &su_kmask, &su_pair_ea, &su_pair_de, &su_sel, &su_fb, &su_halt, &su_trace, &su_plain})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -2133,6 +2137,150 @@ int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_s
     CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
     ctx->last_ms = ms;
     RaiseStatus(st, "multi-vacancy KMC run");
+  });
+}
+
+int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, float threshold_ev,
+                                lmc_kmc_step *trace, double *plain_barrier, uint64_t *num_fallback) {
+  return Guard([&] {
+    if (ctx) ctx->scan_fresh = false;  // atoms move
+    Require(ctx && mlp, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    Require(ctx->multi_ready, LMC_ERR_INVALID_ARGUMENT, "lmc_kmc_multi_init has not been called");
+    Require(ctx->num_replicas == 1, LMC_ERR_UNSUPPORTED, "the surrogate-assisted run takes one lattice");
+    Require(ctx->multi_kind == LMC_BARRIER_QUARTIC, LMC_ERR_UNSUPPORTED, "the surrogate predicts Quartic barriers");
+    Require(threshold_ev >= 0.f, LMC_ERR_INVALID_ARGUMENT, "threshold_ev < 0");
+    CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int nv = ctx->m_off_host.back();
+    const size_t rows = static_cast<size_t>(nv) * 12;
+    ctx->su_pairs.Ensure(16 * rows);
+    ctx->su_dirty.Ensure(4 * nv);
+    ctx->su_rows.Ensure(4);
+    ctx->su_mean.Ensure(4 * rows);
+    ctx->su_spread.Ensure(4 * rows);
+    ctx->su_cum.Ensure(8 * rows);
+    ctx->su_ea.Ensure(8 * rows);
+    ctx->su_tgt.Ensure(8 * rows);
+    ctx->su_kmask.Ensure(4 * nv);
+    ctx->su_pair_ea.Ensure(8 * rows);
+    ctx->su_pair_de.Ensure(8 * rows);
+    ctx->su_sel.Ensure(32);
+    ctx->su_fb.Ensure(8);
+    ctx->su_halt.Ensure(4);
+    // the network on the listed jumps, its row count on the device
+    lmc::FusedJumps j;
+    Require(FusedJumpsFor(ctx, 0, ctx->su_pairs.as<long long>(), static_cast<long long>(rows),
+                          ctx->su_mean.as<float>(), ctx->su_spread.as<float>(), &j) &&
+                lmc::MlpFusedChannels(lmc::MlpDevOf(mlp)) == j.channels,
+            LMC_ERR_UNSUPPORTED,
+            "the surrogate-assisted run needs the solute-channel encoding and a network the fused jump kernel serves "
+            "(2 members, hidden 128, 128 / 192 inputs)");
+    j.m_dev = ctx->su_rows.as<int>();
+    unsigned long long step0 = 0;
+    CudaCheck(cudaMemcpy(&step0, ctx->m_steps.p, 8, cudaMemcpyDeviceToHost), "D2H");
+    uint32_t key[2] = {0, 0};
+    CudaCheck(cudaMemcpy(key, ctx->m_key.p, 8, cudaMemcpyDeviceToHost), "D2H");
+    double temp = 0;
+    CudaCheck(cudaMemcpy(&temp, ctx->m_temp.p, 8, cudaMemcpyDeviceToHost), "D2H");
+    lmc::KmcSurrogateArgs a{};
+    a.vac_pos = ctx->m_pos.as<long long>();
+    a.nv = nv;
+    a.steps = ctx->m_steps.as<unsigned long long>();
+    a.time = ctx->m_time.as<double>();
+    a.energy = ctx->m_energy.as<double>();
+    a.temperature = temp;
+    a.key0 = key[0];
+    a.key1 = key[1];
+    a.replica = 0;
+    a.lat_off = ctx->offsets[0];
+    a.n = ctx->n[0];
+    a.barrier_kind = ctx->multi_kind;
+    a.threshold = threshold_ev;
+    a.mean = ctx->su_mean.as<float>();
+    a.spread = ctx->su_spread.as<float>();
+    a.pairs = ctx->su_pairs.as<long long>();
+    a.dirty = ctx->su_dirty.as<int>();
+    a.rows = ctx->su_rows.as<int>();
+    a.cum = ctx->su_cum.as<double>();
+    a.ea = ctx->su_ea.as<double>();
+    a.tgt = ctx->su_tgt.as<long long>();
+    a.kmask = ctx->su_kmask.as<uint32_t>();
+    a.pair_ea = ctx->su_pair_ea.as<double>();
+    a.pair_de = ctx->su_pair_de.as<double>();
+    a.sel_pair = ctx->su_sel.as<long long>();
+    a.sel_out = ctx->su_sel.as<double>() + 2;
+    a.fallbacks = ctx->su_fb.as<unsigned long long>();
+    a.halt = ctx->su_halt.as<int>();
+    a.trace_base = step0;
+    if (trace || plain_barrier) {
+      ctx->su_trace.Ensure(sizeof(lmc::KmcTraceRec) * steps);
+      ctx->su_plain.Ensure(8 * steps);
+      CudaCheck(cudaMemsetAsync(ctx->su_trace.p, 0, sizeof(lmc::KmcTraceRec) * steps, ctx->stream), "memset");
+      a.trace = ctx->su_trace.as<lmc::KmcTraceRec>();
+      a.plain_ea = ctx->su_plain.as<double>();
+      a.trace_len = steps;
+    }
+    a.stop_flag = ctx->d_stop;
+    a.status = ctx->status.as<int>();
+    std::copy(ctx->local_bits.begin(), ctx->local_bits.end(), a.local_bits);
+    ctx->ClearStatus();
+    CudaCheck(cudaMemsetAsync(ctx->su_fb.p, 0, 8, ctx->stream), "memset");
+    CudaCheck(cudaMemsetAsync(ctx->su_halt.p, 0, 4, ctx->stream), "memset");
+    CudaCheck(cudaMemsetAsync(const_cast<int *>(lmc::MlpStatusDev(mlp)), 0, sizeof(int), ctx->stream), "memset");
+    CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    // every slot listed at the start of the run, as kmc_multi_kernel evaluates every slot at the
+    // start of a launch
+    CudaCheck(lmc::LaunchKmcSurrogateList(ctx->t, a, ctx->stream), "surrogate KMC list kernel");
+    // one step = the network on the listed jumps, then the step kernel; chunks of steps are
+    // captured once into a CUDA graph and replayed (all state lives on the device)
+    const auto one_step = [&] {
+      CudaCheck(lmc::MlpFusedLaunch(mlp, j, ctx->stream), "fused surrogate kernel");
+      CudaCheck(lmc::LaunchKmcSurrogateStep(ctx->t, ctx->species.as<int8_t>(), a, ctx->stream),
+                "surrogate KMC step kernel");
+    };
+    constexpr uint64_t kChunk = 256;
+    uint64_t done = 0;
+    if (steps >= kChunk) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      CudaCheck(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed), "begin capture");
+      try {
+        for (uint64_t i = 0; i < kChunk; ++i) one_step();
+      } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      CudaCheck(cudaStreamEndCapture(ctx->stream, &graph), "end capture");
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      CudaCheck(ie, "graph instantiate");
+      try {
+        for (; done + kChunk <= steps; done += kChunk) CudaCheck(cudaGraphLaunch(exec, ctx->stream), "graph launch");
+      } catch (...) {
+        cudaGraphExecDestroy(exec);
+        throw;
+      }
+      cudaGraphExecDestroy(exec);
+    }
+    for (; done < steps; ++done) one_step();
+    CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    if (trace)
+      CudaCheck(cudaMemcpyAsync(trace, ctx->su_trace.p, sizeof(lmc::KmcTraceRec) * steps, cudaMemcpyDeviceToHost,
+                                ctx->stream),
+                "D2H trace");
+    if (plain_barrier)
+      CudaCheck(cudaMemcpyAsync(plain_barrier, ctx->su_plain.p, 8 * steps, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    int *h = ctx->Pinned();
+    CudaCheck(cudaMemcpyAsync(h, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    unsigned long long fb = 0;
+    CudaCheck(cudaMemcpyAsync(&fb, ctx->su_fb.p, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    const int st = ctx->ReadStatus();  // synchronises
+    float ms = 0;
+    CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
+    ctx->last_ms = ms;
+    if (num_fallback) *num_fallback = fb;
+    Require(h[0] == 0, LMC_ERR_STOPPED, "surrogate inference: a tensor-core wait expired");
+    RaiseStatus(st, "surrogate-assisted multi-vacancy KMC run");
   });
 }
 

@@ -2677,6 +2677,245 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
 }
 
+// ---------------------------------------------------------------------------
+// K4s: surrogate-assisted multi-vacancy KMC on one lattice, one step per launch,
+// interleaved with the fused network kernel (mlp_fused.cu) that evaluates the
+// jumps listed by the previous step (both captured in a CUDA graph). Per step:
+//  1. the listed slots' 12 events (one warp per slot): the ensemble mean for the
+//     barrier, the plain predictor (dense sums, FP64 epilogue) where the ensemble
+//     spread exceeds the threshold or the network does not describe the jump; a
+//     jump onto a vacancy has rate 0; rates, id order and inclusive scan as in
+//     kmc_multi_kernel;
+//  2. warp 0: selection over all slots exactly as kmc_multi_kernel (Philox draw of
+//     counter = step), the plain predictor's energy change of the selected jump
+//     (before the move: the energy sums stay exact), the move, and the list of
+//     slots whose neighbourhood holds a changed site with their 12 jumps each for
+//     the next step's network launch.
+// With threshold 0 every jump takes the plain predictor and the trajectory is
+// kmc_multi_kernel's (dense evaluation). A stop or an error sets *halt, after
+// which the remaining launches of the run return at once.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMultiWarps * 32, 1)
+    kmc_surrogate_list_kernel(const __grid_constant__ DevTables t, const __grid_constant__ KmcSurrogateArgs a) {
+  // every slot listed, 12 jumps each in direction order (the start of a run)
+  for (int i = threadIdx.x; i < a.nv * 12; i += blockDim.x) {
+    const int v = i / 12, d = i % 12;
+    const long long pos = a.vac_pos[v];
+    const int8_t *o = t.dir + d * 4;
+    a.pairs[2 * i] = pos;
+    a.pairs[2 * i + 1] = NeighborId(SiteCoord(pos, a.n), o[0], o[1], o[2], a.n);
+    if (d == 0) a.dirty[v] = v;
+  }
+  if (threadIdx.x == 0) *a.rows = a.nv * 12;
+}
+
+__global__ void __launch_bounds__(kMultiWarps * 32, 1)
+    kmc_surrogate_step_kernel(const __grid_constant__ DevTables t, int8_t *species,
+                              const __grid_constant__ KmcSurrogateArgs a) {
+  __shared__ SmallTables s_small;
+  __shared__ __align__(16) int8_t s_arr[kMultiWarps * kArr];
+  __shared__ uint32_t s_bits[kLocalBitWords];
+  __shared__ double s_incl[kMaxMultiVac];
+  if (*a.halt) return;  // block-uniform, before any barrier
+  StageSmall(t, &s_small);
+  for (int i = threadIdx.x; i < kLocalBitWords; i += blockDim.x) s_bits[i] = a.local_bits[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = a.n, nv = a.nv;
+  int8_t *lat = species + a.lat_off;
+  const int x_code = t.x_code;
+  const double beta = 1.0 / kBoltzmannEv / a.temperature;
+  const ExpConsts ec{t.exp_tab, t.exp_l1, t.exp_l2};
+  int8_t *st = s_arr + warp * kArr;
+  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  constexpr unsigned kVacancyBits = kStatusXInEnv | kStatusBadCluster;  // a second vacancy contributes nothing
+  unsigned bad_all = 0;
+  unsigned long long nfb = 0;
+  // ---- phase 1: the listed slots' events ----
+  const int listed = *a.rows / 12;
+  for (int q = warp; q < listed; q += kMultiWarps) {
+    const int v = a.dirty[q];
+    const int row = q * 12 + (lane < 12 ? lane : 0);
+    long long id = 0x7fffffffffffffffLL;
+    bool onto_x = true, need = false;
+    double ea = 0.0;
+    if (lane < 12) {
+      id = a.pairs[2 * row + 1];
+      onto_x = lat[id] == x_code;
+      const float mu = a.mean[row], sp = a.spread[row];
+      if (!onto_x) {
+        if (sp <= a.threshold && isfinite(mu)) ea = static_cast<double>(mu);
+        else need = true;
+      }
+    }
+    unsigned fbm = __ballot_sync(0xffffffffu, need);
+    nfb += __popc(fbm);
+    while (fbm) {
+      const int l = __ffs(fbm) - 1;
+      fbm &= fbm - 1;
+      bad_all |= DensePairBarrier(t, lat, n, a.pairs, q * 12 + l, a.barrier_kind, t.de_cl, t.mmm_cl, t.mm2_cl,
+                                  &s_small, st, rm, rf, rb, a.pair_ea, a.pair_de, nullptr, nullptr, lane) &
+                 ~kVacancyBits;
+    }
+    if (need) ea = a.pair_ea[row];
+    const double k = (lane < 12 && !onto_x) ? ExpFast(-ea * beta, ec) : 0.0;
+    // events in id order (the sorted 1NN list), then their inclusive scan
+    int rank = 0;
+    for (int q2 = 0; q2 < 12; ++q2) {
+      const long long oid = __shfl_sync(0xffffffffu, id, q2);
+      rank += (q2 != lane) && (oid < id);
+    }
+    int src = 0;
+    for (int q2 = 0; q2 < 12; ++q2)
+      if (__shfl_sync(0xffffffffu, rank, q2) == lane) src = q2;
+    const double k_s = __shfl_sync(0xffffffffu, k, src);
+    const double ea_s = __shfl_sync(0xffffffffu, ea, src);
+    const long long id_s = __shfl_sync(0xffffffffu, id, src);
+    double cum = lane < 12 ? k_s : 0.0;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      const double u = __shfl_up_sync(0xffffffffu, cum, o);
+      if (lane >= o) cum += u;
+    }
+    const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
+    if (lane < 12) {
+      a.cum[v * 12 + lane] = cum;
+      a.ea[v * 12 + lane] = ea_s;
+      a.tgt[v * 12 + lane] = id_s;
+    }
+    if (lane == 0) a.kmask[v] = kpos;
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- phase 2: selection, energy change, move and the next list (warp 0) ----
+  if (warp == 0) {
+    const unsigned long long step = *a.steps;
+    bool halt = false;
+    if (a.stop_flag && (step & 63) == 0 && *a.stop_flag) {
+      bad_all |= kStatusStopped;
+      halt = true;
+    }
+    if (!halt) {
+      const uint4 xr = PhiloxRound10(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32),
+                                     static_cast<uint32_t>(a.replica), 0x4b4d43u, a.key0, a.key1);
+      const double nlog_u1 = -log(U01Open(xr.x, xr.y));
+      const double u2 = U01(xr.z, xr.w);
+      const int chunks = (nv + 31) >> 5;
+      double run = 0.0;
+      for (int c = 0; c < chunks; ++c) {
+        const int v = c * 32 + lane;
+        double sc = v < nv ? a.cum[v * 12 + 11] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const double u = __shfl_up_sync(0xffffffffu, sc, o);
+          if (lane >= o) sc += u;
+        }
+        if (v < nv) s_incl[v] = run + sc;
+        run = run + __shfl_sync(0xffffffffu, sc, 31);
+      }
+      const double total = run;
+      __syncwarp();
+      const double xs = __dmul_rn(u2, total);  // not contracted with the subtraction below
+      int vsel = -1, vlast = -1;
+      for (int c = 0; c < chunks; ++c) {
+        const int v = c * 32 + lane;
+        const bool pos = v < nv && a.kmask[v] != 0;
+        const unsigned hit = __ballot_sync(0xffffffffu, pos && s_incl[v] >= xs);
+        const unsigned any = __ballot_sync(0xffffffffu, pos);
+        if (vsel < 0 && hit) vsel = c * 32 + __ffs(hit) - 1;
+        if (any) vlast = c * 32 + 31 - __clz(any);
+      }
+      if (vsel < 0) vsel = vlast;
+      if (vsel < 0 || !(total > 0.0) || !isfinite(total)) {
+        bad_all |= kStatusNumeric;
+        halt = true;
+      } else {
+        const double y = __dsub_rn(xs, vsel > 0 ? s_incl[vsel - 1] : 0.0);
+        const unsigned km = a.kmask[vsel];
+        const bool pos = lane < 12 && ((km >> lane) & 1u);
+        const unsigned hit = __ballot_sync(0xffffffffu, pos && a.cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
+        const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
+        const int e = vsel * 12 + sel;
+        const long long p_old = a.vac_pos[vsel];
+        const long long tgt = a.tgt[e];
+        const double ea_sel = a.ea[e];
+        // the plain predictor's energy change (and barrier) of the selected jump, before the move
+        if (lane == 0) {
+          a.sel_pair[0] = p_old;
+          a.sel_pair[1] = tgt;
+        }
+        __syncwarp();
+        bad_all |= DensePairBarrier(t, lat, n, a.sel_pair, 0, a.barrier_kind, t.de_cl, t.mmm_cl, t.mm2_cl, &s_small,
+                                    st, rm, rf, rb, a.sel_out, a.sel_out + 1, nullptr, nullptr, lane) &
+                   ~kVacancyBits;
+        const double ea_plain = a.sel_out[0], de_sel = a.sel_out[1];
+        const double time = *a.time + nlog_u1 * RcpFast(total * kPrefactor);
+        const double energy = *a.energy + de_sel;
+        const H3 h_old = SiteCoord(p_old, n), h_new = SiteCoord(tgt, n);
+        if (lane == 0) {
+          lat[p_old] = lat[tgt];  // Config::LatticeJump
+          lat[tgt] = static_cast<int8_t>(x_code);
+          a.vac_pos[vsel] = tgt;
+          *a.time = time;
+          *a.energy = energy;
+          *a.steps = step + 1;
+          const unsigned long long ti = step - a.trace_base;
+          if (a.trace && ti < a.trace_len) {
+            KmcTraceRec rec;
+            rec.vacancy = p_old;
+            rec.target = tgt;
+            rec.selected = sel;
+            rec.slot = vsel;
+            rec.ea = ea_sel;
+            rec.de = de_sel;
+            rec.total_rate = total;
+            rec.time = time;
+            rec.energy = energy;
+            a.trace[ti] = rec;
+            if (a.plain_ea) a.plain_ea[ti] = ea_plain;
+          }
+        }
+        __syncwarp();
+        // slots to re-evaluate: the moved one and those whose neighbourhood holds a changed
+        // site, with their 12 jumps in direction order for the next network launch
+        int nd2 = 0;
+        for (int c = 0; c < chunks; ++c) {
+          const int v = c * 32 + lane;
+          bool d = false;
+          if (v < nv) {
+            const H3 hv = v == vsel ? h_new : SiteCoord(a.vac_pos[v], n);
+            d = v == vsel ||
+                InLocal(s_bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
+                        WrapDelta(h_old.z - hv.z, n)) ||
+                InLocal(s_bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
+                        WrapDelta(h_new.z - hv.z, n));
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, d);
+          if (d) a.dirty[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
+          nd2 += __popc(m);
+        }
+        __syncwarp();
+        for (int i = 0; i < nd2; ++i) {
+          const int v = a.dirty[i];
+          if (lane < 12) {
+            const long long pv = v == vsel ? tgt : a.vac_pos[v];
+            const int8_t *o = t.dir + lane * 4;
+            a.pairs[2 * (i * 12 + lane)] = pv;
+            a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : SiteCoord(pv, n), o[0], o[1], o[2], n);
+          }
+        }
+        if (lane == 0) *a.rows = nd2 * 12;
+      }
+    }
+    if (halt && lane == 0) *a.halt = 1;
+  }
+  const unsigned bad = __reduce_or_sync(0xffffffffu, bad_all);
+  if (lane == 0) {
+    if (nfb) atomicAdd(a.fallbacks, nfb);
+    if (bad) atomicOr(a.status, static_cast<int>(bad));
+  }
+}
+
 constexpr int kCmcRefMaxBatch = 256;
 // The reference's mt19937_64 stream read by a whole warp: the current block of
 // 312 raw state words and the next one (twisted ahead, warp-parallel) sit in
@@ -3618,6 +3857,19 @@ cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiAr
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
   if (err != cudaSuccess) return err;
   kern<<<a.num_replicas, kMultiWarps * 32, sm, stream>>>(t, species, a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchKmcSurrogateList(const DevTables &t, const KmcSurrogateArgs &a, cudaStream_t stream) {
+  if (a.nv < 1 || a.nv > kMaxMultiVac) return cudaErrorInvalidValue;
+  kmc_surrogate_list_kernel<<<1, kMultiWarps * 32, 0, stream>>>(t, a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchKmcSurrogateStep(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a,
+                                   cudaStream_t stream) {
+  if (a.nv < 1 || a.nv > kMaxMultiVac) return cudaErrorInvalidValue;
+  kmc_surrogate_step_kernel<<<1, kMultiWarps * 32, 0, stream>>>(t, species, a);
   return cudaGetLastError();
 }
 

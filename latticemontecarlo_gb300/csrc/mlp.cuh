@@ -126,6 +126,7 @@ struct FusedJumps {
   int n;
   const long long *pairs;    // [m][2] (vacancy site, migrant site)
   long long m;
+  const int *m_dev;          // nullable: the row count on the device (m is then its upper bound)
   const int8_t *mmm_off;     // [12][58][4] MMM-ordered offsets per jump direction (half units)
   const int8_t *dir_of;      // [27] 1NN direction of an offset, -1 none
   int channels;              // channels per site (2 or 3)
@@ -152,6 +153,9 @@ bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean
 // The fused jump kernel queued on `stream` (status word as above); false when this network
 // or the inference path setting does not allow it.
 bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream);
+// The fused jump kernel alone (no status reset: stream capture of repeated launches).
+cudaError_t MlpFusedLaunch(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream);
+const MlpDev &MlpDevOf(const lmc_mlp *mlp);
 int MlpInputs(const lmc_mlp *mlp);
 const int *MlpStatusDev(const lmc_mlp *mlp);
 }  // namespace lmc

@@ -167,16 +167,19 @@ __device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, co
   return acc;
 }
 
-// Producer of half kHalf of every row of the CTA's tiles: sites [32 kHalf, 32 kHalf + 32)
-// of the row (MMM-ordered environment, then the migrant; past site 58 nothing), i.e.
-// features [kIn / 2 kHalf, kIn / 2 (kHalf + 1)) (feature kC s + c is channel c of site s).
-// Returns the status bits of rejected pairs.
-template <int kC, int kHalf>
-__device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *bars, unsigned char *sx,
-                                                long long tiles, int warp, int lane, volatile int *abort) {
+// Producer of half `half` (warps 0-3: 0, warps 4-7: 1) of every row of the CTA's tiles:
+// sites [32 half, 32 half + 32) of the row (MMM-ordered environment, then the migrant; past
+// site 58 nothing), i.e. features [kIn / 2 half, kIn / 2 (half + 1)) (feature kC s + c is
+// channel c of site s). One code path for both halves keeps the kernel's instruction
+// footprint small. Returns the status bits of rejected pairs.
+template <int kC>
+__device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, long long m_rows, FusedBars *bars,
+                                                unsigned char *sx, long long tiles, int warp, int lane,
+                                                volatile int *abort) {
   constexpr int kIn = Shape<kC>::kIn;
   constexpr int kHalfFeat = kIn / 2;
   static_assert(kHalfFeat == kC * kHalfSites, "a half row is 32 sites");
+  const int half = warp >> 2;
   const int r = (warp & 3) * 32 + lane;
   const int n = j.n;
   const long long nsites = 4LL * n * n * n;
@@ -186,7 +189,7 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
     const long long row = tile * kRows + r;
     int code[kHalfSites];
     bool fallback = true;
-    if (row < j.m) {
+    if (row < m_rows) {
       const long long a = __ldg(&j.pairs[2 * row]), b = __ldg(&j.pairs[2 * row + 1]);
       unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
       int di = -1;
@@ -199,13 +202,13 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
           di = __ldg(&j.dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
         if (di < 0) bad = kStatusNotNeighbor;
       }
-      if (kHalf == 0) bad_all |= bad;
+      if (half == 0) bad_all |= bad;
       if (!bad) {
         // the offsets of this direction, 4 bytes (dx, dy, dz, 0) per site
         const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
 #pragma unroll
         for (int k = 0; k < kHalfSites; ++k) {
-          const int site = kHalf * kHalfSites + k;
+          const int site = half * kHalfSites + k;
           int c = -1;
           if (site < kEnvSites) {
             const int o = __ldg(off + site);
@@ -219,7 +222,7 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
         unsigned seen = 0;
 #pragma unroll
         for (int k = 0; k < kHalfSites; ++k)
-          if (kHalf * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
+          if (half * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
         fallback = (seen & j.fallback_codes) != 0;
       }
     }
@@ -234,21 +237,21 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, FusedBars *
       uint32_t w[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int f = kHalf * kHalfFeat + 8 * c + 2 * e;  // features f (low half), f + 1 (high half)
+        const int f = 8 * c + 2 * e;  // features f (low half), f + 1 (high half) of this half row
         uint32_t word;
         if constexpr (kC == 2) {
-          const int k = (f - kHalf * kHalfFeat) / 2;  // site of features f, f + 1 in this half
+          const int k = f / 2;  // site of features f, f + 1
           word = code[k] >= 0 ? bars->site_word[code[k] & 7] : 0u;
         } else {
-          const int k0 = (f - kHalf * kHalfFeat) / kC, k1 = (f + 1 - kHalf * kHalfFeat) / kC;
+          const int k0 = f / kC, k1 = (f + 1) / kC;
           const int ch0 = bars->chan[code[k0] & 7], ch1 = bars->chan[code[k1] & 7];
           word = ((code[k0] >= 0 && ch0 == f % kC) ? 0x3F80u : 0u) |
                  ((code[k1] >= 0 && ch1 == (f + 1) % kC) ? 0x3F800000u : 0u);
         }
-        if (f + 1 == kIn - 1) word |= 0x3F800000u;  // the last feature is 1: the bias column
+        if (f + 1 == kHalfFeat - 1 && half == 1) word |= 0x3F800000u;  // the last feature is 1: the bias column
         w[e] = word;
       }
-      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, kHalf * (kHalfFeat / 8) + c)) =
+      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, half * (kHalfFeat / 8) + c)) =
           make_uint4(w[0], w[1], w[2], w[3]);
     }
     const unsigned fb = __ballot_sync(0xffffffffu, fallback);
@@ -303,7 +306,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   FenceAfterSync();
   const uint32_t tmem = bars->tmem;
-  const long long tiles = (j.m + kRows - 1) / kRows;
+  const long long m_rows = j.m_dev ? min(j.m, static_cast<long long>(*j.m_dev)) : j.m;
+  const long long tiles = (m_rows + kRows - 1) / kRows;
 
   if (warp < kProdWarps) {
     // ---- producer: weights once, then half a row per thread and tile ----
@@ -312,8 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       BulkCopy(sw1, d.w1_tiles, S::kW1Bytes, &bars->w_full);
       BulkCopy(sw2, d.w2_tiles, kW2Bytes, &bars->w_full);
     }
-    const unsigned bad_all = warp < 4 ? ProduceRows<kC, 0>(j, bars, sx, tiles, warp, lane, abort)
-                                      : ProduceRows<kC, 1>(j, bars, sx, tiles, warp, lane, abort);
+    const unsigned bad_all = ProduceRows<kC>(j, m_rows, bars, sx, tiles, warp, lane, abort);
     if (bad_all) atomicOr(j.pair_status, static_cast<int>(bad_all));
     // the weight copies must land before the CTA exits
     if (warp == 0 && lane == 0 && !WaitDrain(&bars->w_full, 0)) *abort = 1;
@@ -419,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           ymax = fmaxf(ymax, y);
         }
       }
-      if (ok && q == 0 && row < j.m) {
+      if (ok && q == 0 && row < m_rows) {
         j.mean[row] = mean_label + std_label * ysum * (1.0f / kMembers);
         j.spread[row] = fallback ? __int_as_float(0x7f800000) : std_label * (ymax - ymin);
       }

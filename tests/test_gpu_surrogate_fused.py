@@ -157,3 +157,85 @@ def test_fused_kernel_rejects_non_jumps(trained):
     pd = torch.from_numpy(_jumps_of(N, n, vac[:2])).cuda()
     m, s = api.surrogate_predict(ctx, net, pd)
     assert torch.isfinite(m).all()
+
+
+def _vacancy_grid(S, n, spacing, frac, seed, el):
+    """Vacancies on every site whose half-lattice coordinates are multiples of `spacing` (no jump
+    environment holds a second vacancy), the rest i.i.d. from `frac`; with each vacancy's 12 jumps."""
+    alpha = S.alphabet(el)
+    rng = np.random.default_rng(seed)
+    names = list(frac)
+    p = np.array([frac[k] for k in names], float)
+    sp = np.array([alpha.index(k) for k in names], np.int8)[rng.choice(len(names), size=4 * n ** 3, p=p / p.sum())]
+    m = 2 * n
+    g = np.arange(0, m, spacing)
+    hx, hy, hz = (a.ravel() for a in np.meshgrid(g, g, g, indexing="ij"))
+    vac = hx * 2 * n * n + hy * n + hz // 2
+    sp[vac] = alpha.index("X")
+    dirs = [(a, b, 0) for a in (-1, 1) for b in (-1, 1)] + [(a, 0, b) for a in (-1, 1) for b in (-1, 1)] + \
+        [(0, a, b) for a in (-1, 1) for b in (-1, 1)]
+    pairs = [np.stack([vac, ((hx + d[0]) % m) * 2 * n * n + ((hy + d[1]) % m) * n + ((hz + d[2]) % m) // 2], 1)
+             for d in dirs]
+    return sp, np.stack(pairs, 1).reshape(-1, 2).astype(np.int64)
+
+
+def test_trained_network_gain(native):
+    """What the trained network gains over the method without it. On a solute-rich lattice (Al .70,
+    Mg .15, Zn .15: the plain predictor's sparse lists overflow and every jump takes the dense
+    cluster sums) the compact ensemble, trained on 2e6 plain barriers of random environments with
+    20-40 % solutes, gives the barriers of the lattice's jumps (fallback to the plain predictor where
+    its two members differ by more than 10 meV) at least twice as fast as the best plain evaluation,
+    within 5 meV mean absolute error of the plain FP64 barriers."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    import time
+    from latticemontecarlo_gb300 import api, synthetic as S
+    N = native
+    ctx = api.Context(api.Model.from_coefficients(S.make_coefficients(EL, 1234), list(EL)))
+    n = 128
+    sp, pairs = _vacancy_grid(S, n, 8, {"Al": 0.70, "Mg": 0.15, "Zn": 0.15}, 77, EL)
+    ctx.set_lattices([n], sp)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
+    x, ea, _, _ = api.surrogate_dataset(ctx, 1, 2_000_000, 0.2, 0.4, 128)
+    net = api.Surrogate(128, 128, 2, seed=1)
+    net.set_label_scale(float(ea.mean()), float(ea.std()))
+    net.train(x, ea, batch=2048, epochs=80, lr=3e-3, seed=2)
+    del x, ea
+    pd = torch.from_numpy(pairs).cuda()
+    m = pd.shape[0]
+    ea_p = torch.empty(m, dtype=torch.float64, device="cuda")
+    de_p = torch.empty_like(ea_p)
+
+    def plain():
+        N.check(N.lib.lmc_barrier_batch_device(ctx._h, 0, 0, C.c_void_p(pd.data_ptr()), m,
+                                               C.c_void_p(ea_p.data_ptr()), C.c_void_p(de_p.data_ptr())))
+        N.check(N.lib.lmc_ctx_synchronize(ctx._h))
+
+    out = {}
+
+    def surrogate():
+        out["s"] = api.surrogate_barriers(ctx, net, pd, 0.010)
+
+    def median_time(fn):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(9):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        return float(np.median(ts))
+
+    t_plain = []
+    for ev in (N.LMC_EVAL_SPARSE, N.LMC_EVAL_DENSE):
+        ctx.set_barrier_evaluation(ev)
+        t_plain.append(median_time(plain))
+    t_sur = median_time(surrogate)
+    ea_s, _, nfb = out["s"]
+    mae = float((ea_s - ea_p).abs().mean())
+    gain = min(t_plain) / t_sur
+    info = dict(gain=gain, mae_mev=1e3 * mae, fallback=nfb / m, plain_per_s=m / min(t_plain), surrogate_per_s=m / t_sur)
+    assert mae <= 0.005, info
+    assert gain >= 2.0, info
