@@ -571,6 +571,8 @@ def run_large(args, device):
             "launch": "one block of 8 warps (a single lattice is one sequential trajectory)",
             "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
+        if args.surrogate_samples > 0:
+            out["kmc_multi_vacancy_surrogate"] = run_large_surrogate(args, ctx, sp, T)
     if not args.no_cpu_baseline:
         # the oracle's EnergyPredictor census (serial, as the reference's) and CanonicalMcOmp on all
         # host cores, on the same lattice; clusters holding two vacancies count nothing, as on the GPU
@@ -599,6 +601,51 @@ def run_large(args, device):
                                                     f"lattice with its vacancies filled by Al, oracle C restatement, "
                                                     f"{w:.1f} s"}
     return out
+
+
+def run_large_surrogate(args, ctx, sp, T):
+    """Surrogate-assisted multi-vacancy KMC on the large lattice (the same lattice, seed and
+    temperature as the plain run): the compact ensemble (2 members of 128-128 GELU over the
+    solute-channel features, 192 for the four species) trained on barriers of random environments
+    with 0-15 % solutes; per step the fused jump kernel evaluates the jumps of the vacancies whose
+    neighbourhood changed, the plain predictor takes the jumps where the ensemble spread exceeds
+    10 meV, and the energy change of each selected jump is the plain predictor's."""
+    import torch
+
+    from latticemontecarlo_gb300 import api
+    from latticemontecarlo_gb300 import _native as N
+    from latticemontecarlo_gb300 import synthetic as S
+
+    L = S.LARGE
+    ctx.set_lattices([L["n"]], sp)
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_SOLUTE)
+    nin = api.surrogate_feature_count(ctx)
+    x, ea, _, _ = api.surrogate_dataset(ctx, 1, args.surrogate_samples, 0.0, 0.15, nin)
+    net = api.Surrogate(nin, 128, 2, seed=1, device=ctx.device)
+    net.set_label_scale(float(ea.mean()), float(ea.std()))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.train(x, ea, batch=2048, epochs=args.surrogate_epochs_compact, lr=3e-3, seed=2)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del x, ea
+    ctx.kmc_multi_init([T], seed=3)
+    # a traced run: the barriers used for the selected events against the plain predictor's
+    traced = 20_000
+    tr, plain_ea, nfb_traced = ctx.kmc_multi_surrogate_run(net, traced, 0.010, trace=True)
+    err = np.abs(tr["ea"] - plain_ea)
+    events = args.large_kmc_events
+    _, fb = ctx.kmc_multi_surrogate_run(net, events, 0.010)[1:]
+    ms = ctx.last_run_ms()
+    off, vac, steps, tm, en = ctx.kmc_multi_state()
+    ctx.set_surrogate_encoding(N.LMC_FEATURES_ONEHOT)
+    return {"events": events, "ms": ms, "value": events / (ms / 1e3), "unit": "events/s",
+            "simulated_time_s": float(tm[0]), "network": f"2 x {nin}-128-128-1, fused jump kernel",
+            "train_s": t_train, "fallback_jumps_per_event": fb / events,
+            "selected_event_barrier_mae_mev": 1e3 * float(err.mean()),
+            "selected_event_barrier_max_err_mev": 1e3 * float(err.max()), "traced_events": traced,
+            "launch": "per step: the fused network kernel on the re-evaluated slots' jumps, then a one-block "
+                      "step kernel; chunks of 256 steps captured in a CUDA graph"}
 
 
 def _vacancy_grid_lattice(n: int, spacing: int, fractions, seed: int, elements):
@@ -658,7 +705,7 @@ def run_surrogate(args, device):
     coeffs = S.make_coefficients(el, 1234)
     model = api.Model.from_coefficients(coeffs, list(el))
     ctx = api.Context(model, device=device)
-    n, spacing = 192, 8
+    n, spacing = args.surrogate_n, 8
     # composition of the lattice, solute-fraction range of the training environments
     cases = {"dilute": ({"Al": 0.96, "Mg": 0.02, "Zn": 0.02}, (0.0, 0.1)),
              "solute_rich": ({"Al": 0.70, "Mg": 0.15, "Zn": 0.15}, (0.2, 0.4))}
@@ -880,6 +927,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--surrogate-samples", type=int, default=2_000_000, help="0 skips the surrogate block")
     ap.add_argument("--surrogate-epochs", type=int, default=30, help="epochs of the 4 x 256 one-hot ensemble")
+    ap.add_argument("--surrogate-n", type=int, default=192, help="cube edge of the surrogate block's lattices")
     ap.add_argument("--surrogate-epochs-compact", type=int, default=80,
                     help="epochs of the 2 x 128 solute-channel ensemble (fused jump kernel)")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch (profiles/)")

@@ -129,8 +129,8 @@ struct lmc_ctx {
   DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_trace;
   std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
   // surrogate-assisted multi-vacancy KMC (lmc_kmc_multi_surrogate_run)
-  DevBuf su_pairs, su_dirty, su_rows, su_mean, su_spread, su_cum, su_ea, su_tgt, su_kmask, su_pair_ea, su_pair_de,
-      su_sel, su_fb, su_halt, su_trace, su_plain;
+  DevBuf su_pairs, su_dirty, su_rows, su_mean, su_spread, su_cum, su_ea, su_tgt, su_kmask, su_pair_ea, su_fb,
+      su_halt, su_trace, su_plain;
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
@@ -141,7 +141,7 @@ struct lmc_ctx {
       b->Free();
     for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace, &sa_state, &sa_rng,
                       &sa_trace, &su_pairs, &su_dirty, &su_rows, &su_mean, &su_spread, &su_cum, &su_ea, &su_tgt,
-                      &su_kmask, &su_pair_ea, &su_pair_de, &su_sel, &su_fb, &su_halt, &su_trace, &su_plain})
+                      &su_kmask, &su_pair_ea, &su_fb, &su_halt, &su_trace, &su_plain})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
     for (auto &b : sparse_bufs) b.Free();
@@ -2162,8 +2162,6 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     ctx->su_tgt.Ensure(8 * rows);
     ctx->su_kmask.Ensure(4 * nv);
     ctx->su_pair_ea.Ensure(8 * rows);
-    ctx->su_pair_de.Ensure(8 * rows);
-    ctx->su_sel.Ensure(32);
     ctx->su_fb.Ensure(8);
     ctx->su_halt.Ensure(4);
     // the network on the listed jumps, its row count on the device
@@ -2205,9 +2203,6 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     a.tgt = ctx->su_tgt.as<long long>();
     a.kmask = ctx->su_kmask.as<uint32_t>();
     a.pair_ea = ctx->su_pair_ea.as<double>();
-    a.pair_de = ctx->su_pair_de.as<double>();
-    a.sel_pair = ctx->su_sel.as<long long>();
-    a.sel_out = ctx->su_sel.as<double>() + 2;
     a.fallbacks = ctx->su_fb.as<unsigned long long>();
     a.halt = ctx->su_halt.as<int>();
     a.trace_base = step0;

@@ -95,18 +95,20 @@ struct JumpAcc {
 //       W(end tuple) - W(start tuple)   (clusters with both pair sites cancel)
 //   d : sum over MMM clusters of the D (Quartic) or e0 (E0) weights
 //   ks: sum over MM2 clusters of the forward and backward lists (Quartic)
+// `lane` and `stride`: this thread's first cluster and the step (a warp: lane, 32; a block:
+// thread index, block size).
 template <bool kQuartic>
 __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const int8_t *st, const int8_t *rm,
                                             const int8_t *rf, const int8_t *rb, const uint32_t *s_de,
                                             const uint32_t *s_mmm, const uint32_t *s_mm2, const int8_t *s_pt,
-                                            int lane) {
+                                            int lane, int stride = 32) {
   JumpAcc a{0, 0, 0, 0u};
   const int e = t.num_species;
   const int x = t.x_code;
   const int si = st[t.pos_first];
   const int sj = st[t.pos_second];
   const long long *__restrict__ wde = t.w_de;
-  for (int c = lane; c < t.n_de_cl; c += 32) {
+  for (int c = lane; c < t.n_de_cl; c += stride) {
     const uint32_t w = s_de[c];
     const int label = w & 7, side = (w >> 3) & 1, o1 = (w >> 4) & 63, o2 = (w >> 10) & 63;
     const int c1 = st[o1];
@@ -125,7 +127,7 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
     // Clusters holding both pair sites and the two singlets keep their
     // multiset (and cancel) only when the first site is the vacancy; for any
     // other first species GetDe counts them (VacancyMigrationPredictorQuartic.cpp:127-154).
-    for (int c = lane; c < t.n_de_both; c += 32) {
+    for (int c = lane; c < t.n_de_both; c += stride) {
       const uint32_t w = t.de_both[c];
       const int label = w & 7, kind = (w >> 3) & 3, o = (w >> 5) & 63;
       const int co = o == 63 ? 0 : st[o];
@@ -146,7 +148,7 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
     }
   }
   const long long *__restrict__ wd = (kQuartic ? t.w_d : t.w_e0) + static_cast<long long>(slot) * t.f_mmm;
-  for (int c = lane; c < t.n_mmm_cl; c += 32) {
+  for (int c = lane; c < t.n_mmm_cl; c += stride) {
     const uint32_t w = s_mmm[c];
     const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
     const int ra = rm[ia];
@@ -157,7 +159,7 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
   }
   if (kQuartic) {
     const long long *__restrict__ wk = t.w_ks + static_cast<long long>(slot) * t.f_mm2;
-    for (int c = lane; c < t.n_mm2_cl; c += 32) {
+    for (int c = lane; c < t.n_mm2_cl; c += stride) {
       const uint32_t w = s_mm2[c];
       const int ia = w & 63, ib = (w >> 6) & 63, mode = (w >> 12) & 3, base = w >> 14;
       const int fa = rf[ia], ba = rb[ia];
@@ -2709,16 +2711,99 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   if (threadIdx.x == 0) *a.rows = a.nv * 12;
 }
 
+// The plain predictor's barrier and energy change of jump a -> b on the current lattice,
+// evaluated by the whole block: the sorted arrays gathered into shared memory, the cluster sums
+// split over all threads (int64 sums, independent of their order: the same bits as one warp's),
+// the FP64 epilogue by thread 0 into out[0] (barrier) and out[1] (energy change). Called by every
+// thread of the block (it holds block-wide barriers); returns the status bits (thread 0).
+__device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int n, long long a, long long b, int kind,
+                                     const SmallTables *small, int8_t *st, int8_t *rm, int8_t *rf, int8_t *rb,
+                                     long long *red, unsigned *red_bad, double *out) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, warps = blockDim.x >> 5;
+  H3 hi, hj;
+  int di = -1, db = -1;
+  unsigned bad = ResolvePair(t.dir_of, a, b, n, &hi, &hj, &di, &db);  // block-uniform
+  if (!bad) {
+    for (int k = tid; k < kStateSites; k += blockDim.x) {
+      const int8_t *o = t.state_off + (di * kStateSites + k) * 4;
+      st[k] = lat[NeighborId(hi, o[0], o[1], o[2], n)];
+    }
+    for (int k = tid; k < kEnvSites; k += blockDim.x) {
+      const int8_t *oa = t.mmm_off + (di * kEnvSites + k) * 4;
+      const int8_t *ob = t.mm2_off + (di * kEnvSites + k) * 4;
+      const int8_t *oc = t.mm2_off + (db * kEnvSites + k) * 4;
+      rm[k] = small->rank[lat[NeighborId(hi, oa[0], oa[1], oa[2], n)]];
+      rf[k] = small->rank[lat[NeighborId(hi, ob[0], ob[1], ob[2], n)]];
+      rb[k] = small->rank[lat[NeighborId(hj, oc[0], oc[1], oc[2], n)]];
+    }
+  }
+  __syncthreads();
+  int slot = -1;
+  if (!bad) {
+    slot = small->slot[st[t.pos_second]];
+    if (slot < 0 || (kind == 0 ? !small->has_quartic[slot] : !small->has_e0[slot])) bad = kStatusNoCoefficients;
+  }
+  if (!bad) {
+    const JumpAcc acc = kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl,
+                                                   small->pairtype, tid, blockDim.x)
+                                  : EvalJump<false>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl,
+                                                    small->pairtype, tid, blockDim.x);
+    const long long s_de = WarpSum(acc.de), s_d = WarpSum(acc.d), s_ks = WarpSum(acc.ks);
+    const unsigned s_bad = __reduce_or_sync(0xffffffffu, acc.bad);
+    if (lane == 0) {
+      red[3 * warp] = s_de;
+      red[3 * warp + 1] = s_d;
+      red[3 * warp + 2] = s_ks;
+      red_bad[warp] = s_bad;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (bad) {
+      out[0] = nan("");
+      out[1] = nan("");
+    } else {
+      long long acc_de = 0, acc_d = 0, acc_ks = 0;
+      for (int w = 0; w < warps; ++w) {
+        acc_de += red[3 * w];
+        acc_d += red[3 * w + 1];
+        acc_ks += red[3 * w + 2];
+        bad |= red_bad[w];
+      }
+      const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
+      out[0] = o.ea;
+      out[1] = o.de;
+      if (!isfinite(o.ea)) bad |= kStatusNumeric;
+    }
+  }
+  __syncthreads();
+  return bad;
+}
+
+constexpr int kSurrogateRows = kMaxMultiVac * 12;
+
 __global__ void __launch_bounds__(kMultiWarps * 32, 1)
     kmc_surrogate_step_kernel(const __grid_constant__ DevTables t, int8_t *species,
                               const __grid_constant__ KmcSurrogateArgs a) {
   __shared__ SmallTables s_small;
-  __shared__ __align__(16) int8_t s_arr[kMultiWarps * kArr];
+  __shared__ __align__(16) int8_t s_arr[kArr];  // the block's sorted arrays (BlockPairBarrier)
   __shared__ uint32_t s_bits[kLocalBitWords];
   __shared__ double s_incl[kMaxMultiVac];
+  __shared__ long long s_red[3 * kMultiWarps];
+  __shared__ unsigned s_red_bad[kMultiWarps];
+  __shared__ double s_out[2];
+  __shared__ int s_fb[kSurrogateRows];  // rows that take the plain predictor
+  __shared__ int s_nfb, s_halt;
+  __shared__ long long s_sel[2];  // the selected jump
+  __shared__ int s_sel_e, s_sel_v;
+  __shared__ double s_sel_total, s_sel_nlog;
   if (*a.halt) return;  // block-uniform, before any barrier
   StageSmall(t, &s_small);
   for (int i = threadIdx.x; i < kLocalBitWords; i += blockDim.x) s_bits[i] = a.local_bits[i];
+  if (threadIdx.x == 0) {
+    s_nfb = 0;
+    s_halt = 0;
+  }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = a.n, nv = a.nv;
@@ -2726,39 +2811,52 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   const int x_code = t.x_code;
   const double beta = 1.0 / kBoltzmannEv / a.temperature;
   const ExpConsts ec{t.exp_tab, t.exp_l1, t.exp_l2};
-  int8_t *st = s_arr + warp * kArr;
-  int8_t *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  int8_t *st = s_arr, *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
   constexpr unsigned kVacancyBits = kStatusXInEnv | kStatusBadCluster;  // a second vacancy contributes nothing
   unsigned bad_all = 0;
-  unsigned long long nfb = 0;
-  // ---- phase 1: the listed slots' events ----
   const int listed = *a.rows / 12;
+  // ---- phase 1a: the listed rows whose barrier the network does not give ----
+  for (int q = warp; q < listed; q += kMultiWarps) {
+    const int row = q * 12 + lane;
+    bool need = false;
+    if (lane < 12) {
+      const long long id = a.pairs[2 * row + 1];
+      const float mu = a.mean[row], sp = a.spread[row];
+      need = lat[id] != x_code && !(sp <= a.threshold && isfinite(mu));
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&s_nfb, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) s_fb[base + __popc(m & ((1u << lane) - 1u))] = row;
+  }
+  __syncthreads();
+  // ---- phase 1b: those rows by the plain predictor, the whole block per row ----
+  const int nfb = s_nfb;
+  for (int i = 0; i < nfb; ++i) {
+    const int row = s_fb[i];
+    const unsigned b = BlockPairBarrier(t, lat, n, a.pairs[2 * row], a.pairs[2 * row + 1], a.barrier_kind, &s_small,
+                                        st, rm, rf, rb, s_red, s_red_bad, s_out);
+    if (threadIdx.x == 0) {
+      bad_all |= b & ~kVacancyBits;
+      a.pair_ea[row] = s_out[0];
+    }
+  }
+  __syncthreads();
+  // ---- phase 1c: the listed slots' rates, id order and scan (one warp per slot) ----
   for (int q = warp; q < listed; q += kMultiWarps) {
     const int v = a.dirty[q];
     const int row = q * 12 + (lane < 12 ? lane : 0);
     long long id = 0x7fffffffffffffffLL;
-    bool onto_x = true, need = false;
-    double ea = 0.0;
+    double ea = 0.0, k = 0.0;
     if (lane < 12) {
       id = a.pairs[2 * row + 1];
-      onto_x = lat[id] == x_code;
-      const float mu = a.mean[row], sp = a.spread[row];
-      if (!onto_x) {
-        if (sp <= a.threshold && isfinite(mu)) ea = static_cast<double>(mu);
-        else need = true;
+      if (lat[id] != x_code) {
+        const float mu = a.mean[row], sp = a.spread[row];
+        ea = (sp <= a.threshold && isfinite(mu)) ? static_cast<double>(mu) : a.pair_ea[row];
+        k = ExpFast(-ea * beta, ec);
       }
     }
-    unsigned fbm = __ballot_sync(0xffffffffu, need);
-    nfb += __popc(fbm);
-    while (fbm) {
-      const int l = __ffs(fbm) - 1;
-      fbm &= fbm - 1;
-      bad_all |= DensePairBarrier(t, lat, n, a.pairs, q * 12 + l, a.barrier_kind, t.de_cl, t.mmm_cl, t.mm2_cl,
-                                  &s_small, st, rm, rf, rb, a.pair_ea, a.pair_de, nullptr, nullptr, lane) &
-                 ~kVacancyBits;
-    }
-    if (need) ea = a.pair_ea[row];
-    const double k = (lane < 12 && !onto_x) ? ExpFast(-ea * beta, ec) : 0.0;
     // events in id order (the sorted 1NN list), then their inclusive scan
     int rank = 0;
     for (int q2 = 0; q2 < 12; ++q2) {
@@ -2787,9 +2885,9 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
     __syncwarp();
   }
   __syncthreads();
-  // ---- phase 2: selection, energy change, move and the next list (warp 0) ----
+  // ---- phase 2: selection (warp 0) ----
+  const unsigned long long step = *a.steps;
   if (warp == 0) {
-    const unsigned long long step = *a.steps;
     bool halt = false;
     if (a.stop_flag && (step & 63) == 0 && *a.stop_flag) {
       bad_all |= kStatusStopped;
@@ -2835,83 +2933,93 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
         const bool pos = lane < 12 && ((km >> lane) & 1u);
         const unsigned hit = __ballot_sync(0xffffffffu, pos && a.cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
         const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
-        const int e = vsel * 12 + sel;
-        const long long p_old = a.vac_pos[vsel];
-        const long long tgt = a.tgt[e];
-        const double ea_sel = a.ea[e];
-        // the plain predictor's energy change (and barrier) of the selected jump, before the move
         if (lane == 0) {
-          a.sel_pair[0] = p_old;
-          a.sel_pair[1] = tgt;
+          s_sel_e = vsel * 12 + sel;
+          s_sel_v = vsel;
+          s_sel[0] = a.vac_pos[vsel];
+          s_sel[1] = a.tgt[vsel * 12 + sel];
+          s_sel_total = total;
+          s_sel_nlog = nlog_u1;
         }
-        __syncwarp();
-        bad_all |= DensePairBarrier(t, lat, n, a.sel_pair, 0, a.barrier_kind, t.de_cl, t.mmm_cl, t.mm2_cl, &s_small,
-                                    st, rm, rf, rb, a.sel_out, a.sel_out + 1, nullptr, nullptr, lane) &
-                   ~kVacancyBits;
-        const double ea_plain = a.sel_out[0], de_sel = a.sel_out[1];
-        const double time = *a.time + nlog_u1 * RcpFast(total * kPrefactor);
-        const double energy = *a.energy + de_sel;
-        const H3 h_old = SiteCoord(p_old, n), h_new = SiteCoord(tgt, n);
-        if (lane == 0) {
-          lat[p_old] = lat[tgt];  // Config::LatticeJump
-          lat[tgt] = static_cast<int8_t>(x_code);
-          a.vac_pos[vsel] = tgt;
-          *a.time = time;
-          *a.energy = energy;
-          *a.steps = step + 1;
-          const unsigned long long ti = step - a.trace_base;
-          if (a.trace && ti < a.trace_len) {
-            KmcTraceRec rec;
-            rec.vacancy = p_old;
-            rec.target = tgt;
-            rec.selected = sel;
-            rec.slot = vsel;
-            rec.ea = ea_sel;
-            rec.de = de_sel;
-            rec.total_rate = total;
-            rec.time = time;
-            rec.energy = energy;
-            a.trace[ti] = rec;
-            if (a.plain_ea) a.plain_ea[ti] = ea_plain;
-          }
-        }
-        __syncwarp();
-        // slots to re-evaluate: the moved one and those whose neighbourhood holds a changed
-        // site, with their 12 jumps in direction order for the next network launch
-        int nd2 = 0;
-        for (int c = 0; c < chunks; ++c) {
-          const int v = c * 32 + lane;
-          bool d = false;
-          if (v < nv) {
-            const H3 hv = v == vsel ? h_new : SiteCoord(a.vac_pos[v], n);
-            d = v == vsel ||
-                InLocal(s_bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
-                        WrapDelta(h_old.z - hv.z, n)) ||
-                InLocal(s_bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
-                        WrapDelta(h_new.z - hv.z, n));
-          }
-          const unsigned m = __ballot_sync(0xffffffffu, d);
-          if (d) a.dirty[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
-          nd2 += __popc(m);
-        }
-        __syncwarp();
-        for (int i = 0; i < nd2; ++i) {
-          const int v = a.dirty[i];
-          if (lane < 12) {
-            const long long pv = v == vsel ? tgt : a.vac_pos[v];
-            const int8_t *o = t.dir + lane * 4;
-            a.pairs[2 * (i * 12 + lane)] = pv;
-            a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : SiteCoord(pv, n), o[0], o[1], o[2], n);
-          }
-        }
-        if (lane == 0) *a.rows = nd2 * 12;
       }
     }
-    if (halt && lane == 0) *a.halt = 1;
+    if (lane == 0) s_halt = halt ? 1 : 0;
+  }
+  __syncthreads();
+  if (s_halt) {
+    if (threadIdx.x == 0) *a.halt = 1;
+  } else {
+    // ---- phase 3: the plain predictor's energy change (and barrier) of the selected jump, before the move ----
+    const long long p_old = s_sel[0], tgt = s_sel[1];
+    const unsigned b = BlockPairBarrier(t, lat, n, p_old, tgt, a.barrier_kind, &s_small, st, rm, rf, rb, s_red,
+                                        s_red_bad, s_out);
+    if (threadIdx.x == 0) bad_all |= b & ~kVacancyBits;
+    // ---- phase 4: the move and the next list (warp 0) ----
+    if (warp == 0) {
+      const int vsel = s_sel_v, e = s_sel_e;
+      const double ea_plain = s_out[0], de_sel = s_out[1];
+      const double time = *a.time + s_sel_nlog * RcpFast(s_sel_total * kPrefactor);
+      const double energy = *a.energy + de_sel;
+      const H3 h_old = SiteCoord(p_old, n), h_new = SiteCoord(tgt, n);
+      if (lane == 0) {
+        lat[p_old] = lat[tgt];  // Config::LatticeJump
+        lat[tgt] = static_cast<int8_t>(x_code);
+        a.vac_pos[vsel] = tgt;
+        *a.time = time;
+        *a.energy = energy;
+        *a.steps = step + 1;
+        const unsigned long long ti = step - a.trace_base;
+        if (a.trace && ti < a.trace_len) {
+          KmcTraceRec rec;
+          rec.vacancy = p_old;
+          rec.target = tgt;
+          rec.selected = e - vsel * 12;
+          rec.slot = vsel;
+          rec.ea = a.ea[e];
+          rec.de = de_sel;
+          rec.total_rate = s_sel_total;
+          rec.time = time;
+          rec.energy = energy;
+          a.trace[ti] = rec;
+          if (a.plain_ea) a.plain_ea[ti] = ea_plain;
+        }
+      }
+      __syncwarp();
+      // slots to re-evaluate: the moved one and those whose neighbourhood holds a changed
+      // site, with their 12 jumps in direction order for the next network launch
+      const int chunks = (nv + 31) >> 5;
+      int nd2 = 0;
+      for (int c = 0; c < chunks; ++c) {
+        const int v = c * 32 + lane;
+        bool d = false;
+        if (v < nv) {
+          const H3 hv = v == vsel ? h_new : SiteCoord(a.vac_pos[v], n);
+          d = v == vsel ||
+              InLocal(s_bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
+                      WrapDelta(h_old.z - hv.z, n)) ||
+              InLocal(s_bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
+                      WrapDelta(h_new.z - hv.z, n));
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, d);
+        if (d) a.dirty[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
+        nd2 += __popc(m);
+      }
+      __syncwarp();
+      for (int i = 0; i < nd2; ++i) {
+        const int v = a.dirty[i];
+        if (lane < 12) {
+          const long long pv = v == vsel ? tgt : a.vac_pos[v];
+          const int8_t *o = t.dir + lane * 4;
+          a.pairs[2 * (i * 12 + lane)] = pv;
+          a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : SiteCoord(pv, n), o[0], o[1], o[2], n);
+        }
+      }
+      if (lane == 0) *a.rows = nd2 * 12;
+    }
   }
   const unsigned bad = __reduce_or_sync(0xffffffffu, bad_all);
   if (lane == 0) {
-    if (nfb) atomicAdd(a.fallbacks, nfb);
+    if (warp == 0 && nfb) atomicAdd(a.fallbacks, static_cast<unsigned long long>(nfb));
     if (bad) atomicOr(a.status, static_cast<int>(bad));
   }
 }

@@ -177,9 +177,7 @@ struct KmcSurrogateArgs {
   double *cum, *ea;               // [nv * 12] per slot in id order: inclusive rate scan, barrier used
   long long *tgt;                 // [nv * 12]
   uint32_t *kmask;                // [nv] bit e: event e of the slot has a positive rate
-  double *pair_ea, *pair_de;      // [nv * 12] plain results of the rows that fell back
-  long long *sel_pair;            // [2] the selected jump
-  double *sel_out;                // [2] its plain barrier and energy change
+  double *pair_ea;                // [nv * 12] plain barriers of the rows that fell back
   unsigned long long *fallbacks;  // [1] jumps sent to the plain predictor
   int *halt;                      // [1] set by a stop or an error
   KmcTraceRec *trace;             // nullable: step s at trace[s - trace_base], s - trace_base < trace_len

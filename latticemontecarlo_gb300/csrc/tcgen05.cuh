@@ -109,10 +109,10 @@ __device__ __forceinline__ uint64_t GlobalTimerNs() {
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 // Wait as above with sleeping probes, bounded by kWaitLimitNs of wall time.
 __device__ __forceinline__ bool WaitSleep(uint64_t *bar, uint32_t parity, volatile int *abort) {
-  if (TryWaitSleep(bar, parity, 1000)) return true;
+  if (TryWaitSleep(bar, parity, 200)) return true;
   const uint64_t t0 = GlobalTimerNs();
   for (;;) {
-    if (TryWaitSleep(bar, parity, 20000)) return true;
+    if (TryWaitSleep(bar, parity, 2000)) return true;
     if (*abort) return false;
     if (GlobalTimerNs() - t0 > kWaitLimitNs) {
       *abort = 1;
