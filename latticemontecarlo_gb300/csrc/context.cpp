@@ -129,8 +129,8 @@ struct lmc_ctx {
   DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_trace;
   std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
   // surrogate-assisted multi-vacancy KMC (lmc_kmc_multi_surrogate_run)
-  DevBuf su_pairs, su_dirty, su_rows, su_mean, su_spread, su_cum, su_ea, su_tgt, su_kmask, su_pair_ea, su_fb,
-      su_halt, su_trace, su_plain;
+  DevBuf su_pairs, su_dirty, su_mean, su_spread, su_cum, su_ea, su_tgt, su_kmask, su_pair_ea, su_fb, su_halt,
+      su_trace, su_plain;
 
   ~lmc_ctx() {
     for (auto &b : tables) b.Free();
@@ -140,7 +140,7 @@ struct lmc_ctx {
                       &s_fb_pairs, &s_fb_index, &s_fb_ea, &s_fb_de, &c_claim, &c_cand, &c_eacc, &c_stats})
       b->Free();
     for (DevBuf *b : {&m_pos, &m_off, &m_steps, &m_time, &m_energy, &m_temp, &m_key, &m_trace, &sa_state, &sa_rng,
-                      &sa_trace, &su_pairs, &su_dirty, &su_rows, &su_mean, &su_spread, &su_cum, &su_ea, &su_tgt,
+                      &sa_trace, &su_pairs, &su_dirty, &su_mean, &su_spread, &su_cum, &su_ea, &su_tgt,
                       &su_kmask, &su_pair_ea, &su_fb, &su_halt, &su_trace, &su_plain})
       b->Free();
     for (auto &kv : c_mt) kv.second.second.Free();
@@ -2150,11 +2150,12 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     Require(ctx->multi_kind == LMC_BARRIER_QUARTIC, LMC_ERR_UNSUPPORTED, "the surrogate predicts Quartic barriers");
     Require(threshold_ev >= 0.f, LMC_ERR_INVALID_ARGUMENT, "threshold_ev < 0");
     CudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (num_fallback) *num_fallback = 0;
+    if (steps == 0) return;
     const int nv = ctx->m_off_host.back();
     const size_t rows = static_cast<size_t>(nv) * 12;
     ctx->su_pairs.Ensure(16 * rows);
     ctx->su_dirty.Ensure(4 * nv);
-    ctx->su_rows.Ensure(4);
     ctx->su_mean.Ensure(4 * rows);
     ctx->su_spread.Ensure(4 * rows);
     ctx->su_cum.Ensure(8 * rows);
@@ -2163,16 +2164,15 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     ctx->su_kmask.Ensure(4 * nv);
     ctx->su_pair_ea.Ensure(8 * rows);
     ctx->su_fb.Ensure(8);
-    ctx->su_halt.Ensure(4);
-    // the network on the listed jumps, its row count on the device
+    ctx->su_halt.Ensure(8);
+    // the lattice and encoding of the network's gather
     lmc::FusedJumps j;
-    Require(FusedJumpsFor(ctx, 0, ctx->su_pairs.as<long long>(), static_cast<long long>(rows),
-                          ctx->su_mean.as<float>(), ctx->su_spread.as<float>(), &j) &&
+    Require(FusedJumpsFor(ctx, 0, nullptr, 0, nullptr, nullptr, &j) &&
                 lmc::MlpFusedChannels(lmc::MlpDevOf(mlp)) == j.channels,
             LMC_ERR_UNSUPPORTED,
             "the surrogate-assisted run needs the solute-channel encoding and a network the fused jump kernel serves "
             "(2 members, hidden 128, 128 / 192 inputs)");
-    j.m_dev = ctx->su_rows.as<int>();
+    lmc::MlpLabelScaleOf(mlp, &j.mean_label, &j.std_label);
     unsigned long long step0 = 0;
     CudaCheck(cudaMemcpy(&step0, ctx->m_steps.p, 8, cudaMemcpyDeviceToHost), "D2H");
     uint32_t key[2] = {0, 0};
@@ -2182,6 +2182,7 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     lmc::KmcSurrogateArgs a{};
     a.vac_pos = ctx->m_pos.as<long long>();
     a.nv = nv;
+    a.nsteps = steps;
     a.steps = ctx->m_steps.as<unsigned long long>();
     a.time = ctx->m_time.as<double>();
     a.energy = ctx->m_energy.as<double>();
@@ -2197,7 +2198,6 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     a.spread = ctx->su_spread.as<float>();
     a.pairs = ctx->su_pairs.as<long long>();
     a.dirty = ctx->su_dirty.as<int>();
-    a.rows = ctx->su_rows.as<int>();
     a.cum = ctx->su_cum.as<double>();
     a.ea = ctx->su_ea.as<double>();
     a.tgt = ctx->su_tgt.as<long long>();
@@ -2205,6 +2205,7 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     a.pair_ea = ctx->su_pair_ea.as<double>();
     a.fallbacks = ctx->su_fb.as<unsigned long long>();
     a.halt = ctx->su_halt.as<int>();
+    a.net_status = ctx->su_halt.as<int>() + 1;
     a.trace_base = step0;
     if (trace || plain_barrier) {
       ctx->su_trace.Ensure(sizeof(lmc::KmcTraceRec) * steps);
@@ -2219,45 +2220,11 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     std::copy(ctx->local_bits.begin(), ctx->local_bits.end(), a.local_bits);
     ctx->ClearStatus();
     CudaCheck(cudaMemsetAsync(ctx->su_fb.p, 0, 8, ctx->stream), "memset");
-    CudaCheck(cudaMemsetAsync(ctx->su_halt.p, 0, 4, ctx->stream), "memset");
-    CudaCheck(cudaMemsetAsync(const_cast<int *>(lmc::MlpStatusDev(mlp)), 0, sizeof(int), ctx->stream), "memset");
+    CudaCheck(cudaMemsetAsync(ctx->su_halt.p, 0, 8, ctx->stream), "memset");
+    // one persistent launch: the network's weights stay in shared memory for the whole run
     CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
-    // every slot listed at the start of the run, as kmc_multi_kernel evaluates every slot at the
-    // start of a launch
-    CudaCheck(lmc::LaunchKmcSurrogateList(ctx->t, a, ctx->stream), "surrogate KMC list kernel");
-    // one step = the network on the listed jumps, then the step kernel; chunks of steps are
-    // captured once into a CUDA graph and replayed (all state lives on the device)
-    const auto one_step = [&] {
-      CudaCheck(lmc::MlpFusedLaunch(mlp, j, ctx->stream), "fused surrogate kernel");
-      CudaCheck(lmc::LaunchKmcSurrogateStep(ctx->t, ctx->species.as<int8_t>(), a, ctx->stream),
-                "surrogate KMC step kernel");
-    };
-    constexpr uint64_t kChunk = 256;
-    uint64_t done = 0;
-    if (steps >= kChunk) {
-      cudaGraph_t graph = nullptr;
-      cudaGraphExec_t exec = nullptr;
-      CudaCheck(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed), "begin capture");
-      try {
-        for (uint64_t i = 0; i < kChunk; ++i) one_step();
-      } catch (...) {
-        cudaStreamEndCapture(ctx->stream, &graph);
-        if (graph) cudaGraphDestroy(graph);
-        throw;
-      }
-      CudaCheck(cudaStreamEndCapture(ctx->stream, &graph), "end capture");
-      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-      cudaGraphDestroy(graph);
-      CudaCheck(ie, "graph instantiate");
-      try {
-        for (; done + kChunk <= steps; done += kChunk) CudaCheck(cudaGraphLaunch(exec, ctx->stream), "graph launch");
-      } catch (...) {
-        cudaGraphExecDestroy(exec);
-        throw;
-      }
-      cudaGraphExecDestroy(exec);
-    }
-    for (; done < steps; ++done) one_step();
+    CudaCheck(lmc::LaunchKmcSurrogate(ctx->t, ctx->species.as<int8_t>(), a, lmc::MlpDevOf(mlp), j, ctx->stream),
+              "surrogate-assisted KMC kernel");
     CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
     if (trace)
       CudaCheck(cudaMemcpyAsync(trace, ctx->su_trace.p, sizeof(lmc::KmcTraceRec) * steps, cudaMemcpyDeviceToHost,
@@ -2266,7 +2233,7 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     if (plain_barrier)
       CudaCheck(cudaMemcpyAsync(plain_barrier, ctx->su_plain.p, 8 * steps, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     int *h = ctx->Pinned();
-    CudaCheck(cudaMemcpyAsync(h, lmc::MlpStatusDev(mlp), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    CudaCheck(cudaMemcpyAsync(h, ctx->su_halt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     unsigned long long fb = 0;
     CudaCheck(cudaMemcpyAsync(&fb, ctx->su_fb.p, 8, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     const int st = ctx->ReadStatus();  // synchronises
@@ -2274,7 +2241,7 @@ int lmc_kmc_multi_surrogate_run(lmc_ctx *ctx, lmc_mlp *mlp, uint64_t steps, floa
     CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
     ctx->last_ms = ms;
     if (num_fallback) *num_fallback = fb;
-    Require(h[0] == 0, LMC_ERR_STOPPED, "surrogate inference: a tensor-core wait expired");
+    Require(h[1] == 0, LMC_ERR_STOPPED, "surrogate-assisted KMC: a tensor-core wait expired");
     RaiseStatus(st, "surrogate-assisted multi-vacancy KMC run");
   });
 }

@@ -26,6 +26,7 @@
 #include "kernels.cuh"
 #include "fastmath.cuh"
 #include "lattice_index.cuh"
+#include "mlp_fused.cuh"
 #include <cuda_bf16.h>
 
 namespace cg = cooperative_groups;
@@ -2680,37 +2681,27 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
 }
 
 // ---------------------------------------------------------------------------
-// K4s: surrogate-assisted multi-vacancy KMC on one lattice, one step per launch,
-// interleaved with the fused network kernel (mlp_fused.cu) that evaluates the
-// jumps listed by the previous step (both captured in a CUDA graph). Per step:
-//  1. the listed slots' 12 events (one warp per slot): the ensemble mean for the
-//     barrier, the plain predictor (dense sums, FP64 epilogue) where the ensemble
-//     spread exceeds the threshold or the network does not describe the jump; a
-//     jump onto a vacancy has rate 0; rates, id order and inclusive scan as in
-//     kmc_multi_kernel;
-//  2. warp 0: selection over all slots exactly as kmc_multi_kernel (Philox draw of
-//     counter = step), the plain predictor's energy change of the selected jump
-//     (before the move: the energy sums stay exact), the move, and the list of
-//     slots whose neighbourhood holds a changed site with their 12 jumps each for
-//     the next step's network launch.
+// K4s: surrogate-assisted multi-vacancy KMC of one lattice in one persistent CTA
+// (kmc_surrogate_kernel): the step loop of kmc_multi_kernel with the barriers of the
+// re-evaluated jumps taken from the compact ensemble on the tensor cores. The ensemble's
+// weights are loaded into shared memory once per run and TMEM is allocated once; per step:
+//  A. the listed jumps (12 per slot whose neighbourhood changed), 128 per tile: threads
+//     0-255 gather the feature rows from the lattice (two threads per row), thread 0 issues
+//     both members' layer-1 MMAs, the 16 warps turn D into H1 (GELU, packed half, tcgen05.st),
+//     thread 0 issues layer 2 (A = H1 in TMEM), the warps fold GELU . w3 per column half and
+//     member, warps 0-3 form each row's ensemble mean and spread (fused::* in mlp_fused.cuh);
+//  B. the rows whose ensemble spread exceeds the threshold (or that the network does not
+//     describe) by the plain predictor, the whole block per row (BlockPairBarrier);
+//  C. per listed slot (one warp): rates, id order and inclusive scan, as kmc_multi_kernel;
+//  D. warp 0 selects among all slots exactly as kmc_multi_kernel (Philox draw of counter =
+//     step), the block evaluates the plain predictor's energy change of the selected jump
+//     (before the move: the energy sums stay exact), warp 0 moves the vacancy and lists the
+//     slots whose neighbourhood holds a changed site with their 12 jumps.
 // With threshold 0 every jump takes the plain predictor and the trajectory is
-// kmc_multi_kernel's (dense evaluation). A stop or an error sets *halt, after
-// which the remaining launches of the run return at once.
+// kmc_multi_kernel's. Phases are separated by __syncthreads; the MMA completions are
+// mbarrier waits with a 2 s bound, after which the kernel records a status, drains its
+// MMAs and copies, frees TMEM and returns.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMultiWarps * 32, 1)
-    kmc_surrogate_list_kernel(const __grid_constant__ DevTables t, const __grid_constant__ KmcSurrogateArgs a) {
-  // every slot listed, 12 jumps each in direction order (the start of a run)
-  for (int i = threadIdx.x; i < a.nv * 12; i += blockDim.x) {
-    const int v = i / 12, d = i % 12;
-    const long long pos = a.vac_pos[v];
-    const int8_t *o = t.dir + d * 4;
-    a.pairs[2 * i] = pos;
-    a.pairs[2 * i + 1] = NeighborId(SiteCoord(pos, a.n), o[0], o[1], o[2], a.n);
-    if (d == 0) a.dirty[v] = v;
-  }
-  if (threadIdx.x == 0) *a.rows = a.nv * 12;
-}
-
 // The plain predictor's barrier and energy change of jump a -> b on the current lattice,
 // evaluated by the whole block: the sorted arrays gathered into shared memory, the cluster sums
 // split over all threads (int64 sums, independent of their order: the same bits as one warp's),
@@ -2780,185 +2771,324 @@ __device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int 
   return bad;
 }
 
-constexpr int kSurrogateRows = kMaxMultiVac * 12;
+constexpr int kSurWarps = 16;
 
-__global__ void __launch_bounds__(kMultiWarps * 32, 1)
-    kmc_surrogate_step_kernel(const __grid_constant__ DevTables t, int8_t *species,
-                              const __grid_constant__ KmcSurrogateArgs a) {
-  __shared__ SmallTables s_small;
-  __shared__ __align__(16) int8_t s_arr[kArr];  // the block's sorted arrays (BlockPairBarrier)
-  __shared__ uint32_t s_bits[kLocalBitWords];
-  __shared__ double s_incl[kMaxMultiVac];
-  __shared__ long long s_red[3 * kMultiWarps];
-  __shared__ unsigned s_red_bad[kMultiWarps];
-  __shared__ double s_out[2];
-  __shared__ int s_fb[kSurrogateRows];  // rows that take the plain predictor
-  __shared__ int s_nfb, s_halt;
-  __shared__ long long s_sel[2];  // the selected jump
-  __shared__ int s_sel_e, s_sel_v;
-  __shared__ double s_sel_total, s_sel_nlog;
-  if (*a.halt) return;  // block-uniform, before any barrier
-  StageSmall(t, &s_small);
-  for (int i = threadIdx.x; i < kLocalBitWords; i += blockDim.x) s_bits[i] = a.local_bits[i];
-  if (threadIdx.x == 0) {
-    s_nfb = 0;
-    s_halt = 0;
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+struct SurShared {
+  uint64_t w_full, mma, done;
+  int abort, halt, rows, nfb;
+  uint32_t tmem;
+  uint32_t site_word[8];
+  int8_t chan[8];
+  uint32_t flag[2][4];                 // per half row and lane group: bit l, row 32 lg + l takes the plain predictor
+  float partial[2][fused::kMembers][fused::kRows];  // per column half and member: GELU . w3 of each row
+  SmallTables small;
+  int8_t arr[kArr];                    // the block's sorted arrays (BlockPairBarrier)
+  uint32_t bits[kLocalBitWords];
+  double incl[kMaxMultiVac];
+  long long red[3 * kSurWarps];
+  unsigned red_bad[kSurWarps];
+  double out[2];
+  long long sel[2];                    // the selected jump
+  int sel_e, sel_v;
+  double sel_total, sel_nlog;
+  int16_t fb[kMaxMultiVac * 12];       // listed rows that take the plain predictor
+};
+
+template <int kC>
+constexpr size_t SurrogateSmemBytes() {
+  return static_cast<size_t>(fused::Shape<kC>::kW1Bytes) + fused::kW2Bytes + fused::Shape<kC>::kXBytes +
+         sizeof(SurShared);
+}
+static_assert(SurrogateSmemBytes<3>() <= 232448, "the surrogate KMC kernel's shared memory exceeds 227 KB");
+
+// Bounded wait by lane 0 (sleeping probes), its outcome broadcast to the warp.
+__device__ __forceinline__ bool SurWarpWait(uint64_t *bar, uint32_t parity, volatile int *abort, int lane) {
+  int ok = 1;
+  if (lane == 0) ok = tc::WaitSleep(bar, parity, abort) ? 1 : 0;
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+template <int kC>
+__global__ void __launch_bounds__(kSurWarps * 32, 1)
+    kmc_surrogate_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcSurrogateArgs a,
+                         const __grid_constant__ MlpDev d, const __grid_constant__ FusedJumps j) {
+  using S = fused::Shape<kC>;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char *sw1 = smem, *sw2 = sw1 + S::kW1Bytes, *sx = sw2 + fused::kW2Bytes;
+  SurShared *sh = reinterpret_cast<SurShared *>(sx + S::kXBytes);
+  volatile int *abort = &sh->abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n = a.n, nv = a.nv;
   int8_t *lat = species + a.lat_off;
   const int x_code = t.x_code;
   const double beta = 1.0 / kBoltzmannEv / a.temperature;
   const ExpConsts ec{t.exp_tab, t.exp_l1, t.exp_l2};
-  int8_t *st = s_arr, *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
+  int8_t *st = sh->arr, *rm = st + kStateSites, *rf = rm + kEnvSites, *rb = rf + kEnvSites;
   constexpr unsigned kVacancyBits = kStatusXInEnv | kStatusBadCluster;  // a second vacancy contributes nothing
+
+  if (tid == 0) {
+    tc::BarInit(&sh->w_full, 1);
+    tc::BarInit(&sh->mma, 1);
+    tc::BarInit(&sh->done, 1);
+    sh->abort = 0;
+    sh->halt = 0;
+    sh->rows = nv * 12;
+    tc::FenceBarrierInit();
+    tc::ArriveExpectTx(&sh->w_full, S::kW1Bytes + fused::kW2Bytes);
+    tc::BulkCopy(sw1, d.w1_tiles, S::kW1Bytes, &sh->w_full);
+    tc::BulkCopy(sw2, d.w2_tiles, fused::kW2Bytes, &sh->w_full);
+  }
+  if (tid < 8) {
+    sh->site_word[tid] = j.site_word[tid];
+    sh->chan[tid] = j.chan[tid];
+  }
+  StageSmall(t, &sh->small);
+  for (int i = tid; i < kLocalBitWords; i += blockDim.x) sh->bits[i] = a.local_bits[i];
+  // every slot listed at the start of the run, 12 jumps each in direction order
+  for (int i = tid; i < nv * 12; i += blockDim.x) {
+    const int v = i / 12, dd = i % 12;
+    const long long pos = a.vac_pos[v];
+    const int8_t *o = t.dir + dd * 4;
+    a.pairs[2 * i] = pos;
+    a.pairs[2 * i + 1] = NeighborId(SiteCoord(pos, n), o[0], o[1], o[2], n);
+    if (dd == 0) a.dirty[v] = v;
+  }
+  if (warp == 0) tc::TmemAlloc(&sh->tmem, fused::kCols);
+  tc::FenceBeforeSync();
+  __syncthreads();
+  tc::FenceAfterSync();
+  const uint32_t tmem = sh->tmem;
+  const uint32_t a_x = tc::Smem(sx), a_w1 = tc::Smem(sw1), a_w2 = tc::Smem(sw2);
+  // epilogue split: lane group (TMEM lanes 32 lg ..), member, column half
+  const int lg = warp & 3, em = (warp >> 2) & 1, hh = warp >> 3;
+  const uint32_t ecol = tmem + (static_cast<uint32_t>(lg * 32) << 16) + em * fused::kMemberCols;
+  uint32_t mma_phase = 0;
+  bool weights = false;
   unsigned bad_all = 0;
-  const int listed = *a.rows / 12;
-  // ---- phase 1a: the listed rows whose barrier the network does not give ----
-  for (int q = warp; q < listed; q += kMultiWarps) {
-    const int row = q * 12 + lane;
-    bool need = false;
-    if (lane < 12) {
-      const long long id = a.pairs[2 * row + 1];
-      const float mu = a.mean[row], sp = a.spread[row];
-      need = lat[id] != x_code && !(sp <= a.threshold && isfinite(mu));
+  unsigned long long nfb_total = 0;
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    const int rows = sh->rows;
+    // ---- A: the network on the listed rows, 128 per tile ----
+    for (int t0 = 0; t0 < rows; t0 += fused::kRows) {
+      if (tid < 2 * fused::kRows) {
+        const int half = tid >> 7, r = tid & 127, row = t0 + r;
+        int code[fused::kHalfSites];
+        bool fb = true;
+        if (row < rows) {
+          unsigned b = 0;
+          fb = fused::LoadHalfRow<false>(j, a.pairs[2 * row], a.pairs[2 * row + 1], half, code, &b);
+          bad_all |= b;
+        }
+        if (fb) {
+#pragma unroll
+          for (int k = 0; k < fused::kHalfSites; ++k) code[k] = -1;
+        }
+        fused::WriteHalfRow<kC>(code, sh->site_word, sh->chan, half, r, sx);
+        const unsigned m = __ballot_sync(0xffffffffu, fb);
+        if (lane == 0) sh->flag[half][(tid >> 5) & 3] = m;
+        tc::FenceAsyncSmem();
+      }
+      __syncthreads();
+      if (tid == 0) {
+        if (!weights) weights = tc::WaitSleep(&sh->w_full, 0, abort);
+        if (weights) {
+          tc::FenceAfterSync();
+          fused::IssueLayer1<kC>(tmem, a_x, a_w1, 0);
+          fused::IssueLayer1<kC>(tmem, a_x, a_w1, 1);
+          tc::Commit(&sh->mma);
+        }
+      }
+      SurWarpWait(&sh->mma, mma_phase, abort, lane);
+      mma_phase ^= 1;
+      __syncthreads();
+      if (*abort) break;
+      tc::FenceAfterSync();
+      fused::Layer1Epilogue(ecol, hh * 64);
+      fused::Layer1Epilogue(ecol, hh * 64 + 32);
+      tc::FenceBeforeSync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::FenceAfterSync();
+        fused::IssueLayer2(tmem, a_w2, 0);
+        fused::IssueLayer2(tmem, a_w2, 1);
+        tc::Commit(&sh->mma);
+      }
+      SurWarpWait(&sh->mma, mma_phase, abort, lane);
+      mma_phase ^= 1;
+      __syncthreads();
+      if (*abort) break;
+      tc::FenceAfterSync();
+      {
+        float v[32];
+        float acc = 0.f;
+#pragma unroll 1
+        for (int cb = 0; cb < 2; ++cb) {
+          const int col0 = hh * 64 + cb * 32;
+          tc::TmemLoad32(ecol + col0, v);
+          acc += fused::GeluDotHalf(v, d.b2h + em * fused::kHid + col0, d.w3h + em * fused::kHid + col0);
+        }
+        sh->partial[hh][em][lg * 32 + lane] = acc;
+      }
+      tc::FenceBeforeSync();
+      __syncthreads();
+      if (warp < 4) {
+        const int r = warp * 32 + lane, row = t0 + r;
+        if (row < rows) {
+          const float y0 = sh->partial[0][0][r] + sh->partial[1][0][r] + __ldg(&d.b3[0]);
+          const float y1 = sh->partial[0][1][r] + sh->partial[1][1][r] + __ldg(&d.b3[1]);
+          const bool fb = (((sh->flag[0][warp] | sh->flag[1][warp]) >> lane) & 1u) != 0;
+          a.mean[row] = j.mean_label + j.std_label * 0.5f * (y0 + y1);
+          a.spread[row] = fb ? __int_as_float(0x7f800000) : j.std_label * fabsf(y0 - y1);
+        }
+      }
+      __syncthreads();
     }
-    const unsigned m = __ballot_sync(0xffffffffu, need);
-    int base = 0;
-    if (lane == 0 && m) base = atomicAdd(&s_nfb, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (need) s_fb[base + __popc(m & ((1u << lane) - 1u))] = row;
-  }
-  __syncthreads();
-  // ---- phase 1b: those rows by the plain predictor, the whole block per row ----
-  const int nfb = s_nfb;
-  for (int i = 0; i < nfb; ++i) {
-    const int row = s_fb[i];
-    const unsigned b = BlockPairBarrier(t, lat, n, a.pairs[2 * row], a.pairs[2 * row + 1], a.barrier_kind, &s_small,
-                                        st, rm, rf, rb, s_red, s_red_bad, s_out);
-    if (threadIdx.x == 0) {
-      bad_all |= b & ~kVacancyBits;
-      a.pair_ea[row] = s_out[0];
-    }
-  }
-  __syncthreads();
-  // ---- phase 1c: the listed slots' rates, id order and scan (one warp per slot) ----
-  for (int q = warp; q < listed; q += kMultiWarps) {
-    const int v = a.dirty[q];
-    const int row = q * 12 + (lane < 12 ? lane : 0);
-    long long id = 0x7fffffffffffffffLL;
-    double ea = 0.0, k = 0.0;
-    if (lane < 12) {
-      id = a.pairs[2 * row + 1];
-      if (lat[id] != x_code) {
+    if (*abort) break;
+    // ---- B: the listed rows whose barrier the network does not give, by the plain predictor ----
+    if (tid == 0) sh->nfb = 0;
+    __syncthreads();
+    const int listed = rows / 12;
+    for (int q = warp; q < listed; q += kSurWarps) {
+      const int row = q * 12 + lane;
+      bool need = false;
+      if (lane < 12) {
+        const long long id = a.pairs[2 * row + 1];
         const float mu = a.mean[row], sp = a.spread[row];
-        ea = (sp <= a.threshold && isfinite(mu)) ? static_cast<double>(mu) : a.pair_ea[row];
-        k = ExpFast(-ea * beta, ec);
+        need = lat[id] != x_code && !(sp <= a.threshold && isfinite(mu));
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, need);
+      int base = 0;
+      if (lane == 0 && m) base = atomicAdd(&sh->nfb, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (need) sh->fb[base + __popc(m & ((1u << lane) - 1u))] = static_cast<int16_t>(row);
+    }
+    __syncthreads();
+    const int nfb = sh->nfb;
+    for (int i = 0; i < nfb; ++i) {
+      const int row = sh->fb[i];
+      const unsigned b = BlockPairBarrier(t, lat, n, a.pairs[2 * row], a.pairs[2 * row + 1], a.barrier_kind,
+                                          &sh->small, st, rm, rf, rb, sh->red, sh->red_bad, sh->out);
+      if (tid == 0) {
+        bad_all |= b & ~kVacancyBits;
+        a.pair_ea[row] = sh->out[0];
       }
     }
-    // events in id order (the sorted 1NN list), then their inclusive scan
-    int rank = 0;
-    for (int q2 = 0; q2 < 12; ++q2) {
-      const long long oid = __shfl_sync(0xffffffffu, id, q2);
-      rank += (q2 != lane) && (oid < id);
-    }
-    int src = 0;
-    for (int q2 = 0; q2 < 12; ++q2)
-      if (__shfl_sync(0xffffffffu, rank, q2) == lane) src = q2;
-    const double k_s = __shfl_sync(0xffffffffu, k, src);
-    const double ea_s = __shfl_sync(0xffffffffu, ea, src);
-    const long long id_s = __shfl_sync(0xffffffffu, id, src);
-    double cum = lane < 12 ? k_s : 0.0;
-#pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
-      const double u = __shfl_up_sync(0xffffffffu, cum, o);
-      if (lane >= o) cum += u;
-    }
-    const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
-    if (lane < 12) {
-      a.cum[v * 12 + lane] = cum;
-      a.ea[v * 12 + lane] = ea_s;
-      a.tgt[v * 12 + lane] = id_s;
-    }
-    if (lane == 0) a.kmask[v] = kpos;
-    __syncwarp();
-  }
-  __syncthreads();
-  // ---- phase 2: selection (warp 0) ----
-  const unsigned long long step = *a.steps;
-  if (warp == 0) {
-    bool halt = false;
-    if (a.stop_flag && (step & 63) == 0 && *a.stop_flag) {
-      bad_all |= kStatusStopped;
-      halt = true;
-    }
-    if (!halt) {
-      const uint4 xr = PhiloxRound10(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32),
-                                     static_cast<uint32_t>(a.replica), 0x4b4d43u, a.key0, a.key1);
-      const double nlog_u1 = -log(U01Open(xr.x, xr.y));
-      const double u2 = U01(xr.z, xr.w);
-      const int chunks = (nv + 31) >> 5;
-      double run = 0.0;
-      for (int c = 0; c < chunks; ++c) {
-        const int v = c * 32 + lane;
-        double sc = v < nv ? a.cum[v * 12 + 11] : 0.0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const double u = __shfl_up_sync(0xffffffffu, sc, o);
-          if (lane >= o) sc += u;
+    if (tid == 0) nfb_total += nfb;
+    __syncthreads();
+    // ---- C: the listed slots' rates, id order and scan (one warp per slot) ----
+    for (int q = warp; q < listed; q += kSurWarps) {
+      const int v = a.dirty[q];
+      const int row = q * 12 + (lane < 12 ? lane : 0);
+      long long id = 0x7fffffffffffffffLL;
+      double ea = 0.0, k = 0.0;
+      if (lane < 12) {
+        id = a.pairs[2 * row + 1];
+        if (lat[id] != x_code) {
+          const float mu = a.mean[row], sp = a.spread[row];
+          ea = (sp <= a.threshold && isfinite(mu)) ? static_cast<double>(mu) : a.pair_ea[row];
+          k = ExpFast(-ea * beta, ec);
         }
-        if (v < nv) s_incl[v] = run + sc;
-        run = run + __shfl_sync(0xffffffffu, sc, 31);
       }
-      const double total = run;
+      // events in id order (the sorted 1NN list), then their inclusive scan
+      int rank = 0;
+      for (int q2 = 0; q2 < 12; ++q2) {
+        const long long oid = __shfl_sync(0xffffffffu, id, q2);
+        rank += (q2 != lane) && (oid < id);
+      }
+      int src = 0;
+      for (int q2 = 0; q2 < 12; ++q2)
+        if (__shfl_sync(0xffffffffu, rank, q2) == lane) src = q2;
+      const double k_s = __shfl_sync(0xffffffffu, k, src);
+      const double ea_s = __shfl_sync(0xffffffffu, ea, src);
+      const long long id_s = __shfl_sync(0xffffffffu, id, src);
+      double cum = lane < 12 ? k_s : 0.0;
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, cum, o);
+        if (lane >= o) cum += u;
+      }
+      const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
+      if (lane < 12) {
+        a.cum[v * 12 + lane] = cum;
+        a.ea[v * 12 + lane] = ea_s;
+        a.tgt[v * 12 + lane] = id_s;
+      }
+      if (lane == 0) a.kmask[v] = kpos;
       __syncwarp();
-      const double xs = __dmul_rn(u2, total);  // not contracted with the subtraction below
-      int vsel = -1, vlast = -1;
-      for (int c = 0; c < chunks; ++c) {
-        const int v = c * 32 + lane;
-        const bool pos = v < nv && a.kmask[v] != 0;
-        const unsigned hit = __ballot_sync(0xffffffffu, pos && s_incl[v] >= xs);
-        const unsigned any = __ballot_sync(0xffffffffu, pos);
-        if (vsel < 0 && hit) vsel = c * 32 + __ffs(hit) - 1;
-        if (any) vlast = c * 32 + 31 - __clz(any);
-      }
-      if (vsel < 0) vsel = vlast;
-      if (vsel < 0 || !(total > 0.0) || !isfinite(total)) {
-        bad_all |= kStatusNumeric;
+    }
+    __syncthreads();
+    // ---- D: selection (warp 0) ----
+    const unsigned long long step = *a.steps;
+    if (warp == 0) {
+      bool halt = false;
+      if (a.stop_flag && (step & 63) == 0 && *a.stop_flag) {
+        bad_all |= kStatusStopped;
         halt = true;
-      } else {
-        const double y = __dsub_rn(xs, vsel > 0 ? s_incl[vsel - 1] : 0.0);
-        const unsigned km = a.kmask[vsel];
-        const bool pos = lane < 12 && ((km >> lane) & 1u);
-        const unsigned hit = __ballot_sync(0xffffffffu, pos && a.cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
-        const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
-        if (lane == 0) {
-          s_sel_e = vsel * 12 + sel;
-          s_sel_v = vsel;
-          s_sel[0] = a.vac_pos[vsel];
-          s_sel[1] = a.tgt[vsel * 12 + sel];
-          s_sel_total = total;
-          s_sel_nlog = nlog_u1;
+      }
+      if (!halt) {
+        const uint4 xr = PhiloxRound10(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32),
+                                       static_cast<uint32_t>(a.replica), 0x4b4d43u, a.key0, a.key1);
+        const double nlog_u1 = -log(U01Open(xr.x, xr.y));
+        const double u2 = U01(xr.z, xr.w);
+        const int chunks = (nv + 31) >> 5;
+        double run = 0.0;
+        for (int c = 0; c < chunks; ++c) {
+          const int v = c * 32 + lane;
+          double sc = v < nv ? a.cum[v * 12 + 11] : 0.0;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, sc, o);
+            if (lane >= o) sc += u;
+          }
+          if (v < nv) sh->incl[v] = run + sc;
+          run = run + __shfl_sync(0xffffffffu, sc, 31);
+        }
+        const double total = run;
+        __syncwarp();
+        const double xs = __dmul_rn(u2, total);  // not contracted with the subtraction below
+        int vsel = -1, vlast = -1;
+        for (int c = 0; c < chunks; ++c) {
+          const int v = c * 32 + lane;
+          const bool pos = v < nv && a.kmask[v] != 0;
+          const unsigned hit = __ballot_sync(0xffffffffu, pos && sh->incl[v] >= xs);
+          const unsigned any = __ballot_sync(0xffffffffu, pos);
+          if (vsel < 0 && hit) vsel = c * 32 + __ffs(hit) - 1;
+          if (any) vlast = c * 32 + 31 - __clz(any);
+        }
+        if (vsel < 0) vsel = vlast;
+        if (vsel < 0 || !(total > 0.0) || !isfinite(total)) {
+          bad_all |= kStatusNumeric;
+          halt = true;
+        } else {
+          const double y = __dsub_rn(xs, vsel > 0 ? sh->incl[vsel - 1] : 0.0);
+          const unsigned km = a.kmask[vsel];
+          const bool pos = lane < 12 && ((km >> lane) & 1u);
+          const unsigned hit = __ballot_sync(0xffffffffu, pos && a.cum[vsel * 12 + (lane < 12 ? lane : 0)] >= y);
+          const int sel = hit ? __ffs(hit) - 1 : 31 - __clz(km);
+          if (lane == 0) {
+            sh->sel_e = vsel * 12 + sel;
+            sh->sel_v = vsel;
+            sh->sel[0] = a.vac_pos[vsel];
+            sh->sel[1] = a.tgt[vsel * 12 + sel];
+            sh->sel_total = total;
+            sh->sel_nlog = nlog_u1;
+          }
         }
       }
+      if (lane == 0) sh->halt = halt ? 1 : 0;
     }
-    if (lane == 0) s_halt = halt ? 1 : 0;
-  }
-  __syncthreads();
-  if (s_halt) {
-    if (threadIdx.x == 0) *a.halt = 1;
-  } else {
-    // ---- phase 3: the plain predictor's energy change (and barrier) of the selected jump, before the move ----
-    const long long p_old = s_sel[0], tgt = s_sel[1];
-    const unsigned b = BlockPairBarrier(t, lat, n, p_old, tgt, a.barrier_kind, &s_small, st, rm, rf, rb, s_red,
-                                        s_red_bad, s_out);
-    if (threadIdx.x == 0) bad_all |= b & ~kVacancyBits;
-    // ---- phase 4: the move and the next list (warp 0) ----
+    __syncthreads();
+    if (sh->halt) break;
+    // ---- D: the plain predictor's energy change of the selected jump (before the move) ----
+    const long long p_old = sh->sel[0], tgt = sh->sel[1];
+    const unsigned b = BlockPairBarrier(t, lat, n, p_old, tgt, a.barrier_kind, &sh->small, st, rm, rf, rb, sh->red,
+                                        sh->red_bad, sh->out);
+    if (tid == 0) bad_all |= b & ~kVacancyBits;
+    // ---- D: the move and the next list (warp 0) ----
     if (warp == 0) {
-      const int vsel = s_sel_v, e = s_sel_e;
-      const double ea_plain = s_out[0], de_sel = s_out[1];
-      const double time = *a.time + s_sel_nlog * RcpFast(s_sel_total * kPrefactor);
+      const int vsel = sh->sel_v, e = sh->sel_e;
+      const double ea_plain = sh->out[0], de_sel = sh->out[1];
+      const double time = *a.time + sh->sel_nlog * RcpFast(sh->sel_total * kPrefactor);
       const double energy = *a.energy + de_sel;
       const H3 h_old = SiteCoord(p_old, n), h_new = SiteCoord(tgt, n);
       if (lane == 0) {
@@ -2977,7 +3107,7 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
           rec.slot = vsel;
           rec.ea = a.ea[e];
           rec.de = de_sel;
-          rec.total_rate = s_sel_total;
+          rec.total_rate = sh->sel_total;
           rec.time = time;
           rec.energy = energy;
           a.trace[ti] = rec;
@@ -2986,22 +3116,22 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
       }
       __syncwarp();
       // slots to re-evaluate: the moved one and those whose neighbourhood holds a changed
-      // site, with their 12 jumps in direction order for the next network launch
+      // site, with their 12 jumps in direction order for the next step's network
       const int chunks = (nv + 31) >> 5;
       int nd2 = 0;
       for (int c = 0; c < chunks; ++c) {
         const int v = c * 32 + lane;
-        bool d = false;
+        bool dv = false;
         if (v < nv) {
           const H3 hv = v == vsel ? h_new : SiteCoord(a.vac_pos[v], n);
-          d = v == vsel ||
-              InLocal(s_bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
-                      WrapDelta(h_old.z - hv.z, n)) ||
-              InLocal(s_bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
-                      WrapDelta(h_new.z - hv.z, n));
+          dv = v == vsel ||
+               InLocal(sh->bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
+                       WrapDelta(h_old.z - hv.z, n)) ||
+               InLocal(sh->bits, WrapDelta(h_new.x - hv.x, n), WrapDelta(h_new.y - hv.y, n),
+                       WrapDelta(h_new.z - hv.z, n));
         }
-        const unsigned m = __ballot_sync(0xffffffffu, d);
-        if (d) a.dirty[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
+        const unsigned m = __ballot_sync(0xffffffffu, dv);
+        if (dv) a.dirty[nd2 + __popc(m & ((1u << lane) - 1u))] = v;
         nd2 += __popc(m);
       }
       __syncwarp();
@@ -3014,14 +3144,27 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
           a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : SiteCoord(pv, n), o[0], o[1], o[2], n);
         }
       }
-      if (lane == 0) *a.rows = nd2 * 12;
+      if (lane == 0) sh->rows = nd2 * 12;
     }
+    __syncthreads();
   }
+  // drain: every MMA issued has completed when `done` does; the weight copies have landed
+  if (tid == 0) {
+    tc::Commit(&sh->done);
+    if (!tc::WaitDrain(&sh->done, 0)) *abort = 1;
+    if (!weights && !tc::WaitDrain(&sh->w_full, 0)) *abort = 1;
+  }
+  __syncthreads();
   const unsigned bad = __reduce_or_sync(0xffffffffu, bad_all);
-  if (lane == 0) {
-    if (warp == 0 && nfb) atomicAdd(a.fallbacks, static_cast<unsigned long long>(nfb));
-    if (bad) atomicOr(a.status, static_cast<int>(bad));
+  if (lane == 0 && bad) atomicOr(a.status, static_cast<int>(bad));
+  if (tid == 0) {
+    if (nfb_total) atomicAdd(a.fallbacks, nfb_total);
+    if (*abort) atomicOr(a.net_status, 1);
+    if (sh->halt || *abort) *a.halt = 1;
   }
+  tc::FenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) tc::TmemFree(tmem, fused::kCols);
 }
 
 constexpr int kCmcRefMaxBatch = 256;
@@ -3968,17 +4111,24 @@ cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiAr
   return cudaGetLastError();
 }
 
-cudaError_t LaunchKmcSurrogateList(const DevTables &t, const KmcSurrogateArgs &a, cudaStream_t stream) {
-  if (a.nv < 1 || a.nv > kMaxMultiVac) return cudaErrorInvalidValue;
-  kmc_surrogate_list_kernel<<<1, kMultiWarps * 32, 0, stream>>>(t, a);
+template <int kC>
+static cudaError_t LaunchSurrogateKmcC(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a, const MlpDev &d,
+                                       const FusedJumps &j, cudaStream_t stream) {
+  constexpr size_t sm = SurrogateSmemBytes<kC>();
+  const cudaError_t err = cudaFuncSetAttribute(kmc_surrogate_kernel<kC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(sm));
+  if (err != cudaSuccess) return err;
+  kmc_surrogate_kernel<kC><<<1, kSurWarps * 32, sm, stream>>>(t, species, a, d, j);
   return cudaGetLastError();
 }
 
-cudaError_t LaunchKmcSurrogateStep(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a,
-                                   cudaStream_t stream) {
-  if (a.nv < 1 || a.nv > kMaxMultiVac) return cudaErrorInvalidValue;
-  kmc_surrogate_step_kernel<<<1, kMultiWarps * 32, 0, stream>>>(t, species, a);
-  return cudaGetLastError();
+cudaError_t LaunchKmcSurrogate(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a, const MlpDev &d,
+                               const FusedJumps &j, cudaStream_t stream) {
+  if (a.nv < 1 || a.nv > kMaxMultiVac || a.nsteps == 0) return cudaErrorInvalidValue;
+  const int kc = MlpFusedChannels(d);
+  if (kc != j.channels) return cudaErrorInvalidValue;
+  return kc == 2 ? LaunchSurrogateKmcC<2>(t, species, a, d, j, stream)
+                 : LaunchSurrogateKmcC<3>(t, species, a, d, j, stream);
 }
 
 cudaError_t LaunchCmcReference(const DevTables &t, int8_t *species, const CmcRefArgs &a, cudaStream_t stream) {

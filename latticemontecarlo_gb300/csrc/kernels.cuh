@@ -7,6 +7,7 @@
 
 #include "device_tables.hpp"
 #include "model.hpp"
+#include "mlp.cuh"
 
 namespace lmc {
 
@@ -156,11 +157,12 @@ size_t KmcMultiSharedBytes(const DevTables &t, bool sparse);
 cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiArgs &a, bool sparse,
                            cudaStream_t stream);
 
-// Surrogate-assisted multi-vacancy KMC on one lattice (kmc_surrogate_step_kernel): the
-// device state of a run; one launch per step after the fused network kernel.
+// Surrogate-assisted multi-vacancy KMC of one lattice (kmc_surrogate_kernel, one persistent
+// CTA): the device state of a run.
 struct KmcSurrogateArgs {
   long long *vac_pos;             // [nv] vacancy site of each slot
   int nv;
+  unsigned long long nsteps;      // steps of this launch
   unsigned long long *steps;      // [1] steps taken (the Philox counter of the next draw)
   double *time, *energy;          // [1]
   double temperature;
@@ -170,16 +172,16 @@ struct KmcSurrogateArgs {
   int n;
   int barrier_kind;
   float threshold;                // ensemble spread (eV) above which a jump takes the plain predictor
-  const float *mean, *spread;     // [nv * 12] network outputs of the listed jumps
+  float *mean, *spread;           // [nv * 12] network outputs of the listed jumps
   long long *pairs;               // [nv * 12][2] listed jumps, 12 per listed slot in direction order
   int *dirty;                     // [nv] listed slots
-  int *rows;                      // [1] listed jumps
   double *cum, *ea;               // [nv * 12] per slot in id order: inclusive rate scan, barrier used
   long long *tgt;                 // [nv * 12]
   uint32_t *kmask;                // [nv] bit e: event e of the slot has a positive rate
   double *pair_ea;                // [nv * 12] plain barriers of the rows that fell back
   unsigned long long *fallbacks;  // [1] jumps sent to the plain predictor
   int *halt;                      // [1] set by a stop or an error
+  int *net_status;                // [1] set when a tensor-core wait expired
   KmcTraceRec *trace;             // nullable: step s at trace[s - trace_base], s - trace_base < trace_len
   double *plain_ea;               // nullable: the plain barrier of the selected event, same index
   unsigned long long trace_base, trace_len;
@@ -187,9 +189,10 @@ struct KmcSurrogateArgs {
   int *status;
   uint32_t local_bits[kLocalBitWords];
 };
-cudaError_t LaunchKmcSurrogateList(const DevTables &t, const KmcSurrogateArgs &a, cudaStream_t stream);
-cudaError_t LaunchKmcSurrogateStep(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a,
-                                   cudaStream_t stream);
+// j: the lattice and encoding of the fused jump gather (species, n, offsets, channels; its pairs,
+// counts and outputs are unused), with the network's label scale in mean_label / std_label.
+cudaError_t LaunchKmcSurrogate(const DevTables &t, int8_t *species, const KmcSurrogateArgs &a, const MlpDev &d,
+                               const FusedJumps &j, cudaStream_t stream);
 
 // Second-order chain KMC (KineticMcChainOmpi semantics): one block of 12 warps
 // per replica, warp d evaluating the 12 jumps after the jump along direction d.

@@ -135,6 +135,7 @@ struct FusedJumps {
   uint32_t fallback_codes;   // bit c: species code c in the environment sends the row to the plain predictor
   float *mean, *spread;      // [m] ensemble mean (eV) and spread (+inf: plain predictor)
   int *pair_status;          // kStatusBadSite / kStatusNotNeighbor of rejected pairs
+  float mean_label, std_label;  // the network's label scale (the persistent KMC kernel)
 };
 // The fused kernel serves ensembles of 2 members, 128 or 192 inputs (2 or 3 channels per
 // site), hidden 128 (weights kept in shared memory); an expired wait sets *status.
@@ -153,9 +154,8 @@ bool MlpPredictAsync(lmc_mlp *mlp, const uint16_t *x_dev, int64_t n, float *mean
 // The fused jump kernel queued on `stream` (status word as above); false when this network
 // or the inference path setting does not allow it.
 bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream);
-// The fused jump kernel alone (no status reset: stream capture of repeated launches).
-cudaError_t MlpFusedLaunch(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream);
 const MlpDev &MlpDevOf(const lmc_mlp *mlp);
+void MlpLabelScaleOf(const lmc_mlp *mlp, float *mean, float *std_dev);
 int MlpInputs(const lmc_mlp *mlp);
 const int *MlpStatusDev(const lmc_mlp *mlp);
 }  // namespace lmc

@@ -35,23 +35,19 @@
 // while it works on the other member.
 //
 // Operand layout in shared memory: K-major 8-row x 16-byte core matrices, 32-wide K
-// tiles of 128 rows (tcgen05.cuh). Every wait is bounded (sleeping probes, 2 s of wall
+// tiles of 128 rows (tcgen05.cuh); the gather, MMA and epilogue pieces are in mlp_fused.cuh. Every wait is bounded (sleeping probes, 2 s of wall
 // time) and polls a shared abort flag: on expiry the kernel records kMlpFusedTimeout,
 // drains its MMAs and copies, frees its TMEM and returns.
-#include <cuda_bf16.h>
-#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-#include "kernels.cuh"
-#include "lattice_index.cuh"
-#include "mlp.cuh"
-#include "tcgen05.cuh"
+#include "mlp_fused.cuh"
 
 namespace lmc {
 namespace {
 
+using namespace fused;
 using tc::Arrive;
 using tc::ArriveExpectTx;
 using tc::BarInit;
@@ -61,43 +57,19 @@ using tc::FenceAfterSync;
 using tc::FenceAsyncSmem;
 using tc::FenceBarrierInit;
 using tc::FenceBeforeSync;
-using tc::IdescBf16;
-using tc::Mma;
-using tc::MmaTmemA;
-using tc::OperandDesc;
 using tc::Smem;
 using tc::TmemAlloc;
 using tc::TmemFree;
 using tc::TmemLoad32;
-using tc::TmemStore16;
 using tc::WaitDrain;
 using tc::WaitSleep;
 
-constexpr int kRows = 128;      // jumps per tile (MMA M)
-constexpr int kHid = 128;       // hidden width (MMA N of both layers)
-constexpr int kMembers = 2;
-constexpr int kSites = kEnvSites + 1;       // 58 environment sites and the migrant
-constexpr int kTileBytes = kRows * 32 * 2;  // one 128 x 32 operand tile (8 KB)
-constexpr int kProdWarps = 8;               // two per row: sites [0, 32) and [32, 64)
-constexpr int kHalfSites = 32;
+constexpr int kProdWarps = 8;  // two per row: sites [0, 32) and [32, 64)
 constexpr int kMmaWarp = kProdWarps;
 constexpr int kFirstEpi = kProdWarps + 1;
 constexpr int kEpiWarps = 16;
 constexpr int kThreads = 32 * (kFirstEpi + kEpiWarps);
-constexpr uint32_t kCols = 512;
-constexpr uint32_t kMemberCols = 192;       // D (128) and H1 (64) of one member
 constexpr int kFlagRing = 4;
-constexpr uint32_t kIdescL1 = IdescBf16(kRows, kHid);                                    // bf16 x bf16
-constexpr uint32_t kIdescL2 = (1u << 4) | ((kHid >> 3) << 17) | ((kRows >> 4) << 24);  // f16 x f16
-constexpr int kW2Bytes = kMembers * kHid * kHid * 2;
-
-template <int kC>
-struct Shape {
-  static constexpr int kIn = (kSites * kC + 63) / 64 * 64;  // 128 (kC = 2) or 192 (kC = 3)
-  static constexpr int kKt = kIn / 32;                      // layer-1 K tiles
-  static constexpr int kW1Bytes = kMembers * kHid * kIn * 2;
-  static constexpr int kXBytes = kRows * kIn * 2;
-};
 
 struct FusedBars {
   uint64_t w_full, x_full, x_empty;
@@ -120,24 +92,6 @@ constexpr size_t SmemBytes() {
   return static_cast<size_t>(Shape<kC>::kW1Bytes) + kW2Bytes + Shape<kC>::kXBytes + sizeof(FusedBars);
 }
 static_assert(SmemBytes<3>() <= 232448, "the fused kernel's shared memory exceeds 227 KB");
-static_assert(kSites <= 2 * kHalfSites, "a row is gathered in two halves of 32 sites");
-static_assert(2 * kMemberCols <= kCols, "both members' TMEM columns");
-
-// GELU(z) of two values in packed half precision from h = z / 2:
-// u = z (c0 + c1 z^2) = h (2 c0 + 8 c1 h^2), GELU = h + h tanh(u).
-__device__ __forceinline__ __half2 GeluHalf2FromHalfZ(__half2 h) {
-  const __half2 u = __hmul2(h, __hfma2(__hmul2(h, h), __float2half2_rn(8.0f * 0.0356774081363001f),
-                                       __float2half2_rn(2.0f * 0.7978845608028654f)));
-  uint32_t ub = *reinterpret_cast<const uint32_t *>(&u), tb;
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(tb) : "r"(ub));
-  const __half2 t = *reinterpret_cast<const __half2 *>(&tb);
-  return __hfma2(h, t, h);
-}
-
-// Byte offset of row r, 16-byte chunk c (columns 8c .. 8c + 7) in a sequence of 32-wide operand tiles.
-__device__ __forceinline__ uint32_t ChunkOffset(int r, int c) {
-  return static_cast<uint32_t>((c >> 2) * kTileBytes + (r >> 3) * 512 + (c & 3) * 128 + (r & 7) * 16);
-}
 
 // Bounded wait by lane 0 (sleeping probes), its outcome broadcast to the warp.
 __device__ __forceinline__ bool WarpWait(uint64_t *bar, uint32_t parity, volatile int *abort, int lane) {
@@ -146,43 +100,15 @@ __device__ __forceinline__ bool WarpWait(uint64_t *bar, uint32_t parity, volatil
   return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
-// Packed half GELU(2 (v + b)) . w over 32 columns (v and b halved), summed in FP32 per 8 columns.
-__device__ __forceinline__ float GeluDotHalf(const float *v, const __half *b, const __half *w) {
-  float acc = 0.f;
-#pragma unroll
-  for (int g8 = 0; g8 < 4; ++g8) {
-    const uint4 bb = __ldg(reinterpret_cast<const uint4 *>(b + g8 * 8));
-    const uint4 ww = __ldg(reinterpret_cast<const uint4 *>(w + g8 * 8));
-    const uint32_t bw[4] = {bb.x, bb.y, bb.z, bb.w}, wv[4] = {ww.x, ww.y, ww.z, ww.w};
-    __half2 s2 = __float2half2_rn(0.f);
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const __half2 z = __hadd2(__floats2half2_rn(v[g8 * 8 + 2 * e], v[g8 * 8 + 2 * e + 1]),
-                                *reinterpret_cast<const __half2 *>(&bw[e]));
-      s2 = __hfma2(GeluHalf2FromHalfZ(z), *reinterpret_cast<const __half2 *>(&wv[e]), s2);
-    }
-    const float2 f = __half22float2(s2);
-    acc += f.x + f.y;
-  }
-  return acc;
-}
-
-// Producer of half `half` (warps 0-3: 0, warps 4-7: 1) of every row of the CTA's tiles:
-// sites [32 half, 32 half + 32) of the row (MMM-ordered environment, then the migrant; past
-// site 58 nothing), i.e. features [kIn / 2 half, kIn / 2 (half + 1)) (feature kC s + c is
-// channel c of site s). One code path for both halves keeps the kernel's instruction
-// footprint small. Returns the status bits of rejected pairs.
+// Producer of half `half` (warps 0-3: 0, warps 4-7: 1) of every row of the CTA's tiles, with
+// its loads issued before the wait for the feature buffer. One code path for both halves keeps
+// the kernel's instruction footprint small. Returns the status bits of rejected pairs.
 template <int kC>
 __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, long long m_rows, FusedBars *bars,
                                                 unsigned char *sx, long long tiles, int warp, int lane,
                                                 volatile int *abort) {
-  constexpr int kIn = Shape<kC>::kIn;
-  constexpr int kHalfFeat = kIn / 2;
-  static_assert(kHalfFeat == kC * kHalfSites, "a half row is 32 sites");
   const int half = warp >> 2;
   const int r = (warp & 3) * 32 + lane;
-  const int n = j.n;
-  const long long nsites = 4LL * n * n * n;
   unsigned bad_all = 0;
   int t_local = 0;
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
@@ -190,41 +116,9 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, long long m
     int code[kHalfSites];
     bool fallback = true;
     if (row < m_rows) {
-      const long long a = __ldg(&j.pairs[2 * row]), b = __ldg(&j.pairs[2 * row + 1]);
-      unsigned bad = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
-      int di = -1;
-      H3 hi{0, 0, 0};
-      if (!bad) {
-        hi = SiteCoord(a, n);
-        const H3 hj = SiteCoord(b, n);
-        const int dx = WrapDelta(hj.x - hi.x, n), dy = WrapDelta(hj.y - hi.y, n), dz = WrapDelta(hj.z - hi.z, n);
-        if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
-          di = __ldg(&j.dir_of[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)]);
-        if (di < 0) bad = kStatusNotNeighbor;
-      }
+      unsigned bad = 0;
+      fallback = LoadHalfRow(j, __ldg(&j.pairs[2 * row]), __ldg(&j.pairs[2 * row + 1]), half, code, &bad);
       if (half == 0) bad_all |= bad;
-      if (!bad) {
-        // the offsets of this direction, 4 bytes (dx, dy, dz, 0) per site
-        const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
-#pragma unroll
-        for (int k = 0; k < kHalfSites; ++k) {
-          const int site = half * kHalfSites + k;
-          int c = -1;
-          if (site < kEnvSites) {
-            const int o = __ldg(off + site);
-            c = __ldg(&j.species[NeighborId(hi, static_cast<int8_t>(o), static_cast<int8_t>(o >> 8),
-                                            static_cast<int8_t>(o >> 16), n)]);
-          } else if (site == kEnvSites) {
-            c = __ldg(&j.species[b]);
-          }
-          code[k] = c;
-        }
-        unsigned seen = 0;
-#pragma unroll
-        for (int k = 0; k < kHalfSites; ++k)
-          if (half * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
-        fallback = (seen & j.fallback_codes) != 0;
-      }
     }
     if (fallback) {
 #pragma unroll
@@ -232,28 +126,7 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, long long m
     }
     // the X buffer is free once the previous tile's layer-1 MMAs have completed
     if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
-#pragma unroll
-    for (int c = 0; c < kHalfFeat / 8; ++c) {
-      uint32_t w[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int f = 8 * c + 2 * e;  // features f (low half), f + 1 (high half) of this half row
-        uint32_t word;
-        if constexpr (kC == 2) {
-          const int k = f / 2;  // site of features f, f + 1
-          word = code[k] >= 0 ? bars->site_word[code[k] & 7] : 0u;
-        } else {
-          const int k0 = f / kC, k1 = (f + 1) / kC;
-          const int ch0 = bars->chan[code[k0] & 7], ch1 = bars->chan[code[k1] & 7];
-          word = ((code[k0] >= 0 && ch0 == f % kC) ? 0x3F80u : 0u) |
-                 ((code[k1] >= 0 && ch1 == (f + 1) % kC) ? 0x3F800000u : 0u);
-        }
-        if (f + 1 == kHalfFeat - 1 && half == 1) word |= 0x3F800000u;  // the last feature is 1: the bias column
-        w[e] = word;
-      }
-      *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, half * (kHalfFeat / 8) + c)) =
-          make_uint4(w[0], w[1], w[2], w[3]);
-    }
+    WriteHalfRow<kC>(code, bars->site_word, bars->chan, half, r, sx);
     const unsigned fb = __ballot_sync(0xffffffffu, fallback);
     if (lane == 0) bars->flag[t_local % kFlagRing][warp] = fb;
     FenceAsyncSmem();
@@ -333,25 +206,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int m = 0; m < kMembers && ok; ++m) {
           if (t_local >= 1 && !(ok = WaitSleep(&bars->acc_empty[m], (t_local - 1) & 1, abort))) break;
           FenceAfterSync();
-          const uint32_t dcol = tmem + m * kMemberCols;
-          for (int c = 0; c < S::kKt; ++c) {
-            const uint32_t a = a1 + c * kTileBytes, b = b1 + (m * S::kKt + c) * kTileBytes;
-            Mma(dcol, OperandDesc(a), OperandDesc(b), kIdescL1, c > 0);
-            Mma(dcol, OperandDesc(a + 256), OperandDesc(b + 256), kIdescL1, true);
-          }
+          IssueLayer1<kC>(tmem, a1, b1, m);
           Commit(&bars->acc_full[m]);
         }
         if (!ok) break;
         Commit(&bars->x_empty);
-        // layer 2, A = H1 in TMEM (16 K per MMA = 8 columns), once the epilogue has written it
+        // layer 2, A = H1 in TMEM, once the epilogue has written it
         for (int m = 0; m < kMembers && ok; ++m) {
           if (!(ok = WaitSleep(&bars->h1_full[m], t_local & 1, abort))) break;
           FenceAfterSync();
-          const uint32_t dcol = tmem + m * kMemberCols, hcol = dcol + kHid;
-          for (int c = 0; c < kHid / 16; ++c) {
-            const uint32_t b = b2 + (m * (kHid / 32) + (c >> 1)) * kTileBytes + (c & 1) * 256;
-            MmaTmemA(dcol, hcol + c * 8, OperandDesc(b), kIdescL2, c > 0);
-          }
+          IssueLayer2(tmem, b2, m);
           Commit(&bars->acc_full[m]);
         }
       }
@@ -380,16 +244,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int m = 0; m < kMembers && ok; ++m) {
         if (!(ok = WarpWait(&bars->acc_full[m], 0, abort, lane))) break;
         FenceAfterSync();
-        const uint32_t dcol = tmem + lane_base + m * kMemberCols;
-        float v[32];
-        TmemLoad32(dcol + q * 32, v);
-        uint32_t packed[16];
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const __half2 p = GeluHalf2FromHalfZ(__floats2half2_rn(v[2 * e], v[2 * e + 1]));
-          packed[e] = *reinterpret_cast<const uint32_t *>(&p);
-        }
-        TmemStore16(dcol + kHid + q * 16, packed);
+        Layer1Epilogue(tmem + lane_base + m * kMemberCols, q * 32);
         FenceBeforeSync();
         __syncwarp();
         if (lane == 0) Arrive(&bars->h1_full[m]);

@@ -123,10 +123,11 @@ bool MlpFusedJumpsAsync(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream) 
             "fused surrogate kernel");
   return true;
 }
-cudaError_t MlpFusedLaunch(lmc_mlp *mlp, const FusedJumps &j, cudaStream_t stream) {
-  return lmc::MlpFusedPredict(mlp->d, j, mlp->label_mean, mlp->label_std, mlp->status, stream);
-}
 const MlpDev &MlpDevOf(const lmc_mlp *mlp) { return mlp->d; }
+void MlpLabelScaleOf(const lmc_mlp *mlp, float *mean, float *std_dev) {
+  *mean = mlp->label_mean;
+  *std_dev = mlp->label_std;
+}
 int MlpInputs(const lmc_mlp *mlp) { return mlp->d.in; }
 const int *MlpStatusDev(const lmc_mlp *mlp) { return mlp->status; }
 
