@@ -631,7 +631,7 @@ def run_large_surrogate(args, ctx, sp, T):
     del x, ea
     ctx.kmc_multi_init([T], seed=3)
     # a traced run: the barriers used for the selected events against the plain predictor's
-    traced = 20_000
+    traced = args.large_surrogate_traced
     tr, plain_ea, nfb_traced = ctx.kmc_multi_surrogate_run(net, traced, 0.010, trace=True)
     err = np.abs(tr["ea"] - plain_ea)
     events = args.large_kmc_events
@@ -936,6 +936,8 @@ def main():
     ap.add_argument("--sa-steps", type=int, default=200_000, help="simulated-annealing trial moves (0 skips)")
     ap.add_argument("--large-cmc-sweeps", type=int, default=100, help="CMC sweeps on the n=64 lattice")
     ap.add_argument("--large-kmc-events", type=int, default=1_000_000, help="multi-vacancy KMC events, n=64")
+    ap.add_argument("--large-surrogate-traced", type=int, default=20_000,
+                    help="traced surrogate-assisted steps (barrier error of the selected events), n=64")
     ap.add_argument("--no-large", action="store_true", help="skip the n=64, 64-vacancy block")
     ap.add_argument("--tune-probe-steps", type=int, default=100, help="KMC steps per autotuner probe")
     ap.add_argument("--tune-cache", default=os.environ.get("LMC_KMC_TUNE_CACHE", ""),

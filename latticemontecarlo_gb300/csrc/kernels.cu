@@ -89,21 +89,11 @@ struct JumpAcc {
   unsigned bad;
 };
 
-// Per-lane partial sums of one jump's three linear forms from the sorted
-// species arrays: st = state list codes (60), rm/rf/rb = MMM / MM2-forward /
-// MM2-backward one-hot ranks (58 each, rank 7 = no slot).
-//   de: sum over state clusters with exactly one pair site of
-//       W(end tuple) - W(start tuple)   (clusters with both pair sites cancel)
-//   d : sum over MMM clusters of the D (Quartic) or e0 (E0) weights
-//   ks: sum over MM2 clusters of the forward and backward lists (Quartic)
-// `lane` and `stride`: this thread's first cluster and the step (a warp: lane, 32; a block:
-// thread index, block size).
-template <bool kQuartic>
-__device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const int8_t *st, const int8_t *rm,
-                                            const int8_t *rf, const int8_t *rb, const uint32_t *s_de,
-                                            const uint32_t *s_mmm, const uint32_t *s_mm2, const int8_t *s_pt,
-                                            int lane, int stride = 32) {
-  JumpAcc a{0, 0, 0, 0u};
+// The energy-change part of EvalJump: state clusters with exactly one pair site, and (first
+// site not a vacancy) the clusters holding both pair sites and the two singlets.
+__device__ __forceinline__ void AccumulateDe(const DevTables &t, const int8_t *st, const uint32_t *s_de, int lane,
+                                             int stride, JumpAcc *acc) {
+  JumpAcc &a = *acc;
   const int e = t.num_species;
   const int x = t.x_code;
   const int si = st[t.pos_first];
@@ -148,6 +138,24 @@ __device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const 
       a.de += we - ws;
     }
   }
+}
+
+// Per-lane partial sums of one jump's three linear forms from the sorted
+// species arrays: st = state list codes (60), rm/rf/rb = MMM / MM2-forward /
+// MM2-backward one-hot ranks (58 each, rank 7 = no slot).
+//   de: sum over state clusters with exactly one pair site of
+//       W(end tuple) - W(start tuple)   (clusters with both pair sites cancel)
+//   d : sum over MMM clusters of the D (Quartic) or e0 (E0) weights
+//   ks: sum over MM2 clusters of the forward and backward lists (Quartic)
+// `lane` and `stride`: this thread's first cluster and the step (a warp: lane, 32; a block:
+// thread index, block size).
+template <bool kQuartic>
+__device__ __forceinline__ JumpAcc EvalJump(const DevTables &t, int slot, const int8_t *st, const int8_t *rm,
+                                            const int8_t *rf, const int8_t *rb, const uint32_t *s_de,
+                                            const uint32_t *s_mmm, const uint32_t *s_mm2, const int8_t *s_pt,
+                                            int lane, int stride = 32) {
+  JumpAcc a{0, 0, 0, 0u};
+  AccumulateDe(t, st, s_de, lane, stride, &a);
   const long long *__restrict__ wd = (kQuartic ? t.w_d : t.w_e0) + static_cast<long long>(slot) * t.f_mmm;
   for (int c = lane; c < t.n_mmm_cl; c += stride) {
     const uint32_t w = s_mmm[c];
@@ -2705,11 +2713,12 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
 // The plain predictor's barrier and energy change of jump a -> b on the current lattice,
 // evaluated by the whole block: the sorted arrays gathered into shared memory, the cluster sums
 // split over all threads (int64 sums, independent of their order: the same bits as one warp's),
-// the FP64 epilogue by thread 0 into out[0] (barrier) and out[1] (energy change). Called by every
-// thread of the block (it holds block-wide barriers); returns the status bits (thread 0).
+// the FP64 epilogue by thread 0 into out[0] (barrier) and out[1] (energy change). With full =
+// false only the energy change (state clusters; out[0] is NaN). Called by every thread of the
+// block (it holds block-wide barriers); returns the status bits (thread 0).
 __device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int n, long long a, long long b, int kind,
-                                     const SmallTables *small, int8_t *st, int8_t *rm, int8_t *rf, int8_t *rb,
-                                     long long *red, unsigned *red_bad, double *out) {
+                                     bool full, const SmallTables *small, int8_t *st, int8_t *rm, int8_t *rf,
+                                     int8_t *rb, long long *red, unsigned *red_bad, double *out) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, warps = blockDim.x >> 5;
   H3 hi, hj;
   int di = -1, db = -1;
@@ -2719,7 +2728,7 @@ __device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int 
       const int8_t *o = t.state_off + (di * kStateSites + k) * 4;
       st[k] = lat[NeighborId(hi, o[0], o[1], o[2], n)];
     }
-    for (int k = tid; k < kEnvSites; k += blockDim.x) {
+    for (int k = tid; full && k < kEnvSites; k += blockDim.x) {
       const int8_t *oa = t.mmm_off + (di * kEnvSites + k) * 4;
       const int8_t *ob = t.mm2_off + (di * kEnvSites + k) * 4;
       const int8_t *oc = t.mm2_off + (db * kEnvSites + k) * 4;
@@ -2730,15 +2739,18 @@ __device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int 
   }
   __syncthreads();
   int slot = -1;
-  if (!bad) {
+  if (!bad && full) {
     slot = small->slot[st[t.pos_second]];
     if (slot < 0 || (kind == 0 ? !small->has_quartic[slot] : !small->has_e0[slot])) bad = kStatusNoCoefficients;
   }
   if (!bad) {
-    const JumpAcc acc = kind == 0 ? EvalJump<true>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl,
-                                                   small->pairtype, tid, blockDim.x)
-                                  : EvalJump<false>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl,
-                                                    small->pairtype, tid, blockDim.x);
+    JumpAcc acc{0, 0, 0, 0u};
+    if (!full)
+      AccumulateDe(t, st, t.de_cl, tid, blockDim.x, &acc);
+    else if (kind == 0)
+      acc = EvalJump<true>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl, small->pairtype, tid, blockDim.x);
+    else
+      acc = EvalJump<false>(t, slot, st, rm, rf, rb, t.de_cl, t.mmm_cl, t.mm2_cl, small->pairtype, tid, blockDim.x);
     const long long s_de = WarpSum(acc.de), s_d = WarpSum(acc.d), s_ks = WarpSum(acc.ks);
     const unsigned s_bad = __reduce_or_sync(0xffffffffu, acc.bad);
     if (lane == 0) {
@@ -2761,10 +2773,15 @@ __device__ unsigned BlockPairBarrier(const DevTables &t, const int8_t *lat, int 
         acc_ks += red[3 * w + 2];
         bad |= red_bad[w];
       }
-      const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
-      out[0] = o.ea;
-      out[1] = o.de;
-      if (!isfinite(o.ea)) bad |= kStatusNumeric;
+      if (full) {
+        const JumpOut o = JumpEpilogue(t, ExpConsts{t.exp_tab, t.exp_l1, t.exp_l2}, kind, slot, acc_de, acc_d, acc_ks);
+        out[0] = o.ea;
+        out[1] = o.de;
+        if (!isfinite(o.ea)) bad |= kStatusNumeric;
+      } else {
+        out[0] = nan("");
+        out[1] = static_cast<double>(acc_de) * t.de_scale;  // as JumpEpilogue
+      }
     }
   }
   __syncthreads();
@@ -2779,7 +2796,8 @@ struct SurShared {
   uint32_t tmem;
   uint32_t site_word[8];
   int8_t chan[8];
-  uint32_t flag[2][4];                 // per half row and lane group: bit l, row 32 lg + l takes the plain predictor
+  uint32_t flag[4][4];                 // per row part and lane group: bit l, row 32 lg + l takes the plain predictor
+  H3 h[kMaxMultiVac];                  // coordinates of each slot's vacancy
   float partial[2][fused::kMembers][fused::kRows];  // per column half and member: GELU . w3 of each row
   SmallTables small;
   int8_t arr[kArr];                    // the block's sorted arrays (BlockPairBarrier)
@@ -2848,10 +2866,14 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
   for (int i = tid; i < nv * 12; i += blockDim.x) {
     const int v = i / 12, dd = i % 12;
     const long long pos = a.vac_pos[v];
+    const H3 hv = SiteCoord(pos, n);
     const int8_t *o = t.dir + dd * 4;
     a.pairs[2 * i] = pos;
-    a.pairs[2 * i + 1] = NeighborId(SiteCoord(pos, n), o[0], o[1], o[2], n);
-    if (dd == 0) a.dirty[v] = v;
+    a.pairs[2 * i + 1] = NeighborId(hv, o[0], o[1], o[2], n);
+    if (dd == 0) {
+      a.dirty[v] = v;
+      sh->h[v] = hv;
+    }
   }
   if (warp == 0) tc::TmemAlloc(&sh->tmem, fused::kCols);
   tc::FenceBeforeSync();
@@ -2866,26 +2888,30 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
   bool weights = false;
   unsigned bad_all = 0;
   unsigned long long nfb_total = 0;
+  const unsigned long long step0 = *a.steps;
+  // Philox draws for 32 steps at a time (warp 0): lane l holds -log(u1) and u2 of step (it & ~31) + l
+  double nlog_blk = 0.0, u2_blk = 0.0;
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
     const int rows = sh->rows;
     // ---- A: the network on the listed rows, 128 per tile ----
     for (int t0 = 0; t0 < rows; t0 += fused::kRows) {
-      if (tid < 2 * fused::kRows) {
-        const int half = tid >> 7, r = tid & 127, row = t0 + r;
-        int code[fused::kHalfSites];
+      {
+        // four threads per row: part = tid / 128 takes sites [16 part, 16 part + 16)
+        const int part = tid >> 7, r = tid & 127, row = t0 + r;
+        int code[16];
         bool fb = true;
         if (row < rows) {
           unsigned b = 0;
-          fb = fused::LoadHalfRow<false>(j, a.pairs[2 * row], a.pairs[2 * row + 1], half, code, &b);
+          fb = fused::LoadRowPart<4, false>(j, a.pairs[2 * row], a.pairs[2 * row + 1], part, code, &b);
           bad_all |= b;
         }
         if (fb) {
 #pragma unroll
-          for (int k = 0; k < fused::kHalfSites; ++k) code[k] = -1;
+          for (int k = 0; k < 16; ++k) code[k] = -1;
         }
-        fused::WriteHalfRow<kC>(code, sh->site_word, sh->chan, half, r, sx);
+        fused::WriteRowPart<kC, 4>(code, sh->site_word, sh->chan, part, r, sx);
         const unsigned m = __ballot_sync(0xffffffffu, fb);
-        if (lane == 0) sh->flag[half][(tid >> 5) & 3] = m;
+        if (lane == 0) sh->flag[part][(tid >> 5) & 3] = m;
         tc::FenceAsyncSmem();
       }
       __syncthreads();
@@ -2903,8 +2929,12 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
       __syncthreads();
       if (*abort) break;
       tc::FenceAfterSync();
-      fused::Layer1Epilogue(ecol, hh * 64);
-      fused::Layer1Epilogue(ecol, hh * 64 + 32);
+      // lane groups past the tile's last listed row hold no rows: their warps skip the epilogues
+      const bool rows_here = lg * 32 < rows - t0;
+      if (rows_here) {
+        fused::Layer1Epilogue(ecol, hh * 64);
+        fused::Layer1Epilogue(ecol, hh * 64 + 32);
+      }
       tc::FenceBeforeSync();
       __syncthreads();
       if (tid == 0) {
@@ -2918,7 +2948,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
       __syncthreads();
       if (*abort) break;
       tc::FenceAfterSync();
-      {
+      if (rows_here) {
         float v[32];
         float acc = 0.f;
 #pragma unroll 1
@@ -2936,7 +2966,8 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
         if (row < rows) {
           const float y0 = sh->partial[0][0][r] + sh->partial[1][0][r] + __ldg(&d.b3[0]);
           const float y1 = sh->partial[0][1][r] + sh->partial[1][1][r] + __ldg(&d.b3[1]);
-          const bool fb = (((sh->flag[0][warp] | sh->flag[1][warp]) >> lane) & 1u) != 0;
+          const bool fb = (((sh->flag[0][warp] | sh->flag[1][warp] | sh->flag[2][warp] | sh->flag[3][warp]) >> lane) &
+                           1u) != 0;
           a.mean[row] = j.mean_label + j.std_label * 0.5f * (y0 + y1);
           a.spread[row] = fb ? __int_as_float(0x7f800000) : j.std_label * fabsf(y0 - y1);
         }
@@ -2966,7 +2997,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
     const int nfb = sh->nfb;
     for (int i = 0; i < nfb; ++i) {
       const int row = sh->fb[i];
-      const unsigned b = BlockPairBarrier(t, lat, n, a.pairs[2 * row], a.pairs[2 * row + 1], a.barrier_kind,
+      const unsigned b = BlockPairBarrier(t, lat, n, a.pairs[2 * row], a.pairs[2 * row + 1], a.barrier_kind, true,
                                           &sh->small, st, rm, rf, rb, sh->red, sh->red_bad, sh->out);
       if (tid == 0) {
         bad_all |= b & ~kVacancyBits;
@@ -3018,7 +3049,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
     }
     __syncthreads();
     // ---- D: selection (warp 0) ----
-    const unsigned long long step = *a.steps;
+    const unsigned long long step = step0 + it;
     if (warp == 0) {
       bool halt = false;
       if (a.stop_flag && (step & 63) == 0 && *a.stop_flag) {
@@ -3026,10 +3057,15 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
         halt = true;
       }
       if (!halt) {
-        const uint4 xr = PhiloxRound10(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32),
-                                       static_cast<uint32_t>(a.replica), 0x4b4d43u, a.key0, a.key1);
-        const double nlog_u1 = -log(U01Open(xr.x, xr.y));
-        const double u2 = U01(xr.z, xr.w);
+        if ((it & 31) == 0) {
+          const unsigned long long ctr = step + lane;
+          const uint4 xr = PhiloxRound10(static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                         static_cast<uint32_t>(a.replica), 0x4b4d43u, a.key0, a.key1);
+          nlog_blk = -log(U01Open(xr.x, xr.y));
+          u2_blk = U01(xr.z, xr.w);
+        }
+        const double nlog_u1 = __shfl_sync(0xffffffffu, nlog_blk, static_cast<int>(it & 31));
+        const double u2 = __shfl_sync(0xffffffffu, u2_blk, static_cast<int>(it & 31));
         const int chunks = (nv + 31) >> 5;
         double run = 0.0;
         for (int c = 0; c < chunks; ++c) {
@@ -3081,8 +3117,9 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
     if (sh->halt) break;
     // ---- D: the plain predictor's energy change of the selected jump (before the move) ----
     const long long p_old = sh->sel[0], tgt = sh->sel[1];
-    const unsigned b = BlockPairBarrier(t, lat, n, p_old, tgt, a.barrier_kind, &sh->small, st, rm, rf, rb, sh->red,
-                                        sh->red_bad, sh->out);
+    // the energy change alone, unless the run records the plain barrier of each selected event
+    const unsigned b = BlockPairBarrier(t, lat, n, p_old, tgt, a.barrier_kind, a.plain_ea != nullptr, &sh->small, st,
+                                        rm, rf, rb, sh->red, sh->red_bad, sh->out);
     if (tid == 0) bad_all |= b & ~kVacancyBits;
     // ---- D: the move and the next list (warp 0) ----
     if (warp == 0) {
@@ -3090,11 +3127,12 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
       const double ea_plain = sh->out[0], de_sel = sh->out[1];
       const double time = *a.time + sh->sel_nlog * RcpFast(sh->sel_total * kPrefactor);
       const double energy = *a.energy + de_sel;
-      const H3 h_old = SiteCoord(p_old, n), h_new = SiteCoord(tgt, n);
+      const H3 h_old = sh->h[vsel], h_new = SiteCoord(tgt, n);
       if (lane == 0) {
         lat[p_old] = lat[tgt];  // Config::LatticeJump
         lat[tgt] = static_cast<int8_t>(x_code);
         a.vac_pos[vsel] = tgt;
+        sh->h[vsel] = h_new;
         *a.time = time;
         *a.energy = energy;
         *a.steps = step + 1;
@@ -3123,7 +3161,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
         const int v = c * 32 + lane;
         bool dv = false;
         if (v < nv) {
-          const H3 hv = v == vsel ? h_new : SiteCoord(a.vac_pos[v], n);
+          const H3 hv = v == vsel ? h_new : sh->h[v];
           dv = v == vsel ||
                InLocal(sh->bits, WrapDelta(h_old.x - hv.x, n), WrapDelta(h_old.y - hv.y, n),
                        WrapDelta(h_old.z - hv.z, n)) ||
@@ -3141,7 +3179,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
           const long long pv = v == vsel ? tgt : a.vac_pos[v];
           const int8_t *o = t.dir + lane * 4;
           a.pairs[2 * (i * 12 + lane)] = pv;
-          a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : SiteCoord(pv, n), o[0], o[1], o[2], n);
+          a.pairs[2 * (i * 12 + lane) + 1] = NeighborId(v == vsel ? h_new : sh->h[v], o[0], o[1], o[2], n);
         }
       }
       if (lane == 0) sh->rows = nd2 * 12;

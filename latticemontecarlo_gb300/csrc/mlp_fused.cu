@@ -113,20 +113,20 @@ __device__ __forceinline__ unsigned ProduceRows(const FusedJumps &j, long long m
   int t_local = 0;
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
     const long long row = tile * kRows + r;
-    int code[kHalfSites];
+    int code[32];
     bool fallback = true;
     if (row < m_rows) {
       unsigned bad = 0;
-      fallback = LoadHalfRow(j, __ldg(&j.pairs[2 * row]), __ldg(&j.pairs[2 * row + 1]), half, code, &bad);
+      fallback = LoadRowPart<2>(j, __ldg(&j.pairs[2 * row]), __ldg(&j.pairs[2 * row + 1]), half, code, &bad);
       if (half == 0) bad_all |= bad;
     }
     if (fallback) {
 #pragma unroll
-      for (int k = 0; k < kHalfSites; ++k) code[k] = -1;
+      for (int k = 0; k < 32; ++k) code[k] = -1;
     }
     // the X buffer is free once the previous tile's layer-1 MMAs have completed
     if (t_local >= 1 && !WarpWait(&bars->x_empty, (t_local - 1) & 1, abort, lane)) break;
-    WriteHalfRow<kC>(code, bars->site_word, bars->chan, half, r, sx);
+    WriteRowPart<kC, 2>(code, bars->site_word, bars->chan, half, r, sx);
     const unsigned fb = __ballot_sync(0xffffffffu, fallback);
     if (lane == 0) bars->flag[t_local % kFlagRing][warp] = fb;
     FenceAsyncSmem();

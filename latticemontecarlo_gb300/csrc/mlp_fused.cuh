@@ -31,13 +31,12 @@ constexpr int kHid = 128;                   // hidden width (MMA N of both layer
 constexpr int kMembers = 2;
 constexpr int kSites = kEnvSites + 1;       // 58 environment sites and the migrant
 constexpr int kTileBytes = kRows * 32 * 2;  // one 128 x 32 operand tile (8 KB)
-constexpr int kHalfSites = 32;              // sites gathered per half row
 constexpr uint32_t kCols = 512;             // TMEM columns allocated
 constexpr uint32_t kMemberCols = 192;       // D (128) and H1 (64) of one member
 constexpr uint32_t kIdescL1 = tc::IdescBf16(kRows, kHid);                                // bf16 x bf16
 constexpr uint32_t kIdescL2 = (1u << 4) | ((kHid >> 3) << 17) | ((kRows >> 4) << 24);  // f16 x f16
 constexpr int kW2Bytes = kMembers * kHid * kHid * 2;
-static_assert(kSites <= 2 * kHalfSites, "a row is gathered in two halves of 32 sites");
+static_assert(kSites <= 64, "a row is gathered in parts of 64 sites");
 static_assert(2 * kMemberCols <= kCols, "both members' TMEM columns");
 
 template <int kC>
@@ -46,8 +45,6 @@ struct Shape {
   static constexpr int kKt = kIn / 32;                      // layer-1 K tiles
   static constexpr int kW1Bytes = kMembers * kHid * kIn * 2;
   static constexpr int kXBytes = kRows * kIn * 2;
-  static constexpr int kHalfFeat = kIn / 2;
-  static_assert(kHalfFeat == kC * kHalfSites, "a half row is 32 sites");
 };
 
 // GELU(z) of two values in packed half precision from h = z / 2:
@@ -95,13 +92,14 @@ __device__ __forceinline__ int8_t LatticeLoad(const int8_t *p) {
   return *p;
 }
 
-// Species codes of half `half` of jump a -> b: sites [32 half, 32 half + 32) of the row
-// (MMM-ordered environment, then the migrant at site 58; past it -1). Returns whether the
-// row must take the plain predictor (rejected pair, or a species without a one-hot slot in
-// its environment); *bad receives the rejected-pair status bits.
-template <bool kReadOnly = true>
-__device__ __forceinline__ bool LoadHalfRow(const FusedJumps &j, long long a, long long b, int half,
-                                            int (&code)[kHalfSites], unsigned *bad) {
+// Species codes of part `part` of kParts of jump a -> b: sites [S part, S part + S) of the row,
+// S = 64 / kParts (MMM-ordered environment, then the migrant at site 58; past it -1). Returns
+// whether the row must take the plain predictor (rejected pair, or a species without a one-hot
+// slot in its environment); *bad receives the rejected-pair status bits.
+template <int kParts, bool kReadOnly = true>
+__device__ __forceinline__ bool LoadRowPart(const FusedJumps &j, long long a, long long b, int part,
+                                            int (&code)[64 / kParts], unsigned *bad) {
+  constexpr int kS = 64 / kParts;
   const int n = j.n;
   const long long nsites = 4LL * n * n * n;
   unsigned st = (a < 0 || b < 0 || a >= nsites || b >= nsites) ? kStatusBadSite : 0u;
@@ -120,8 +118,8 @@ __device__ __forceinline__ bool LoadHalfRow(const FusedJumps &j, long long a, lo
   // the offsets of this direction, 4 bytes (dx, dy, dz, 0) per site
   const int *off = reinterpret_cast<const int *>(j.mmm_off) + di * kEnvSites;
 #pragma unroll
-  for (int k = 0; k < kHalfSites; ++k) {
-    const int site = half * kHalfSites + k;
+  for (int k = 0; k < kS; ++k) {
+    const int site = part * kS + k;
     int c = -1;
     if (site < kEnvSites) {
       const int o = __ldg(off + site);
@@ -134,24 +132,25 @@ __device__ __forceinline__ bool LoadHalfRow(const FusedJumps &j, long long a, lo
   }
   unsigned seen = 0;
 #pragma unroll
-  for (int k = 0; k < kHalfSites; ++k)
-    if (half * kHalfSites + k < kSites) seen |= 1u << (code[k] & 7);
+  for (int k = 0; k < kS; ++k)
+    if (part * kS + k < kSites) seen |= 1u << (code[k] & 7);
   return (seen & j.fallback_codes) != 0;
 }
 
-// Writes half `half` of feature row r into the operand tiles at sx (code -1: an all-zero site;
-// the last feature of the row, in half 1, is 1: the bias column). kC = 2 takes the per-species
-// row words site_word, kC = 3 the per-species channels chan (shared memory).
-template <int kC>
-__device__ __forceinline__ void WriteHalfRow(const int (&code)[kHalfSites], const uint32_t *site_word,
-                                             const int8_t *chan, int half, int r, unsigned char *sx) {
-  constexpr int kHalfFeat = Shape<kC>::kHalfFeat;
+// Writes part `part` of kParts of feature row r into the operand tiles at sx (code -1: an
+// all-zero site; the last feature of the row, in the last part, is 1: the bias column). kC = 2
+// takes the per-species row words site_word, kC = 3 the per-species channels chan.
+template <int kC, int kParts>
+__device__ __forceinline__ void WriteRowPart(const int (&code)[64 / kParts], const uint32_t *site_word,
+                                             const int8_t *chan, int part, int r, unsigned char *sx) {
+  constexpr int kPartFeat = kC * (64 / kParts);
+  static_assert(kPartFeat % 8 == 0 && kPartFeat * kParts == Shape<kC>::kIn, "a part is whole 16-byte chunks");
 #pragma unroll
-  for (int c = 0; c < kHalfFeat / 8; ++c) {
+  for (int c = 0; c < kPartFeat / 8; ++c) {
     uint32_t w[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int f = 8 * c + 2 * e;  // features f (low half), f + 1 (high half) of this half row
+      const int f = 8 * c + 2 * e;  // features f (low half), f + 1 (high half) of this part
       uint32_t word;
       if constexpr (kC == 2) {
         const int k = f / 2;  // site of features f, f + 1
@@ -162,10 +161,10 @@ __device__ __forceinline__ void WriteHalfRow(const int (&code)[kHalfSites], cons
         word = ((code[k0] >= 0 && ch0 == f % kC) ? 0x3F80u : 0u) |
                ((code[k1] >= 0 && ch1 == (f + 1) % kC) ? 0x3F800000u : 0u);
       }
-      if (f + 1 == kHalfFeat - 1 && half == 1) word |= 0x3F800000u;  // bf16 1.0: the bias column
+      if (f + 1 == kPartFeat - 1 && part == kParts - 1) word |= 0x3F800000u;  // bf16 1.0: the bias column
       w[e] = word;
     }
-    *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, half * (kHalfFeat / 8) + c)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(sx + ChunkOffset(r, part * (kPartFeat / 8) + c)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
