@@ -289,7 +289,7 @@ def run_cmc(args, device, flush, barrier):
     e = 0.0
     for _ in range(2):
         e, _, _ = ctx.cmc_run(cfg["T"], attempts, mode=N.LMC_CMC_THROUGHPUT, seed=1, energy=e)
-    ms, done_total = [], 0
+    ms, done_total, rounds = [], 0, 0
     barrier()
     for k in range(args.cmc_steps):
         flush.fill_(1.0)
@@ -297,6 +297,7 @@ def run_cmc(args, device, flush, barrier):
         e, done, acc = ctx.cmc_run(cfg["T"], attempts, mode=N.LMC_CMC_THROUGHPUT, seed=2 + k, energy=e)
         ms.append(ctx.last_run_ms())
         done_total += done
+        rounds += ctx.cmc_rounds()
     barrier()
     value = done_total / (np.sum(ms) / 1e3)
     peak, _ = peaks()
@@ -304,6 +305,8 @@ def run_cmc(args, device, flush, barrier):
            "workload": "CMC 30^3 FCC (108000 sites), Al/Mg/Zn/Cu .94/.02/.02/.02, T=500 K, "
                        f"{args.cmc_sweeps_per_step} sweeps per step, non-overlapping pairs per round",
            "steps": args.cmc_steps, "ms_per_step": float(np.mean(ms)),
+           "rounds": {"count": rounds, "survivors_per_round": done_total / max(1, rounds),
+                      "us_per_round": float(np.sum(ms)) * 1e3 / max(1, rounds)},
            "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * value / 1e9, "peak": peak,
                         "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * value / 1e9 / peak}}
     if args.cmc_ref_attempts > 0:
@@ -553,8 +556,11 @@ def run_large(args, device):
         e, done, acc = ctx.cmc_run(T, attempts, mode=N.LMC_CMC_THROUGHPUT, seed=2, energy=e0)
         ms = ctx.last_run_ms()
         v = done / (ms / 1e3)
+        rounds = ctx.cmc_rounds()
         out["cmc"] = {"sweeps": args.large_cmc_sweeps, "attempts": int(done), "accepted": int(acc), "ms": ms,
                       "value": v, "unit": "swaps/s (Metropolis attempts)",
+                      "rounds": {"count": rounds, "survivors_per_round": done / max(1, rounds),
+                                 "us_per_round": ms * 1e3 / max(1, rounds)},
                       "roofline": {"bound": "hbm", "achieved": BYTES_PER_ATTEMPT * v / 1e9, "peak": peak,
                                    "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * v / 1e9 / peak}}
         ctx.set_lattices([L["n"]], sp)

@@ -524,6 +524,11 @@ typedef struct lmc_cmc_options {
 int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts, const lmc_cmc_options *opt,
                 double *energy_io, uint64_t *attempts_done, uint64_t *accepted);
 
+/* Rounds of the last throughput-mode lmc_cmc_run (each round: draw, claim, grid barrier, dE and
+ * Metropolis tests of the survivors, grid barrier); 0 after a reference-batch run. Diagnostic, no
+ * reference counterpart. */
+int lmc_cmc_rounds(const lmc_ctx *ctx, uint64_t *rounds);
+
 /* Host-writable stop flag polled by persistent kernels; also clears it when value = 0. */
 int lmc_request_stop(lmc_ctx *ctx, int value);
 

@@ -405,6 +405,12 @@ class Context:
                                 C.byref(acc)))
         return e.value, done.value, acc.value
 
+    def cmc_rounds(self) -> int:
+        """Rounds of the last throughput-mode cmc_run."""
+        r = C.c_uint64()
+        check(N.lib.lmc_cmc_rounds(self._h, C.byref(r)))
+        return r.value
+
     def request_stop(self, value: int = 1) -> None:
         check(N.lib.lmc_request_stop(self._h, value))
 

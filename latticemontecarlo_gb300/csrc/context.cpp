@@ -105,6 +105,7 @@ struct lmc_ctx {
   lmc::KmcSparse sparse{};
   // CMC
   DevBuf c_claim, c_cand, c_eacc, c_stats;
+  unsigned long long cmc_rounds{0};  // rounds of the last throughput-mode run
   std::map<int, std::pair<uint64_t, DevBuf>> c_mt;  // per replica: seed and MT state
   // host-mapped stop flag
   int *h_stop{nullptr};
@@ -2773,6 +2774,7 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
       a.quit = d_quit;
       a.status = ctx->status.as<int>();
       a.stop_flag = ctx->d_stop;
+      a.rounds = d_done + 3;
       CudaCheck(cudaEventRecord(ctx->ev0, ctx->stream), "event");
       CudaCheck(lmc::LaunchCmcThroughput(ctx->t, lat, a, ctx->device, ctx->stream), "CMC kernel");
       CudaCheck(cudaEventRecord(ctx->ev1, ctx->stream), "event");
@@ -2785,16 +2787,24 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
     } else {
       throw LmcError(LMC_ERR_INVALID_ARGUMENT, "unknown CMC mode");
     }
-    unsigned long long stats[2] = {0, 0};
+    unsigned long long stats[4] = {0, 0, 0, 0};
     CudaCheck(cudaMemcpyAsync(stats, d_done, sizeof(stats), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
     const int st = ctx->ReadStatus();
     float ms = 0;
     CudaCheck(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "elapsed");
     ctx->last_ms = ms;
+    ctx->cmc_rounds = opt->mode == LMC_CMC_THROUGHPUT ? stats[3] : 0;
     RaiseStatus(st, "CMC run");
     *energy_io = e_out;
     if (attempts_done) *attempts_done = stats[0];
     if (accepted) *accepted = stats[1];
+  });
+}
+
+int lmc_cmc_rounds(const lmc_ctx *ctx, uint64_t *rounds) {
+  return Guard([&] {
+    Require(ctx && rounds, LMC_ERR_INVALID_ARGUMENT, "null argument");
+    *rounds = ctx->cmc_rounds;
   });
 }
 

@@ -3720,6 +3720,7 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
       atomicOr(a.status, kStatusStopped);
       atomicExch(a.quit, 1);
     }
+    if (gtid == 0 && a.rounds) ++*a.rounds;
     grid.sync();
   }
   __syncthreads();

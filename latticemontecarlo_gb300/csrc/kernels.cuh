@@ -355,6 +355,7 @@ struct CmcTpArgs {
   int *quit;                 // device word, zero on entry
   int *status;
   volatile int *stop_flag;
+  unsigned long long *rounds;  // nullable: rounds run (zero on entry)
 };
 // Warps of the throughput CMC grid that fit on the device at once (0 on error).
 int CmcThroughputResidentWarps(const DevTables &t, int device);

@@ -232,6 +232,9 @@ def test_cmc_throughput_properties(api, golden):
     e0, _ = ctx.energy()
     e, done, acc = ctx.cmc_run(500.0, 20 * sp.size, mode=1, seed=4)
     assert done >= 20 * sp.size and 0 < acc < done
+    # rounds counted; the survivors of a round are disjoint pairs of sites
+    rounds = ctx.cmc_rounds()
+    assert 0 < rounds and done / rounds <= sp.size / 2
     out = ctx.get_lattices()
     assert np.array_equal(np.bincount(out, minlength=5), np.bincount(sp, minlength=5))
     e1, _ = ctx.energy()
