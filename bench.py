@@ -565,18 +565,29 @@ def run_large(args, device):
                                    "unit": "GB/s", "frac": BYTES_PER_ATTEMPT * v / 1e9 / peak}}
         ctx.set_lattices([L["n"]], sp)
     if args.large_kmc_events > 0:
-        ctx.kmc_multi_init([T], seed=3)
+        # production arithmetic (FP32 barriers and rates, FP64 rate sums and clock), then the
+        # FP64 mode (the oracle's operations) on a shorter run of the same lattice
+        ctx.kmc_multi_init([T], seed=3, rates=N.LMC_RATES_FP32)
         ctx.kmc_multi_run(2000)  # warm-up
         ctx.kmc_multi_run(args.large_kmc_events)
         ms = ctx.last_run_ms()
         off, vac, steps, tm, en = ctx.kmc_multi_state()
         v = args.large_kmc_events / (ms / 1e3)
+        ctx.set_lattices([L["n"]], sp)
+        ctx.kmc_multi_init([T], seed=3, rates=N.LMC_RATES_FP64)
+        ctx.kmc_multi_run(2000)
+        ev64 = min(args.large_kmc_events, 200_000)
+        ctx.kmc_multi_run(ev64)
+        v64 = ev64 / (ctx.last_run_ms() / 1e3)
         out["kmc_multi_vacancy"] = {
             "events": args.large_kmc_events, "ms": ms, "value": v, "unit": "events/s",
             "simulated_time_s": float(tm[0]), "vacancies": int(off[-1]),
+            "rates": "FP32 barriers and rates, FP64 rate sums and clock, exact energy sums",
+            "fp64_rates": {"events": ev64, "value": v64, "unit": "events/s"},
             "launch": "one block of 8 warps (a single lattice is one sequential trajectory)",
             "roofline": {"bound": "latency", "achieved": BYTES_PER_EVENT * v / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": BYTES_PER_EVENT * v / 1e9 / peak}}
+        ctx.set_lattices([L["n"]], sp)
         if args.surrogate_samples > 0:
             out["kmc_multi_vacancy_surrogate"] = run_large_surrogate(args, ctx, sp, T)
     if not args.no_cpu_baseline:

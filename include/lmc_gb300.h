@@ -307,7 +307,8 @@ typedef struct lmc_kmc_options {
   int rates;               /* LMC_RATES_FP32 (default) or LMC_RATES_FP64, for the first-order KMC on
                               LMC_RNG_PHILOX streams: FP32 barriers and rates (within 1e-6 relative of the
                               FP64 ones), FP64 rate sum and clock, exact energy sums. The reference's
-                              mt19937_64 stream, the chain KMC and the multi-vacancy KMC always use FP64. */
+                              mt19937_64 stream and the chain KMC always use FP64; the multi-vacancy
+                              KMC takes lmc_kmc_multi_set_rates. */
 } lmc_kmc_options;
 
 #define LMC_RATES_FP32 0
@@ -385,6 +386,11 @@ int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, i
 /* Runs `steps` steps on every lattice; trace (NULL or `steps` records) receives
  * lattice trace_replica's events, `slot` naming the vacancy that moved. */
 int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace);
+/* Arithmetic of the following lmc_kmc_multi_run calls: LMC_RATES_FP64 (the default; the oracle's
+ * operations exactly) or LMC_RATES_FP32 (barriers and rates in FP32, within 1e-6 relative of the
+ * FP64 ones; rate sums and the clock in FP64; energy sums exact in fixed point). The trajectories
+ * agree except where a draw falls within the rates' rounding of an event boundary. */
+int lmc_kmc_multi_set_rates(lmc_ctx *ctx, int rates);
 /* First slot of every lattice, R + 1 entries (the last is the slot count). */
 int lmc_kmc_multi_slots(lmc_ctx *ctx, int32_t *slot_offsets);
 /* Vacancy site of every slot and per-lattice steps, time, energy (any may be NULL). */

@@ -175,6 +175,7 @@ SIGNATURES = {
     "lmc_kmc_multi_run": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(KmcStep)]),
     "lmc_kmc_multi_slots": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "lmc_kmc_multi_get_state": (C.c_int, [_P, _I64P, _U64P, _DP, _DP]),
+    "lmc_kmc_multi_set_rates": (C.c_int, [_P, C.c_int]),
     "lmc_kmc_multi_surrogate_run": (C.c_int, [_P, _P, C.c_uint64, C.c_float, C.POINTER(KmcStep), _DP, _U64P]),
     "lmc_cmc_rounds": (C.c_int, [_P, _U64P]),
     "lmc_kmc_autotune": (C.c_int, [_P, C.c_uint64, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),

@@ -347,10 +347,12 @@ class Context:
 
     # multi-vacancy kinetic MC ---------------------------------------------
     def kmc_multi_init(self, temperatures, seed: int = 0, kind: int = N.LMC_BARRIER_QUARTIC,
-                       evaluation: int = N.LMC_EVAL_SPARSE):
-        """Tracks every vacancy of every lattice (slots in ascending site order)."""
+                       evaluation: int = N.LMC_EVAL_SPARSE, rates: int = N.LMC_RATES_FP64):
+        """Tracks every vacancy of every lattice (slots in ascending site order); `rates` selects
+        FP64 (the oracle's operations) or FP32 barriers and rates for the following runs."""
         temps = np.ascontiguousarray(np.broadcast_to(np.asarray(temperatures, np.float64), (self.ns.size,)))
         check(N.lib.lmc_kmc_multi_init(self._h, ptr(temps, C.c_double), seed, kind, evaluation))
+        check(N.lib.lmc_kmc_multi_set_rates(self._h, rates))
         off = np.zeros(self.ns.size + 1, np.int32)
         check(N.lib.lmc_kmc_multi_slots(self._h, ptr(off, C.c_int32)))
         self._multi_off = off

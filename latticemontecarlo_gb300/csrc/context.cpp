@@ -126,6 +126,7 @@ struct lmc_ctx {
   // multi-vacancy KMC (every vacancy of a lattice tracked; slots per lattice)
   bool multi_ready{false};
   int multi_kind{0}, multi_eval{0};
+  int multi_rates{LMC_RATES_FP64};  // lmc_kmc_multi_set_rates
   std::vector<int> m_off_host;
   DevBuf m_pos, m_off, m_steps, m_time, m_energy, m_temp, m_key, m_trace;
   std::array<uint32_t, lmc::kLocalBitWords> local_bits{};
@@ -2093,6 +2094,14 @@ int lmc_kmc_multi_init(lmc_ctx *ctx, const double *temperature, uint64_t seed, i
   });
 }
 
+int lmc_kmc_multi_set_rates(lmc_ctx *ctx, int rates) {
+  return Guard([&] {
+    Require(ctx, LMC_ERR_INVALID_ARGUMENT, "null context");
+    Require(rates == LMC_RATES_FP32 || rates == LMC_RATES_FP64, LMC_ERR_INVALID_ARGUMENT, "unknown rates mode");
+    ctx->multi_rates = rates;
+  });
+}
+
 int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_step *trace) {
   return Guard([&] {
     if (ctx) ctx->scan_fresh = false;  // atoms move
@@ -2111,6 +2120,7 @@ int lmc_kmc_multi_run(lmc_ctx *ctx, uint64_t steps, int trace_replica, lmc_kmc_s
     a.lat_n = ctx->lat_n.as<int>();
     a.num_replicas = ctx->num_replicas;
     a.barrier_kind = ctx->multi_kind;
+    a.f32 = ctx->multi_rates == LMC_RATES_FP32 ? 1 : 0;
     a.nsteps = steps;
     a.trace_replica = -1;
     if (trace) {

@@ -1231,6 +1231,86 @@ __device__ __forceinline__ LaneAcc EvalJumpPairsT(const KmcSparse &sp, const uin
   return {acc_a, acc_b, bad};
 }
 
+// EvalJumpPairsT over the work units first, first + stride, ... of the item only (unit u < Gs:
+// the four listed sites from 4u; unit Gs + v: the two pairs from 2v; Gs = the site groups), so
+// that `stride` threads share the item and their partial sums add up to the whole (int64, exact).
+template <bool kCheckX>
+__device__ __forceinline__ LaneAcc EvalJumpPairsStrided(const KmcSparse &sp, const uint8_t *s_pos,
+                                                       const uint16_t *s_pxst, const uint32_t *s_pxenv,
+                                                       const SmallTables *sm, const KmcShared &rs, int e, int x,
+                                                       int c, int part, int mig, int slot, bool quartic, int first,
+                                                       int stride) {
+  long long acc_a = 0, acc_b = 0;
+  unsigned bad = 0;
+  const int rb0 = sm->rank[sp.base_code];
+  const uint8_t *pos_a = s_pos + ((part == 0 ? 0 : 2) * 12 + c) * 136;
+  const uint8_t *pos_b = s_pos + ((part == 0 ? 1 : 3) * 12 + c) * 136;
+  constexpr int kEnvRows = kEnvSites + 1, kStateRows = kStateSites + 1;
+  const long long *__restrict__ sg_a =
+      part == 0 ? sp.s_de + mig * kStateRows * e : sp.s_env + (slot * 3 + 1) * kEnvRows * 8;
+  const long long *__restrict__ sg_b = sp.s_env + (slot * 3 + (part == 1 ? 1 : (quartic ? 0 : 2))) * kEnvRows * 8;
+  const int stride_a = part == 0 ? e : 8, zero_a = part == 0 ? kStateSites : kEnvSites;
+  const long long *__restrict__ w_a = sp.dw_ks + static_cast<long long>(slot) * sp.dw_stride_mm2;
+  const long long *__restrict__ w_b =
+      part == 1 ? w_a : (quartic ? sp.dw_d : sp.dw_e0) + static_cast<long long>(slot) * sp.dw_stride_mmm;
+  const uint32_t *px_a = s_pxenv + (kTriEnv + 1);
+  const uint32_t *px_b = s_pxenv + (part == 1 ? kTriEnv + 1 : 0);
+  const long long *__restrict__ pde = sp.p_de + mig * e * e;
+  // single-site terms
+  const int k_sites = rs.nbk;
+  // the four listed sites from k0
+  auto site_group = [&](int k0) {
+    long long va[4], vb[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int l = rs.nb_l[k0 + i], code = rs.nb_code[k0 + i];
+      const int rp = sm->rank[code];
+      const int pa = pos_a[l], pb = pos_b[l];
+      const bool in_a = pa != 255, in_b = pb != 255;
+      va[i] = __ldg(&sg_a[(in_a ? pa : zero_a) * stride_a + (part == 0 ? code : rp)]);
+      vb[i] = __ldg(&sg_b[(in_b ? pb : kEnvSites) * 8 + rp]);
+      if constexpr (kCheckX) {  // only a vacancy lacks a one-hot rank
+        const bool bad_rank = rp == kMaxOnehot - 1;
+        bad |= (part == 0 && in_a && code == x) ? kStatusBadCluster : 0u;
+        bad |= (((part == 1 && in_a) || in_b) && bad_rank) ? kStatusXInEnv : 0u;
+      }
+    }
+    acc_a += (va[0] + va[1]) + (va[2] + va[3]);
+    acc_b += (vb[0] + vb[1]) + (vb[2] + vb[3]);
+  };
+  // pair terms over the pairs that share a cluster in some jump: the two pairs from i0
+  auto pair_group = [&](int i0) {
+    long long va[2], vb[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const unsigned pk = rs.pairs[i0 + i];
+      const int k = pk & 0xFF, k2 = pk >> 8;
+      const int l = rs.nb_l[k], l2 = rs.nb_l[k2];
+      const int code = rs.nb_code[k], c2 = rs.nb_code[k2];
+      const int pa = pos_a[l], qa = pos_a[l2], pb = pos_b[l], qb = pos_b[l2];
+      const int rp = sm->rank[code], rq = sm->rank[c2];
+      const bool both_a = pa != 255 && qa != 255, both_b = pb != 255 && qb != 255;
+      if (part == 0) {
+        const unsigned tv = s_pxst[both_a ? Tri(pa, qa) : kTriState];
+        const unsigned t0 = tv & 0xFF, t1 = tv >> 8;
+        const long long f0 = __ldg(&pde[((t0 & 7) * e * e) * e + code * e + c2]);
+        const long long f1 = __ldg(&pde[((t1 & 7) * e * e) * e + code * e + c2]);
+        va[i] = ((t0 & 8) ? -f0 : f0) + ((t1 & 8) ? -f1 : f1);
+      } else {
+        va[i] = EnvPairTerm(px_a[both_a ? Tri(pa, qa) : kTriEnv], w_a, pa, qa, rp, rq, rb0, sm->pairtype);
+      }
+      vb[i] = EnvPairTerm(px_b[both_b ? Tri(pb, qb) : kTriEnv], w_b, pb, qb, rp, rq, rb0, sm->pairtype);
+    }
+    acc_a += va[0] + va[1];
+    acc_b += vb[0] + vb[1];
+  };
+  const int n_pairs = rs.npairs;
+  int u = first;
+  for (; 4 * u < k_sites; u += stride) site_group(4 * u);
+  for (int v = u - (k_sites + 3) / 4; 2 * v < n_pairs; v += stride) pair_group(2 * v);
+  return {acc_a, acc_b, bad};
+}
+
 // Shared-memory layout of the KMC kernels: jump cluster tables, small tables,
 // local-index tables of the 12 jumps, the 135-site neighbourhood offsets, the
 // ExpFast table, one KmcShared per replica, per-warp sorted arrays, then the
@@ -1376,6 +1456,51 @@ __device__ __forceinline__ unsigned SparseItem(const DevTables &t, const KmcSpar
                                            part, mig, slot, quartic)
                     : EvalJumpPairsT<false>(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code, c,
                                             part, mig, slot, quartic);
+    if (ok) {
+      const long long *bf = sp.base_form + slot * 3;
+      if (part == 0) {
+        rs.acc[c][0] = sp.base_de[mig] + la.a;
+        rs.acc[c][1] = (quartic ? bf[0] : bf[2]) + la.b;
+      } else {
+        rs.acc[c][2] = bf[1] + la.a + la.b;
+      }
+    }
+    if (part == 0) rs.slot[c] = ok ? slot : (mig == t.x_code ? -2 : -1);
+  }
+  return __reduce_or_sync(0xffffffffu, la.bad);
+}
+
+// The 24 items of SparseItem shared by `subs` threads each (subs a power of two up to 16):
+// thread tid of the group takes item tid / subs and every subs-th work unit of it, the subs
+// partial sums meet by shuffles within their aligned lane group (int64: the same bits as one
+// lane per item) and the group's first thread writes rs.acc / rs.slot. Every thread of a warp
+// calls it (threads with tid >= 24 subs only take part in the shuffles). Returns the warp's
+// status bits.
+__device__ __forceinline__ unsigned SparseItemGroup(const DevTables &t, const KmcSparse &sp, const uint8_t *s_lst,
+                                                    const uint8_t *s_pos, const uint16_t *s_pxst,
+                                                    const uint32_t *s_pxenv, const SmallTables *s_small,
+                                                    KmcShared &rs, int barrier_kind, int tid, int subs) {
+  const int item = tid / subs, sub = tid - item * subs;
+  const int c = item % 12, part = item / 12;
+  LaneAcc la{0, 0, 0u};
+  int mig = 0, slot = -1;
+  bool ok = false;
+  const bool quartic = barrier_kind == 0;
+  if (item < 24) {
+    mig = rs.local[s_lst[c * kStateSites + t.pos_second]];
+    slot = s_small->slot[mig];
+    ok = slot >= 0 && (quartic ? s_small->has_quartic[slot] : s_small->has_e0[slot]);
+    if (ok && (part == 0 || quartic))
+      la = rs.has_x ? EvalJumpPairsStrided<true>(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code,
+                                                 c, part, mig, slot, quartic, sub, subs)
+                    : EvalJumpPairsStrided<false>(sp, s_pos, s_pxst, s_pxenv, s_small, rs, t.num_species, t.x_code,
+                                                  c, part, mig, slot, quartic, sub, subs);
+  }
+  for (int o = subs >> 1; o > 0; o >>= 1) {
+    la.a += __shfl_xor_sync(0xffffffffu, la.a, o);
+    la.b += __shfl_xor_sync(0xffffffffu, la.b, o);
+  }
+  if (item < 24 && sub == 0) {
     if (ok) {
       const long long *bf = sp.base_form + slot * 3;
       if (part == 0) {
@@ -1546,6 +1671,10 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     rs.beta_f = static_cast<float>(rs.beta);
   }
   H3 hv = SiteCoord(vac, n);  // vacancy coordinates, advanced by the selected direction each step
+  // threads per sparse item when several warps share a replica: the largest power of two (up to
+  // 16) with 24 items x item_subs <= the replica's threads
+  int item_subs = 1;
+  while (item_subs < 16 && 48 * item_subs <= 32 * g_per) item_subs *= 2;
   for (unsigned long long it = 0; it < l.steps; ++it) {
     // ---- phase 1: neighbourhood gather, neighbour ids, temperature ----
     if (active) {
@@ -1579,8 +1708,14 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     }
     const bool sparse_step = kSparse && rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
     if (sparse_step) {
-      // one lane per (jump, half): item = lane * G + g, items 0..23
-      bad_all |= SparseItem(t, l.sp, s_lst, s_pos, s_pxst, s_pxenv, s_small, rs, s.barrier_kind, lane * g_per + g);
+      if (kShape == 2 || g_per == 1) {
+        // one lane per (jump, half): item = lane * G + g, items 0..23
+        bad_all |= SparseItem(t, l.sp, s_lst, s_pos, s_pxst, s_pxenv, s_small, rs, s.barrier_kind, lane * g_per + g);
+      } else {
+        // the replica's warps share the 24 items, item_subs threads each
+        bad_all |= SparseItemGroup(t, l.sp, s_lst, s_pos, s_pxst, s_pxenv, s_small, rs, s.barrier_kind,
+                                   g * 32 + lane, item_subs);
+      }
     }
     if (!sparse_step) {
       const DenseArgs da{s_lst, s_lmmm, s_lmm2f, s_lmm2b, s_de, s_mmm, s_mm2, s_small, st, rm, rf, rb};
@@ -1763,6 +1898,7 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
     s.energy[r] = kF32 ? energy + static_cast<double>(energy_fix) * t.de_scale : energy;
     s.steps[r] = step0 + steps_done;
   }
+  bad_all = __reduce_or_sync(0xffffffffu, bad_all);  // a jump's status bits may sit in lanes 1-11
   if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
 }
 
@@ -2044,6 +2180,7 @@ __global__ void __launch_bounds__(kChainWarps * 32, 2)
     s.energy[r] = energy;
     s.steps[r] = step0 + steps_done;
   }
+  bad_all = __reduce_or_sync(0xffffffffu, bad_all);  // a jump's status bits may sit in lanes 1-11
   if (bad_all && lane == 0) atomicOr(l.status, static_cast<int>(bad_all));
 }
 
@@ -2397,8 +2534,10 @@ __global__ void __launch_bounds__(kClusterThreads) cluster_census_kernel(DevTabl
 // K4b: multi-vacancy KMC, one block of kMultiWarps warps per lattice.
 // Every vacancy of the lattice is tracked (slots 0..V-1). Per step:
 //  1. the warps re-evaluate the 12 events of each vacancy whose 135-site
-//     neighbourhood changed (one warp per vacancy, the sparse / dense
-//     evaluation of kmc_kernel). A neighbourhood holding a second vacancy takes
+//     neighbourhood changed, with the sparse / dense evaluation of kmc_kernel:
+//     a single such vacancy (the usual step: only the moved one) by the whole
+//     block (gather by all threads, the 24 sparse items shared by kMultiItemSubs
+//     threads each), several by one warp each. A neighbourhood holding a second vacancy takes
 //     the dense sums in which that vacancy contributes nothing: clusters with two
 //     vacancies have no coefficients and a vacancy has no one-hot slot (the
 //     reference throws there; this is the defined extension). A jump onto a
@@ -2410,9 +2549,12 @@ __global__ void __launch_bounds__(kClusterThreads) cluster_census_kernel(DevTabl
 //     step, lattice), takes x = u2 * total, the first slot v with prefix >= x and
 //     K_v > 0, then y = x - prefix(v - 1) and the first event with scan >= y and a
 //     positive rate (past the end: the last positive one); dt = -log(u1) / (total
-//     * prefactor); the vacancy moves and the slots whose neighbourhoods contain
-//     one of the two changed sites are marked for step 1.
-// The oracle restates exactly these operations (orc_kmc_multi).
+//     * prefactor); the vacancy moves (the migrating atom's species comes from the
+//     slot tables, filled at the slot's evaluation) and the slots whose
+//     neighbourhoods contain one of the two changed sites are marked for step 1.
+// The oracle restates exactly these operations (orc_kmc_multi). kF32 (production
+// arithmetic, KmcMultiArgs::f32): FP32 barriers and rates (MultiSlotRates), the
+// rate sums and the clock in FP64 as above, the energy as an exact fixed-point sum.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool InLocal(const uint32_t *bits, int dx, int dy, int dz) {
   if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) return false;
@@ -2436,11 +2578,95 @@ size_t MultiSharedBytes(const DevTables &t, bool sparse) {
   b += sizeof(H3) * kMaxMultiVac;           // coordinates
   b += sizeof(int) * kMaxMultiVac;          // dirty list
   b += sizeof(uint16_t) * kMaxMultiVac;     // positive-rate masks
+  b += kMaxMultiVac * 12;                   // target species
   b += sizeof(int) * 4 + sizeof(uint32_t) * kLocalBitWords;
   return (b + 15) & ~size_t(15);
 }
 
-template <bool kSparse>
+// Multi-vacancy KMC: rates of slot v from the sums in q (one warp): the 12 events in id order
+// (the sorted 1NN list; the order depends only on which axes of the vacancy lie on the periodic
+// boundary), their inclusive scan in FP64 (4 shuffle steps over 16 lanes), Ea, dE, targets, the
+// targets' species (mig_local[d * kStateSites]: local index of direction d's migrant) and the
+// positive-rate mask into the slot tables. Returns the status bits.
+// kF32: JumpEpilogueF32 (barriers within 1e-6 relative of the FP64 epilogue) and rates
+// 2^64 exp(-Ea / kT) = exp2(64 - Ea log2(e) / kT) in FP32 (the power-of-two scale keeps barriers
+// up to about 130 kT above zero; the clock divides it out exactly); ea holds FP32 barriers (as
+// float), de the energy change's exact fixed-point sum (as long long). Otherwise FP64 throughout.
+struct MultiSlotTables {
+  double *cum, *ea, *de;
+  long long *tgt;
+  uint16_t *kmask;
+  int8_t *tsp;  // species on each target site (the migrating atom)
+};
+constexpr double kMultiRateScale = 18446744073709551616.0;  // 2^64, the FP32 rates' scale
+template <bool kF32>
+__device__ __forceinline__ unsigned MultiSlotRates(const DevTables &t, const ExpConsts &ec, int kind, double beta,
+                                                   float beta_l2e, const KmcShared &q, H3 h, int n, int v,
+                                                   const uint8_t *mig_local, const MultiSlotTables &o, int lane) {
+  unsigned bad = 0;
+  double ea = 0.0, de = 0.0, k = 0.0;
+  float ea_f = 0.0f;
+  long long de_fix = 0, id = 0x7fffffffffffffffLL;
+  if (lane < 12) {
+    const int slot = q.slot[lane];
+    id = q.ids[lane];
+    if (slot >= 0) {
+      if constexpr (kF32) {
+        const JumpOutF jo = JumpEpilogueF32(t, kind, slot, q.acc[lane][0], q.acc[lane][1], q.acc[lane][2]);
+        ea_f = jo.ea;
+        de_fix = q.acc[lane][0];
+        const float kf = exp2f(fmaf(-ea_f, beta_l2e, 64.0f));
+        if (!(kf < INFINITY)) bad |= kStatusNumeric;  // a barrier below -44 kT
+        k = FloatToDouble(kf);
+      } else {
+        const JumpOut jo = JumpEpilogue(t, ec, kind, slot, q.acc[lane][0], q.acc[lane][1], q.acc[lane][2]);
+        ea = jo.ea;
+        de = jo.de;
+        k = ExpFast(-ea * beta, ec);
+      }
+    } else if (slot == -1) {
+      bad |= kStatusNoCoefficients;
+    }
+  }
+  const int m2 = 2 * n - 1;
+  const int bcase = (h.x == 0 ? 9 : (h.x == m2 ? 18 : 0)) + (h.y == 0 ? 3 : (h.y == m2 ? 6 : 0)) +
+                    (h.z == 0 ? 1 : (h.z == m2 ? 2 : 0));
+  const int src = lane < 12 ? __ldg(&t.id_order[bcase * 12 + lane]) : lane;
+  const double k_s = __shfl_sync(0xffffffffu, k, src);
+  const long long id_s = __shfl_sync(0xffffffffu, id, src);
+  double cum = lane < 12 ? k_s : 0.0;
+#pragma unroll
+  for (int off = 1; off < 16; off <<= 1) {
+    const double u = __shfl_up_sync(0xffffffffu, cum, off);
+    if (lane >= off) cum += u;
+  }
+  const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
+  if constexpr (kF32) {
+    const float ea_s = __shfl_sync(0xffffffffu, ea_f, src);
+    const long long de_s = __shfl_sync(0xffffffffu, de_fix, src);
+    if (lane < 12) {
+      reinterpret_cast<float *>(o.ea)[v * 12 + lane] = ea_s;
+      reinterpret_cast<long long *>(o.de)[v * 12 + lane] = de_s;
+    }
+  } else {
+    const double ea_s = __shfl_sync(0xffffffffu, ea, src);
+    const double de_s = __shfl_sync(0xffffffffu, de, src);
+    if (lane < 12) {
+      o.ea[v * 12 + lane] = ea_s;
+      o.de[v * 12 + lane] = de_s;
+    }
+  }
+  if (lane < 12) {
+    o.cum[v * 12 + lane] = cum;
+    o.tgt[v * 12 + lane] = id_s;
+    o.tsp[v * 12 + lane] = q.local[mig_local[src * kStateSites]];
+  }
+  if (lane == 0) o.kmask[v] = static_cast<uint16_t>(kpos);
+  __syncwarp();
+  return bad;
+}
+
+template <bool kSparse, bool kF32>
 __global__ void __launch_bounds__(kMultiWarps * 32, 1)
     kmc_multi_kernel(const __grid_constant__ DevTables t, int8_t *species, const __grid_constant__ KmcMultiArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2455,8 +2681,10 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   H3 *s_h = reinterpret_cast<H3 *>(s_pos + kMaxMultiVac);
   int *s_list = reinterpret_cast<int *>(s_h + kMaxMultiVac);
   uint16_t *s_kmask = reinterpret_cast<uint16_t *>(s_list + kMaxMultiVac);
-  int *s_ctl = reinterpret_cast<int *>(s_kmask + kMaxMultiVac);      // [0] dirty count, [1] stop
+  int8_t *s_tsp = reinterpret_cast<int8_t *>(s_kmask + kMaxMultiVac);  // [kMaxMultiVac][12] target species
+  int *s_ctl = reinterpret_cast<int *>(s_tsp + kMaxMultiVac * 12);     // [0] dirty count, [1] stop
   uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_ctl + 4);
+  const MultiSlotTables slot_tab{s_cum, s_ea, s_de, s_tgt, s_kmask, s_tsp};
 
   const int r = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2484,8 +2712,10 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   const int x_code = t.x_code;
   const int center = sm.lst[t.pos_first];  // local index of the vacancy site itself
   const double beta = 1.0 / kBoltzmannEv / a.temperature[r];
+  const float beta_l2e = static_cast<float>(beta * 1.4426950408889634);  // FP32 rates: log2(e) / kT
   unsigned bad_all = 0;
   double time = 0.0, energy = 0.0;
+  long long energy_fix = 0;  // FP32 mode: this launch's energy change in the dE fixed point (exact)
   unsigned long long step0 = 0, steps_done = 0;
   uint32_t key0 = 0, key1 = 0;
   if (warp == 0) {
@@ -2497,81 +2727,79 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   }
   double nlog_blk = 0.0, u2_blk = 0.0;
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
-    // ---- phase 1: re-evaluate the marked slots, one warp per slot ----
+    // ---- phase 1: re-evaluate the marked slots ----
     const int nd = s_ctl[0];
-    for (int q = warp; q < nd; q += kMultiWarps) {
-      const int v = s_list[q];
+    if (kSparse && nd == 1) {
+      // one slot (the usual step: only the moved vacancy): the block gathers its neighbourhood,
+      // warp 0 lists the non-base sites, kMultiItemWarps warps share the 24 sparse items
+      const int v = s_list[0];
+      KmcShared &q = sm.rep[0];
       const H3 h = s_h[v];
       bool other = false;  // a second vacancy in the neighbourhood
-      for (int k = lane; k < kLocalSites; k += 32) {
+      for (int k = threadIdx.x; k < kLocalSites; k += blockDim.x) {
         const int8_t *o = sm.loff + k * 4;
         const int8_t c = lat[NeighborId(h, o[0], o[1], o[2], n)];
-        rs.local[k] = c;
+        q.local[k] = c;
         other |= c == x_code && k != center;
       }
-      if (lane < 12) {
-        const int8_t *o = t.dir + lane * 4;
-        rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
+      if (threadIdx.x < 12) {
+        const int8_t *o = t.dir + threadIdx.x * 4;
+        q.ids[threadIdx.x] = NeighborId(h, o[0], o[1], o[2], n);
       }
-      const bool extra_x = __any_sync(0xffffffffu, other);
-      __syncwarp();
-      bool sparse_v = false;
-      if (kSparse && !extra_x) {
-        SparseList(rs, sm.inter, a.sp, lane);
-        __syncwarp();
-        sparse_v = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
-      }
+      const bool extra_x = __syncthreads_or(other);
+      if (!extra_x && warp == 0) SparseList(q, sm.inter, a.sp, lane);
+      __syncthreads();
+      const bool sparse_v = !extra_x && q.nbk <= kMaxSparseSites && q.npairs <= kMaxSparsePairs;
       if (sparse_v) {
-        bad_all |= SparseItem(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, a.barrier_kind, lane);
-      } else {
+        if (warp < kMultiItemWarps)
+          bad_all |= SparseItemGroup(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, q, a.barrier_kind,
+                                     threadIdx.x, kMultiItemSubs);
+      } else if (warp == 0) {
         const DenseArgs da{sm.lst, sm.lmmm, sm.lmm2f, sm.lmm2b, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb};
-        unsigned b = DenseJumpsCold(t, rs, da, a.barrier_kind, 0, 1, lane);
+        unsigned b = DenseJumpsCold(t, q, da, a.barrier_kind, 0, 1, lane);
         if (extra_x) b &= ~static_cast<unsigned>(kStatusXInEnv | kStatusBadCluster);
         bad_all |= b;
       }
-      __syncwarp();
-      double ea = 0.0, de = 0.0, k = 0.0;
-      long long id = 0x7fffffffffffffffLL;
-      if (lane < 12) {
-        const int slot = rs.slot[lane];
-        id = rs.ids[lane];
-        if (slot >= 0) {
-          const JumpOut o = JumpEpilogue(t, ec, a.barrier_kind, slot, rs.acc[lane][0], rs.acc[lane][1], rs.acc[lane][2]);
-          ea = o.ea;
-          de = o.de;
-          k = ExpFast(-ea * beta, ec);
-        } else if (slot == -1) {
-          bad_all |= kStatusNoCoefficients;
+      __syncthreads();
+      if (warp == 0)
+        bad_all |= MultiSlotRates<kF32>(t, ec, a.barrier_kind, beta, beta_l2e, q, h, n, v, sm.lst + t.pos_second,
+                                        slot_tab, lane);
+    } else {
+      // several slots (the first step, or a move next to another vacancy): one warp per slot
+      for (int qi = warp; qi < nd; qi += kMultiWarps) {
+        const int v = s_list[qi];
+        const H3 h = s_h[v];
+        bool other = false;  // a second vacancy in the neighbourhood
+        for (int k = lane; k < kLocalSites; k += 32) {
+          const int8_t *o = sm.loff + k * 4;
+          const int8_t c = lat[NeighborId(h, o[0], o[1], o[2], n)];
+          rs.local[k] = c;
+          other |= c == x_code && k != center;
         }
+        if (lane < 12) {
+          const int8_t *o = t.dir + lane * 4;
+          rs.ids[lane] = NeighborId(h, o[0], o[1], o[2], n);
+        }
+        const bool extra_x = __any_sync(0xffffffffu, other);
+        __syncwarp();
+        bool sparse_v = false;
+        if (kSparse && !extra_x) {
+          SparseList(rs, sm.inter, a.sp, lane);
+          __syncwarp();
+          sparse_v = rs.nbk <= kMaxSparseSites && rs.npairs <= kMaxSparsePairs;
+        }
+        if (sparse_v) {
+          bad_all |= SparseItem(t, a.sp, sm.lst, sm.pos, sm.pxst, sm.pxenv, sm.small, rs, a.barrier_kind, lane);
+        } else {
+          const DenseArgs da{sm.lst, sm.lmmm, sm.lmm2f, sm.lmm2b, sm.de, sm.mmm, sm.mm2, sm.small, st, rm, rf, rb};
+          unsigned b = DenseJumpsCold(t, rs, da, a.barrier_kind, 0, 1, lane);
+          if (extra_x) b &= ~static_cast<unsigned>(kStatusXInEnv | kStatusBadCluster);
+          bad_all |= b;
+        }
+        __syncwarp();
+        bad_all |= MultiSlotRates<kF32>(t, ec, a.barrier_kind, beta, beta_l2e, rs, h, n, v, sm.lst + t.pos_second,
+                                        slot_tab, lane);
       }
-      // events in id order (the sorted 1NN list), then their inclusive scan
-      int rank = 0;
-      for (int q2 = 0; q2 < 12; ++q2) {
-        const long long oid = __shfl_sync(0xffffffffu, id, q2);
-        rank += (q2 != lane) && (oid < id);
-      }
-      int src = 0;
-      for (int q2 = 0; q2 < 12; ++q2)
-        if (__shfl_sync(0xffffffffu, rank, q2) == lane) src = q2;
-      const double k_s = __shfl_sync(0xffffffffu, k, src);
-      const double ea_s = __shfl_sync(0xffffffffu, ea, src);
-      const double de_s = __shfl_sync(0xffffffffu, de, src);
-      const long long id_s = __shfl_sync(0xffffffffu, id, src);
-      double cum = lane < 12 ? k_s : 0.0;
-#pragma unroll
-      for (int o = 1; o < 16; o <<= 1) {
-        const double u = __shfl_up_sync(0xffffffffu, cum, o);
-        if (lane >= o) cum += u;
-      }
-      const unsigned kpos = __ballot_sync(0xffffffffu, lane < 12 && k_s > 0.0);
-      if (lane < 12) {
-        s_cum[v * 12 + lane] = cum;
-        s_ea[v * 12 + lane] = ea_s;
-        s_de[v * 12 + lane] = de_s;
-        s_tgt[v * 12 + lane] = id_s;
-      }
-      if (lane == 0) s_kmask[v] = static_cast<uint16_t>(kpos);
-      __syncwarp();
     }
     __syncthreads();
     // ---- phase 2: selection over all slots and the move (warp 0) ----
@@ -2626,14 +2854,26 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
           const int e = vsel * 12 + sel;
           const long long p_old = s_pos[vsel];
           const long long tgt = s_tgt[e];
-          const double ea_sel = s_ea[e], de_sel = s_de[e];
-          time += nlog_u1 * RcpFast(total * kPrefactor);
-          energy += de_sel;
+          const int8_t mig = s_tsp[e];  // the migrating atom's species
+          double ea_sel, de_sel;
+          if constexpr (kF32) {
+            // rates carry the 2^64 scale: dt = -log(u1) 2^64 / (total x prefactor)
+            ea_sel = FloatToDouble(reinterpret_cast<const float *>(s_ea)[e]);
+            const long long de_fix = reinterpret_cast<const long long *>(s_de)[e];
+            energy_fix += de_fix;
+            de_sel = static_cast<double>(de_fix) * t.de_scale;  // the trace only
+            time += nlog_u1 * RcpFast(total * (kPrefactor / kMultiRateScale));
+          } else {
+            ea_sel = s_ea[e];
+            de_sel = s_de[e];
+            time += nlog_u1 * RcpFast(total * kPrefactor);
+            energy += de_sel;
+          }
           const H3 h_old = s_h[vsel];
           const H3 h_new = SiteCoord(tgt, n);
           __syncwarp();
           if (lane == 0) {
-            lat[p_old] = lat[tgt];  // Config::LatticeJump
+            lat[p_old] = mig;  // Config::LatticeJump
             lat[tgt] = static_cast<int8_t>(x_code);
             s_pos[vsel] = tgt;
             s_h[vsel] = h_new;
@@ -2645,9 +2885,9 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
               rec.slot = vsel;
               rec.ea = ea_sel;
               rec.de = de_sel;
-              rec.total_rate = total;
+              rec.total_rate = kF32 ? total / kMultiRateScale : total;
               rec.time = time;
-              rec.energy = energy;
+              rec.energy = kF32 ? energy + static_cast<double>(energy_fix) * t.de_scale : energy;
               a.trace[it] = rec;
             }
           }
@@ -2681,10 +2921,11 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
   }
   if (warp == 0 && lane == 0) {
     a.time[r] = time;
-    a.energy[r] = energy;
+    a.energy[r] = kF32 ? energy + static_cast<double>(energy_fix) * t.de_scale : energy;
     a.steps[r] = step0 + steps_done;
   }
   for (int i = threadIdx.x; i < nv; i += blockDim.x) a.vac_pos[v0 + i] = s_pos[i];
+  bad_all = __reduce_or_sync(0xffffffffu, bad_all);
   if (bad_all && lane == 0) atomicOr(a.status, static_cast<int>(bad_all));
 }
 
@@ -4143,7 +4384,8 @@ size_t KmcMultiSharedBytes(const DevTables &t, bool sparse) { return MultiShared
 cudaError_t LaunchKmcMulti(const DevTables &t, int8_t *species, const KmcMultiArgs &a, bool sparse,
                            cudaStream_t stream) {
   const size_t sm = MultiSharedBytes(t, sparse);
-  auto kern = sparse ? kmc_multi_kernel<true> : kmc_multi_kernel<false>;
+  auto kern = sparse ? (a.f32 ? kmc_multi_kernel<true, true> : kmc_multi_kernel<true, false>)
+                     : (a.f32 ? kmc_multi_kernel<false, true> : kmc_multi_kernel<false, false>);
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
   if (err != cudaSuccess) return err;
   kern<<<a.num_replicas, kMultiWarps * 32, sm, stream>>>(t, species, a);

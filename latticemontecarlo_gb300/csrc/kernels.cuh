@@ -132,6 +132,9 @@ cudaError_t LaunchCensus(const DevTables &t, const int8_t *species, int n, int b
 // id at initialisation), kept when they move.
 constexpr int kMaxMultiVac = 256;
 constexpr int kMultiWarps = 8;
+constexpr int kMultiItemSubs = 8;                         // threads per sparse item, one re-evaluated slot
+constexpr int kMultiItemWarps = 24 * kMultiItemSubs / 32;  // the warps that share the 24 items
+static_assert(kMultiItemWarps <= kMultiWarps, "items fit the block");
 constexpr int kLocalSpan = 9;  // neighbourhood displacements lie in [-4, 4]^3 (half-lattice units)
 constexpr int kLocalBitWords = (kLocalSpan * kLocalSpan * kLocalSpan + 31) / 32;
 struct KmcMultiArgs {
@@ -145,6 +148,7 @@ struct KmcMultiArgs {
   const int *lat_n;
   int num_replicas;
   int barrier_kind;
+  int f32;                          // 1: FP32 barriers and rates, FP64 rate sums and clock, exact energy
   unsigned long long nsteps;        // steps per launch
   int trace_replica;                // -1 = none
   KmcTraceRec *trace;               // [nsteps] records of lattice trace_replica

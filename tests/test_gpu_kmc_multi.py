@@ -150,3 +150,60 @@ def test_large_lattice_64_vacancies(native):
     assert sorted(vac.tolist()) == sorted(np.flatnonzero(final == x).tolist())
     e1, _ = ctx.energy()
     np.testing.assert_allclose(e1 - e0, energy[0], rtol=0, atol=1e-8)
+
+
+def test_fp32_rates_large_lattice(native):
+    """LMC_RATES_FP32 on the large-lattice workload: conservation, vacancies where the state says,
+    and the exact fixed-point energy sum equal to the census difference."""
+    from latticemontecarlo_gb300 import api
+    L = S.LARGE
+    el = L["elements"]
+    coeffs = S.make_coefficients(el, 31)
+    sp = S.make_lattice(L["n"], L["fractions"], L["vacancies"], 31, el)
+    ctx = api.Context(api.Model.from_coefficients(coeffs, list(el)))
+    ctx.set_lattices([L["n"]], sp)
+    e0, _ = ctx.energy()
+    ctx.kmc_multi_init([500.0], seed=3, rates=native.LMC_RATES_FP32)
+    tr = ctx.kmc_multi_run(3000, trace_replica=0)
+    off, vac, steps, time, energy = ctx.kmc_multi_state()
+    final = ctx.get_lattices()
+    x = S.alphabet(el).index("X")
+    assert steps[0] == 3000 and time[0] > 0 and np.all(np.diff(tr["time"]) > 0)
+    assert np.array_equal(np.bincount(sp, minlength=len(el) + 1), np.bincount(final, minlength=len(el) + 1))
+    assert sorted(vac.tolist()) == sorted(np.flatnonzero(final == x).tolist())
+    e1, _ = ctx.energy()
+    np.testing.assert_allclose(e1 - e0, energy[0], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(tr["energy"][-1], energy[0], rtol=0, atol=1e-12)
+
+
+def test_fp32_and_fp64_rates_agree(native):
+    """The same lattices and Philox streams with FP32 and FP64 barriers and rates: the trajectories
+    agree except where a draw falls within the rates' rounding of an event boundary (a lattice or
+    two at most); on the common steps the barriers agree within 1e-6 relative, the clock to the
+    FP32 rates' precision and the energies (exact fixed point against FP64 sums) to rounding."""
+    from latticemontecarlo_gb300 import api
+    coeffs = S.make_coefficients(EL, 41)
+    R, n, vac = 8, 16, 8
+    sp = np.concatenate([S.make_lattice(n, FRAC, vac, 100 + r, EL) for r in range(R)])
+    out = []
+    for rates in (native.LMC_RATES_FP32, native.LMC_RATES_FP64):
+        ctx = api.Context(api.Model.from_coefficients(coeffs, list(EL)))
+        ctx.set_lattices([n] * R, sp)
+        ctx.kmc_multi_init([480.0] * R, seed=19, rates=rates)
+        tr = ctx.kmc_multi_run(400, trace_replica=0)
+        out.append((tr, ctx.get_lattices(), ctx.kmc_multi_state()))
+    (t32, l32, s32), (t64, l64, s64) = out
+    size = 4 * n ** 3
+    same = np.array([np.array_equal(l32[r * size:(r + 1) * size], l64[r * size:(r + 1) * size]) for r in range(R)])
+    rel_t = np.abs(s32[3] - s64[3]) / s64[3]
+    same &= rel_t < 3e-5
+    assert same.sum() >= R - 2, f"{R - same.sum()} trajectories differ"
+    assert np.median(rel_t[same]) < 3e-6
+    np.testing.assert_allclose(s32[4][same], s64[4][same], rtol=0, atol=1e-9)
+    # replica 0's events up to the first difference
+    diff = np.flatnonzero((t32["slot"] != t64["slot"]) | (t32["target"] != t64["target"]))
+    k = int(diff[0]) if diff.size else t32.size
+    assert k >= 100
+    np.testing.assert_allclose(t32["ea"][:k], t64["ea"][:k], rtol=1e-6)
+    np.testing.assert_allclose(t32["de"][:k], t64["de"][:k], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(t32["total_rate"][:k], t64["total_rate"][:k], rtol=3e-5)
