@@ -3576,6 +3576,10 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
   __shared__ H3 s_h[2 * kCmcRefMaxBatch];
   __shared__ double s_de[kCmcRefMaxBatch], s_p[kCmcRefMaxBatch];
   __shared__ int s_nb, s_fail, s_stop;
+  // warp 0's set of candidate pairs while it builds a batch
+  __shared__ long long s_c1[32], s_c2[32];
+  __shared__ unsigned s_cend[32];
+  __shared__ H3 s_ch[64];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = a.n;
   const long long nsites_ll = 4LL * n * n * n;
@@ -3610,35 +3614,117 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
   bool stop = a.attempts == 0;
   while (!stop) {
     if (warp == 0) {
-      int nb = 0;
-      bool failed = false;
-      for (int i = 0; i < a.batch; ++i) {
-        long long l1 = 0, l2 = 0;
-        H3 h1{}, h2{};
-        int ct = 0;
-        for (;;) {
-          // GenerateLatticeIdJumpPair (the host rejects single-species lattices)
+      // The batch: pair slot after pair slot, the stream's different-species pairs in order, each
+      // kept when neither site lies in the shells of the pairs kept before, the batch given up at
+      // a slot's 50th pair. The different-species pairs are found a set at a time (lanes 0-15
+      // test 16 consecutive draw pairs per ballot, up to 32 pairs or 312 draws ahead), then taken
+      // in order; only the draws up to the pair that completes the batch are consumed.
+      int nb = 0, ct = 0, empty_sets = 0;
+      bool failed = false, ended = false;
+      while (nb < a.batch && !failed && !ended) {
+        int m = 0;          // pairs found in this set (s_c1 / s_c2 / s_cend [0, m))
+        unsigned off = 0;   // draws examined
+        bool rejected = false;
+        const unsigned window = 624 - mw.idx;  // draws readable before the stream advances
+        while (m < 32 && off + 64 <= window) {
+          const unsigned long long x1 = MtWarpOut(mw, off + 2 * lane), x2 = MtWarpOut(mw, off + 2 * lane + 1);
+          const bool rej = x1 * nsites < threshold || x2 * nsites < threshold;
+          const long long pa = static_cast<long long>(__umul64hi(x1, nsites));
+          const long long pb = static_cast<long long>(__umul64hi(x2, nsites));
+          const bool diff = species[pa] != species[pb];
+          const unsigned mrej = __ballot_sync(0xffffffffu, rej);
+          const int r0 = mrej ? __ffs(mrej) - 1 : 32;
+          const unsigned below = r0 == 32 ? 0xffffffffu : (1u << r0) - 1u;
+          const unsigned mdiff = __ballot_sync(0xffffffffu, diff) & below;
+          const int rank = m + __popc(mdiff & ((1u << lane) - 1u));
+          const bool take = ((mdiff >> lane) & 1u) && rank < 32;
+          if (take) {
+            s_c1[rank] = pa;
+            s_c2[rank] = pb;
+            s_cend[rank] = off + 2 * static_cast<unsigned>(lane + 1);
+          }
+          if (m + __popc(mdiff) >= 32) {  // the set ends at its 32nd pair
+            off += 2 * static_cast<unsigned>(__ffs(__ballot_sync(0xffffffffu, take && rank == 31)));
+            m = 32;
+            break;
+          }
+          m += __popc(mdiff);
+          if (r0 < 32) {  // a draw Lemire's method rejects: the pairing shifts from there
+            off += 2 * static_cast<unsigned>(r0);
+            rejected = true;
+            break;
+          }
+          off += 64;
+        }
+        empty_sets = m == 0 ? empty_sets + 1 : 0;
+        if (empty_sets > (1 << 15)) {  // no different-species pair in millions of draws
+          failed = true;
+          break;
+        }
+        __syncwarp();
+        if (lane < m) {
+          s_ch[2 * lane] = SiteCoord(s_c1[lane], n);
+          s_ch[2 * lane + 1] = SiteCoord(s_c2[lane], n);
+        }
+        __syncwarp();
+        // the pairs in order: a slot's 50th pair ends the batch, a pair clear of the shells of
+        // the chosen ones fills the slot
+        int jend = -1;
+        for (int j = 0; j < m; ++j) {
+          if (++ct == 50) {
+            jend = j;
+            ended = true;
+            break;
+          }
+          const H3 q1 = s_ch[2 * j], q2 = s_ch[2 * j + 1];
+          bool hit = false;
+          for (int q = lane; q < 2 * nb; q += 32) hit |= CmcRefNear(q1, s_h[q], n) || CmcRefNear(q2, s_h[q], n);
+          if (!__any_sync(0xffffffffu, hit)) {
+            if (lane == 0) {
+              s_pair[nb][0] = s_c1[j];
+              s_pair[nb][1] = s_c2[j];
+              s_h[2 * nb] = q1;
+              s_h[2 * nb + 1] = q2;
+            }
+            __syncwarp();
+            ++nb;
+            ct = 0;
+            if (nb == a.batch) {
+              jend = j;
+              break;
+            }
+          }
+        }
+        const unsigned used = jend >= 0 ? s_cend[jend] : off;  // draws this set consumes
+        __syncwarp();
+        MtWarpAdvance(mw, used > 312 ? 312 : used, lane);
+        if (used > 312) MtWarpAdvance(mw, used - 312, lane);
+        if (rejected && used == off && nb < a.batch && !ended) {
+          // the pair at the rejected draw and its successors, one at a time
+          long long l1 = 0, l2 = 0;
           if (!MtWarpPair(mw, species, nsites, threshold, lane, &l1, &l2)) {
             failed = true;
             break;
           }
-          ++ct;
-          if (ct == 50) break;
-          h1 = SiteCoord(l1, n);
-          h2 = SiteCoord(l2, n);
+          if (++ct == 50) {
+            ended = true;
+            break;
+          }
+          const H3 q1 = SiteCoord(l1, n), q2 = SiteCoord(l2, n);
           bool hit = false;
-          for (int j = lane; j < 2 * nb; j += 32) hit |= CmcRefNear(h1, s_h[j], n) || CmcRefNear(h2, s_h[j], n);
-          if (!__any_sync(0xffffffffu, hit)) break;
+          for (int q = lane; q < 2 * nb; q += 32) hit |= CmcRefNear(q1, s_h[q], n) || CmcRefNear(q2, s_h[q], n);
+          if (!__any_sync(0xffffffffu, hit)) {
+            if (lane == 0) {
+              s_pair[nb][0] = l1;
+              s_pair[nb][1] = l2;
+              s_h[2 * nb] = q1;
+              s_h[2 * nb + 1] = q2;
+            }
+            __syncwarp();
+            ++nb;
+            ct = 0;
+          }
         }
-        if (failed || ct == 50) break;
-        if (lane == 0) {
-          s_pair[nb][0] = l1;
-          s_pair[nb][1] = l2;
-          s_h[2 * nb] = h1;
-          s_h[2 * nb + 1] = h2;
-        }
-        __syncwarp();
-        ++nb;
       }
       if (lane == 0) {
         s_nb = nb;
@@ -3661,26 +3747,37 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
     }
     __syncthreads();
     if (warp == 0) {
-      for (int i = 0; i < nb; ++i) {
-        const double dE = s_de[i];
-        if (a.energy_trace && lane == 0) a.energy_trace[done] = energy;
-        bool acc = dE < 0;
-        if (!acc) {
-          const double u0 = __ull2double_rn(MtWarpOut(mw, 0)) * 5.421010862427522170e-20;  // 2^-64
-          MtWarpAdvance(mw, 1, lane);
+      // The Metropolis tests of the batch, 32 pairs at a time in parallel: pair i draws a uniform
+      // only when dE_i >= 0, so its draw is the stream's next output after those of the earlier
+      // pairs with dE >= 0, and its acceptance does not depend on theirs (the dE values are
+      // those of the unchanged lattice; the pairs' sites are disjoint). The energy is summed in
+      // batch order, as the serial loop does.
+      for (int c0 = 0; c0 < nb; c0 += 32) {
+        const int i = c0 + lane, m = min(32, nb - c0);
+        const bool in = lane < m;
+        const double dE = in ? s_de[i] : 0.0;
+        const bool need = in && !(dE < 0);
+        const unsigned mneed = __ballot_sync(0xffffffffu, need);
+        bool acc = in && dE < 0;
+        if (need) {
+          const unsigned k = static_cast<unsigned>(__popc(mneed & ((1u << lane) - 1u)));
+          const double u0 = __ull2double_rn(MtWarpOut(mw, k)) * 5.421010862427522170e-20;  // 2^-64
           acc = (u0 >= 1.0 ? 0.99999999999999988898 : u0) < s_p[i];
         }
+        const unsigned macc = __ballot_sync(0xffffffffu, acc);
         if (acc) {
-          if (lane == 0) {
-            const long long l1 = s_pair[i][0], l2 = s_pair[i][1];
-            const int8_t v = species[l1];
-            species[l1] = species[l2];
-            species[l2] = v;
-          }
-          energy += dE;
-          ++accepted;
+          const long long l1 = s_pair[i][0], l2 = s_pair[i][1];
+          const int8_t v = species[l1];
+          species[l1] = species[l2];
+          species[l2] = v;
         }
-        ++done;
+        for (int j = 0; j < m; ++j) {
+          if (a.energy_trace && lane == 0) a.energy_trace[done + j] = energy;
+          if ((macc >> j) & 1u) energy += s_de[c0 + j];
+        }
+        done += static_cast<unsigned long long>(m);
+        accepted += static_cast<unsigned long long>(__popc(macc));
+        MtWarpAdvance(mw, static_cast<unsigned>(__popc(mneed)), lane);
       }
       if (nb == 0) done = a.attempts;  // no pair could be placed: stop rather than spin
       if (lane == 0) s_stop = done >= a.attempts;
