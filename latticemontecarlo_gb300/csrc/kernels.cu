@@ -3557,9 +3557,11 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
 // with n >= 6 a site lies in the shell of c exactly when its minimum-image
 // displacement from c has squared length <= 6 (half units: 1NN 2, 2NN 4, 3NN 6,
 // 4NN 8), so the lanes test the candidates against the chosen sites directly.
-// The block's warps then compute the batch's dE values (and the Metropolis
-// factors) on the unchanged lattice, one pair per warp, as the reference's OpenMP
-// threads do; warp 0 runs the Metropolis tests in batch order.
+// The block's warps then compute the batch's dE values on the unchanged lattice,
+// one pair per warp, as the reference's OpenMP threads do; warp 0 runs the
+// Metropolis tests of up to 32 pairs at once (a pair's uniform is the stream's
+// output after those of the earlier pairs with dE >= 0, its factor exp(-dE / kT)
+// one lane's FP64 exp) and sums the energy in batch order.
 // ---------------------------------------------------------------------------
 constexpr int kCmcRefWarps = 16;
 // Lattices up to this many sites are copied into shared memory for the launch.
@@ -3574,7 +3576,7 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
   __shared__ unsigned long long s_mt[2][312];
   __shared__ long long s_pair[kCmcRefMaxBatch][2];
   __shared__ H3 s_h[2 * kCmcRefMaxBatch];
-  __shared__ double s_de[kCmcRefMaxBatch], s_p[kCmcRefMaxBatch];
+  __shared__ double s_de[kCmcRefMaxBatch];
   __shared__ int s_nb, s_fail, s_stop;
   // warp 0's set of candidate pairs while it builds a batch
   __shared__ long long s_c1[32], s_c2[32];
@@ -3739,11 +3741,7 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
       int pa, pb;
       GatherSwap(s.off, species, n, s_h[2 * i], s_h[2 * i + 1], sa, sb, &pa, &pb, lane);
       const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
-      if (lane == 0) {
-        const double dE = static_cast<double>(acc) * t.de_scale;
-        s_de[i] = dE;
-        s_p[i] = dE < 0 ? 1.0 : exp(-dE * a.beta);
-      }
+      if (lane == 0) s_de[i] = static_cast<double>(acc) * t.de_scale;
     }
     __syncthreads();
     if (warp == 0) {
@@ -3759,10 +3757,10 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
         const bool need = in && !(dE < 0);
         const unsigned mneed = __ballot_sync(0xffffffffu, need);
         bool acc = in && dE < 0;
-        if (need) {
+        if (need) {  // the Metropolis factors of the 32 pairs in one warp: one FP64 exp per lane
           const unsigned k = static_cast<unsigned>(__popc(mneed & ((1u << lane) - 1u)));
           const double u0 = __ull2double_rn(MtWarpOut(mw, k)) * 5.421010862427522170e-20;  // 2^-64
-          acc = (u0 >= 1.0 ? 0.99999999999999988898 : u0) < s_p[i];
+          acc = (u0 >= 1.0 ? 0.99999999999999988898 : u0) < exp(-dE * a.beta);
         }
         const unsigned macc = __ballot_sync(0xffffffffu, acc);
         if (acc) {
