@@ -3804,6 +3804,10 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
 // trial pair redrawn until the species differ (:138-146), its PairSite dE (warp
 // cluster sums), Metropolis (:148-167), then UpdateTemperature (:99-137):
 // windowed acceptance cool-down, bounded reheats, the baseline exponential decay.
+// The same FP64 operations as the reference, with the ones whose result a step may
+// not use deferred: 1 / kT is formed when a step draws a uniform (and at the end),
+// the acceptance estimate only when the reheat's integer conditions hold, the decay
+// factor once per launch (it is the same every step).
 // ---------------------------------------------------------------------------
 constexpr double kSaEpsilon = 1e-4;  // kEpsilon, lmc/cfg/include/VectorMatrix.hpp:65
 // Lattices up to this many sites are copied into shared memory for the launch:
@@ -3842,6 +3846,9 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
   const unsigned long long threshold = (0ULL - nsites) % nsites;
   int8_t *sa = s.arr, *sb = sa + 44;
   SaState st = *a.state;  // every lane keeps the same copy; lane 0 writes memory
+  // the baseline decay factor of every step (UpdateTemperature's exp(-3 / maximum_steps))
+  const double decay = exp(-3.0 / static_cast<double>(st.maximum_steps > 1ULL ? st.maximum_steps : 1ULL));
+  bool beta_fresh = true;  // st.beta belongs to st.temperature
   unsigned bad = 0;
   for (unsigned long long it = 0; it < a.steps; ++it) {
     int stop = 0;
@@ -3868,6 +3875,10 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
       const double u0 = __ull2double_rn(MtWarpOut(mw, 0)) * 5.421010862427522170e-20;
       MtWarpAdvance(mw, 1, lane);
       const double u = u0 >= 1.0 ? 0.99999999999999988898 : u0;
+      if (!beta_fresh) {
+        st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
+        beta_fresh = true;
+      }
       accepted = u < exp(-dE * st.beta);
     }
     __syncwarp();
@@ -3894,19 +3905,22 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
       st.window_trials = 0;
       st.window_accepts = 0;
     }
-    const double acc_est = st.window_trials > 0u
-                               ? static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials)
-                               : 1.0;
+    // (the acceptance estimate, an FP64 division, only when the integer conditions hold)
     if (st.reheats_done < 5 && st.steps - st.last_improvement >= st.reheat_trigger &&
-        st.steps - st.last_reheat >= st.reheat_cooldown && acc_est < 0.05) {
-      st.temperature *= 1.10;
-      st.last_improvement = st.steps;
-      st.last_reheat = st.steps;
-      st.recent_best = st.energy;
-      ++st.reheats_done;
+        st.steps - st.last_reheat >= st.reheat_cooldown) {
+      const double acc_est = st.window_trials > 0u
+                                 ? static_cast<double>(st.window_accepts) / static_cast<double>(st.window_trials)
+                                 : 1.0;
+      if (acc_est < 0.05) {
+        st.temperature *= 1.10;
+        st.last_improvement = st.steps;
+        st.last_reheat = st.steps;
+        st.recent_best = st.energy;
+        ++st.reheats_done;
+      }
     }
-    st.temperature *= exp(-3.0 / static_cast<double>(st.maximum_steps > 1ULL ? st.maximum_steps : 1ULL));
-    st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
+    st.temperature *= decay;
+    beta_fresh = false;  // 1 / kT is formed when a step needs it (and at the end)
     if (a.trace && lane == 0) {
       SaStepRec rec;
       rec.site1 = l1;
@@ -3921,6 +3935,7 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
     ++st.steps;
     __syncwarp();
   }
+  if (!beta_fresh) st.beta = 1.0 / kBoltzmannEv / fmax(st.temperature, 1e-12);
   if (lane == 0) {
     *a.state = st;
     if (bad) atomicOr(a.status, static_cast<int>(bad));
