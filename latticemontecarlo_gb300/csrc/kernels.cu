@@ -3509,22 +3509,21 @@ __device__ __forceinline__ unsigned long long MtWarpBelow(MtWarp &w, unsigned lo
   return __umul64hi(x, range);
 }
 // GenerateLatticeIdJumpPair on the stream: pairs of draws until the species differ.
-// Lanes 0-15 test the next 16 candidate pairs at once; the first different-species
-// candidate wins and exactly its draws and those before it are consumed. A draw that
-// Lemire's method would reject (probability below range / 2^64) shifts the pairing,
-// so from the first such candidate on the draws are taken one by one.
+// The 32 lanes test the next 32 candidate pairs (64 draws) at once; the first
+// different-species candidate wins and exactly its draws and those before it are
+// consumed. A draw that Lemire's method would reject (probability below range / 2^64)
+// shifts the pairing, so from the first such candidate on the draws are taken one by one.
 // `threshold` = (2^64 - range) mod range, Lemire's rejection bound (hoisted out of the loops).
 __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, unsigned long long range,
                                            unsigned long long threshold, int lane, long long *l1, long long *l2) {
-  const int k = lane & 15;
-  for (unsigned round = 0; round < (1u << 20); ++round) {
-    const unsigned long long x1 = MtWarpOut(w, 2 * k), x2 = MtWarpOut(w, 2 * k + 1);
+  for (unsigned round = 0; round < (1u << 19); ++round) {
+    const unsigned long long x1 = MtWarpOut(w, 2 * lane), x2 = MtWarpOut(w, 2 * lane + 1);
     const bool rej = x1 * range < threshold || x2 * range < threshold;
     const long long a = static_cast<long long>(__umul64hi(x1, range)), b = static_cast<long long>(__umul64hi(x2, range));
     const bool diff = species[a] != species[b];
-    const unsigned mrej = __ballot_sync(0xffffffffu, lane < 16 && rej);
-    const int r0 = mrej ? __ffs(mrej) - 1 : 16;
-    const unsigned mdiff = __ballot_sync(0xffffffffu, lane < 16 && diff) & ((1u << r0) - 1u);
+    const unsigned mrej = __ballot_sync(0xffffffffu, rej);
+    const int r0 = mrej ? __ffs(mrej) - 1 : 32;
+    const unsigned mdiff = __ballot_sync(0xffffffffu, diff) & (r0 == 32 ? 0xffffffffu : (1u << r0) - 1u);
     if (mdiff) {
       const int g = __ffs(mdiff) - 1;
       *l1 = __shfl_sync(0xffffffffu, a, g);
@@ -3532,7 +3531,7 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
       MtWarpAdvance(w, 2 * (g + 1), lane);
       return true;
     }
-    if (r0 < 16) {
+    if (r0 < 32) {
       MtWarpAdvance(w, 2 * r0, lane);
       const long long c1 = static_cast<long long>(MtWarpBelow(w, range, lane));
       const long long c2 = static_cast<long long>(MtWarpBelow(w, range, lane));
@@ -3543,7 +3542,7 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
       }
       continue;
     }
-    MtWarpAdvance(w, 32, lane);
+    MtWarpAdvance(w, 64, lane);
   }
   return false;
 }
