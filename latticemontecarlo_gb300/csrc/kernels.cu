@@ -3953,19 +3953,21 @@ __global__ void sa_kernel(DevTables t, int8_t *species_global, SaArgs a) {
 // priority is the largest on every site within 3NN of both its sites, so two
 // survivors are never within 3NN of each other and their dE terms are
 // independent), evaluates dE on the unchanged lattice and applies Metropolis to
-// each survivor independently. Survivors are the Metropolis attempts.
+// each survivor independently (FP32 factor exp(-dE / kT) and 24-bit uniform; the
+// energy change summed exactly in the dE fixed point). Survivors are the
+// Metropolis attempts.
 // ---------------------------------------------------------------------------
 constexpr int kCmcTpThreads = 256;
 __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8_t *species, CmcTpArgs a) {
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem[];
   const SiteSmem s = CarveSiteSmem(t, smem);
-  __shared__ double s_energy;
+  __shared__ unsigned long long s_energy_fix;  // the block's accepted dE sum in the dE fixed point
   __shared__ unsigned long long s_done, s_acc;
   StageArray(t.site_cl, s.cl, t.n_site_cl);
   StageArray(t.site_off, s.off, kSiteSites * 4);
   if (threadIdx.x == 0) {
-    s_energy = 0.0;
+    s_energy_fix = 0;
     s_done = 0;
     s_acc = 0;
   }
@@ -3976,6 +3978,7 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
   int8_t *sa = s.arr + warp * 88, *sb = sa + 44;
   const long long gtid = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   const uint32_t k0 = static_cast<uint32_t>(a.seed), k1 = static_cast<uint32_t>(a.seed >> 32);
+  const float de_beta = static_cast<float>(t.de_scale * a.beta);  // dE / kT per fixed-point unit
   unsigned long long prev_done = 0;
   int empty_rounds = 0;
   for (unsigned long long round = 1;; ++round) {
@@ -3992,27 +3995,40 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
     // phase A: one warp per candidate (candidates spread over the blocks). The
     // lanes make 32 draws at once; the first different-species draw in try
     // order wins, exactly as a sequential search would. Then the lanes claim
-    // the 2 x 43 sites within 3NN of the pair.
-    for (long long c = static_cast<long long>(blockIdx.x) * warps + warp; c < a.candidates;
-         c += static_cast<long long>(gridDim.x) * warps) {
+    // the 2 x 43 sites within 3NN of the pair. The warp keeps its first
+    // candidate (and the two species) in registers for phase B.
+    const long long c_first = static_cast<long long>(blockIdx.x) * warps + warp;
+    const long long c_stride = static_cast<long long>(gridDim.x) * warps;
+    long long r_l1 = -1, r_l2 = -1;
+    int r_s1 = 0, r_s2 = 0;
+    for (long long c = c_first; c < a.candidates; c += c_stride) {
       long long l1 = -1, l2 = -1;
+      int s1 = 0, s2 = 0;
       uint32_t prio = 0;
       for (uint32_t tr0 = 0; tr0 < 64; tr0 += 32) {
         const uint4 x = PhiloxRound10(static_cast<uint32_t>(round), static_cast<uint32_t>(round >> 32),
                                       static_cast<uint32_t>(c), tr0 + lane, k0, k1);
         const long long c1 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.x) << 32) | x.y, nsites));
         const long long c2 = static_cast<long long>(__umul64hi((static_cast<unsigned long long>(x.z) << 32) | x.w, nsites));
-        const bool ok = c1 != c2 && species[c1] != species[c2];
+        const int sp1 = species[c1], sp2 = species[c2];
+        const bool ok = c1 != c2 && sp1 != sp2;
         const unsigned m = __ballot_sync(0xffffffffu, ok);
         if (m) {
           const int src = __ffs(m) - 1;
           l1 = __shfl_sync(0xffffffffu, c1, src);
           l2 = __shfl_sync(0xffffffffu, c2, src);
+          s1 = __shfl_sync(0xffffffffu, sp1, src);
+          s2 = __shfl_sync(0xffffffffu, sp2, src);
           prio = __shfl_sync(0xffffffffu, (x.x ^ x.w) & 0xFFFF0000u, src);
           break;
         }
       }
-      if (lane == 0) {
+      if (c == c_first) {
+        r_l1 = l1;
+        r_l2 = l2;
+        r_s1 = s1;
+        r_s2 = s2;
+      } else if (lane == 0) {
         a.cand[2 * c] = l1;
         a.cand[2 * c + 1] = l2;
       }
@@ -4026,31 +4042,42 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
       }
     }
     grid.sync();
-    // phase B: survivors -> dE -> Metropolis
-    for (long long c = static_cast<long long>(blockIdx.x) * warps + warp; c < a.candidates;
-         c += static_cast<long long>(gridDim.x) * warps) {
-      const long long l1 = a.cand[2 * c], l2 = a.cand[2 * c + 1];
+    // phase B: survivors -> dE -> Metropolis (FP32 factor and uniform; the energy as an exact
+    // fixed-point sum). The claim words and the pair's neighbourhood are read together; a pair
+    // that lost a claim drops its gathered copy.
+    for (long long c = c_first; c < a.candidates; c += c_stride) {
+      long long l1, l2;
+      int s1, s2;
+      if (c == c_first) {
+        l1 = r_l1;
+        l2 = r_l2;
+        s1 = r_s1;
+        s2 = r_s2;
+      } else {
+        l1 = a.cand[2 * c];
+        l2 = a.cand[2 * c + 1];
+        s1 = l1 >= 0 ? species[l1] : 0;  // survivors' sites are written only by themselves
+        s2 = l1 >= 0 ? species[l2] : 0;
+      }
       if (l1 < 0) continue;
       const unsigned long long c1 = a.claim[l1], c2 = a.claim[l2];
+      int pa, pb;
+      GatherSwap(s.off, species, n, SiteCoord(l1, n), SiteCoord(l2, n), sa, sb, &pa, &pb, lane);
       const uint32_t lowbits = static_cast<uint32_t>(c1);
       // our key: round in the high word and candidate index in the low 16 bits
       if (c1 != c2 || (c1 >> 32) != round || (lowbits & 0xFFFF) != static_cast<uint32_t>(c & 0xFFFF)) continue;
-      int pa, pb;
-      GatherSwap(s.off, species, n, SiteCoord(l1, n), SiteCoord(l2, n), sa, sb, &pa, &pb, lane);
       const long long acc = WarpSum(SwapDePartial(t, s.cl, sa, sb, pa, pb, lane));
       if (lane == 0) {
-        const double dE = static_cast<double>(acc) * t.de_scale;
-        bool ok = dE < 0;
+        bool ok = acc < 0;  // dE = acc x de_scale, de_scale > 0
         if (!ok) {
           const uint4 x = PhiloxRound10(static_cast<uint32_t>(round), static_cast<uint32_t>(round >> 32),
                                         static_cast<uint32_t>(c), 0xACCE97u, k0, k1);
-          ok = U01(x.x, x.y) < exp(-dE * a.beta);
+          ok = static_cast<float>(x.x >> 8) * 5.9604644775390625e-8f < expf(-(I64ToFloat(acc) * de_beta));
         }
         if (ok) {
-          const int8_t v = species[l1];
-          species[l1] = species[l2];
-          species[l2] = v;
-          atomicAdd(&s_energy, dE);
+          species[l1] = static_cast<int8_t>(s2);
+          species[l2] = static_cast<int8_t>(s1);
+          atomicAdd(&s_energy_fix, static_cast<unsigned long long>(acc));
           atomicAdd(&s_acc, 1ULL);
         }
         atomicAdd(&s_done, 1ULL);
@@ -4074,7 +4101,8 @@ __global__ void __launch_bounds__(kCmcTpThreads) cmc_tp_kernel(DevTables t, int8
     grid.sync();
   }
   __syncthreads();
-  if (threadIdx.x == 0) a.energy_acc[blockIdx.x] = s_energy;
+  if (threadIdx.x == 0)
+    a.energy_acc[blockIdx.x] = static_cast<double>(static_cast<long long>(s_energy_fix)) * t.de_scale;
 }
 
 // Lowest-id vacancy (Config::GetVacancyLatticeId, Config.cpp:298-310) and a
