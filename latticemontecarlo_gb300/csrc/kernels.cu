@@ -797,9 +797,36 @@ __device__ __forceinline__ unsigned long long MtNext(Mt s) {
 }
 // generate_canonical<double, 53>(mt19937_64): one draw scaled by 2^-64, values
 // that round up to 1 become the largest double below 1.
-__device__ __forceinline__ double MtUniform(Mt s) {
-  const double u = __ull2double_rn(MtNext(s)) * 5.421010862427522170e-20;  // 2^-64
+__device__ __forceinline__ double MtCanonical(unsigned long long x) {
+  const double u = __ull2double_rn(x) * 5.421010862427522170e-20;  // 2^-64
   return u >= 1.0 ? 0.99999999999999988898 : u;
+}
+__device__ __forceinline__ double MtUniform(Mt s) { return MtCanonical(MtNext(s)); }
+__device__ __forceinline__ unsigned long long MtTemperOut(unsigned long long y) {
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  return y ^ (y >> 43);
+}
+// MtNext's in-place twist of the 312 state words, by a whole warp, 32 words at a time:
+// every lane reads its word's three inputs before any lane of the chunk writes. Word k reads
+// words k + 1 and k + 156 (mod 312); the serial loop sees the new values of the words below k
+// and the old ones above, and so does this order: a chunk's inputs below it were written by
+// earlier chunks, those above it (and inside it, read before the writes) are still old.
+__device__ __forceinline__ void MtTwistInPlaceWarp(unsigned long long *mt, int lane) {
+  constexpr unsigned long long kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL;
+  constexpr unsigned long long kA = 0xB5026F5AA96619E9ULL;
+  for (int b = 0; b < 312; b += 32) {
+    const int k = b + lane;
+    unsigned long long v = 0;
+    if (k < 312) {
+      const unsigned long long x = (mt[k] & kUpper) | (mt[k + 1 < 312 ? k + 1 : 0] & kLower);
+      v = mt[k + 156 < 312 ? k + 156 : k - 156] ^ (x >> 1) ^ ((x & 1ULL) ? kA : 0ULL);
+    }
+    __syncwarp();
+    if (k < 312) mt[k] = v;
+    __syncwarp();
+  }
 }
 
 struct Philox {
@@ -1660,6 +1687,8 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
   // step (it & ~31) + j, so the FP64 logarithm runs once per 32 steps
   double nlog_blk = 0.0, u2_blk = 0.0;
   Mt mt{nullptr, nullptr};
+  int mt_left = 0, mt_pos = 0;  // steps of draws left in the warp's batch, the next one
+  unsigned mt_base = 0;         // stream position of the batch's first draw
   if (active && kMt) {
     uint32_t *w = s.rng + static_cast<long long>(r) * kRngWords;
     mt.mt = reinterpret_cast<unsigned long long *>(w);
@@ -1796,12 +1825,41 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       }
       double nlog_u1 = 0, u2 = 0;  // -log(u1) for the clock, u2 for the selection
       if (kMt) {
-        if (lane == 0) {
-          const double2 d = MtStepDraws(mt);
-          nlog_u1 = d.x;
-          u2 = d.y;
+        // the step's two draws; up to 32 steps' draws are read by the warp at once (lane j:
+        // step j), within the current 312-word block, the index stored after every step
+        if (mt_left == 0) {
+          unsigned i = *mt.idx;
+          if (i >= 312) {  // the serial generator twists on its next draw
+            MtTwistInPlaceWarp(mt.mt, lane);
+            i = 0;
+          }
+          if ((i & 1u) == 0) {
+            mt_left = static_cast<int>(min(32u, (312u - i) / 2u));
+            mt_base = i;
+            mt_pos = 0;
+            if (lane < mt_left) {
+              nlog_blk = -log(MtCanonical(MtTemperOut(mt.mt[i + 2 * lane])));  // CalculateTime draws first
+              u2_blk = MtCanonical(MtTemperOut(mt.mt[i + 2 * lane + 1]));      // then SelectEvent
+            }
+          } else if (lane == 0) {
+            *mt.idx = i;  // an odd position: this step's draws one at a time
+          }
+          __syncwarp();
         }
-        u2 = __shfl_sync(0xffffffffu, u2, 0);
+        if (mt_left > 0) {
+          nlog_u1 = __shfl_sync(0xffffffffu, nlog_blk, mt_pos);
+          u2 = __shfl_sync(0xffffffffu, u2_blk, mt_pos);
+          ++mt_pos;
+          --mt_left;
+          if (lane == 0) *mt.idx = mt_base + 2u * static_cast<unsigned>(mt_pos);
+        } else {
+          if (lane == 0) {
+            const double2 d = MtStepDraws(mt);
+            nlog_u1 = d.x;
+            u2 = d.y;
+          }
+          u2 = __shfl_sync(0xffffffffu, u2, 0);
+        }
       } else {
         if ((it & 31) == 0) {
           const unsigned long long ctr = step0 + it + lane;
