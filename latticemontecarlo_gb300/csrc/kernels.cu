@@ -1874,14 +1874,18 @@ __global__ void __launch_bounds__(kShapeThreads[kShape], kShapeBlocks[kShape])
       bool hit;
       if (kMt) {
         // cumulative probabilities k_i / total summed in order, first one >= u2
-        // (std::lower_bound in KineticMcFirstAbstract::SelectEvent)
+        // (std::lower_bound in KineticMcFirstAbstract::SelectEvent); the sum stops there
         const double p = k_s / total;
-        double cp = 0.0, mycp = 0.0;
+        double cp = 0.0;
+        int first = 11;  // none: the last event
         for (int q = 0; q < 12; ++q) {
           cp += __shfl_sync(0xffffffffu, p, q);
-          if (lane == q) mycp = cp;
+          if (cp >= u2) {
+            first = q;
+            break;
+          }
         }
-        hit = lane < 12 && mycp >= u2;
+        hit = lane == first;
       } else {
         hit = lane < 12 && mycum >= u2 * total;
       }
