@@ -326,7 +326,8 @@ def run_cmc(args, device, flush, barrier):
 def run_single(args, device):
     """One trajectory (KineticMcFirstOmp's own case: n = 10, 1 vacancy, Al/Mg/Zn .96/.02/.02, 400 K)
     on the reference's mt19937_64 stream: the latency of a step, one replica on the GPU (12 warps,
-    one per jump), beside the oracle's restatement of the reference loop on one host core."""
+    one per jump), beside the oracle's restatement of the reference loop on one host core and with the
+    12 barriers of a step on 12 host threads (the reference's OpenMP loop)."""
     from latticemontecarlo_gb300 import Context, Model
     from latticemontecarlo_gb300 import _native as N
     from latticemontecarlo_gb300 import synthetic as S
@@ -355,6 +356,13 @@ def run_single(args, device):
         out["cpu_baseline"] = {"value": steps / w, "unit": "events/s", "cores": 1, "kind": "port",
                                "sample": f"{steps} steps of the same trajectory, oracle C restatement with "
                                          f"barrier memo, {w:.1f} s"}
+        # the reference's OpenMP loop over the 12 jumps of a step, on 12 host threads (more cannot help)
+        threads = min(12, os.cpu_count() or 1)
+        _, loop_s = O.kmc_threads(m, lat, sp.copy(), cfg["T"], 5, steps, threads)
+        out["cpu_baseline_threads"] = {
+            "value": steps / loop_s, "unit": "events/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the same trajectory, oracle C restatement with the 12 barriers of a "
+                      f"step on {threads} OpenMP threads (id tables built first, not timed), {loop_s:.1f} s"}
     return out
 
 

@@ -22,6 +22,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <omp.h>
 
 #define EPS 1e-4 /* kEpsilon, VectorMatrix.hpp:65 */
 static const double kLatticeConstant = 4.046;
@@ -1716,6 +1717,94 @@ int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T,
   }
   free(tab);
   free(itab);
+  return rc;
+}
+
+/* KineticMcFirstOmp's step with the 12 jump barriers evaluated by `threads` OpenMP threads, as
+ * KineticMcFirstOmp.cpp:52-82 parallelises that loop; the id lists of every (site, jump) are built
+ * before the steps, as the predictor's constructor builds its tables. Rates, sums, draws, selection
+ * and move are orc_kmc_ex's (no rate corrector, schedule or early stop), so the trajectory is
+ * orc_kmc's. *loop_s receives the wall time of the step loop alone. Returns 0, or -1. */
+int orc_kmc_threads(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
+                    int kind, int threads, double *trace8, double *loop_s) {
+  orc_mt g;
+  orc_mt_seed(&g, seed);
+  const mappings *mp = maps_for(m, lat); /* built before any parallel region */
+  const double beta = 1.0 / kBoltzmann / T;
+  int64_t vac = -1;
+  for (int64_t at = 0; at < lat->N && vac < 0; ++at)
+    if (sp[lat->atom_lattice[at]] == m->x_code) vac = lat->atom_lattice[at];
+  if (vac < 0 || threads < 1) return -1;
+  pair_ids *ids = (pair_ids *)malloc(sizeof(pair_ids) * (size_t)lat->N * 12);
+  if (!ids) return -1;
+  int failed = 0;
+#pragma omp parallel for num_threads(threads) schedule(static) reduction(| : failed)
+  for (int64_t q = 0; q < lat->N * 12; ++q)
+    if (make_pair_ids(lat, q / 12, lat->nn[q / 12][q % 12], &ids[q])) failed |= 1;
+  if (failed) {
+    free(ids);
+    return -1;
+  }
+  double time = 0.0, energy = 0.0;
+  int rc = 0;
+  const double t0 = omp_get_wtime();
+  for (int64_t st = 0; st < steps; ++st) {
+    double ea[12], de[12], k[12];
+    const int64_t *nb = lat->nn[vac];
+    int bad = 0;
+#pragma omp parallel for num_threads(threads) schedule(static, 1) reduction(| : bad)
+    for (int i = 0; i < 12; ++i) {
+      double o[4];
+      if (barrier_from_ids(m, mp, sp, vac, nb[i], &ids[vac * 12 + i], kind, o)) {
+        bad |= 1;
+      } else {
+        ea[i] = o[0];
+        de[i] = o[1];
+      }
+    }
+    if (bad) {
+      rc = -1;
+      break;
+    }
+    double total = 0.0;
+    for (int i = 0; i < 12; ++i) {
+      k[i] = exp(-ea[i] * beta); /* JumpEvent forward rate (JumpEvent.cpp:6-13) */
+      total += k[i];
+    }
+    double cum[12], cp = 0.0;
+    for (int i = 0; i < 12; ++i) {
+      cp += k[i] / total;
+      cum[i] = cp;
+    }
+    const double u1 = orc_mt_uniform(&g);
+    const double dt = -log(u1) / total / kPrefactor;
+    const double u2 = orc_mt_uniform(&g);
+    int sel = 11;
+    for (int i = 0; i < 12; ++i)
+      if (!(cum[i] < u2)) {
+        sel = i;
+        break;
+      }
+    const int64_t j = nb[sel];
+    time += dt;
+    energy += de[sel];
+    if (trace8) {
+      double *t = trace8 + st * 8;
+      t[0] = (double)vac;
+      t[1] = (double)j;
+      t[2] = sel;
+      t[3] = ea[sel];
+      t[4] = de[sel];
+      t[5] = total;
+      t[6] = time;
+      t[7] = energy;
+    }
+    sp[vac] = sp[j];
+    sp[j] = (int8_t)m->x_code;
+    vac = j;
+  }
+  if (loop_s) *loop_s = omp_get_wtime() - t0;
+  free(ids);
   return rc;
 }
 

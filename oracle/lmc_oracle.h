@@ -113,6 +113,12 @@ int orc_kmc_ex(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T,
                int kind, int memo, double *trace8, double *events36, const double *tt_time, const double *tt_temp,
                int tt_len, int rate_corrector, int early_stop, int64_t *steps_done);
 
+/* KineticMcFirstOmp with the 12 barriers of a step on `threads` OpenMP threads
+ * (KineticMcFirstOmp.cpp:52-82), the id lists of every (site, jump) built first; the
+ * trajectory is orc_kmc's without memo, rate corrector, schedule or early stop. *loop_s
+ * receives the wall time of the step loop. Returns 0, or -1. */
+int orc_kmc_threads(const orc_model *m, const orc_lattice *lat, int8_t *sp, double T, uint64_t seed, int64_t steps,
+                    int kind, int threads, double *trace8, double *loop_s);
 /* CanonicalMcOmp with batch size `batch` (CanonicalMcOmp.cpp:40-92,
  * CanonicalMcAbstract.cpp:43-101): runs until `attempts` Metropolis tests were
  * made (whole batches). energy_trace (NULL or capacity `cap`) receives energy_

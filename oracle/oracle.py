@@ -72,6 +72,7 @@ def lib() -> C.CDLL:
             "orc_kmc_ex": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, DP, DP, DP, DP,
                                      C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]),
             "orc_cmc": (I64, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, DP, DP, I64, I64P]),
+            "orc_kmc_threads": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, DP, DP]),
             "orc_model_set_vacancy_zero": (None, [P, C.c_int]),
             "orc_sa": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, C.c_uint64, I64, C.c_double, DP, DP]),
             "orc_kmc_chain": (C.c_int, [P, P, I8P, C.c_double, C.c_uint64, I64, C.c_int, C.c_int, C.c_uint32, DP]),
@@ -300,6 +301,19 @@ def kmc(model: Model, lat: Lattice, species, T: float, seed: int, steps: int, ki
         trace = trace[:done.value]
         ev = ev[:done.value] if ev is not None else None
     return trace, ev
+
+
+def kmc_threads(model: Model, lat: Lattice, species, T: float, seed: int, steps: int, threads: int, kind: int = 0):
+    """KineticMcFirstOmp with the 12 barriers of each step on `threads` OpenMP threads (the
+    reference's parallel loop), id tables built first; species is modified in place. Returns
+    (trace [steps][8] as kmc's, wall seconds of the step loop)."""
+    trace = np.zeros((steps, 8))
+    loop_s = C.c_double()
+    rc = lib().orc_kmc_threads(model.h, lat.h, _sp(species), T, seed, steps, kind, threads, _p(trace, C.c_double),
+                               C.byref(loop_s))
+    if rc != 0:
+        raise OracleError("orc_kmc_threads failed")
+    return trace, loop_s.value
 
 
 def cmc(model: Model, lat: Lattice, species, T: float, seed: int, attempts: int, batch: int, energy0: float = 0.0,

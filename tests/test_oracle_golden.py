@@ -151,6 +151,23 @@ def test_kmc_trajectory(oracle_mod, golden):
     assert np.array_equal(ev[: G.KMC_DETAIL], fx["events"])
 
 
+def test_threaded_kmc_is_the_serial_trajectory(oracle_mod, golden):
+    """The CPU baseline's threaded KineticMcFirstOmp restatement (12 barriers of a step on OpenMP
+    threads) takes the reference's trajectory: the golden fixture's events, as the serial loop."""
+    G, load = golden
+    el, coeffs, n, sp = G.case_inputs("kmc_ternary")
+    fx = load("kmc_ternary")
+    lat = oracle_mod.Lattice(n)
+    m = oracle_mod.Model(el, coeffs, lat)
+    steps = 600
+    tr, loop_s = oracle_mod.kmc_threads(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, steps, 4)
+    ref = fx["steps"][:steps]  # steps vacancy target selected Ea dE total time energy
+    assert np.array_equal(tr[:, 1], ref[:, 2]) and np.array_equal(tr[:, 2], ref[:, 3])
+    assert np.array_equal(tr[:, 3], ref[:, 4]) and np.array_equal(tr[:, 4], ref[:, 5])
+    np.testing.assert_allclose(tr[:, 6], ref[:, 7], rtol=1e-15)
+    assert loop_s > 0
+
+
 def test_cmc_trajectory(oracle_mod, golden):
     G, load = golden
     el, coeffs, n, sp = G.case_inputs("cmc_quaternary")
