@@ -775,6 +775,13 @@ struct Mt {
   unsigned long long *mt;  // 312 words
   unsigned *idx;
 };
+// mt19937_64's output tempering.
+__device__ __forceinline__ unsigned long long MtTemperOut(unsigned long long y) {
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  return y ^ (y >> 43);
+}
 __device__ __forceinline__ unsigned long long MtNext(Mt s) {
   constexpr int kN = 312, kM = 156;
   constexpr unsigned long long kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL;
@@ -787,13 +794,9 @@ __device__ __forceinline__ unsigned long long MtNext(Mt s) {
     }
     i = 0;
   }
-  unsigned long long y = s.mt[i];
+  const unsigned long long y = s.mt[i];
   *s.idx = i + 1;
-  y ^= (y >> 29) & 0x5555555555555555ULL;
-  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
-  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
-  y ^= y >> 43;
-  return y;
+  return MtTemperOut(y);
 }
 // generate_canonical<double, 53>(mt19937_64): one draw scaled by 2^-64, values
 // that round up to 1 become the largest double below 1.
@@ -802,12 +805,6 @@ __device__ __forceinline__ double MtCanonical(unsigned long long x) {
   return u >= 1.0 ? 0.99999999999999988898 : u;
 }
 __device__ __forceinline__ double MtUniform(Mt s) { return MtCanonical(MtNext(s)); }
-__device__ __forceinline__ unsigned long long MtTemperOut(unsigned long long y) {
-  y ^= (y >> 29) & 0x5555555555555555ULL;
-  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
-  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
-  return y ^ (y >> 43);
-}
 // MtNext's in-place twist of the 312 state words, by a whole warp, 32 words at a time:
 // every lane reads its word's three inputs before any lane of the chunk writes. Word k reads
 // words k + 1 and k + 156 (mod 312); the serial loop sees the new values of the words below k
@@ -3518,12 +3515,6 @@ struct MtWarp {
   unsigned long long *cur, *nxt;  // raw words of the current and the following block
   unsigned idx;                   // next unread position in cur (0..311)
 };
-__device__ __forceinline__ unsigned long long MtTemper(unsigned long long y) {
-  y ^= (y >> 29) & 0x5555555555555555ULL;
-  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
-  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
-  return y ^ (y >> 43);
-}
 // dst = the block after src (the serial in-place twist, split into its two
 // dependency-free halves: words 0-155 read only src, words 156-311 read dst 0-155).
 __device__ __forceinline__ void MtTwistWarp(const unsigned long long *src, unsigned long long *dst, int lane) {
@@ -3542,7 +3533,7 @@ __device__ __forceinline__ void MtTwistWarp(const unsigned long long *src, unsig
 }
 __device__ __forceinline__ unsigned long long MtWarpOut(const MtWarp &w, unsigned p) {
   const unsigned q = w.idx + p;  // p < 312
-  return MtTemper(q < 312 ? w.cur[q] : w.nxt[q - 312]);
+  return MtTemperOut(q < 312 ? w.cur[q] : w.nxt[q - 312]);
 }
 __device__ __forceinline__ void MtWarpAdvance(MtWarp &w, unsigned count, int lane) {
   w.idx += count;  // count <= 312
