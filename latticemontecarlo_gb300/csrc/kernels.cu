@@ -2877,16 +2877,34 @@ __global__ void __launch_bounds__(kMultiWarps * 32, 1)
         const double u2 = __shfl_sync(0xffffffffu, u2_blk, static_cast<int>(it & 31));
         const int chunks = (nv + 31) >> 5;
         double run = 0.0;
-        for (int c = 0; c < chunks; ++c) {
-          const int v = c * 32 + lane;
-          double sc = v < nv ? s_cum[v * 12 + 11] : 0.0;
+        for (int c = 0; c < chunks; c += 2) {
+          // two chunks' scans side by side (the same additions as one after the other)
+          const int v0 = c * 32 + lane, v1 = v0 + 32;
+          double sc0 = v0 < nv ? s_cum[v0 * 12 + 11] : 0.0;
+          if (c + 1 < chunks) {  // warp-uniform
+            double sc1 = v1 < nv ? s_cum[v1 * 12 + 11] : 0.0;
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const double u = __shfl_up_sync(0xffffffffu, sc, o);
-            if (lane >= o) sc += u;
+            for (int o = 1; o < 32; o <<= 1) {
+              const double u0 = __shfl_up_sync(0xffffffffu, sc0, o);
+              const double u1 = __shfl_up_sync(0xffffffffu, sc1, o);
+              if (lane >= o) {
+                sc0 += u0;
+                sc1 += u1;
+              }
+            }
+            if (v0 < nv) s_incl[v0] = run + sc0;
+            run = run + __shfl_sync(0xffffffffu, sc0, 31);
+            if (v1 < nv) s_incl[v1] = run + sc1;
+            run = run + __shfl_sync(0xffffffffu, sc1, 31);
+          } else {
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const double u0 = __shfl_up_sync(0xffffffffu, sc0, o);
+              if (lane >= o) sc0 += u0;
+            }
+            if (v0 < nv) s_incl[v0] = run + sc0;
+            run = run + __shfl_sync(0xffffffffu, sc0, 31);
           }
-          if (v < nv) s_incl[v] = run + sc;
-          run = run + __shfl_sync(0xffffffffu, sc, 31);
         }
         const double total = run;
         __syncwarp();
