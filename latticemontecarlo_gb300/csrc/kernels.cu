@@ -3650,7 +3650,7 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
   __shared__ int s_nb, s_fail, s_stop;
   // warp 0's set of candidate pairs while it builds a batch
   __shared__ long long s_c1[32], s_c2[32];
-  __shared__ unsigned s_cend[32];
+  __shared__ unsigned s_cend[32], s_cmask[32];
   __shared__ H3 s_ch[64];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = a.n;
@@ -3734,40 +3734,69 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
           break;
         }
         __syncwarp();
-        if (lane < m) {
-          s_ch[2 * lane] = SiteCoord(s_c1[lane], n);
-          s_ch[2 * lane + 1] = SiteCoord(s_c2[lane], n);
+        // the set's first mm pairs (enough to fill the batch with 8 rejections to spare): lane j
+        // forms pair j's coordinates and whether it lies in the shells of a pair chosen before
+        // this set (bit 31); then the lanes test the set's pairs against each other (bit k of
+        // word j: pair k < j conflicts with pair j)
+        const int mm = min(m, a.batch - nb + 8);
+        if (lane < mm) {
+          const H3 e1 = SiteCoord(s_c1[lane], n), e2 = SiteCoord(s_c2[lane], n);
+          s_ch[2 * lane] = e1;
+          s_ch[2 * lane + 1] = e2;
+          bool prev = false;
+          for (int q = 0; q < 2 * nb; ++q) prev |= CmcRefNear(e1, s_h[q], n) | CmcRefNear(e2, s_h[q], n);
+          s_cmask[lane] = prev ? 0x80000000u : 0u;
         }
         __syncwarp();
-        // the pairs in order: a slot's 50th pair ends the batch, a pair clear of the shells of
-        // the chosen ones fills the slot
-        int jend = -1;
-        for (int j = 0; j < m; ++j) {
-          if (++ct == 50) {
-            jend = j;
-            ended = true;
-            break;
-          }
-          const H3 q1 = s_ch[2 * j], q2 = s_ch[2 * j + 1];
-          bool hit = false;
-          for (int q = lane; q < 2 * nb; q += 32) hit |= CmcRefNear(q1, s_h[q], n) || CmcRefNear(q2, s_h[q], n);
-          if (!__any_sync(0xffffffffu, hit)) {
-            if (lane == 0) {
-              s_pair[nb][0] = s_c1[j];
-              s_pair[nb][1] = s_c2[j];
-              s_h[2 * nb] = q1;
-              s_h[2 * nb + 1] = q2;
-            }
-            __syncwarp();
-            ++nb;
-            ct = 0;
-            if (nb == a.batch) {
+        const int npairs = mm * (mm - 1) / 2;
+        for (int p = lane; p < npairs; p += 32) {
+          int j = static_cast<int>((1.0f + sqrtf(1.0f + 8.0f * static_cast<float>(p))) * 0.5f);
+          while (j * (j - 1) / 2 > p) --j;
+          while ((j + 1) * j / 2 <= p) ++j;
+          const int kk = p - j * (j - 1) / 2;
+          const H3 a1 = s_ch[2 * j], a2 = s_ch[2 * j + 1], b1 = s_ch[2 * kk], b2 = s_ch[2 * kk + 1];
+          if (CmcRefNear(a1, b1, n) | CmcRefNear(a1, b2, n) | CmcRefNear(a2, b1, n) | CmcRefNear(a2, b2, n))
+            atomicOr(&s_cmask[j], 1u << kk);
+        }
+        __syncwarp();
+        // the pairs in order (lane 0): a slot's 50th pair ends the batch, a pair clear of the
+        // shells of the chosen ones fills the slot
+        unsigned chosen = 0;
+        int add = 0, jend = -1, ended_i = 0;
+        if (lane == 0) {
+          for (int j = 0; j < mm; ++j) {
+            if (++ct == 50) {
               jend = j;
+              ended_i = 1;
               break;
+            }
+            const unsigned cm = s_cmask[j];
+            if (!(cm & 0x80000000u) && !(cm & chosen)) {
+              chosen |= 1u << j;
+              ct = 0;
+              if (nb + ++add == a.batch) {
+                jend = j;
+                break;
+              }
             }
           }
         }
-        const unsigned used = jend >= 0 ? s_cend[jend] : off;  // draws this set consumes
+        chosen = __shfl_sync(0xffffffffu, chosen, 0);
+        add = __shfl_sync(0xffffffffu, add, 0);
+        jend = __shfl_sync(0xffffffffu, jend, 0);
+        ct = __shfl_sync(0xffffffffu, ct, 0);
+        ended = __shfl_sync(0xffffffffu, ended_i, 0) != 0;
+        if (lane < mm && ((chosen >> lane) & 1u)) {
+          const int idx = nb + __popc(chosen & ((1u << lane) - 1u));
+          s_pair[idx][0] = s_c1[lane];
+          s_pair[idx][1] = s_c2[lane];
+          s_h[2 * idx] = s_ch[2 * lane];
+          s_h[2 * idx + 1] = s_ch[2 * lane + 1];
+        }
+        nb += add;
+        // draws this set consumes: through the pair that ended or completed the batch, else through
+        // the last pair examined (all examined slots when every pair of the set was examined)
+        const unsigned used = jend >= 0 ? s_cend[jend] : (mm < m ? s_cend[mm - 1] : off);
         __syncwarp();
         MtWarpAdvance(mw, used > 312 ? 312 : used, lane);
         if (used > 312) MtWarpAdvance(mw, used - 312, lane);
