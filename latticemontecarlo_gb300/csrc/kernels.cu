@@ -3626,7 +3626,8 @@ __device__ __forceinline__ bool MtWarpPair(MtWarp &w, const int8_t *species, uns
 // tries. The shells are not marked on a lattice-sized array: on an FCC supercell
 // with n >= 6 a site lies in the shell of c exactly when its minimum-image
 // displacement from c has squared length <= 6 (half units: 1NN 2, 2NN 4, 3NN 6,
-// 4NN 8), so the lanes test the candidates against the chosen sites directly.
+// 4NN 8), so the lanes test the candidates' coordinates against each other and
+// against the chosen sites directly.
 // The block's warps then compute the batch's dE values on the unchanged lattice,
 // one pair per warp, as the reference's OpenMP threads do; warp 0 runs the
 // Metropolis tests of up to 32 pairs at once (a pair's uniform is the stream's
@@ -3688,9 +3689,11 @@ __global__ void __launch_bounds__(kCmcRefWarps * 32, 1) cmc_ref_kernel(DevTables
     if (warp == 0) {
       // The batch: pair slot after pair slot, the stream's different-species pairs in order, each
       // kept when neither site lies in the shells of the pairs kept before, the batch given up at
-      // a slot's 50th pair. The different-species pairs are found a set at a time (lanes 0-15
-      // test 16 consecutive draw pairs per ballot, up to 32 pairs or 312 draws ahead), then taken
-      // in order; only the draws up to the pair that completes the batch are consumed.
+      // a slot's 50th pair. The different-species pairs are found a set at a time (the 32 lanes
+      // test 32 consecutive draw pairs per ballot, up to 32 pairs within the draws readable
+      // before the stream advances), tested against each other and the pairs kept before as bit
+      // masks, then taken in order; only the draws up to the pair that completes the batch are
+      // consumed.
       int nb = 0, ct = 0, empty_sets = 0;
       bool failed = false, ended = false;
       while (nb < a.batch && !failed && !ended) {
