@@ -2756,10 +2756,11 @@ int lmc_cmc_run(lmc_ctx *ctx, int replica, double temperature, uint64_t attempts
         // Surviving pairs per round grow with the candidates until the lattice
         // is saturated (about N / 172 pairs fit 3NN apart); the round's latency
         // grows once candidates outnumber the resident warps (measured on GB300:
-        // the optimum is near N / 80, capped at 3/5 of the resident warps).
+        // the optimum is near N / 80 at n = 30, and at n = 64 near 4/5 of the
+        // resident warps: 2.1e8 swaps/s against 1.95e8 at 3/5 and 1.6e8 at 1.03x).
         const long long warps = lmc::CmcThroughputResidentWarps(ctx->t, ctx->device);
         long long c = nsites / 80;
-        if (warps > 0) c = std::min(c, warps * 3 / 5);
+        if (warps > 0) c = std::min(c, warps * 4 / 5);
         cand = static_cast<int>(std::min<long long>(65535, std::max<long long>(32, c)));
       }
       Require(cand <= 65535, LMC_ERR_INVALID_ARGUMENT, "at most 65535 candidates per round");
