@@ -166,6 +166,10 @@ def test_threaded_kmc_is_the_serial_trajectory(oracle_mod, golden):
     assert np.array_equal(tr[:, 3], ref[:, 4]) and np.array_equal(tr[:, 4], ref[:, 5])
     np.testing.assert_allclose(tr[:, 6], ref[:, 7], rtol=1e-15)
     assert loop_s > 0
+    # the thread count changes nothing but the time
+    tr1, _ = oracle_mod.kmc_threads(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, 200, 1)
+    tr3, _ = oracle_mod.kmc_threads(m, lat, sp.copy(), G.KMC_T, G.KMC_SEED, 200, 3)
+    assert np.array_equal(tr1, tr3) and np.array_equal(tr1, tr[:200])
 
 
 def test_cmc_trajectory(oracle_mod, golden):
